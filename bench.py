@@ -1,0 +1,452 @@
+"""Benchmark of the imaginary-time bubble + RPA path on GB300.
+
+One step = the whole path on the 3-orbital cubic workload (32^3 k, beta = 20,
+256 fermionic / 256 bosonic Matsubara frequencies, 9 x 9 Kanamori vertex):
+Dyson G0(iv, k) -> k->r -> iv->tau -> bubble fused with tau->iw -> r->q ->
+RPA. The metric is (q, iw) points per second: (2 nw - 1) * N_k per step.
+
+  value : device-resident inputs, preallocated buffers, C-ABI calls.
+  e2e   : the public Python API (lattice_dyson_g0_wk, imtime_bubble_chi0_wk,
+          solve_rpa_PH) from a pinned host e(k) to chi(iw, q) copied back
+          into pinned host memory, both copies inside the timed region.
+
+``--impl reference`` times the CPU implementation of the same path (the FP64
+restatement of the reference, run on all host cores) on a bounded sample of
+the same workload. With torchrun (N > 1) every rank runs an independent
+replica (the path has no cross-instance exchange): weak scaling.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "RPA chi(q,iw) points/s (complex128, <=1e-10 rel err vs FP64 oracle)"
+UNIT = "points/s"
+C16 = 16  # bytes per complex128
+
+
+# ---------------------------------------------------------------------------
+# algorithmic traffic and flops per stage (one read of inputs, one write of outputs)
+
+def stage_model(nb, nk, n_nu, n_tau, nw):
+    nb2, nb4, nwt = nb * nb, nb ** 4, 2 * nw - 1
+    L = n_tau - 1
+    fft_flops = lambda n: 5.0 * n * math.log2(n) if n > 1 else 0.0  # noqa: E731
+    return {
+        "dyson": dict(bytes=C16 * nb2 * n_nu * nk, flops=n_nu * nk * 8.0 * nb ** 3),
+        "fft_k_to_r": dict(bytes=2 * C16 * nb2 * n_nu * nk, flops=n_nu * nb2 * fft_flops(nk)),
+        "nu_to_tau": dict(bytes=C16 * nb2 * nk * (n_nu + n_tau), flops=nk * nb2 * fft_flops(L)),
+        "bubble_tau_to_w": dict(bytes=C16 * nk * (nb2 * n_tau + nb4 * nwt),
+                                flops=nk * nb4 * (6.0 * n_tau + fft_flops(L))),
+        "fft_r_to_q": dict(bytes=2 * C16 * nb4 * nwt * nk, flops=nwt * nb4 * fft_flops(nk)),
+        "rpa": dict(bytes=2 * C16 * nb4 * nwt * nk, flops=nwt * nk * 8.0 * (nb2 ** 3 * 2 + nb2 ** 3 / 3.0)),
+    }
+
+
+# ---------------------------------------------------------------------------
+# clocks sampled during the timed region
+
+class ClockSampler:
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, ValueError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            if self.thread:
+                self.thread.join(timeout=2)
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": mx, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# distributed helpers (replicas)
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def max_over_ranks(value: float, world: int, device=None) -> float:
+    """Max of a per-rank float over all ranks (identity for one rank)."""
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world: int, device=None):
+    if world > 1:
+        import torch.distributed as dist
+        if device is not None and device.type == "cuda":
+            dist.barrier(device_ids=[device.index])
+        else:
+            dist.barrier()
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the oracle on a bounded sample of the workload
+
+def cpu_sample_seconds(cfg, frac_seed=0, scale=1.0):
+    """Extrapolated seconds for one full step of the oracle, from timed slices.
+
+    Each stage is timed on a slice (a few frequencies, r points, columns or
+    (w, q) points) and scaled linearly by the slice fraction.
+    """
+    import numpy as np
+    import oracle as O
+    dims, beta, mu, n_max, nw = cfg["dims"], cfg["beta"], cfg["mu"], cfg["n_max"], cfg["nw"]
+    ek = O.ek_from_hoppings(cfg["hoppings"], dims)
+    nk, nb = ek.shape[0], ek.shape[-1]
+    n_nu, n_tau = 2 * n_max, 6 * n_max + 1
+    nwt = 2 * nw - 1
+    rng = np.random.default_rng(frac_seed)
+    t = {}
+    # Dyson on a few frequencies
+    s_nu = max(1, int(4 * scale))
+    t0 = time.perf_counter()
+    g_part = np.linalg.inv((O.fermionic_iw(beta, n_max)[:s_nu] + mu)[:, None, None, None] * np.eye(nb) - ek[None])
+    t["dyson"] = (time.perf_counter() - t0) * n_nu / s_nu
+    # k -> r on the same frequencies
+    t0 = time.perf_counter()
+    g_r = O.fourier_wk_to_wr(g_part, dims)
+    t["fft_k_to_r"] = (time.perf_counter() - t0) * n_nu / s_nu
+    # iv -> tau on a slice of columns (G(iv, r) for all frequencies of a few columns)
+    s_col = max(16, int(256 * scale))
+    g_cols = O.lattice_dyson_g0_wk(mu, ek[:s_col // (nb * nb) + 1], beta, n_max).reshape(n_nu, -1)[:, :s_col]
+    t0 = time.perf_counter()
+    g_t = O.fourier_wr_to_tr(g_cols[:, :, None], beta, n_tau)
+    t["nu_to_tau"] = (time.perf_counter() - t0) * (nk * nb * nb) / s_col
+    # bubble + tau -> w for a few r points
+    s_r = max(1, int(2 * scale))
+    gt = rng.standard_normal((n_tau, 2, nb, nb)) + 0j
+    t0 = time.perf_counter()
+    for _ in range(s_r):
+        chi_t = np.einsum("tda,tbc->tabcd", gt[:, 0], gt[::-1, 1]).reshape(n_tau, -1)
+        O.chi_wr_from_chi_tr(chi_t, beta, nw)
+    t["bubble_tau_to_w"] = (time.perf_counter() - t0) * nk / s_r
+    # r -> q for a few (w, element) slices
+    s_w = max(1, int(8 * scale))
+    x = rng.standard_normal((s_w, nk, 1)) + 0j
+    t0 = time.perf_counter()
+    O.fourier_wr_to_wk(x, dims)
+    t["fft_r_to_q"] = (time.perf_counter() - t0) * nwt * nb ** 4 / s_w
+    # RPA on a slice of points
+    s_p = max(64, int(4096 * scale))
+    c0 = 0.05 * (rng.standard_normal((s_p, nb, nb, nb, nb)) + 1j * rng.standard_normal((s_p, nb, nb, nb, nb)))
+    t0 = time.perf_counter()
+    O.solve_rpa_PH(c0, cfg["U"])
+    t["rpa"] = (time.perf_counter() - t0) * nwt * nk / s_p
+    del g_r, g_t
+    return sum(t.values()), t
+
+
+def _cpu_worker(args):
+    key, seed, scale = args
+    from tprf_gb300 import workloads
+    return cpu_sample_seconds(workloads.config(key), seed, scale)[0]
+
+
+def cpu_throughput(cfg_key, procs: int, scale=1.0, pool=None):
+    """(points/s, cores, seconds of wall time) of the oracle on `procs` host processes.
+
+    Every process times one slice-sampled full step (``cpu_sample_seconds``);
+    with several processes they run concurrently on separate cores, as the
+    reference's OpenMP loops over r and w do, and the throughput adds up.
+    """
+    from tprf_gb300 import workloads
+    cfg = workloads.config(cfg_key)
+    points = (2 * cfg["nw"] - 1) * int(math.prod(cfg["dims"]))
+    t0 = time.perf_counter()
+    if procs <= 1 or pool is None:
+        sec, _ = cpu_sample_seconds(cfg, 0, scale)
+        return points / sec, 1, time.perf_counter() - t0
+    secs = pool.map(_cpu_worker, [(cfg_key, i, scale) for i in range(procs)])
+    wall = time.perf_counter() - t0
+    return procs * points / statistics.mean(secs), procs, wall
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+
+def run_gpu(args):
+    import numpy as np
+    import torch
+
+    import tprf_gb300 as T
+    from tprf_gb300 import _native, workloads
+    from tprf_gb300._native import check, dims3
+    from tprf_gb300.tight_binding import ek_tensor
+
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    lib = _native.lib()
+    cfg = workloads.config(args.config)
+    dims, beta, mu, n_max, nw = cfg["dims"], cfg["beta"], cfg["mu"], cfg["n_max"], cfg["nw"]
+    nk = int(math.prod(dims))
+    e_k = ek_tensor(cfg["hoppings"], dims, device=dev)
+    nb = e_k.shape[-1]
+    nb2, nb4 = nb * nb, nb ** 4
+    n_nu, n_tau, nwt = 2 * n_max, 6 * n_max + 1, 2 * nw - 1
+    points = nwt * nk
+    U = torch.as_tensor(cfg["U"], dtype=torch.complex128, device=dev).contiguous()
+    g_wk = torch.empty(n_nu, nk, nb, nb, dtype=torch.complex128, device=dev)
+    g_wr = torch.empty_like(g_wk)
+    g_tr = torch.empty(n_tau, nk, nb, nb, dtype=torch.complex128, device=dev)
+    chi0 = torch.empty(nwt, nk, nb4, dtype=torch.complex128, device=dev)
+    chi = torch.empty_like(chi0)
+    d3 = dims3(dims)
+    stream = torch.cuda.current_stream()
+    sh = stream.cuda_stream
+    lib.tprf_set_sync_checks(0)
+    n_fft_dims = sum(1 for d in dims if d > 1)
+    launches_per_step = 1 + n_fft_dims + 1 + 1 + n_fft_dims + 1
+
+    stages = ["dyson", "fft_k_to_r", "nu_to_tau", "bubble_tau_to_w", "fft_r_to_q", "rpa"]
+
+    def step(ev=None):
+        def mark(i):
+            if ev is not None:
+                ev[i].record(stream)
+        mark(0)
+        check(lib.tprf_lattice_dyson_g_wk(beta, n_max, nk, nb, mu, e_k.data_ptr(), None, 0, g_wk.data_ptr(), sh))
+        mark(1)
+        check(lib.tprf_fourier_wk_to_wr(n_nu, d3, nb2, g_wk.data_ptr(), g_wr.data_ptr(), sh))
+        mark(2)
+        check(lib.tprf_fourier_wr_to_tr(beta, n_max, n_tau, nk, nb2, g_wr.data_ptr(), None, g_tr.data_ptr(), sh))
+        mark(3)
+        check(lib.tprf_chi0_wr_from_grt_PH(beta, n_tau, nw, d3, nb, g_tr.data_ptr(), chi0.data_ptr(), sh))
+        mark(4)
+        check(lib.tprf_fourier_wr_to_wk(nwt, d3, nb4, chi0.data_ptr(), chi0.data_ptr(), sh))
+        mark(5)
+        check(lib.tprf_solve_rpa_PH(points, nb, chi0.data_ptr(), U.data_ptr(), chi.data_ptr(), sh))
+        mark(6)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    check(lib.tprf_check_device_status(sh), "warm-up")
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(7)] for _ in range(args.steps)]
+    clocks = ClockSampler(local)
+    barrier(world, dev)
+    torch.cuda.synchronize()
+    with clocks:
+        t_start = torch.cuda.Event(enable_timing=True)
+        t_end = torch.cuda.Event(enable_timing=True)
+        t_start.record(stream)
+        for k in range(args.steps):
+            step(evs[k])
+        t_end.record(stream)
+        torch.cuda.synchronize()
+    barrier(world, dev)
+    check(lib.tprf_check_device_status(sh), "timed steps")
+    elapsed_ms = t_start.elapsed_time(t_end)
+    elapsed_ms = max_over_ranks(elapsed_ms, world, dev)
+    ms_per_step = elapsed_ms / args.steps
+    stage_ms = {s: statistics.mean(evs[k][i].elapsed_time(evs[k][i + 1]) for k in range(args.steps))
+                for i, s in enumerate(stages)}
+    value = world * points / (ms_per_step / 1e3)
+
+    # ---- end to end through the public API, host buffers in and out
+    ek_host = e_k.cpu().pin_memory()
+    out_host = torch.empty((nwt, nk) + (nb,) * 4, dtype=torch.complex128, pin_memory=True)
+    wmesh = T.MeshImFreq(beta, "Fermion", n_max)
+    kmesh = T.MeshBrZone(dims=dims)
+    ws = torch.empty(T.lattice_utils.bubble_workspace_bytes(n_max, n_tau, dims, nb), dtype=torch.uint8, device=dev)
+    del g_wk, g_wr, g_tr, chi0, chi
+    torch.cuda.empty_cache()
+    lib.tprf_set_sync_checks(1)
+
+    def e2e_step():
+        ekd = ek_host.to(dev, non_blocking=True)
+        g = T.lattice_dyson_g0_wk(mu, T.Gf(mesh=kmesh, data=ekd), wmesh)
+        c0 = T.imtime_bubble_chi0_wk(g, nw=nw, verbose=False, workspace=ws)
+        del g
+        c = T.solve_rpa_PH(c0, cfg["U"])
+        del c0
+        out_host.copy_(c.data, non_blocking=True)
+        del c
+
+    e2e_steps = max(1, min(args.steps, 3))
+    e2e_step()
+    torch.cuda.synchronize()
+    barrier(world, dev)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks((time.perf_counter() - t0) / e2e_steps, world, dev)
+    e2e_value = world * points / e2e_s
+
+    # ---- roofline of the dominant kernel
+    model = stage_model(nb, nk, n_nu, n_tau, nw)
+    top = max(stage_ms, key=stage_ms.get)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except OSError:
+        pass
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    achieved = model[top]["bytes"] / (stage_ms[top] * 1e-3) / 1e9
+    fp64_peak_tflops = 1.0  # FP64 FMA throughput measured on this GB300 pool (probe in profiles/)
+    per_stage = {s: {"ms": round(stage_ms[s], 3), "share": round(stage_ms[s] / sum(stage_ms.values()), 4),
+                     "hbm_gbs": round(model[s]["bytes"] / (stage_ms[s] * 1e-3) / 1e9, 1),
+                     "hbm_frac": round(model[s]["bytes"] / (stage_ms[s] * 1e-3) / 1e9 / hbm_peak, 4),
+                     "fp64_tflops": round(model[s]["flops"] / (stage_ms[s] * 1e-3) / 1e12, 3)}
+                 for s in stages}
+    roofline = {"bound": "hbm", "kernel": top, "achieved": round(achieved, 1), "peak": hbm_peak, "unit": "GB/s",
+                "frac": round(achieved / hbm_peak, 4), "peak_source": peak_src,
+                "algorithmic_bytes": model[top]["bytes"], "traffic": TRAFFIC.get((args.config, top)),
+                "fp64": {"achieved_tflops": per_stage[top]["fp64_tflops"], "peak_tflops": fp64_peak_tflops,
+                         "frac": round(per_stage[top]["fp64_tflops"] / fp64_peak_tflops, 4)},
+                "stages": per_stage}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "c128", "data": "synthetic (seeded tight-binding model)",
+        "config": {"workload": cfg["name"], "dims": list(dims), "nb": nb, "beta": beta, "n_max": n_max, "nw": nw,
+                   "n_tau": n_tau, "points_per_step": points, "vertex": "Kanamori spin channel U=2.3 J=0.4",
+                   "l2": "inputs larger than L2 (G(tau,r) 7.2 GB, chi 21.7 GB per step)",
+                   "parallelism": f"replicas x{world}"},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(ek_host.numel() * C16),
+                "d2h_bytes_per_step": int(out_host.numel() * C16)},
+        "gpu_launches": launches_per_step * args.steps,
+        "roofline": roofline,
+        "clocks": clocks.summary(),
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        v, cores, wall = cpu_throughput(args.config, 1, scale=40)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                                "sample": f"FP64 oracle, every stage timed on a slice and scaled to one full step "
+                                          f"({wall:.1f} s of CPU work)"}
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+# DRAM traffic per launch of the dominant kernel, from the ncu captures
+# summarised under profiles/ (None until captured).
+TRAFFIC = {}
+
+
+# ---------------------------------------------------------------------------
+# reference arm: the CPU implementation on the host cores
+
+def run_reference(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    import multiprocessing as mp
+    os.environ["OMP_NUM_THREADS"] = "1"
+    os.environ["OPENBLAS_NUM_THREADS"] = "1"
+    procs = max(1, os.cpu_count() or 1)
+    vals, walls = [], []
+    with mp.get_context("spawn").Pool(procs) as pool:
+        for _ in range(args.warmup):
+            cpu_throughput(args.config, procs, scale=10, pool=pool)
+        for _ in range(args.steps):
+            v, cores, wall = cpu_throughput(args.config, procs, scale=10, pool=pool)
+            vals.append(v)
+            walls.append(wall)
+    from tprf_gb300 import workloads
+    cfg = workloads.config(args.config)
+    value = statistics.mean(vals)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(walls), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic (seeded tight-binding model)",
+        "config": {"workload": cfg["name"], "dims": list(cfg["dims"]), "beta": cfg["beta"], "n_max": cfg["n_max"],
+                   "nw": cfg["nw"]},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": procs, "kind": "port",
+                         "sample": "FP64 restatement of the reference (numpy), one process per host core, each "
+                                   "timing every stage on a slice (~2 s) and scaling it to one full step"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="cfg1")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

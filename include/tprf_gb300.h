@@ -1,0 +1,176 @@
+/*
+ * tprf_gb300 — C ABI of the GB300-native imaginary-time bubble + RPA path.
+ *
+ * Every entry point replaces one function of TPRF (TRIQS/tprf 3.2); the
+ * reference declaration each one stands in for is cited beside it
+ * (paths relative to the TPRF source tree).
+ *
+ * Conventions shared by all entry points
+ *  - Complex data is complex128, interleaved (re, im) doubles, passed as
+ *    `double*`. Layout is TRIQS gf data order: mesh indices first, then the
+ *    target indices, C order. Example: G(iv, k) is [2 n_iw, N_k, nb, nb].
+ *  - Fermionic Matsubara meshes are full meshes n = -n_iw .. n_iw-1
+ *    (2 n_iw points); bosonic meshes are m = -(nw-1) .. nw-1 (2 nw - 1
+ *    points); imaginary time has n_tau points tau_i = i beta / (n_tau - 1).
+ *  - k / r meshes are 3-dimensional `dims[3]` (unused dimensions 1), linear
+ *    index (i1 * n2 + i2) * n3 + i3.
+ *  - All pointers are DEVICE pointers owned by the caller; nothing is freed
+ *    or retained. `stream` is a cudaStream_t (NULL = legacy default stream).
+ *    Work is stream-ordered; a call returns after the launches are queued,
+ *    except where a synchronous check is enabled (tprf_set_sync_checks).
+ *  - Return value: TPRF_OK (0) or a negative status; no C++ exception ever
+ *    crosses the ABI. tprf_last_error() gives a one-line reason (per thread).
+ *  - The first call for a new mesh / FFT length builds a plan (twiddle and
+ *    tail tables, uploaded synchronously, cached for the process); make that
+ *    first call before capturing a stream into a CUDA graph.
+ *  - FFT lengths may be any integer: factors 2, 3, 4, 5, 7, 8 use fixed
+ *    butterflies, any other prime factor p a direct p-point stage (slower).
+ */
+#ifndef TPRF_GB300_H
+#define TPRF_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define TPRF_OK 0
+#define TPRF_ERR_INVALID_ARGUMENT (-1)  /* bad shape, null pointer, nb out of range */
+#define TPRF_ERR_UNSUPPORTED_SIZE (-2)  /* FFT tile does not fit one CTA (mesh dimension or time mesh too long) */
+#define TPRF_ERR_MESH_TOO_SHORT (-3)    /* time mesh shorter than 2x the frequency mesh (fourier_matsubara.cpp:105-108,128-131) */
+#define TPRF_ERR_TAIL_FIT (-4)          /* tail fit error above 1e-3 (fourier_matsubara.cpp:227-230) */
+#define TPRF_ERR_NONFINITE (-5)         /* NaN / Inf produced or found */
+#define TPRF_ERR_CUDA (-6)              /* a CUDA runtime call failed */
+#define TPRF_ERR_ALLOC (-7)             /* device allocation failed or workspace too small */
+#define TPRF_ERR_SINGULAR (-8)          /* exactly singular matrix in Dyson or RPA */
+
+const char *tprf_status_string(int status);
+const char *tprf_last_error(void);
+/* Library version, e.g. "0.1.0". */
+const char *tprf_version(void);
+
+/* When on (default), entry points that can detect data-dependent errors
+ * (tail-fit error, singular matrices) synchronise `stream` once at the end
+ * and report them. Switch off for CUDA-graph capture or pipelining; the
+ * device-side error word is then read by tprf_check_device_status. */
+void tprf_set_sync_checks(int on);
+int tprf_check_device_status(void *stream);
+
+/* Host-only (no GPU): the tail-fit definition tprf_fourier_wr_to_tr applies
+ * when moments == NULL. A least-squares fit of g(iv) ~ sum_{p<=P} c_p (iv)^-p
+ * on the outer 20% of the fermionic mesh (at most 30 points a side, both
+ * signs), the stand-in for TRIQS fit_tail called at
+ * fourier/fourier_matsubara.cpp:226. Writes n_fit and n_mom = P + 1; when rows
+ * and F are non-NULL and capacity >= n_fit * n_mom, also the data rows of the
+ * fit points and F [n_mom][n_fit] complex, with moments c = F g[rows]. */
+int tprf_tail_fit_matrix(double beta, int n_iw, int capacity, int *n_fit, int *n_mom, int *rows, double *F);
+
+/* Host-only: exact inverse of the 8x8 Vandermonde matrix V[m][j] = m^j
+ * (m = 1..8), the matrix fourier_matsubara.cpp:56-71 approximates (used by
+ * the fit_derivatives moments of the tau -> i omega transform). */
+void tprf_vandermonde_inverse8(double out[64]);
+
+/* ---- (a) Dyson equation -------------------------------------------------
+ * G(iv_n, k) = [(iv_n + mu) I - e(k) - Sigma]^-1, per (v, k).
+ * Replaces triqs_tprf::lattice_dyson_g0_wk(double mu, e_k_cvt, mesh::imfreq)
+ *   (c++/triqs_tprf/lattice/gf.hpp:44, gf.cpp:42-58) when sigma == NULL, and
+ * triqs_tprf::lattice_dyson_g_wk(double mu, e_k_cvt, g_w_cvt | g_wk_cvt)
+ *   (gf.hpp:83,123, gf.cpp:91-132) otherwise.
+ * e_k [n_k, nb, nb]; sigma_kind 0: none, 1: sigma_w [2 n_iw, nb, nb],
+ * 2: sigma_wk [2 n_iw, n_k, nb, nb]. g_wk [2 n_iw, n_k, nb, nb]. nb <= 8. */
+int tprf_lattice_dyson_g_wk(double beta, int n_iw, long n_k, int nb, double mu,
+                            const double *e_k, const double *sigma, int sigma_kind,
+                            double *g_wk, void *stream);
+
+/* ---- (b) lattice FFTs ---------------------------------------------------
+ * k -> r: FFTW_FORWARD over the k dims, divided by N_k, for each of n_w
+ * mesh slices and n_target target elements.
+ * Replaces triqs_tprf::fourier_wk_to_wr(g_wk_cvt) (gf.hpp:286, gf.cpp:209;
+ * lattice/fourier.hpp:166-197; fourier/fourier_lattice.cpp:39-50).
+ * in [n_w, N_k, n_target] -> out [n_w, N_r, n_target]; in == out allowed. */
+int tprf_fourier_wk_to_wr(long n_w, const int dims[3], long n_target,
+                          const double *g_wk, double *g_wr, void *stream);
+
+/* r -> k: FFTW_BACKWARD, unscaled.
+ * Replaces triqs_tprf::fourier_wr_to_wk (gf.cpp:214) and
+ * triqs_tprf::chi_wk_from_chi_wr(chi_wr_cvt) (lattice/chi_imtime.hpp:141,
+ * chi_imtime.cpp:289-292; lattice/fourier.hpp:200-231). */
+int tprf_fourier_wr_to_wk(long n_w, const int dims[3], long n_target,
+                          const double *g_wr, double *g_wk, void *stream);
+
+/* iv -> tau, fermionic, per r and target element, with the three-pole
+ * high-frequency tail model (fourier/fourier_matsubara.cpp:218-308).
+ * Replaces triqs_tprf::fourier_wr_to_tr(g_wr_cvt, int nt = -1)
+ *   (gf.hpp:306, gf.cpp:262; lattice/fourier.hpp:99-130).
+ * n_tau = -1 selects 6 n_iw + 1. moments == NULL: moments m1..m3 come from
+ * the least-squares tail fit (the reference's fit_tail call at
+ * fourier_matsubara.cpp:226); otherwise moments [3, n_r, n_target] holds
+ * m1, m2, m3. g_wr [2 n_iw, n_r, n_target] -> g_tr [n_tau, n_r, n_target]. */
+int tprf_fourier_wr_to_tr(double beta, int n_iw, int n_tau, long n_r, long n_target,
+                          const double *g_wr, const double *moments, double *g_tr,
+                          void *stream);
+
+/* ---- (c) bubble ----------------------------------------------------------
+ * chi0_abcd(tau_i, r) = G_da(tau_i, r) G_bc(tau_{n_tau-1-i}, -r).
+ * Replaces triqs_tprf::chi0_tr_from_grt_PH(g_tr_cvt)
+ *   (lattice/chi_imtime.hpp:38, chi_imtime.cpp:88-136).
+ * g_tr [n_tau, N_r, nb, nb] -> chi0_tr [n_tau, N_r, nb, nb, nb, nb]. */
+int tprf_chi0_tr_from_grt_PH(int n_tau, const int dims[3], int nb,
+                             const double *g_tr, double *chi0_tr, void *stream);
+
+/* Bubble fused with the bosonic tau -> i omega transform per r (chi0(tau, r)
+ * never materialised). Replaces triqs_tprf::chi0_wr_from_grt_PH(g_tr_cvt, int nw)
+ *   (chi_imtime.hpp:40, chi_imtime.cpp:139-182).
+ * -> chi0_wr [2 nw - 1, N_r, nb^4]. */
+int tprf_chi0_wr_from_grt_PH(double beta, int n_tau, int nw, const int dims[3], int nb,
+                             const double *g_tr, double *chi0_wr, void *stream);
+
+/* Bubble + trapezoid integral over tau (static chi0).
+ * Replaces triqs_tprf::chi0_w0r_from_grt_PH(g_tr_cvt) (chi_imtime.hpp:56,
+ * chi_imtime.cpp:185-228). -> chi0_wr [1, N_r, nb^4]. */
+int tprf_chi0_w0r_from_grt_PH(double beta, int n_tau, const int dims[3], int nb,
+                              const double *g_tr, double *chi0_wr, void *stream);
+
+/* Bosonic tau -> i omega with the fit_derivatives tail
+ * (fourier_matsubara.cpp:42-97,123-184).
+ * Replaces triqs_tprf::chi_wr_from_chi_tr(chi_tr_cvt, int nw)
+ *   (chi_imtime.hpp:104, chi_imtime.cpp:279-282; lattice/fourier.hpp:133-163).
+ * chi_tr [n_tau, n_r, n_target] -> chi_wr [2 nw - 1, n_r, n_target]. */
+int tprf_chi_wr_from_chi_tr(double beta, int n_tau, int nw, long n_r, long n_target,
+                            const double *chi_tr, double *chi_wr, void *stream);
+
+/* Trapezoid integral over tau.
+ * Replaces triqs_tprf::chi_w0r_from_chi_tr(chi_tr_cvt) (chi_imtime.hpp:82,
+ * chi_imtime.cpp:250-276). -> chi_wr [1, n_r, n_target]. */
+int tprf_chi_w0r_from_chi_tr(double beta, int n_tau, long n_r, long n_target,
+                             const double *chi_tr, double *chi_wr, void *stream);
+
+/* ---- (d) RPA --------------------------------------------------------------
+ * chi = [I - chi0 U]^-1 chi0 on PH-grouped (rows (a,b), columns (d,c))
+ * nb^2 x nb^2 matrices, for each of n_points (omega, q) points.
+ * Replaces triqs_tprf::solve_rpa_PH(chi_wk_vt, array_contiguous_view<dcomplex,4>)
+ *   (lattice/rpa.hpp:43, rpa.cpp:29-68).
+ * chi0 [n_points, nb, nb, nb, nb], U [nb, nb, nb, nb] -> chi (same as chi0).
+ * nb <= 5. */
+int tprf_solve_rpa_PH(long n_points, int nb, const double *chi0, const double *U,
+                      double *chi, void *stream);
+
+/* ---- whole chain ------------------------------------------------------------
+ * g_wk -> chi0_wk as triqs_tprf.lattice_utils.imtime_bubble_chi0_wk
+ * (python/triqs_tprf/lattice_utils.py:191-269): k->r, iv->tau, bubble, tau->iw
+ * (nw > 1) or trapezoid (nw == 1), r->q. chi0(tau, r) is never stored.
+ * Intermediate G(iv, r) and G(tau, r) live in the caller's workspace, whose
+ * size tprf_imtime_bubble_workspace_bytes returns. chi0_wk [2nw-1, N_k, nb^4]. */
+size_t tprf_imtime_bubble_workspace_bytes(int n_iw, int n_tau, const int dims[3], int nb);
+int tprf_imtime_bubble_chi0_wk(double beta, int n_iw, int n_tau, int nw, const int dims[3],
+                               int nb, const double *g_wk, const double *moments,
+                               double *chi0_wk, void *workspace, size_t workspace_bytes,
+                               void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TPRF_GB300_H */

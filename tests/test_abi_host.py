@@ -1,0 +1,100 @@
+"""CPU tests of the C-ABI library: it loads, exports what include/tprf_gb300.h
+declares, and its host-only logic (argument checks, tail-fit definition,
+Vandermonde table) agrees with the oracle. No kernel is launched."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+import oracle as O
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from tprf_gb300.build import build_library
+    build_library()
+    from tprf_gb300 import _native
+    return _native.lib()
+
+
+def declared_functions():
+    text = open(os.path.join(ROOT, "include", "tprf_gb300.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(tprf_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_every_declared_symbol_is_exported(lib):
+    from tprf_gb300 import _native
+    names = declared_functions()
+    assert len(names) >= 15
+    for name in names:
+        assert hasattr(lib, name), f"{name} declared but not exported"
+        assert name in _native.SIGNATURES, f"{name} has no ctypes signature"
+
+
+def test_status_strings(lib):
+    assert lib.tprf_version().decode() == "0.1.0"
+    assert lib.tprf_status_string(0).decode() == "ok"
+    assert "tail" in lib.tprf_status_string(-4).decode()
+
+
+def test_tail_fit_matrix_matches_oracle(lib):
+    for beta, n_max in [(10.0, 64), (20.0, 256), (40.0, 512), (5.0, 32), (0.544, 20), (2.0, 3)]:
+        nf, nm = ctypes.c_int(), ctypes.c_int()
+        assert lib.tprf_tail_fit_matrix(beta, n_max, 0, ctypes.byref(nf), ctypes.byref(nm), None, None) == 0
+        rows = (ctypes.c_int * nf.value)()
+        F = (ctypes.c_double * (2 * nf.value * nm.value))()
+        assert lib.tprf_tail_fit_matrix(beta, n_max, nf.value * nm.value, ctypes.byref(nf), ctypes.byref(nm),
+                                        rows, F) == 0
+        idx, Fo, _ = O.tail_fit_matrix(beta, n_max)
+        assert np.array_equal(np.array(rows[:]), idx)
+        Fc = np.frombuffer(F, dtype=np.complex128).reshape(nm.value, nf.value)
+        assert np.abs(Fc - Fo).max() <= 1e-10 * np.abs(Fo).max()
+
+
+def test_vandermonde_inverse_bitwise(lib):
+    v = (ctypes.c_double * 64)()
+    lib.tprf_vandermonde_inverse8(v)
+    assert np.array_equal(np.array(v[:]).reshape(8, 8), O.vandermonde_inverse(8))
+
+
+def test_argument_errors_are_reported_without_a_gpu(lib):
+    from tprf_gb300 import _native
+    fake = ctypes.c_void_p(0x1000)
+    # time mesh shorter than twice the frequency mesh (fourier_matsubara.cpp:128-131)
+    st = lib.tprf_fourier_wr_to_tr(1.0, 10, 15, 4, 1, fake, None, fake, None)
+    assert st == -3 and "twice" in lib.tprf_last_error().decode()
+    st = lib.tprf_chi_wr_from_chi_tr(1.0, 21, 11, 4, 1, fake, fake, None)
+    assert st == -3
+    assert lib.tprf_solve_rpa_PH(0, 2, fake, fake, fake, None) == -1
+    assert lib.tprf_lattice_dyson_g_wk(-1.0, 4, 4, 2, 0.0, fake, None, 0, fake, None) == -1
+    assert lib.tprf_fourier_wk_to_wr(1, _native.dims3((0, 1, 1)), 1, fake, fake, None) == -1
+    assert lib.tprf_imtime_bubble_chi0_wk(1.0, 4, 25, 2, _native.dims3((2, 2, 1)), 2, fake, None, fake, fake, 16,
+                                          None) == -7
+    with pytest.raises(_native.TprfError):
+        _native.check(lib.tprf_solve_rpa_PH(0, 2, fake, fake, fake, None), "solve_rpa_PH")
+
+
+def test_workspace_size(lib):
+    from tprf_gb300 import _native
+    n = lib.tprf_imtime_bubble_workspace_bytes(256, -1, _native.dims3((32, 32, 32)), 3)
+    expect = (512 + 1537) * 32768 * 9 * 16 + 256
+    assert n == expect
+
+
+def test_meshes():
+    from tprf_gb300.mesh import MeshBrZone, MeshImFreq, MeshImTime, MeshProduct
+    wf = MeshImFreq(10.0, "Fermion", 64)
+    wb = MeshImFreq(10.0, "Boson", 64)
+    assert len(wf) == 128 and len(wb) == 127
+    np.testing.assert_allclose(wf.values(), O.fermionic_iw(10.0, 64))
+    np.testing.assert_allclose(wb.values(), O.bosonic_iw(10.0, 64))
+    np.testing.assert_allclose(MeshImTime(10.0, "Fermion", 385).values(), O.tau_points(10.0, 385))
+    k = MeshBrZone(dims=(4, 2))
+    assert k.dims == (4, 2, 1) and len(k) == 8
+    np.testing.assert_allclose(k.values(), O.kpoints((4, 2, 1)))
+    assert len(MeshProduct(wf, k)) == 128 * 8

@@ -1,0 +1,265 @@
+"""Parity of every CUDA kernel with the FP64 oracle (``-m gpu``).
+
+Each test calls the C ABI through the ``tprf_gb300`` package on seeded inputs
+small enough for the oracle, and compares with the oracle at the relative bar
+PARITY_RTOL (max-abs error / max-abs value over the whole tensor). Mesh
+indexing (output shapes, frequency and time ordering) is checked exactly.
+"""
+import numpy as np
+import pytest
+import torch
+
+import oracle as O
+from conftest import PARITY_RTOL, rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def tp():
+    import tprf_gb300 as T
+    return T
+
+
+def gf_ek(hop, dims):
+    T = tp()
+    ek = O.ek_from_hoppings(hop, dims)
+    return ek, T.Gf(mesh=T.MeshBrZone(dims=dims), data=ek)
+
+
+def rand_c(rng, *shape):
+    return rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+
+
+# ---------------------------------------------------------------------------
+# (a) Dyson
+
+@pytest.mark.parametrize("nb", [1, 2, 3, 4, 5, 8])
+def test_dyson_g0_and_sigma(cuda_lib, nb):
+    T = tp()
+    rng = np.random.default_rng(nb)
+    dims = (4, 3, 2)
+    hop = {(1, 0, 0): rand_c(rng, nb, nb) * 0.3, (0, 1, 0): rand_c(rng, nb, nb) * 0.3}
+    hop = {**hop, **{tuple(-x for x in R): t.conj().T for R, t in hop.items()}}
+    ek, e_k = gf_ek(hop, dims)
+    beta, n_max, mu = 7.0, 10, 0.3
+    wmesh = T.MeshImFreq(beta, "Fermion", n_max)
+    g0 = T.lattice_dyson_g0_wk(mu, e_k, wmesh)
+    ref = O.lattice_dyson_g0_wk(mu, ek, beta, n_max)
+    assert tuple(g0.data.shape) == ref.shape
+    assert rel_err(g0.data, ref) < PARITY_RTOL
+    sig_w = rand_c(rng, 2 * n_max, nb, nb)
+    g1 = T.lattice_dyson_g_wk(mu, e_k, sigma_w=T.Gf(mesh=wmesh, data=sig_w))
+    assert rel_err(g1.data, O.lattice_dyson_g_wk(mu, ek, beta, n_max, sigma=sig_w)) < PARITY_RTOL
+    sig_wk = rand_c(rng, 2 * n_max, len(ek), nb, nb)
+    g2 = T.lattice_dyson_g_wk(mu, e_k, sigma_wk=T.Gf(mesh=T.MeshProduct(wmesh, e_k.mesh), data=sig_wk))
+    assert rel_err(g2.data, O.lattice_dyson_g_wk(mu, ek, beta, n_max, sigma=sig_wk)) < PARITY_RTOL
+
+
+def test_dyson_matches_numpy_inverse(cuda_lib):
+    """test/python/gf.py:60-73: G0 equals np.linalg.inv((iv + mu) I - e_k) per point."""
+    T = tp()
+    nb, dims, beta, mu, n_max = 2, (8, 1, 1), 3.0, 0.1, 16
+    hop = {(1,): np.array([[-1.0, 0.2], [0.2, -0.5]]), (-1,): np.array([[-1.0, 0.2], [0.2, -0.5]])}
+    ek, e_k = gf_ek(hop, dims)
+    g0 = T.lattice_dyson_g0_wk(mu, e_k, T.MeshImFreq(beta, "Fermion", n_max)).data.cpu().numpy()
+    iw = O.fermionic_iw(beta, n_max)
+    for n in range(2 * n_max):
+        for k in range(len(ek)):
+            ref = np.linalg.inv((iw[n] + mu) * np.eye(nb) - ek[k])
+            np.testing.assert_array_almost_equal(g0[n, k], ref, decimal=12)
+
+
+# ---------------------------------------------------------------------------
+# (b) lattice FFTs
+
+@pytest.mark.parametrize("dims", [(16, 16, 1), (4, 6, 5), (8, 1, 1), (7, 3, 10), (2, 2, 1), (1, 1, 1), (32, 8, 3),
+                                  (64, 1, 1), (24, 48, 1)])
+def test_lattice_fft(cuda_lib, dims):
+    from tprf_gb300 import _native
+    rng = np.random.default_rng(sum(dims))
+    nw, nt = 3, 5
+    x = rand_c(rng, nw, int(np.prod(dims)), nt)
+    xd = torch.as_tensor(x).cuda()
+    out = torch.empty_like(xd)
+    lib = _native.lib()
+    _native.check(lib.tprf_fourier_wk_to_wr(nw, _native.dims3(dims), nt, xd.data_ptr(), out.data_ptr(), None))
+    assert rel_err(out, O.fourier_wk_to_wr(x, dims)) < PARITY_RTOL
+    back = torch.empty_like(xd)
+    _native.check(lib.tprf_fourier_wr_to_wk(nw, _native.dims3(dims), nt, out.data_ptr(), back.data_ptr(), None))
+    assert rel_err(back, x) < PARITY_RTOL
+    # in place
+    _native.check(lib.tprf_fourier_wr_to_wk(nw, _native.dims3(dims), nt, xd.data_ptr(), xd.data_ptr(), None))
+    assert rel_err(xd, O.fourier_wr_to_wk(x, dims)) < PARITY_RTOL
+
+
+@pytest.mark.parametrize("dims", [(11, 1, 1), (13, 22, 1), (3, 17, 2), (41, 1, 1)])
+def test_lattice_fft_prime_lengths(cuda_lib, dims):
+    """FFTW takes any length; so do the generic-radix stages."""
+    from tprf_gb300 import _native
+    rng = np.random.default_rng(7)
+    x = rand_c(rng, 2, int(np.prod(dims)), 3)
+    xd = torch.as_tensor(x).cuda()
+    out = torch.empty_like(xd)
+    _native.check(_native.lib().tprf_fourier_wk_to_wr(2, _native.dims3(dims), 3, xd.data_ptr(), out.data_ptr(), None))
+    assert rel_err(out, O.fourier_wk_to_wr(x, dims)) < PARITY_RTOL
+
+
+# ---------------------------------------------------------------------------
+# (b) Matsubara transforms
+
+def _g_wr(hop, dims, beta, n_max, mu=0.0):
+    T = tp()
+    ek, e_k = gf_ek(hop, dims)
+    g_wk = T.lattice_dyson_g0_wk(mu, e_k, T.MeshImFreq(beta, "Fermion", n_max))
+    g_wr = T.fourier_wk_to_wr(g_wk)
+    ref = O.fourier_wk_to_wr(O.lattice_dyson_g0_wk(mu, ek, beta, n_max), dims)
+    assert rel_err(g_wr.data, ref) < PARITY_RTOL
+    return ek, g_wk, g_wr, ref
+
+
+CASES = [
+    (lambda: {(0, 1): -np.eye(1), (0, -1): -np.eye(1), (1, 0): -np.eye(1), (-1, 0): -np.eye(1)}, (8, 8, 1), 10.0, 64),
+    (lambda: __import__("tprf_gb300.workloads", fromlist=["x"]).cubic_3orb(0), (4, 4, 4), 20.0, 32),
+    (lambda: __import__("tprf_gb300.workloads", fromlist=["x"]).square_2orb(1), (6, 6, 1), 5.0, 45),
+]
+
+
+@pytest.mark.parametrize("case", range(len(CASES)))
+@pytest.mark.parametrize("mode", ["fit", "moments"])
+def test_nu_to_tau(cuda_lib, case, mode):
+    T = tp()
+    hopf, dims, beta, n_max = CASES[case]
+    hop = hopf()
+    ek, _, g_wr, g_wr_ref = _g_wr(hop, dims, beta, n_max)
+    mom = O.g0_tail_moments_wr(ek, 0.0, dims) if mode == "moments" else None
+    g_tr = T.fourier_wr_to_tr(g_wr, moments=mom)
+    ref = O.fourier_wr_to_tr(g_wr_ref, beta, moments=mom)
+    assert tuple(g_tr.data.shape) == ref.shape == (6 * n_max + 1,) + g_wr_ref.shape[1:]
+    assert rel_err(g_tr.data, ref) < PARITY_RTOL
+    for nt in (5 * n_max + 1, 4 * n_max + 7):  # a 5-smooth and a generic-prime time mesh
+        g_tr2 = T.fourier_wr_to_tr(g_wr, nt=nt, moments=mom)
+        assert rel_err(g_tr2.data, O.fourier_wr_to_tr(g_wr_ref, beta, nt, moments=mom)) < PARITY_RTOL
+
+
+def test_nu_to_tau_tail_fit_error_is_reported(cuda_lib):
+    T = tp()
+    rng = np.random.default_rng(3)
+    wmesh, rmesh = T.MeshImFreq(2.0, "Fermion", 16), T.MeshCycLat(dims=(2, 1, 1))
+    g = T.Gf(mesh=T.MeshProduct(wmesh, rmesh), data=rand_c(rng, 32, 2, 1, 1))
+    with pytest.raises(RuntimeError, match="1e-3"):
+        T.fourier_wr_to_tr(g)
+
+
+@pytest.mark.parametrize("nw", [1, 2, 16, 64])
+def test_tau_to_w(cuda_lib, nw):
+    T = tp()
+    hopf, dims, beta, n_max = CASES[0]
+    _, _, g_wr, g_wr_ref = _g_wr(hopf(), dims, beta, n_max)
+    g_tr_ref = O.fourier_wr_to_tr(g_wr_ref, beta)
+    chi_tr_ref = O.chi0_tr_from_grt_PH(g_tr_ref, dims)
+    tmesh = T.MeshImTime(beta, "Boson", chi_tr_ref.shape[0])
+    chi_tr = T.Gf(mesh=T.MeshProduct(tmesh, T.MeshCycLat(dims=dims)), data=chi_tr_ref)
+    chi_wr = T.chi_wr_from_chi_tr(chi_tr, nw)
+    ref = O.chi_wr_from_chi_tr(chi_tr_ref, beta, nw)
+    assert tuple(chi_wr.data.shape) == ref.shape == (2 * nw - 1,) + chi_tr_ref.shape[1:]
+    assert rel_err(chi_wr.data, ref) < PARITY_RTOL
+    assert rel_err(T.chi_w0r_from_chi_tr(chi_tr).data, O.chi_w0r_from_chi_tr(chi_tr_ref, beta)) < PARITY_RTOL
+
+
+# ---------------------------------------------------------------------------
+# (c) bubble
+
+@pytest.mark.parametrize("case", range(len(CASES)))
+def test_bubble_variants(cuda_lib, case):
+    T = tp()
+    hopf, dims, beta, n_max = CASES[case]
+    _, _, g_wr, g_wr_ref = _g_wr(hopf(), dims, beta, n_max)
+    g_tr = T.fourier_wr_to_tr(g_wr)
+    g_tr_ref = O.fourier_wr_to_tr(g_wr_ref, beta)
+    chi_tr = T.chi0_tr_from_grt_PH(g_tr)
+    chi_tr_ref = O.chi0_tr_from_grt_PH(g_tr_ref, dims)
+    assert rel_err(chi_tr.data, chi_tr_ref) < PARITY_RTOL
+    nw = min(16, n_max)
+    fused = T.chi0_wr_from_grt_PH(g_tr, nw)
+    assert rel_err(fused.data, O.chi_wr_from_chi_tr(chi_tr_ref, beta, nw)) < PARITY_RTOL
+    assert rel_err(T.chi0_w0r_from_grt_PH(g_tr).data, O.chi0_w0r_from_grt_PH(g_tr_ref, beta, dims)) < PARITY_RTOL
+
+
+# ---------------------------------------------------------------------------
+# (d) RPA
+
+@pytest.mark.parametrize("nb", [1, 2, 3, 4, 5])
+def test_rpa_random(cuda_lib, nb):
+    T = tp()
+    rng = np.random.default_rng(10 + nb)
+    npts = 300
+    chi0 = 0.1 * rand_c(rng, 3, npts // 3, nb, nb, nb, nb)
+    U = 0.5 * rand_c(rng, nb, nb, nb, nb)
+    mesh = T.MeshProduct(T.MeshImFreq(1.0, "Boson", 2), T.MeshBrZone(dims=(npts // 3, 1, 1)))
+    chi = T.solve_rpa_PH(T.Gf(mesh=mesh, data=chi0), U)
+    assert rel_err(chi.data, O.solve_rpa_PH(chi0, U)) < PARITY_RTOL
+
+
+def test_rpa_singular_is_reported(cuda_lib):
+    T = tp()
+    mesh = T.MeshProduct(T.MeshImFreq(1.0, "Boson", 1), T.MeshBrZone(dims=(1, 1, 1)))
+    chi0 = T.Gf(mesh=mesh, data=np.ones((1, 1, 1, 1, 1, 1), complex))
+    with pytest.raises(RuntimeError, match="singular"):
+        T.solve_rpa_PH(chi0, np.ones((1, 1, 1, 1), complex))
+
+
+# ---------------------------------------------------------------------------
+# whole chain and the reference's known answers
+
+@pytest.mark.parametrize("nw", [1, 8])
+@pytest.mark.parametrize("case", range(len(CASES)))
+def test_imtime_bubble_chain_and_rpa(cuda_lib, case, nw):
+    T = tp()
+    hopf, dims, beta, n_max = CASES[case]
+    hop = hopf()
+    ek, g_wk, _, _ = _g_wr(hop, dims, beta, n_max)
+    chi0 = T.imtime_bubble_chi0_wk(g_wk, nw=nw, verbose=False)
+    ref = O.imtime_bubble_chi0_wk(O.lattice_dyson_g0_wk(0.0, ek, beta, n_max), beta, dims, nw=nw)
+    assert tuple(chi0.data.shape) == ref.shape
+    assert rel_err(chi0.data, ref) < PARITY_RTOL
+    nb = ek.shape[-1]
+    rng = np.random.default_rng(case)
+    U = 0.3 * (rng.standard_normal((nb,) * 4) + 0j)
+    chi = T.solve_rpa_PH(chi0, U)
+    assert rel_err(chi.data, O.solve_rpa_PH(ref, U)) < PARITY_RTOL
+
+
+def test_lindhard_square_lattice_known_answer(cuda_lib):
+    """test/python/chi00_square_lattice.py:90-180 through the CUDA path."""
+    import os
+    T = tp()
+    f = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "lindhard_square_2orb.npz")))
+    dims, beta = tuple(int(x) for x in f["dims"]), float(f["beta"])
+    e_k = T.Gf(mesh=T.MeshBrZone(dims=dims), data=f["e_k"])
+    g0 = T.lattice_dyson_g0_wk(0.0, e_k, T.MeshImFreq(beta, "Fermion", 500))
+    g_tr = T.fourier_wr_to_tr(T.fourier_wk_to_wr(g0))
+    chi_wr = T.chi_wr_from_chi_tr(T.chi0_tr_from_grt_PH(g_tr), 1)
+    lin_wr = O.chi_wr_from_chi_wk(f["chi00_wk_nw1"], dims)
+    np.testing.assert_array_almost_equal(lin_wr, chi_wr.data.cpu().numpy(), decimal=8)
+    chi_wk = T.imtime_bubble_chi0_wk(g0, nw=4, verbose=False)
+    np.testing.assert_array_almost_equal(f["chi00_wk_nw4"], chi_wk.data.cpu().numpy(), decimal=7)
+    np.testing.assert_array_almost_equal(f["chi00_wk_nw1"][0], T.imtime_bubble_chi0_wk(g0, nw=1, verbose=False)
+                                         .data.cpu().numpy()[0], decimal=4)
+
+
+def test_kanamori_rpa_closed_form(cuda_lib):
+    """test/python/mean_field_kanamori.py:52-162 through the CUDA path."""
+    import os
+    T = tp()
+    f = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "kanamori_1d_q0.npz")))
+    beta, U, J = float(f["beta"]), float(f["U"]), float(f["J"])
+    hop = {(1,): -np.eye(4), (-1,): -np.eye(4)}
+    _, e_k = gf_ek(hop, (256, 1, 1))
+    g0 = T.lattice_dyson_g0_wk(0.0, e_k, T.MeshImFreq(beta, "Fermion", 20))
+    chi00 = T.imtime_bubble_chi0_wk(g0, nw=1, verbose=False)
+    perm = [0, 2, 1, 3]
+    U_abcd = O.kanamori_quartic_tensor(2, U, U - 2 * J, J, J)[np.ix_(perm, perm, perm, perm)]
+    chi = T.solve_rpa_PH(chi00, U_abcd).data.cpu().numpy()
+    Sz = 0.5 * np.diag([1.0, -1.0, 1.0, -1.0])
+    szsz = np.einsum("wkabcd,ab,cd->wk", chi, Sz, Sz)
+    np.testing.assert_array_almost_equal(szsz[0, 0].real, f["chi_szsz_q0"])

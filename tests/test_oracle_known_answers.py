@@ -1,0 +1,140 @@
+"""Pin the FP64 oracle against the known answers of the reference's own tests.
+
+Tolerances are the reference tests' own (``np.testing`` decimal = d means
+|diff| < 1.5 * 10**-d). Files cited relative to the TPRF source tree.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def _load(name):
+    return dict(np.load(os.path.join(GOLDEN, name)))
+
+
+def test_lindhard_square_lattice():
+    """test/python/chi00_square_lattice.py:90-180 (n_max = 500)."""
+    f = _load("lindhard_square_2orb.npz")
+    dims, beta, mu, ek = tuple(f["dims"]), float(f["beta"]), float(f["mu"]), f["e_k"]
+    g0 = O.lattice_dyson_g0_wk(mu, ek, beta, 500)
+    g0_tr = O.fourier_wr_to_tr(O.fourier_wk_to_wr(g0, dims), beta)
+    chi_tr = O.chi0_tr_from_grt_PH(g0_tr, dims)
+    lin_wr = O.chi_wr_from_chi_wk(f["chi00_wk_nw1"], dims)
+    np.testing.assert_array_almost_equal(lin_wr, O.chi_wr_from_chi_tr(chi_tr, beta, 1), decimal=8)
+    np.testing.assert_array_almost_equal(lin_wr, O.chi_w0r_from_chi_tr(chi_tr, beta), decimal=4)
+    np.testing.assert_array_almost_equal(lin_wr, O.chi0_w0r_from_grt_PH(g0_tr, beta, dims), decimal=4)
+    chi_wk = O.chi_wk_from_chi_wr(O.chi_wr_from_chi_tr(chi_tr, beta, 1), dims)
+    np.testing.assert_array_almost_equal(f["chi00_wk_nw1"][0], chi_wk[0], decimal=7)
+    np.testing.assert_array_almost_equal(f["chi00_wk_nw1"][0], O.imtime_bubble_chi0_wk(g0, beta, dims, nw=1)[0],
+                                         decimal=4)
+    # all bosonic frequencies, not only w = 0 (same bar as the w = 0 comparison)
+    np.testing.assert_array_almost_equal(f["chi00_wk_nw4"], O.imtime_bubble_chi0_wk(g0, beta, dims, nw=4), decimal=7)
+
+
+def _chain_1d(nk, nb, beta, mu, n_max, t=1.0):
+    hop = {(0,): np.zeros((nb, nb)), (1,): -t * np.eye(nb), (-1,): -t * np.eye(nb)}
+    dims = (nk, 1, 1)
+    ek = O.ek_from_hoppings(hop, dims)
+    return ek, dims, O.lattice_dyson_g0_wk(mu, ek, beta, n_max)
+
+
+def test_hubbard_1d_bubble_and_fazekas_rpa():
+    """test/python/mean_field.py:295-351 (half filling, m = 0: e(k) = -2 t cos k, mu = 0)."""
+    f = _load("hubbard_1d_q0.npz")
+    beta, U = float(f["beta"]), float(f["U"])
+    ek, dims, g0 = _chain_1d(128, 2, beta, 0.0, 400)
+    chi00 = O.imtime_bubble_chi0_wk(g0, beta, dims, nw=1)
+    lin = O.lindhard_chi00(ek, dims, beta, 0.0, 1)
+    np.testing.assert_almost_equal(chi00, lin, decimal=5)
+    np.testing.assert_almost_equal(lin[0, 0, 0, 0, 0, 0], f["chi0_q0"])
+    U_abcd = O.kanamori_quartic_tensor(1, U, 0.0, 0.0, 0.0)
+    chi = O.solve_rpa_PH(chi00, U_abcd)
+    Sz = 0.5 * np.diag([1.0, -1.0])
+    szsz = np.einsum("wkabcd,ab,cd->wk", chi, Sz, Sz)
+    np.testing.assert_almost_equal(szsz[0, 0], f["chi_szsz_q0"])
+
+
+def test_kanamori_1d_rpa_closed_form():
+    """test/python/mean_field_kanamori.py:52-162 (2 orbitals x spin, spin fastest)."""
+    f = _load("kanamori_1d_q0.npz")
+    beta, U, J = float(f["beta"]), float(f["U"]), float(f["J"])
+    ek, dims, g0 = _chain_1d(256, 4, beta, 0.0, 20)
+    chi00 = O.imtime_bubble_chi0_wk(g0, beta, dims, nw=1)
+    # Kanamori vertex (U' = U - 2J, J' = J), spin slow -> spin fast (up_0, do_0, up_1, do_1)
+    Us = O.kanamori_quartic_tensor(2, U, U - 2 * J, J, J)
+    perm = [0, 2, 1, 3]
+    U_abcd = Us[np.ix_(perm, perm, perm, perm)]
+    chi = O.solve_rpa_PH(chi00, U_abcd)
+    Sz = 0.5 * np.diag([1.0, -1.0, 1.0, -1.0])
+    szsz = np.einsum("wkabcd,ab,cd->wk", chi, Sz, Sz)
+    np.testing.assert_array_almost_equal(szsz[0, 0].real, f["chi_szsz_q0"])
+
+
+def test_k_r_round_trip():
+    """test/python/g_wk_to_from_g_wr_py.py:13-31 (10 x 10, n_max = 1024, mu = 1)."""
+    hop = {(1, 0): -np.eye(1), (-1, 0): -np.eye(1), (0, 1): -np.eye(1), (0, -1): -np.eye(1)}
+    dims = (10, 10, 1)
+    g0 = O.lattice_dyson_g0_wk(1.0, O.ek_from_hoppings(hop, dims), 1.0, 1024)
+    np.testing.assert_array_almost_equal(g0, O.fourier_wr_to_wk(O.fourier_wk_to_wr(g0, dims), dims))
+
+
+def test_save_memory_equals_plain():
+    """test/python/chi0_save_memory.py:27-48 (create_model_for_tests, norb 2, dim 2)."""
+    t_mat = -np.array([[1.0, 0.1], [0.1, 0.5]])
+    hop = {(1, 0): t_mat, (-1, 0): t_mat, (0, 1): t_mat, (0, -1): t_mat}
+    dims = (2, 2, 1)
+    g0 = O.lattice_dyson_g0_wk(0.0, O.ek_from_hoppings(hop, dims), 1.0, 20)
+    a = O.imtime_bubble_chi0_wk(g0, 1.0, dims, nw=10, save_memory=False)
+    b = O.imtime_bubble_chi0_wk(g0, 1.0, dims, nw=10, save_memory=True)
+    assert np.allclose(a, b)
+
+
+def test_vandermonde_inverse_is_exact():
+    V = np.array([[float(m) ** j for j in range(8)] for m in range(1, 9)])
+    Vi = O.vandermonde_inverse(8)
+    assert np.abs(Vi @ V - np.eye(8)).max() < 1e-8
+    assert Vi[1, 3] == 172.75 and Vi[0, 0] == 8.0
+
+
+def test_fit_derivatives_table_sensitivity():
+    """The reference hard-codes a rounded copy of the 8x8 table
+    (fourier_matsubara.cpp:56-71; entries off by up to ~3.5e-12 relative), the
+    oracle and the CUDA path use the exact rationals. Perturbing the table by
+    1e-11 relative (about 3x that rounding) moves chi(i w) by < 1e-11 relative."""
+    f = _load("lindhard_square_2orb.npz")
+    dims, beta, ek = tuple(f["dims"]), float(f["beta"]), f["e_k"]
+    g0 = O.lattice_dyson_g0_wk(0.0, ek, beta, 64)
+    chi_tr = O.chi0_tr_from_grt_PH(O.fourier_wr_to_tr(O.fourier_wk_to_wr(g0, dims), beta), dims)
+    base = O.chi_wr_from_chi_tr(chi_tr, beta, 16)
+    saved = O.tprf_oracle._VINV.copy()
+    try:
+        rng = np.random.default_rng(1)
+        O.tprf_oracle._VINV[...] = saved * (1 + 1e-11 * rng.standard_normal(saved.shape))
+        pert = O.chi_wr_from_chi_tr(chi_tr, beta, 16)
+    finally:
+        O.tprf_oracle._VINV[...] = saved
+    assert np.abs(pert - base).max() / np.abs(base).max() < 1e-11
+
+
+def test_tail_fit_recovers_exact_g0_moments():
+    f = _load("lindhard_square_2orb.npz")
+    dims, beta, ek = tuple(f["dims"]), float(f["beta"]), f["e_k"]
+    g_wr = O.fourier_wk_to_wr(O.lattice_dyson_g0_wk(0.0, ek, beta, 256), dims)
+    g_fit, mom = O.fourier_wr_to_tr(g_wr, beta, return_moments=True)
+    exact = O.g0_tail_moments_wr(ek, 0.0, dims)
+    assert np.abs(mom - exact).max() < 1e-5
+    g_exact = O.fourier_wr_to_tr(g_wr, beta, moments=exact)
+    assert np.abs(g_fit - g_exact).max() < 1e-9
+
+
+def test_mesh_too_short_raises():
+    g = np.zeros((2 * 10, 1, 1, 1), complex)
+    with pytest.raises(RuntimeError):
+        O.fourier_wr_to_tr(g, 1.0, n_tau=20)
+    with pytest.raises(RuntimeError):
+        O.chi_wr_from_chi_tr(np.zeros((21, 1), complex), 1.0, nw=11)

@@ -1,0 +1,89 @@
+"""ctypes binding of the C ABI in ``include/tprf_gb300.h``.
+
+The CUDA library is the only compute path: if it is missing or cannot be
+loaded, every call raises. There is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+_LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "libtprf_gb300.so")
+_lock = threading.Lock()
+_lib = None
+
+c_int, c_long, c_double, c_void_p, c_size_t = ctypes.c_int, ctypes.c_long, ctypes.c_double, ctypes.c_void_p, ctypes.c_size_t
+c_int3 = ctypes.c_int * 3
+
+# name -> (restype, argtypes); mirrors include/tprf_gb300.h
+SIGNATURES = {
+    "tprf_status_string": (ctypes.c_char_p, [c_int]),
+    "tprf_last_error": (ctypes.c_char_p, []),
+    "tprf_version": (ctypes.c_char_p, []),
+    "tprf_set_sync_checks": (None, [c_int]),
+    "tprf_check_device_status": (c_int, [c_void_p]),
+    "tprf_tail_fit_matrix": (c_int, [c_double, c_int, c_int, ctypes.POINTER(c_int), ctypes.POINTER(c_int),
+                                     ctypes.POINTER(c_int), ctypes.POINTER(c_double)]),
+    "tprf_vandermonde_inverse8": (None, [ctypes.POINTER(c_double)]),
+    "tprf_lattice_dyson_g_wk": (c_int, [c_double, c_int, c_long, c_int, c_double, c_void_p, c_void_p, c_int,
+                                        c_void_p, c_void_p]),
+    "tprf_fourier_wk_to_wr": (c_int, [c_long, c_int3, c_long, c_void_p, c_void_p, c_void_p]),
+    "tprf_fourier_wr_to_wk": (c_int, [c_long, c_int3, c_long, c_void_p, c_void_p, c_void_p]),
+    "tprf_fourier_wr_to_tr": (c_int, [c_double, c_int, c_int, c_long, c_long, c_void_p, c_void_p, c_void_p,
+                                      c_void_p]),
+    "tprf_chi0_tr_from_grt_PH": (c_int, [c_int, c_int3, c_int, c_void_p, c_void_p, c_void_p]),
+    "tprf_chi0_wr_from_grt_PH": (c_int, [c_double, c_int, c_int, c_int3, c_int, c_void_p, c_void_p, c_void_p]),
+    "tprf_chi0_w0r_from_grt_PH": (c_int, [c_double, c_int, c_int3, c_int, c_void_p, c_void_p, c_void_p]),
+    "tprf_chi_wr_from_chi_tr": (c_int, [c_double, c_int, c_int, c_long, c_long, c_void_p, c_void_p, c_void_p]),
+    "tprf_chi_w0r_from_chi_tr": (c_int, [c_double, c_int, c_long, c_long, c_void_p, c_void_p, c_void_p]),
+    "tprf_solve_rpa_PH": (c_int, [c_long, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "tprf_imtime_bubble_workspace_bytes": (c_size_t, [c_int, c_int, c_int3, c_int]),
+    "tprf_imtime_bubble_chi0_wk": (c_int, [c_double, c_int, c_int, c_int, c_int3, c_int, c_void_p, c_void_p,
+                                           c_void_p, c_void_p, c_size_t, c_void_p]),
+}
+
+
+class TprfError(RuntimeError):
+    """Raised when a tprf_gb300 entry point returns a non-zero status."""
+
+    def __init__(self, status: int, message: str):
+        super().__init__(message)
+        self.status = status
+
+
+def library_path() -> str:
+    return _LIB_PATH
+
+
+def lib():
+    """Load (once) and return the CUDA library; raise if it is not built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(_LIB_PATH):
+                raise RuntimeError(
+                    f"tprf_gb300 CUDA library not found at {_LIB_PATH}; build it with "
+                    "tprf_gb300.build.build_library() (there is no CPU fallback)")
+            import torch  # noqa: F401  (load torch's CUDA runtime first so both share it)
+            handle = ctypes.CDLL(_LIB_PATH)
+            for name, (res, args) in SIGNATURES.items():
+                fn = getattr(handle, name)
+                fn.restype = res
+                fn.argtypes = args
+            _lib = handle
+    return _lib
+
+
+def check(status: int, what: str = "") -> None:
+    if status != 0:
+        l = lib()
+        msg = l.tprf_last_error().decode() or l.tprf_status_string(status).decode()
+        raise TprfError(status, f"{what}: {msg}" if what else msg)
+
+
+def dims3(dims) -> ctypes.Array:
+    d = list(dims) + [1] * (3 - len(dims))
+    return c_int3(*[int(x) for x in d[:3]])

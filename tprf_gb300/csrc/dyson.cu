@@ -1,0 +1,173 @@
+// Kernel (a): the Dyson equation G(iv_n, k) = [(iv_n + mu) I - e(k) - Sigma]^-1,
+// one complex128 nb x nb inversion per (v, k) point.
+//
+// Restates c++/triqs_tprf/lattice/gf.cpp:42-58 (lattice_dyson_g0_Xk) and
+// gf.cpp:91-123 (lattice_dyson_g_Xk): same matrix, (w + mu) I - e_k[k] - sigma,
+// inverted per point (the reference calls nda::inverse, an LU-based inverse).
+//
+// Design: one thread per point; the matrix lives in registers and is inverted
+// in place by Gauss-Jordan elimination with partial pivoting. Row swaps use
+// compile-time indices with predicated selects and the final column
+// permutation is folded into the store addresses, so the matrix stays in
+// registers (nb <= 5; larger nb spill but stay correct).
+#include "common.cuh"
+
+namespace tprf {
+namespace {
+
+template <int NB>
+__device__ __forceinline__ void swap_rows_if(double2 (&M)[NB][NB], int j, int p) {
+#pragma unroll
+  for (int i = 0; i < NB; ++i) {
+    if (i > j && i == p) {
+#pragma unroll
+      for (int c = 0; c < NB; ++c) {
+        double2 t = M[i][c];
+        M[i][c] = M[j][c];
+        M[j][c] = t;
+      }
+    }
+  }
+}
+
+// In-place Gauss-Jordan inverse of the row-pivoted matrix. The inverse of the
+// original matrix is M with its columns permuted; the permutation is returned
+// packed (destination column of column c in bits [4c, 4c+4)) and applied by
+// the caller when storing, so no register array is indexed at run time.
+// Returns false on an exactly zero pivot.
+template <int NB>
+__device__ __forceinline__ bool invert_in_place(double2 (&M)[NB][NB], unsigned &dest) {
+  unsigned perm = 0u;  // pivot row of step j in bits [4j, 4j+4)
+  bool ok = true;
+#pragma unroll
+  for (int j = 0; j < NB; ++j) {
+    int p = j;
+    double best = cabs2(M[j][j]);
+#pragma unroll
+    for (int i = j + 1; i < NB; ++i) {
+      const double v = cabs2(M[i][j]);
+      if (v > best) {
+        best = v;
+        p = i;
+      }
+    }
+    perm |= (unsigned)p << (4 * j);
+    swap_rows_if<NB>(M, j, p);
+    if (best == 0.0) ok = false;
+    const double2 inv = crecip(M[j][j]);
+    M[j][j] = make_double2(1.0, 0.0);
+#pragma unroll
+    for (int c = 0; c < NB; ++c) M[j][c] = cmul(M[j][c], inv);
+#pragma unroll
+    for (int i = 0; i < NB; ++i) {
+      if (i != j) {
+        const double2 f = M[i][j];
+        M[i][j] = make_double2(0.0, 0.0);
+#pragma unroll
+        for (int c = 0; c < NB; ++c) M[i][c] = cfms(f, M[j][c], M[i][c]);
+      }
+    }
+  }
+  // The row swaps become column swaps of the inverse, applied last pivot first.
+  dest = 0u;
+#pragma unroll
+  for (int c = 0; c < NB; ++c) dest |= (unsigned)c << (4 * c);
+#pragma unroll
+  for (int jj = 0; jj < NB; ++jj) {
+    const unsigned j = NB - 1 - jj;
+    const unsigned p = (perm >> (4 * j)) & 15u;
+#pragma unroll
+    for (int c = 0; c < NB; ++c) {
+      const unsigned d = (dest >> (4 * c)) & 15u;
+      const unsigned nd = (d == j) ? p : ((d == p) ? j : d);
+      dest = (dest & ~(15u << (4 * c))) | (nd << (4 * c));
+    }
+  }
+  return ok;
+}
+
+template <int NB>
+__global__ void __launch_bounds__(128) dyson_kernel(double beta, int n_iw, long n_k, double mu,
+                                                    const double2 *__restrict__ e_k,
+                                                    const double2 *__restrict__ sigma, int sigma_kind,
+                                                    double2 *__restrict__ g, unsigned *status) {
+  const long total = 2L * n_iw * n_k;
+  for (long idx = blockIdx.x * (long)blockDim.x + threadIdx.x; idx < total; idx += (long)gridDim.x * blockDim.x) {
+    const int n = (int)(idx / n_k);
+    const long k = idx - (long)n * n_k;
+    const double nu = (2.0 * (n - n_iw) + 1.0) * M_PI / beta;
+    double2 M[NB][NB];
+    const double2 *ek = e_k + k * NB * NB;
+#pragma unroll
+    for (int i = 0; i < NB; ++i)
+#pragma unroll
+      for (int j = 0; j < NB; ++j) {
+        const double2 e = ek[i * NB + j];
+        M[i][j] = (i == j) ? make_double2(mu - e.x, nu - e.y) : make_double2(-e.x, -e.y);
+      }
+    if (sigma_kind != 0) {
+      const double2 *s = (sigma_kind == 1) ? sigma + (long)n * NB * NB : sigma + idx * NB * NB;
+#pragma unroll
+      for (int i = 0; i < NB; ++i)
+#pragma unroll
+        for (int j = 0; j < NB; ++j) M[i][j] = csub(M[i][j], s[i * NB + j]);
+    }
+    unsigned dest;
+    if (!invert_in_place<NB>(M, dest)) atomicOr(status, kDevErrSingular);
+    double2 *out = g + idx * NB * NB;
+#pragma unroll
+    for (int j = 0; j < NB; ++j) {
+      const int dj = (int)((dest >> (4 * j)) & 15u);
+#pragma unroll
+      for (int i = 0; i < NB; ++i) out[i * NB + dj] = M[i][j];
+    }
+  }
+}
+
+template <int NB>
+int launch_dyson_nb(double beta, int n_iw, long n_k, double mu, const double2 *e_k, const double2 *sigma,
+                    int sigma_kind, double2 *g, cudaStream_t stream, unsigned *status) {
+  const long total = 2L * n_iw * n_k;
+  const int threads = 128;
+  long blocks = (total + threads - 1) / threads;
+  const long cap = (long)num_sms() * 16;
+  if (blocks > cap) blocks = cap;
+  dyson_kernel<NB><<<(unsigned)blocks, threads, 0, stream>>>(beta, n_iw, n_k, mu, e_k, sigma, sigma_kind, g, status);
+  TPRF_LAUNCH_CHECK("dyson_kernel");
+  return TPRF_OK;
+}
+
+}  // namespace
+
+int launch_dyson(double beta, int n_iw, long n_k, int nb, double mu, const double2 *e_k, const double2 *sigma,
+                 int sigma_kind, double2 *g, cudaStream_t stream) {
+  unsigned *status = device_status_word();
+  if (!status) return TPRF_ERR_CUDA;
+  switch (nb) {
+    case 1: return launch_dyson_nb<1>(beta, n_iw, n_k, mu, e_k, sigma, sigma_kind, g, stream, status);
+    case 2: return launch_dyson_nb<2>(beta, n_iw, n_k, mu, e_k, sigma, sigma_kind, g, stream, status);
+    case 3: return launch_dyson_nb<3>(beta, n_iw, n_k, mu, e_k, sigma, sigma_kind, g, stream, status);
+    case 4: return launch_dyson_nb<4>(beta, n_iw, n_k, mu, e_k, sigma, sigma_kind, g, stream, status);
+    case 5: return launch_dyson_nb<5>(beta, n_iw, n_k, mu, e_k, sigma, sigma_kind, g, stream, status);
+    case 6: return launch_dyson_nb<6>(beta, n_iw, n_k, mu, e_k, sigma, sigma_kind, g, stream, status);
+    case 7: return launch_dyson_nb<7>(beta, n_iw, n_k, mu, e_k, sigma, sigma_kind, g, stream, status);
+    case 8: return launch_dyson_nb<8>(beta, n_iw, n_k, mu, e_k, sigma, sigma_kind, g, stream, status);
+    default: return set_error(TPRF_ERR_INVALID_ARGUMENT, "lattice_dyson_g_wk: nb must be 1..8");
+  }
+}
+
+}  // namespace tprf
+
+extern "C" int tprf_lattice_dyson_g_wk(double beta, int n_iw, long n_k, int nb, double mu, const double *e_k,
+                                       const double *sigma, int sigma_kind, double *g_wk, void *stream) {
+  using namespace tprf;
+  if (!(beta > 0.0) || n_iw < 1 || n_k < 1 || !e_k || !g_wk)
+    return set_error(TPRF_ERR_INVALID_ARGUMENT, "lattice_dyson_g_wk: bad mesh or null pointer");
+  if (sigma_kind < 0 || sigma_kind > 2 || (sigma_kind != 0 && !sigma))
+    return set_error(TPRF_ERR_INVALID_ARGUMENT, "lattice_dyson_g_wk: bad sigma_kind / sigma");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int st = launch_dyson(beta, n_iw, n_k, nb, mu, reinterpret_cast<const double2 *>(e_k),
+                        reinterpret_cast<const double2 *>(sigma), sigma_kind, reinterpret_cast<double2 *>(g_wk), s);
+  if (st) return st;
+  return finish_with_checks(s, "lattice_dyson_g_wk");
+}

@@ -1,0 +1,90 @@
+// Internal declarations shared by the tprf_gb300 CUDA translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <string>
+
+#include "../../include/tprf_gb300.h"
+
+namespace tprf {
+
+// ---------------------------------------------------------------------------
+// Errors: every entry point returns a status; a one-line reason is kept per
+// thread for tprf_last_error().
+int set_error(int status, const std::string &msg);
+int cuda_status(cudaError_t e, const char *what);
+#define TPRF_CUDA(call)                                              \
+  do {                                                               \
+    cudaError_t e_ = (call);                                         \
+    if (e_ != cudaSuccess) return ::tprf::cuda_status(e_, #call);    \
+  } while (0)
+#define TPRF_LAUNCH_CHECK(what)                                      \
+  do {                                                               \
+    cudaError_t e_ = cudaGetLastError();                             \
+    if (e_ != cudaSuccess) return ::tprf::cuda_status(e_, what);     \
+  } while (0)
+
+bool sync_checks_enabled();
+
+// Device-side error word (one per device). Kernels OR flag bits into it.
+enum : unsigned {
+  kDevErrTailFit = 1u,      // tail-fit residual above 1e-3
+  kDevErrSingular = 2u,     // zero pivot in Dyson / RPA
+  kDevErrNonFinite = 4u,    // NaN / Inf in a result
+  kDevErrTimeout = 8u,      // bounded wait expired (persistent kernels)
+};
+unsigned *device_status_word();  // nullptr on failure (error set)
+// Reads and clears the device word after synchronising `stream`.
+int finish_with_checks(cudaStream_t stream, const char *what);
+
+// ---------------------------------------------------------------------------
+// FFT plans. A length-n transform is a list of radix stages (Stockham,
+// self-sorting) and a table tw[t] = exp(-2 pi i t / n), t < n.
+constexpr int kMaxStages = 24;
+struct FftDesc {
+  int n;
+  int nst;
+  int radix[kMaxStages];
+  const double2 *tw;  // device
+};
+// Returns 0 or a status; fills *out. Cached per (device, n).
+int get_fft(int n, FftDesc *out);
+
+// iv -> tau (fermion) tables for one (beta, n_iw, n_tau).
+struct NuTauPlan {
+  double beta;
+  int n_iw, n_tau, L;
+  FftDesc fft;
+  const double2 *den;    // [3][2 n_iw]: 1/(iv_n - b_j), b = (0, 1, -1)
+  const double2 *phase;  // [L]: exp(-i pi tau_t / beta)
+  const double *ftail;   // [3][L]: oneFermion(1, b_j, tau_t)
+  int n_fit, n_mom;      // fit points, number of fitted moments (P+1)
+  const int *fit_row;    // [n_fit]: data index of each fit point
+  const double2 *fitF;   // [n_mom][n_fit]: moments = F g
+  const double2 *fitG;   // [n_fit][n_mom]: model value = sum_p c_p G[i][p]
+};
+int get_nu_tau_plan(double beta, int n_iw, int n_tau, const NuTauPlan **out);
+
+// tau -> i omega (boson) tables for one (beta, n_tau, nw).
+struct TauWPlan {
+  double beta;
+  int n_tau, nw, L;
+  FftDesc fft;
+  const double *btail;   // [3][L]: oneBoson(1, b_j, tau_t), b = (-1/2, -1, 1)
+  const double2 *den;    // [3][2 nw - 1]: 1/(i w_m - b_j)
+};
+int get_tau_w_plan(double beta, int n_tau, int nw, const TauWPlan **out);
+
+// Exact inverse of the 8x8 Vandermonde V[m][j] = m^j (m = 1..8), uploaded to
+// __constant__ memory of the TU that needs it.
+void vandermonde_inverse8(double out[64]);
+
+// Default time mesh of the reference's make_adjoint_mesh for a fermionic
+// mesh with n_iw positive frequencies.
+inline int default_n_tau(int n_iw) { return 6 * n_iw + 1; }
+
+int max_smem_optin();
+int num_sms();
+
+}  // namespace tprf

@@ -1,0 +1,455 @@
+// Kernel (b), Matsubara part, and kernel (c), the particle-hole bubble.
+//
+//  * iv -> tau (fermion) with the three-pole tail model and the tail fit:
+//    restates c++/triqs_tprf/fourier/fourier_matsubara.cpp:218-308 as driven
+//    per r by lattice/fourier.hpp:99-130.
+//  * tau -> i omega (boson) with the fit_derivatives moments: restates
+//    fourier_matsubara.cpp:42-97 and :123-184, driven by lattice/fourier.hpp:133-163.
+//  * bubble chi0_abcd(tau_i, r) = G_da(tau_i, r) G_bc(tau_{N-1-i}, -r):
+//    restates lattice/chi_imtime.cpp:88-136 (product at :127); the fused
+//    bubble + tau -> w of chi_imtime.cpp:139-182; the trapezoid branch of
+//    chi_imtime.cpp:185-276.
+//
+// Design: every transform works on "columns" (one (r, target element) pair
+// each; columns are contiguous in HBM), a tile of `ic` columns per CTA. The
+// whole tau or nu series of the tile sits in shared memory, the tail model is
+// fitted, subtracted and added back around a Stockham FFT in the same CTA, so
+// each transform reads its input once and writes its output once. The fused
+// bubble builds chi0(tau) for its columns directly in shared memory from
+// G(tau, r) and G(beta - tau, -r): chi0(tau, r) never reaches HBM.
+#include <algorithm>
+
+#include "common.cuh"
+
+namespace tprf {
+namespace {
+
+struct VinvRows {
+  double r0[8];  // row 0 of the inverse Vandermonde: first derivative
+  double r1[8];  // row 1: second-order coefficient
+};
+
+VinvRows make_vinv_rows() {
+  double v[64];
+  vandermonde_inverse8(v);
+  VinvRows r;
+  for (int m = 0; m < 8; ++m) {
+    r.r0[m] = v[0 * 8 + m];
+    r.r1[m] = v[1 * 8 + m];
+  }
+  return r;
+}
+
+__device__ __forceinline__ void fmax_shared(unsigned *slot, double v) {
+  // non-negative floats order like their bit patterns
+  atomicMax(slot, __float_as_uint((float)v));
+}
+
+// ---------------------------------------------------------------------------
+// iv -> tau
+
+__global__ void __launch_bounds__(512) nu_to_tau_kernel(NuTauPlan p, const double2 *__restrict__ gw,
+                                                        const double2 *__restrict__ mom, double2 *__restrict__ gt,
+                                                        long C, int ic, unsigned *status) {
+  extern __shared__ double2 smem[];
+  __shared__ unsigned s_res;
+  const int L = p.L, n_iw = p.n_iw, nnu = 2 * p.n_iw;
+  double2 *a = smem;
+  double2 *b = a + (size_t)L * ic;
+  double2 *coef = b + (size_t)L * ic;  // [n_mom][ic]
+  double2 *am = coef + 10 * ic;        // [4][ic]: a1, a2, a3, m1
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  const long col0 = blockIdx.x * (long)ic;
+  const int ncol = (int)min((long)ic, C - col0);
+
+  for (int w = tid; w < L * ic; w += nthr) a[w] = make_double2(0.0, 0.0);
+  if (tid == 0) s_res = 0u;
+  __syncthreads();
+  for (int w = tid; w < nnu * ic; w += nthr) {
+    const int c = w % ic, n = w / ic;
+    if (c < ncol) a[((n - n_iw + L) % L) * ic + c] = gw[(long)n * C + col0 + c];
+  }
+  __syncthreads();
+  if (mom == nullptr) {
+    const int nf = p.n_fit, nm = p.n_mom;
+    for (int w = tid; w < nm * ic; w += nthr) {
+      const int c = w % ic, q = w / ic;
+      double2 acc = make_double2(0.0, 0.0);
+      for (int i = 0; i < nf; ++i) {
+        const int row = (p.fit_row[i] - n_iw + L) % L;
+        acc = cfma(p.fitF[q * nf + i], a[row * ic + c], acc);
+      }
+      coef[q * ic + c] = acc;
+    }
+    __syncthreads();
+    for (int w = tid; w < nf * ic; w += nthr) {
+      const int c = w % ic, i = w / ic;
+      if (c >= ncol) continue;
+      double2 model = make_double2(0.0, 0.0);
+      for (int q = 0; q < nm; ++q) model = cfma(p.fitG[i * nm + q], coef[q * ic + c], model);
+      const int row = (p.fit_row[i] - n_iw + L) % L;
+      const double2 d = csub(model, a[row * ic + c]);
+      fmax_shared(&s_res, sqrt(cabs2(d)));
+    }
+    for (int c = tid; c < ic; c += nthr) {
+      const double2 m1 = coef[1 * ic + c], m2 = coef[2 * ic + c], m3 = coef[3 * ic + c];
+      am[0 * ic + c] = csub(m1, m3);
+      am[1 * ic + c] = cscale(cadd(m2, m3), 0.5);
+      am[2 * ic + c] = cscale(csub(m3, m2), 0.5);
+      am[3 * ic + c] = m1;
+    }
+  } else {
+    for (int c = tid; c < ic; c += nthr) {
+      double2 m1 = make_double2(0.0, 0.0), m2 = m1, m3 = m1;
+      if (c < ncol) {
+        m1 = mom[0 * C + col0 + c];
+        m2 = mom[1 * C + col0 + c];
+        m3 = mom[2 * C + col0 + c];
+      }
+      am[0 * ic + c] = csub(m1, m3);
+      am[1 * ic + c] = cscale(cadd(m2, m3), 0.5);
+      am[2 * ic + c] = cscale(csub(m3, m2), 0.5);
+      am[3 * ic + c] = m1;
+    }
+  }
+  __syncthreads();
+  if (tid == 0 && __uint_as_float(s_res) > 1e-3f) atomicOr(status, kDevErrTailFit);
+  const double inv_beta = 1.0 / p.beta;
+  for (int w = tid; w < nnu * ic; w += nthr) {
+    const int c = w % ic, n = w / ic;
+    const int j = (n - n_iw + L) % L;
+    double2 model = cmul(am[0 * ic + c], p.den[0 * nnu + n]);
+    model = cfma(am[1 * ic + c], p.den[1 * nnu + n], model);
+    model = cfma(am[2 * ic + c], p.den[2 * nnu + n], model);
+    a[j * ic + c] = cscale(csub(a[j * ic + c], model), inv_beta);
+  }
+  double2 *r = fft_smem<true>(a, b, p.fft, ic);
+  for (int w = tid; w < (L + 1) * ic; w += nthr) {
+    const int c = w % ic, t = w / ic;
+    if (c >= ncol) continue;
+    const int tt = (t < L) ? t : 0;
+    double2 v = cmul(r[tt * ic + c], p.phase[tt]);
+    double2 model = cscale(am[0 * ic + c], p.ftail[0 * L + tt]);
+    model = cadd(model, cscale(am[1 * ic + c], p.ftail[1 * L + tt]));
+    model = cadd(model, cscale(am[2 * ic + c], p.ftail[2 * L + tt]));
+    v = cadd(v, model);
+    if (t == L) v = make_double2(-(v.x + am[3 * ic + c].x), -(v.y + am[3 * ic + c].y));
+    gt[(long)t * C + col0 + c] = v;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Column loaders for the tau -> w transform and the trapezoid integral.
+
+struct ArrayLoader {  // chi(tau, col) stored as [n_tau][C]
+  const double2 *x;
+  long C;
+  __device__ __forceinline__ double2 operator()(int t, long col) const { return x[(long)t * C + col]; }
+};
+
+struct BubbleLoader {  // chi0 columns computed from G(tau, r): col = r * nb^4 + abcd
+  const double2 *g;    // [n_tau][N_r][nb][nb]
+  long Nr;
+  int nb, n_tau;
+  int d0, d1, d2;
+  __device__ __forceinline__ double2 operator()(int t, long col) const {
+    const int nb2 = nb * nb, nb4 = nb2 * nb2;
+    const long r = col / nb4;
+    int e = (int)(col - r * nb4);
+    const int d = e % nb;
+    e /= nb;
+    const int c = e % nb;
+    e /= nb;
+    const int b = e % nb;
+    const int a = e / nb;
+    const int i2 = (int)(r % d2);
+    const int i1 = (int)((r / d2) % d1);
+    const int i0 = (int)(r / ((long)d2 * d1));
+    const long mr = ((long)((d0 - i0) % d0) * d1 + (d1 - i1) % d1) * d2 + (d2 - i2) % d2;
+    const double2 x = g[((long)t * Nr + r) * nb2 + d * nb + a];
+    const double2 y = g[((long)(n_tau - 1 - t) * Nr + mr) * nb2 + b * nb + c];
+    return cmul(x, y);
+  }
+};
+
+template <class Loader>
+__global__ void __launch_bounds__(512) tau_to_w_kernel(TauWPlan p, Loader ld, VinvRows vr, double2 *__restrict__ out,
+                                                       long C, int ic) {
+  extern __shared__ double2 smem[];
+  const int L = p.L, nw = p.nw, nwt = 2 * p.nw - 1;
+  double2 *a = smem;
+  double2 *b = a + (size_t)L * ic;
+  double2 *last = b + (size_t)L * ic;  // [ic] row L
+  double2 *am = last + ic;             // [3][ic]
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  const long col0 = blockIdx.x * (long)ic;
+  const int ncol = (int)min((long)ic, C - col0);
+  for (int w = tid; w < (L + 1) * ic; w += nthr) {
+    const int c = w % ic, t = w / ic;
+    double2 v = make_double2(0.0, 0.0);
+    if (c < ncol) v = ld(t, col0 + c);
+    if (t < L)
+      a[t * ic + c] = v;
+    else
+      last[c] = v;
+  }
+  __syncthreads();
+  const double dtau = p.beta / (double)(p.n_tau - 1);
+  for (int c = tid; c < ic; c += nthr) {
+    const double2 g0 = a[c], gL = last[c];
+    double2 gl0 = make_double2(0.0, 0.0), gl1 = gl0, gr0 = gl0, gr1 = gl0;
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+      const double tau_m = (double)(m + 1) * dtau;
+      const int rl = m + 1, rr = L - 1 - m;
+      const double2 xl = (rl < L) ? a[rl * ic + c] : gL;
+      const double2 dl = make_double2((xl.x - g0.x) / tau_m, (xl.y - g0.y) / tau_m);
+      const double2 xr = a[rr * ic + c];
+      const double2 dr = make_double2((gL.x - xr.x) / tau_m, (gL.y - xr.y) / tau_m);
+      gl0 = make_double2(fma(vr.r0[m], dl.x, gl0.x), fma(vr.r0[m], dl.y, gl0.y));
+      gl1 = make_double2(fma(vr.r1[m], dl.x, gl1.x), fma(vr.r1[m], dl.y, gl1.y));
+      gr0 = make_double2(fma(vr.r0[m], dr.x, gr0.x), fma(vr.r0[m], dr.y, gr0.y));
+      gr1 = make_double2(fma(vr.r1[m], dr.x, gr1.x), fma(vr.r1[m], dr.y, gr1.y));
+    }
+    const double2 m1 = make_double2(-(g0.x - gL.x), -(g0.y - gL.y));
+    const double2 m2 = csub(gl0, gr0);                                  // sign = +1 (boson)
+    const double2 m3 = cscale(cadd(gl1, gr1), -2.0 / dtau);
+    am[0 * ic + c] = cscale(csub(m1, m3), 4.0 / 3.0);
+    am[1 * ic + c] = csub(m3, cscale(cadd(m1, m2), 0.5));
+    am[2 * ic + c] = cadd(cadd(cscale(m1, 1.0 / 6.0), cscale(m2, 0.5)), cscale(m3, 1.0 / 3.0));
+  }
+  __syncthreads();
+  const double fact = p.beta / (double)L;
+  for (int w = tid; w < L * ic; w += nthr) {
+    const int c = w % ic, t = w / ic;
+    double2 model = cscale(am[0 * ic + c], p.btail[0 * L + t]);
+    model = cadd(model, cscale(am[1 * ic + c], p.btail[1 * L + t]));
+    model = cadd(model, cscale(am[2 * ic + c], p.btail[2 * L + t]));
+    a[t * ic + c] = cscale(csub(a[t * ic + c], model), fact);
+  }
+  double2 *r = fft_smem<false>(a, b, p.fft, ic);
+  for (int w = tid; w < nwt * ic; w += nthr) {
+    const int c = w % ic, mi = w / ic;
+    if (c >= ncol) continue;
+    const int m = mi - (nw - 1);
+    double2 v = r[((m + L) % L) * ic + c];
+    v = cfma(am[0 * ic + c], p.den[0 * nwt + mi], v);
+    v = cfma(am[1 * ic + c], p.den[1 * nwt + mi], v);
+    v = cfma(am[2 * ic + c], p.den[2 * nwt + mi], v);
+    out[(long)mi * C + col0 + c] = v;
+  }
+}
+
+template <class Loader>
+__global__ void __launch_bounds__(256) trapz_kernel(Loader ld, double2 *__restrict__ out, long C, int n_tau,
+                                                    double beta) {
+  for (long col = blockIdx.x * (long)blockDim.x + threadIdx.x; col < C; col += (long)gridDim.x * blockDim.x) {
+    double2 s = make_double2(0.0, 0.0);
+    for (int t = 0; t < n_tau; ++t) s = cadd(s, ld(t, col));
+    s = csub(s, cscale(ld(0, col), 0.5));
+    s = csub(s, cscale(ld(n_tau - 1, col), 0.5));
+    out[col] = cscale(s, beta / (double)(n_tau - 1));
+  }
+}
+
+__global__ void __launch_bounds__(256) bubble_kernel(BubbleLoader ld, double2 *__restrict__ out, long C) {
+  const long total = C * ld.n_tau;
+  for (long idx = blockIdx.x * (long)blockDim.x + threadIdx.x; idx < total; idx += (long)gridDim.x * blockDim.x) {
+    const int t = (int)(idx / C);
+    out[idx] = ld(t, idx - (long)t * C);
+  }
+}
+
+int pick_ic(int L, size_t extra_per_col, int *ic_out, size_t *smem_out) {
+  const size_t budget = (size_t)std::min(max_smem_optin(), 220 * 1024);
+  int ic = 32;
+  while (ic > 1 && (2ull * L * ic * sizeof(double2) + extra_per_col * ic) > budget) ic /= 2;
+  const size_t smem = 2ull * L * ic * sizeof(double2) + extra_per_col * ic;
+  if (smem > budget)
+    return set_error(TPRF_ERR_UNSUPPORTED_SIZE, "Matsubara FFT: time mesh too long for one CTA (n_tau > ~6900)");
+  *ic_out = ic;
+  *smem_out = smem;
+  return TPRF_OK;
+}
+
+long grid_for(long work, int threads) {
+  long blocks = (work + threads - 1) / threads;
+  const long cap = (long)num_sms() * 32;
+  return std::max(1L, std::min(blocks, cap));
+}
+
+template <class Loader>
+int launch_tau_to_w_with(const TauWPlan *p, Loader ld, double2 *out, long C, cudaStream_t stream) {
+  int ic;
+  size_t smem;
+  int st = pick_ic(p->L, 4 * sizeof(double2), &ic, &smem);
+  if (st) return st;
+  TPRF_CUDA(cudaFuncSetAttribute(tau_to_w_kernel<Loader>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const long blocks = (C + ic - 1) / ic;
+  tau_to_w_kernel<Loader><<<(unsigned)blocks, 512, smem, stream>>>(*p, ld, make_vinv_rows(), out, C, ic);
+  TPRF_LAUNCH_CHECK("tau_to_w_kernel");
+  return TPRF_OK;
+}
+
+int check_tau_w(double beta, int n_tau, int nw) {
+  if (!(beta > 0.0) || n_tau < 10 || nw < 1)
+    return set_error(TPRF_ERR_INVALID_ARGUMENT, "tau -> w: need beta > 0, n_tau >= 10, nw >= 1");
+  if (n_tau - 1 < 2 * nw)
+    return set_error(TPRF_ERR_MESH_TOO_SHORT,
+                     "Fourier: the time mesh must be at least twice as long as the number of positive frequencies");
+  return TPRF_OK;
+}
+
+BubbleLoader make_bubble(const double2 *g, int n_tau, const int dims[3], int nb) {
+  BubbleLoader ld;
+  ld.g = g;
+  ld.Nr = (long)dims[0] * dims[1] * dims[2];
+  ld.nb = nb;
+  ld.n_tau = n_tau;
+  ld.d0 = dims[0];
+  ld.d1 = dims[1];
+  ld.d2 = dims[2];
+  return ld;
+}
+
+int check_bubble(int n_tau, const int dims[3], int nb, const void *g, const void *out) {
+  if (!dims || !g || !out || n_tau < 2 || nb < 1 || nb > 8)
+    return set_error(TPRF_ERR_INVALID_ARGUMENT, "bubble: bad shape (nb 1..8, n_tau >= 2) or null pointer");
+  for (int a = 0; a < 3; ++a)
+    if (dims[a] < 1) return set_error(TPRF_ERR_INVALID_ARGUMENT, "bubble: mesh dims must be >= 1");
+  return TPRF_OK;
+}
+
+}  // namespace
+
+// ---- internal launchers (no synchronisation) --------------------------------
+
+int launch_nu_to_tau(double beta, int n_iw, int n_tau, long C, const double2 *gw, const double2 *mom, double2 *gt,
+                     cudaStream_t stream) {
+  if (n_tau < 0) n_tau = default_n_tau(n_iw);
+  if (!(beta > 0.0) || n_iw < 1 || n_tau < 2 || C < 1)
+    return set_error(TPRF_ERR_INVALID_ARGUMENT, "fourier_wr_to_tr: bad mesh");
+  if (n_tau - 1 < 2 * n_iw)
+    return set_error(TPRF_ERR_MESH_TOO_SHORT,
+                     "Inverse Fourier: the time mesh must be at least twice as long as the freq mesh");
+  const NuTauPlan *p = nullptr;
+  int st = get_nu_tau_plan(beta, n_iw, n_tau, &p);
+  if (st) return st;
+  if (!mom && p->n_mom < 4)
+    return set_error(TPRF_ERR_TAIL_FIT, "Inverse Fourier requires at least a proper 3rd high-frequency moment");
+  unsigned *status = device_status_word();
+  if (!status) return TPRF_ERR_CUDA;
+  int ic;
+  size_t smem;
+  st = pick_ic(p->L, 14 * sizeof(double2), &ic, &smem);
+  if (st) return st;
+  TPRF_CUDA(cudaFuncSetAttribute(nu_to_tau_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const long blocks = (C + ic - 1) / ic;
+  nu_to_tau_kernel<<<(unsigned)blocks, 512, smem, stream>>>(*p, gw, mom, gt, C, ic, status);
+  TPRF_LAUNCH_CHECK("nu_to_tau_kernel");
+  return TPRF_OK;
+}
+
+int launch_chi_wr_from_chi_tr(double beta, int n_tau, int nw, long C, const double2 *chi_tr, double2 *chi_wr,
+                              cudaStream_t stream) {
+  int st = check_tau_w(beta, n_tau, nw);
+  if (st) return st;
+  const TauWPlan *p = nullptr;
+  if ((st = get_tau_w_plan(beta, n_tau, nw, &p))) return st;
+  return launch_tau_to_w_with(p, ArrayLoader{chi_tr, C}, chi_wr, C, stream);
+}
+
+int launch_chi0_wr_from_grt(double beta, int n_tau, int nw, const int dims[3], int nb, const double2 *g,
+                            double2 *chi0_wr, cudaStream_t stream) {
+  int st = check_tau_w(beta, n_tau, nw);
+  if (st) return st;
+  const TauWPlan *p = nullptr;
+  if ((st = get_tau_w_plan(beta, n_tau, nw, &p))) return st;
+  const BubbleLoader ld = make_bubble(g, n_tau, dims, nb);
+  const long C = ld.Nr * nb * nb * nb * nb;
+  return launch_tau_to_w_with(p, ld, chi0_wr, C, stream);
+}
+
+int launch_chi0_w0r_from_grt(double beta, int n_tau, const int dims[3], int nb, const double2 *g, double2 *chi0_wr,
+                             cudaStream_t stream) {
+  const BubbleLoader ld = make_bubble(g, n_tau, dims, nb);
+  const long C = ld.Nr * nb * nb * nb * nb;
+  trapz_kernel<BubbleLoader><<<(unsigned)grid_for(C, 256), 256, 0, stream>>>(ld, chi0_wr, C, n_tau, beta);
+  TPRF_LAUNCH_CHECK("trapz_kernel<bubble>");
+  return TPRF_OK;
+}
+
+}  // namespace tprf
+
+// ---- C ABI ------------------------------------------------------------------
+
+using namespace tprf;
+
+extern "C" int tprf_fourier_wr_to_tr(double beta, int n_iw, int n_tau, long n_r, long n_target, const double *g_wr,
+                                     const double *moments, double *g_tr, void *stream) {
+  if (!g_wr || !g_tr || n_r < 1 || n_target < 1)
+    return set_error(TPRF_ERR_INVALID_ARGUMENT, "fourier_wr_to_tr: bad shape or null pointer");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int st = launch_nu_to_tau(beta, n_iw, n_tau, n_r * n_target, reinterpret_cast<const double2 *>(g_wr),
+                            reinterpret_cast<const double2 *>(moments), reinterpret_cast<double2 *>(g_tr), s);
+  if (st) return st;
+  return finish_with_checks(s, "fourier_wr_to_tr");
+}
+
+extern "C" int tprf_chi_wr_from_chi_tr(double beta, int n_tau, int nw, long n_r, long n_target, const double *chi_tr,
+                                       double *chi_wr, void *stream) {
+  if (!chi_tr || !chi_wr || n_r < 1 || n_target < 1)
+    return set_error(TPRF_ERR_INVALID_ARGUMENT, "chi_wr_from_chi_tr: bad shape or null pointer");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int st = launch_chi_wr_from_chi_tr(beta, n_tau, nw, n_r * n_target, reinterpret_cast<const double2 *>(chi_tr),
+                                     reinterpret_cast<double2 *>(chi_wr), s);
+  if (st) return st;
+  TPRF_LAUNCH_CHECK("chi_wr_from_chi_tr");
+  return TPRF_OK;
+}
+
+extern "C" int tprf_chi_w0r_from_chi_tr(double beta, int n_tau, long n_r, long n_target, const double *chi_tr,
+                                        double *chi_wr, void *stream) {
+  if (!chi_tr || !chi_wr || n_r < 1 || n_target < 1 || n_tau < 2 || !(beta > 0.0))
+    return set_error(TPRF_ERR_INVALID_ARGUMENT, "chi_w0r_from_chi_tr: bad shape or null pointer");
+  const long C = n_r * n_target;
+  trapz_kernel<ArrayLoader><<<(unsigned)grid_for(C, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+      ArrayLoader{reinterpret_cast<const double2 *>(chi_tr), C}, reinterpret_cast<double2 *>(chi_wr), C, n_tau, beta);
+  TPRF_LAUNCH_CHECK("trapz_kernel<array>");
+  return TPRF_OK;
+}
+
+extern "C" int tprf_chi0_tr_from_grt_PH(int n_tau, const int dims[3], int nb, const double *g_tr, double *chi0_tr,
+                                        void *stream) {
+  int st = check_bubble(n_tau, dims, nb, g_tr, chi0_tr);
+  if (st) return st;
+  const BubbleLoader ld = make_bubble(reinterpret_cast<const double2 *>(g_tr), n_tau, dims, nb);
+  const long C = ld.Nr * nb * nb * nb * nb;
+  bubble_kernel<<<(unsigned)grid_for(C * n_tau, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+      ld, reinterpret_cast<double2 *>(chi0_tr), C);
+  TPRF_LAUNCH_CHECK("bubble_kernel");
+  return TPRF_OK;
+}
+
+extern "C" int tprf_chi0_wr_from_grt_PH(double beta, int n_tau, int nw, const int dims[3], int nb, const double *g_tr,
+                                        double *chi0_wr, void *stream) {
+  int st = check_bubble(n_tau, dims, nb, g_tr, chi0_wr);
+  if (st) return st;
+  st = launch_chi0_wr_from_grt(beta, n_tau, nw, dims, nb, reinterpret_cast<const double2 *>(g_tr),
+                               reinterpret_cast<double2 *>(chi0_wr), static_cast<cudaStream_t>(stream));
+  if (st) return st;
+  TPRF_LAUNCH_CHECK("chi0_wr_from_grt_PH");
+  return TPRF_OK;
+}
+
+extern "C" int tprf_chi0_w0r_from_grt_PH(double beta, int n_tau, const int dims[3], int nb, const double *g_tr,
+                                         double *chi0_wr, void *stream) {
+  int st = check_bubble(n_tau, dims, nb, g_tr, chi0_wr);
+  if (st) return st;
+  if (!(beta > 0.0)) return set_error(TPRF_ERR_INVALID_ARGUMENT, "chi0_w0r_from_grt_PH: beta must be > 0");
+  st = launch_chi0_w0r_from_grt(beta, n_tau, dims, nb, reinterpret_cast<const double2 *>(g_tr),
+                                reinterpret_cast<double2 *>(chi0_wr), static_cast<cudaStream_t>(stream));
+  if (st) return st;
+  TPRF_LAUNCH_CHECK("chi0_w0r_from_grt_PH");
+  return TPRF_OK;
+}

@@ -1,0 +1,63 @@
+// The whole bubble chain g_wk -> chi0_wk, as the Python driver
+// python/triqs_tprf/lattice_utils.py:191-269 (imtime_bubble_chi0_wk) chains it:
+// fourier_wk_to_wr, fourier_wr_to_tr, then the static trapezoid branch
+// (nw == 1, chi0_w0r_from_grt_PH) or the bubble + tau -> w transform, then
+// chi_wk_from_chi_wr. The reference's save_memory switch only changes how
+// much it stores; here the bubble is always fused with tau -> w, so chi0(tau, r)
+// is never stored and both settings give the same numbers.
+//
+// The caller provides all memory: G(iv, r) and G(tau, r) in `workspace`
+// (tprf_imtime_bubble_workspace_bytes), chi0(w, r) is built in the output
+// buffer and transformed r -> q in place.
+#include "common.cuh"
+
+namespace tprf {
+int launch_lattice_fft(bool forward, long n_w, const int dims[3], long n_target, const double2 *in, double2 *out,
+                       cudaStream_t stream);
+int launch_nu_to_tau(double beta, int n_iw, int n_tau, long C, const double2 *gw, const double2 *mom, double2 *gt,
+                     cudaStream_t stream);
+int launch_chi0_wr_from_grt(double beta, int n_tau, int nw, const int dims[3], int nb, const double2 *g,
+                            double2 *chi0_wr, cudaStream_t stream);
+int launch_chi0_w0r_from_grt(double beta, int n_tau, const int dims[3], int nb, const double2 *g, double2 *chi0_wr,
+                             cudaStream_t stream);
+}  // namespace tprf
+
+using namespace tprf;
+
+extern "C" size_t tprf_imtime_bubble_workspace_bytes(int n_iw, int n_tau, const int dims[3], int nb) {
+  if (n_tau < 0) n_tau = default_n_tau(n_iw);
+  const size_t nk = (size_t)dims[0] * dims[1] * dims[2];
+  const size_t t = (size_t)nb * nb * nk;
+  const size_t g_wr = 2ull * n_iw * t, g_tr = (size_t)n_tau * t;
+  return (g_wr + g_tr) * sizeof(double2) + 256;
+}
+
+extern "C" int tprf_imtime_bubble_chi0_wk(double beta, int n_iw, int n_tau, int nw, const int dims[3], int nb,
+                                          const double *g_wk, const double *moments, double *chi0_wk,
+                                          void *workspace, size_t workspace_bytes, void *stream) {
+  if (!dims || !g_wk || !chi0_wk || !workspace || nb < 1 || nb > 8 || nw < 1 || n_iw < 1)
+    return set_error(TPRF_ERR_INVALID_ARGUMENT, "imtime_bubble_chi0_wk: bad shape or null pointer");
+  if (n_tau < 0) n_tau = default_n_tau(n_iw);
+  const size_t need = tprf_imtime_bubble_workspace_bytes(n_iw, n_tau, dims, nb);
+  if (workspace_bytes < need)
+    return set_error(TPRF_ERR_ALLOC, "imtime_bubble_chi0_wk: workspace smaller than tprf_imtime_bubble_workspace_bytes");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const long nk = (long)dims[0] * dims[1] * dims[2];
+  const long nb2 = (long)nb * nb, nb4 = nb2 * nb2;
+  uintptr_t ws = (reinterpret_cast<uintptr_t>(workspace) + 255) & ~uintptr_t(255);
+  double2 *g_wr = reinterpret_cast<double2 *>(ws);
+  double2 *g_tr = g_wr + 2L * n_iw * nk * nb2;
+  double2 *out = reinterpret_cast<double2 *>(chi0_wk);
+  int st = launch_lattice_fft(true, 2L * n_iw, dims, nb2, reinterpret_cast<const double2 *>(g_wk), g_wr, s);
+  if (st) return st;
+  st = launch_nu_to_tau(beta, n_iw, n_tau, nk * nb2, g_wr, reinterpret_cast<const double2 *>(moments), g_tr, s);
+  if (st) return st;
+  if (nw == 1)
+    st = launch_chi0_w0r_from_grt(beta, n_tau, dims, nb, g_tr, out, s);
+  else
+    st = launch_chi0_wr_from_grt(beta, n_tau, nw, dims, nb, g_tr, out, s);
+  if (st) return st;
+  st = launch_lattice_fft(false, 2L * nw - 1, dims, nb4, out, out, s);
+  if (st) return st;
+  return finish_with_checks(s, "imtime_bubble_chi0_wk");
+}

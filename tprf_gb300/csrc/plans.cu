@@ -1,0 +1,474 @@
+// Host-side context of tprf_gb300: status reporting, the per-device error
+// word, and the plan caches (FFT twiddles, Matsubara tail tables, tail-fit
+// matrices). Plans are built once per key, uploaded synchronously and kept
+// for the life of the process.
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <complex>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <tuple>
+#include <vector>
+
+#include "internal.hpp"
+
+namespace tprf {
+
+namespace {
+thread_local std::string g_last_error;
+std::atomic<bool> g_sync_checks{true};
+std::mutex g_mutex;
+
+using cd = std::complex<double>;
+
+// Device allocations owned by the plan caches; released at process exit by
+// the driver, never by us (a static destructor may run after the context).
+template <class T>
+int upload(const std::vector<T> &h, const T **out) {
+  void *d = nullptr;
+  size_t bytes = std::max<size_t>(1, h.size()) * sizeof(T);
+  cudaError_t e = cudaMalloc(&d, bytes);
+  if (e != cudaSuccess) return cuda_status(e, "cudaMalloc(plan table)");
+  if (!h.empty()) {
+    e = cudaMemcpy(d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_status(e, "cudaMemcpy(plan table)");
+  }
+  *out = static_cast<const T *>(d);
+  return TPRF_OK;
+}
+
+int current_device(int *dev) {
+  cudaError_t e = cudaGetDevice(dev);
+  if (e != cudaSuccess) return cuda_status(e, "cudaGetDevice");
+  return TPRF_OK;
+}
+
+double2 to_d2(cd z) { return make_double2(z.real(), z.imag()); }
+
+}  // namespace
+
+int set_error(int status, const std::string &msg) {
+  g_last_error = msg;
+  return status;
+}
+
+int cuda_status(cudaError_t e, const char *what) {
+  return set_error(TPRF_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+bool sync_checks_enabled() { return g_sync_checks.load(); }
+
+unsigned *device_status_word() {
+  static std::map<int, unsigned *> words;
+  int dev = 0;
+  if (current_device(&dev) != TPRF_OK) return nullptr;
+  std::lock_guard<std::mutex> lock(g_mutex);
+  auto it = words.find(dev);
+  if (it != words.end()) return it->second;
+  void *p = nullptr;
+  cudaError_t e = cudaMalloc(&p, sizeof(unsigned));
+  if (e != cudaSuccess) {
+    cuda_status(e, "cudaMalloc(status word)");
+    return nullptr;
+  }
+  e = cudaMemset(p, 0, sizeof(unsigned));
+  if (e != cudaSuccess) {
+    cuda_status(e, "cudaMemset(status word)");
+    return nullptr;
+  }
+  words[dev] = static_cast<unsigned *>(p);
+  return static_cast<unsigned *>(p);
+}
+
+int read_and_clear_status(cudaStream_t stream, unsigned *flags) {
+  unsigned *w = device_status_word();
+  if (!w) return TPRF_ERR_CUDA;
+  TPRF_CUDA(cudaMemcpyAsync(flags, w, sizeof(unsigned), cudaMemcpyDeviceToHost, stream));
+  TPRF_CUDA(cudaMemsetAsync(w, 0, sizeof(unsigned), stream));
+  TPRF_CUDA(cudaStreamSynchronize(stream));
+  return TPRF_OK;
+}
+
+int status_from_flags(unsigned f, const char *what) {
+  if (f & kDevErrTailFit)
+    return set_error(TPRF_ERR_TAIL_FIT, std::string(what) + ": high frequency moments have an error greater than 1e-3");
+  if (f & kDevErrSingular) return set_error(TPRF_ERR_SINGULAR, std::string(what) + ": singular matrix");
+  if (f & kDevErrNonFinite) return set_error(TPRF_ERR_NONFINITE, std::string(what) + ": non-finite value");
+  if (f & kDevErrTimeout) return set_error(TPRF_ERR_CUDA, std::string(what) + ": device wait timed out");
+  return TPRF_OK;
+}
+
+int finish_with_checks(cudaStream_t stream, const char *what) {
+  TPRF_LAUNCH_CHECK(what);
+  if (!sync_checks_enabled()) return TPRF_OK;
+  unsigned f = 0;
+  int st = read_and_clear_status(stream, &f);
+  if (st != TPRF_OK) return st;
+  return status_from_flags(f, what);
+}
+
+int max_smem_optin() {
+  int dev = 0, v = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  return v > 0 ? v : 48 * 1024;
+}
+
+int num_sms() {
+  int dev = 0, v = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+  return v > 0 ? v : 1;
+}
+
+// ---------------------------------------------------------------------------
+// FFT plans
+
+static bool factorize(int n, int *radix, int *nst) {
+  int m = n, s = 0;
+  while (m % 8 == 0 && s < kMaxStages) { radix[s++] = 8; m /= 8; }
+  if (m % 4 == 0 && s < kMaxStages) { radix[s++] = 4; m /= 4; }
+  if (m % 2 == 0 && s < kMaxStages) { radix[s++] = 2; m /= 2; }
+  for (int r : {3, 5, 7})
+    while (m % r == 0 && s < kMaxStages) { radix[s++] = r; m /= r; }
+  // remaining prime factors: generic radix stages
+  for (int r = 11; (long)r * r <= m && s < kMaxStages; r += 2)
+    while (m % r == 0 && s < kMaxStages) { radix[s++] = r; m /= r; }
+  if (m > 1 && s < kMaxStages) { radix[s++] = m; m = 1; }
+  *nst = s;
+  return m == 1;
+}
+
+int get_fft(int n, FftDesc *out) {
+  if (n < 1) return set_error(TPRF_ERR_INVALID_ARGUMENT, "FFT length must be >= 1");
+  int dev = 0;
+  int st = current_device(&dev);
+  if (st) return st;
+  static std::map<std::pair<int, int>, FftDesc> cache;
+  std::lock_guard<std::mutex> lock(g_mutex);
+  auto key = std::make_pair(dev, n);
+  auto it = cache.find(key);
+  if (it != cache.end()) {
+    *out = it->second;
+    return TPRF_OK;
+  }
+  FftDesc d{};
+  d.n = n;
+  if (!factorize(n, d.radix, &d.nst))
+    return set_error(TPRF_ERR_UNSUPPORTED_SIZE, "FFT length " + std::to_string(n) + " has too many factors");
+  std::vector<double2> tw(n);
+  for (int t = 0; t < n; ++t) {
+    const double a = -2.0 * M_PI * (double)t / (double)n;
+    tw[t] = make_double2(std::cos(a), std::sin(a));
+  }
+  st = upload(tw, &d.tw);
+  if (st) return st;
+  cache[key] = d;
+  *out = d;
+  return TPRF_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Tail fit: a linear least-squares fit of g(iv) ~ sum_{p<=P} c_p (iv)^-p on
+// the outer 20% of the fermionic mesh (at most 30 points a side, both signs),
+// frequencies normalised by omega_max; the order P is the largest with
+// omega_max^P <= 1e16, at most 9. This restates the method of TRIQS's
+// fit_tail (called at fourier_matsubara.cpp:226); the TRIQS code itself is not
+// part of the reference tree.
+
+static void tail_fit_points(int n_max, std::vector<int> *rows) {
+  int n_pts = std::max(1, std::min((2 * n_max + 5) / 10, 30));
+  int n_hi = n_max - 1;
+  int n_lo = std::min(n_hi, (8 * n_max + 5) / 10);
+  std::vector<int> pos;
+  if (n_pts == 1) {
+    pos.push_back(n_hi);
+  } else {
+    const int span = n_hi - n_lo;
+    for (int j = 0; j < n_pts; ++j) pos.push_back(n_lo + (2 * j * span + (n_pts - 1)) / (2 * (n_pts - 1)));
+  }
+  rows->clear();
+  for (int i = (int)pos.size() - 1; i >= 0; --i) rows->push_back(-pos[i] - 1 + n_max);
+  for (int p : pos) rows->push_back(p + n_max);
+}
+
+static int tail_order(double beta, int n_max, int n_eq) {
+  const double omega_max = (2.0 * n_max - 1.0) * M_PI / beta;
+  int order = 9;
+  if (omega_max > 1.0) order = (int)std::floor(16.0 * std::log(10.0) / std::log(omega_max));
+  order = std::min(order, 9);
+  order = std::min(order, n_eq - 1);
+  return std::max(order, 0);
+}
+
+// Pseudo-inverse of a full-column-rank m x n complex matrix (row-major) by
+// Householder QR: pinv = R^-1 Q^H. Returns false if rank deficient.
+static bool pinv_householder(std::vector<cd> A, int m, int n, std::vector<cd> *pinv) {
+  std::vector<cd> QH(m * m, cd(0));
+  for (int i = 0; i < m; ++i) QH[i * m + i] = 1.0;
+  std::vector<cd> v(m);
+  for (int k = 0; k < n; ++k) {
+    double nrm2 = 0;
+    for (int i = k; i < m; ++i) nrm2 += std::norm(A[i * n + k]);
+    const double nrm = std::sqrt(nrm2);
+    if (nrm == 0.0) return false;
+    const cd akk = A[k * n + k];
+    const cd phase = (std::abs(akk) > 0) ? akk / std::abs(akk) : cd(1.0);
+    const cd alpha = -phase * nrm;
+    double vn2 = 0;
+    for (int i = k; i < m; ++i) {
+      v[i] = A[i * n + k] - (i == k ? alpha : cd(0));
+      vn2 += std::norm(v[i]);
+    }
+    if (vn2 == 0.0) continue;
+    for (int j = k; j < n; ++j) {
+      cd s = 0;
+      for (int i = k; i < m; ++i) s += std::conj(v[i]) * A[i * n + j];
+      s *= 2.0 / vn2;
+      for (int i = k; i < m; ++i) A[i * n + j] -= v[i] * s;
+    }
+    for (int j = 0; j < m; ++j) {
+      cd s = 0;
+      for (int i = k; i < m; ++i) s += std::conj(v[i]) * QH[i * m + j];
+      s *= 2.0 / vn2;
+      for (int i = k; i < m; ++i) QH[i * m + j] -= v[i] * s;
+    }
+  }
+  pinv->assign(n * m, cd(0));
+  for (int j = 0; j < m; ++j) {
+    for (int i = n - 1; i >= 0; --i) {
+      cd s = QH[i * m + j];
+      for (int l = i + 1; l < n; ++l) s -= A[i * n + l] * (*pinv)[l * m + j];
+      if (A[i * n + i] == cd(0)) return false;
+      (*pinv)[i * m + j] = s / A[i * n + i];
+    }
+  }
+  return true;
+}
+
+static double one_fermion(double b, double tau, double beta) {
+  return -(b >= 0 ? std::exp(-b * tau) / (1 + std::exp(-beta * b))
+                  : std::exp(b * (beta - tau)) / (1 + std::exp(beta * b)));
+}
+
+static double one_boson(double b, double tau, double beta) {
+  return (b >= 0 ? std::exp(-b * tau) / (std::exp(-beta * b) - 1)
+                 : std::exp(b * (beta - tau)) / (1 - std::exp(b * beta)));
+}
+
+// Host-side definition of the tail fit for a fermionic mesh (beta, n_iw):
+// the data rows of the fit points, F (moments = F g[rows], [n_mom][n_fit])
+// and G (model value at fit point i = sum_p c_p G[i][p], G = (iv_i)^-p).
+int build_tail_fit(double beta, int n_iw, std::vector<int> *rows, std::vector<double2> *F,
+                   std::vector<double2> *G, int *n_mom_out) {
+  tail_fit_points(n_iw, rows);
+  const int n_fit = (int)rows->size();
+  const int P = tail_order(beta, n_iw, n_fit);
+  const int n_mom = P + 1;
+  const double omega_max = (2.0 * n_iw - 1.0) * M_PI / beta;
+  std::vector<cd> A(n_fit * n_mom);
+  G->assign(n_fit * n_mom, make_double2(0, 0));
+  for (int i = 0; i < n_fit; ++i) {
+    const cd iw(0.0, (2.0 * ((*rows)[i] - n_iw) + 1.0) * M_PI / beta);
+    const cd z = omega_max / iw;
+    cd zp = 1.0, wp = 1.0;
+    for (int q = 0; q < n_mom; ++q) {
+      A[i * n_mom + q] = zp;
+      (*G)[i * n_mom + q] = to_d2(wp);
+      zp *= z;
+      wp /= iw;
+    }
+  }
+  std::vector<cd> pinv;
+  if (!pinv_householder(A, n_fit, n_mom, &pinv))
+    return set_error(TPRF_ERR_TAIL_FIT, "tail fit design matrix is rank deficient");
+  F->assign(n_mom * n_fit, make_double2(0, 0));
+  double scale = 1.0;
+  for (int q = 0; q < n_mom; ++q) {
+    for (int i = 0; i < n_fit; ++i) (*F)[q * n_fit + i] = to_d2(scale * pinv[q * n_fit + i]);
+    scale *= omega_max;
+  }
+  *n_mom_out = n_mom;
+  return TPRF_OK;
+}
+
+int get_nu_tau_plan(double beta, int n_iw, int n_tau, const NuTauPlan **out) {
+  int dev = 0;
+  int st = current_device(&dev);
+  if (st) return st;
+  static std::map<std::tuple<int, uint64_t, int, int>, std::unique_ptr<NuTauPlan>> cache;
+  uint64_t bbits;
+  std::memcpy(&bbits, &beta, 8);
+  auto key = std::make_tuple(dev, bbits, n_iw, n_tau);
+  {
+    std::lock_guard<std::mutex> lock(g_mutex);
+    auto it = cache.find(key);
+    if (it != cache.end()) {
+      *out = it->second.get();
+      return TPRF_OK;
+    }
+  }
+  auto p = std::make_unique<NuTauPlan>();
+  p->beta = beta;
+  p->n_iw = n_iw;
+  p->n_tau = n_tau;
+  p->L = n_tau - 1;
+  const int L = p->L, nnu = 2 * n_iw;
+  st = get_fft(L, &p->fft);
+  if (st) return st;
+  const double bj[3] = {0.0, 1.0, -1.0};
+  std::vector<double2> den(3 * nnu);
+  for (int j = 0; j < 3; ++j)
+    for (int n = 0; n < nnu; ++n) {
+      const cd iw(0.0, (2.0 * (n - n_iw) + 1.0) * M_PI / beta);
+      den[j * nnu + n] = to_d2(1.0 / (iw - bj[j]));
+    }
+  std::vector<double2> phase(L);
+  std::vector<double> ftail(3 * L);
+  const double dtau = beta / (double)(n_tau - 1);
+  for (int t = 0; t < L; ++t) {
+    const double tau = (double)t * dtau;
+    phase[t] = to_d2(std::exp(cd(0.0, -M_PI * tau / beta)));
+    for (int j = 0; j < 3; ++j) ftail[j * L + t] = one_fermion(bj[j], tau, beta);
+  }
+  // tail fit
+  std::vector<int> rows;
+  std::vector<double2> F, G;
+  int n_mom = 0;
+  st = build_tail_fit(beta, n_iw, &rows, &F, &G, &n_mom);
+  if (st) return st;
+  const int n_fit = (int)rows.size();
+  p->n_fit = n_fit;
+  p->n_mom = n_mom;
+  if ((st = upload(den, &p->den)) || (st = upload(phase, &p->phase)) || (st = upload(ftail, &p->ftail)) ||
+      (st = upload(rows, &p->fit_row)) || (st = upload(F, &p->fitF)) || (st = upload(G, &p->fitG)))
+    return st;
+  std::lock_guard<std::mutex> lock(g_mutex);
+  auto &slot = cache[key];
+  if (!slot) slot = std::move(p);
+  *out = slot.get();
+  return TPRF_OK;
+}
+
+int get_tau_w_plan(double beta, int n_tau, int nw, const TauWPlan **out) {
+  int dev = 0;
+  int st = current_device(&dev);
+  if (st) return st;
+  static std::map<std::tuple<int, uint64_t, int, int>, std::unique_ptr<TauWPlan>> cache;
+  uint64_t bbits;
+  std::memcpy(&bbits, &beta, 8);
+  auto key = std::make_tuple(dev, bbits, n_tau, nw);
+  {
+    std::lock_guard<std::mutex> lock(g_mutex);
+    auto it = cache.find(key);
+    if (it != cache.end()) {
+      *out = it->second.get();
+      return TPRF_OK;
+    }
+  }
+  auto p = std::make_unique<TauWPlan>();
+  p->beta = beta;
+  p->n_tau = n_tau;
+  p->nw = nw;
+  p->L = n_tau - 1;
+  const int L = p->L, nwt = 2 * nw - 1;
+  st = get_fft(L, &p->fft);
+  if (st) return st;
+  const double bj[3] = {-0.5, -1.0, 1.0};
+  std::vector<double> btail(3 * L);
+  const double dtau = beta / (double)(n_tau - 1);
+  for (int t = 0; t < L; ++t)
+    for (int j = 0; j < 3; ++j) btail[j * L + t] = one_boson(bj[j], (double)t * dtau, beta);
+  std::vector<double2> den(3 * nwt);
+  for (int j = 0; j < 3; ++j)
+    for (int m = 0; m < nwt; ++m) {
+      const cd iw(0.0, 2.0 * (m - (nw - 1)) * M_PI / beta);
+      den[j * nwt + m] = to_d2(1.0 / (iw - bj[j]));
+    }
+  if ((st = upload(btail, &p->btail)) || (st = upload(den, &p->den))) return st;
+  std::lock_guard<std::mutex> lock(g_mutex);
+  auto &slot = cache[key];
+  if (!slot) slot = std::move(p);
+  *out = slot.get();
+  return TPRF_OK;
+}
+
+void vandermonde_inverse8(double out[64]) {
+  // Column m of the inverse holds the coefficients of the Lagrange basis
+  // polynomial through nodes 1..8 that is 1 at node m+1: integer polynomial
+  // prod_{k != m+1}(x - k) divided by the integer prod_{k != m+1}(m+1 - k).
+  for (int col = 0; col < 8; ++col) {
+    const long long node = col + 1;
+    long long poly[9] = {1, 0, 0, 0, 0, 0, 0, 0, 0};
+    int deg = 0;
+    long long den = 1;
+    for (long long k = 1; k <= 8; ++k) {
+      if (k == node) continue;
+      for (int i = deg + 1; i >= 1; --i) poly[i] = poly[i - 1] - k * poly[i];
+      poly[0] = -k * poly[0];
+      ++deg;
+      den *= (node - k);
+    }
+    for (int j = 0; j < 8; ++j) out[j * 8 + col] = (double)poly[j] / (double)den;
+  }
+}
+
+}  // namespace tprf
+
+// ---------------------------------------------------------------------------
+// C ABI: status helpers
+
+extern "C" const char *tprf_status_string(int status) {
+  switch (status) {
+    case TPRF_OK: return "ok";
+    case TPRF_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case TPRF_ERR_UNSUPPORTED_SIZE: return "unsupported FFT length";
+    case TPRF_ERR_MESH_TOO_SHORT: return "time mesh too short";
+    case TPRF_ERR_TAIL_FIT: return "tail fit error";
+    case TPRF_ERR_NONFINITE: return "non-finite value";
+    case TPRF_ERR_CUDA: return "CUDA error";
+    case TPRF_ERR_ALLOC: return "allocation failed or workspace too small";
+    case TPRF_ERR_SINGULAR: return "singular matrix";
+    default: return "unknown status";
+  }
+}
+
+extern "C" const char *tprf_last_error(void) { return tprf::g_last_error.c_str(); }
+
+extern "C" const char *tprf_version(void) { return "0.1.0"; }
+
+extern "C" void tprf_set_sync_checks(int on) { tprf::g_sync_checks.store(on != 0); }
+
+extern "C" int tprf_check_device_status(void *stream) {
+  unsigned f = 0;
+  int st = tprf::read_and_clear_status(static_cast<cudaStream_t>(stream), &f);
+  if (st != TPRF_OK) return st;
+  return tprf::status_from_flags(f, "device status");
+}
+
+extern "C" int tprf_tail_fit_matrix(double beta, int n_iw, int capacity, int *n_fit, int *n_mom, int *rows,
+                                    double *F) {
+  if (!(beta > 0.0) || n_iw < 1 || !n_fit || !n_mom)
+    return tprf::set_error(TPRF_ERR_INVALID_ARGUMENT, "tail_fit_matrix: bad mesh or null pointer");
+  std::vector<int> r;
+  std::vector<double2> f, g;
+  int nm = 0;
+  int st = tprf::build_tail_fit(beta, n_iw, &r, &f, &g, &nm);
+  if (st) return st;
+  *n_fit = (int)r.size();
+  *n_mom = nm;
+  if (rows && F) {
+    if (capacity < (int)f.size()) return tprf::set_error(TPRF_ERR_INVALID_ARGUMENT, "tail_fit_matrix: capacity");
+    for (size_t i = 0; i < r.size(); ++i) rows[i] = r[i];
+    for (size_t i = 0; i < f.size(); ++i) {
+      F[2 * i] = f[i].x;
+      F[2 * i + 1] = f[i].y;
+    }
+  }
+  return TPRF_OK;
+}
+
+extern "C" void tprf_vandermonde_inverse8(double out[64]) { tprf::vandermonde_inverse8(out); }

@@ -1,0 +1,96 @@
+"""Synthetic tight-binding workloads with the shapes of the benchmark configs.
+
+No dataset is involved: every model is a seeded tight-binding Hamiltonian.
+
+* ``cfg0``: 1-band square lattice, t = 1, mu = 0, 16 x 16 k, beta = 10,
+  n_max = 64 fermionic frequencies, nw = 64, Hubbard U = 1 (1x1x1x1 vertex).
+* ``cfg1``: 3-orbital cubic lattice, nearest- and next-nearest-neighbour
+  hoppings: t(R) = -I (nearest) plus N(0, 0.25^2) entries drawn from the seed,
+  t(-R) = t(R)^T so e(k) is Hermitian; 32^3 k, beta = 20, n_max = 256, nw = 256,
+  Kanamori spin-channel vertex U = 2.3, J = 0.4 (U' = U - 2J, J' = J), 9 x 9.
+* ``cfg3``: 2-orbital square lattice, 32 x 32, beta = 16, n_max = 128, nw = 128,
+  Kanamori spin-channel vertex (U = 1.2, J = 0.2, 4 x 4), 8 seeded hoppings.
+* ``cfg4``: 5-orbital layered lattice (bandwidth ~4), 64 x 64 x 4, beta = 40,
+  n_max = 512, Kanamori U = 3, J = 0.5 (25 x 25).
+"""
+from __future__ import annotations
+
+import itertools
+
+import numpy as np
+
+from .rpa_tensor import kanamori_charge_and_spin_quartic_interaction_tensors
+
+__all__ = ["square_1band", "cubic_3orb", "square_2orb", "layered_5orb", "config", "CONFIGS"]
+
+
+def square_1band(t: float = 1.0):
+    T = -t * np.eye(1)
+    return {(0, 1): T, (0, -1): T, (1, 0): T, (-1, 0): T}
+
+
+def _symmetrise(hop):
+    out = {}
+    for R, t in hop.items():
+        out[R] = t
+        out[tuple(-x for x in R)] = t.T
+    return out
+
+
+def cubic_3orb(seed: int = 0, sigma: float = 0.25):
+    rng = np.random.default_rng(seed)
+    hop = {}
+    nn = [(1, 0, 0), (0, 1, 0), (0, 0, 1)]
+    nnn = [(1, 1, 0), (1, -1, 0), (1, 0, 1), (1, 0, -1), (0, 1, 1), (0, 1, -1)]
+    for R in nn:
+        hop[R] = -np.eye(3) + sigma * rng.standard_normal((3, 3))
+    for R in nnn:
+        hop[R] = sigma * rng.standard_normal((3, 3))
+    return _symmetrise(hop)
+
+
+def square_2orb(seed: int = 0, sigma: float = 0.25):
+    rng = np.random.default_rng(seed)
+    hop = {}
+    for R in [(1, 0), (0, 1), (1, 1), (1, -1)]:
+        base = -np.eye(2) if abs(R[0]) + abs(R[1]) == 1 else np.zeros((2, 2))
+        hop[R] = base + sigma * rng.standard_normal((2, 2))
+    return _symmetrise(hop)
+
+
+def layered_5orb(seed: int = 0):
+    rng = np.random.default_rng(seed)
+    hop = {}
+    for R in [(1, 0, 0), (0, 1, 0), (1, 1, 0), (1, -1, 0)]:
+        base = -0.5 * np.eye(5) if sum(abs(x) for x in R) == 1 else np.zeros((5, 5))
+        hop[R] = base + 0.1 * rng.standard_normal((5, 5))
+    hop[(0, 0, 1)] = 0.05 * rng.standard_normal((5, 5))
+    out = _symmetrise(hop)
+    onsite = 0.2 * rng.standard_normal((5, 5))
+    out[(0, 0, 0)] = 0.5 * (onsite + onsite.T)
+    return out
+
+
+def kanamori_spin_vertex(norb, U, J):
+    _, U_s = kanamori_charge_and_spin_quartic_interaction_tensors(norb, U, U - 2 * J, J, J)
+    return U_s
+
+
+CONFIGS = {
+    "cfg0": dict(name="square_1band_16x16_beta10_nmax64", hop=lambda: square_1band(1.0), dims=(16, 16, 1),
+                 beta=10.0, mu=0.0, n_max=64, nw=64, vertex=lambda: np.full((1, 1, 1, 1), 1.0 + 0j)),
+    "cfg1": dict(name="cubic_3orb_32x32x32_beta20_nmax256", hop=lambda: cubic_3orb(0), dims=(32, 32, 32),
+                 beta=20.0, mu=0.0, n_max=256, nw=256, vertex=lambda: kanamori_spin_vertex(3, 2.3, 0.4)),
+    "cfg3": dict(name="square_2orb_32x32_beta16_nmax128", hop=lambda: square_2orb(0), dims=(32, 32, 1),
+                 beta=16.0, mu=0.0, n_max=128, nw=128, vertex=lambda: kanamori_spin_vertex(2, 1.2, 0.2)),
+    "cfg4": dict(name="layered_5orb_64x64x4_beta40_nmax512", hop=lambda: layered_5orb(0), dims=(64, 64, 4),
+                 beta=40.0, mu=0.0, n_max=512, nw=256, vertex=lambda: kanamori_spin_vertex(5, 3.0, 0.5)),
+}
+
+
+def config(key: str, **overrides) -> dict:
+    c = dict(CONFIGS[key])
+    c["hoppings"] = c.pop("hop")()
+    c["U"] = c.pop("vertex")()
+    c.update(overrides)
+    return c
