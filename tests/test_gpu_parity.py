@@ -144,10 +144,16 @@ def test_nu_to_tau(cuda_lib, case, mode):
 def test_nu_to_tau_tail_fit_error_is_reported(cuda_lib):
     T = tp()
     rng = np.random.default_rng(3)
-    wmesh, rmesh = T.MeshImFreq(2.0, "Fermion", 16), T.MeshCycLat(dims=(2, 1, 1))
-    g = T.Gf(mesh=T.MeshProduct(wmesh, rmesh), data=rand_c(rng, 32, 2, 1, 1))
+    wmesh, rmesh = T.MeshImFreq(2.0, "Fermion", 100), T.MeshCycLat(dims=(2, 1, 1))
+    data = rand_c(rng, 200, 2, 1, 1)
+    assert O.tail_fit(data.reshape(200, -1), 2.0, 100)[1] > 1e-3  # the oracle sees the same misfit
+    g = T.Gf(mesh=T.MeshProduct(wmesh, rmesh), data=data)
     with pytest.raises(RuntimeError, match="1e-3"):
         T.fourier_wr_to_tr(g)
+    # the device error word is cleared: the next good call succeeds
+    ek = O.ek_from_hoppings({(1,): -np.eye(1), (-1,): -np.eye(1)}, (2, 1, 1))
+    g0 = O.fourier_wk_to_wr(O.lattice_dyson_g0_wk(0.0, ek, 2.0, 100), (2, 1, 1))
+    T.fourier_wr_to_tr(T.Gf(mesh=g.mesh, data=g0))
 
 
 @pytest.mark.parametrize("nw", [1, 2, 16, 64])
