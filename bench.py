@@ -310,35 +310,39 @@ def run_gpu(args):
     value = world * points / (ms_per_step / 1e3)
 
     # ---- end to end through the public API, host buffers in and out
-    ek_host = e_k.cpu().pin_memory()
-    out_host = torch.empty((nwt, nk) + (nb,) * 4, dtype=torch.complex128, pin_memory=True)
-    wmesh = T.MeshImFreq(beta, "Fermion", n_max)
-    kmesh = T.MeshBrZone(dims=dims)
-    ws = torch.empty(T.lattice_utils.bubble_workspace_bytes(n_max, n_tau, dims, nb), dtype=torch.uint8, device=dev)
-    del g_wk, g_wr, g_tr, chi0, chi
-    torch.cuda.empty_cache()
-    lib.tprf_set_sync_checks(1)
+    e2e = None
+    if not args.no_e2e:
+        ek_host = e_k.cpu().pin_memory()
+        out_host = torch.empty((nwt, nk) + (nb,) * 4, dtype=torch.complex128, pin_memory=True)
+        wmesh = T.MeshImFreq(beta, "Fermion", n_max)
+        kmesh = T.MeshBrZone(dims=dims)
+        ws = torch.empty(T.lattice_utils.bubble_workspace_bytes(n_max, n_tau, dims, nb), dtype=torch.uint8,
+                         device=dev)
+        del g_wk, g_wr, g_tr, chi0, chi
+        torch.cuda.empty_cache()
+        lib.tprf_set_sync_checks(1)
 
-    def e2e_step():
-        ekd = ek_host.to(dev, non_blocking=True)
-        g = T.lattice_dyson_g0_wk(mu, T.Gf(mesh=kmesh, data=ekd), wmesh)
-        c0 = T.imtime_bubble_chi0_wk(g, nw=nw, verbose=False, workspace=ws)
-        del g
-        c = T.solve_rpa_PH(c0, cfg["U"])
-        del c0
-        out_host.copy_(c.data, non_blocking=True)
-        del c
+        def e2e_step():
+            ekd = ek_host.to(dev, non_blocking=True)
+            g = T.lattice_dyson_g0_wk(mu, T.Gf(mesh=kmesh, data=ekd), wmesh)
+            c0 = T.imtime_bubble_chi0_wk(g, nw=nw, verbose=False, workspace=ws)
+            del g
+            c = T.solve_rpa_PH(c0, cfg["U"])
+            del c0
+            out_host.copy_(c.data, non_blocking=True)
+            del c
 
-    e2e_steps = max(1, min(args.steps, 3))
-    e2e_step()
-    torch.cuda.synchronize()
-    barrier(world, dev)
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
+        e2e_steps = max(1, min(args.steps, 3))
         e2e_step()
-    torch.cuda.synchronize()
-    e2e_s = max_over_ranks((time.perf_counter() - t0) / e2e_steps, world, dev)
-    e2e_value = world * points / e2e_s
+        torch.cuda.synchronize()
+        barrier(world, dev)
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            e2e_step()
+        torch.cuda.synchronize()
+        e2e_s = max_over_ranks((time.perf_counter() - t0) / e2e_steps, world, dev)
+        e2e = {"value": world * points / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(ek_host.numel() * C16),
+               "d2h_bytes_per_step": int(out_host.numel() * C16)}
 
     # ---- roofline of the dominant kernel
     model = stage_model(nb, nk, n_nu, n_tau, nw)
@@ -351,7 +355,7 @@ def run_gpu(args):
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
     achieved = model[top]["bytes"] / (stage_ms[top] * 1e-3) / 1e9
-    fp64_peak_tflops = 1.0  # FP64 FMA throughput measured on this GB300 pool (probe in profiles/)
+    fp64_peak_tflops = measure_fp64_peak(lib, dev)
     per_stage = {s: {"ms": round(stage_ms[s], 3), "share": round(stage_ms[s] / sum(stage_ms.values()), 4),
                      "hbm_gbs": round(model[s]["bytes"] / (stage_ms[s] * 1e-3) / 1e9, 1),
                      "hbm_frac": round(model[s]["bytes"] / (stage_ms[s] * 1e-3) / 1e9 / hbm_peak, 4),
@@ -370,10 +374,10 @@ def run_gpu(args):
         "dtype": "c128", "data": "synthetic (seeded tight-binding model)",
         "config": {"workload": cfg["name"], "dims": list(dims), "nb": nb, "beta": beta, "n_max": n_max, "nw": nw,
                    "n_tau": n_tau, "points_per_step": points, "vertex": "Kanamori spin channel U=2.3 J=0.4",
-                   "l2": "inputs larger than L2 (G(tau,r) 7.2 GB, chi 21.7 GB per step)",
+                   "l2": f"inputs larger than L2 (G(tau,r) {n_tau * nk * nb2 * C16 / 1e9:.2f} GB, "
+                         f"chi {points * nb4 * C16 / 1e9:.2f} GB per step)",
                    "parallelism": f"replicas x{world}"},
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(ek_host.numel() * C16),
-                "d2h_bytes_per_step": int(out_host.numel() * C16)},
+        "e2e": e2e,
         "gpu_launches": launches_per_step * args.steps,
         "roofline": roofline,
         "clocks": clocks.summary(),
@@ -390,9 +394,26 @@ def run_gpu(args):
         print(json.dumps(line), flush=True)
 
 
-# DRAM traffic per launch of the dominant kernel, from the ncu captures
-# summarised under profiles/ (None until captured).
-TRAFFIC = {}
+def measure_fp64_peak(lib, dev) -> float:
+    """Live FP64 FMA throughput of this GPU (TFLOP/s), the denominator of the FP64 fractions."""
+    import ctypes
+
+    import torch
+    from tprf_gb300._native import check
+    scratch = torch.empty(2048 * 256, dtype=torch.float64, device=dev)
+    out = ctypes.c_double(0.0)
+    check(lib.tprf_measure_fp64_tflops(ctypes.byref(out), scratch.data_ptr(), scratch.numel() * 8,
+                                       torch.cuda.current_stream().cuda_stream), "measure_fp64_tflops")
+    return round(out.value, 3)
+
+
+# DRAM traffic (read + write) per launch, from the ncu captures summarised under
+# profiles/ (16x16x8 case, 2048 r points), scaled to 32^3 (x16) by the number of r
+# points: the kernels stream their columns, so traffic grows in proportion.
+TRAFFIC = {
+    ("cfg1", "bubble_tau_to_w"): 16 * 2.183e9,  # profiles/tau_to_w_bubble_cubic3orb_16x16x8.md
+    ("cfg1", "rpa"): 16 * 2.665e9,              # profiles/rpa_kernel_cubic3orb_16x16x8.md
+}
 
 
 # ---------------------------------------------------------------------------
@@ -439,6 +460,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="cfg1")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

@@ -59,6 +59,13 @@ const char *tprf_version(void);
 void tprf_set_sync_checks(int on);
 int tprf_check_device_status(void *stream);
 
+/* Device capability: sustained FP64 FMA throughput (TFLOP/s) of the current
+ * GPU, best of three timed runs of a fixed-length FMA loop; synchronises
+ * `stream`. The path's kernels are bound by this pipe on GB300, so the
+ * benchmark reports FP64 fractions against it. No reference counterpart.
+ * scratch: device buffer of at least 2048 doubles per SM. */
+int tprf_measure_fp64_tflops(double *tflops, void *scratch, size_t scratch_bytes, void *stream);
+
 /* Host-only (no GPU): the tail-fit definition tprf_fourier_wr_to_tr applies
  * when moments == NULL. A least-squares fit of g(iv) ~ sum_{p<=P} c_p (iv)^-p
  * on the outer 20% of the fermionic mesh (at most 30 points a side, both
