@@ -59,6 +59,16 @@ const char *tprf_version(void);
 void tprf_set_sync_checks(int on);
 int tprf_check_device_status(void *stream);
 
+/* Arithmetic of the FFT stages (lattice FFTs, iv -> tau, tau -> i omega).
+ * TPRF_ARITH_DF64 (default): butterflies in double-float pairs on the FP32
+ * pipe (~48-bit significand; on GB300 FP32 runs ~70x faster than FP64);
+ * TPRF_ARITH_FP64: native FP64. Inputs and outputs are complex128 either way.
+ * Process-wide; no reference counterpart (the reference has one CPU path). */
+#define TPRF_ARITH_DF64 0
+#define TPRF_ARITH_FP64 1
+int tprf_set_arithmetic(int mode);
+int tprf_get_arithmetic(void);
+
 /* Device capability: sustained FP64 FMA throughput (TFLOP/s) of the current
  * GPU, best of three timed runs of a fixed-length FMA loop; synchronises
  * `stream`. The path's kernels are bound by this pipe on GB300, so the

@@ -15,6 +15,15 @@ from conftest import PARITY_RTOL, rel_err
 pytestmark = pytest.mark.gpu
 
 
+@pytest.fixture(autouse=True, params=["df64", "fp64"])
+def arithmetic(request, cuda_lib):
+    """Every parity test runs with the FFT stages in double-float and in native FP64."""
+    mode = {"df64": 0, "fp64": 1}[request.param]
+    assert cuda_lib.tprf_set_arithmetic(mode) == 0
+    yield request.param
+    cuda_lib.tprf_set_arithmetic(0)
+
+
 def tp():
     import tprf_gb300 as T
     return T
@@ -157,11 +166,12 @@ def test_nu_to_tau_tail_fit_error_is_reported(cuda_lib):
 
 
 @pytest.mark.parametrize("nw", [1, 2, 16, 64])
-def test_tau_to_w(cuda_lib, nw):
+@pytest.mark.parametrize("n_tau", [-1, 263])  # L = 384 (7-smooth) and L = 262 = 2 x 131 (generic radix)
+def test_tau_to_w(cuda_lib, nw, n_tau):
     T = tp()
     hopf, dims, beta, n_max = CASES[0]
     _, _, g_wr, g_wr_ref = _g_wr(hopf(), dims, beta, n_max)
-    g_tr_ref = O.fourier_wr_to_tr(g_wr_ref, beta)
+    g_tr_ref = O.fourier_wr_to_tr(g_wr_ref, beta, n_tau)
     chi_tr_ref = O.chi0_tr_from_grt_PH(g_tr_ref, dims)
     tmesh = T.MeshImTime(beta, "Boson", chi_tr_ref.shape[0])
     chi_tr = T.Gf(mesh=T.MeshProduct(tmesh, T.MeshCycLat(dims=dims)), data=chi_tr_ref)

@@ -23,6 +23,8 @@ SIGNATURES = {
     "tprf_version": (ctypes.c_char_p, []),
     "tprf_set_sync_checks": (None, [c_int]),
     "tprf_check_device_status": (c_int, [c_void_p]),
+    "tprf_set_arithmetic": (c_int, [c_int]),
+    "tprf_get_arithmetic": (c_int, []),
     "tprf_measure_fp64_tflops": (c_int, [ctypes.POINTER(c_double), c_void_p, c_size_t, c_void_p]),
     "tprf_tail_fit_matrix": (c_int, [c_double, c_int, c_int, ctypes.POINTER(c_int), ctypes.POINTER(c_int),
                                      ctypes.POINTER(c_int), ctypes.POINTER(c_double)]),

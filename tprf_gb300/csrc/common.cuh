@@ -1,9 +1,11 @@
 // Device-side helpers shared by the tprf_gb300 kernels (complex128 arithmetic,
-// small DFT butterflies, the shared-memory Stockham FFT).
+// small DFT butterflies and the shared-memory Stockham FFT, generic over the
+// element type: double2 or the double-float cdf of dfloat.cuh).
 #pragma once
 
 #include <cuda_runtime.h>
 
+#include "dfloat.cuh"
 #include "internal.hpp"
 
 namespace tprf {
@@ -35,35 +37,67 @@ __device__ __forceinline__ double2 mul_mi(double2 a) {
 }
 
 // ---------------------------------------------------------------------------
-// Small DFTs, y_q = sum_r v_r exp(-+ 2 pi i r q / R) (FWD: minus sign).
-template <int R, bool FWD> struct Dft;
+// Generic complex element types for the FFT: double2 (native FP64) and cdf
+// (double-float on the FP32 pipe). RealT<C> is the matching real type, kc<C>
+// turns a literal into it at compile time.
+template <class C> struct RealT;
+template <> struct RealT<double2> { using type = double; };
+template <> struct RealT<cdf> { using type = dfl; };
 
-template <bool FWD> struct Dft<2, FWD> {
-  static __device__ __forceinline__ void run(double2 *v) {
-    double2 a = v[0], b = v[1];
+template <class C> __host__ __device__ constexpr typename RealT<C>::type kc(double v);
+template <> __host__ __device__ constexpr double kc<double2>(double v) { return v; }
+template <> __host__ __device__ constexpr dfl kc<cdf>(double v) { return kdf(v); }
+
+__device__ __forceinline__ double2 caxpy(double k, double2 x, double2 y) {
+  return make_double2(fma(k, x.x, y.x), fma(k, x.y, y.y));
+}
+
+template <class C> __device__ __forceinline__ C czero();
+template <> __device__ __forceinline__ double2 czero<double2>() { return make_double2(0.0, 0.0); }
+template <> __device__ __forceinline__ cdf czero<cdf>() { return cdf{dfl{0.f, 0.f}, dfl{0.f, 0.f}}; }
+
+// Twiddle table of a plan in element type C: exp(-2 pi i t / n), t < n.
+template <class C> __device__ __forceinline__ const C *twiddles(const FftDesc &d);
+template <> __device__ __forceinline__ const double2 *twiddles<double2>(const FftDesc &d) { return d.tw; }
+template <> __device__ __forceinline__ const cdf *twiddles<cdf>(const FftDesc &d) {
+  return reinterpret_cast<const cdf *>(d.twf);
+}
+
+template <bool FWD, class C>
+__device__ __forceinline__ C root(const C *tw, long idx) {
+  const C t = tw[idx];
+  return FWD ? t : cconj(t);
+}
+
+// ---------------------------------------------------------------------------
+// Small DFTs, y_q = sum_r v_r exp(-+ 2 pi i r q / R) (FWD: minus sign).
+template <int R, bool FWD, class C> struct Dft;
+
+template <bool FWD, class C> struct Dft<2, FWD, C> {
+  static __device__ __forceinline__ void run(C *v) {
+    const C a = v[0], b = v[1];
     v[0] = cadd(a, b);
     v[1] = csub(a, b);
   }
 };
 
-template <bool FWD> struct Dft<3, FWD> {
-  static __device__ __forceinline__ void run(double2 *v) {
-    const double s3 = 0.86602540378443864676;  // sin(2 pi / 3)
-    double2 t1 = cadd(v[1], v[2]);
-    double2 t2 = make_double2(fma(-0.5, t1.x, v[0].x), fma(-0.5, t1.y, v[0].y));
-    double2 t3 = csub(v[1], v[2]);
-    // -i s3 t3 (FWD) or +i s3 t3
-    double2 t4 = FWD ? make_double2(s3 * t3.y, -s3 * t3.x) : make_double2(-s3 * t3.y, s3 * t3.x);
+template <bool FWD, class C> struct Dft<3, FWD, C> {
+  static __device__ __forceinline__ void run(C *v) {
+    constexpr auto s3 = kc<C>(0.86602540378443864676);  // sin(2 pi / 3)
+    constexpr auto mh = kc<C>(-0.5);
+    const C t1 = cadd(v[1], v[2]);
+    const C t2 = caxpy(mh, t1, v[0]);
+    const C t4 = mul_mi<FWD>(cscale(csub(v[1], v[2]), s3));
     v[0] = cadd(v[0], t1);
     v[1] = cadd(t2, t4);
     v[2] = csub(t2, t4);
   }
 };
 
-template <bool FWD> struct Dft<4, FWD> {
-  static __device__ __forceinline__ void run(double2 *v) {
-    double2 a = cadd(v[0], v[2]), b = csub(v[0], v[2]);
-    double2 c = cadd(v[1], v[3]), d = mul_mi<FWD>(csub(v[1], v[3]));
+template <bool FWD, class C> struct Dft<4, FWD, C> {
+  static __device__ __forceinline__ void run(C *v) {
+    const C a = cadd(v[0], v[2]), b = csub(v[0], v[2]);
+    const C c = cadd(v[1], v[3]), d = mul_mi<FWD>(csub(v[1], v[3]));
     v[0] = cadd(a, c);
     v[2] = csub(a, c);
     v[1] = cadd(b, d);
@@ -71,22 +105,21 @@ template <bool FWD> struct Dft<4, FWD> {
   }
 };
 
-template <bool FWD> struct Dft<5, FWD> {
-  static __device__ __forceinline__ void run(double2 *v) {
-    const double c1 = 0.30901699437494742410;   // cos(2 pi / 5)
-    const double c2 = -0.80901699437494742410;  // cos(4 pi / 5)
-    const double s1 = 0.95105651629515357212;   // sin(2 pi / 5)
-    const double s2 = 0.58778525229247312917;   // sin(4 pi / 5)
-    double2 a1 = cadd(v[1], v[4]), b1 = csub(v[1], v[4]);
-    double2 a2 = cadd(v[2], v[3]), b2 = csub(v[2], v[3]);
-    double2 x0 = v[0];
-    double2 r1 = make_double2(x0.x + c1 * a1.x + c2 * a2.x, x0.y + c1 * a1.y + c2 * a2.y);
-    double2 r2 = make_double2(x0.x + c2 * a1.x + c1 * a2.x, x0.y + c2 * a1.y + c1 * a2.y);
-    // i-parts: q=1: -i(s1 b1 + s2 b2), q=2: -i(s2 b1 - s1 b2)  (FWD)
-    double2 i1 = make_double2(s1 * b1.x + s2 * b2.x, s1 * b1.y + s2 * b2.y);
-    double2 i2 = make_double2(s2 * b1.x - s1 * b2.x, s2 * b1.y - s1 * b2.y);
-    i1 = mul_mi<FWD>(i1);
-    i2 = mul_mi<FWD>(i2);
+template <bool FWD, class C> struct Dft<5, FWD, C> {
+  static __device__ __forceinline__ void run(C *v) {
+    constexpr auto c1 = kc<C>(0.30901699437494742410);   // cos(2 pi / 5)
+    constexpr auto c2 = kc<C>(-0.80901699437494742410);  // cos(4 pi / 5)
+    constexpr auto s1 = kc<C>(0.95105651629515357212);   // sin(2 pi / 5)
+    constexpr auto s2 = kc<C>(0.58778525229247312917);   // sin(4 pi / 5)
+    constexpr auto ms1 = kc<C>(-0.95105651629515357212);
+    const C a1 = cadd(v[1], v[4]), b1 = csub(v[1], v[4]);
+    const C a2 = cadd(v[2], v[3]), b2 = csub(v[2], v[3]);
+    const C x0 = v[0];
+    const C r1 = caxpy(c2, a2, caxpy(c1, a1, x0));
+    const C r2 = caxpy(c1, a2, caxpy(c2, a1, x0));
+    // q = 1: -i (s1 b1 + s2 b2), q = 2: -i (s2 b1 - s1 b2)  (FWD)
+    const C i1 = mul_mi<FWD>(caxpy(s2, b2, cscale(b1, s1)));
+    const C i2 = mul_mi<FWD>(caxpy(ms1, b2, cscale(b1, s2)));
     v[0] = cadd(x0, cadd(a1, a2));
     v[1] = cadd(r1, i1);
     v[4] = csub(r1, i1);
@@ -95,28 +128,29 @@ template <bool FWD> struct Dft<5, FWD> {
   }
 };
 
-template <bool FWD> struct Dft<7, FWD> {
-  static __device__ __forceinline__ void run(double2 *v) {
-    const double c[3] = {0.62348980185873353053, -0.22252093395631440429, -0.90096886790241912624};
-    const double s[3] = {0.78183148246802980871, 0.97492791218182360702, 0.43388373911755812048};
-    double2 a[3], b[3];
+template <bool FWD, class C> struct Dft<7, FWD, C> {
+  static __device__ __forceinline__ void run(C *v) {
+    // cos and sin of 2 pi m / 7, m = 1..6
+    constexpr double cs[6] = {0.62348980185873353053, -0.22252093395631440429, -0.90096886790241912624,
+                              -0.90096886790241912624, -0.22252093395631440429, 0.62348980185873353053};
+    constexpr double sn[6] = {0.78183148246802980871, 0.97492791218182360702, 0.43388373911755812048,
+                              -0.43388373911755812048, -0.97492791218182360702, -0.78183148246802980871};
+    C a[3], b[3];
 #pragma unroll
     for (int q = 0; q < 3; ++q) {
       a[q] = cadd(v[q + 1], v[6 - q]);
       b[q] = csub(v[q + 1], v[6 - q]);
     }
-    double2 x0 = v[0];
+    const C x0 = v[0];
     v[0] = cadd(x0, cadd(a[0], cadd(a[1], a[2])));
 #pragma unroll
     for (int q = 1; q <= 3; ++q) {
-      double2 re = x0, im = make_double2(0.0, 0.0);
+      C re = x0, im = czero<C>();
 #pragma unroll
       for (int r = 1; r <= 3; ++r) {
         const int m = (q * r) % 7;
-        const double cc = (m <= 3) ? c[m - 1] : c[7 - m - 1];
-        const double ss = (m <= 3) ? s[m - 1] : -s[7 - m - 1];
-        re = make_double2(fma(cc, a[r - 1].x, re.x), fma(cc, a[r - 1].y, re.y));
-        im = make_double2(fma(ss, b[r - 1].x, im.x), fma(ss, b[r - 1].y, im.y));
+        re = caxpy(kc<C>(cs[m - 1]), a[r - 1], re);
+        im = caxpy(kc<C>(sn[m - 1]), b[r - 1], im);
       }
       im = mul_mi<FWD>(im);
       v[q] = cadd(re, im);
@@ -125,22 +159,17 @@ template <bool FWD> struct Dft<7, FWD> {
   }
 };
 
-template <bool FWD> struct Dft<8, FWD> {
-  static __device__ __forceinline__ void run(double2 *v) {
-    const double h = 0.70710678118654752440;
-    // radix-2 split into even / odd halves, each a 4-point DFT
-    double2 e[4] = {v[0], v[2], v[4], v[6]};
-    double2 o[4] = {v[1], v[3], v[5], v[7]};
-    Dft<4, FWD>::run(e);
-    Dft<4, FWD>::run(o);
-    // twiddles W8^q for q = 0..3
-    double2 o1 = o[1], o3 = o[3];
-    // W8 = (1 - i)/sqrt2 (FWD) ; W8^3 = (-1 - i)/sqrt2 (FWD)
-    double2 t1 = FWD ? make_double2(h * (o1.x + o1.y), h * (o1.y - o1.x))
-                     : make_double2(h * (o1.x - o1.y), h * (o1.y + o1.x));
-    double2 t2 = mul_mi<FWD>(o[2]);
-    double2 t3 = FWD ? make_double2(h * (o3.y - o3.x), -h * (o3.x + o3.y))
-                     : make_double2(-h * (o3.x + o3.y), h * (o3.x - o3.y));
+template <bool FWD, class C> struct Dft<8, FWD, C> {
+  static __device__ __forceinline__ void run(C *v) {
+    constexpr auto h = kc<C>(0.70710678118654752440);
+    C e[4] = {v[0], v[2], v[4], v[6]};
+    C o[4] = {v[1], v[3], v[5], v[7]};
+    Dft<4, FWD, C>::run(e);
+    Dft<4, FWD, C>::run(o);
+    // W8^1 o1 = h (o1 + mul_mi(o1)),  W8^2 o2 = mul_mi(o2),  W8^3 o3 = h (mul_mi(o3) - o3)
+    const C t1 = cscale(cadd(o[1], mul_mi<FWD>(o[1])), h);
+    const C t2 = mul_mi<FWD>(o[2]);
+    const C t3 = cscale(csub(mul_mi<FWD>(o[3]), o[3]), h);
     v[0] = cadd(e[0], o[0]);
     v[4] = csub(e[0], o[0]);
     v[1] = cadd(e[1], t1);
@@ -153,87 +182,94 @@ template <bool FWD> struct Dft<8, FWD> {
 };
 
 // ---------------------------------------------------------------------------
-// One Stockham stage on `ncol` interleaved columns: element i of column c is
-// at [i * ncol + c]. Ns = product of the radices of the earlier stages.
-template <int R, bool FWD>
-__device__ __forceinline__ void fft_stage(const double2 *__restrict__ in, double2 *__restrict__ out, int n,
-                                          int Ns, int ncol, const double2 *__restrict__ tw, int tid, int nthr) {
+// In-place decimation-in-time FFT on `ncol` interleaved columns held in
+// shared memory: element i of column c is at [i * ncol + c]. The input must
+// be loaded in mixed-radix digit-reversed order (element t of a column goes to
+// position FftDesc::rev[t]); the output comes out in natural order. Stage s
+// with radix R and Ns = R_0 ... R_{s-1} combines, for every butterfly j, the R
+// elements base + r Ns (base = (j - j mod Ns) R + j mod Ns) after twiddling
+// element r by W_{Ns R}^{(j mod Ns) r}. Butterflies of a stage touch disjoint
+// elements, so one buffer suffices.
+//
+// Threads: ncol divides blockDim.x; a thread keeps one column and walks the
+// butterflies j = j0, j0 + step, ..., so no integer division happens inside
+// the loops.
+template <int R, bool FWD, class C>
+__device__ __forceinline__ void fft_stage(C *__restrict__ a, int n, int Ns, int ncol, const C *__restrict__ tw) {
   const int nbf = n / R;
   const int tws = n / (Ns * R);
-  const int total = nbf * ncol;
-  for (int w = tid; w < total; w += nthr) {
-    const int col = w % ncol;
-    const int j = w / ncol;
-    const int k = j % Ns;
-    double2 v[R];
+  const int col = threadIdx.x % ncol;
+  const int j0 = threadIdx.x / ncol;
+  const int step = blockDim.x / ncol;
+  const int kstep = step % Ns;
+  int k = j0 % Ns;
+  for (int j = j0; j < nbf; j += step) {
+    const int base = (j - k) * R + k;
+    C v[R];
 #pragma unroll
-    for (int r = 0; r < R; ++r) v[r] = in[(j + r * nbf) * ncol + col];
+    for (int r = 0; r < R; ++r) v[r] = a[(base + r * Ns) * ncol + col];
     if (Ns > 1) {
 #pragma unroll
-      for (int r = 1; r < R; ++r) {
-        double2 t = __ldg(&tw[k * r * tws]);
-        if (!FWD) t.y = -t.y;
-        v[r] = cmul(v[r], t);
-      }
+      for (int r = 1; r < R; ++r) v[r] = cmul(v[r], root<FWD>(tw, (long)k * r * tws));
     }
-    Dft<R, FWD>::run(v);
-    const int base = (j - k) * R + k;
+    Dft<R, FWD, C>::run(v);
 #pragma unroll
-    for (int r = 0; r < R; ++r) out[(base + r * Ns) * ncol + col] = v[r];
+    for (int r = 0; r < R; ++r) a[(base + r * Ns) * ncol + col] = v[r];
+    k += kstep;
+    if (k >= Ns) k -= Ns;
   }
 }
 
-// Stage with an arbitrary radix R (any prime factor the fixed butterflies do
-// not cover): each work item computes one output of one butterfly as a direct
-// R-point sum, y_q = sum_r v_r W_n^(k r n/(Ns R)) W_R^(r q), with both roots
-// read from the length-n table. Cost R complex multiply-adds per output.
-template <bool FWD>
-__device__ __noinline__ void fft_stage_generic(const double2 *__restrict__ in, double2 *__restrict__ out, int n,
-                                               int R, int Ns, int ncol, const double2 *__restrict__ tw, int tid,
-                                               int nthr) {
-  const int nbf = n / R;
+// Stage with an arbitrary radix R (a prime factor the fixed butterflies do
+// not cover): each work item computes one output q of one butterfly as a
+// direct R-point sum, reading buffer `in` and writing the same positions of
+// `out`. Cost R complex multiply-adds per output.
+template <bool FWD, class C>
+__device__ __noinline__ void fft_stage_generic(const C *__restrict__ in, C *__restrict__ out, int n, int R, int Ns,
+                                               int ncol, const C *__restrict__ tw) {
   const int tws = n / (Ns * R);
-  const long total = (long)n * ncol;
-  for (long w = tid; w < total; w += nthr) {
-    const int col = (int)(w % ncol);
-    const long t = w / ncol;
-    const int q = (int)(t % R);
-    const int j = (int)(t / R);
+  const int nbf = n / R;
+  const int col = threadIdx.x % ncol;
+  const int step = blockDim.x / ncol;
+  for (int w = threadIdx.x / ncol; w < n; w += step) {
+    const int j = w / R, q = w - (w / R) * R;
     const int k = j % Ns;
-    double2 acc = make_double2(0.0, 0.0);
+    const int base = (j - k) * R + k;
+    C acc = czero<C>();
     for (int r = 0; r < R; ++r) {
       const long e = ((long)k * r * tws + (long)((r * q) % R) * nbf) % n;
-      double2 root = __ldg(&tw[e]);
-      if (!FWD) root.y = -root.y;
-      acc = cfma(in[(j + r * nbf) * ncol + col], root, acc);
+      acc = cadd(acc, cmul(in[(base + r * Ns) * ncol + col], root<FWD>(tw, e)));
     }
-    out[((j - k) * R + k + q * Ns) * ncol + col] = acc;
+    out[(base + q * Ns) * ncol + col] = acc;
   }
 }
 
-// Full transform of `ncol` columns held in buffer a (b is scratch of the same
-// size). Returns the buffer that holds the result. Starts and ends with a
-// block-wide barrier.
-template <bool FWD>
-__device__ double2 *fft_smem(double2 *a, double2 *b, const FftDesc &d, int ncol) {
+// Full transform of the `ncol` columns in buffer a (digit-reversed order in,
+// natural order out). b is a second buffer of the same size, used only when
+// the plan has a generic-radix stage (d.has_generic), else may be null.
+// Returns the buffer holding the result. Starts and ends with a barrier.
+template <bool FWD, class C>
+__device__ C *fft_smem(C *a, C *b, const FftDesc &d, int ncol) {
   __syncthreads();
-  const int tid = threadIdx.x, nthr = blockDim.x;
+  const C *tw = twiddles<C>(d);
   int Ns = 1;
   for (int s = 0; s < d.nst; ++s) {
     const int R = d.radix[s];
     switch (R) {
-      case 2: fft_stage<2, FWD>(a, b, d.n, Ns, ncol, d.tw, tid, nthr); break;
-      case 3: fft_stage<3, FWD>(a, b, d.n, Ns, ncol, d.tw, tid, nthr); break;
-      case 4: fft_stage<4, FWD>(a, b, d.n, Ns, ncol, d.tw, tid, nthr); break;
-      case 5: fft_stage<5, FWD>(a, b, d.n, Ns, ncol, d.tw, tid, nthr); break;
-      case 7: fft_stage<7, FWD>(a, b, d.n, Ns, ncol, d.tw, tid, nthr); break;
-      case 8: fft_stage<8, FWD>(a, b, d.n, Ns, ncol, d.tw, tid, nthr); break;
-      default: fft_stage_generic<FWD>(a, b, d.n, R, Ns, ncol, d.tw, tid, nthr); break;
+      case 2: fft_stage<2, FWD>(a, d.n, Ns, ncol, tw); break;
+      case 3: fft_stage<3, FWD>(a, d.n, Ns, ncol, tw); break;
+      case 4: fft_stage<4, FWD>(a, d.n, Ns, ncol, tw); break;
+      case 5: fft_stage<5, FWD>(a, d.n, Ns, ncol, tw); break;
+      case 7: fft_stage<7, FWD>(a, d.n, Ns, ncol, tw); break;
+      case 8: fft_stage<8, FWD>(a, d.n, Ns, ncol, tw); break;
+      default: {
+        fft_stage_generic<FWD>(a, b, d.n, R, Ns, ncol, tw);
+        C *t = a;
+        a = b;
+        b = t;
+      }
     }
     Ns *= R;
-    double2 *t = a;
-    a = b;
-    b = t;
     __syncthreads();
   }
   return a;

@@ -1,0 +1,134 @@
+// Double-float ("df64") arithmetic: a real number is an unevaluated sum
+// hi + lo of two FP32 values, |lo| <= ulp(hi), about 48 significant bits.
+//
+// GB300 executes FP32 at ~70x its FP64 rate, so the FFT stages of this path
+// run their butterflies in this representation on the FP32 pipe. The
+// operations are the classical error-free transformations: Knuth's TwoSum,
+// Dekker's Fast2Sum (quick_two_sum) and the FMA-based TwoProduct, combined as
+// in the published double-double algorithms (Hida, Li & Bailey, "Algorithms
+// for quad-double precision floating point arithmetic", 2001), applied to two
+// floats instead of two doubles. Additions use the "sloppy" variant (one
+// TwoSum plus a Fast2Sum): its error is bounded relative to |a| + |b|, which
+// is what an FFT needs. Every float operation uses a _rn intrinsic so the
+// compiler can neither contract nor reassociate it.
+//
+// Conversions from and to FP64 use integer bit operations (and one FP64 add
+// per real on the way back), not the conversion instructions.
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace tprf {
+
+struct dfl {
+  float hi, lo;
+};
+
+struct __align__(16) cdf {
+  dfl x, y;  // real, imaginary
+};
+
+__host__ __device__ constexpr dfl kdf(double v) { return dfl{(float)v, (float)(v - (double)(float)v)}; }
+
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+__device__ __forceinline__ dfl fast_two_sum(float a, float b) {  // requires |a| >= |b| or a == 0
+  const float s = __fadd_rn(a, b);
+  return dfl{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+
+__device__ __forceinline__ dfl dneg(dfl a) { return dfl{-a.hi, -a.lo}; }
+
+__device__ __forceinline__ dfl dadd(dfl a, dfl b) {
+  float s, e;
+  two_sum(a.hi, b.hi, s, e);
+  e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
+  return fast_two_sum(s, e);
+}
+
+__device__ __forceinline__ dfl dsub(dfl a, dfl b) { return dadd(a, dneg(b)); }
+
+__device__ __forceinline__ dfl dmul(dfl a, dfl b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  return fast_two_sum(p, e);
+}
+
+// a1 b1 - a2 b2 with one rounding-error accumulator
+__device__ __forceinline__ dfl ddot_sub(dfl a1, dfl b1, dfl a2, dfl b2) {
+  const float p1 = __fmul_rn(a1.hi, b1.hi);
+  const float e1 = __fmaf_rn(a1.hi, b1.hi, -p1);
+  const float p2 = __fmul_rn(a2.hi, b2.hi);
+  const float e2 = __fmaf_rn(a2.hi, b2.hi, -p2);
+  float s, es;
+  two_sum(p1, -p2, s, es);
+  float e = __fadd_rn(es, __fsub_rn(e1, e2));
+  e = __fmaf_rn(a1.hi, b1.lo, e);
+  e = __fmaf_rn(a1.lo, b1.hi, e);
+  e = __fmaf_rn(-a2.hi, b2.lo, e);
+  e = __fmaf_rn(-a2.lo, b2.hi, e);
+  return fast_two_sum(s, e);
+}
+
+// a1 b1 + a2 b2
+__device__ __forceinline__ dfl ddot_add(dfl a1, dfl b1, dfl a2, dfl b2) { return ddot_sub(a1, b1, dneg(a2), b2); }
+
+// ---- complex ----------------------------------------------------------------
+__device__ __forceinline__ cdf cadd(cdf a, cdf b) { return cdf{dadd(a.x, b.x), dadd(a.y, b.y)}; }
+__device__ __forceinline__ cdf csub(cdf a, cdf b) { return cdf{dsub(a.x, b.x), dsub(a.y, b.y)}; }
+__device__ __forceinline__ cdf cmul(cdf a, cdf b) { return cdf{ddot_sub(a.x, b.x, a.y, b.y), ddot_add(a.x, b.y, a.y, b.x)}; }
+__device__ __forceinline__ cdf cscale(cdf a, dfl s) { return cdf{dmul(a.x, s), dmul(a.y, s)}; }
+__device__ __forceinline__ cdf cconj(cdf a) { return cdf{a.x, dneg(a.y)}; }
+// y + k x
+__device__ __forceinline__ cdf caxpy(dfl k, cdf x, cdf y) { return cadd(y, cscale(x, k)); }
+template <bool FWD>
+__device__ __forceinline__ cdf mul_mi(cdf a) {  // -i a (FWD) or +i a
+  return FWD ? cdf{a.y, dneg(a.x)} : cdf{dneg(a.y), a.x};
+}
+
+// ---- conversions --------------------------------------------------------------
+// hi = x truncated to 24 significant bits, lo = the remaining bits (rounded
+// down to 24 significant bits). Values below 2^-126 in magnitude become 0;
+// NaN and infinities go to hi.
+__device__ __forceinline__ dfl split_double(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned h = (unsigned)(b >> 32), l = (unsigned)b;
+  const unsigned sign = h & 0x80000000u;
+  const int e = (int)((h >> 20) & 0x7ffu);
+  const int fe = e - 1023 + 127;
+  if (fe <= 0) return dfl{0.f, 0.f};
+  if (fe >= 255) return dfl{__double2float_rn(x), 0.f};
+  const float hi = __uint_as_float(sign | ((unsigned)fe << 23) | ((h & 0xfffffu) << 3) | (l >> 29));
+  const unsigned r = l & 0x1fffffffu;  // remaining 29 bits, weight 2^(e - 1075)
+  if (r == 0u) return dfl{hi, 0.f};
+  const int lz = __clz(r);               // >= 3
+  const int sh = lz - 8;                 // bring the leading bit to position 23
+  const unsigned m = sh >= 0 ? (r << sh) : (r >> (-sh));
+  const int le = e - 925 - sh;           // float exponent field of lo
+  if (le <= 0) return dfl{hi, 0.f};
+  return dfl{hi, __uint_as_float(sign | ((unsigned)le << 23) | (m & 0x7fffffu))};
+}
+
+__device__ __forceinline__ double float_to_double_exact(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xffu;
+  if (e == 0u) return 0.0;
+  if (e == 0xffu) return (double)f;
+  const unsigned long long bits = ((unsigned long long)(u & 0x80000000u) << 32) |
+                                  ((unsigned long long)(e - 127u + 1023u) << 52) |
+                                  ((unsigned long long)(u & 0x7fffffu) << 29);
+  return __longlong_as_double((long long)bits);
+}
+
+__device__ __forceinline__ double to_double(dfl a) { return float_to_double_exact(a.hi) + float_to_double_exact(a.lo); }
+
+__device__ __forceinline__ cdf to_cdf(double2 z) { return cdf{split_double(z.x), split_double(z.y)}; }
+__device__ __forceinline__ double2 to_double2(cdf z) { return make_double2(to_double(z.x), to_double(z.y)); }
+
+}  // namespace tprf

@@ -8,11 +8,12 @@
 // unscaled. lattice/fourier.hpp:166-231 loops over the frequency slices.
 //
 // Design: the array is viewed as [outer, n, inner] for each transformed axis
-// (target index fastest, as in HBM). One CTA loads a tile of columns
-// (consecutive inner indices, and several outer slices when inner is short)
-// into shared memory with coalesced row reads, runs a mixed-radix Stockham
-// FFT on all columns at once and writes the tile back. One pass per mesh
-// dimension with n > 1; later passes run in place.
+// (target index fastest, as in HBM). One CTA loads a tile of up to 64
+// consecutive columns of the flattened (outer, inner) index into shared
+// memory with coalesced row reads (in digit-reversed row order), runs an
+// in-place mixed-radix FFT on all columns at once and writes the tile back. One pass per mesh
+// dimension with n > 1; later passes run in place. The butterflies run in
+// double-float pairs on the FP32 pipe by default (tprf_set_arithmetic).
 #include <algorithm>
 
 #include "common.cuh"
@@ -20,66 +21,75 @@
 namespace tprf {
 namespace {
 
-template <bool FWD>
-__global__ void __launch_bounds__(256) lattice_axis_kernel(const double2 *in, double2 *out, long outer, long inner,
-                                                           int oc, int ic, FftDesc d, double scale) {
-  extern __shared__ double2 smem[];
+template <class E> __device__ __forceinline__ E load_el(double2 z);
+template <> __device__ __forceinline__ double2 load_el<double2>(double2 z) { return z; }
+template <> __device__ __forceinline__ cdf load_el<cdf>(double2 z) { return to_cdf(z); }
+__device__ __forceinline__ double2 store_el(double2 z, double s) { return cscale(z, s); }
+__device__ __forceinline__ double2 store_el(cdf z, double s) {
+  return to_double2(s == 1.0 ? z : cscale(z, split_double(s)));
+}
+
+template <bool FWD, class E>
+__global__ void __launch_bounds__(256) lattice_axis_kernel(const double2 *in, double2 *out, long ncols_total,
+                                                           long inner, int ncol, int lgcol, FftDesc d, double scale) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
   const int n = d.n;
-  const int ncol = oc * ic;
-  double2 *a = smem;
-  double2 *b = smem + (size_t)n * ncol;
-  const long n_ichunk = (inner + ic - 1) / ic;
-  const long o0 = (blockIdx.x / n_ichunk) * oc;
-  const long i0 = (blockIdx.x % n_ichunk) * ic;
-  const int tid = threadIdx.x, nthr = blockDim.x;
+  E *a = reinterpret_cast<E *>(smem_raw);
+  E *b = d.has_generic ? a + (size_t)n * ncol : nullptr;
+  long *base = reinterpret_cast<long *>(smem_raw + (size_t)(d.has_generic ? 2 : 1) * n * ncol * sizeof(E));
+  // The tile is ncol consecutive columns of the flattened (outer, inner) index;
+  // element (row, column f) sits at (f / inner) * n * inner + row * inner + f % inner.
+  const long f0 = blockIdx.x * (long)ncol;
+  for (int c = threadIdx.x; c < ncol; c += blockDim.x) {
+    const long f = f0 + c;
+    const long o = f / inner;
+    base[c] = (f < ncols_total) ? o * n * inner + (f - o * inner) : -1;
+  }
+  __syncthreads();
   const int tile = n * ncol;
-  for (int w = tid; w < tile; w += nthr) {
-    const int il = w % ic;
-    const int row = (w / ic) % n;
-    const int ol = w / (ic * n);
-    const long o = o0 + ol, i = i0 + il;
-    double2 v = make_double2(0.0, 0.0);
-    if (o < outer && i < inner) v = in[(o * n + row) * inner + i];
-    a[row * ncol + ol * ic + il] = v;
+  for (int w = threadIdx.x; w < tile; w += blockDim.x) {
+    const int c = w & (ncol - 1), row = w >> lgcol;
+    const long bs = base[c];
+    const double2 v = bs >= 0 ? in[bs + (long)row * inner] : make_double2(0.0, 0.0);
+    a[d.rev[row] * ncol + c] = load_el<E>(v);
   }
-  double2 *r = fft_smem<FWD>(a, b, d, ncol);
-  for (int w = tid; w < tile; w += nthr) {
-    const int il = w % ic;
-    const int row = (w / ic) % n;
-    const int ol = w / (ic * n);
-    const long o = o0 + ol, i = i0 + il;
-    if (o < outer && i < inner) out[(o * n + row) * inner + i] = cscale(r[row * ncol + ol * ic + il], scale);
+  E *r = fft_smem<FWD>(a, b, d, ncol);
+  for (int w = threadIdx.x; w < tile; w += blockDim.x) {
+    const int c = w & (ncol - 1), row = w >> lgcol;
+    const long bs = base[c];
+    if (bs >= 0) out[bs + (long)row * inner] = store_el(r[row * ncol + c], scale);
   }
+}
+
+template <bool FWD, class E>
+int launch_axis_as(const double2 *in, double2 *out, long outer, int n, long inner, double scale, cudaStream_t stream) {
+  FftDesc d;
+  int st = get_fft(n, &d);
+  if (st) return st;
+  // Tile of up to 64 columns (a power of two dividing the 256 threads), limited
+  // by shared memory: one buffer of n x ncol elements (two with a generic radix).
+  const int bufs = d.has_generic ? 2 : 1;
+  const size_t budget = (size_t)std::min(max_smem_optin(), 200 * 1024);
+  int ncol = 64;
+  while (ncol > 1 && (size_t)bufs * n * ncol * sizeof(E) + ncol * sizeof(long) > budget) ncol /= 2;
+  const long ncols_total = outer * inner;
+  while (ncol > 8 && ncol / 2 >= ncols_total) ncol /= 2;
+  const size_t smem = (size_t)bufs * n * ncol * sizeof(E) + ncol * sizeof(long);
+  if (smem > budget) return set_error(TPRF_ERR_UNSUPPORTED_SIZE, "lattice FFT: mesh dimension too long for one CTA");
+  int lg = 0;
+  while ((1 << lg) < ncol) ++lg;
+  const long blocks = (ncols_total + ncol - 1) / ncol;
+  if (blocks > 0x7fffffffL) return set_error(TPRF_ERR_INVALID_ARGUMENT, "lattice FFT: too many tiles");
+  TPRF_CUDA(cudaFuncSetAttribute(lattice_axis_kernel<FWD, E>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  lattice_axis_kernel<FWD, E><<<(unsigned)blocks, 256, smem, stream>>>(in, out, ncols_total, inner, ncol, lg, d, scale);
+  TPRF_LAUNCH_CHECK("lattice_axis_kernel");
+  return TPRF_OK;
 }
 
 template <bool FWD>
 int launch_axis(const double2 *in, double2 *out, long outer, int n, long inner, double scale, cudaStream_t stream) {
-  FftDesc d;
-  int st = get_fft(n, &d);
-  if (st) return st;
-  // Tile of ~64 columns, limited by shared memory (two buffers of n x ncol).
-  const int budget = std::min(max_smem_optin(), 200 * 1024);
-  int max_cols = budget / (2 * n * (int)sizeof(double2));
-  if (max_cols < 1) return set_error(TPRF_ERR_UNSUPPORTED_SIZE, "lattice FFT: mesh dimension too long for one CTA");
-  int want = std::min(64, max_cols);
-  int ic, oc;
-  if (inner >= want) {
-    ic = want;
-    oc = 1;
-  } else {
-    ic = (int)inner;
-    oc = std::max(1, want / ic);
-    oc = (int)std::min<long>(oc, outer);
-  }
-  const size_t smem = 2ull * n * oc * ic * sizeof(double2);
-  const long n_ichunk = (inner + ic - 1) / ic;
-  const long n_ochunk = (outer + oc - 1) / oc;
-  const long blocks = n_ichunk * n_ochunk;
-  if (blocks > 0x7fffffffL) return set_error(TPRF_ERR_INVALID_ARGUMENT, "lattice FFT: too many tiles");
-  TPRF_CUDA(cudaFuncSetAttribute(lattice_axis_kernel<FWD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  lattice_axis_kernel<FWD><<<(unsigned)blocks, 256, smem, stream>>>(in, out, outer, inner, oc, ic, d, scale);
-  TPRF_LAUNCH_CHECK("lattice_axis_kernel");
-  return TPRF_OK;
+  if (arith_mode() == kArithFP64) return launch_axis_as<FWD, double2>(in, out, outer, n, inner, scale, stream);
+  return launch_axis_as<FWD, cdf>(in, out, outer, n, inner, scale, stream);
 }
 
 }  // namespace

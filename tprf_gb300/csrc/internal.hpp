@@ -45,8 +45,11 @@ constexpr int kMaxStages = 24;
 struct FftDesc {
   int n;
   int nst;
+  int has_generic;  // a stage with a prime radix > 7 (needs a second buffer)
   int radix[kMaxStages];
-  const double2 *tw;  // device
+  const double2 *tw;  // device, exp(-2 pi i t / n) in FP64
+  const float4 *twf;  // device, the same roots as double-float pairs (re.hi, re.lo, im.hi, im.lo)
+  const int *rev;     // device, position of natural index t in the digit-reversed input order
 };
 // Returns 0 or a status; fills *out. Cached per (device, n).
 int get_fft(int n, FftDesc *out);
@@ -63,6 +66,12 @@ struct NuTauPlan {
   const int *fit_row;    // [n_fit]: data index of each fit point
   const double2 *fitF;   // [n_mom][n_fit]: moments = F g
   const double2 *fitG;   // [n_fit][n_mom]: model value = sum_p c_p G[i][p]
+  // Tail model folded after the FFT (linear in the moments):
+  //   G(tau_t) = P[t] FFT(g)[t] + sum_j a_j Q[j][t],  P = phase / beta,
+  //   Q[j][t] = ftail[j][t] - P[t] FFT(den[j])[t].
+  const double2 *P, *Q;     // [L], [3][L]
+  const float4 *Pf, *Qf;    // the same as double-float pairs
+  const float4 *fitFf, *fitGf;
 };
 int get_nu_tau_plan(double beta, int n_iw, int n_tau, const NuTauPlan **out);
 
@@ -73,7 +82,16 @@ struct TauWPlan {
   FftDesc fft;
   const double *btail;   // [3][L]: oneBoson(1, b_j, tau_t), b = (-1/2, -1, 1)
   const double2 *den;    // [3][2 nw - 1]: 1/(i w_m - b_j)
+  // Tail model folded after the FFT: chi(i w_m) = (beta/L) FFT(chi)[k_m] + sum_j a_j K[j][m],
+  //   K[j][m] = den[j][m] - (beta/L) FFT(btail[j])[k_m],  k_m = (m + L) % L.
+  const double2 *K;      // [3][2 nw - 1]
+  const float4 *Kf;
 };
+
+// Element type used by the FFT stages: double-float on the FP32 pipe (default)
+// or native FP64.
+enum Arith : int { kArithDF64 = 0, kArithFP64 = 1 };
+int arith_mode();
 int get_tau_w_plan(double beta, int n_tau, int nw, const TauWPlan **out);
 
 // Exact inverse of the 8x8 Vandermonde V[m][j] = m^j (m = 1..8), uploaded to

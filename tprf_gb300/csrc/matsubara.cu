@@ -12,11 +12,17 @@
 //
 // Design: every transform works on "columns" (one (r, target element) pair
 // each; columns are contiguous in HBM), a tile of `ic` columns per CTA. The
-// whole tau or nu series of the tile sits in shared memory, the tail model is
-// fitted, subtracted and added back around a Stockham FFT in the same CTA, so
-// each transform reads its input once and writes its output once. The fused
-// bubble builds chi0(tau) for its columns directly in shared memory from
-// G(tau, r) and G(beta - tau, -r): chi0(tau, r) never reaches HBM.
+// whole tau or nu series of the tile sits in shared memory, the tail moments
+// are fitted in the same CTA and the Stockham FFT runs there, so each
+// transform reads its input once and writes its output once. The reference
+// subtracts the tail model before the FFT and adds it back after; because
+// that is linear in the moments, the per-pole parts are folded into tables
+// precomputed once per mesh and applied after the FFT (same result up to
+// rounding, and no per-element work before the FFT). The fused bubble builds
+// chi0(tau) for its columns directly in shared memory from G(tau, r) and
+// G(beta - tau, -r): chi0(tau, r) never reaches HBM. The FFT and the tail
+// arithmetic run in double-float pairs on the FP32 pipe by default
+// (tprf_set_arithmetic), with inputs and outputs in complex128.
 #include <algorithm>
 
 #include "common.cuh"
@@ -40,101 +46,110 @@ VinvRows make_vinv_rows() {
   return r;
 }
 
-__device__ __forceinline__ void fmax_shared(unsigned *slot, double v) {
-  // non-negative floats order like their bit patterns
-  atomicMax(slot, __float_as_uint((float)v));
+// element-type plumbing: double2 (FP64) or cdf (double-float)
+template <class C> __device__ __forceinline__ C from_d2(double2 z);
+template <> __device__ __forceinline__ double2 from_d2<double2>(double2 z) { return z; }
+template <> __device__ __forceinline__ cdf from_d2<cdf>(double2 z) { return to_cdf(z); }
+__device__ __forceinline__ double2 as_d2(double2 z) { return z; }
+__device__ __forceinline__ double2 as_d2(cdf z) { return to_double2(z); }
+template <class C> __device__ __forceinline__ C table(const double2 *d, const float4 *f, long i);
+template <> __device__ __forceinline__ double2 table<double2>(const double2 *d, const float4 *, long i) { return d[i]; }
+template <> __device__ __forceinline__ cdf table<cdf>(const double2 *, const float4 *f, long i) {
+  const float4 v = f[i];
+  return cdf{dfl{v.x, v.y}, dfl{v.z, v.w}};
+}
+template <class C> __device__ __forceinline__ typename RealT<C>::type real_of(double v);
+template <> __device__ __forceinline__ double real_of<double2>(double v) { return v; }
+template <> __device__ __forceinline__ dfl real_of<cdf>(double v) { return split_double(v); }
+__device__ __forceinline__ float cabsf_approx(double2 z) { return (float)sqrt(cabs2(z)); }
+__device__ __forceinline__ float cabsf_approx(cdf z) {
+  const float x = __fadd_rn(z.x.hi, z.x.lo), y = __fadd_rn(z.y.hi, z.y.lo);
+  return sqrtf(x * x + y * y);
 }
 
 // ---------------------------------------------------------------------------
-// iv -> tau
+// iv -> tau. The tail model enters after the FFT through the folded tables
+// (exactly the reference's model subtracted before and added after the FFT,
+// by linearity): G(tau_t) = P[t] FFT(g)[t] + sum_j a_j Q[j][t].
 
+template <class C>
 __global__ void __launch_bounds__(512) nu_to_tau_kernel(NuTauPlan p, const double2 *__restrict__ gw,
                                                         const double2 *__restrict__ mom, double2 *__restrict__ gt,
-                                                        long C, int ic, unsigned *status) {
-  extern __shared__ double2 smem[];
+                                                        long Ccols, int ic, int lg, unsigned *status) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ unsigned s_res;
+  C *a = reinterpret_cast<C *>(smem_raw);
   const int L = p.L, n_iw = p.n_iw, nnu = 2 * p.n_iw;
-  double2 *a = smem;
-  double2 *b = a + (size_t)L * ic;
-  double2 *coef = b + (size_t)L * ic;  // [n_mom][ic]
-  double2 *am = coef + 10 * ic;        // [4][ic]: a1, a2, a3, m1
+  const int *rev = p.fft.rev;
+  C *b = p.fft.has_generic ? a + (size_t)L * ic : nullptr;
+  C *coef = a + (size_t)(p.fft.has_generic ? 2 : 1) * L * ic;  // [n_mom <= 10][ic]
+  C *am = coef + 10 * ic;                                       // [4][ic]: a1, a2, a3, m1
   const int tid = threadIdx.x, nthr = blockDim.x;
   const long col0 = blockIdx.x * (long)ic;
-  const int ncol = (int)min((long)ic, C - col0);
+  const int ncol = (int)min((long)ic, Ccols - col0);
 
-  for (int w = tid; w < L * ic; w += nthr) a[w] = make_double2(0.0, 0.0);
+  for (int w = tid; w < L * ic; w += nthr) a[w] = czero<C>();
   if (tid == 0) s_res = 0u;
   __syncthreads();
+  // frequency n sits at FFT row (n + L) % L, stored at its digit-reversed position
   for (int w = tid; w < nnu * ic; w += nthr) {
-    const int c = w % ic, n = w / ic;
-    if (c < ncol) a[((n - n_iw + L) % L) * ic + c] = gw[(long)n * C + col0 + c];
+    const int c = w & (ic - 1), n = w >> lg;
+    if (c < ncol) a[rev[(n - n_iw + L) % L] * ic + c] = from_d2<C>(gw[(long)n * Ccols + col0 + c]);
   }
   __syncthreads();
   if (mom == nullptr) {
     const int nf = p.n_fit, nm = p.n_mom;
     for (int w = tid; w < nm * ic; w += nthr) {
-      const int c = w % ic, q = w / ic;
-      double2 acc = make_double2(0.0, 0.0);
+      const int c = w & (ic - 1), q = w >> lg;
+      C acc = czero<C>();
       for (int i = 0; i < nf; ++i) {
-        const int row = (p.fit_row[i] - n_iw + L) % L;
-        acc = cfma(p.fitF[q * nf + i], a[row * ic + c], acc);
+        const int row = rev[(p.fit_row[i] - n_iw + L) % L];
+        acc = cadd(acc, cmul(table<C>(p.fitF, p.fitFf, q * nf + i), a[row * ic + c]));
       }
       coef[q * ic + c] = acc;
     }
     __syncthreads();
     for (int w = tid; w < nf * ic; w += nthr) {
-      const int c = w % ic, i = w / ic;
+      const int c = w & (ic - 1), i = w >> lg;
       if (c >= ncol) continue;
-      double2 model = make_double2(0.0, 0.0);
-      for (int q = 0; q < nm; ++q) model = cfma(p.fitG[i * nm + q], coef[q * ic + c], model);
-      const int row = (p.fit_row[i] - n_iw + L) % L;
-      const double2 d = csub(model, a[row * ic + c]);
-      fmax_shared(&s_res, sqrt(cabs2(d)));
+      C model = czero<C>();
+      for (int q = 0; q < nm; ++q) model = cadd(model, cmul(table<C>(p.fitG, p.fitGf, i * nm + q), coef[q * ic + c]));
+      const int row = rev[(p.fit_row[i] - n_iw + L) % L];
+      atomicMax(&s_res, __float_as_uint(cabsf_approx(csub(model, a[row * ic + c]))));
     }
     for (int c = tid; c < ic; c += nthr) {
-      const double2 m1 = coef[1 * ic + c], m2 = coef[2 * ic + c], m3 = coef[3 * ic + c];
+      const C m1 = coef[1 * ic + c], m2 = coef[2 * ic + c], m3 = coef[3 * ic + c];
       am[0 * ic + c] = csub(m1, m3);
-      am[1 * ic + c] = cscale(cadd(m2, m3), 0.5);
-      am[2 * ic + c] = cscale(csub(m3, m2), 0.5);
+      am[1 * ic + c] = cscale(cadd(m2, m3), kc<C>(0.5));
+      am[2 * ic + c] = cscale(csub(m3, m2), kc<C>(0.5));
       am[3 * ic + c] = m1;
     }
   } else {
     for (int c = tid; c < ic; c += nthr) {
       double2 m1 = make_double2(0.0, 0.0), m2 = m1, m3 = m1;
       if (c < ncol) {
-        m1 = mom[0 * C + col0 + c];
-        m2 = mom[1 * C + col0 + c];
-        m3 = mom[2 * C + col0 + c];
+        m1 = mom[0 * Ccols + col0 + c];
+        m2 = mom[1 * Ccols + col0 + c];
+        m3 = mom[2 * Ccols + col0 + c];
       }
-      am[0 * ic + c] = csub(m1, m3);
-      am[1 * ic + c] = cscale(cadd(m2, m3), 0.5);
-      am[2 * ic + c] = cscale(csub(m3, m2), 0.5);
-      am[3 * ic + c] = m1;
+      am[0 * ic + c] = from_d2<C>(csub(m1, m3));
+      am[1 * ic + c] = from_d2<C>(cscale(cadd(m2, m3), 0.5));
+      am[2 * ic + c] = from_d2<C>(cscale(csub(m3, m2), 0.5));
+      am[3 * ic + c] = from_d2<C>(m1);
     }
   }
   __syncthreads();
   if (tid == 0 && __uint_as_float(s_res) > 1e-3f) atomicOr(status, kDevErrTailFit);
-  const double inv_beta = 1.0 / p.beta;
-  for (int w = tid; w < nnu * ic; w += nthr) {
-    const int c = w % ic, n = w / ic;
-    const int j = (n - n_iw + L) % L;
-    double2 model = cmul(am[0 * ic + c], p.den[0 * nnu + n]);
-    model = cfma(am[1 * ic + c], p.den[1 * nnu + n], model);
-    model = cfma(am[2 * ic + c], p.den[2 * nnu + n], model);
-    a[j * ic + c] = cscale(csub(a[j * ic + c], model), inv_beta);
-  }
-  double2 *r = fft_smem<true>(a, b, p.fft, ic);
+  C *r = fft_smem<true>(a, b, p.fft, ic);
   for (int w = tid; w < (L + 1) * ic; w += nthr) {
-    const int c = w % ic, t = w / ic;
+    const int c = w & (ic - 1), t = w >> lg;
     if (c >= ncol) continue;
     const int tt = (t < L) ? t : 0;
-    double2 v = cmul(r[tt * ic + c], p.phase[tt]);
-    double2 model = cscale(am[0 * ic + c], p.ftail[0 * L + tt]);
-    model = cadd(model, cscale(am[1 * ic + c], p.ftail[1 * L + tt]));
-    model = cadd(model, cscale(am[2 * ic + c], p.ftail[2 * L + tt]));
-    v = cadd(v, model);
-    if (t == L) v = make_double2(-(v.x + am[3 * ic + c].x), -(v.y + am[3 * ic + c].y));
-    gt[(long)t * C + col0 + c] = v;
+    C v = cmul(table<C>(p.P, p.Pf, tt), r[tt * ic + c]);
+#pragma unroll
+    for (int j = 0; j < 3; ++j) v = cadd(v, cmul(am[j * ic + c], table<C>(p.Q, p.Qf, (long)j * L + tt)));
+    if (t == L) v = csub(czero<C>(), cadd(v, am[3 * ic + c]));  // G[L] = -(G[0] + m1)
+    gt[(long)t * Ccols + col0 + c] = as_d2(v);
   }
 }
 
@@ -145,6 +160,11 @@ struct ArrayLoader {  // chi(tau, col) stored as [n_tau][C]
   const double2 *x;
   long C;
   __device__ __forceinline__ double2 operator()(int t, long col) const { return x[(long)t * C + col]; }
+  __device__ __forceinline__ void setup(long, int, int, long *) const {}
+  template <class E>
+  __device__ __forceinline__ E get(int t, int c, long col0, int, const long *) const {
+    return from_d2<E>(x[(long)t * C + col0 + c]);
+  }
 };
 
 struct BubbleLoader {  // chi0 columns computed from G(tau, r): col = r * nb^4 + abcd
@@ -152,7 +172,8 @@ struct BubbleLoader {  // chi0 columns computed from G(tau, r): col = r * nb^4 +
   long Nr;
   int nb, n_tau;
   int d0, d1, d2;
-  __device__ __forceinline__ double2 operator()(int t, long col) const {
+  // offsets of G_da(., r) and G_bc(., -r) within one tau slice of G
+  __device__ __forceinline__ void offsets(long col, long &ox, long &oy) const {
     const int nb2 = nb * nb, nb4 = nb2 * nb2;
     const long r = col / nb4;
     int e = (int)(col - r * nb4);
@@ -166,45 +187,71 @@ struct BubbleLoader {  // chi0 columns computed from G(tau, r): col = r * nb^4 +
     const int i1 = (int)((r / d2) % d1);
     const int i0 = (int)(r / ((long)d2 * d1));
     const long mr = ((long)((d0 - i0) % d0) * d1 + (d1 - i1) % d1) * d2 + (d2 - i2) % d2;
-    const double2 x = g[((long)t * Nr + r) * nb2 + d * nb + a];
-    const double2 y = g[((long)(n_tau - 1 - t) * Nr + mr) * nb2 + b * nb + c];
-    return cmul(x, y);
+    ox = r * nb2 + d * nb + a;
+    oy = mr * nb2 + b * nb + c;
+  }
+  __device__ __forceinline__ double2 operator()(int t, long col) const {
+    long ox, oy;
+    offsets(col, ox, oy);
+    const long slice = Nr * nb * nb;
+    return cmul(g[(long)t * slice + ox], g[(long)(n_tau - 1 - t) * slice + oy]);
+  }
+  // per CTA: the two offsets of each of its ic columns, once
+  __device__ __forceinline__ void setup(long col0, int ic, int ncol, long *s) const {
+    for (int c = threadIdx.x; c < ic; c += blockDim.x) {
+      long ox = 0, oy = 0;
+      if (c < ncol) offsets(col0 + c, ox, oy);
+      s[c] = ox;
+      s[ic + c] = oy;
+    }
+  }
+  template <class E>
+  __device__ __forceinline__ E get(int t, int c, long, int ic, const long *s) const {
+    const long slice = Nr * nb * nb;
+    return cmul(from_d2<E>(g[(long)t * slice + s[c]]), from_d2<E>(g[(long)(n_tau - 1 - t) * slice + s[ic + c]]));
   }
 };
 
-template <class Loader>
+// tau -> i omega. fit_derivatives moments in FP64 from the end rows; the tail
+// model enters after the FFT: chi(i w_m) = (beta/L) FFT(chi)[k_m] + sum_j a_j K[j][m].
+template <class Loader, class C>
 __global__ void __launch_bounds__(512) tau_to_w_kernel(TauWPlan p, Loader ld, VinvRows vr, double2 *__restrict__ out,
-                                                       long C, int ic) {
-  extern __shared__ double2 smem[];
+                                                       long Ccols, int ic, int lg) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C *a = reinterpret_cast<C *>(smem_raw);
   const int L = p.L, nw = p.nw, nwt = 2 * p.nw - 1;
-  double2 *a = smem;
-  double2 *b = a + (size_t)L * ic;
-  double2 *last = b + (size_t)L * ic;  // [ic] row L
-  double2 *am = last + ic;             // [3][ic]
+  const int *rev = p.fft.rev;
+  C *b = p.fft.has_generic ? a + (size_t)L * ic : nullptr;
+  C *last = a + (size_t)(p.fft.has_generic ? 2 : 1) * L * ic;  // [ic] row L
+  C *am = last + ic;                                            // [3][ic]
+  long *soff = reinterpret_cast<long *>(am + 3 * ic);           // [2][ic] loader offsets
   const int tid = threadIdx.x, nthr = blockDim.x;
   const long col0 = blockIdx.x * (long)ic;
-  const int ncol = (int)min((long)ic, C - col0);
+  const int ncol = (int)min((long)ic, Ccols - col0);
+  ld.setup(col0, ic, ncol, soff);
+  __syncthreads();
+  // rows t < L go to their digit-reversed FFT positions, row L aside
   for (int w = tid; w < (L + 1) * ic; w += nthr) {
-    const int c = w % ic, t = w / ic;
-    double2 v = make_double2(0.0, 0.0);
-    if (c < ncol) v = ld(t, col0 + c);
+    const int c = w & (ic - 1), t = w >> lg;
+    C v = czero<C>();
+    if (c < ncol) v = ld.template get<C>(t, c, col0, ic, soff);
     if (t < L)
-      a[t * ic + c] = v;
+      a[rev[t] * ic + c] = v;
     else
       last[c] = v;
   }
   __syncthreads();
   const double dtau = p.beta / (double)(p.n_tau - 1);
   for (int c = tid; c < ic; c += nthr) {
-    const double2 g0 = a[c], gL = last[c];
+    const double2 g0 = as_d2(a[rev[0] * ic + c]), gL = as_d2(last[c]);
     double2 gl0 = make_double2(0.0, 0.0), gl1 = gl0, gr0 = gl0, gr1 = gl0;
 #pragma unroll
     for (int m = 0; m < 8; ++m) {
       const double tau_m = (double)(m + 1) * dtau;
       const int rl = m + 1, rr = L - 1 - m;
-      const double2 xl = (rl < L) ? a[rl * ic + c] : gL;
+      const double2 xl = (rl < L) ? as_d2(a[rev[rl] * ic + c]) : gL;
       const double2 dl = make_double2((xl.x - g0.x) / tau_m, (xl.y - g0.y) / tau_m);
-      const double2 xr = a[rr * ic + c];
+      const double2 xr = as_d2(a[rev[rr] * ic + c]);
       const double2 dr = make_double2((gL.x - xr.x) / tau_m, (gL.y - xr.y) / tau_m);
       gl0 = make_double2(fma(vr.r0[m], dl.x, gl0.x), fma(vr.r0[m], dl.y, gl0.y));
       gl1 = make_double2(fma(vr.r1[m], dl.x, gl1.x), fma(vr.r1[m], dl.y, gl1.y));
@@ -212,31 +259,22 @@ __global__ void __launch_bounds__(512) tau_to_w_kernel(TauWPlan p, Loader ld, Vi
       gr1 = make_double2(fma(vr.r1[m], dr.x, gr1.x), fma(vr.r1[m], dr.y, gr1.y));
     }
     const double2 m1 = make_double2(-(g0.x - gL.x), -(g0.y - gL.y));
-    const double2 m2 = csub(gl0, gr0);                                  // sign = +1 (boson)
+    const double2 m2 = csub(gl0, gr0);  // sign = +1 (boson)
     const double2 m3 = cscale(cadd(gl1, gr1), -2.0 / dtau);
-    am[0 * ic + c] = cscale(csub(m1, m3), 4.0 / 3.0);
-    am[1 * ic + c] = csub(m3, cscale(cadd(m1, m2), 0.5));
-    am[2 * ic + c] = cadd(cadd(cscale(m1, 1.0 / 6.0), cscale(m2, 0.5)), cscale(m3, 1.0 / 3.0));
+    am[0 * ic + c] = from_d2<C>(cscale(csub(m1, m3), 4.0 / 3.0));
+    am[1 * ic + c] = from_d2<C>(csub(m3, cscale(cadd(m1, m2), 0.5)));
+    am[2 * ic + c] = from_d2<C>(cadd(cadd(cscale(m1, 1.0 / 6.0), cscale(m2, 0.5)), cscale(m3, 1.0 / 3.0)));
   }
-  __syncthreads();
-  const double fact = p.beta / (double)L;
-  for (int w = tid; w < L * ic; w += nthr) {
-    const int c = w % ic, t = w / ic;
-    double2 model = cscale(am[0 * ic + c], p.btail[0 * L + t]);
-    model = cadd(model, cscale(am[1 * ic + c], p.btail[1 * L + t]));
-    model = cadd(model, cscale(am[2 * ic + c], p.btail[2 * L + t]));
-    a[t * ic + c] = cscale(csub(a[t * ic + c], model), fact);
-  }
-  double2 *r = fft_smem<false>(a, b, p.fft, ic);
+  C *r = fft_smem<false>(a, b, p.fft, ic);
+  const auto fact = real_of<C>(p.beta / (double)L);
   for (int w = tid; w < nwt * ic; w += nthr) {
-    const int c = w % ic, mi = w / ic;
+    const int c = w & (ic - 1), mi = w >> lg;
     if (c >= ncol) continue;
     const int m = mi - (nw - 1);
-    double2 v = r[((m + L) % L) * ic + c];
-    v = cfma(am[0 * ic + c], p.den[0 * nwt + mi], v);
-    v = cfma(am[1 * ic + c], p.den[1 * nwt + mi], v);
-    v = cfma(am[2 * ic + c], p.den[2 * nwt + mi], v);
-    out[(long)mi * C + col0 + c] = v;
+    C v = cscale(r[((m + L) % L) * ic + c], fact);
+#pragma unroll
+    for (int j = 0; j < 3; ++j) v = cadd(v, cmul(am[j * ic + c], table<C>(p.K, p.Kf, (long)j * nwt + mi)));
+    out[(long)mi * Ccols + col0 + c] = as_d2(v);
   }
 }
 
@@ -260,14 +298,22 @@ __global__ void __launch_bounds__(256) bubble_kernel(BubbleLoader ld, double2 *_
   }
 }
 
-int pick_ic(int L, size_t extra_per_col, int *ic_out, size_t *smem_out) {
+// Columns per CTA: a power of two (dividing the 512 threads) such that one
+// length-L buffer (two when the FFT has a generic-radix stage) plus the
+// per-column extras fit in shared memory.
+int pick_ic(const FftDesc &fft, size_t extra_per_col, int *ic_out, int *lg_out, size_t *smem_out) {
   const size_t budget = (size_t)std::min(max_smem_optin(), 220 * 1024);
+  const size_t bufs = fft.has_generic ? 2 : 1;
+  const size_t L = fft.n;
   int ic = 32;
-  while (ic > 1 && (2ull * L * ic * sizeof(double2) + extra_per_col * ic) > budget) ic /= 2;
-  const size_t smem = 2ull * L * ic * sizeof(double2) + extra_per_col * ic;
+  while (ic > 1 && (bufs * L * ic * sizeof(double2) + extra_per_col * ic) > budget) ic /= 2;
+  const size_t smem = bufs * L * ic * sizeof(double2) + extra_per_col * ic;
   if (smem > budget)
-    return set_error(TPRF_ERR_UNSUPPORTED_SIZE, "Matsubara FFT: time mesh too long for one CTA (n_tau > ~6900)");
+    return set_error(TPRF_ERR_UNSUPPORTED_SIZE, "Matsubara FFT: time mesh too long for one CTA");
+  int lg = 0;
+  while ((1 << lg) < ic) ++lg;
   *ic_out = ic;
+  *lg_out = lg;
   *smem_out = smem;
   return TPRF_OK;
 }
@@ -278,17 +324,23 @@ long grid_for(long work, int threads) {
   return std::max(1L, std::min(blocks, cap));
 }
 
-template <class Loader>
-int launch_tau_to_w_with(const TauWPlan *p, Loader ld, double2 *out, long C, cudaStream_t stream) {
-  int ic;
+template <class Loader, class E>
+int launch_tau_to_w_as(const TauWPlan *p, Loader ld, double2 *out, long C, cudaStream_t stream) {
+  int ic, lg;
   size_t smem;
-  int st = pick_ic(p->L, 4 * sizeof(double2), &ic, &smem);
+  int st = pick_ic(p->fft, 4 * sizeof(double2) + 2 * sizeof(long), &ic, &lg, &smem);
   if (st) return st;
-  TPRF_CUDA(cudaFuncSetAttribute(tau_to_w_kernel<Loader>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  TPRF_CUDA(cudaFuncSetAttribute(tau_to_w_kernel<Loader, E>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const long blocks = (C + ic - 1) / ic;
-  tau_to_w_kernel<Loader><<<(unsigned)blocks, 512, smem, stream>>>(*p, ld, make_vinv_rows(), out, C, ic);
+  tau_to_w_kernel<Loader, E><<<(unsigned)blocks, 512, smem, stream>>>(*p, ld, make_vinv_rows(), out, C, ic, lg);
   TPRF_LAUNCH_CHECK("tau_to_w_kernel");
   return TPRF_OK;
+}
+
+template <class Loader>
+int launch_tau_to_w_with(const TauWPlan *p, Loader ld, double2 *out, long C, cudaStream_t stream) {
+  if (arith_mode() == kArithFP64) return launch_tau_to_w_as<Loader, double2>(p, ld, out, C, stream);
+  return launch_tau_to_w_as<Loader, cdf>(p, ld, out, C, stream);
 }
 
 int check_tau_w(double beta, int n_tau, int nw) {
@@ -339,13 +391,18 @@ int launch_nu_to_tau(double beta, int n_iw, int n_tau, long C, const double2 *gw
     return set_error(TPRF_ERR_TAIL_FIT, "Inverse Fourier requires at least a proper 3rd high-frequency moment");
   unsigned *status = device_status_word();
   if (!status) return TPRF_ERR_CUDA;
-  int ic;
+  int ic, lg;
   size_t smem;
-  st = pick_ic(p->L, 14 * sizeof(double2), &ic, &smem);
+  st = pick_ic(p->fft, 14 * sizeof(double2), &ic, &lg, &smem);
   if (st) return st;
-  TPRF_CUDA(cudaFuncSetAttribute(nu_to_tau_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const long blocks = (C + ic - 1) / ic;
-  nu_to_tau_kernel<<<(unsigned)blocks, 512, smem, stream>>>(*p, gw, mom, gt, C, ic, status);
+  if (arith_mode() == kArithFP64) {
+    TPRF_CUDA(cudaFuncSetAttribute(nu_to_tau_kernel<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    nu_to_tau_kernel<double2><<<(unsigned)blocks, 512, smem, stream>>>(*p, gw, mom, gt, C, ic, lg, status);
+  } else {
+    TPRF_CUDA(cudaFuncSetAttribute(nu_to_tau_kernel<cdf>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    nu_to_tau_kernel<cdf><<<(unsigned)blocks, 512, smem, stream>>>(*p, gw, mom, gt, C, ic, lg, status);
+  }
   TPRF_LAUNCH_CHECK("nu_to_tau_kernel");
   return TPRF_OK;
 }

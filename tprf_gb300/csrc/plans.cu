@@ -20,6 +20,7 @@ namespace tprf {
 namespace {
 thread_local std::string g_last_error;
 std::atomic<bool> g_sync_checks{true};
+std::atomic<int> g_arith{kArithDF64};
 std::mutex g_mutex;
 
 using cd = std::complex<double>;
@@ -48,6 +49,27 @@ int current_device(int *dev) {
 
 double2 to_d2(cd z) { return make_double2(z.real(), z.imag()); }
 
+float4 to_df(cd z) {
+  const float rh = (float)z.real(), ih = (float)z.imag();
+  return make_float4(rh, (float)(z.real() - (double)rh), ih, (float)(z.imag() - (double)ih));
+}
+
+std::vector<float4> to_df(const std::vector<double2> &v) {
+  std::vector<float4> out(v.size());
+  for (size_t i = 0; i < v.size(); ++i) out[i] = to_df(cd(v[i].x, v[i].y));
+  return out;
+}
+
+// exp(sign 2 pi i k / L) for k < L, with the angle reduced exactly
+std::vector<cd> unit_roots(int L, double sign) {
+  std::vector<cd> w(L);
+  for (int k = 0; k < L; ++k) {
+    const double a = sign * 2.0 * M_PI * (double)k / (double)L;
+    w[k] = cd(std::cos(a), std::sin(a));
+  }
+  return w;
+}
+
 }  // namespace
 
 int set_error(int status, const std::string &msg) {
@@ -60,6 +82,8 @@ int cuda_status(cudaError_t e, const char *what) {
 }
 
 bool sync_checks_enabled() { return g_sync_checks.load(); }
+
+int arith_mode() { return g_arith.load(); }
 
 unsigned *device_status_word() {
   static std::map<int, unsigned *> words;
@@ -164,7 +188,34 @@ int get_fft(int n, FftDesc *out) {
     const double a = -2.0 * M_PI * (double)t / (double)n;
     tw[t] = make_double2(std::cos(a), std::sin(a));
   }
+  std::vector<float4> twf(n);
+  for (int t = 0; t < n; ++t) {
+    const float rh = (float)tw[t].x, ih = (float)tw[t].y;
+    twf[t] = make_float4(rh, (float)(tw[t].x - (double)rh), ih, (float)(tw[t].y - (double)ih));
+  }
+  // digit reversal for the in-place decimation-in-time stages: position
+  // p = p_0 + R_0 p_1 + R_0 R_1 p_2 + ... holds natural index
+  // sigma(p) = sum_k p_k n / (R_0 ... R_k); rev is its inverse.
+  std::vector<int> rev(n);
+  for (int p = 0; p < n; ++p) {
+    long q = p, prod = 1, sig = 0;
+    for (int s = 0; s < d.nst; ++s) {
+      const int R = d.radix[s];
+      const long dg = q % R;
+      q /= R;
+      prod *= R;
+      sig += dg * (n / prod);
+    }
+    rev[sig] = p;
+  }
+  d.has_generic = 0;
+  for (int s = 0; s < d.nst; ++s)
+    if (d.radix[s] > 8 || d.radix[s] == 6) d.has_generic = 1;
   st = upload(tw, &d.tw);
+  if (st) return st;
+  st = upload(twf, &d.twf);
+  if (st) return st;
+  st = upload(rev, &d.rev);
   if (st) return st;
   cache[key] = d;
   *out = d;
@@ -343,8 +394,25 @@ int get_nu_tau_plan(double beta, int n_iw, int n_tau, const NuTauPlan **out) {
   const int n_fit = (int)rows.size();
   p->n_fit = n_fit;
   p->n_mom = n_mom;
+  // folded tail tables: FFT_FORWARD of each pole column, placed at rows (n+L)%L
+  const std::vector<cd> wr = unit_roots(L, -1.0);
+  std::vector<double2> P(L), Q(3 * L);
+  for (int t = 0; t < L; ++t) {
+    const cd Pt = cd(phase[t].x, phase[t].y) / beta;
+    P[t] = to_d2(Pt);
+    for (int j = 0; j < 3; ++j) {
+      cd acc = 0.0;
+      for (int n = 0; n < nnu; ++n) {
+        const long row = ((long)(n - n_iw) + L) % L;
+        acc += cd(den[j * nnu + n].x, den[j * nnu + n].y) * wr[(row * t) % L];
+      }
+      Q[j * L + t] = to_d2(ftail[j * L + t] - Pt * acc);
+    }
+  }
   if ((st = upload(den, &p->den)) || (st = upload(phase, &p->phase)) || (st = upload(ftail, &p->ftail)) ||
-      (st = upload(rows, &p->fit_row)) || (st = upload(F, &p->fitF)) || (st = upload(G, &p->fitG)))
+      (st = upload(rows, &p->fit_row)) || (st = upload(F, &p->fitF)) || (st = upload(G, &p->fitG)) ||
+      (st = upload(P, &p->P)) || (st = upload(Q, &p->Q)) || (st = upload(to_df(P), &p->Pf)) ||
+      (st = upload(to_df(Q), &p->Qf)) || (st = upload(to_df(F), &p->fitFf)) || (st = upload(to_df(G), &p->fitGf)))
     return st;
   std::lock_guard<std::mutex> lock(g_mutex);
   auto &slot = cache[key];
@@ -388,7 +456,20 @@ int get_tau_w_plan(double beta, int n_tau, int nw, const TauWPlan **out) {
       const cd iw(0.0, 2.0 * (m - (nw - 1)) * M_PI / beta);
       den[j * nwt + m] = to_d2(1.0 / (iw - bj[j]));
     }
-  if ((st = upload(btail, &p->btail)) || (st = upload(den, &p->den))) return st;
+  // folded tail tables: FFT_BACKWARD of each one-pole tau function, at the output rows
+  const std::vector<cd> wb = unit_roots(L, +1.0);
+  const double fact = beta / (double)L;
+  std::vector<double2> K(3 * nwt);
+  for (int j = 0; j < 3; ++j)
+    for (int m = 0; m < nwt; ++m) {
+      const long k = ((long)(m - (nw - 1)) + L) % L;
+      cd acc = 0.0;
+      for (int t = 0; t < L; ++t) acc += btail[j * L + t] * wb[(k * t) % L];
+      K[j * nwt + m] = to_d2(cd(den[j * nwt + m].x, den[j * nwt + m].y) - fact * acc);
+    }
+  if ((st = upload(btail, &p->btail)) || (st = upload(den, &p->den)) || (st = upload(K, &p->K)) ||
+      (st = upload(to_df(K), &p->Kf)))
+    return st;
   std::lock_guard<std::mutex> lock(g_mutex);
   auto &slot = cache[key];
   if (!slot) slot = std::move(p);
@@ -441,6 +522,15 @@ extern "C" const char *tprf_last_error(void) { return tprf::g_last_error.c_str()
 extern "C" const char *tprf_version(void) { return "0.1.0"; }
 
 extern "C" void tprf_set_sync_checks(int on) { tprf::g_sync_checks.store(on != 0); }
+
+extern "C" int tprf_set_arithmetic(int mode) {
+  if (mode != TPRF_ARITH_DF64 && mode != TPRF_ARITH_FP64)
+    return tprf::set_error(TPRF_ERR_INVALID_ARGUMENT, "set_arithmetic: mode must be TPRF_ARITH_DF64 or TPRF_ARITH_FP64");
+  tprf::g_arith.store(mode);
+  return TPRF_OK;
+}
+
+extern "C" int tprf_get_arithmetic(void) { return tprf::g_arith.load(); }
 
 extern "C" int tprf_check_device_status(void *stream) {
   unsigned f = 0;

@@ -7,10 +7,14 @@
 // solved without forming the inverse: A = I - chi0 U, then Gaussian
 // elimination with partial pivoting on [A | chi0] and back substitution.
 //
-// Design: one thread per point; the grouped U is shared by the CTA in shared
-// memory; each thread's A and right-hand sides live in shared memory laid out
-// [element][thread], so every access is conflict-free although each thread
-// pivots independently. All loops are unrolled for the compile-time size.
+// Design: one thread per point. A = I - chi0 U is formed from the non-zeros of
+// U only (compacted once per CTA into shared memory), LU-factorised with
+// partial pivoting in the thread's slice of shared memory ([element][thread]
+// layout: conflict-free although every thread pivots independently), and the
+// nb^2 right-hand sides (columns of chi0, re-read from L1/L2 through the row
+// permutation) are solved one at a time in registers. Keeping only the LU
+// factors in shared memory halves the per-thread footprint of a full
+// [A | chi0] elimination, which doubles the warps per SM.
 #include <algorithm>
 
 #include "common.cuh"
@@ -24,126 +28,142 @@ __device__ __forceinline__ int colmap(int c) {  // grouped column (d, c') -> off
 }
 
 template <int NB, int NT>
-__global__ void __launch_bounds__(NT) rpa_kernel(long n_points, const double2 *chi0,
-                                                 const double2 *__restrict__ U, double2 *chi,
-                                                 unsigned *status) {
+__global__ void __launch_bounds__(NT) rpa_lu_kernel(long n_points, const double2 *chi0, const double2 *__restrict__ U,
+                                                    double2 *chi, unsigned *status) {
   constexpr int N = NB * NB;
-  constexpr int UNR = (N <= 9) ? 32 : 1;  // full unroll only for the small systems
   extern __shared__ double2 smem[];
-  double2 *Ug = smem;  // [N][N], shared by the CTA
-  // Per-thread systems, [element][thread], real and imaginary planes. Declared
-  // volatile so each access is a real shared-memory access: without it the
-  // compiler may keep a thread's private rows in registers and spill them.
-  volatile double *ws = reinterpret_cast<volatile double *>(smem + N * N);
-  const int tid = threadIdx.x;
-  volatile double *Ar = ws + tid;
-  volatile double *Ai = Ar + (size_t)N * N * NT;
-  volatile double *Br = Ai + (size_t)N * N * NT;
-  volatile double *Bi = Br + (size_t)N * N * NT;
-  for (int w = tid; w < N * N; w += NT) {
-    const int m = w / N, c = w % N;
-    Ug[w] = U[m * N + colmap<NB>(c)];
-  }
-  __syncthreads();
-#define AOFF(i, j) (((i) * N + (j)) * NT)
-#define LDA(i, j) make_double2(Ar[AOFF(i, j)], Ai[AOFF(i, j)])
-#define LDB(i, j) make_double2(Br[AOFF(i, j)], Bi[AOFF(i, j)])
-#define STA(i, j, v) (Ar[AOFF(i, j)] = (v).x, Ai[AOFF(i, j)] = (v).y)
-#define STB(i, j, v) (Br[AOFF(i, j)] = (v).x, Bi[AOFF(i, j)] = (v).y)
-  for (long base = blockIdx.x * (long)NT; base < n_points; base += (long)gridDim.x * NT) {
-    const long pt = base + tid;
-    if (pt < n_points) {
-      const double2 *x = chi0 + pt * N * N;
-#pragma unroll UNR
-      for (int r = 0; r < N; ++r)
-#pragma unroll
-        for (int c = 0; c < N; ++c) STB(r, c, x[r * N + colmap<NB>(c)]);
-      // A = I - chi0 U
-#pragma unroll UNR
-      for (int r = 0; r < N; ++r) {
-#pragma unroll UNR
-        for (int c = 0; c < N; ++c) {
-          double2 s = make_double2(r == c ? 1.0 : 0.0, 0.0);
-#pragma unroll
-          for (int m = 0; m < N; ++m) s = cfms(LDB(r, m), Ug[m * N + c], s);
-          STA(r, c, s);
+  double2 *s_val = smem;                                     // [nnz] non-zeros of the grouped U
+  double2 *A = smem + N * N + threadIdx.x;                   // per thread LU, [N*N][NT]
+  int *s_off = reinterpret_cast<int *>(smem + N * N + (size_t)N * N * NT);  // [nnz]
+  int *s_cs = s_off + N * N;                                 // [N + 1] column starts
+  int *perm = s_cs + N + 1 + threadIdx.x;                    // per thread row permutation, [N][NT]
+  // Sparse form of the grouped vertex Ug[m][c] = U[m][colmap(c)], column by
+  // column: entry t of column c has grouped row m_t, kept as the offset
+  // colmap(m_t) into a chi0 row. Exact zeros are dropped (the Kanamori vertex
+  // keeps 21 of 81 entries for nb = 3). One thread builds it; it is tiny.
+  if (threadIdx.x == 0) {
+    int t = 0;
+    for (int c = 0; c < N; ++c) {
+      s_cs[c] = t;
+      for (int m = 0; m < N; ++m) {
+        const double2 u = U[m * N + colmap<NB>(c)];
+        if (u.x != 0.0 || u.y != 0.0) {
+          s_off[t] = colmap<NB>(m);
+          s_val[t] = u;
+          ++t;
         }
       }
-      bool singular = false;
-#pragma unroll UNR
-      for (int j = 0; j < N; ++j) {
-        int p = j;
-        double best = cabs2(LDA(j, j));
-#pragma unroll UNR
-        for (int i = j + 1; i < N; ++i) {
-          const double v = cabs2(LDA(i, j));
+    }
+    s_cs[N] = t;
+  }
+  __syncthreads();
+#define AE(i, k) A[((i) * N + (k)) * NT]
+  for (long base = blockIdx.x * (long)NT; base < n_points; base += (long)gridDim.x * NT) {
+    const long pt = base + threadIdx.x;
+    if (pt >= n_points) continue;
+    const double2 *x = chi0 + pt * N * N;
+    // A = I - chi0 U over the non-zeros of U
+#pragma unroll
+    for (int r = 0; r < N; ++r) {
+#pragma unroll
+      for (int c = 0; c < N; ++c) {
+        double2 s = make_double2(r == c ? 1.0 : 0.0, 0.0);
+        for (int t = s_cs[c]; t < s_cs[c + 1]; ++t) s = cfms(x[r * N + s_off[t]], s_val[t], s);
+        AE(r, c) = s;
+      }
+      perm[r * NT] = r;
+    }
+    // LU with partial pivoting; the step loop stays rolled so that the factors
+    // live in shared memory, not in registers.
+    bool singular = false;
+#pragma unroll 1
+    for (int j = 0; j < N; ++j) {
+      int p = j;
+      double best = cabs2(AE(j, j));
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        if (i > j) {
+          const double v = cabs2(AE(i, j));
           if (v > best) {
             best = v;
             p = i;
           }
         }
-        if (best == 0.0) singular = true;
-        if (p != j) {
-#pragma unroll UNR
-          for (int k = j; k < N; ++k) {
-            const double2 t = LDA(j, k);
-            STA(j, k, LDA(p, k));
-            STA(p, k, t);
-          }
-#pragma unroll UNR
-          for (int k = 0; k < N; ++k) {
-            const double2 t = LDB(j, k);
-            STB(j, k, LDB(p, k));
-            STB(p, k, t);
-          }
-        }
-        const double2 inv = crecip(LDA(j, j));
-        STA(j, j, inv);
-#pragma unroll UNR
-        for (int i = j + 1; i < N; ++i) {
-          const double2 f = cmul(LDA(i, j), inv);
-#pragma unroll UNR
-          for (int k = j + 1; k < N; ++k) STA(i, k, cfms(f, LDA(j, k), LDA(i, k)));
-#pragma unroll UNR
-          for (int k = 0; k < N; ++k) STB(i, k, cfms(f, LDB(j, k), LDB(i, k)));
-        }
       }
-      if (singular) atomicOr(status, kDevErrSingular);
-      double2 *y = chi + pt * N * N;
-#pragma unroll UNR
-      for (int j = N - 1; j >= 0; --j) {
-        const double2 inv = LDA(j, j);
-#pragma unroll UNR
+      if (best == 0.0) singular = true;
+      if (p != j) {
+#pragma unroll
         for (int k = 0; k < N; ++k) {
-          double2 s = LDB(j, k);
-#pragma unroll UNR
-          for (int l = j + 1; l < N; ++l) s = cfms(LDA(j, l), LDB(l, k), s);
-          s = cmul(s, inv);
-          STB(j, k, s);
-          y[j * N + colmap<NB>(k)] = s;
+          const double2 t = AE(j, k);
+          AE(j, k) = AE(p, k);
+          AE(p, k) = t;
+        }
+        const int t = perm[j * NT];
+        perm[j * NT] = perm[p * NT];
+        perm[p * NT] = t;
+      }
+      const double2 inv = crecip(AE(j, j));
+      AE(j, j) = inv;
+      double2 pr[N];
+#pragma unroll
+      for (int k = 0; k < N; ++k)
+        if (k > j) pr[k] = AE(j, k);
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        if (i > j) {
+          const double2 f = cmul(AE(i, j), inv);
+          AE(i, j) = f;
+#pragma unroll
+          for (int k = 0; k < N; ++k)
+            if (k > j) AE(i, k) = cfms(f, pr[k], AE(i, k));
         }
       }
     }
+    if (singular) atomicOr(status, kDevErrSingular);
+    // one right-hand side (a column of chi0) at a time, in registers
+    double2 *y = chi + pt * N * N;
+#pragma unroll 1
+    for (int c = 0; c < N; ++c) {
+      // An opaque zero added to the factor offsets keeps the compiler from
+      // hoisting all N^2 factor loads out of this loop into registers.
+      int z = 0;
+      asm volatile("" : "+r"(z));
+      const double2 *F = A + z;
+      const int cm = colmap<NB>(c);
+      double2 b[N];
+#pragma unroll
+      for (int r = 0; r < N; ++r) b[r] = x[perm[r * NT] * N + cm];
+#pragma unroll
+      for (int r = 1; r < N; ++r)
+#pragma unroll
+        for (int l = 0; l < r; ++l) b[r] = cfms(F[(r * N + l) * NT], b[l], b[r]);
+#pragma unroll
+      for (int rr = 0; rr < N; ++rr) {
+        const int r = N - 1 - rr;
+#pragma unroll
+        for (int l = r + 1; l < N; ++l) b[r] = cfms(F[(r * N + l) * NT], b[l], b[r]);
+        b[r] = cmul(b[r], F[(r * N + r) * NT]);
+      }
+#pragma unroll
+      for (int r = 0; r < N; ++r) y[r * N + cm] = b[r];
+    }
   }
-#undef AOFF
-#undef LDA
-#undef LDB
-#undef STA
-#undef STB
+#undef AE
 }
 
 template <int NB, int NT>
 int launch_rpa_nb(long n_points, const double2 *chi0, const double2 *U, double2 *chi, cudaStream_t stream,
                   unsigned *status) {
   constexpr int N = NB * NB;
-  const size_t smem = (size_t)N * N * sizeof(double2) * (1 + 2 * NT);
+  const size_t smem = (size_t)N * N * sizeof(double2) * (1 + NT) + (size_t)(N * N + N + 1) * sizeof(int) +
+                      (size_t)N * NT * sizeof(int);
   if (smem > (size_t)max_smem_optin()) return set_error(TPRF_ERR_INVALID_ARGUMENT, "solve_rpa_PH: nb too large");
-  TPRF_CUDA(cudaFuncSetAttribute(rpa_kernel<NB, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  TPRF_CUDA(cudaFuncSetAttribute(rpa_lu_kernel<NB, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   long blocks = (n_points + NT - 1) / NT;
   const long cap = (long)num_sms() * 64;
   blocks = std::max(1L, std::min(blocks, cap));
-  rpa_kernel<NB, NT><<<(unsigned)blocks, NT, smem, stream>>>(n_points, chi0, U, chi, status);
-  TPRF_LAUNCH_CHECK("rpa_kernel");
+  rpa_lu_kernel<NB, NT><<<(unsigned)blocks, NT, smem, stream>>>(n_points, chi0, U, chi, status);
+  TPRF_LAUNCH_CHECK("rpa_lu_kernel");
   return TPRF_OK;
 }
 
@@ -155,9 +175,9 @@ int launch_rpa(long n_points, int nb, const double2 *chi0, const double2 *U, dou
   switch (nb) {
     case 1: return launch_rpa_nb<1, 256>(n_points, chi0, U, chi, stream, status);
     case 2: return launch_rpa_nb<2, 256>(n_points, chi0, U, chi, stream, status);
-    case 3: return launch_rpa_nb<3, 64>(n_points, chi0, U, chi, stream, status);
-    case 4: return launch_rpa_nb<4, 16>(n_points, chi0, U, chi, stream, status);
-    case 5: return launch_rpa_nb<5, 8>(n_points, chi0, U, chi, stream, status);
+    case 3: return launch_rpa_nb<3, 128>(n_points, chi0, U, chi, stream, status);
+    case 4: return launch_rpa_nb<4, 32>(n_points, chi0, U, chi, stream, status);
+    case 5: return launch_rpa_nb<5, 16>(n_points, chi0, U, chi, stream, status);
     default: return set_error(TPRF_ERR_INVALID_ARGUMENT, "solve_rpa_PH: nb must be 1..5");
   }
 }
