@@ -62,10 +62,13 @@ int tprf_check_device_status(void *stream);
 /* Arithmetic of the FFT stages (lattice FFTs, iv -> tau, tau -> i omega).
  * TPRF_ARITH_DF64 (default): butterflies in double-float pairs on the FP32
  * pipe (~48-bit significand; on GB300 FP32 runs ~70x faster than FP64);
- * TPRF_ARITH_FP64: native FP64. Inputs and outputs are complex128 either way.
+ * TPRF_ARITH_FP64: native FP64; TPRF_ARITH_DF64_ALL: double-float also in the
+ * RPA solve, where points whose conditioning estimate exceeds 100 are
+ * re-solved in FP64. Inputs and outputs are complex128 in every mode.
  * Process-wide; no reference counterpart (the reference has one CPU path). */
 #define TPRF_ARITH_DF64 0
 #define TPRF_ARITH_FP64 1
+#define TPRF_ARITH_DF64_ALL 2
 int tprf_set_arithmetic(int mode);
 int tprf_get_arithmetic(void);
 

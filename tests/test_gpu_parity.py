@@ -15,10 +15,11 @@ from conftest import PARITY_RTOL, rel_err
 pytestmark = pytest.mark.gpu
 
 
-@pytest.fixture(autouse=True, params=["df64", "fp64"])
+@pytest.fixture(autouse=True, params=["df64", "fp64", "df64_all"])
 def arithmetic(request, cuda_lib):
-    """Every parity test runs with the FFT stages in double-float and in native FP64."""
-    mode = {"df64": 0, "fp64": 1}[request.param]
+    """Every parity test runs with the FFT stages in double-float (default), in
+    native FP64, and with the RPA solve in double-float as well."""
+    mode = {"df64": 0, "fp64": 1, "df64_all": 2}[request.param]
     assert cuda_lib.tprf_set_arithmetic(mode) == 0
     yield request.param
     cuda_lib.tprf_set_arithmetic(0)
@@ -212,6 +213,40 @@ def test_rpa_random(cuda_lib, nb):
     chi0 = 0.1 * rand_c(rng, 3, npts // 3, nb, nb, nb, nb)
     U = 0.5 * rand_c(rng, nb, nb, nb, nb)
     mesh = T.MeshProduct(T.MeshImFreq(1.0, "Boson", 2), T.MeshBrZone(dims=(npts // 3, 1, 1)))
+    chi = T.solve_rpa_PH(T.Gf(mesh=mesh, data=chi0), U)
+    assert rel_err(chi.data, O.solve_rpa_PH(chi0, U)) < PARITY_RTOL
+
+
+@pytest.mark.parametrize("gap", [1e-2, 1e-4, 1e-6])
+def test_rpa_near_instability(cuda_lib, gap):
+    """1 - U chi0 -> 0 at q = (pi, pi): the denominator's cancellation needs FP64
+    (double-float points are re-solved in FP64 there)."""
+    T = tp()
+    dims, beta, n_max = (8, 8, 1), 10.0, 32
+    ek = O.ek_from_hoppings({(0, 1): -np.eye(1), (0, -1): -np.eye(1), (1, 0): -np.eye(1), (-1, 0): -np.eye(1)}, dims)
+    chi0 = O.imtime_bubble_chi0_wk(O.lattice_dyson_g0_wk(0.0, ek, beta, n_max), beta, dims, nw=4)
+    c_max = chi0[:, :, 0, 0, 0, 0].real.max()
+    U = np.full((1, 1, 1, 1), (1.0 - gap) / c_max + 0j)
+    mesh = T.MeshProduct(T.MeshImFreq(beta, "Boson", 4), T.MeshBrZone(dims=dims))
+    chi = T.solve_rpa_PH(T.Gf(mesh=mesh, data=chi0), U)
+    ref = O.solve_rpa_PH(chi0, U)
+    assert np.abs(ref).max() > 0.5 / gap * c_max  # the divergence is really there
+    assert rel_err(chi.data, ref) < PARITY_RTOL
+
+
+@pytest.mark.parametrize("gap", [1e-3, 1e-5])
+def test_rpa_near_instability_multiorbital(cuda_lib, gap):
+    T = tp()
+    from tprf_gb300 import workloads
+    dims, beta, n_max = (4, 4, 4), 20.0, 32
+    ek = O.ek_from_hoppings(workloads.cubic_3orb(0), dims)
+    chi0 = O.imtime_bubble_chi0_wk(O.lattice_dyson_g0_wk(0.0, ek, beta, n_max), beta, dims, nw=2)
+    Us = workloads.kanamori_spin_vertex(3, 1.0, 0.2)
+    # scale U so that the largest eigenvalue of chi0 U (grouped) is 1 - gap
+    g = lambda x: np.swapaxes(x, -1, -2).reshape(x.shape[:-4] + (9, 9))  # noqa: E731
+    lam = max(np.abs(np.linalg.eigvals(g(chi0) @ g(Us))).max(axis=-1).ravel())
+    U = Us * (1.0 - gap) / lam
+    mesh = T.MeshProduct(T.MeshImFreq(beta, "Boson", 2), T.MeshBrZone(dims=dims))
     chi = T.solve_rpa_PH(T.Gf(mesh=mesh, data=chi0), U)
     assert rel_err(chi.data, O.solve_rpa_PH(chi0, U)) < PARITY_RTOL
 

@@ -12,8 +12,7 @@
 // is what an FFT needs. Every float operation uses a _rn intrinsic so the
 // compiler can neither contract nor reassociate it.
 //
-// Conversions from and to FP64 use integer bit operations (and one FP64 add
-// per real on the way back), not the conversion instructions.
+// Conversions from and to FP64 use integer bit operations only.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -93,17 +92,24 @@ __device__ __forceinline__ cdf mul_mi(cdf a) {  // -i a (FWD) or +i a
 }
 
 // ---- conversions --------------------------------------------------------------
-// hi = x truncated to 24 significant bits, lo = the remaining bits (rounded
-// down to 24 significant bits). Values below 2^-126 in magnitude become 0;
-// NaN and infinities go to hi.
+// All conversions are integer bit operations: on GB300 the FP64 pipe is the
+// scarce one, and the conversion instructions would run there.
+//
+// hi = x truncated to 24 significant bits, lo = the remaining bits (truncated
+// to 24 significant bits). Values below 2^-126 in magnitude become 0; NaN and
+// infinities keep their class in hi; finite values beyond the float range
+// become infinities.
 __device__ __forceinline__ dfl split_double(double x) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(x);
   const unsigned h = (unsigned)(b >> 32), l = (unsigned)b;
   const unsigned sign = h & 0x80000000u;
   const int e = (int)((h >> 20) & 0x7ffu);
   const int fe = e - 1023 + 127;
-  if (fe <= 0) return dfl{0.f, 0.f};
-  if (fe >= 255) return dfl{__double2float_rn(x), 0.f};
+  if (fe <= 0) return dfl{__uint_as_float(sign), 0.f};
+  if (fe >= 255) {
+    const bool nan = (e == 0x7ff) && (((h & 0xfffffu) | l) != 0u);
+    return dfl{__uint_as_float(sign | 0x7f800000u | (nan ? 0x400000u : 0u)), 0.f};
+  }
   const float hi = __uint_as_float(sign | ((unsigned)fe << 23) | ((h & 0xfffffu) << 3) | (l >> 29));
   const unsigned r = l & 0x1fffffffu;  // remaining 29 bits, weight 2^(e - 1075)
   if (r == 0u) return dfl{hi, 0.f};
@@ -118,15 +124,42 @@ __device__ __forceinline__ dfl split_double(double x) {
 __device__ __forceinline__ double float_to_double_exact(float f) {
   const unsigned u = __float_as_uint(f);
   const unsigned e = (u >> 23) & 0xffu;
-  if (e == 0u) return 0.0;
-  if (e == 0xffu) return (double)f;
-  const unsigned long long bits = ((unsigned long long)(u & 0x80000000u) << 32) |
-                                  ((unsigned long long)(e - 127u + 1023u) << 52) |
-                                  ((unsigned long long)(u & 0x7fffffu) << 29);
-  return __longlong_as_double((long long)bits);
+  const unsigned long long sign = (unsigned long long)(u & 0x80000000u) << 32;
+  if (e == 0u) return __longlong_as_double((long long)sign);
+  const unsigned long long ex = (e == 0xffu) ? 0x7ffull : (unsigned long long)(e - 127u + 1023u);
+  return __longlong_as_double((long long)(sign | (ex << 52) | ((unsigned long long)(u & 0x7fffffu) << 29)));
 }
 
-__device__ __forceinline__ double to_double(dfl a) { return float_to_double_exact(a.hi) + float_to_double_exact(a.lo); }
+// hi + lo as a double, by integer arithmetic: lo is aligned to hi's 53-bit
+// significand and added or subtracted; lo bits below it are truncated (error
+// below one double ulp).
+__device__ __forceinline__ double to_double(dfl a) {
+  const unsigned hb = __float_as_uint(a.hi), lb = __float_as_uint(a.lo);
+  const unsigned eh = (hb >> 23) & 0xffu, el = (lb >> 23) & 0xffu;
+  if (eh == 0u) return float_to_double_exact(a.lo);
+  if (eh == 0xffu || el == 0u) return float_to_double_exact(a.hi);
+  const int d = (int)eh - (int)el;
+  if (d < 0 || d >= 53) return float_to_double_exact(a.hi);  // lo below double precision (or not normalised)
+  unsigned long long M = (unsigned long long)((hb & 0x7fffffu) | 0x800000u) << 29;  // 53-bit significand
+  const unsigned long long Lm = ((unsigned long long)((lb & 0x7fffffu) | 0x800000u) << 29) >> d;
+  int e = (int)eh;
+  if ((hb ^ lb) & 0x80000000u) {
+    M -= Lm;
+    while (M != 0ull && M < (1ull << 52)) {
+      M <<= 1;
+      --e;
+    }
+    if (M == 0ull) return 0.0;
+  } else {
+    M += Lm;
+    if (M >= (1ull << 53)) {
+      M >>= 1;
+      ++e;
+    }
+  }
+  const unsigned long long sign = (unsigned long long)(hb & 0x80000000u) << 32;
+  return __longlong_as_double((long long)(sign | ((unsigned long long)(e - 127 + 1023) << 52) | (M & ((1ull << 52) - 1))));
+}
 
 __device__ __forceinline__ cdf to_cdf(double2 z) { return cdf{split_double(z.x), split_double(z.y)}; }
 __device__ __forceinline__ double2 to_double2(cdf z) { return make_double2(to_double(z.x), to_double(z.y)); }

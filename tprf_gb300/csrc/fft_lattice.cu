@@ -24,9 +24,9 @@ namespace {
 template <class E> __device__ __forceinline__ E load_el(double2 z);
 template <> __device__ __forceinline__ double2 load_el<double2>(double2 z) { return z; }
 template <> __device__ __forceinline__ cdf load_el<cdf>(double2 z) { return to_cdf(z); }
-__device__ __forceinline__ double2 store_el(double2 z, double s) { return cscale(z, s); }
-__device__ __forceinline__ double2 store_el(cdf z, double s) {
-  return to_double2(s == 1.0 ? z : cscale(z, split_double(s)));
+__device__ __forceinline__ double2 store_el(double2 z, double s, dfl, bool scaled) { return scaled ? cscale(z, s) : z; }
+__device__ __forceinline__ double2 store_el(cdf z, double, dfl sd, bool scaled) {
+  return to_double2(scaled ? cscale(z, sd) : z);
 }
 
 template <bool FWD, class E>
@@ -54,10 +54,12 @@ __global__ void __launch_bounds__(256) lattice_axis_kernel(const double2 *in, do
     a[d.rev[row] * ncol + c] = load_el<E>(v);
   }
   E *r = fft_smem<FWD>(a, b, d, ncol);
+  const bool scaled = scale != 1.0;
+  const dfl sd = split_double(scale);
   for (int w = threadIdx.x; w < tile; w += blockDim.x) {
     const int c = w & (ncol - 1), row = w >> lgcol;
     const long bs = base[c];
-    if (bs >= 0) out[bs + (long)row * inner] = store_el(r[row * ncol + c], scale);
+    if (bs >= 0) out[bs + (long)row * inner] = store_el(r[row * ncol + c], scale, sd, scaled);
   }
 }
 

@@ -89,8 +89,8 @@ struct TauWPlan {
 };
 
 // Element type used by the FFT stages: double-float on the FP32 pipe (default)
-// or native FP64.
-enum Arith : int { kArithDF64 = 0, kArithFP64 = 1 };
+// or native FP64; kArithDF64All also runs the RPA solve in double-float.
+enum Arith : int { kArithDF64 = 0, kArithFP64 = 1, kArithDF64All = 2 };
 int arith_mode();
 int get_tau_w_plan(double beta, int n_tau, int nw, const TauWPlan **out);
 

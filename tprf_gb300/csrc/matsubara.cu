@@ -30,6 +30,8 @@
 namespace tprf {
 namespace {
 
+constexpr int kMatsubaraThreads = 256;  // columns per CTA (<= 32) divide it
+
 struct VinvRows {
   double r0[8];  // row 0 of the inverse Vandermonde: first derivative
   double r1[8];  // row 1: second-order coefficient
@@ -73,7 +75,7 @@ __device__ __forceinline__ float cabsf_approx(cdf z) {
 // by linearity): G(tau_t) = P[t] FFT(g)[t] + sum_j a_j Q[j][t].
 
 template <class C>
-__global__ void __launch_bounds__(512) nu_to_tau_kernel(NuTauPlan p, const double2 *__restrict__ gw,
+__global__ void __launch_bounds__(kMatsubaraThreads, 2) nu_to_tau_kernel(NuTauPlan p, const double2 *__restrict__ gw,
                                                         const double2 *__restrict__ mom, double2 *__restrict__ gt,
                                                         long Ccols, int ic, int lg, unsigned *status) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -215,7 +217,7 @@ struct BubbleLoader {  // chi0 columns computed from G(tau, r): col = r * nb^4 +
 // tau -> i omega. fit_derivatives moments in FP64 from the end rows; the tail
 // model enters after the FFT: chi(i w_m) = (beta/L) FFT(chi)[k_m] + sum_j a_j K[j][m].
 template <class Loader, class C>
-__global__ void __launch_bounds__(512) tau_to_w_kernel(TauWPlan p, Loader ld, VinvRows vr, double2 *__restrict__ out,
+__global__ void __launch_bounds__(kMatsubaraThreads, 2) tau_to_w_kernel(TauWPlan p, Loader ld, VinvRows vr, double2 *__restrict__ out,
                                                        long Ccols, int ic, int lg) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C *a = reinterpret_cast<C *>(smem_raw);
@@ -302,7 +304,11 @@ __global__ void __launch_bounds__(256) bubble_kernel(BubbleLoader ld, double2 *_
 // length-L buffer (two when the FFT has a generic-radix stage) plus the
 // per-column extras fit in shared memory.
 int pick_ic(const FftDesc &fft, size_t extra_per_col, int *ic_out, int *lg_out, size_t *smem_out) {
-  const size_t budget = (size_t)std::min(max_smem_optin(), 220 * 1024);
+  // Two CTAs per SM where the mesh allows: while one waits at a stage barrier
+  // or on its loads, the other computes.
+  const size_t full = (size_t)std::min(max_smem_optin(), 220 * 1024);
+  size_t budget = full / 2 - 1024;
+  if ((fft.has_generic ? 2 : 1) * (size_t)fft.n * sizeof(double2) + extra_per_col > budget) budget = full;
   const size_t bufs = fft.has_generic ? 2 : 1;
   const size_t L = fft.n;
   int ic = 32;
@@ -332,7 +338,7 @@ int launch_tau_to_w_as(const TauWPlan *p, Loader ld, double2 *out, long C, cudaS
   if (st) return st;
   TPRF_CUDA(cudaFuncSetAttribute(tau_to_w_kernel<Loader, E>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const long blocks = (C + ic - 1) / ic;
-  tau_to_w_kernel<Loader, E><<<(unsigned)blocks, 512, smem, stream>>>(*p, ld, make_vinv_rows(), out, C, ic, lg);
+  tau_to_w_kernel<Loader, E><<<(unsigned)blocks, kMatsubaraThreads, smem, stream>>>(*p, ld, make_vinv_rows(), out, C, ic, lg);
   TPRF_LAUNCH_CHECK("tau_to_w_kernel");
   return TPRF_OK;
 }
@@ -398,10 +404,10 @@ int launch_nu_to_tau(double beta, int n_iw, int n_tau, long C, const double2 *gw
   const long blocks = (C + ic - 1) / ic;
   if (arith_mode() == kArithFP64) {
     TPRF_CUDA(cudaFuncSetAttribute(nu_to_tau_kernel<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    nu_to_tau_kernel<double2><<<(unsigned)blocks, 512, smem, stream>>>(*p, gw, mom, gt, C, ic, lg, status);
+    nu_to_tau_kernel<double2><<<(unsigned)blocks, kMatsubaraThreads, smem, stream>>>(*p, gw, mom, gt, C, ic, lg, status);
   } else {
     TPRF_CUDA(cudaFuncSetAttribute(nu_to_tau_kernel<cdf>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    nu_to_tau_kernel<cdf><<<(unsigned)blocks, 512, smem, stream>>>(*p, gw, mom, gt, C, ic, lg, status);
+    nu_to_tau_kernel<cdf><<<(unsigned)blocks, kMatsubaraThreads, smem, stream>>>(*p, gw, mom, gt, C, ic, lg, status);
   }
   TPRF_LAUNCH_CHECK("nu_to_tau_kernel");
   return TPRF_OK;

@@ -524,8 +524,8 @@ extern "C" const char *tprf_version(void) { return "0.1.0"; }
 extern "C" void tprf_set_sync_checks(int on) { tprf::g_sync_checks.store(on != 0); }
 
 extern "C" int tprf_set_arithmetic(int mode) {
-  if (mode != TPRF_ARITH_DF64 && mode != TPRF_ARITH_FP64)
-    return tprf::set_error(TPRF_ERR_INVALID_ARGUMENT, "set_arithmetic: mode must be TPRF_ARITH_DF64 or TPRF_ARITH_FP64");
+  if (mode != TPRF_ARITH_DF64 && mode != TPRF_ARITH_FP64 && mode != TPRF_ARITH_DF64_ALL)
+    return tprf::set_error(TPRF_ERR_INVALID_ARGUMENT, "set_arithmetic: unknown mode");
   tprf::g_arith.store(mode);
   return TPRF_OK;
 }

@@ -27,16 +27,156 @@ __device__ __forceinline__ int colmap(int c) {  // grouped column (d, c') -> off
   return (c % NB) * NB + c / NB;
 }
 
-template <int NB, int NT>
+// element-type plumbing: double2 (FP64) or cdf (double-float)
+__device__ __forceinline__ double2 el_from(double2 z, double2 *) { return z; }
+__device__ __forceinline__ cdf el_from(double2 z, cdf *) { return to_cdf(z); }
+__device__ __forceinline__ double2 el_to(double2 z) { return z; }
+__device__ __forceinline__ double2 el_to(cdf z) { return to_double2(z); }
+__device__ __forceinline__ double2 el_one(double2 *) { return make_double2(1.0, 0.0); }
+__device__ __forceinline__ cdf el_one(cdf *) { return cdf{dfl{1.f, 0.f}, dfl{0.f, 0.f}}; }
+__device__ __forceinline__ double2 el_zero(double2 *) { return make_double2(0.0, 0.0); }
+__device__ __forceinline__ cdf el_zero(cdf *) { return cdf{dfl{0.f, 0.f}, dfl{0.f, 0.f}}; }
+__device__ __forceinline__ double el_abs2(double2 z) { return cabs2(z); }
+__device__ __forceinline__ double el_abs2(cdf z) { return (double)(z.x.hi * z.x.hi + z.y.hi * z.y.hi); }
+__device__ __forceinline__ float el_absf(double2 z) { return (float)sqrt(cabs2(z)); }
+__device__ __forceinline__ float el_absf(cdf z) { return sqrtf(z.x.hi * z.x.hi + z.y.hi * z.y.hi); }
+template <class E> struct IsDf { static constexpr bool value = false; };
+template <> struct IsDf<cdf> { static constexpr bool value = true; };
+__device__ __forceinline__ double2 el_fms(double2 a, double2 b, double2 acc) { return cfms(a, b, acc); }
+__device__ __forceinline__ cdf el_fms(cdf a, cdf b, cdf acc) { return csub(acc, cmul(a, b)); }
+__device__ __forceinline__ double2 el_recip(double2 a) { return crecip(a); }
+__device__ __forceinline__ cdf el_recip(cdf a) {
+  // 1/(x + iy) = (x - iy) / (x^2 + y^2); the real reciprocal by one Newton step from the float one
+  const dfl d = ddot_add(a.x, a.x, a.y, a.y);
+  const float r0 = __frcp_rn(d.hi);
+  const dfl e = dsub(dfl{1.f, 0.f}, dmul(d, dfl{r0, 0.f}));
+  const dfl r = dadd(dfl{r0, 0.f}, dmul(dfl{r0, 0.f}, e));
+  return cdf{dmul(a.x, r), dneg(dmul(a.y, r))};
+}
+
+// One (w, q) point: A = I - chi0 U from the non-zeros of U, LU with partial
+// pivoting in the thread's shared-memory slice, then the nb^2 right-hand
+// sides in registers. Returns the conditioning estimate
+// (max_ij s_ij / min_j |U_jj|)^2, where s_ij = delta_ij + sum_m |chi0_im| |U_mj|
+// is the size of the terms that formed A_ij (so cancellation in forming
+// 1 - chi0 U counts as well as small pivots); it sends ill-conditioned points
+// from double-float to FP64.
+template <int NB, int NT, class E>
+__device__ double rpa_point(const double2 *x, double2 *y, E *A, int *perm, const E *s_val, const int *s_off,
+                            const int *s_cs, bool &singular) {
+  constexpr int N = NB * NB;
+#define AE(i, k) A[((i) * N + (k)) * NT]
+  double amax = 0.0;
+#pragma unroll
+  for (int r = 0; r < N; ++r) {
+#pragma unroll
+    for (int c = 0; c < N; ++c) {
+      E s = (r == c) ? el_one((E *)nullptr) : el_zero((E *)nullptr);
+      float mag = (r == c) ? 1.f : 0.f;
+      for (int t = s_cs[c]; t < s_cs[c + 1]; ++t) {
+        const E xv = el_from(x[r * N + s_off[t]], (E *)nullptr);
+        s = el_fms(xv, s_val[t], s);
+        mag = fmaf(el_absf(xv), el_absf(s_val[t]), mag);
+      }
+      amax = fmax(amax, (double)mag * (double)mag);
+      AE(r, c) = s;
+    }
+    perm[r * NT] = r;
+  }
+  double pmin = 1e300;
+  singular = false;
+#pragma unroll 1
+  for (int j = 0; j < N; ++j) {
+    int p = j;
+    double best = el_abs2(AE(j, j));
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      if (i > j) {
+        const double v = el_abs2(AE(i, j));
+        if (v > best) {
+          best = v;
+          p = i;
+        }
+      }
+    }
+    if (best == 0.0) singular = true;
+    pmin = fmin(pmin, best);
+    if (p != j) {
+#pragma unroll
+      for (int k = 0; k < N; ++k) {
+        const E t = AE(j, k);
+        AE(j, k) = AE(p, k);
+        AE(p, k) = t;
+      }
+      const int t = perm[j * NT];
+      perm[j * NT] = perm[p * NT];
+      perm[p * NT] = t;
+    }
+    const E inv = el_recip(AE(j, j));
+    AE(j, j) = inv;
+    E pr[N];
+#pragma unroll
+    for (int k = 0; k < N; ++k)
+      if (k > j) pr[k] = AE(j, k);
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      if (i > j) {
+        const E f = cmul(AE(i, j), inv);
+        AE(i, j) = f;
+#pragma unroll
+        for (int k = 0; k < N; ++k)
+          if (k > j) AE(i, k) = el_fms(f, pr[k], AE(i, k));
+      }
+    }
+  }
+#pragma unroll 1
+  for (int c = 0; c < N; ++c) {
+    // An opaque zero added to the factor offsets keeps the compiler from
+    // hoisting all N^2 factor loads out of this loop into registers.
+    int z = 0;
+    asm volatile("" : "+r"(z));
+    const E *F = A + z;
+    const int cm = colmap<NB>(c);
+    E b[N];
+#pragma unroll
+    for (int r = 0; r < N; ++r) b[r] = el_from(x[perm[r * NT] * N + cm], (E *)nullptr);
+#pragma unroll
+    for (int r = 1; r < N; ++r)
+#pragma unroll
+      for (int l = 0; l < r; ++l) b[r] = el_fms(F[(r * N + l) * NT], b[l], b[r]);
+#pragma unroll
+    for (int rr = 0; rr < N; ++rr) {
+      const int r = N - 1 - rr;
+#pragma unroll
+      for (int l = r + 1; l < N; ++l) b[r] = el_fms(F[(r * N + l) * NT], b[l], b[r]);
+      b[r] = cmul(b[r], F[(r * N + r) * NT]);
+    }
+#pragma unroll
+    for (int r = 0; r < N; ++r) y[r * N + cm] = el_to(b[r]);
+  }
+#undef AE
+  return pmin > 0.0 ? amax / pmin : 1e300;
+}
+
+// Squared conditioning estimate above which a double-float solution is
+// recomputed in FP64: (max|A| / min pivot)^2 > 1e4, i.e. the estimate > 100.
+// Double-float carries ~2^-48 per operation, so below it the solve stays well
+// inside 1e-10 relative; near an RPA instability (1 - chi0 U nearly singular)
+// the point is solved in FP64.
+constexpr double kDf64CondLimit2 = 1e4;
+
+template <int NB, int NT, class E>
 __global__ void __launch_bounds__(NT) rpa_lu_kernel(long n_points, const double2 *chi0, const double2 *__restrict__ U,
                                                     double2 *chi, unsigned *status) {
   constexpr int N = NB * NB;
-  extern __shared__ double2 smem[];
-  double2 *s_val = smem;                                     // [nnz] non-zeros of the grouped U
-  double2 *A = smem + N * N + threadIdx.x;                   // per thread LU, [N*N][NT]
-  int *s_off = reinterpret_cast<int *>(smem + N * N + (size_t)N * N * NT);  // [nnz]
-  int *s_cs = s_off + N * N;                                 // [N + 1] column starts
-  int *perm = s_cs + N + 1 + threadIdx.x;                    // per thread row permutation, [N][NT]
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  // Layout: [N*N] sparse U values (E), [N*N][NT] per-thread LU (16 B elements
+  // of either type), [N*N] offsets, [N+1] column starts, [N][NT] permutations.
+  E *s_val = reinterpret_cast<E *>(smem_raw);
+  unsigned char *lu_base = smem_raw + (size_t)N * N * sizeof(E);
+  int *s_off = reinterpret_cast<int *>(lu_base + (size_t)N * N * NT * 16);
+  int *s_cs = s_off + N * N;
+  int *perm = s_cs + N + 1 + threadIdx.x;
   // Sparse form of the grouped vertex Ug[m][c] = U[m][colmap(c)], column by
   // column: entry t of column c has grouped row m_t, kept as the offset
   // colmap(m_t) into a chi0 row. Exact zeros are dropped (the Kanamori vertex
@@ -49,7 +189,7 @@ __global__ void __launch_bounds__(NT) rpa_lu_kernel(long n_points, const double2
         const double2 u = U[m * N + colmap<NB>(c)];
         if (u.x != 0.0 || u.y != 0.0) {
           s_off[t] = colmap<NB>(m);
-          s_val[t] = u;
+          s_val[t] = el_from(u, (E *)nullptr);
           ++t;
         }
       }
@@ -57,114 +197,54 @@ __global__ void __launch_bounds__(NT) rpa_lu_kernel(long n_points, const double2
     s_cs[N] = t;
   }
   __syncthreads();
-#define AE(i, k) A[((i) * N + (k)) * NT]
   for (long base = blockIdx.x * (long)NT; base < n_points; base += (long)gridDim.x * NT) {
     const long pt = base + threadIdx.x;
     if (pt >= n_points) continue;
     const double2 *x = chi0 + pt * N * N;
-    // A = I - chi0 U over the non-zeros of U
-#pragma unroll
-    for (int r = 0; r < N; ++r) {
-#pragma unroll
-      for (int c = 0; c < N; ++c) {
-        double2 s = make_double2(r == c ? 1.0 : 0.0, 0.0);
-        for (int t = s_cs[c]; t < s_cs[c + 1]; ++t) s = cfms(x[r * N + s_off[t]], s_val[t], s);
-        AE(r, c) = s;
-      }
-      perm[r * NT] = r;
-    }
-    // LU with partial pivoting; the step loop stays rolled so that the factors
-    // live in shared memory, not in registers.
+    double2 *y = chi + pt * N * N;
     bool singular = false;
-#pragma unroll 1
-    for (int j = 0; j < N; ++j) {
-      int p = j;
-      double best = cabs2(AE(j, j));
-#pragma unroll
-      for (int i = 0; i < N; ++i) {
-        if (i > j) {
-          const double v = cabs2(AE(i, j));
-          if (v > best) {
-            best = v;
-            p = i;
-          }
-        }
+    const double cond2 = rpa_point<NB, NT, E>(x, y, reinterpret_cast<E *>(lu_base) + threadIdx.x, perm, s_val, s_off,
+                                              s_cs, singular);
+    if (IsDf<E>::value && !(cond2 <= kDf64CondLimit2)) {
+      // FP64 re-solve of an ill-conditioned point, with U in FP64 from global memory
+      double2 uval[N * N];
+      for (int t = 0; t < s_cs[N]; ++t) {
+        int c = 0;
+        while (s_cs[c + 1] <= t) ++c;
+        const int m = (s_off[t] % NB) * NB + s_off[t] / NB;  // colmap is an involution
+        uval[t] = U[m * N + colmap<NB>(c)];
       }
-      if (best == 0.0) singular = true;
-      if (p != j) {
-#pragma unroll
-        for (int k = 0; k < N; ++k) {
-          const double2 t = AE(j, k);
-          AE(j, k) = AE(p, k);
-          AE(p, k) = t;
-        }
-        const int t = perm[j * NT];
-        perm[j * NT] = perm[p * NT];
-        perm[p * NT] = t;
-      }
-      const double2 inv = crecip(AE(j, j));
-      AE(j, j) = inv;
-      double2 pr[N];
-#pragma unroll
-      for (int k = 0; k < N; ++k)
-        if (k > j) pr[k] = AE(j, k);
-#pragma unroll
-      for (int i = 0; i < N; ++i) {
-        if (i > j) {
-          const double2 f = cmul(AE(i, j), inv);
-          AE(i, j) = f;
-#pragma unroll
-          for (int k = 0; k < N; ++k)
-            if (k > j) AE(i, k) = cfms(f, pr[k], AE(i, k));
-        }
-      }
+      rpa_point<NB, NT, double2>(x, y, reinterpret_cast<double2 *>(lu_base) + threadIdx.x, perm, uval, s_off, s_cs,
+                                 singular);
     }
     if (singular) atomicOr(status, kDevErrSingular);
-    // one right-hand side (a column of chi0) at a time, in registers
-    double2 *y = chi + pt * N * N;
-#pragma unroll 1
-    for (int c = 0; c < N; ++c) {
-      // An opaque zero added to the factor offsets keeps the compiler from
-      // hoisting all N^2 factor loads out of this loop into registers.
-      int z = 0;
-      asm volatile("" : "+r"(z));
-      const double2 *F = A + z;
-      const int cm = colmap<NB>(c);
-      double2 b[N];
-#pragma unroll
-      for (int r = 0; r < N; ++r) b[r] = x[perm[r * NT] * N + cm];
-#pragma unroll
-      for (int r = 1; r < N; ++r)
-#pragma unroll
-        for (int l = 0; l < r; ++l) b[r] = cfms(F[(r * N + l) * NT], b[l], b[r]);
-#pragma unroll
-      for (int rr = 0; rr < N; ++rr) {
-        const int r = N - 1 - rr;
-#pragma unroll
-        for (int l = r + 1; l < N; ++l) b[r] = cfms(F[(r * N + l) * NT], b[l], b[r]);
-        b[r] = cmul(b[r], F[(r * N + r) * NT]);
-      }
-#pragma unroll
-      for (int r = 0; r < N; ++r) y[r * N + cm] = b[r];
-    }
   }
-#undef AE
+}
+
+template <int NB, int NT, class E>
+int launch_rpa_as(long n_points, const double2 *chi0, const double2 *U, double2 *chi, cudaStream_t stream,
+                  unsigned *status) {
+  constexpr int N = NB * NB;
+  const size_t smem = (size_t)N * N * 16 * (1 + NT) + (size_t)(N * N + N + 1) * sizeof(int) +
+                      (size_t)N * NT * sizeof(int);
+  if (smem > (size_t)max_smem_optin()) return set_error(TPRF_ERR_INVALID_ARGUMENT, "solve_rpa_PH: nb too large");
+  TPRF_CUDA(cudaFuncSetAttribute(rpa_lu_kernel<NB, NT, E>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  long blocks = (n_points + NT - 1) / NT;
+  const long cap = (long)num_sms() * 64;
+  blocks = std::max(1L, std::min(blocks, cap));
+  rpa_lu_kernel<NB, NT, E><<<(unsigned)blocks, NT, smem, stream>>>(n_points, chi0, U, chi, status);
+  TPRF_LAUNCH_CHECK("rpa_lu_kernel");
+  return TPRF_OK;
 }
 
 template <int NB, int NT>
 int launch_rpa_nb(long n_points, const double2 *chi0, const double2 *U, double2 *chi, cudaStream_t stream,
                   unsigned *status) {
-  constexpr int N = NB * NB;
-  const size_t smem = (size_t)N * N * sizeof(double2) * (1 + NT) + (size_t)(N * N + N + 1) * sizeof(int) +
-                      (size_t)N * NT * sizeof(int);
-  if (smem > (size_t)max_smem_optin()) return set_error(TPRF_ERR_INVALID_ARGUMENT, "solve_rpa_PH: nb too large");
-  TPRF_CUDA(cudaFuncSetAttribute(rpa_lu_kernel<NB, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  long blocks = (n_points + NT - 1) / NT;
-  const long cap = (long)num_sms() * 64;
-  blocks = std::max(1L, std::min(blocks, cap));
-  rpa_lu_kernel<NB, NT><<<(unsigned)blocks, NT, smem, stream>>>(n_points, chi0, U, chi, status);
-  TPRF_LAUNCH_CHECK("rpa_lu_kernel");
-  return TPRF_OK;
+  // One thread per point leaves one warp per scheduler: enough for the FP64
+  // pipe, too few to hide double-float's dependent chains, so FP64 is the
+  // default here and double-float only on request.
+  if (arith_mode() == kArithDF64All) return launch_rpa_as<NB, NT, cdf>(n_points, chi0, U, chi, stream, status);
+  return launch_rpa_as<NB, NT, double2>(n_points, chi0, U, chi, stream, status);
 }
 
 }  // namespace
