@@ -121,6 +121,19 @@ int tprf_fourier_wk_to_wr(long n_w, const int dims[3], long n_target,
 int tprf_fourier_wr_to_wk(long n_w, const int dims[3], long n_target,
                           const double *g_wr, double *g_wk, void *stream);
 
+/* Allocation-free lattice FFT: the same transforms as tprf_fourier_wk_to_wr
+ * (forward != 0) and tprf_fourier_wr_to_wk (forward == 0), for callers that
+ * cannot let a library allocate device memory (codes whose device memory all
+ * belongs to their own pool allocator, hosts with a fixed device-memory
+ * budget). No counterpart in the reference: it is an addition of this library.
+ * Its FFT tables live in a static 1 MiB device array inside the library
+ * image, 36 bytes per point of each distinct mesh length (about 29 000
+ * points); larger requests return TPRF_ERR_INVALID_ARGUMENT. The first call
+ * on a device looks up that array's address, so make it before any stream
+ * capture. Calls share the array: calls overlapping on the GPU race. */
+int tprf_fourier_lattice_noalloc(int forward, long n_w, const int dims[3], long n_target,
+                                 const double *in, double *out, void *stream);
+
 /* iv -> tau, fermionic, per r and target element, with the three-pole
  * high-frequency tail model (fourier/fourier_matsubara.cpp:218-308).
  * Replaces triqs_tprf::fourier_wr_to_tr(g_wr_cvt, int nt = -1)

@@ -33,6 +33,7 @@ SIGNATURES = {
                                         c_void_p, c_void_p]),
     "tprf_fourier_wk_to_wr": (c_int, [c_long, c_int3, c_long, c_void_p, c_void_p, c_void_p]),
     "tprf_fourier_wr_to_wk": (c_int, [c_long, c_int3, c_long, c_void_p, c_void_p, c_void_p]),
+    "tprf_fourier_lattice_noalloc": (c_int, [c_int, c_long, c_int3, c_long, c_void_p, c_void_p, c_void_p]),
     "tprf_fourier_wr_to_tr": (c_int, [c_double, c_int, c_int, c_long, c_long, c_void_p, c_void_p, c_void_p,
                                       c_void_p]),
     "tprf_chi0_tr_from_grt_PH": (c_int, [c_int, c_int3, c_int, c_void_p, c_void_p, c_void_p]),

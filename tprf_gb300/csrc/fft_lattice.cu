@@ -15,6 +15,9 @@
 // dimension with n > 1; later passes run in place. The butterflies run in
 // double-float pairs on the FP32 pipe by default (tprf_set_arithmetic).
 #include <algorithm>
+#include <map>
+#include <mutex>
+#include <string>
 
 #include "common.cuh"
 
@@ -161,5 +164,205 @@ extern "C" int tprf_fourier_wr_to_wk(long n_w, const int dims[3], long n_target,
                                 reinterpret_cast<double2 *>(g_wk), s);
   if (st) return st;
   TPRF_LAUNCH_CHECK("fourier_wr_to_wk");
+  return TPRF_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant of the lattice FFT.
+//
+// The entry points above keep their FFT tables (twiddles and digit-reversal
+// orders, one set per mesh length) in device memory that the library obtains
+// with cudaMalloc the first time a length is seen. Some callers cannot let a
+// library allocate device memory: codes that hand the whole GPU memory to
+// their own pool allocator at start-up and forbid any other device
+// allocation, or hosts that run under a fixed, pre-reserved device-memory
+// budget. tprf_fourier_lattice_noalloc serves them: its tables live in the
+// file-scope array below, which is part of the loaded library image, so no
+// call allocates or frees device memory.
+//
+// Rules of use:
+//  * kNoAllocScratchBytes bounds the tables: each distinct mesh length n
+//    takes 36 n bytes (plus 256-byte alignment); a transform needing more is
+//    refused with TPRF_ERR_INVALID_ARGUMENT before any work is queued.
+//  * Every GPU that loads the library holds the array until the process exits.
+//  * The first call on a device looks up the array's device address
+//    (cudaGetSymbolAddress) with that device current; make that first call
+//    before any stream capture.
+//  * Every call rebuilds the tables it needs at the start of the array, in
+//    stream order before its transform, so nothing from an earlier call is
+//    read. Calls that overlap on the GPU (different streams at the same time)
+//    share the array and race: serialise them.
+
+namespace tprf {
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = 1u << 20;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+std::mutex g_noalloc_mutex;
+std::map<int, unsigned char *> g_noalloc_addr;  // device -> device address of g_noalloc_scratch
+
+int noalloc_scratch_address(unsigned char **out) {
+  int dev = 0;
+  TPRF_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  auto it = g_noalloc_addr.find(dev);
+  if (it == g_noalloc_addr.end()) {
+    void *ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_status(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+    it = g_noalloc_addr.emplace(dev, static_cast<unsigned char *>(ptr)).first;
+  }
+  *out = it->second;
+  return TPRF_OK;
+}
+
+// Radix plan of length n (same factor order as the cached plans: 8s, one 4,
+// one 2, 3s, 5s, 7s, then larger primes).
+bool noalloc_factor(int n, FftDesc *d) {
+  int m = n, s = 0;
+  while (m % 8 == 0 && s < kMaxStages) { d->radix[s++] = 8; m /= 8; }
+  if (m % 4 == 0 && s < kMaxStages) { d->radix[s++] = 4; m /= 4; }
+  if (m % 2 == 0 && s < kMaxStages) { d->radix[s++] = 2; m /= 2; }
+  for (int r : {3, 5, 7})
+    while (m % r == 0 && s < kMaxStages) { d->radix[s++] = r; m /= r; }
+  for (int r = 11; (long)r * r <= m && s < kMaxStages; r += 2)
+    while (m % r == 0 && s < kMaxStages) { d->radix[s++] = r; m /= r; }
+  if (m > 1 && s < kMaxStages) { d->radix[s++] = m; m = 1; }
+  d->nst = s;
+  d->n = n;
+  d->has_generic = 0;
+  for (int i = 0; i < s; ++i)
+    if (d->radix[i] > 8) d->has_generic = 1;
+  return m == 1;
+}
+
+size_t noalloc_table_bytes(int n) {
+  const size_t b = (size_t)n * (sizeof(double2) + sizeof(float4) + sizeof(int));
+  return (b + 255) & ~size_t(255);
+}
+
+// Builds the tables of one length in place: twiddles exp(-2 pi i t / n) in FP64
+// and as double-float pairs, and the digit-reversal positions.
+__global__ void noalloc_tables_kernel(FftDesc d, double2 *tw, float4 *twf, int *rev) {
+  const int n = d.n;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    double s, c;
+    sincospi(-2.0 * (double)t / (double)n, &s, &c);
+    tw[t] = make_double2(c, s);
+    const dfl cr = split_double(c), ci = split_double(s);
+    twf[t] = make_float4(cr.hi, cr.lo, ci.hi, ci.lo);
+    long q = t, prod = 1, sig = 0;
+    for (int k = 0; k < d.nst; ++k) {
+      const int R = d.radix[k];
+      const long dg = q % R;
+      q /= R;
+      prod *= R;
+      sig += dg * (n / prod);
+    }
+    rev[sig] = t;
+  }
+}
+
+template <bool FWD, class E>
+int noalloc_axis(const double2 *in, double2 *out, long outer, long inner, const FftDesc &d, double scale,
+                 cudaStream_t stream) {
+  const int n = d.n;
+  const int bufs = d.has_generic ? 2 : 1;
+  const size_t budget = (size_t)std::min(max_smem_optin(), 200 * 1024);
+  int ncol = 64;
+  while (ncol > 1 && (size_t)bufs * n * ncol * sizeof(E) + ncol * sizeof(long) > budget) ncol /= 2;
+  const long ncols_total = outer * inner;
+  while (ncol > 8 && ncol / 2 >= ncols_total) ncol /= 2;
+  const size_t smem = (size_t)bufs * n * ncol * sizeof(E) + ncol * sizeof(long);
+  int lg = 0;
+  while ((1 << lg) < ncol) ++lg;
+  const long blocks = (ncols_total + ncol - 1) / ncol;
+  TPRF_CUDA(cudaFuncSetAttribute(lattice_axis_kernel<FWD, E>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  lattice_axis_kernel<FWD, E><<<(unsigned)blocks, 256, smem, stream>>>(in, out, ncols_total, inner, ncol, lg, d, scale);
+  TPRF_LAUNCH_CHECK("lattice_axis_kernel (no-alloc)");
+  return TPRF_OK;
+}
+
+}  // namespace
+}  // namespace tprf
+
+extern "C" int tprf_fourier_lattice_noalloc(int forward, long n_w, const int dims[3], long n_target, const double *in,
+                                            double *out, void *stream) {
+  using namespace tprf;
+  int st = check_lattice_args(n_w, dims, n_target, in, out);
+  if (st) return st;
+  // tables needed: one set per distinct mesh length > 1, laid out from the start of the array
+  int lens[3], nl = 0;
+  size_t need = 0;
+  for (int ax = 0; ax < 3; ++ax) {
+    const int n = dims[ax];
+    bool seen = false;
+    for (int i = 0; i < nl; ++i) seen |= (lens[i] == n);
+    if (n > 1 && !seen) {
+      lens[nl++] = n;
+      need += noalloc_table_bytes(n);
+    }
+  }
+  if (need > kNoAllocScratchBytes)
+    return set_error(TPRF_ERR_INVALID_ARGUMENT,
+                     "fourier_lattice_noalloc: FFT tables need " + std::to_string(need) +
+                         " bytes, more than the static scratch of " + std::to_string(kNoAllocScratchBytes) +
+                         " bytes (36 bytes per point of each distinct mesh length)");
+  FftDesc desc[3];
+  for (int i = 0; i < nl; ++i)
+    if (!noalloc_factor(lens[i], &desc[i]))
+      return set_error(TPRF_ERR_UNSUPPORTED_SIZE, "fourier_lattice_noalloc: too many FFT factors");
+  for (int i = 0; i < nl; ++i) {
+    const size_t bufs = desc[i].has_generic ? 2 : 1;
+    if (bufs * (size_t)lens[i] * sizeof(double2) + sizeof(long) > (size_t)std::min(max_smem_optin(), 200 * 1024))
+      return set_error(TPRF_ERR_UNSUPPORTED_SIZE, "fourier_lattice_noalloc: mesh dimension too long for one CTA");
+  }
+  unsigned char *scratch = nullptr;
+  st = noalloc_scratch_address(&scratch);
+  if (st) return st;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  size_t off = 0;
+  for (int i = 0; i < nl; ++i) {
+    const int n = lens[i];
+    double2 *tw = reinterpret_cast<double2 *>(scratch + off);
+    float4 *twf = reinterpret_cast<float4 *>(tw + n);
+    int *rev = reinterpret_cast<int *>(twf + n);
+    desc[i].tw = tw;
+    desc[i].twf = twf;
+    desc[i].rev = rev;
+    noalloc_tables_kernel<<<(n + 255) / 256, 256, 0, s>>>(desc[i], tw, twf, rev);
+    TPRF_LAUNCH_CHECK("noalloc_tables_kernel");
+    off += noalloc_table_bytes(n);
+  }
+  const long nk = (long)dims[0] * dims[1] * dims[2];
+  const double2 *src = reinterpret_cast<const double2 *>(in);
+  double2 *dst = reinterpret_cast<double2 *>(out);
+  if (nl == 0) {
+    if (src != dst) TPRF_CUDA(cudaMemcpyAsync(dst, src, n_w * n_target * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+    return TPRF_OK;
+  }
+  int first_nontrivial = 0;
+  while (dims[first_nontrivial] <= 1) ++first_nontrivial;
+  const bool fp64 = arith_mode() == kArithFP64;
+  for (int ax = 2; ax >= 0; --ax) {
+    const int n = dims[ax];
+    if (n <= 1) continue;
+    const FftDesc *d = nullptr;
+    for (int i = 0; i < nl; ++i)
+      if (lens[i] == n) d = &desc[i];
+    long outer = n_w, inner = n_target;
+    for (int a2 = 0; a2 < ax; ++a2) outer *= dims[a2];
+    for (int a2 = ax + 1; a2 < 3; ++a2) inner *= dims[a2];
+    const double scale = (forward && ax == first_nontrivial) ? 1.0 / (double)nk : 1.0;
+    if (forward)
+      st = fp64 ? noalloc_axis<true, double2>(src, dst, outer, inner, *d, scale, s)
+                : noalloc_axis<true, cdf>(src, dst, outer, inner, *d, scale, s);
+    else
+      st = fp64 ? noalloc_axis<false, double2>(src, dst, outer, inner, *d, scale, s)
+                : noalloc_axis<false, cdf>(src, dst, outer, inner, *d, scale, s);
+    if (st) return st;
+    src = dst;
+  }
   return TPRF_OK;
 }
