@@ -394,6 +394,87 @@ def run_gpu(args):
         print(json.dumps(line), flush=True)
 
 
+def run_gpu_batched(args):
+    """cfg2: 512 uneven instances (1-band / 2-orbital square lattices, k in
+    {8..48}^2, beta in [5, 40], n_max with beta) through tprf_batch_run, one
+    graph launch per step; the plain single-instance API path on the same
+    instances is timed beside it."""
+    import numpy as np
+    import torch
+
+    import tprf_gb300 as T
+    from tprf_gb300 import _native, workloads
+    from tprf_gb300.batch import BatchedRPA, RPAInstance
+    from tprf_gb300.tight_binding import ek_tensor
+
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    lib = _native.lib()
+    specs = workloads.batched_instances(512, seed=0)
+    insts = [RPAInstance(e_k=ek_tensor(d["hoppings"], d["dims"], device=dev), U=d["U"], dims=d["dims"],
+                         beta=d["beta"], mu=d["mu"], n_max=d["n_max"], nw=d["nw"]) for d in specs]
+    lib.tprf_set_sync_checks(0)
+    batch = BatchedRPA(insts, n_streams=args.streams, device=dev)
+    points = batch.points
+    stream = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        batch.run()
+    torch.cuda.synchronize()
+    check = _native.check
+    check(lib.tprf_check_device_status(stream.cuda_stream), "warm-up")
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler(local)
+    barrier(world, dev)
+    torch.cuda.synchronize()
+    with clocks:
+        e0.record(stream)
+        for _ in range(args.steps):
+            batch.run()
+        e1.record(stream)
+        torch.cuda.synchronize()
+    barrier(world, dev)
+    ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, world, dev)
+    value = world * points / (ms / 1e3)
+    # the plain single-instance path: the reference's loop, one instance after the other, public API
+    lib.tprf_set_sync_checks(1)
+    n_plain = min(len(insts), 128)
+    plain_pts = sum(a.points for a in insts[:n_plain])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for a in insts[:n_plain]:
+        g0 = T.lattice_dyson_g0_wk(a.mu, T.Gf(mesh=T.MeshBrZone(dims=a.dims), data=a.e_k),
+                                   T.MeshImFreq(a.beta, "Fermion", a.n_max))
+        T.solve_rpa_PH(T.imtime_bubble_chi0_wk(g0, nw=a.nw, verbose=False), a.U)
+    torch.cuda.synchronize()
+    plain = plain_pts / (time.perf_counter() - t0)
+    nb_counts = {nb: sum(1 for a in insts if a.nb == nb) for nb in (1, 2)}
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
+        "data": "synthetic (seeded tight-binding models)",
+        "config": {"workload": "batched_512_square_lattice_instances", "instances": len(insts),
+                   "nb_counts": nb_counts, "k_meshes": "{8,16,24,32,48}^2", "beta": "U[5,40]",
+                   "n_max": "7-smooth nearest 12.8 beta in [32,512]", "points_per_step": points,
+                   "streams": args.streams, "launch": "one CUDA graph launch per step",
+                   "parallelism": f"replicas x{world}"},
+        "plain_single_instance": {"value": plain, "unit": UNIT, "instances_timed": n_plain,
+                                  "path": "lattice_dyson_g0_wk -> imtime_bubble_chi0_wk -> solve_rpa_PH per instance"},
+        "speedup_vs_plain_single_instance": value / plain,
+        "gpu_launches": None,
+        "clocks": clocks.summary(),
+    }
+    batch.close()
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def measure_fp64_peak(lib, dev) -> float:
     """Live FP64 FMA throughput of this GPU (TFLOP/s), the denominator of the FP64 fractions."""
     import ctypes
@@ -461,11 +542,14 @@ def main():
     ap.add_argument("--config", default="cfg1")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
+    ap.add_argument("--streams", type=int, default=32, help="concurrent streams of the batched graph (cfg2)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.config == "cfg2":
+        run_gpu_batched(args)
     else:
         run_gpu(args)
 

@@ -203,6 +203,39 @@ int tprf_imtime_bubble_chi0_wk(double beta, int n_iw, int n_tau, int nw, const i
                                double *chi0_wk, void *workspace, size_t workspace_bytes,
                                void *stream);
 
+/* ---- batched instances --------------------------------------------------------
+ * Many independent instances of the whole path (Dyson -> k->r -> iv->tau ->
+ * bubble + tau->iw -> r->q -> RPA), each with its own beta, mu, meshes, nb and
+ * vertex, run by one graph launch. The reference runs instances one call at
+ * a time (a Python loop over lattice_dyson_g0_wk / imtime_bubble_chi0_wk /
+ * solve_rpa_PH, python/triqs_tprf/lattice_utils.py:191-269, rpa.cpp:29-68);
+ * this is the batched form of that loop. Per instance: e_k [N_k, nb, nb],
+ * U [nb^4], chi [2 nw - 1, N_k, nb^4] (device pointers, caller owned);
+ * n_tau = -1 selects 6 n_iw + 1; nw == 1 uses the trapezoid (static) branch. */
+typedef struct {
+  double beta, mu;
+  int n_iw, n_tau, nw, nb;
+  int dims[3];
+  const double *e_k;
+  const double *U;
+  double *chi;
+} tprf_instance;
+typedef struct tprf_batch tprf_batch;
+
+/* Workspace for tprf_batch_create with n_streams concurrent streams: each
+ * stream reuses one slot sized for its largest instance. */
+size_t tprf_batch_workspace_bytes(const tprf_instance *inst, int n, int n_streams);
+/* Plans every instance, runs it once (eagerly, to build the plans), then
+ * captures all instances, spread longest-first over n_streams streams, into
+ * one CUDA graph. The instance array is copied; the device buffers it points
+ * to and the workspace must stay valid until tprf_batch_destroy. */
+int tprf_batch_create(const tprf_instance *inst, int n, int n_streams, void *workspace, size_t workspace_bytes,
+                      tprf_batch **out);
+/* One graph launch on `stream` computing chi for every instance. */
+int tprf_batch_run(tprf_batch *batch, void *stream);
+int tprf_batch_size(const tprf_batch *batch);
+int tprf_batch_destroy(tprf_batch *batch);
+
 #ifdef __cplusplus
 }
 #endif

@@ -16,6 +16,14 @@ _lib = None
 c_int, c_long, c_double, c_void_p, c_size_t = ctypes.c_int, ctypes.c_long, ctypes.c_double, ctypes.c_void_p, ctypes.c_size_t
 c_int3 = ctypes.c_int * 3
 
+
+class Instance(ctypes.Structure):
+    """C layout of tprf_instance (include/tprf_gb300.h)."""
+    _fields_ = [("beta", ctypes.c_double), ("mu", ctypes.c_double), ("n_iw", ctypes.c_int), ("n_tau", ctypes.c_int),
+                ("nw", ctypes.c_int), ("nb", ctypes.c_int), ("dims", ctypes.c_int * 3), ("e_k", ctypes.c_void_p),
+                ("U", ctypes.c_void_p), ("chi", ctypes.c_void_p)]
+
+
 # name -> (restype, argtypes); mirrors include/tprf_gb300.h
 SIGNATURES = {
     "tprf_status_string": (ctypes.c_char_p, [c_int]),
@@ -42,6 +50,12 @@ SIGNATURES = {
     "tprf_chi_wr_from_chi_tr": (c_int, [c_double, c_int, c_int, c_long, c_long, c_void_p, c_void_p, c_void_p]),
     "tprf_chi_w0r_from_chi_tr": (c_int, [c_double, c_int, c_long, c_long, c_void_p, c_void_p, c_void_p]),
     "tprf_solve_rpa_PH": (c_int, [c_long, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "tprf_batch_workspace_bytes": (c_size_t, [ctypes.POINTER(Instance), c_int, c_int]),
+    "tprf_batch_create": (c_int, [ctypes.POINTER(Instance), c_int, c_int, c_void_p, c_size_t,
+                                  ctypes.POINTER(c_void_p)]),
+    "tprf_batch_run": (c_int, [c_void_p, c_void_p]),
+    "tprf_batch_size": (c_int, [c_void_p]),
+    "tprf_batch_destroy": (c_int, [c_void_p]),
     "tprf_imtime_bubble_workspace_bytes": (c_size_t, [c_int, c_int, c_int3, c_int]),
     "tprf_imtime_bubble_chi0_wk": (c_int, [c_double, c_int, c_int, c_int, c_int3, c_int, c_void_p, c_void_p,
                                            c_void_p, c_void_p, c_size_t, c_void_p]),

@@ -84,8 +84,7 @@ __global__ void __launch_bounds__(kMatsubaraThreads, 2) nu_to_tau_kernel(NuTauPl
   const int L = p.L, n_iw = p.n_iw, nnu = 2 * p.n_iw;
   const int *rev = p.fft.rev;
   C *b = p.fft.has_generic ? a + (size_t)L * ic : nullptr;
-  C *coef = a + (size_t)(p.fft.has_generic ? 2 : 1) * L * ic;  // [n_mom <= 10][ic]
-  C *am = coef + 10 * ic;                                       // [4][ic]: a1, a2, a3, m1
+  C *am = a + (size_t)(p.fft.has_generic ? 2 : 1) * L * ic;  // [4][ic]: a1, a2, a3, m1; then the fit coefficients
   const int tid = threadIdx.x, nthr = blockDim.x;
   const long col0 = blockIdx.x * (long)ic;
   const int ncol = (int)min((long)ic, Ccols - col0);
@@ -100,31 +99,32 @@ __global__ void __launch_bounds__(kMatsubaraThreads, 2) nu_to_tau_kernel(NuTauPl
   }
   __syncthreads();
   if (mom == nullptr) {
+    // The least-squares fit is ill-conditioned for short meshes, so it runs in
+    // FP64 on the original complex128 data (not on the double-float copy).
     const int nf = p.n_fit, nm = p.n_mom;
+    double2 *coef = reinterpret_cast<double2 *>(am + 4 * ic);  // [n_mom <= 10][ic]
     for (int w = tid; w < nm * ic; w += nthr) {
       const int c = w & (ic - 1), q = w >> lg;
-      C acc = czero<C>();
-      for (int i = 0; i < nf; ++i) {
-        const int row = rev[(p.fit_row[i] - n_iw + L) % L];
-        acc = cadd(acc, cmul(table<C>(p.fitF, p.fitFf, q * nf + i), a[row * ic + c]));
-      }
+      double2 acc = make_double2(0.0, 0.0);
+      if (c < ncol)
+        for (int i = 0; i < nf; ++i) acc = cfma(p.fitF[q * nf + i], gw[(long)p.fit_row[i] * Ccols + col0 + c], acc);
       coef[q * ic + c] = acc;
     }
     __syncthreads();
     for (int w = tid; w < nf * ic; w += nthr) {
       const int c = w & (ic - 1), i = w >> lg;
       if (c >= ncol) continue;
-      C model = czero<C>();
-      for (int q = 0; q < nm; ++q) model = cadd(model, cmul(table<C>(p.fitG, p.fitGf, i * nm + q), coef[q * ic + c]));
-      const int row = rev[(p.fit_row[i] - n_iw + L) % L];
-      atomicMax(&s_res, __float_as_uint(cabsf_approx(csub(model, a[row * ic + c]))));
+      double2 model = make_double2(0.0, 0.0);
+      for (int q = 0; q < nm; ++q) model = cfma(p.fitG[i * nm + q], coef[q * ic + c], model);
+      const double2 d = csub(model, gw[(long)p.fit_row[i] * Ccols + col0 + c]);
+      atomicMax(&s_res, __float_as_uint((float)sqrt(cabs2(d))));
     }
     for (int c = tid; c < ic; c += nthr) {
-      const C m1 = coef[1 * ic + c], m2 = coef[2 * ic + c], m3 = coef[3 * ic + c];
-      am[0 * ic + c] = csub(m1, m3);
-      am[1 * ic + c] = cscale(cadd(m2, m3), kc<C>(0.5));
-      am[2 * ic + c] = cscale(csub(m3, m2), kc<C>(0.5));
-      am[3 * ic + c] = m1;
+      const double2 m1 = coef[1 * ic + c], m2 = coef[2 * ic + c], m3 = coef[3 * ic + c];
+      am[0 * ic + c] = from_d2<C>(csub(m1, m3));
+      am[1 * ic + c] = from_d2<C>(cscale(cadd(m2, m3), 0.5));
+      am[2 * ic + c] = from_d2<C>(cscale(csub(m3, m2), 0.5));
+      am[3 * ic + c] = from_d2<C>(m1);
     }
   } else {
     for (int c = tid; c < ic; c += nthr) {
@@ -244,16 +244,23 @@ __global__ void __launch_bounds__(kMatsubaraThreads, 2) tau_to_w_kernel(TauWPlan
   }
   __syncthreads();
   const double dtau = p.beta / (double)(p.n_tau - 1);
+  // fit_derivatives differentiates and then applies the inverse Vandermonde
+  // matrix, which amplifies rounding: its 18 samples are taken in FP64 from
+  // the source, not from the double-float copy in shared memory.
   for (int c = tid; c < ic; c += nthr) {
-    const double2 g0 = as_d2(a[rev[0] * ic + c]), gL = as_d2(last[c]);
+    if (c >= ncol) {
+      am[c] = am[ic + c] = am[2 * ic + c] = czero<C>();
+      continue;
+    }
+    const long col = col0 + c;
+    const double2 g0 = ld(0, col), gL = ld(L, col);
     double2 gl0 = make_double2(0.0, 0.0), gl1 = gl0, gr0 = gl0, gr1 = gl0;
 #pragma unroll
     for (int m = 0; m < 8; ++m) {
       const double tau_m = (double)(m + 1) * dtau;
-      const int rl = m + 1, rr = L - 1 - m;
-      const double2 xl = (rl < L) ? as_d2(a[rev[rl] * ic + c]) : gL;
+      const double2 xl = ld(m + 1, col);
       const double2 dl = make_double2((xl.x - g0.x) / tau_m, (xl.y - g0.y) / tau_m);
-      const double2 xr = as_d2(a[rev[rr] * ic + c]);
+      const double2 xr = ld(L - 1 - m, col);
       const double2 dr = make_double2((gL.x - xr.x) / tau_m, (gL.y - xr.y) / tau_m);
       gl0 = make_double2(fma(vr.r0[m], dl.x, gl0.x), fma(vr.r0[m], dl.y, gl0.y));
       gl1 = make_double2(fma(vr.r1[m], dl.x, gl1.x), fma(vr.r1[m], dl.y, gl1.y));

@@ -91,6 +91,43 @@ CONFIGS = {
 }
 
 
+def smooth7_near(x: float, lo: int, hi: int) -> int:
+    """The 7-smooth integer in [lo, hi] closest to x (FFT-friendly frequency counts)."""
+    cands = [n for n in range(lo, hi + 1) if _smooth7(n)]
+    return min(cands, key=lambda n: (abs(n - x), n))
+
+
+def _smooth7(n: int) -> bool:
+    for p in (2, 3, 5, 7):
+        while n % p == 0:
+            n //= p
+    return n == 1
+
+
+def batched_instances(n: int = 512, seed: int = 0):
+    """cfg2: n instances of the 1-band and 2-orbital square lattices.
+
+    k meshes drawn from {8, 16, 24, 32, 48}^2, beta ~ U[5, 40], mu ~ U[-1, 1],
+    U ~ U[0.5, 2.5] (2-orbital: Kanamori spin vertex with J = U / 10); the
+    fermionic frequency count scales with beta, n_max = the 7-smooth integer
+    nearest 12.8 beta in [32, 512], and nw = n_max. Returns dicts.
+    """
+    rng = np.random.default_rng(seed)
+    two = square_2orb(0)
+    out = []
+    for _ in range(n):
+        nb = int(rng.integers(1, 3))
+        L = int(rng.choice([8, 16, 24, 32, 48]))
+        beta = float(rng.uniform(5.0, 40.0))
+        mu = float(rng.uniform(-1.0, 1.0))
+        U = float(rng.uniform(0.5, 2.5))
+        n_max = smooth7_near(12.8 * beta, 32, 512)
+        hop = square_1band(1.0) if nb == 1 else two
+        vertex = np.full((1, 1, 1, 1), U + 0j) if nb == 1 else kanamori_spin_vertex(2, U, U / 10)
+        out.append(dict(hoppings=hop, dims=(L, L, 1), beta=beta, mu=mu, n_max=n_max, nw=n_max, U=vertex, nb=nb))
+    return out
+
+
 def config(key: str, **overrides) -> dict:
     c = dict(CONFIGS[key])
     c["hoppings"] = c.pop("hop")()
