@@ -203,6 +203,37 @@ int tprf_imtime_bubble_chi0_wk(double beta, int n_iw, int n_tau, int nw, const i
                                double *chi0_wk, void *workspace, size_t workspace_bytes,
                                void *stream);
 
+/* ---- adjoints (differentiable path) ---------------------------------------------
+ * Gradients for a real loss, in the conjugate-Wirtinger convention (for a
+ * linear map y = M x, x_grad = M^H y_grad), used by the torch.autograd
+ * function of the Python package. The reference has no derivatives; each
+ * entry point is the transpose of the forward entry point named.
+ *  - tprf_solve_rpa_PH_adjoint: transpose of tprf_solve_rpa_PH. Writes
+ *    chi0_grad = A^-H chi_grad (I + U chi)^H per point (A = I - chi0 U,
+ *    PH-grouped) and ADDS sum_points chi^H chi_grad chi^H to U_grad [nb^4]
+ *    (zero it first). nb <= 3.
+ *  - tprf_chi_wr_from_chi_tr_adjoint: transpose of tprf_chi_wr_from_chi_tr
+ *    (FFT part and fit_derivatives tail terms).
+ *  - tprf_chi0_tr_from_grt_PH_adjoint: transpose (in the bubble's first
+ *    argument, by the product rule over both G factors) of
+ *    tprf_chi0_tr_from_grt_PH: g_tr_grad [n_tau, N_r, nb, nb].
+ *  - tprf_fourier_wr_to_tr_adjoint: transpose of tprf_fourier_wr_to_tr, with
+ *    the moments from the tail fit (fitted = 1) or held fixed (fitted = 0).
+ *  - tprf_lattice_dyson_g_wk_adjoint: e_k_grad[k] = sum_v G^H G_grad G^H.
+ * The lattice FFTs are their own adjoints up to scaling: the transpose of
+ * k -> r (1/N_k FFTW_FORWARD) is tprf_fourier_wr_to_wk / N_k, that of r -> k
+ * is N_k tprf_fourier_wk_to_wr. */
+int tprf_solve_rpa_PH_adjoint(long n_points, int nb, const double *chi0, const double *U, const double *chi,
+                              const double *chi_grad, double *chi0_grad, double *U_grad, void *stream);
+int tprf_chi_wr_from_chi_tr_adjoint(double beta, int n_tau, int nw, long n_r, long n_target,
+                                    const double *chi_wr_grad, double *chi_tr_grad, void *stream);
+int tprf_chi0_tr_from_grt_PH_adjoint(int n_tau, const int dims[3], int nb, const double *g_tr,
+                                     const double *chi0_tr_grad, double *g_tr_grad, void *stream);
+int tprf_fourier_wr_to_tr_adjoint(double beta, int n_iw, int n_tau, long n_r, long n_target,
+                                  const double *g_tr_grad, int fitted, double *g_wr_grad, void *stream);
+int tprf_lattice_dyson_g_wk_adjoint(int n_iw, long n_k, int nb, const double *g_wk, const double *g_wk_grad,
+                                    double *e_k_grad, void *stream);
+
 /* ---- batched instances --------------------------------------------------------
  * Many independent instances of the whole path (Dyson -> k->r -> iv->tau ->
  * bubble + tau->iw -> r->q -> RPA), each with its own beta, mu, meshes, nb and

@@ -50,6 +50,14 @@ SIGNATURES = {
     "tprf_chi_wr_from_chi_tr": (c_int, [c_double, c_int, c_int, c_long, c_long, c_void_p, c_void_p, c_void_p]),
     "tprf_chi_w0r_from_chi_tr": (c_int, [c_double, c_int, c_long, c_long, c_void_p, c_void_p, c_void_p]),
     "tprf_solve_rpa_PH": (c_int, [c_long, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "tprf_solve_rpa_PH_adjoint": (c_int, [c_long, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                          c_void_p]),
+    "tprf_chi_wr_from_chi_tr_adjoint": (c_int, [c_double, c_int, c_int, c_long, c_long, c_void_p, c_void_p,
+                                                c_void_p]),
+    "tprf_chi0_tr_from_grt_PH_adjoint": (c_int, [c_int, c_int3, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "tprf_fourier_wr_to_tr_adjoint": (c_int, [c_double, c_int, c_int, c_long, c_long, c_void_p, c_int, c_void_p,
+                                              c_void_p]),
+    "tprf_lattice_dyson_g_wk_adjoint": (c_int, [c_int, c_long, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
     "tprf_batch_workspace_bytes": (c_size_t, [ctypes.POINTER(Instance), c_int, c_int]),
     "tprf_batch_create": (c_int, [ctypes.POINTER(Instance), c_int, c_int, c_void_p, c_size_t,
                                   ctypes.POINTER(c_void_p)]),

@@ -10,6 +10,8 @@
 // compile-time indices with predicated selects and the final column
 // permutation is folded into the store addresses, so the matrix stays in
 // registers (nb <= 5; larger nb spill but stay correct).
+#include <algorithm>
+
 #include "common.cuh"
 
 namespace tprf {
@@ -170,4 +172,79 @@ extern "C" int tprf_lattice_dyson_g_wk(double beta, int n_iw, long n_k, int nb, 
                         reinterpret_cast<const double2 *>(sigma), sigma_kind, reinterpret_cast<double2 *>(g_wk), s);
   if (st) return st;
   return finish_with_checks(s, "lattice_dyson_g_wk");
+}
+
+// ---- adjoint (differentiable path) ----------------------------------------------
+// G = [(iv + mu) I - e(k)]^-1 gives dG = G de G, so for a real loss with gradient
+// Gg = dL/dG (conjugate Wirtinger convention, as torch uses) the gradient of e(k)
+// is sum_v G^H Gg G^H. One thread per k sums over the frequencies.
+
+namespace tprf {
+namespace {
+
+template <int NB>
+__global__ void __launch_bounds__(128) dyson_adjoint_kernel(int n_nu, long n_k, const double2 *__restrict__ g,
+                                                            const double2 *__restrict__ gg, double2 *__restrict__ ekg) {
+  for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n_k; k += (long)gridDim.x * blockDim.x) {
+    double2 acc[NB][NB];
+#pragma unroll
+    for (int i = 0; i < NB; ++i)
+#pragma unroll
+      for (int j = 0; j < NB; ++j) acc[i][j] = make_double2(0.0, 0.0);
+    for (int n = 0; n < n_nu; ++n) {
+      const double2 *G = g + ((long)n * n_k + k) * NB * NB;
+      const double2 *Y = gg + ((long)n * n_k + k) * NB * NB;
+      // T = Gg G^H, then acc += G^H T
+      double2 T[NB][NB];
+#pragma unroll
+      for (int i = 0; i < NB; ++i)
+#pragma unroll
+        for (int j = 0; j < NB; ++j) {
+          double2 s = make_double2(0.0, 0.0);
+#pragma unroll
+          for (int l = 0; l < NB; ++l) s = cfma(Y[i * NB + l], cconj(G[j * NB + l]), s);
+          T[i][j] = s;
+        }
+#pragma unroll
+      for (int i = 0; i < NB; ++i)
+#pragma unroll
+        for (int j = 0; j < NB; ++j)
+#pragma unroll
+          for (int l = 0; l < NB; ++l) acc[i][j] = cfma(cconj(G[l * NB + i]), T[l][j], acc[i][j]);
+    }
+#pragma unroll
+    for (int i = 0; i < NB; ++i)
+#pragma unroll
+      for (int j = 0; j < NB; ++j) ekg[k * NB * NB + i * NB + j] = acc[i][j];
+  }
+}
+
+template <int NB>
+int launch_dyson_adjoint_nb(int n_nu, long n_k, const double2 *g, const double2 *gg, double2 *ekg, cudaStream_t s) {
+  long blocks = (n_k + 127) / 128;
+  blocks = std::max(1L, std::min(blocks, (long)num_sms() * 16));
+  dyson_adjoint_kernel<NB><<<(unsigned)blocks, 128, 0, s>>>(n_nu, n_k, g, gg, ekg);
+  TPRF_LAUNCH_CHECK("dyson_adjoint_kernel");
+  return TPRF_OK;
+}
+
+}  // namespace
+}  // namespace tprf
+
+extern "C" int tprf_lattice_dyson_g_wk_adjoint(int n_iw, long n_k, int nb, const double *g_wk, const double *g_wk_grad,
+                                               double *e_k_grad, void *stream) {
+  using namespace tprf;
+  if (n_iw < 1 || n_k < 1 || !g_wk || !g_wk_grad || !e_k_grad)
+    return set_error(TPRF_ERR_INVALID_ARGUMENT, "lattice_dyson_g_wk_adjoint: bad shape or null pointer");
+  const double2 *g = reinterpret_cast<const double2 *>(g_wk), *gg = reinterpret_cast<const double2 *>(g_wk_grad);
+  double2 *out = reinterpret_cast<double2 *>(e_k_grad);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  switch (nb) {
+    case 1: return launch_dyson_adjoint_nb<1>(2 * n_iw, n_k, g, gg, out, s);
+    case 2: return launch_dyson_adjoint_nb<2>(2 * n_iw, n_k, g, gg, out, s);
+    case 3: return launch_dyson_adjoint_nb<3>(2 * n_iw, n_k, g, gg, out, s);
+    case 4: return launch_dyson_adjoint_nb<4>(2 * n_iw, n_k, g, gg, out, s);
+    case 5: return launch_dyson_adjoint_nb<5>(2 * n_iw, n_k, g, gg, out, s);
+    default: return set_error(TPRF_ERR_INVALID_ARGUMENT, "lattice_dyson_g_wk_adjoint: nb must be 1..5");
+  }
 }

@@ -385,6 +385,162 @@ int check_bubble(int n_tau, const int dims[3], int nb, const void *g, const void
   return TPRF_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Adjoints (transposed linear maps) for the differentiable path, in FP64.
+
+// tau -> i omega is linear in chi(tau): chi(i w_m) = (beta/L) sum_{t<L} g_t e^{+2 pi i t k_m / L}
+// + sum_j a_j K[j][m], with a = C m and the moments m linear in the 18 end samples
+// (m1 = -(g_0 - g_L), m2/m3 from fit_derivatives). Its transpose maps the output
+// gradient y to: (beta/L) FFT_FORWARD(y placed at rows k_m)[t] for t < L, plus
+// the moment terms D^T C^T (K^H y) on the end samples.
+__global__ void __launch_bounds__(256) tau_to_w_adjoint_kernel(TauWPlan p, VinvRows vr, const double2 *__restrict__ yg,
+                                                               double2 *__restrict__ xg, long Ccols, int ic, int lg) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double2 *a = reinterpret_cast<double2 *>(smem_raw);
+  const int L = p.L, nw = p.nw, nwt = 2 * p.nw - 1;
+  const int *rev = p.fft.rev;
+  double2 *b = p.fft.has_generic ? a + (size_t)L * ic : nullptr;
+  double2 *ends = a + (size_t)(p.fft.has_generic ? 2 : 1) * L * ic;  // [18][ic]: rows 0..8 and L-8..L
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  const long col0 = blockIdx.x * (long)ic;
+  const int ncol = (int)min((long)ic, Ccols - col0);
+  for (int w = tid; w < L * ic; w += nthr) a[w] = make_double2(0.0, 0.0);
+  __syncthreads();
+  for (int w = tid; w < nwt * ic; w += nthr) {
+    const int c = w & (ic - 1), mi = w >> lg;
+    if (c < ncol) a[rev[(mi - (nw - 1) + L) % L] * ic + c] = yg[(long)mi * Ccols + col0 + c];
+  }
+  const double dtau = p.beta / (double)(p.n_tau - 1);
+  for (int c = tid; c < ic; c += nthr) {
+    double2 e[18];
+#pragma unroll
+    for (int q = 0; q < 18; ++q) e[q] = make_double2(0.0, 0.0);
+    if (c < ncol) {
+      double2 v[3] = {make_double2(0.0, 0.0), make_double2(0.0, 0.0), make_double2(0.0, 0.0)};
+      for (int mi = 0; mi < nwt; ++mi) {
+        const double2 y = yg[(long)mi * Ccols + col0 + c];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) v[j] = cfma(cconj(p.K[j * nwt + mi]), y, v[j]);
+      }
+      // a1 = 4(m1 - m3)/3, a2 = m3 - (m1 + m2)/2, a3 = m1/6 + m2/2 + m3/3: transpose
+      const double2 m1g = cadd(cadd(cscale(v[0], 4.0 / 3.0), cscale(v[1], -0.5)), cscale(v[2], 1.0 / 6.0));
+      const double2 m2g = cadd(cscale(v[1], -0.5), cscale(v[2], 0.5));
+      const double2 m3g = cadd(cadd(cscale(v[0], -4.0 / 3.0), v[1]), cscale(v[2], 1.0 / 3.0));
+      // m1 = -(g0 - gL); m2 = gl0 - gr0; m3 = -(gl1 + gr1) 2/dtau
+      e[0] = csub(e[0], m1g);
+      e[17] = cadd(e[17], m1g);
+      const double2 gl0g = m2g, gr0g = cscale(m2g, -1.0);
+      const double2 gl1g = cscale(m3g, -2.0 / dtau), gr1g = gl1g;
+#pragma unroll
+      for (int m = 0; m < 8; ++m) {
+        const double tau_m = (double)(m + 1) * dtau;
+        const double2 dlg = cscale(cadd(cscale(gl0g, vr.r0[m]), cscale(gl1g, vr.r1[m])), 1.0 / tau_m);
+        const double2 drg = cscale(cadd(cscale(gr0g, vr.r0[m]), cscale(gr1g, vr.r1[m])), 1.0 / tau_m);
+        e[m + 1] = cadd(e[m + 1], dlg);  // dl[m] = (g[m+1] - g[0]) / tau
+        e[0] = csub(e[0], dlg);
+        e[17] = cadd(e[17], drg);        // dr[m] = (g[L] - g[L-1-m]) / tau
+        e[16 - m] = csub(e[16 - m], drg);  // slot 9 + s holds row L - 8 + s; row L-1-m -> s = 7 - m
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 18; ++q) ends[q * ic + c] = e[q];
+  }
+  double2 *r = fft_smem<true>(a, b, p.fft, ic);
+  const double fact = p.beta / (double)L;
+  for (int w = tid; w < (L + 1) * ic; w += nthr) {
+    const int c = w & (ic - 1), t = w >> lg;
+    if (c >= ncol) continue;
+    double2 v = (t < L) ? cscale(r[t * ic + c], fact) : make_double2(0.0, 0.0);
+    if (t <= 8) v = cadd(v, ends[t * ic + c]);
+    if (t >= L - 8) v = cadd(v, ends[(9 + t - (L - 8)) * ic + c]);
+    xg[(long)t * Ccols + col0 + c] = v;
+  }
+}
+
+// iv -> tau is linear in G(iv): G(tau_t) = P[t] F[t] + sum_j a_j Q[j][t] (t < L),
+// G[L] = -(G[0] + m1), F = FFT_FORWARD of g placed at rows (n+L)%L, a = Cf m,
+// m = Fit g[fit rows] (when fitted). Transpose: y_0 -= y_L; BACKWARD FFT of
+// conj(P) y at rows (n+L)%L; plus Fit^H Cf^T (Q^H y) on the fit rows.
+__global__ void __launch_bounds__(256) nu_to_tau_adjoint_kernel(NuTauPlan p, const double2 *__restrict__ yg,
+                                                                double2 *__restrict__ gg, long Ccols, int ic, int lg,
+                                                                int fitted) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double2 *a = reinterpret_cast<double2 *>(smem_raw);
+  const int L = p.L, n_iw = p.n_iw, nnu = 2 * p.n_iw;
+  const int *rev = p.fft.rev;
+  double2 *b = p.fft.has_generic ? a + (size_t)L * ic : nullptr;
+  double2 *mg = a + (size_t)(p.fft.has_generic ? 2 : 1) * L * ic;  // [3][ic] moment gradients
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  const long col0 = blockIdx.x * (long)ic;
+  const int ncol = (int)min((long)ic, Ccols - col0);
+  for (int w = tid; w < L * ic; w += nthr) {
+    const int c = w & (ic - 1), t = w >> lg;
+    double2 y = make_double2(0.0, 0.0);
+    if (c < ncol) {
+      y = yg[(long)t * Ccols + col0 + c];
+      if (t == 0) y = csub(y, yg[(long)L * Ccols + col0 + c]);
+    }
+    a[rev[t] * ic + c] = cmul(cconj(p.P[t]), y);
+  }
+  for (int c = tid; c < ic; c += nthr) {
+    double2 v[3] = {make_double2(0.0, 0.0), make_double2(0.0, 0.0), make_double2(0.0, 0.0)};
+    double2 yL = make_double2(0.0, 0.0);
+    if (c < ncol && fitted) {
+      yL = yg[(long)L * Ccols + col0 + c];
+      for (int t = 0; t < L; ++t) {
+        double2 y = yg[(long)t * Ccols + col0 + c];
+        if (t == 0) y = csub(y, yL);
+#pragma unroll
+        for (int j = 0; j < 3; ++j) v[j] = cfma(cconj(p.Q[j * L + t]), y, v[j]);
+      }
+    }
+    // a1 = m1 - m3, a2 = (m2 + m3)/2, a3 = (m3 - m2)/2; G[L] adds -m1
+    mg[0 * ic + c] = csub(v[0], yL);
+    mg[1 * ic + c] = cscale(csub(v[1], v[2]), 0.5);
+    mg[2 * ic + c] = cadd(cscale(v[0], -1.0), cscale(cadd(v[1], v[2]), 0.5));
+  }
+  double2 *r = fft_smem<false>(a, b, p.fft, ic);
+  for (int w = tid; w < nnu * ic; w += nthr) {
+    const int c = w & (ic - 1), n = w >> lg;
+    if (c >= ncol) continue;
+    double2 v = r[((n - n_iw + L) % L) * ic + c];
+    if (fitted)
+      for (int i = 0; i < p.n_fit; ++i)
+        if (p.fit_row[i] == n)
+          for (int q = 1; q <= 3; ++q) v = cfma(cconj(p.fitF[q * p.n_fit + i]), mg[(q - 1) * ic + c], v);
+    gg[(long)n * Ccols + col0 + c] = v;
+  }
+}
+
+// Bubble adjoint as a gather: G_grad(tau_i, r)_xy =
+//   sum_bc conj(G_bc(tau_{N-1-i}, -r)) chig_{y b c x}(tau_i, r)
+// + sum_ad conj(G_da(tau_{N-1-i}, -r)) chig_{a x y d}(tau_{N-1-i}, -r).
+__global__ void __launch_bounds__(256) bubble_adjoint_kernel(BubbleLoader ld, const double2 *__restrict__ chig,
+                                                             double2 *__restrict__ gg) {
+  const int nb = ld.nb, nb2 = nb * nb, nb4 = nb2 * nb2;
+  const long Nr = ld.Nr, total = (long)ld.n_tau * Nr * nb2;
+  for (long idx = blockIdx.x * (long)blockDim.x + threadIdx.x; idx < total; idx += (long)gridDim.x * blockDim.x) {
+    const int xy = (int)(idx % nb2);
+    const long r = (idx / nb2) % Nr;
+    const int i = (int)(idx / ((long)nb2 * Nr));
+    const int x = xy / nb, y = xy % nb;
+    const int i2 = (int)(r % ld.d2), i1 = (int)((r / ld.d2) % ld.d1), i0 = (int)(r / ((long)ld.d2 * ld.d1));
+    const long mr = ((long)((ld.d0 - i0) % ld.d0) * ld.d1 + (ld.d1 - i1) % ld.d1) * ld.d2 + (ld.d2 - i2) % ld.d2;
+    const int im = ld.n_tau - 1 - i;
+    const double2 *gm = ld.g + ((long)im * Nr + mr) * nb2;  // G(tau_{N-1-i}, -r)
+    const double2 *c1 = chig + ((long)i * Nr + r) * nb4;
+    const double2 *c2 = chig + ((long)im * Nr + mr) * nb4;
+    double2 acc = make_double2(0.0, 0.0);
+    for (int bb = 0; bb < nb; ++bb)
+      for (int cc = 0; cc < nb; ++cc)
+        acc = cfma(cconj(gm[bb * nb + cc]), c1[((y * nb + bb) * nb + cc) * nb + x], acc);
+    for (int aa = 0; aa < nb; ++aa)
+      for (int dd = 0; dd < nb; ++dd)
+        acc = cfma(cconj(gm[dd * nb + aa]), c2[((aa * nb + x) * nb + y) * nb + dd], acc);
+    gg[idx] = acc;
+  }
+}
+
 }  // namespace
 
 // ---- internal launchers (no synchronisation) --------------------------------
@@ -521,5 +677,62 @@ extern "C" int tprf_chi0_w0r_from_grt_PH(double beta, int n_tau, const int dims[
                                 reinterpret_cast<double2 *>(chi0_wr), static_cast<cudaStream_t>(stream));
   if (st) return st;
   TPRF_LAUNCH_CHECK("chi0_w0r_from_grt_PH");
+  return TPRF_OK;
+}
+
+// ---- adjoints (differentiable path) -------------------------------------------
+
+extern "C" int tprf_chi_wr_from_chi_tr_adjoint(double beta, int n_tau, int nw, long n_r, long n_target,
+                                               const double *chi_wr_grad, double *chi_tr_grad, void *stream) {
+  if (!chi_wr_grad || !chi_tr_grad || n_r < 1 || n_target < 1)
+    return set_error(TPRF_ERR_INVALID_ARGUMENT, "chi_wr_from_chi_tr_adjoint: bad shape or null pointer");
+  int st = check_tau_w(beta, n_tau, nw);
+  if (st) return st;
+  const TauWPlan *p = nullptr;
+  if ((st = get_tau_w_plan(beta, n_tau, nw, &p))) return st;
+  const long C = n_r * n_target;
+  int ic, lg;
+  size_t smem;
+  if ((st = pick_ic(p->fft, 18 * sizeof(double2), &ic, &lg, &smem))) return st;
+  TPRF_CUDA(cudaFuncSetAttribute(tau_to_w_adjoint_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  tau_to_w_adjoint_kernel<<<(unsigned)((C + ic - 1) / ic), 256, smem, static_cast<cudaStream_t>(stream)>>>(
+      *p, make_vinv_rows(), reinterpret_cast<const double2 *>(chi_wr_grad), reinterpret_cast<double2 *>(chi_tr_grad),
+      C, ic, lg);
+  TPRF_LAUNCH_CHECK("tau_to_w_adjoint_kernel");
+  return TPRF_OK;
+}
+
+extern "C" int tprf_fourier_wr_to_tr_adjoint(double beta, int n_iw, int n_tau, long n_r, long n_target,
+                                             const double *g_tr_grad, int fitted, double *g_wr_grad, void *stream) {
+  if (!g_tr_grad || !g_wr_grad || n_r < 1 || n_target < 1 || n_iw < 1 || !(beta > 0.0))
+    return set_error(TPRF_ERR_INVALID_ARGUMENT, "fourier_wr_to_tr_adjoint: bad shape or null pointer");
+  if (n_tau < 0) n_tau = default_n_tau(n_iw);
+  if (n_tau - 1 < 2 * n_iw)
+    return set_error(TPRF_ERR_MESH_TOO_SHORT, "Inverse Fourier: the time mesh must be at least twice as long as the freq mesh");
+  const NuTauPlan *p = nullptr;
+  int st = get_nu_tau_plan(beta, n_iw, n_tau, &p);
+  if (st) return st;
+  const long C = n_r * n_target;
+  int ic, lg;
+  size_t smem;
+  if ((st = pick_ic(p->fft, 3 * sizeof(double2), &ic, &lg, &smem))) return st;
+  TPRF_CUDA(cudaFuncSetAttribute(nu_to_tau_adjoint_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  nu_to_tau_adjoint_kernel<<<(unsigned)((C + ic - 1) / ic), 256, smem, static_cast<cudaStream_t>(stream)>>>(
+      *p, reinterpret_cast<const double2 *>(g_tr_grad), reinterpret_cast<double2 *>(g_wr_grad), C, ic, lg,
+      fitted ? 1 : 0);
+  TPRF_LAUNCH_CHECK("nu_to_tau_adjoint_kernel");
+  return TPRF_OK;
+}
+
+extern "C" int tprf_chi0_tr_from_grt_PH_adjoint(int n_tau, const int dims[3], int nb, const double *g_tr,
+                                                const double *chi0_tr_grad, double *g_tr_grad, void *stream) {
+  int st = check_bubble(n_tau, dims, nb, g_tr, g_tr_grad);
+  if (st) return st;
+  if (!chi0_tr_grad) return set_error(TPRF_ERR_INVALID_ARGUMENT, "bubble adjoint: null gradient");
+  const BubbleLoader ld = make_bubble(reinterpret_cast<const double2 *>(g_tr), n_tau, dims, nb);
+  const long total = (long)n_tau * ld.Nr * nb * nb;
+  bubble_adjoint_kernel<<<(unsigned)grid_for(total, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+      ld, reinterpret_cast<const double2 *>(chi0_tr_grad), reinterpret_cast<double2 *>(g_tr_grad));
+  TPRF_LAUNCH_CHECK("bubble_adjoint_kernel");
   return TPRF_OK;
 }

@@ -461,3 +461,177 @@ extern "C" int tprf_solve_rpa_PH(long n_points, int nb, const double *chi0, cons
   if (st) return st;
   return finish_with_checks(s, "solve_rpa_PH");
 }
+
+// ---- adjoint (differentiable path) ----------------------------------------------
+// chi = A^-1 chi0 with A = I - chi0 U (PH-grouped matrices) gives
+// d chi = A^-1 d chi0 (I + U chi) + chi dU chi. For a real loss with gradient
+// Y = dL/d chi (conjugate Wirtinger convention): chi0_grad = A^-H Y (I + U chi)^H
+// and U_grad = sum over points of chi^H Y chi^H. One thread per point, FP64;
+// U_grad is accumulated with atomics into a caller-zeroed [nb^4] buffer.
+
+namespace tprf {
+namespace {
+
+template <int NB>
+__global__ void __launch_bounds__(128) rpa_adjoint_kernel(long n_points, const double2 *__restrict__ chi0,
+                                                          const double2 *__restrict__ Uin,
+                                                          const double2 *__restrict__ chi,
+                                                          const double2 *__restrict__ chig,
+                                                          double2 *__restrict__ chi0g, double2 *Ug, unsigned *status) {
+  constexpr int N = NB * NB;
+  __shared__ double2 Us[N * N];
+  __shared__ double Uacc[2 * N * N];
+  for (int w = threadIdx.x; w < N * N; w += blockDim.x) {
+    Us[w] = Uin[(w / N) * N + colmap<NB>(w % N)];
+    Uacc[2 * w] = Uacc[2 * w + 1] = 0.0;
+  }
+  __syncthreads();
+  double2 ug[N][N];
+#pragma unroll
+  for (int i = 0; i < N; ++i)
+#pragma unroll
+    for (int j = 0; j < N; ++j) ug[i][j] = make_double2(0.0, 0.0);
+  for (long pt = blockIdx.x * (long)blockDim.x + threadIdx.x; pt < n_points; pt += (long)gridDim.x * blockDim.x) {
+    const long o = pt * N * N;
+    double2 A[N][N], Y[N][N], X[N][N];
+    // A^H = I - U^H chi0^H, solved with partial pivoting: A^H Z = Y
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+#pragma unroll
+      for (int j = 0; j < N; ++j) {
+        double2 s = make_double2(i == j ? 1.0 : 0.0, 0.0);
+#pragma unroll
+        for (int m = 0; m < N; ++m) s = cfms(cconj(Us[m * N + i]), cconj(chi0[o + j * N + colmap<NB>(m)]), s);
+        A[i][j] = s;
+        Y[i][j] = chig[o + i * N + colmap<NB>(j)];
+        X[i][j] = chi[o + i * N + colmap<NB>(j)];
+      }
+    bool singular = false;
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+      int p = j;
+      double best = cabs2(A[j][j]);
+#pragma unroll
+      for (int i = j + 1; i < N; ++i)
+        if (cabs2(A[i][j]) > best) {
+          best = cabs2(A[i][j]);
+          p = i;
+        }
+      if (best == 0.0) singular = true;
+#pragma unroll
+      for (int i = j + 1; i < N; ++i)
+        if (i == p) {
+#pragma unroll
+          for (int k = 0; k < N; ++k) {
+            double2 t = A[i][k];
+            A[i][k] = A[j][k];
+            A[j][k] = t;
+            t = Y[i][k];
+            Y[i][k] = Y[j][k];
+            Y[j][k] = t;
+          }
+        }
+      const double2 inv = crecip(A[j][j]);
+      A[j][j] = inv;
+#pragma unroll
+      for (int i = j + 1; i < N; ++i) {
+        const double2 f = cmul(A[i][j], inv);
+#pragma unroll
+        for (int k = j + 1; k < N; ++k) A[i][k] = cfms(f, A[j][k], A[i][k]);
+#pragma unroll
+        for (int k = 0; k < N; ++k) Y[i][k] = cfms(f, Y[j][k], Y[i][k]);
+      }
+    }
+#pragma unroll
+    for (int jj = 0; jj < N; ++jj) {
+      const int j = N - 1 - jj;
+#pragma unroll
+      for (int k = 0; k < N; ++k) {
+        double2 s = Y[j][k];
+#pragma unroll
+        for (int l = j + 1; l < N; ++l) s = cfms(A[j][l], Y[l][k], s);
+        Y[j][k] = cmul(s, A[j][j]);
+      }
+    }
+    if (singular) atomicOr(status, kDevErrSingular);
+    // B = I + U chi; chi0_grad = Z B^H
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+#pragma unroll
+      for (int j = 0; j < N; ++j) {
+        // (B^H)_{l j} = conj(B_{j l}) = delta + conj(sum_m U_{j m} chi_{m l})
+        double2 s = make_double2(0.0, 0.0);
+#pragma unroll
+        for (int l = 0; l < N; ++l) {
+          double2 bjl = make_double2(j == l ? 1.0 : 0.0, 0.0);
+#pragma unroll
+          for (int m = 0; m < N; ++m) bjl = cfma(Us[j * N + m], X[m][l], bjl);
+          s = cfma(Y[i][l], cconj(bjl), s);
+        }
+        chi0g[o + i * N + colmap<NB>(j)] = s;
+      }
+    // U_grad += chi^H Y_in chi^H (Y_in re-read: Y now holds Z)
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+#pragma unroll
+      for (int j = 0; j < N; ++j) {
+        double2 s = make_double2(0.0, 0.0);
+#pragma unroll
+        for (int l = 0; l < N; ++l) {
+          double2 t = make_double2(0.0, 0.0);  // (Y chi^H)_{l j}
+#pragma unroll
+          for (int m = 0; m < N; ++m) t = cfma(chig[o + l * N + colmap<NB>(m)], cconj(X[j][m]), t);
+          s = cfma(cconj(X[l][i]), t, s);
+        }
+        ug[i][j] = cadd(ug[i][j], s);
+      }
+  }
+#pragma unroll
+  for (int i = 0; i < N; ++i)
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+      atomicAdd(&Uacc[2 * (i * N + j)], ug[i][j].x);
+      atomicAdd(&Uacc[2 * (i * N + j) + 1], ug[i][j].y);
+    }
+  __syncthreads();
+  for (int w = threadIdx.x; w < N * N; w += blockDim.x) {
+    // grouped (m, c) -> tensor offset m * N + colmap(c)
+    const int off = (w / N) * N + colmap<NB>(w % N);
+    atomicAdd(&reinterpret_cast<double *>(Ug)[2 * off], Uacc[2 * w]);
+    atomicAdd(&reinterpret_cast<double *>(Ug)[2 * off + 1], Uacc[2 * w + 1]);
+  }
+}
+
+template <int NB>
+int launch_rpa_adjoint_nb(long n_points, const double2 *chi0, const double2 *U, const double2 *chi,
+                          const double2 *chig, double2 *chi0g, double2 *Ug, cudaStream_t s, unsigned *status) {
+  long blocks = (n_points + 127) / 128;
+  blocks = std::max(1L, std::min(blocks, (long)num_sms() * 8));
+  rpa_adjoint_kernel<NB><<<(unsigned)blocks, 128, 0, s>>>(n_points, chi0, U, chi, chig, chi0g, Ug, status);
+  TPRF_LAUNCH_CHECK("rpa_adjoint_kernel");
+  return TPRF_OK;
+}
+
+}  // namespace
+}  // namespace tprf
+
+extern "C" int tprf_solve_rpa_PH_adjoint(long n_points, int nb, const double *chi0, const double *U, const double *chi,
+                                         const double *chi_grad, double *chi0_grad, double *U_grad, void *stream) {
+  using namespace tprf;
+  if (n_points < 1 || !chi0 || !U || !chi || !chi_grad || !chi0_grad || !U_grad)
+    return set_error(TPRF_ERR_INVALID_ARGUMENT, "solve_rpa_PH_adjoint: bad shape or null pointer");
+  unsigned *status = device_status_word();
+  if (!status) return TPRF_ERR_CUDA;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  auto c = [](const double *p) { return reinterpret_cast<const double2 *>(p); };
+  double2 *g0 = reinterpret_cast<double2 *>(chi0_grad), *ug = reinterpret_cast<double2 *>(U_grad);
+  int st;
+  switch (nb) {
+    case 1: st = launch_rpa_adjoint_nb<1>(n_points, c(chi0), c(U), c(chi), c(chi_grad), g0, ug, s, status); break;
+    case 2: st = launch_rpa_adjoint_nb<2>(n_points, c(chi0), c(U), c(chi), c(chi_grad), g0, ug, s, status); break;
+    case 3: st = launch_rpa_adjoint_nb<3>(n_points, c(chi0), c(U), c(chi), c(chi_grad), g0, ug, s, status); break;
+    default: return set_error(TPRF_ERR_INVALID_ARGUMENT, "solve_rpa_PH_adjoint: nb must be 1..3");
+  }
+  if (st) return st;
+  return finish_with_checks(s, "solve_rpa_PH_adjoint");
+}

@@ -128,6 +128,36 @@ def batched_instances(n: int = 512, seed: int = 0):
     return out
 
 
+def cfg3_model(dims=(32, 32, 1), beta=16.0, n_max=128, nw=128, seed=0):
+    """cfg3: the 2-orbital square lattice with 8 seeded hopping amplitudes t(R).
+
+    Pattern a is a seeded real 2 x 2 matrix T_a on a lattice vector R_a (two
+    per R in (1,0), (0,1), (1,1), (1,-1)) with its Hermitian partner on -R_a;
+    theta_a multiplies it. Returns (HoppingModel, theta0 [8], U [2,2,2,2]).
+    """
+    from .autodiff import HoppingModel
+    rng = np.random.default_rng(seed + 7)
+    patterns = []
+    for R in [(1, 0), (0, 1), (1, 1), (1, -1)]:
+        for _ in range(2):
+            T = rng.standard_normal((2, 2))
+            patterns.append({R: T, tuple(-x for x in R): T.T})
+    theta0 = 0.1 * rng.standard_normal(len(patterns))
+    model = HoppingModel(base=square_2orb(seed), patterns=patterns, dims=dims, beta=beta, mu=0.0, n_max=n_max, nw=nw)
+    return model, theta0, kanamori_spin_vertex(2, 1.2, 0.2)
+
+
+def cfg3_loss(chi):
+    """Re Tr chi(q = (pi, pi), i w = 0) over the PH-grouped matrix, plus sum |chi|^2."""
+    nwt, nk = chi.shape[0], chi.shape[1]
+    n1 = int(round(np.sqrt(nk)))
+    q = (n1 // 2) * n1 + n1 // 2
+    static = chi[nwt // 2, q]
+    nb = chi.shape[-1]
+    tr = sum(static[a, b, b, a] for a in range(nb) for b in range(nb))
+    return tr.real + (chi.abs() ** 2).sum()
+
+
 def config(key: str, **overrides) -> dict:
     c = dict(CONFIGS[key])
     c["hoppings"] = c.pop("hop")()
