@@ -475,6 +475,88 @@ def run_gpu_batched(args):
         print(json.dumps(line), flush=True)
 
 
+def run_gpu_grad(args):
+    """cfg3: chi(q, iw) plus the gradient of Re Tr chi(q=(pi,pi), iw=0) + sum |chi|^2
+    with respect to U and 8 hopping amplitudes, through tprf_gb300.autodiff (forward
+    kernels, then the hand-written adjoint kernels). One step = forward + backward.
+    The forward pass alone is timed beside it."""
+    import torch
+
+    from tprf_gb300 import _native
+    from tprf_gb300.autodiff import chi_rpa
+    from tprf_gb300.workloads import cfg3_loss, cfg3_model
+
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    lib = _native.lib()
+    lib.tprf_set_sync_checks(0)
+    model, theta0, U0 = cfg3_model()
+    nk = int(math.prod(model.dims))
+    points = (2 * model.nw - 1) * nk
+    theta_h = torch.as_tensor(theta0, dtype=torch.float64).pin_memory()
+    U_h = torch.as_tensor(U0, dtype=torch.complex128).pin_memory()
+    grads_h = torch.empty(len(theta0) + 2 * U0.size, dtype=torch.float64, pin_memory=True)
+    loss_h = torch.empty(1, dtype=torch.float64, pin_memory=True)
+    stream = torch.cuda.current_stream()
+
+    def step(backward=True):
+        theta = theta_h.to(dev, non_blocking=True).requires_grad_(backward)
+        U = U_h.to(dev, non_blocking=True).requires_grad_(backward)
+        L = cfg3_loss(chi_rpa(theta, U, model))
+        if backward:
+            L.backward()
+            g = torch.cat([theta.grad, torch.view_as_real(U.grad).reshape(-1)])
+            grads_h.copy_(g, non_blocking=True)
+        loss_h.copy_(L.detach().reshape(1), non_blocking=True)
+
+    def timed(backward):
+        for _ in range(args.warmup):
+            step(backward)
+        torch.cuda.synchronize()
+        barrier(world, dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0 = time.perf_counter()
+        e0.record(stream)
+        for _ in range(args.steps):
+            step(backward)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        wall = (time.perf_counter() - t0) / args.steps
+        return max_over_ranks(e0.elapsed_time(e1) / args.steps, world, dev), max_over_ranks(wall, world, dev)
+
+    fwd_ms, _ = timed(False)
+    clocks = ClockSampler(local)
+    with clocks:
+        ms, wall_s = timed(True)
+    _native.check(lib.tprf_check_device_status(stream.cuda_stream), "timed steps")
+    nb = model.patterns[0][(1, 0)].shape[0]
+    line = {
+        "metric": "RPA chi(q,iw) + dL/dU, dL/dt(R) points/s (complex128)", "value": world * points / (ms / 1e3),
+        "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
+        "data": "synthetic (seeded 2-orbital square lattice, 8 seeded hopping patterns)",
+        "config": {"workload": "grad_2orb_square_32x32", "dims": list(model.dims), "nb": nb, "beta": model.beta,
+                   "n_max": model.n_max, "nw": model.nw, "points_per_step": points,
+                   "loss": "Re Tr chi(q=(pi,pi), iw=0) + sum |chi|^2", "parameters": "U [2,2,2,2] complex, 8 real t(R) amplitudes",
+                   "parallelism": f"replicas x{world}"},
+        "forward_only": {"value": world * points / (fwd_ms / 1e3), "unit": UNIT, "ms_per_step": fwd_ms},
+        "e2e": {"value": world * points / wall_s, "unit": UNIT,
+                "h2d_bytes_per_step": int(theta_h.numel() * 8 + U_h.numel() * 16),
+                "d2h_bytes_per_step": int(grads_h.numel() * 8 + 8)},
+        "gpu_launches": None,
+        "clocks": clocks.summary(),
+    }
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def measure_fp64_peak(lib, dev) -> float:
     """Live FP64 FMA throughput of this GPU (TFLOP/s), the denominator of the FP64 fractions."""
     import ctypes
@@ -492,8 +574,9 @@ def measure_fp64_peak(lib, dev) -> float:
 # profiles/ (16x16x8 case, 2048 r points), scaled to 32^3 (x16) by the number of r
 # points: the kernels stream their columns, so traffic grows in proportion.
 TRAFFIC = {
-    ("cfg1", "bubble_tau_to_w"): 16 * 2.183e9,  # profiles/tau_to_w_bubble_cubic3orb_16x16x8.md
-    ("cfg1", "rpa"): 16 * 2.665e9,              # profiles/rpa_kernel_cubic3orb_16x16x8.md
+    ("cfg1", "bubble_tau_to_w"): 16 * 2.176e9,  # profiles/tau_to_w_bubble_cubic3orb_16x16x8.md
+    ("cfg1", "rpa"): 16 * 2.774e9,              # profiles/rpa_coop_cubic3orb_16x16x8.md
+    ("cfg1", "fft_r_to_q"): 3 * 16 * 2.653e9,   # profiles/lattice_axis_r_to_q_cubic3orb_16x16x8.md (3 passes)
 }
 
 
@@ -550,6 +633,8 @@ def main():
         run_reference(args)
     elif args.config == "cfg2":
         run_gpu_batched(args)
+    elif args.config == "cfg3":
+        run_gpu_grad(args)
     else:
         run_gpu(args)
 
