@@ -187,9 +187,22 @@ int tprf_chi_w0r_from_chi_tr(double beta, int n_tau, long n_r, long n_target,
  * Replaces triqs_tprf::solve_rpa_PH(chi_wk_vt, array_contiguous_view<dcomplex,4>)
  *   (lattice/rpa.hpp:43, rpa.cpp:29-68).
  * chi0 [n_points, nb, nb, nb, nb], U [nb, nb, nb, nb] -> chi (same as chi0).
- * nb <= 5. */
+ * nb <= 8. */
 int tprf_solve_rpa_PH(long n_points, int nb, const double *chi0, const double *U,
                       double *chi, void *stream);
+
+/* solve_rpa_PH with chi written to HOST memory, as the reference's C++ function
+ * returns it (rpa.cpp:29-68 returns a host gf). The points are solved in chunks
+ * of `chunk_points` into a device ring held in `workspace` (one slot per chunk of
+ * tprf_solve_rpa_PH_to_host_workspace_bytes(chunk_points, nb, 1); up to 16 slots
+ * are used), and each solved chunk is copied to chi_host on an internal copy
+ * stream while the next one is solved. chi_host should be pinned (page-locked)
+ * for the copies to overlap. Stream-ordered: `stream` waits for the last copy.
+ * Calls are serialised by a process-wide lock while they enqueue. */
+size_t tprf_solve_rpa_PH_to_host_workspace_bytes(long chunk_points, int nb, int slots);
+int tprf_solve_rpa_PH_to_host(long n_points, int nb, const double *chi0, const double *U,
+                              double *chi_host, long chunk_points, void *workspace,
+                              size_t workspace_bytes, void *stream);
 
 /* ---- whole chain ------------------------------------------------------------
  * g_wk -> chi0_wk as triqs_tprf.lattice_utils.imtime_bubble_chi0_wk

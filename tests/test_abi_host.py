@@ -77,6 +77,10 @@ def test_argument_errors_are_reported_without_a_gpu(lib):
                                           None) == -7
     with pytest.raises(_native.TprfError):
         _native.check(lib.tprf_solve_rpa_PH(0, 2, fake, fake, fake, None), "solve_rpa_PH")
+    # streamed RPA: a workspace smaller than one chunk is rejected before any CUDA call
+    assert lib.tprf_solve_rpa_PH_to_host_workspace_bytes(10, 3, 2) == 2 * 10 * 81 * 16 + 256
+    assert lib.tprf_solve_rpa_PH_to_host(100, 3, fake, fake, fake, 10, fake, 1000, None) == -1
+    assert "chunk" in lib.tprf_last_error().decode()
 
 
 def test_workspace_size(lib):

@@ -205,7 +205,7 @@ def test_bubble_variants(cuda_lib, case):
 # ---------------------------------------------------------------------------
 # (d) RPA
 
-@pytest.mark.parametrize("nb", [1, 2, 3, 4, 5])
+@pytest.mark.parametrize("nb", [1, 2, 3, 4, 5, 6, 8])
 def test_rpa_random(cuda_lib, nb):
     T = tp()
     rng = np.random.default_rng(10 + nb)
@@ -215,6 +215,28 @@ def test_rpa_random(cuda_lib, nb):
     mesh = T.MeshProduct(T.MeshImFreq(1.0, "Boson", 2), T.MeshBrZone(dims=(npts // 3, 1, 1)))
     chi = T.solve_rpa_PH(T.Gf(mesh=mesh, data=chi0), U)
     assert rel_err(chi.data, O.solve_rpa_PH(chi0, U)) < PARITY_RTOL
+
+
+@pytest.mark.parametrize("nb,chunk,slots", [(1, 7, 2), (2, 50, 3), (3, 64, 1), (3, 1000, 3)])
+def test_rpa_streamed_to_host(cuda_lib, nb, chunk, slots):
+    """solve_rpa_PH(out=host) (chunks through a device ring, copies overlapped) gives
+    the same bits as the device-resident solve, for ragged last chunks and a
+    one-slot ring."""
+    T = tp()
+    rng = np.random.default_rng(40 + nb)
+    chi0 = 0.1 * rand_c(rng, 7, 43, nb, nb, nb, nb)
+    U = 0.5 * rand_c(rng, nb, nb, nb, nb)
+    mesh = T.MeshProduct(T.MeshImFreq(1.0, "Boson", 4), T.MeshBrZone(dims=(43, 1, 1)))
+    g = T.Gf(mesh=mesh, data=chi0)
+    ref = T.solve_rpa_PH(g, U).data.cpu()
+    out = torch.full(tuple(chi0.shape), complex("nan"), dtype=torch.complex128).pin_memory()
+    ws = torch.empty(cuda_lib.tprf_solve_rpa_PH_to_host_workspace_bytes(chunk, nb, slots), dtype=torch.uint8,
+                     device="cuda")
+    res = T.solve_rpa_PH(g, U, out=out, chunk_points=chunk, workspace=ws)
+    torch.cuda.synchronize()
+    assert res.data.data_ptr() == out.data_ptr()
+    assert torch.equal(out, ref)
+    assert rel_err(out.numpy(), O.solve_rpa_PH(chi0, U)) < PARITY_RTOL
 
 
 @pytest.mark.parametrize("gap", [1e-2, 1e-4, 1e-6])

@@ -7,7 +7,11 @@
 // solved without forming the inverse: A = I - chi0 U, then Gaussian
 // elimination with partial pivoting on [A | chi0] and back substitution.
 //
-// Design: one thread per point. A = I - chi0 U is formed from the non-zeros of
+// Kernels by vertex size: nb = 1, 2 one thread per point (below); nb = 3 four
+// lanes per point (rpa_coop_kernel); nb >= 4 one warp per point
+// (rpa_warp.cu, which also holds the adjoint).
+//
+// Design of the thread-per-point kernel: A = I - chi0 U is formed from the non-zeros of
 // U only (compacted once per CTA into shared memory), LU-factorised with
 // partial pivoting in the thread's slice of shared memory ([element][thread]
 // layout: conflict-free although every thread pivots independently), and the
@@ -16,43 +20,13 @@
 // factors in shared memory halves the per-thread footprint of a full
 // [A | chi0] elimination, which doubles the warps per SM.
 #include <algorithm>
+#include <cstdint>
+#include <mutex>
 
-#include "common.cuh"
+#include "rpa_common.cuh"
 
 namespace tprf {
 namespace {
-
-template <int NB>
-__device__ __forceinline__ int colmap(int c) {  // grouped column (d, c') -> offset c' * nb + d
-  return (c % NB) * NB + c / NB;
-}
-
-// element-type plumbing: double2 (FP64) or cdf (double-float)
-__device__ __forceinline__ double2 el_from(double2 z, double2 *) { return z; }
-__device__ __forceinline__ cdf el_from(double2 z, cdf *) { return to_cdf(z); }
-__device__ __forceinline__ double2 el_to(double2 z) { return z; }
-__device__ __forceinline__ double2 el_to(cdf z) { return to_double2(z); }
-__device__ __forceinline__ double2 el_one(double2 *) { return make_double2(1.0, 0.0); }
-__device__ __forceinline__ cdf el_one(cdf *) { return cdf{dfl{1.f, 0.f}, dfl{0.f, 0.f}}; }
-__device__ __forceinline__ double2 el_zero(double2 *) { return make_double2(0.0, 0.0); }
-__device__ __forceinline__ cdf el_zero(cdf *) { return cdf{dfl{0.f, 0.f}, dfl{0.f, 0.f}}; }
-__device__ __forceinline__ double el_abs2(double2 z) { return cabs2(z); }
-__device__ __forceinline__ double el_abs2(cdf z) { return (double)(z.x.hi * z.x.hi + z.y.hi * z.y.hi); }
-__device__ __forceinline__ float el_absf(double2 z) { return (float)sqrt(cabs2(z)); }
-__device__ __forceinline__ float el_absf(cdf z) { return sqrtf(z.x.hi * z.x.hi + z.y.hi * z.y.hi); }
-template <class E> struct IsDf { static constexpr bool value = false; };
-template <> struct IsDf<cdf> { static constexpr bool value = true; };
-__device__ __forceinline__ double2 el_fms(double2 a, double2 b, double2 acc) { return cfms(a, b, acc); }
-__device__ __forceinline__ cdf el_fms(cdf a, cdf b, cdf acc) { return csub(acc, cmul(a, b)); }
-__device__ __forceinline__ double2 el_recip(double2 a) { return crecip(a); }
-__device__ __forceinline__ cdf el_recip(cdf a) {
-  // 1/(x + iy) = (x - iy) / (x^2 + y^2); the real reciprocal by one Newton step from the float one
-  const dfl d = ddot_add(a.x, a.x, a.y, a.y);
-  const float r0 = __frcp_rn(d.hi);
-  const dfl e = dsub(dfl{1.f, 0.f}, dmul(d, dfl{r0, 0.f}));
-  const dfl r = dadd(dfl{r0, 0.f}, dmul(dfl{r0, 0.f}, e));
-  return cdf{dmul(a.x, r), dneg(dmul(a.y, r))};
-}
 
 // One (w, q) point: A = I - chi0 U from the non-zeros of U, LU with partial
 // pivoting in the thread's shared-memory slice, then the nb^2 right-hand
@@ -158,12 +132,6 @@ __device__ double rpa_point(const double2 *x, double2 *y, E *A, int *perm, const
   return pmin > 0.0 ? amax / pmin : 1e300;
 }
 
-// Squared conditioning estimate above which a double-float solution is
-// recomputed in FP64: (max|A| / min pivot)^2 > 1e4, i.e. the estimate > 100.
-// Double-float carries ~2^-48 per operation, so below it the solve stays well
-// inside 1e-10 relative; near an RPA instability (1 - chi0 U nearly singular)
-// the point is solved in FP64.
-constexpr double kDf64CondLimit2 = 1e4;
 
 template <int NB, int NT, class E>
 __global__ void __launch_bounds__(NT) rpa_lu_kernel(long n_points, const double2 *chi0, const double2 *__restrict__ U,
@@ -433,6 +401,9 @@ int launch_rpa_coop_as(long n_points, const double2 *chi0, const double2 *U, dou
 
 }  // namespace
 
+int launch_rpa_warp(long n_points, int nb, const double2 *chi0, const double2 *U, double2 *chi, cudaStream_t stream,
+                    unsigned *status);
+
 int launch_rpa(long n_points, int nb, const double2 *chi0, const double2 *U, double2 *chi, cudaStream_t stream) {
   unsigned *status = device_status_word();
   if (!status) return TPRF_ERR_CUDA;
@@ -442,9 +413,9 @@ int launch_rpa(long n_points, int nb, const double2 *chi0, const double2 *U, dou
     case 3:
       if (arith_mode() == kArithFP64) return launch_rpa_coop_as<3, 4, 128, double2>(n_points, chi0, U, chi, stream, status);
       return launch_rpa_coop_as<3, 4, 128, cdf>(n_points, chi0, U, chi, stream, status);
-    case 4: return launch_rpa_nb<4, 32>(n_points, chi0, U, chi, stream, status);
-    case 5: return launch_rpa_nb<5, 16>(n_points, chi0, U, chi, stream, status);
-    default: return set_error(TPRF_ERR_INVALID_ARGUMENT, "solve_rpa_PH: nb must be 1..5");
+    default:
+      if (nb < 1 || nb > 8) return set_error(TPRF_ERR_INVALID_ARGUMENT, "solve_rpa_PH: nb must be 1..8");
+      return launch_rpa_warp(n_points, nb, chi0, U, chi, stream, status);
   }
 }
 
@@ -462,157 +433,100 @@ extern "C" int tprf_solve_rpa_PH(long n_points, int nb, const double *chi0, cons
   return finish_with_checks(s, "solve_rpa_PH");
 }
 
-// ---- adjoint (differentiable path) ----------------------------------------------
-// chi = A^-1 chi0 with A = I - chi0 U (PH-grouped matrices) gives
-// d chi = A^-1 d chi0 (I + U chi) + chi dU chi. For a real loss with gradient
-// Y = dL/d chi (conjugate Wirtinger convention): chi0_grad = A^-H Y (I + U chi)^H
-// and U_grad = sum over points of chi^H Y chi^H. One thread per point, FP64;
-// U_grad is accumulated with atomics into a caller-zeroed [nb^4] buffer.
-
+// ---- RPA with the result streamed to host memory -----------------------------------
+// The reference returns chi as a host-side gf. Here the points are solved in chunks
+// into a small device ring (the caller's workspace) and each chunk is copied to the
+// host buffer on a second stream while the next chunk is solved, so the copy of the
+// result (the largest transfer of the path) overlaps the RPA arithmetic. The caller's
+// stream waits for the last copy: a synchronisation of `stream` means chi is on the host.
 namespace tprf {
 namespace {
+constexpr int kMaxRingSlots = 16;
+constexpr int kMaxDevices = 64;
 
-template <int NB>
-__global__ void __launch_bounds__(128) rpa_adjoint_kernel(long n_points, const double2 *__restrict__ chi0,
-                                                          const double2 *__restrict__ Uin,
-                                                          const double2 *__restrict__ chi,
-                                                          const double2 *__restrict__ chig,
-                                                          double2 *__restrict__ chi0g, double2 *Ug, unsigned *status) {
-  constexpr int N = NB * NB;
-  __shared__ double2 Us[N * N];
-  __shared__ double Uacc[2 * N * N];
-  for (int w = threadIdx.x; w < N * N; w += blockDim.x) {
-    Us[w] = Uin[(w / N) * N + colmap<NB>(w % N)];
-    Uacc[2 * w] = Uacc[2 * w + 1] = 0.0;
-  }
-  __syncthreads();
-  double2 ug[N][N];
-#pragma unroll
-  for (int i = 0; i < N; ++i)
-#pragma unroll
-    for (int j = 0; j < N; ++j) ug[i][j] = make_double2(0.0, 0.0);
-  for (long pt = blockIdx.x * (long)blockDim.x + threadIdx.x; pt < n_points; pt += (long)gridDim.x * blockDim.x) {
-    const long o = pt * N * N;
-    double2 A[N][N], Y[N][N], X[N][N];
-    // A^H = I - U^H chi0^H, solved with partial pivoting: A^H Z = Y
-#pragma unroll
-    for (int i = 0; i < N; ++i)
-#pragma unroll
-      for (int j = 0; j < N; ++j) {
-        double2 s = make_double2(i == j ? 1.0 : 0.0, 0.0);
-#pragma unroll
-        for (int m = 0; m < N; ++m) s = cfms(cconj(Us[m * N + i]), cconj(chi0[o + j * N + colmap<NB>(m)]), s);
-        A[i][j] = s;
-        Y[i][j] = chig[o + i * N + colmap<NB>(j)];
-        X[i][j] = chi[o + i * N + colmap<NB>(j)];
-      }
-    bool singular = false;
-#pragma unroll
-    for (int j = 0; j < N; ++j) {
-      int p = j;
-      double best = cabs2(A[j][j]);
-#pragma unroll
-      for (int i = j + 1; i < N; ++i)
-        if (cabs2(A[i][j]) > best) {
-          best = cabs2(A[i][j]);
-          p = i;
-        }
-      if (best == 0.0) singular = true;
-#pragma unroll
-      for (int i = j + 1; i < N; ++i)
-        if (i == p) {
-#pragma unroll
-          for (int k = 0; k < N; ++k) {
-            double2 t = A[i][k];
-            A[i][k] = A[j][k];
-            A[j][k] = t;
-            t = Y[i][k];
-            Y[i][k] = Y[j][k];
-            Y[j][k] = t;
-          }
-        }
-      const double2 inv = crecip(A[j][j]);
-      A[j][j] = inv;
-#pragma unroll
-      for (int i = j + 1; i < N; ++i) {
-        const double2 f = cmul(A[i][j], inv);
-#pragma unroll
-        for (int k = j + 1; k < N; ++k) A[i][k] = cfms(f, A[j][k], A[i][k]);
-#pragma unroll
-        for (int k = 0; k < N; ++k) Y[i][k] = cfms(f, Y[j][k], Y[i][k]);
-      }
-    }
-#pragma unroll
-    for (int jj = 0; jj < N; ++jj) {
-      const int j = N - 1 - jj;
-#pragma unroll
-      for (int k = 0; k < N; ++k) {
-        double2 s = Y[j][k];
-#pragma unroll
-        for (int l = j + 1; l < N; ++l) s = cfms(A[j][l], Y[l][k], s);
-        Y[j][k] = cmul(s, A[j][j]);
-      }
-    }
-    if (singular) atomicOr(status, kDevErrSingular);
-    // B = I + U chi; chi0_grad = Z B^H
-#pragma unroll
-    for (int i = 0; i < N; ++i)
-#pragma unroll
-      for (int j = 0; j < N; ++j) {
-        // (B^H)_{l j} = conj(B_{j l}) = delta + conj(sum_m U_{j m} chi_{m l})
-        double2 s = make_double2(0.0, 0.0);
-#pragma unroll
-        for (int l = 0; l < N; ++l) {
-          double2 bjl = make_double2(j == l ? 1.0 : 0.0, 0.0);
-#pragma unroll
-          for (int m = 0; m < N; ++m) bjl = cfma(Us[j * N + m], X[m][l], bjl);
-          s = cfma(Y[i][l], cconj(bjl), s);
-        }
-        chi0g[o + i * N + colmap<NB>(j)] = s;
-      }
-    // U_grad += chi^H Y_in chi^H (Y_in re-read: Y now holds Z)
-#pragma unroll
-    for (int i = 0; i < N; ++i)
-#pragma unroll
-      for (int j = 0; j < N; ++j) {
-        double2 s = make_double2(0.0, 0.0);
-#pragma unroll
-        for (int l = 0; l < N; ++l) {
-          double2 t = make_double2(0.0, 0.0);  // (Y chi^H)_{l j}
-#pragma unroll
-          for (int m = 0; m < N; ++m) t = cfma(chig[o + l * N + colmap<NB>(m)], cconj(X[j][m]), t);
-          s = cfma(cconj(X[l][i]), t, s);
-        }
-        ug[i][j] = cadd(ug[i][j], s);
-      }
-  }
-#pragma unroll
-  for (int i = 0; i < N; ++i)
-#pragma unroll
-    for (int j = 0; j < N; ++j) {
-      atomicAdd(&Uacc[2 * (i * N + j)], ug[i][j].x);
-      atomicAdd(&Uacc[2 * (i * N + j) + 1], ug[i][j].y);
-    }
-  __syncthreads();
-  for (int w = threadIdx.x; w < N * N; w += blockDim.x) {
-    // grouped (m, c) -> tensor offset m * N + colmap(c)
-    const int off = (w / N) * N + colmap<NB>(w % N);
-    atomicAdd(&reinterpret_cast<double *>(Ug)[2 * off], Uacc[2 * w]);
-    atomicAdd(&reinterpret_cast<double *>(Ug)[2 * off + 1], Uacc[2 * w + 1]);
-  }
-}
+struct HostOutCtx {
+  bool ready = false;
+  cudaStream_t copy = nullptr;
+  cudaEvent_t computed[kMaxRingSlots], copied[kMaxRingSlots], done;
+};
+std::mutex g_host_out_mu;
+HostOutCtx g_host_out[kMaxDevices];
 
-template <int NB>
-int launch_rpa_adjoint_nb(long n_points, const double2 *chi0, const double2 *U, const double2 *chi,
-                          const double2 *chig, double2 *chi0g, double2 *Ug, cudaStream_t s, unsigned *status) {
-  long blocks = (n_points + 127) / 128;
-  blocks = std::max(1L, std::min(blocks, (long)num_sms() * 8));
-  rpa_adjoint_kernel<NB><<<(unsigned)blocks, 128, 0, s>>>(n_points, chi0, U, chi, chig, chi0g, Ug, status);
-  TPRF_LAUNCH_CHECK("rpa_adjoint_kernel");
+int host_out_ctx(HostOutCtx **out) {
+  int dev = 0;
+  TPRF_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) return set_error(TPRF_ERR_INVALID_ARGUMENT, "solve_rpa_PH_to_host: device id");
+  HostOutCtx &c = g_host_out[dev];
+  if (!c.ready) {
+    TPRF_CUDA(cudaStreamCreateWithFlags(&c.copy, cudaStreamNonBlocking));
+    for (int i = 0; i < kMaxRingSlots; ++i) {
+      TPRF_CUDA(cudaEventCreateWithFlags(&c.computed[i], cudaEventDisableTiming));
+      TPRF_CUDA(cudaEventCreateWithFlags(&c.copied[i], cudaEventDisableTiming));
+    }
+    TPRF_CUDA(cudaEventCreateWithFlags(&c.done, cudaEventDisableTiming));
+    c.ready = true;
+  }
+  *out = &c;
   return TPRF_OK;
 }
-
 }  // namespace
+}  // namespace tprf
+
+extern "C" size_t tprf_solve_rpa_PH_to_host_workspace_bytes(long chunk_points, int nb, int slots) {
+  if (chunk_points < 1 || nb < 1 || slots < 1) return 0;
+  return (size_t)slots * (size_t)chunk_points * (size_t)nb * nb * nb * nb * sizeof(double2) + 256;
+}
+
+extern "C" int tprf_solve_rpa_PH_to_host(long n_points, int nb, const double *chi0, const double *U, double *chi_host,
+                                         long chunk_points, void *workspace, size_t workspace_bytes, void *stream) {
+  using namespace tprf;
+  if (n_points < 1 || chunk_points < 1 || nb < 1 || !chi0 || !U || !chi_host || !workspace)
+    return set_error(TPRF_ERR_INVALID_ARGUMENT, "solve_rpa_PH_to_host: bad shape or null pointer");
+  const size_t per_point = (size_t)nb * nb * nb * nb;
+  const size_t slot_bytes = (size_t)chunk_points * per_point * sizeof(double2);
+  const uintptr_t base = (reinterpret_cast<uintptr_t>(workspace) + 255) & ~(uintptr_t)255;
+  const size_t usable = workspace_bytes > (base - reinterpret_cast<uintptr_t>(workspace))
+                            ? workspace_bytes - (base - reinterpret_cast<uintptr_t>(workspace))
+                            : 0;
+  const int slots = (int)std::min<size_t>(kMaxRingSlots, usable / slot_bytes);
+  if (slots < 1)
+    return set_error(TPRF_ERR_INVALID_ARGUMENT, "solve_rpa_PH_to_host: workspace smaller than one chunk");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  std::lock_guard<std::mutex> lock(g_host_out_mu);
+  HostOutCtx *c = nullptr;
+  int st = host_out_ctx(&c);
+  if (st) return st;
+  const double2 *src = reinterpret_cast<const double2 *>(chi0);
+  const double2 *u = reinterpret_cast<const double2 *>(U);
+  double2 *host = reinterpret_cast<double2 *>(chi_host);
+  const long n_chunks = (n_points + chunk_points - 1) / chunk_points;
+  for (long k = 0; k < n_chunks; ++k) {
+    const int slot = (int)(k % slots);
+    const long p0 = k * chunk_points, np = std::min(chunk_points, n_points - p0);
+    double2 *ring = reinterpret_cast<double2 *>(base + (size_t)slot * slot_bytes);
+    if (k >= slots) TPRF_CUDA(cudaStreamWaitEvent(s, c->copied[slot], 0));  // the slot's last copy is done
+    st = launch_rpa(np, nb, src + (size_t)p0 * per_point, u, ring, s);
+    if (st) {
+      // let the caller's stream wait for what was already queued, then report
+      cudaEventRecord(c->done, c->copy);
+      cudaStreamWaitEvent(s, c->done, 0);
+      return st;
+    }
+    TPRF_CUDA(cudaEventRecord(c->computed[slot], s));
+    TPRF_CUDA(cudaStreamWaitEvent(c->copy, c->computed[slot], 0));
+    TPRF_CUDA(cudaMemcpyAsync(host + (size_t)p0 * per_point, ring, (size_t)np * per_point * sizeof(double2),
+                              cudaMemcpyDeviceToHost, c->copy));
+    TPRF_CUDA(cudaEventRecord(c->copied[slot], c->copy));
+  }
+  TPRF_CUDA(cudaEventRecord(c->done, c->copy));
+  TPRF_CUDA(cudaStreamWaitEvent(s, c->done, 0));
+  return finish_with_checks(s, "solve_rpa_PH_to_host");
+}
+
+// ---- adjoint (differentiable path): the warp-per-point kernel of rpa_warp.cu ----
+namespace tprf {
+int launch_rpa_adjoint_warp(long n_points, int nb, const double2 *chi0, const double2 *U, const double2 *chi,
+                            const double2 *chig, double2 *chi0g, double2 *Ug, cudaStream_t stream, unsigned *status);
 }  // namespace tprf
 
 extern "C" int tprf_solve_rpa_PH_adjoint(long n_points, int nb, const double *chi0, const double *U, const double *chi,
@@ -625,13 +539,8 @@ extern "C" int tprf_solve_rpa_PH_adjoint(long n_points, int nb, const double *ch
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   auto c = [](const double *p) { return reinterpret_cast<const double2 *>(p); };
   double2 *g0 = reinterpret_cast<double2 *>(chi0_grad), *ug = reinterpret_cast<double2 *>(U_grad);
-  int st;
-  switch (nb) {
-    case 1: st = launch_rpa_adjoint_nb<1>(n_points, c(chi0), c(U), c(chi), c(chi_grad), g0, ug, s, status); break;
-    case 2: st = launch_rpa_adjoint_nb<2>(n_points, c(chi0), c(U), c(chi), c(chi_grad), g0, ug, s, status); break;
-    case 3: st = launch_rpa_adjoint_nb<3>(n_points, c(chi0), c(U), c(chi), c(chi_grad), g0, ug, s, status); break;
-    default: return set_error(TPRF_ERR_INVALID_ARGUMENT, "solve_rpa_PH_adjoint: nb must be 1..3");
-  }
+  if (nb < 1 || nb > 8) return set_error(TPRF_ERR_INVALID_ARGUMENT, "solve_rpa_PH_adjoint: nb must be 1..8");
+  const int st = launch_rpa_adjoint_warp(n_points, nb, c(chi0), c(U), c(chi), c(chi_grad), g0, ug, s, status);
   if (st) return st;
   return finish_with_checks(s, "solve_rpa_PH_adjoint");
 }

@@ -1,0 +1,387 @@
+// Kernel (d) for larger vertices (nb >= 4, N = nb^2 >= 16): one warp per
+// (w, q) point, the matrix size a runtime value.
+//
+// Same mathematics as rpa.cu (c++/triqs_tprf/lattice/rpa.cpp:29-64): with the
+// particle-hole grouping rows (a, b), columns (d, c), chi = (I - chi0 U)^-1 chi0.
+//
+// Design: the warp keeps the augmented matrix M = [A | B] (N x 2N, row major,
+// A = I - chi0 U, B = chi0) of its point in shared memory. Lanes own columns
+// of M, so every row access of the warp touches consecutive 16-byte elements
+// (no bank conflicts). Elimination with partial pivoting (pivot search by warp
+// shuffles, physical row swaps in A and B) turns A into U and B into L^-1 P B;
+// back substitution then runs per B column with no cross-lane dependency. The
+// loops are not unrolled over N: one instantiation per element type serves
+// every nb, and the code stays small. Double-float by default, with the FP64
+// re-solve of points whose conditioning estimate exceeds the double-float
+// limit (the estimate of rpa.cu).
+#include <algorithm>
+
+#include "rpa_common.cuh"
+
+namespace tprf {
+namespace {
+
+struct SparseU {  // U grouped and compacted by columns: rows and FP64 values
+  const double2 *val;
+  const int *row;
+  const int *cs;  // [N + 1] column starts
+};
+
+// the grouped column index of the memory offset m = c' * nb + d inside a row
+__device__ __forceinline__ int col_of_offset(int m, int nb) { return (m % nb) * nb + m / nb; }
+
+template <class E>
+__device__ double rpa_point_warp(const double2 *__restrict__ x, double2 *__restrict__ y, E *M, int N, int nb,
+                                 const SparseU &u, int lane, bool &singular) {
+  const int W = 2 * N;
+#define MM(i, c) M[(i) * W + (c)]
+  // B = chi0 in the grouped layout (coalesced global reads)
+  for (int o = lane; o < N * N; o += 32) MM(o / N, N + col_of_offset(o % N, nb)) = el_from(x[o], (E *)nullptr);
+  __syncwarp();
+  // A = I - X U from the non-zeros of U; the size of the terms bounds cancellation
+  float amax = 0.f;
+  for (int e = lane; e < N * N; e += 32) {
+    const int r = e / N, c = e % N;
+    E s = (r == c) ? el_one((E *)nullptr) : el_zero((E *)nullptr);
+    float mag = (r == c) ? 1.f : 0.f;
+    for (int t = u.cs[c]; t < u.cs[c + 1]; ++t) {
+      const E xv = MM(r, N + u.row[t]);
+      const E uv = el_from(u.val[t], (E *)nullptr);
+      s = el_fms(xv, uv, s);
+      mag = fmaf(el_absf(xv), el_absf(uv), mag);
+    }
+    amax = fmaxf(amax, mag);
+    MM(r, c) = s;
+  }
+  __syncwarp();
+  double pmin = 1e300;
+  bool sing = false;
+  for (int j = 0; j < N; ++j) {
+    int p = j;
+    double best = -1.0;
+    for (int i = j + lane; i < N; i += 32) {
+      const double v = el_abs2(MM(i, j));
+      if (v > best) {
+        best = v;
+        p = i;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+      const int op = __shfl_xor_sync(0xffffffffu, p, o);
+      if (ob > best || (ob == best && op < p)) {
+        best = ob;
+        p = op;
+      }
+    }
+    if (best == 0.0) sing = true;
+    pmin = fmin(pmin, best);
+    if (p != j) {
+      for (int c = lane; c < W; c += 32) {
+        const E t = MM(j, c);
+        MM(j, c) = MM(p, c);
+        MM(p, c) = t;
+      }
+    }
+    __syncwarp();
+    const E inv = el_recip(MM(j, j));
+    for (int i = j + 1 + lane; i < N; i += 32) MM(i, j) = cmul(MM(i, j), inv);
+    __syncwarp();
+    for (int c = j + 1 + lane; c < W; c += 32) {
+      const E piv = MM(j, c);
+#pragma unroll 2
+      for (int i = j + 1; i < N; ++i) MM(i, c) = el_fms(MM(i, j), piv, MM(i, c));
+    }
+    __syncwarp();
+    if (lane == 0) MM(j, j) = inv;
+    __syncwarp();
+  }
+  singular = sing;
+  // back substitution, one B column per lane, then the grouped -> memory store
+  for (int c = N + lane; c < W; c += 32) {
+    for (int j = N - 1; j >= 0; --j) {
+      const E xj = cmul(MM(j, c), MM(j, j));
+      MM(j, c) = xj;
+#pragma unroll 2
+      for (int i = 0; i < j; ++i) MM(i, c) = el_fms(MM(i, j), xj, MM(i, c));
+    }
+  }
+  __syncwarp();
+  for (int o = lane; o < N * N; o += 32) y[o] = el_to(MM(o / N, N + col_of_offset(o % N, nb)));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, o));
+  __syncwarp();
+#undef MM
+  const double am = (double)amax * (double)amax;
+  return pmin > 0.0 ? am / pmin : 1e300;
+}
+
+template <class E>
+__global__ void __launch_bounds__(512) rpa_warp_kernel(long n_points, int nb, const double2 *__restrict__ chi0,
+                                                       const double2 *__restrict__ U, double2 *__restrict__ chi,
+                                                       unsigned *status) {
+  const int N = nb * nb;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double2 *s_val = reinterpret_cast<double2 *>(smem_raw);
+  int *s_row = reinterpret_cast<int *>(s_val + N * N);
+  int *s_cs = s_row + N * N;
+  const size_t u_bytes = ((size_t)N * N * (sizeof(double2) + sizeof(int)) + (N + 1) * sizeof(int) + 15) & ~(size_t)15;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, n_warps = blockDim.x >> 5;
+  E *M = reinterpret_cast<E *>(smem_raw + u_bytes) + (size_t)warp * 2 * N * N;
+  if (threadIdx.x == 0) {
+    int t = 0;
+    for (int c = 0; c < N; ++c) {
+      s_cs[c] = t;
+      for (int m = 0; m < N; ++m) {
+        // grouped U[m][c] = U_{m_a m_b, c_d c_c}: memory offset m * N + offset(c)
+        const double2 v = U[m * N + (c % nb) * nb + c / nb];
+        if (v.x != 0.0 || v.y != 0.0) {
+          s_row[t] = m;
+          s_val[t] = v;
+          ++t;
+        }
+      }
+    }
+    s_cs[N] = t;
+  }
+  __syncthreads();
+  const SparseU u{s_val, s_row, s_cs};
+  for (long pt = (long)blockIdx.x * n_warps + warp; pt < n_points; pt += (long)gridDim.x * n_warps) {
+    const double2 *x = chi0 + pt * N * N;
+    double2 *y = chi + pt * N * N;
+    bool singular = false;
+    const double cond2 = rpa_point_warp<E>(x, y, M, N, nb, u, lane, singular);
+    if (IsDf<E>::value && !(cond2 <= kDf64CondLimit2))
+      rpa_point_warp<double2>(x, y, reinterpret_cast<double2 *>(M), N, nb, u, lane, singular);
+    if (singular && lane == 0) atomicOr(status, kDevErrSingular);
+  }
+}
+
+template <class E>
+int launch_as(long n_points, int nb, const double2 *chi0, const double2 *U, double2 *chi, cudaStream_t stream,
+              unsigned *status) {
+  const int N = nb * nb;
+  const size_t u_bytes = ((size_t)N * N * (sizeof(double2) + sizeof(int)) + (N + 1) * sizeof(int) + 15) & ~(size_t)15;
+  const size_t per_point = (size_t)2 * N * N * 16;
+  const size_t limit = (size_t)max_smem_optin();
+  if (u_bytes + per_point > limit) return set_error(TPRF_ERR_INVALID_ARGUMENT, "solve_rpa_PH: nb too large");
+  TPRF_CUDA(cudaFuncSetAttribute(rpa_warp_kernel<E>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)limit));
+  // the number of warps per CTA that puts the most warps on an SM
+  int best_w = 1, best_total = 0;
+  for (int w = 1; w <= 16; ++w) {
+    const size_t smem = u_bytes + (size_t)w * per_point;
+    if (smem > limit) break;
+    int per_sm = 0;
+    TPRF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, rpa_warp_kernel<E>, 32 * w, smem));
+    if (per_sm * w >= best_total) {
+      best_total = per_sm * w;
+      best_w = w;
+    }
+  }
+  if (best_total == 0) return set_error(TPRF_ERR_INVALID_ARGUMENT, "solve_rpa_PH: nb too large");
+  const size_t smem = u_bytes + (size_t)best_w * per_point;
+  long blocks = (n_points + best_w - 1) / best_w;
+  blocks = std::max(1L, std::min(blocks, (long)num_sms() * (best_total / best_w) * 8));
+  rpa_warp_kernel<E><<<(unsigned)blocks, 32 * best_w, smem, stream>>>(n_points, nb, chi0, U, chi, status);
+  TPRF_LAUNCH_CHECK("rpa_warp_kernel");
+  return TPRF_OK;
+}
+
+// ---- adjoint -------------------------------------------------------------------
+// With A = I - X0 U (grouped) and X = A^-1 X0: d X = A^-1 dX0 (I + U X) + X dU X.
+// For a real loss with conjugate-Wirtinger gradient Y = dL/dX:
+//   X0_grad = Z B^H with A^H Z = Y and B = I + U X,
+//   U_grad  = sum over points of X^H Y X^H.
+// One warp per point in FP64. Per warp, shared memory holds [A^H | Y] (N x 2N,
+// eliminated in place into [U | Z]), X, a copy of Y and the warp's U_grad
+// accumulator (each lane owns its entries, so no atomics inside the warp); the
+// CTA adds its warps' accumulators into U_grad with one atomic per entry.
+__device__ __forceinline__ int grouped_offset(int c, int nb) { return (c % nb) * nb + c / nb; }
+
+__global__ void __launch_bounds__(512) rpa_adjoint_warp_kernel(long n_points, int nb, const double2 *__restrict__ chi0,
+                                                               const double2 *__restrict__ U,
+                                                               const double2 *__restrict__ chi,
+                                                               const double2 *__restrict__ chig,
+                                                               double2 *__restrict__ chi0g, double2 *Ug,
+                                                               unsigned *status) {
+  const int N = nb * nb, W = 2 * N;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double2 *s_val = reinterpret_cast<double2 *>(smem_raw);
+  int *s_row = reinterpret_cast<int *>(s_val + N * N);
+  int *s_col = s_row + N * N;
+  int *s_cs = s_col + N * N;
+  const size_t u_bytes =
+      ((size_t)N * N * (sizeof(double2) + 2 * sizeof(int)) + (N + 1) * sizeof(int) + 15) & ~(size_t)15;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, n_warps = blockDim.x >> 5;
+  double2 *M = reinterpret_cast<double2 *>(smem_raw + u_bytes) + (size_t)warp * 5 * N * N;
+  double2 *Xs = M + 2 * N * N, *Yc = Xs + N * N, *Acc = Yc + N * N;
+  if (threadIdx.x == 0) {
+    int t = 0;
+    for (int c = 0; c < N; ++c) {
+      s_cs[c] = t;
+      for (int m = 0; m < N; ++m) {
+        const double2 v = U[m * N + grouped_offset(c, nb)];
+        if (v.x != 0.0 || v.y != 0.0) {
+          s_row[t] = m;
+          s_col[t] = c;
+          s_val[t] = v;
+          ++t;
+        }
+      }
+    }
+    s_cs[N] = t;
+  }
+  for (int e = lane; e < N * N; e += 32) Acc[e] = make_double2(0.0, 0.0);
+  __syncthreads();
+  const int nnz = s_cs[N];
+#define MM(i, c) M[(i) * W + (c)]
+  for (long pt = (long)blockIdx.x * n_warps + warp; pt < n_points; pt += (long)gridDim.x * n_warps) {
+    const long o = pt * N * N;
+    for (int e = lane; e < N * N; e += 32) {
+      const int r = e / N, c = col_of_offset(e % N, nb);
+      Xs[r * N + c] = chi[o + e];
+      const double2 y = chig[o + e];
+      Yc[r * N + c] = y;
+      MM(r, N + c) = y;
+    }
+    // A^H[i][j] = delta_ij - sum_m conj(U[m][i]) conj(X0[j][m]), U's column i
+    for (int e = lane; e < N * N; e += 32) {
+      const int i = e / N, j = e % N;
+      double2 s = make_double2(i == j ? 1.0 : 0.0, 0.0);
+      for (int t = s_cs[i]; t < s_cs[i + 1]; ++t)
+        s = cfms(cconj(s_val[t]), cconj(chi0[o + j * N + grouped_offset(s_row[t], nb)]), s);
+      MM(i, j) = s;
+    }
+    __syncwarp();
+    bool sing = false;
+    for (int j = 0; j < N; ++j) {
+      int p = j;
+      double best = -1.0;
+      for (int i = j + lane; i < N; i += 32) {
+        const double v = cabs2(MM(i, j));
+        if (v > best) {
+          best = v;
+          p = i;
+        }
+      }
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        const double ob = __shfl_xor_sync(0xffffffffu, best, off);
+        const int op = __shfl_xor_sync(0xffffffffu, p, off);
+        if (ob > best || (ob == best && op < p)) {
+          best = ob;
+          p = op;
+        }
+      }
+      if (best == 0.0) sing = true;
+      if (p != j)
+        for (int c = lane; c < W; c += 32) {
+          const double2 t = MM(j, c);
+          MM(j, c) = MM(p, c);
+          MM(p, c) = t;
+        }
+      __syncwarp();
+      const double2 inv = crecip(MM(j, j));
+      for (int i = j + 1 + lane; i < N; i += 32) MM(i, j) = cmul(MM(i, j), inv);
+      __syncwarp();
+      for (int c = j + 1 + lane; c < W; c += 32) {
+        const double2 piv = MM(j, c);
+        for (int i = j + 1; i < N; ++i) MM(i, c) = cfms(MM(i, j), piv, MM(i, c));
+      }
+      __syncwarp();
+      if (lane == 0) MM(j, j) = inv;
+      __syncwarp();
+    }
+    for (int c = N + lane; c < W; c += 32)
+      for (int j = N - 1; j >= 0; --j) {
+        const double2 zj = cmul(MM(j, c), MM(j, j));
+        MM(j, c) = zj;
+        for (int i = 0; i < j; ++i) MM(i, c) = cfms(MM(i, j), zj, MM(i, c));
+      }
+    __syncwarp();
+    if (sing && lane == 0) atomicOr(status, kDevErrSingular);
+    // B = I + U X into the left half (lane owns column l)
+    for (int l = lane; l < N; l += 32) {
+      for (int r = 0; r < N; ++r) MM(r, l) = make_double2(r == l ? 1.0 : 0.0, 0.0);
+      for (int t = 0; t < nnz; ++t) MM(s_row[t], l) = cfma(s_val[t], Xs[s_col[t] * N + l], MM(s_row[t], l));
+    }
+    __syncwarp();
+    // X0_grad[i][j] = sum_l Z[i][l] conj(B[j][l])
+    for (int e = lane; e < N * N; e += 32) {
+      const int i = e / N, j = e % N;
+      double2 s = make_double2(0.0, 0.0);
+      for (int l = 0; l < N; ++l) s = cfma(MM(i, N + l), cconj(MM(j, l)), s);
+      chi0g[o + i * N + grouped_offset(j, nb)] = s;
+    }
+    __syncwarp();
+    // T = Y X^H into the left half, then Acc += X^H T
+    for (int e = lane; e < N * N; e += 32) {
+      const int l = e / N, j = e % N;
+      double2 s = make_double2(0.0, 0.0);
+      for (int m = 0; m < N; ++m) s = cfma(Yc[l * N + m], cconj(Xs[j * N + m]), s);
+      MM(l, j) = s;
+    }
+    __syncwarp();
+    for (int e = lane; e < N * N; e += 32) {
+      const int i = e / N, j = e % N;
+      double2 s = Acc[e];
+      for (int l = 0; l < N; ++l) s = cfma(cconj(Xs[l * N + i]), MM(l, j), s);
+      Acc[e] = s;
+    }
+    __syncwarp();
+  }
+#undef MM
+  __syncthreads();
+  for (int e = threadIdx.x; e < N * N; e += blockDim.x) {
+    double2 s = make_double2(0.0, 0.0);
+    for (int w = 0; w < n_warps; ++w) {
+      const double2 *a = reinterpret_cast<double2 *>(smem_raw + u_bytes) + (size_t)w * 5 * N * N + 4 * N * N;
+      s = cadd(s, a[e]);
+    }
+    // grouped (m, c) -> tensor offset m * N + offset(c)
+    const int off = (e / N) * N + grouped_offset(e % N, nb);
+    atomicAdd(&reinterpret_cast<double *>(Ug)[2 * off], s.x);
+    atomicAdd(&reinterpret_cast<double *>(Ug)[2 * off + 1], s.y);
+  }
+}
+
+}  // namespace
+
+int launch_rpa_warp(long n_points, int nb, const double2 *chi0, const double2 *U, double2 *chi, cudaStream_t stream,
+                    unsigned *status) {
+  if (arith_mode() == kArithFP64) return launch_as<double2>(n_points, nb, chi0, U, chi, stream, status);
+  return launch_as<cdf>(n_points, nb, chi0, U, chi, stream, status);
+}
+
+int launch_rpa_adjoint_warp(long n_points, int nb, const double2 *chi0, const double2 *U, const double2 *chi,
+                            const double2 *chig, double2 *chi0g, double2 *Ug, cudaStream_t stream, unsigned *status) {
+  const int N = nb * nb;
+  const size_t u_bytes =
+      ((size_t)N * N * (sizeof(double2) + 2 * sizeof(int)) + (N + 1) * sizeof(int) + 15) & ~(size_t)15;
+  const size_t per_warp = (size_t)5 * N * N * sizeof(double2);
+  const size_t limit = (size_t)max_smem_optin();
+  if (u_bytes + per_warp > limit) return set_error(TPRF_ERR_INVALID_ARGUMENT, "solve_rpa_PH_adjoint: nb too large");
+  TPRF_CUDA(cudaFuncSetAttribute(rpa_adjoint_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)limit));
+  int best_w = 1, best_total = 0;
+  for (int w = 1; w <= 16; ++w) {
+    const size_t smem = u_bytes + (size_t)w * per_warp;
+    if (smem > limit) break;
+    int per_sm = 0;
+    TPRF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, rpa_adjoint_warp_kernel, 32 * w, smem));
+    if (per_sm * w >= best_total) {
+      best_total = per_sm * w;
+      best_w = w;
+    }
+  }
+  if (best_total == 0) return set_error(TPRF_ERR_INVALID_ARGUMENT, "solve_rpa_PH_adjoint: nb too large");
+  const size_t smem = u_bytes + (size_t)best_w * per_warp;
+  long blocks = (n_points + best_w - 1) / best_w;
+  blocks = std::max(1L, std::min(blocks, (long)num_sms() * (best_total / best_w)));
+  rpa_adjoint_warp_kernel<<<(unsigned)blocks, 32 * best_w, smem, stream>>>(n_points, nb, chi0, U, chi, chig, chi0g,
+                                                                          Ug, status);
+  TPRF_LAUNCH_CHECK("rpa_adjoint_warp_kernel");
+  return TPRF_OK;
+}
+
+}  // namespace tprf

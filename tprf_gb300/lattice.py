@@ -227,17 +227,37 @@ def chi_w0r_from_chi_tr(chi_tr):
 # RPA (lattice/rpa.cpp:29-68)
 
 
-def solve_rpa_PH(chi0, U):
-    """chi = [1 - chi0 U]^-1 chi0 in the PH grouping (lattice_desc.py:547)."""
+def solve_rpa_PH(chi0, U, out=None, chunk_points=None, workspace=None):
+    """chi = [1 - chi0 U]^-1 chi0 in the PH grouping (lattice_desc.py:547).
+
+    With ``out`` (a host tensor of chi0's shape, ideally pinned) the result is
+    written to host memory as it is solved: chunks of ``chunk_points`` (q, iw)
+    points go through a device ring in ``workspace`` (allocated here if None) and
+    their copies to the host overlap the solve of the next chunk. The returned Gf
+    then holds the host tensor.
+    """
     if not isinstance(chi0, Gf) or chi0.target_rank != 4:
         raise TypeError("solve_rpa_PH: chi0 must be a rank-4 tensor valued Gf")
     nb = chi0.target_shape[0]
     Ud = as_device_c128(U, chi0.data.device)
     if tuple(Ud.shape) != (nb,) * 4:
         raise ValueError(f"solve_rpa_PH: U must have shape {(nb,) * 4}")
-    out = Gf(mesh=chi0.mesh, data=torch.empty_like(chi0.data))
     n_points = chi0.data.numel() // nb ** 4
     src = chi0.data.contiguous()
-    check(_native.lib().tprf_solve_rpa_PH(n_points, nb, _ptr(src), _ptr(Ud), _ptr(out.data), _stream()),
+    lib = _native.lib()
+    if out is None:
+        res = Gf(mesh=chi0.mesh, data=torch.empty_like(chi0.data))
+        check(lib.tprf_solve_rpa_PH(n_points, nb, _ptr(src), _ptr(Ud), _ptr(res.data), _stream()), "solve_rpa_PH")
+        return res
+    if out.device.type != "cpu" or out.dtype != torch.complex128 or tuple(out.shape) != tuple(chi0.data.shape) \
+            or not out.is_contiguous():
+        raise ValueError("solve_rpa_PH: out must be a contiguous complex128 host tensor of chi0's shape")
+    if chunk_points is None:
+        chunk_points = max(1, -(-n_points // 32))
+    if workspace is None:
+        nbytes = lib.tprf_solve_rpa_PH_to_host_workspace_bytes(chunk_points, nb, 3)
+        workspace = torch.empty(nbytes, dtype=torch.uint8, device=chi0.data.device)
+    check(lib.tprf_solve_rpa_PH_to_host(n_points, nb, _ptr(src), _ptr(Ud), out.data_ptr(), chunk_points,
+                                        _ptr(workspace), workspace.numel() * workspace.element_size(), _stream()),
           "solve_rpa_PH")
-    return out
+    return Gf(mesh=chi0.mesh, data=out, device=torch.device("cpu"))

@@ -78,16 +78,21 @@ def kanamori_spin_vertex(norb, U, J):
 
 CONFIGS = {
     "cfg0": dict(name="square_1band_16x16_beta10_nmax64", hop=lambda: square_1band(1.0), dims=(16, 16, 1),
-                 beta=10.0, mu=0.0, n_max=64, nw=64, vertex=lambda: np.full((1, 1, 1, 1), 1.0 + 0j)),
+                 beta=10.0, mu=0.0, n_max=64, nw=64, vertex=lambda: np.full((1, 1, 1, 1), 1.0 + 0j),
+                 vertex_label="Hubbard U=1"),
     "cfg1": dict(name="cubic_3orb_32x32x32_beta20_nmax256", hop=lambda: cubic_3orb(0), dims=(32, 32, 32),
-                 beta=20.0, mu=0.0, n_max=256, nw=256, vertex=lambda: kanamori_spin_vertex(3, 2.3, 0.4)),
+                 beta=20.0, mu=0.0, n_max=256, nw=256, vertex=lambda: kanamori_spin_vertex(3, 2.3, 0.4),
+                 vertex_label="Kanamori spin channel U=2.3 J=0.4"),
     # cfg1's model on a 16 x 16 x 8 mesh: the profiling case (about 2 GB on the device)
     "cfg1_small": dict(name="cubic_3orb_16x16x8_beta20_nmax256", hop=lambda: cubic_3orb(0), dims=(16, 16, 8),
-                       beta=20.0, mu=0.0, n_max=256, nw=256, vertex=lambda: kanamori_spin_vertex(3, 2.3, 0.4)),
+                       beta=20.0, mu=0.0, n_max=256, nw=256, vertex=lambda: kanamori_spin_vertex(3, 2.3, 0.4),
+                 vertex_label="Kanamori spin channel U=2.3 J=0.4"),
     "cfg3": dict(name="square_2orb_32x32_beta16_nmax128", hop=lambda: square_2orb(0), dims=(32, 32, 1),
-                 beta=16.0, mu=0.0, n_max=128, nw=128, vertex=lambda: kanamori_spin_vertex(2, 1.2, 0.2)),
+                 beta=16.0, mu=0.0, n_max=128, nw=128, vertex=lambda: kanamori_spin_vertex(2, 1.2, 0.2),
+                 vertex_label="Kanamori spin channel U=1.2 J=0.2"),
     "cfg4": dict(name="layered_5orb_64x64x4_beta40_nmax512", hop=lambda: layered_5orb(0), dims=(64, 64, 4),
-                 beta=40.0, mu=0.0, n_max=512, nw=256, vertex=lambda: kanamori_spin_vertex(5, 3.0, 0.5)),
+                 beta=40.0, mu=0.0, n_max=512, nw=256, vertex=lambda: kanamori_spin_vertex(5, 3.0, 0.5),
+                 vertex_label="Kanamori spin channel U=3 J=0.5"),
 }
 
 
