@@ -64,7 +64,7 @@ template <> __device__ __forceinline__ const cdf *twiddles<cdf>(const FftDesc &d
 }
 
 template <bool FWD, class C>
-__device__ __forceinline__ C root(const C *tw, long idx) {
+__device__ __forceinline__ C root(const C *tw, int idx) {
   const C t = tw[idx];
   return FWD ? t : cconj(t);
 }
@@ -210,7 +210,7 @@ __device__ __forceinline__ void fft_stage(C *__restrict__ a, int n, int Ns, int 
     for (int r = 0; r < R; ++r) v[r] = a[(base + r * Ns) * ncol + col];
     if (Ns > 1) {
 #pragma unroll
-      for (int r = 1; r < R; ++r) v[r] = cmul(v[r], root<FWD>(tw, (long)k * r * tws));
+      for (int r = 1; r < R; ++r) v[r] = cmul(v[r], root<FWD>(tw, k * r * tws));
     }
     Dft<R, FWD, C>::run(v);
 #pragma unroll
@@ -237,7 +237,7 @@ __device__ __noinline__ void fft_stage_generic(const C *__restrict__ in, C *__re
     const int base = (j - k) * R + k;
     C acc = czero<C>();
     for (int r = 0; r < R; ++r) {
-      const long e = ((long)k * r * tws + (long)((r * q) % R) * nbf) % n;
+      const int e = (int)(((long)k * r * tws + (long)((r * q) % R) * nbf) % n);
       acc = cadd(acc, cmul(in[(base + r * Ns) * ncol + col], root<FWD>(tw, e)));
     }
     out[(base + q * Ns) * ncol + col] = acc;
@@ -248,12 +248,14 @@ __device__ __noinline__ void fft_stage_generic(const C *__restrict__ in, C *__re
 // natural order out). b is a second buffer of the same size, used only when
 // the plan has a generic-radix stage (d.has_generic), else may be null.
 // Returns the buffer holding the result. Starts and ends with a barrier.
+// With n_stages >= 0 only the first n_stages stages run (see last_stage_output).
 template <bool FWD, class C>
-__device__ C *fft_smem(C *a, C *b, const FftDesc &d, int ncol) {
+__device__ C *fft_smem(C *a, C *b, const FftDesc &d, int ncol, int n_stages = -1) {
   __syncthreads();
   const C *tw = twiddles<C>(d);
   int Ns = 1;
-  for (int s = 0; s < d.nst; ++s) {
+  const int nst = n_stages < 0 ? d.nst : n_stages;
+  for (int s = 0; s < nst; ++s) {
     const int R = d.radix[s];
     switch (R) {
       case 2: fft_stage<2, FWD>(a, d.n, Ns, ncol, tw); break;
@@ -273,6 +275,26 @@ __device__ C *fft_smem(C *a, C *b, const FftDesc &d, int ncol) {
     __syncthreads();
   }
   return a;
+}
+
+// One output i of the last DIT stage (radix R, Ns = n / R) computed directly
+// from the buffer left by the other stages: X[i] = sum_r W_n^{r i} v[i mod Ns + r Ns]
+// (the butterfly k = i mod Ns, its output q = i / Ns, with the twiddle and the
+// R-point DFT root combined into one power of W_n). Used where only some
+// outputs are needed.
+template <bool FWD, class C>
+__device__ __forceinline__ C last_stage_output(const C *__restrict__ a, const FftDesc &d, int ncol, int col, int i) {
+  const C *tw = twiddles<C>(d);
+  const int n = d.n, R = d.radix[d.nst - 1], Ns = n / R;
+  const int k = i % Ns;
+  C v = a[k * ncol + col];
+  int e = 0;
+  for (int r = 1; r < R; ++r) {
+    e += i;
+    if (e >= n) e -= n;
+    v = cadd(v, cmul(a[(k + r * Ns) * ncol + col], root<FWD>(tw, e)));
+  }
+  return v;
 }
 
 }  // namespace tprf

@@ -207,10 +207,11 @@ struct BubbleLoader {  // chi0 columns computed from G(tau, r): col = r * nb^4 +
       s[ic + c] = oy;
     }
   }
+  // the product in FP64, then one conversion (two would cost more than the product)
   template <class E>
   __device__ __forceinline__ E get(int t, int c, long, int ic, const long *s) const {
     const long slice = Nr * nb * nb;
-    return cmul(from_d2<E>(g[(long)t * slice + s[c]]), from_d2<E>(g[(long)(n_tau - 1 - t) * slice + s[ic + c]]));
+    return from_d2<E>(cmul(g[(long)t * slice + s[c]], g[(long)(n_tau - 1 - t) * slice + s[ic + c]]));
   }
 };
 
@@ -274,13 +275,14 @@ __global__ void __launch_bounds__(kMatsubaraThreads, 2) tau_to_w_kernel(TauWPlan
     am[1 * ic + c] = from_d2<C>(csub(m3, cscale(cadd(m1, m2), 0.5)));
     am[2 * ic + c] = from_d2<C>(cadd(cadd(cscale(m1, 1.0 / 6.0), cscale(m2, 0.5)), cscale(m3, 1.0 / 3.0)));
   }
-  C *r = fft_smem<false>(a, b, p.fft, ic);
+  // all stages but the last; the last is evaluated only at the 2 nw - 1 kept frequencies
+  C *r = fft_smem<false>(a, b, p.fft, ic, p.fft.nst - 1);
   const auto fact = real_of<C>(p.beta / (double)L);
   for (int w = tid; w < nwt * ic; w += nthr) {
     const int c = w & (ic - 1), mi = w >> lg;
     if (c >= ncol) continue;
     const int m = mi - (nw - 1);
-    C v = cscale(r[((m + L) % L) * ic + c], fact);
+    C v = cscale(last_stage_output<false>(r, p.fft, ic, c, m < 0 ? m + L : m), fact);
 #pragma unroll
     for (int j = 0; j < 3; ++j) v = cadd(v, cmul(am[j * ic + c], table<C>(p.K, p.Kf, (long)j * nwt + mi)));
     out[(long)mi * Ccols + col0 + c] = as_d2(v);
