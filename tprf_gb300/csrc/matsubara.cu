@@ -167,6 +167,9 @@ struct ArrayLoader {  // chi(tau, col) stored as [n_tau][C]
   __device__ __forceinline__ E get(int t, int c, long col0, int, const long *) const {
     return from_d2<E>(x[(long)t * C + col0 + c]);
   }
+  __device__ __forceinline__ double2 get64(int t, int c, long col0, int, const long *) const {
+    return x[(long)t * C + col0 + c];
+  }
 };
 
 struct BubbleLoader {  // chi0 columns computed from G(tau, r): col = r * nb^4 + abcd
@@ -209,9 +212,12 @@ struct BubbleLoader {  // chi0 columns computed from G(tau, r): col = r * nb^4 +
   }
   // the product in FP64, then one conversion (two would cost more than the product)
   template <class E>
-  __device__ __forceinline__ E get(int t, int c, long, int ic, const long *s) const {
+  __device__ __forceinline__ E get(int t, int c, long col0, int ic, const long *s) const {
+    return from_d2<E>(get64(t, c, col0, ic, s));
+  }
+  __device__ __forceinline__ double2 get64(int t, int c, long, int ic, const long *s) const {
     const long slice = Nr * nb * nb;
-    return from_d2<E>(cmul(g[(long)t * slice + s[c]], g[(long)(n_tau - 1 - t) * slice + s[ic + c]]));
+    return cmul(g[(long)t * slice + s[c]], g[(long)(n_tau - 1 - t) * slice + s[ic + c]]);
   }
 };
 
@@ -228,40 +234,57 @@ __global__ void __launch_bounds__(kMatsubaraThreads, 2) tau_to_w_kernel(TauWPlan
   C *last = a + (size_t)(p.fft.has_generic ? 2 : 1) * L * ic;  // [ic] row L
   C *am = last + ic;                                            // [3][ic]
   long *soff = reinterpret_cast<long *>(am + 3 * ic);           // [2][ic] loader offsets
+  double2 *smp = reinterpret_cast<double2 *>(soff + 2 * ic);    // [18][ic] FP64 rows 0..8, L-8..L
   const int tid = threadIdx.x, nthr = blockDim.x;
   const long col0 = blockIdx.x * (long)ic;
   const int ncol = (int)min((long)ic, Ccols - col0);
   ld.setup(col0, ic, ncol, soff);
   __syncthreads();
-  // rows t < L go to their digit-reversed FFT positions, row L aside
-  for (int w = tid; w < (L + 1) * ic; w += nthr) {
-    const int c = w & (ic - 1), t = w >> lg;
-    C v = czero<C>();
-    if (c < ncol) v = ld.template get<C>(t, c, col0, ic, soff);
-    if (t < L)
-      a[rev[t] * ic + c] = v;
-    else
-      last[c] = v;
+  // Rows t < L go to their digit-reversed FFT positions, row L aside. The loads
+  // of four iterations are issued before any is used (their latency overlaps),
+  // and the FP64 values of the 18 rows that fit_derivatives samples are kept.
+  const int total = (L + 1) * ic;
+  for (int w0 = tid; w0 < total; w0 += 4 * nthr) {
+    double2 v[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int w = w0 + u * nthr;
+      const int c = w & (ic - 1), t = w >> lg;
+      v[u] = (w < total && c < ncol) ? ld.get64(t, c, col0, ic, soff) : make_double2(0.0, 0.0);
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int w = w0 + u * nthr;
+      if (w < total) {
+        const int c = w & (ic - 1), t = w >> lg;
+        if (t <= 8) smp[t * ic + c] = v[u];
+        if (t >= L - 8) smp[(t - L + 17) * ic + c] = v[u];
+        const C x = from_d2<C>(v[u]);
+        if (t < L)
+          a[rev[t] * ic + c] = x;
+        else
+          last[c] = x;
+      }
+    }
   }
   __syncthreads();
   const double dtau = p.beta / (double)(p.n_tau - 1);
   // fit_derivatives differentiates and then applies the inverse Vandermonde
-  // matrix, which amplifies rounding: its 18 samples are taken in FP64 from
-  // the source, not from the double-float copy in shared memory.
+  // matrix, which amplifies rounding: its 18 samples are the FP64 values, not
+  // the double-float copy in the FFT buffer.
   for (int c = tid; c < ic; c += nthr) {
     if (c >= ncol) {
       am[c] = am[ic + c] = am[2 * ic + c] = czero<C>();
       continue;
     }
-    const long col = col0 + c;
-    const double2 g0 = ld(0, col), gL = ld(L, col);
+    const double2 g0 = smp[c], gL = smp[17 * ic + c];
     double2 gl0 = make_double2(0.0, 0.0), gl1 = gl0, gr0 = gl0, gr1 = gl0;
 #pragma unroll
     for (int m = 0; m < 8; ++m) {
       const double tau_m = (double)(m + 1) * dtau;
-      const double2 xl = ld(m + 1, col);
+      const double2 xl = smp[(m + 1) * ic + c];
       const double2 dl = make_double2((xl.x - g0.x) / tau_m, (xl.y - g0.y) / tau_m);
-      const double2 xr = ld(L - 1 - m, col);
+      const double2 xr = smp[(16 - m) * ic + c];
       const double2 dr = make_double2((gL.x - xr.x) / tau_m, (gL.y - xr.y) / tau_m);
       gl0 = make_double2(fma(vr.r0[m], dl.x, gl0.x), fma(vr.r0[m], dl.y, gl0.y));
       gl1 = make_double2(fma(vr.r1[m], dl.x, gl1.x), fma(vr.r1[m], dl.y, gl1.y));
@@ -343,7 +366,7 @@ template <class Loader, class E>
 int launch_tau_to_w_as(const TauWPlan *p, Loader ld, double2 *out, long C, cudaStream_t stream) {
   int ic, lg;
   size_t smem;
-  int st = pick_ic(p->fft, 4 * sizeof(double2) + 2 * sizeof(long), &ic, &lg, &smem);
+  int st = pick_ic(p->fft, 4 * sizeof(double2) + 2 * sizeof(long) + 18 * sizeof(double2), &ic, &lg, &smem);
   if (st) return st;
   TPRF_CUDA(cudaFuncSetAttribute(tau_to_w_kernel<Loader, E>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const long blocks = (C + ic - 1) / ic;
