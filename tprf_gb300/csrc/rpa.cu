@@ -7,9 +7,8 @@
 // solved without forming the inverse: A = I - chi0 U, then Gaussian
 // elimination with partial pivoting on [A | chi0] and back substitution.
 //
-// Kernels by vertex size: nb = 1, 2 one thread per point (below); nb = 3 four
-// lanes per point (rpa_coop_kernel); nb >= 4 one warp per point
-// (rpa_warp.cu, which also holds the adjoint).
+// Kernels by vertex size: nb = 1, 2 one thread per point (below); nb >= 3 a
+// group of lanes per point (rpa_warp.cu, which also holds the adjoint).
 //
 // Design of the thread-per-point kernel: A = I - chi0 U is formed from the non-zeros of
 // U only (compacted once per CTA into shared memory), LU-factorised with
@@ -215,190 +214,6 @@ int launch_rpa_nb(long n_points, const double2 *chi0, const double2 *U, double2 
   return launch_rpa_as<NB, NT, double2>(n_points, chi0, U, chi, stream, status);
 }
 
-// ---------------------------------------------------------------------------
-// Cooperative variant: T adjacent lanes solve one point together. The point's
-// A / LU factors sit in one shared-memory slice ([element][point] layout); in
-// each elimination step the T lanes split the pivot search, the row swap and
-// the trailing update by rows, then split the nb^2 right-hand sides by
-// columns. With the same shared memory per point as one thread per point,
-// the CTA holds T times more warps, which hides the latency of the dependent
-// double-float chains. Lanes of one point synchronise with __syncwarp on
-// their own mask; all of them take the same branches (the same point, the
-// same conditioning estimate), so no lane waits for an absent partner.
-template <int NB, int T, int PPB, class E>
-__device__ double rpa_point_coop(const double2 *x, double2 *y, E *A, int *perm, const E *s_val, const int *s_off,
-                                 const int *s_cs, unsigned mask, int tq, bool &singular) {
-  constexpr int N = NB * NB;
-#define AE(i, k) A[((i) * N + (k)) * PPB]
-  double amax = 0.0;
-  for (int r = tq; r < N; r += T) {
-#pragma unroll
-    for (int c = 0; c < N; ++c) {
-      E s = (r == c) ? el_one((E *)nullptr) : el_zero((E *)nullptr);
-      float mag = (r == c) ? 1.f : 0.f;
-      for (int t = s_cs[c]; t < s_cs[c + 1]; ++t) {
-        const E xv = el_from(x[r * N + s_off[t]], (E *)nullptr);
-        s = el_fms(xv, s_val[t], s);
-        mag = fmaf(el_absf(xv), el_absf(s_val[t]), mag);
-      }
-      amax = fmax(amax, (double)mag * (double)mag);
-      AE(r, c) = s;
-    }
-    perm[r * PPB] = r;
-  }
-  __syncwarp(mask);
-  double pmin = 1e300;
-  bool sing = false;
-#pragma unroll 1
-  for (int j = 0; j < N; ++j) {
-    // pivot search: this lane's rows, then the best over the T lanes
-    int p = j;
-    double best = -1.0;
-    for (int i = j + tq; i < N; i += T) {
-      const double v = el_abs2(AE(i, j));
-      if (v > best) {
-        best = v;
-        p = i;
-      }
-    }
-#pragma unroll
-    for (int o = 1; o < T; o <<= 1) {
-      const double ob = __shfl_xor_sync(mask, best, o);
-      const int op = __shfl_xor_sync(mask, p, o);
-      if (ob > best || (ob == best && op < p)) {
-        best = ob;
-        p = op;
-      }
-    }
-    if (best == 0.0) sing = true;
-    pmin = fmin(pmin, best);
-    if (p != j) {
-      for (int k = tq; k < N; k += T) {
-        const E t = AE(j, k);
-        AE(j, k) = AE(p, k);
-        AE(p, k) = t;
-      }
-      if (tq == 0) {
-        const int t = perm[j * PPB];
-        perm[j * PPB] = perm[p * PPB];
-        perm[p * PPB] = t;
-      }
-    }
-    __syncwarp(mask);
-    const E inv = el_recip(AE(j, j));
-    // rows below j, split over the lanes
-    for (int i = j + 1 + tq; i < N; i += T) {
-      const E f = cmul(AE(i, j), inv);
-      AE(i, j) = f;
-#pragma unroll
-      for (int k = 0; k < N; ++k)
-        if (k > j) AE(i, k) = el_fms(f, AE(j, k), AE(i, k));
-    }
-    __syncwarp(mask);
-    if (tq == 0) AE(j, j) = inv;
-    __syncwarp(mask);
-  }
-  singular = sing;
-  // right-hand sides: columns split over the lanes
-  for (int c = tq; c < N; c += T) {
-    int z = 0;
-    asm volatile("" : "+r"(z));
-    const E *F = A + z;
-    const int cm = colmap<NB>(c);
-    E b[N];
-#pragma unroll
-    for (int r = 0; r < N; ++r) b[r] = el_from(x[perm[r * PPB] * N + cm], (E *)nullptr);
-#pragma unroll
-    for (int r = 1; r < N; ++r)
-#pragma unroll
-      for (int l = 0; l < r; ++l) b[r] = el_fms(F[(r * N + l) * PPB], b[l], b[r]);
-#pragma unroll
-    for (int rr = 0; rr < N; ++rr) {
-      const int r = N - 1 - rr;
-#pragma unroll
-      for (int l = r + 1; l < N; ++l) b[r] = el_fms(F[(r * N + l) * PPB], b[l], b[r]);
-      b[r] = cmul(b[r], F[(r * N + r) * PPB]);
-    }
-#pragma unroll
-    for (int r = 0; r < N; ++r) y[r * N + cm] = el_to(b[r]);
-  }
-  // every lane of the point returns the same estimate
-#pragma unroll
-  for (int o = 1; o < T; o <<= 1) amax = fmax(amax, __shfl_xor_sync(mask, amax, o));
-  __syncwarp(mask);
-#undef AE
-  return pmin > 0.0 ? amax / pmin : 1e300;
-}
-
-template <int NB, int T, int PPB, class E>
-__global__ void __launch_bounds__(T *PPB, 1) rpa_coop_kernel(long n_points, const double2 *chi0,
-                                                            const double2 *__restrict__ U, double2 *chi,
-                                                            unsigned *status) {
-  constexpr int N = NB * NB;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  E *s_val = reinterpret_cast<E *>(smem_raw);
-  unsigned char *lu_base = smem_raw + (size_t)N * N * sizeof(E);
-  int *s_off = reinterpret_cast<int *>(lu_base + (size_t)N * N * PPB * 16);
-  int *s_cs = s_off + N * N;
-  int *perm_base = s_cs + N + 1;
-  if (threadIdx.x == 0) {
-    int t = 0;
-    for (int c = 0; c < N; ++c) {
-      s_cs[c] = t;
-      for (int m = 0; m < N; ++m) {
-        const double2 u = U[m * N + colmap<NB>(c)];
-        if (u.x != 0.0 || u.y != 0.0) {
-          s_off[t] = colmap<NB>(m);
-          s_val[t] = el_from(u, (E *)nullptr);
-          ++t;
-        }
-      }
-    }
-    s_cs[N] = t;
-  }
-  __syncthreads();
-  const int pidx = threadIdx.x / T, tq = threadIdx.x % T;
-  const unsigned mask = (T == 32) ? 0xffffffffu : (((1u << T) - 1u) << ((threadIdx.x & 31) & ~(T - 1)));
-  for (long base = blockIdx.x * (long)PPB; base < n_points; base += (long)gridDim.x * PPB) {
-    const long pt = base + pidx;
-    if (pt >= n_points) continue;  // all T lanes of this point skip together
-    const double2 *x = chi0 + pt * N * N;
-    double2 *y = chi + pt * N * N;
-    bool singular = false;
-    const double cond2 = rpa_point_coop<NB, T, PPB, E>(x, y, reinterpret_cast<E *>(lu_base) + pidx,
-                                                       perm_base + pidx, s_val, s_off, s_cs, mask, tq, singular);
-    if (IsDf<E>::value && !(cond2 <= kDf64CondLimit2)) {
-      double2 uval[N * N];
-      for (int t = 0; t < s_cs[N]; ++t) {
-        int c = 0;
-        while (s_cs[c + 1] <= t) ++c;
-        const int m = (s_off[t] % NB) * NB + s_off[t] / NB;
-        uval[t] = U[m * N + colmap<NB>(c)];
-      }
-      rpa_point_coop<NB, T, PPB, double2>(x, y, reinterpret_cast<double2 *>(lu_base) + pidx, perm_base + pidx, uval,
-                                          s_off, s_cs, mask, tq, singular);
-    }
-    if (singular && tq == 0) atomicOr(status, kDevErrSingular);
-  }
-}
-
-template <int NB, int T, int PPB, class E>
-int launch_rpa_coop_as(long n_points, const double2 *chi0, const double2 *U, double2 *chi, cudaStream_t stream,
-                       unsigned *status) {
-  constexpr int N = NB * NB;
-  const size_t smem = (size_t)N * N * 16 * (1 + PPB) + (size_t)(N * N + N + 1) * sizeof(int) +
-                      (size_t)N * PPB * sizeof(int);
-  if (smem > (size_t)max_smem_optin()) return set_error(TPRF_ERR_INVALID_ARGUMENT, "solve_rpa_PH: nb too large");
-  TPRF_CUDA(cudaFuncSetAttribute(rpa_coop_kernel<NB, T, PPB, E>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem));
-  long blocks = (n_points + PPB - 1) / PPB;
-  const long cap = (long)num_sms() * 64;
-  blocks = std::max(1L, std::min(blocks, cap));
-  rpa_coop_kernel<NB, T, PPB, E><<<(unsigned)blocks, T * PPB, smem, stream>>>(n_points, chi0, U, chi, status);
-  TPRF_LAUNCH_CHECK("rpa_coop_kernel");
-  return TPRF_OK;
-}
-
 }  // namespace
 
 int launch_rpa_warp(long n_points, int nb, const double2 *chi0, const double2 *U, double2 *chi, cudaStream_t stream,
@@ -410,9 +225,6 @@ int launch_rpa(long n_points, int nb, const double2 *chi0, const double2 *U, dou
   switch (nb) {
     case 1: return launch_rpa_nb<1, 256>(n_points, chi0, U, chi, stream, status);
     case 2: return launch_rpa_nb<2, 256>(n_points, chi0, U, chi, stream, status);
-    case 3:
-      if (arith_mode() == kArithFP64) return launch_rpa_coop_as<3, 4, 128, double2>(n_points, chi0, U, chi, stream, status);
-      return launch_rpa_coop_as<3, 4, 128, cdf>(n_points, chi0, U, chi, stream, status);
     default:
       if (nb < 1 || nb > 8) return set_error(TPRF_ERR_INVALID_ARGUMENT, "solve_rpa_PH: nb must be 1..8");
       return launch_rpa_warp(n_points, nb, chi0, U, chi, stream, status);

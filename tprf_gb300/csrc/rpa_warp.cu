@@ -30,17 +30,17 @@ struct SparseU {  // U grouped and compacted by columns: rows and FP64 values
 // the grouped column index of the memory offset m = c' * nb + d inside a row
 __device__ __forceinline__ int col_of_offset(int m, int nb) { return (m % nb) * nb + m / nb; }
 
-template <class E>
+template <class E, int G>
 __device__ double rpa_point_warp(const double2 *__restrict__ x, double2 *__restrict__ y, E *M, int N, int nb,
-                                 const SparseU &u, int lane, bool &singular) {
+                                 const SparseU &u, int lane, unsigned gmask, bool &singular) {
   const int W = 2 * N;
 #define MM(i, c) M[(i) * W + (c)]
   // B = chi0 in the grouped layout (coalesced global reads)
-  for (int o = lane; o < N * N; o += 32) MM(o / N, N + col_of_offset(o % N, nb)) = el_from(x[o], (E *)nullptr);
-  __syncwarp();
+  for (int o = lane; o < N * N; o += G) MM(o / N, N + col_of_offset(o % N, nb)) = el_from(x[o], (E *)nullptr);
+  __syncwarp(gmask);
   // A = I - X U from the non-zeros of U; the size of the terms bounds cancellation
   float amax = 0.f;
-  for (int e = lane; e < N * N; e += 32) {
+  for (int e = lane; e < N * N; e += G) {
     const int r = e / N, c = e % N;
     E s = (r == c) ? el_one((E *)nullptr) : el_zero((E *)nullptr);
     float mag = (r == c) ? 1.f : 0.f;
@@ -53,13 +53,13 @@ __device__ double rpa_point_warp(const double2 *__restrict__ x, double2 *__restr
     amax = fmaxf(amax, mag);
     MM(r, c) = s;
   }
-  __syncwarp();
+  __syncwarp(gmask);
   double pmin = 1e300;
   bool sing = false;
   for (int j = 0; j < N; ++j) {
     int p = j;
     double best = -1.0;
-    for (int i = j + lane; i < N; i += 32) {
+    for (int i = j + lane; i < N; i += G) {
       const double v = el_abs2(MM(i, j));
       if (v > best) {
         best = v;
@@ -67,9 +67,9 @@ __device__ double rpa_point_warp(const double2 *__restrict__ x, double2 *__restr
       }
     }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      const double ob = __shfl_xor_sync(0xffffffffu, best, o);
-      const int op = __shfl_xor_sync(0xffffffffu, p, o);
+    for (int o = G / 2; o > 0; o >>= 1) {
+      const double ob = __shfl_xor_sync(gmask, best, o);
+      const int op = __shfl_xor_sync(gmask, p, o);
       if (ob > best || (ob == best && op < p)) {
         best = ob;
         p = op;
@@ -78,28 +78,28 @@ __device__ double rpa_point_warp(const double2 *__restrict__ x, double2 *__restr
     if (best == 0.0) sing = true;
     pmin = fmin(pmin, best);
     if (p != j) {
-      for (int c = lane; c < W; c += 32) {
+      for (int c = lane; c < W; c += G) {
         const E t = MM(j, c);
         MM(j, c) = MM(p, c);
         MM(p, c) = t;
       }
     }
-    __syncwarp();
+    __syncwarp(gmask);
     const E inv = el_recip(MM(j, j));
-    for (int i = j + 1 + lane; i < N; i += 32) MM(i, j) = cmul(MM(i, j), inv);
-    __syncwarp();
-    for (int c = j + 1 + lane; c < W; c += 32) {
+    for (int i = j + 1 + lane; i < N; i += G) MM(i, j) = cmul(MM(i, j), inv);
+    __syncwarp(gmask);
+    for (int c = j + 1 + lane; c < W; c += G) {
       const E piv = MM(j, c);
 #pragma unroll 2
       for (int i = j + 1; i < N; ++i) MM(i, c) = el_fms(MM(i, j), piv, MM(i, c));
     }
-    __syncwarp();
+    __syncwarp(gmask);
     if (lane == 0) MM(j, j) = inv;
-    __syncwarp();
+    __syncwarp(gmask);
   }
   singular = sing;
   // back substitution, one B column per lane, then the grouped -> memory store
-  for (int c = N + lane; c < W; c += 32) {
+  for (int c = N + lane; c < W; c += G) {
     for (int j = N - 1; j >= 0; --j) {
       const E xj = cmul(MM(j, c), MM(j, j));
       MM(j, c) = xj;
@@ -107,17 +107,17 @@ __device__ double rpa_point_warp(const double2 *__restrict__ x, double2 *__restr
       for (int i = 0; i < j; ++i) MM(i, c) = el_fms(MM(i, j), xj, MM(i, c));
     }
   }
-  __syncwarp();
-  for (int o = lane; o < N * N; o += 32) y[o] = el_to(MM(o / N, N + col_of_offset(o % N, nb)));
+  __syncwarp(gmask);
+  for (int o = lane; o < N * N; o += G) y[o] = el_to(MM(o / N, N + col_of_offset(o % N, nb)));
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, o));
-  __syncwarp();
+  for (int o = G / 2; o > 0; o >>= 1) amax = fmaxf(amax, __shfl_xor_sync(gmask, amax, o));
+  __syncwarp(gmask);
 #undef MM
   const double am = (double)amax * (double)amax;
   return pmin > 0.0 ? am / pmin : 1e300;
 }
 
-template <class E>
+template <class E, int G>
 __global__ void __launch_bounds__(512) rpa_warp_kernel(long n_points, int nb, const double2 *__restrict__ chi0,
                                                        const double2 *__restrict__ U, double2 *__restrict__ chi,
                                                        unsigned *status) {
@@ -127,8 +127,10 @@ __global__ void __launch_bounds__(512) rpa_warp_kernel(long n_points, int nb, co
   int *s_row = reinterpret_cast<int *>(s_val + N * N);
   int *s_cs = s_row + N * N;
   const size_t u_bytes = ((size_t)N * N * (sizeof(double2) + sizeof(int)) + (N + 1) * sizeof(int) + 15) & ~(size_t)15;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, n_warps = blockDim.x >> 5;
-  E *M = reinterpret_cast<E *>(smem_raw + u_bytes) + (size_t)warp * 2 * N * N;
+  // groups of G lanes, one point per group
+  const int grp = threadIdx.x / G, lane = threadIdx.x & (G - 1), n_grp = blockDim.x / G;
+  const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (threadIdx.x & 31 & ~(G - 1)));
+  E *M = reinterpret_cast<E *>(smem_raw + u_bytes) + (size_t)grp * 2 * N * N;
   if (threadIdx.x == 0) {
     int t = 0;
     for (int c = 0; c < N; ++c) {
@@ -147,45 +149,54 @@ __global__ void __launch_bounds__(512) rpa_warp_kernel(long n_points, int nb, co
   }
   __syncthreads();
   const SparseU u{s_val, s_row, s_cs};
-  for (long pt = (long)blockIdx.x * n_warps + warp; pt < n_points; pt += (long)gridDim.x * n_warps) {
+  for (long pt = (long)blockIdx.x * n_grp + grp; pt < n_points; pt += (long)gridDim.x * n_grp) {
     const double2 *x = chi0 + pt * N * N;
     double2 *y = chi + pt * N * N;
     bool singular = false;
-    const double cond2 = rpa_point_warp<E>(x, y, M, N, nb, u, lane, singular);
+    const double cond2 = rpa_point_warp<E, G>(x, y, M, N, nb, u, lane, gmask, singular);
     if (IsDf<E>::value && !(cond2 <= kDf64CondLimit2))
-      rpa_point_warp<double2>(x, y, reinterpret_cast<double2 *>(M), N, nb, u, lane, singular);
+      rpa_point_warp<double2, G>(x, y, reinterpret_cast<double2 *>(M), N, nb, u, lane, gmask, singular);
     if (singular && lane == 0) atomicOr(status, kDevErrSingular);
   }
 }
 
-template <class E>
+template <class E, int G>
 int launch_as(long n_points, int nb, const double2 *chi0, const double2 *U, double2 *chi, cudaStream_t stream,
               unsigned *status) {
   const int N = nb * nb;
   const size_t u_bytes = ((size_t)N * N * (sizeof(double2) + sizeof(int)) + (N + 1) * sizeof(int) + 15) & ~(size_t)15;
   const size_t per_point = (size_t)2 * N * N * 16;
+  const int ppw = 32 / G;  // points per warp
   const size_t limit = (size_t)max_smem_optin();
-  if (u_bytes + per_point > limit) return set_error(TPRF_ERR_INVALID_ARGUMENT, "solve_rpa_PH: nb too large");
-  TPRF_CUDA(cudaFuncSetAttribute(rpa_warp_kernel<E>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)limit));
+  if (u_bytes + ppw * per_point > limit) return set_error(TPRF_ERR_INVALID_ARGUMENT, "solve_rpa_PH: nb too large");
+  TPRF_CUDA(cudaFuncSetAttribute(rpa_warp_kernel<E, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)limit));
   // the number of warps per CTA that puts the most warps on an SM
   int best_w = 1, best_total = 0;
   for (int w = 1; w <= 16; ++w) {
-    const size_t smem = u_bytes + (size_t)w * per_point;
+    const size_t smem = u_bytes + (size_t)w * ppw * per_point;
     if (smem > limit) break;
     int per_sm = 0;
-    TPRF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, rpa_warp_kernel<E>, 32 * w, smem));
+    TPRF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, rpa_warp_kernel<E, G>, 32 * w, smem));
     if (per_sm * w >= best_total) {
       best_total = per_sm * w;
       best_w = w;
     }
   }
   if (best_total == 0) return set_error(TPRF_ERR_INVALID_ARGUMENT, "solve_rpa_PH: nb too large");
-  const size_t smem = u_bytes + (size_t)best_w * per_point;
-  long blocks = (n_points + best_w - 1) / best_w;
+  const size_t smem = u_bytes + (size_t)best_w * ppw * per_point;
+  const long per_block = (long)best_w * ppw;
+  long blocks = (n_points + per_block - 1) / per_block;
   blocks = std::max(1L, std::min(blocks, (long)num_sms() * (best_total / best_w) * 8));
-  rpa_warp_kernel<E><<<(unsigned)blocks, 32 * best_w, smem, stream>>>(n_points, nb, chi0, U, chi, status);
+  rpa_warp_kernel<E, G><<<(unsigned)blocks, 32 * best_w, smem, stream>>>(n_points, nb, chi0, U, chi, status);
   TPRF_LAUNCH_CHECK("rpa_warp_kernel");
   return TPRF_OK;
+}
+
+template <int G>
+int launch_g(long n_points, int nb, const double2 *chi0, const double2 *U, double2 *chi, cudaStream_t stream,
+             unsigned *status) {
+  if (arith_mode() == kArithFP64) return launch_as<double2, G>(n_points, nb, chi0, U, chi, stream, status);
+  return launch_as<cdf, G>(n_points, nb, chi0, U, chi, stream, status);
 }
 
 // ---- adjoint -------------------------------------------------------------------
@@ -348,10 +359,18 @@ __global__ void __launch_bounds__(512) rpa_adjoint_warp_kernel(long n_points, in
 
 }  // namespace
 
+// lanes per point (measured on GB300: nb = 3 8 lanes, 102 ms for 16.7 M points,
+// against 109 ms with 16 lanes; nb = 5 32 lanes, 1.08 s for 8.4 M points,
+// against 1.61 s with 16)
+int rpa_group_lanes(int nb) { return nb <= 3 ? 8 : 32; }
+
 int launch_rpa_warp(long n_points, int nb, const double2 *chi0, const double2 *U, double2 *chi, cudaStream_t stream,
                     unsigned *status) {
-  if (arith_mode() == kArithFP64) return launch_as<double2>(n_points, nb, chi0, U, chi, stream, status);
-  return launch_as<cdf>(n_points, nb, chi0, U, chi, stream, status);
+  switch (rpa_group_lanes(nb)) {
+    case 8: return launch_g<8>(n_points, nb, chi0, U, chi, stream, status);
+    case 16: return launch_g<16>(n_points, nb, chi0, U, chi, stream, status);
+    default: return launch_g<32>(n_points, nb, chi0, U, chi, stream, status);
+  }
 }
 
 int launch_rpa_adjoint_warp(long n_points, int nb, const double2 *chi0, const double2 *U, const double2 *chi,
