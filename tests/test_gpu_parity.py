@@ -82,12 +82,17 @@ def test_dyson_matches_numpy_inverse(cuda_lib):
 # ---------------------------------------------------------------------------
 # (b) lattice FFTs
 
-@pytest.mark.parametrize("dims", [(16, 16, 1), (4, 6, 5), (8, 1, 1), (7, 3, 10), (2, 2, 1), (1, 1, 1), (32, 8, 3),
-                                  (64, 1, 1), (24, 48, 1)])
-def test_lattice_fft(cuda_lib, dims):
+@pytest.mark.parametrize("dims,nt", [((16, 16, 1), 5), ((4, 6, 5), 5), ((8, 1, 1), 5), ((7, 3, 10), 5),
+                                     ((2, 2, 1), 5), ((1, 1, 1), 5), ((32, 8, 3), 5), ((64, 1, 1), 5),
+                                     ((24, 48, 1), 5), ((8, 16, 32), 9), ((4, 64, 4), 25), ((2, 256, 1), 3),
+                                     ((16, 1, 8), 1), ((32, 32, 4), 81)])
+def test_lattice_fft(cuda_lib, dims, nt):
+    """Every axis pattern: one-axis passes, the two-axis plane pass (powers of
+    two, with and without a third axis, a trivial axis between), ragged target
+    tiles."""
     from tprf_gb300 import _native
     rng = np.random.default_rng(sum(dims))
-    nw, nt = 3, 5
+    nw = 3
     x = rand_c(rng, nw, int(np.prod(dims)), nt)
     xd = torch.as_tensor(x).cuda()
     out = torch.empty_like(xd)

@@ -194,11 +194,21 @@ template <bool FWD, class C> struct Dft<8, FWD, C> {
 // Threads: ncol divides blockDim.x; a thread keeps one column and walks the
 // butterflies j = j0, j0 + step, ..., so no integer division happens inside
 // the loops.
+// Column layout of an FFT buffer: element i of column c sits at
+// cbase(c) + i * stride, cbase(c) = (c >> lgt) * blk + (c & (2^lgt - 1)).
+// The plain interleaved layout is stride = ncol, lgt >= log2(ncol).
+struct ColLayout {
+  int stride, blk, lgt;
+  __device__ __forceinline__ int cbase(int c) const { return ((c >> lgt) * blk) + (c & ((1 << lgt) - 1)); }
+};
+__device__ __forceinline__ ColLayout interleaved(int ncol) { return ColLayout{ncol, 0, 30}; }
+
 template <int R, bool FWD, class C>
-__device__ __forceinline__ void fft_stage(C *__restrict__ a, int n, int Ns, int ncol, const C *__restrict__ tw) {
+__device__ __forceinline__ void fft_stage(C *__restrict__ a, int n, int Ns, int ncol, const C *__restrict__ tw,
+                                          ColLayout lay) {
   const int nbf = n / R;
   const int tws = n / (Ns * R);
-  const int col = threadIdx.x % ncol;
+  const int cb = lay.cbase(threadIdx.x % ncol);
   const int j0 = threadIdx.x / ncol;
   const int step = blockDim.x / ncol;
   const int kstep = step % Ns;
@@ -207,14 +217,14 @@ __device__ __forceinline__ void fft_stage(C *__restrict__ a, int n, int Ns, int 
     const int base = (j - k) * R + k;
     C v[R];
 #pragma unroll
-    for (int r = 0; r < R; ++r) v[r] = a[(base + r * Ns) * ncol + col];
+    for (int r = 0; r < R; ++r) v[r] = a[(base + r * Ns) * lay.stride + cb];
     if (Ns > 1) {
 #pragma unroll
       for (int r = 1; r < R; ++r) v[r] = cmul(v[r], root<FWD>(tw, k * r * tws));
     }
     Dft<R, FWD, C>::run(v);
 #pragma unroll
-    for (int r = 0; r < R; ++r) a[(base + r * Ns) * ncol + col] = v[r];
+    for (int r = 0; r < R; ++r) a[(base + r * Ns) * lay.stride + cb] = v[r];
     k += kstep;
     if (k >= Ns) k -= Ns;
   }
@@ -226,10 +236,10 @@ __device__ __forceinline__ void fft_stage(C *__restrict__ a, int n, int Ns, int 
 // `out`. Cost R complex multiply-adds per output.
 template <bool FWD, class C>
 __device__ __noinline__ void fft_stage_generic(const C *__restrict__ in, C *__restrict__ out, int n, int R, int Ns,
-                                               int ncol, const C *__restrict__ tw) {
+                                               int ncol, const C *__restrict__ tw, ColLayout lay) {
   const int tws = n / (Ns * R);
   const int nbf = n / R;
-  const int col = threadIdx.x % ncol;
+  const int cb = lay.cbase(threadIdx.x % ncol);
   const int step = blockDim.x / ncol;
   for (int w = threadIdx.x / ncol; w < n; w += step) {
     const int j = w / R, q = w - (w / R) * R;
@@ -238,9 +248,9 @@ __device__ __noinline__ void fft_stage_generic(const C *__restrict__ in, C *__re
     C acc = czero<C>();
     for (int r = 0; r < R; ++r) {
       const int e = (int)(((long)k * r * tws + (long)((r * q) % R) * nbf) % n);
-      acc = cadd(acc, cmul(in[(base + r * Ns) * ncol + col], root<FWD>(tw, e)));
+      acc = cadd(acc, cmul(in[(base + r * Ns) * lay.stride + cb], root<FWD>(tw, e)));
     }
-    out[(base + q * Ns) * ncol + col] = acc;
+    out[(base + q * Ns) * lay.stride + cb] = acc;
   }
 }
 
@@ -250,22 +260,23 @@ __device__ __noinline__ void fft_stage_generic(const C *__restrict__ in, C *__re
 // Returns the buffer holding the result. Starts and ends with a barrier.
 // With n_stages >= 0 only the first n_stages stages run (see last_stage_output).
 template <bool FWD, class C>
-__device__ C *fft_smem(C *a, C *b, const FftDesc &d, int ncol, int n_stages = -1) {
+__device__ C *fft_smem(C *a, C *b, const FftDesc &d, int ncol, int n_stages = -1, ColLayout lay = ColLayout{0, 0, 30}) {
   __syncthreads();
   const C *tw = twiddles<C>(d);
   int Ns = 1;
   const int nst = n_stages < 0 ? d.nst : n_stages;
+  if (lay.stride == 0) lay = interleaved(ncol);
   for (int s = 0; s < nst; ++s) {
     const int R = d.radix[s];
     switch (R) {
-      case 2: fft_stage<2, FWD>(a, d.n, Ns, ncol, tw); break;
-      case 3: fft_stage<3, FWD>(a, d.n, Ns, ncol, tw); break;
-      case 4: fft_stage<4, FWD>(a, d.n, Ns, ncol, tw); break;
-      case 5: fft_stage<5, FWD>(a, d.n, Ns, ncol, tw); break;
-      case 7: fft_stage<7, FWD>(a, d.n, Ns, ncol, tw); break;
-      case 8: fft_stage<8, FWD>(a, d.n, Ns, ncol, tw); break;
+      case 2: fft_stage<2, FWD>(a, d.n, Ns, ncol, tw, lay); break;
+      case 3: fft_stage<3, FWD>(a, d.n, Ns, ncol, tw, lay); break;
+      case 4: fft_stage<4, FWD>(a, d.n, Ns, ncol, tw, lay); break;
+      case 5: fft_stage<5, FWD>(a, d.n, Ns, ncol, tw, lay); break;
+      case 7: fft_stage<7, FWD>(a, d.n, Ns, ncol, tw, lay); break;
+      case 8: fft_stage<8, FWD>(a, d.n, Ns, ncol, tw, lay); break;
       default: {
-        fft_stage_generic<FWD>(a, b, d.n, R, Ns, ncol, tw);
+        fft_stage_generic<FWD>(a, b, d.n, R, Ns, ncol, tw, lay);
         C *t = a;
         a = b;
         b = t;

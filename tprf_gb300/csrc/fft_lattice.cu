@@ -97,6 +97,90 @@ int launch_axis(const double2 *in, double2 *out, long outer, int n, long inner, 
   return launch_axis_as<FWD, cdf>(in, out, outer, n, inner, scale, stream);
 }
 
+// Two adjacent mesh axes in one pass: the array is [outer, n1, n2, n_target]
+// and a CTA transforms the n1 x n2 plane of nt consecutive targets. The tile
+// sits in shared memory as [i1][i2][t] with both axes digit-reversed; the
+// n2-point transforms see columns (i1, t) with element stride nt, the
+// n1-point ones columns (i2, t) with stride n2 * nt. Each element is read,
+// converted, written and converted back once for both axes. n1, n2 and nt are
+// powers of two with n1 * nt and n2 * nt dividing the 256 threads.
+template <bool FWD, class E>
+__global__ void __launch_bounds__(256) lattice_plane_kernel(const double2 *in, double2 *out, long outer, long n_target,
+                                                            int nt, int lgt, FftDesc d1, FftDesc d2, int lg2,
+                                                            double scale) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  E *a = reinterpret_cast<E *>(smem_raw);
+  const int n1 = d1.n, n2 = d2.n, P = n1 * n2;
+  const long tiles_t = (n_target + nt - 1) / nt;
+  const long o = blockIdx.x / tiles_t;
+  const long t0 = (blockIdx.x - o * tiles_t) * (long)nt;
+  const int ntv = (int)min((long)nt, n_target - t0);
+  const long gbase = o * P * n_target + t0;
+  for (int w = threadIdx.x; w < P * nt; w += blockDim.x) {
+    const int t = w & (nt - 1), p = w >> lgt;
+    const int i1 = p >> lg2, i2 = p & (n2 - 1);
+    const double2 v = t < ntv ? in[gbase + (long)p * n_target + t] : make_double2(0.0, 0.0);
+    a[((d1.rev[i1] << lg2) + d2.rev[i2]) * nt + t] = load_el<E>(v);
+  }
+  // axis 2: columns (i1, t), element i2 at i1 * n2 * nt + i2 * nt + t
+  fft_smem<FWD>(a, (E *)nullptr, d2, n1 * nt, -1, ColLayout{nt, n2 * nt, lgt});
+  // axis 1: columns (i2, t), element i1 at i1 * n2 * nt + (i2 * nt + t)
+  E *r = fft_smem<FWD>(a, (E *)nullptr, d1, n2 * nt);
+  const bool scaled = scale != 1.0;
+  const dfl sd = split_double(scale);
+  for (int w = threadIdx.x; w < P * nt; w += blockDim.x) {
+    const int t = w & (nt - 1), p = w >> lgt;
+    if (t < ntv) out[gbase + (long)p * n_target + t] = store_el(r[p * nt + t], scale, sd, scaled);
+  }
+}
+
+bool pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
+int log2i(int n) {
+  int l = 0;
+  while ((1 << l) < n) ++l;
+  return l;
+}
+
+// Whether the plane pass serves axes of lengths n1, n2 (and with how many targets per tile).
+int plane_targets(int n1, int n2, long n_target) {
+  if (!pow2(n1) || !pow2(n2) || n1 < 2 || n2 < 2) return 0;
+  const int big = std::max(n1, n2);
+  if (big > 256) return 0;
+  int nt = 256 / big;
+  // shared memory: a plane of nt targets, at most 64 KB so that three CTAs share an SM
+  while (nt > 1 && (size_t)n1 * n2 * nt * sizeof(double2) > 64 * 1024) nt /= 2;
+  if ((size_t)n1 * n2 * nt * sizeof(double2) > 64 * 1024) return 0;
+  // generic-radix stages need a second buffer: not used for powers of two
+  while (nt > 1 && nt / 2 >= n_target) nt /= 2;
+  return nt;
+}
+
+template <bool FWD, class E>
+int launch_plane_as(const double2 *in, double2 *out, long outer, int n1, int n2, long n_target, double scale,
+                    cudaStream_t stream) {
+  FftDesc d1, d2;
+  int st = get_fft(n1, &d1);
+  if (st) return st;
+  if ((st = get_fft(n2, &d2))) return st;
+  const int nt = plane_targets(n1, n2, n_target);
+  if (nt < 1) return set_error(TPRF_ERR_UNSUPPORTED_SIZE, "lattice FFT: plane pass does not apply");
+  const size_t smem = (size_t)n1 * n2 * nt * sizeof(E);
+  const long tiles = outer * ((n_target + nt - 1) / nt);
+  if (tiles > 0x7fffffffL) return set_error(TPRF_ERR_INVALID_ARGUMENT, "lattice FFT: too many tiles");
+  TPRF_CUDA(cudaFuncSetAttribute(lattice_plane_kernel<FWD, E>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  lattice_plane_kernel<FWD, E><<<(unsigned)tiles, 256, smem, stream>>>(in, out, outer, n_target, nt, log2i(nt), d1, d2,
+                                                                     log2i(n2), scale);
+  TPRF_LAUNCH_CHECK("lattice_plane_kernel");
+  return TPRF_OK;
+}
+
+template <bool FWD>
+int launch_plane(const double2 *in, double2 *out, long outer, int n1, int n2, long n_target, double scale,
+                 cudaStream_t stream) {
+  if (arith_mode() == kArithFP64) return launch_plane_as<FWD, double2>(in, out, outer, n1, n2, n_target, scale, stream);
+  return launch_plane_as<FWD, cdf>(in, out, outer, n1, n2, n_target, scale, stream);
+}
+
 }  // namespace
 
 // Transform over the 3 mesh dims of [n_w, dims..., n_target]; in == out allowed.
@@ -112,6 +196,32 @@ int launch_lattice_fft(bool forward, long n_w, const int dims[3], long n_target,
   }
   const double scale_last = forward ? 1.0 / (double)nk : 1.0;
   const double2 *src = in;
+  // The two fastest-varying non-trivial axes in one pass where they are powers
+  // of two; the remaining axis (if any) in a one-axis pass, which then scales.
+  int nontriv[3], nn = 0;
+  for (int ax = 0; ax < 3; ++ax)
+    if (dims[ax] > 1) nontriv[nn++] = ax;
+  if (nn >= 2) {
+    const int A = nontriv[nn - 2], B = nontriv[nn - 1];
+    if (plane_targets(dims[A], dims[B], n_target) > 0) {
+      long outer = n_w;
+      for (int a2 = 0; a2 < A; ++a2) outer *= dims[a2];
+      const double scale = (nn == 2) ? scale_last : 1.0;
+      int st = forward ? launch_plane<true>(src, out, outer, dims[A], dims[B], n_target, scale, stream)
+                       : launch_plane<false>(src, out, outer, dims[A], dims[B], n_target, scale, stream);
+      if (st) return st;
+      if (nn == 3) {
+        const int ax = nontriv[0];
+        long outer0 = n_w, inner0 = n_target;
+        for (int a2 = 0; a2 < ax; ++a2) outer0 *= dims[a2];
+        for (int a2 = ax + 1; a2 < 3; ++a2) inner0 *= dims[a2];
+        st = forward ? launch_axis<true>(out, out, outer0, dims[ax], inner0, scale_last, stream)
+                     : launch_axis<false>(out, out, outer0, dims[ax], inner0, scale_last, stream);
+        if (st) return st;
+      }
+      return TPRF_OK;
+    }
+  }
   // fastest-varying mesh dimension first: its pass has the longest contiguous rows
   for (int ax = 2; ax >= 0; --ax) {
     const int n = dims[ax];
