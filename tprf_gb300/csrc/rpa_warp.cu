@@ -30,6 +30,20 @@ struct SparseU {  // U grouped and compacted by columns: rows and FP64 values
 // the grouped column index of the memory offset m = c' * nb + d inside a row
 __device__ __forceinline__ int col_of_offset(int m, int nb) { return (m % nb) * nb + m / nb; }
 
+// Pivot magnitudes: float for double-float elements (from the high words; an
+// underflow to zero reads as a zero pivot and sends the point to the FP64
+// re-solve), double for FP64 elements.
+template <class E> struct Mag {
+  using type = double;
+  static constexpr double big = 1e300;
+};
+template <> struct Mag<cdf> {
+  using type = float;
+  static constexpr float big = 3.0e38f;
+};
+__device__ __forceinline__ double mag2(double2 z) { return cabs2(z); }
+__device__ __forceinline__ float mag2(cdf z) { return __fmaf_rn(z.x.hi, z.x.hi, z.y.hi * z.y.hi); }
+
 template <class E, int G>
 __device__ double rpa_point_warp(const double2 *__restrict__ x, double2 *__restrict__ y, E *M, int N, int nb,
                                  const SparseU &u, int lane, unsigned gmask, bool &singular) {
@@ -54,13 +68,14 @@ __device__ double rpa_point_warp(const double2 *__restrict__ x, double2 *__restr
     MM(r, c) = s;
   }
   __syncwarp(gmask);
-  double pmin = 1e300;
+  using MagT = typename Mag<E>::type;
+  MagT pmin = Mag<E>::big;
   bool sing = false;
   for (int j = 0; j < N; ++j) {
     int p = j;
-    double best = -1.0;
+    MagT best = -1;
     for (int i = j + lane; i < N; i += G) {
-      const double v = el_abs2(MM(i, j));
+      const MagT v = mag2(MM(i, j));
       if (v > best) {
         best = v;
         p = i;
@@ -68,15 +83,15 @@ __device__ double rpa_point_warp(const double2 *__restrict__ x, double2 *__restr
     }
 #pragma unroll
     for (int o = G / 2; o > 0; o >>= 1) {
-      const double ob = __shfl_xor_sync(gmask, best, o);
+      const MagT ob = __shfl_xor_sync(gmask, best, o);
       const int op = __shfl_xor_sync(gmask, p, o);
       if (ob > best || (ob == best && op < p)) {
         best = ob;
         p = op;
       }
     }
-    if (best == 0.0) sing = true;
-    pmin = fmin(pmin, best);
+    if (best == 0) sing = true;
+    pmin = pmin < best ? pmin : best;
     if (p != j) {
       for (int c = lane; c < W; c += G) {
         const E t = MM(j, c);
@@ -114,7 +129,7 @@ __device__ double rpa_point_warp(const double2 *__restrict__ x, double2 *__restr
   __syncwarp(gmask);
 #undef MM
   const double am = (double)amax * (double)amax;
-  return pmin > 0.0 ? am / pmin : 1e300;
+  return pmin > 0 ? am / (double)pmin : 1e300;
 }
 
 template <class E, int G>
