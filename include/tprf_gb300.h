@@ -87,6 +87,11 @@ int tprf_measure_fp64_tflops(double *tflops, void *scratch, size_t scratch_bytes
  * and F are non-NULL and capacity >= n_fit * n_mom, also the data rows of the
  * fit points and F [n_mom][n_fit] complex, with moments c = F g[rows]. */
 int tprf_tail_fit_matrix(double beta, int n_iw, int capacity, int *n_fit, int *n_mom, int *rows, double *F);
+/* The same for either statistic (fermion != 0: n = n_max, data index n + n_max of
+ * iv_n; fermion == 0: n = nw, data index m + nw - 1 of iw_m, fitting the positive
+ * indices 1 .. nw-1 and their mirrors), as tprf_chi_tr_from_chi_wr applies it. */
+int tprf_tail_fit_matrix_stat(double beta, int n, int fermion, int capacity, int *n_fit, int *n_mom,
+                              int *rows, double *F);
 
 /* Host-only: exact inverse of the 8x8 Vandermonde matrix V[m][j] = m^j
  * (m = 1..8), the matrix fourier_matsubara.cpp:56-71 approximates (used by
@@ -174,6 +179,27 @@ int tprf_chi0_w0r_from_grt_PH(double beta, int n_tau, const int dims[3], int nb,
  * chi_tr [n_tau, n_r, n_target] -> chi_wr [2 nw - 1, n_r, n_target]. */
 int tprf_chi_wr_from_chi_tr(double beta, int n_tau, int nw, long n_r, long n_target,
                             const double *chi_tr, double *chi_wr, void *stream);
+
+/* ---- inverse transforms -------------------------------------------------------
+ * Fermionic tau -> i nu with the fit_derivatives tail (fermion branch of
+ * fourier_matsubara.cpp:123-184: input multiplied by exp(i pi tau / beta),
+ * b = (0, 1, -1)).
+ * Replaces triqs_tprf::fourier_tr_to_wr(g_tr_cvt, int nw) (gf.hpp:306,
+ *   gf.cpp:257-260; lattice/fourier.hpp:133-163).
+ * g_tr [n_tau, n_r, n_target] -> g_wr [2 n_iw, n_r, n_target] (n = -n_iw .. n_iw-1);
+ * n_iw < 0: (n_tau - 1) / 6. Requires n_tau - 1 >= 2 n_iw. */
+int tprf_fourier_tr_to_wr(double beta, int n_tau, int n_iw, long n_r, long n_target,
+                          const double *g_tr, double *g_wr, void *stream);
+
+/* Bosonic i omega -> tau with the tail fit on the bosonic mesh (boson branch of
+ * fourier_matsubara.cpp:218-308: b = (-1/2, -1, 1), chi[L] = +(chi[0] + m1)).
+ * Replaces triqs_tprf::chi_tr_from_chi_wr(chi_wr_cvt, int ntau)
+ *   (chi_imtime.hpp:105, chi_imtime.cpp:284-287; lattice/fourier.hpp:99-130).
+ * chi_wr [2 nw - 1, n_r, n_target] -> chi_tr [n_tau, n_r, n_target];
+ * n_tau < 0: 6 nw + 1. moments: NULL (fit) or [3][n_r * n_target] m1, m2, m3. */
+int tprf_chi_tr_from_chi_wr(double beta, int nw, int n_tau, long n_r, long n_target,
+                            const double *chi_wr, const double *moments, double *chi_tr,
+                            void *stream);
 
 /* Trapezoid integral over tau.
  * Replaces triqs_tprf::chi_w0r_from_chi_tr(chi_tr_cvt) (chi_imtime.hpp:82,

@@ -27,6 +27,7 @@ __all__ = [
     "tail_fit_indices", "tail_fit_matrix", "tail_fit",
     "g0_tail_moments_wr",
     "fourier_wr_to_tr", "fit_derivatives", "vandermonde_inverse",
+    "fourier_tr_to_wr", "chi_tr_from_chi_wr", "default_n_iw", "tail_order",
     "chi0_tr_from_grt_PH", "chi_wr_from_chi_tr", "chi_wk_from_chi_wr",
     "chi_wr_from_chi_wk", "chi_trapz_tau", "chi_w0r_from_chi_tr",
     "chi0_w0r_from_grt_PH", "chi0_wr_from_grt_PH",
@@ -178,43 +179,60 @@ TAIL_N_MAX = 30
 TAIL_MAX_ORDER = 9
 
 
-def tail_fit_indices(n_max: int):
-    """Data indices (0 .. 2 n_max - 1) of the fit points: n_pts on each side.
+def tail_fit_indices(n_max: int, statistic: str = "Fermion"):
+    """Data indices of the fit points: n_pts on each side of the mesh.
 
-    n_pts = round(0.2 n_max) capped at 30, placed evenly (rounded half up) from
-    round(0.8 n_max) to n_max - 1, mirrored to the negative frequencies.
+    Fermion (data index n + n_max for n = -n_max .. n_max-1): the positive
+    indices 0 .. n_max-1. Boson (data index m + n_max - 1 for m = -(n_max-1) ..
+    n_max-1, n_max = nw): the positive indices 1 .. nw-1. Over that range of
+    `count` indices, n_pts = round(0.2 count) capped at 30, placed evenly
+    (rounded half up) over its top 20 %, mirrored to the negative frequencies.
     """
-    n_pts = max(1, min((2 * n_max + 5) // 10, TAIL_N_MAX))
-    n_hi = n_max - 1
-    n_lo = min(n_hi, (8 * n_max + 5) // 10)
+    if statistic == "Fermion":
+        i_min, i_max = 0, n_max - 1
+    else:
+        i_min, i_max = 1, n_max - 1
+    count = i_max - i_min + 1
+    n_pts = max(1, min((2 * count + 5) // 10, TAIL_N_MAX))
+    n_hi = i_max
+    n_lo = min(n_hi, i_min + (8 * count + 5) // 10)
     if n_pts == 1:
         pos = [n_hi]
     else:
         span = n_hi - n_lo
         pos = [n_lo + (2 * j * span + (n_pts - 1)) // (2 * (n_pts - 1)) for j in range(n_pts)]
-    ns = [-n - 1 for n in reversed(pos)] + pos  # Matsubara integers
-    return np.array([n + n_max for n in ns], dtype=np.int64)
+    if statistic == "Fermion":
+        ns = [-n - 1 for n in reversed(pos)] + pos  # Matsubara integers
+        return np.array([n + n_max for n in ns], dtype=np.int64)
+    ms = [-m for m in reversed(pos)] + pos
+    return np.array([m + n_max - 1 for m in ms], dtype=np.int64)
 
 
-def tail_order(beta: float, n_max: int) -> int:
-    omega_max = (2 * n_max - 1) * np.pi / beta
+def _omega_max(beta: float, n_max: int, statistic: str) -> float:
+    return (2 * n_max - 1) * np.pi / beta if statistic == "Fermion" else 2 * (n_max - 1) * np.pi / beta
+
+
+def tail_order(beta: float, n_max: int, statistic: str = "Fermion") -> int:
+    omega_max = _omega_max(beta, n_max, statistic)
     if omega_max > 1.0:
         order = int(math.floor(16.0 * math.log(10.0) / math.log(omega_max)))
     else:
         order = TAIL_MAX_ORDER
-    n_eq = len(tail_fit_indices(n_max))
+    n_eq = len(tail_fit_indices(n_max, statistic))
     return max(0, min(order, TAIL_MAX_ORDER, n_eq - 1))
 
 
-def tail_fit_matrix(beta: float, n_max: int):
+def tail_fit_matrix(beta: float, n_max: int, statistic: str = "Fermion"):
     """Return (idx, F, A): moments c = F @ g[idx]; A is the fit design matrix.
 
-    c_p are the coefficients of 1/(iv)^p, p = 0..P.
+    c_p are the coefficients of 1/(iw)^p, p = 0..P. n_max is the fermionic
+    n_max or the bosonic nw.
     """
-    idx = tail_fit_indices(n_max)
-    P = tail_order(beta, n_max)
-    iw = fermionic_iw(beta, n_max)[idx]
-    omega_max = (2 * n_max - 1) * np.pi / beta
+    idx = tail_fit_indices(n_max, statistic)
+    P = tail_order(beta, n_max, statistic)
+    freqs = fermionic_iw(beta, n_max) if statistic == "Fermion" else bosonic_iw(beta, n_max)
+    iw = freqs[idx]
+    omega_max = _omega_max(beta, n_max, statistic)
     z = omega_max / iw
     A = z[:, None] ** np.arange(P + 1)[None, :]
     pinv = np.linalg.pinv(A)
@@ -222,13 +240,13 @@ def tail_fit_matrix(beta: float, n_max: int):
     return idx, F, A
 
 
-def tail_fit(g_w: np.ndarray, beta: float, n_max: int):
-    """Fit moments for every column of g_w [2 n_max, ...]. Returns (c [P+1, ...], err)."""
-    idx, F, A = tail_fit_matrix(beta, n_max)
+def tail_fit(g_w: np.ndarray, beta: float, n_max: int, statistic: str = "Fermion"):
+    """Fit moments for every column of g_w [n_freq, ...]. Returns (c [P+1, ...], err)."""
+    idx, F, A = tail_fit_matrix(beta, n_max, statistic)
     rest = g_w.shape[1:]
     g = g_w.reshape(g_w.shape[0], -1)[idx]
     c = F @ g
-    omega_max = (2 * n_max - 1) * np.pi / beta
+    omega_max = _omega_max(beta, n_max, statistic)
     d = c / (omega_max ** np.arange(c.shape[0]))[:, None]
     err = np.max(np.abs(A @ d - g)) if g.size else 0.0
     return c.reshape((c.shape[0],) + rest), float(err)
@@ -401,6 +419,88 @@ def chi_wr_from_chi_tr(chi_tr: np.ndarray, beta: float, nw: int) -> np.ndarray:
     iw = bosonic_iw(beta, nw)[:, None]
     gw = out[(m + L) % L] + a1 / (iw - b1) + a2 / (iw - b2) + a3 / (iw - b3)
     return gw.reshape((2 * nw - 1,) + rest)
+
+
+def default_n_iw(n_tau: int) -> int:
+    """Frequency count of the adjoint of a time mesh: (n_tau - 1) / 6, the inverse of
+    default_n_tau (TRIQS make_adjoint_mesh, recalled; callers can pass it)."""
+    return (n_tau - 1) // 6
+
+
+def fourier_tr_to_wr(g_tr: np.ndarray, beta: float, n_max: int = -1) -> np.ndarray:
+    """Fermionic tau -> i nu per r and element (``gf.cpp:257-260`` ->
+    ``lattice/fourier.hpp:133-163`` -> ``fourier_matsubara.cpp:123-184``, fermion branch).
+
+    m1 = -(g[0] + g[L]); m2, m3 from ``fit_derivatives`` with the fermion sign;
+    b = (0, 1, -1), a = (m1-m3, (m2+m3)/2, (m3-m2)/2); gin[t] = (beta/L)
+    exp(i pi tau_t/beta) (g(tau_t) - model(tau_t)) for t < L; FFTW_BACKWARD;
+    g(i nu_n) = out[(n+L)%L] + sum_j a_j/(i nu_n - b_j), n = -n_max .. n_max-1.
+    """
+    n_tau = g_tr.shape[0]
+    L = n_tau - 1
+    if n_max < 0:
+        n_max = default_n_iw(n_tau)
+    if L < 2 * n_max:
+        raise RuntimeError("Fourier: the time mesh must be at least twice as long as the number of positive frequencies")
+    rest = g_tr.shape[1:]
+    g = g_tr.reshape(n_tau, -1)
+    m23 = fit_derivatives(g, beta, "Fermion")
+    m1 = -(g[0] + g[L])
+    m2, m3 = m23[0], m23[1]
+    b1, b2, b3 = 0.0, 1.0, -1.0
+    a1, a2, a3 = m1 - m3, (m2 + m3) / 2, (m3 - m2) / 2
+    tau = tau_points(beta, n_tau)[:L]
+    model = _one_fermion(a1, b1, tau, beta) + _one_fermion(a2, b2, tau, beta) + _one_fermion(a3, b3, tau, beta)
+    gin = (beta / L) * np.exp(1j * np.pi * tau / beta)[:, None] * (g[:L] - model)
+    out = np.fft.ifft(gin, axis=0) * L  # FFTW_BACKWARD, unscaled
+    n = np.arange(-n_max, n_max)
+    iw = fermionic_iw(beta, n_max)[:, None]
+    gw = out[(n + L) % L] + a1 / (iw - b1) + a2 / (iw - b2) + a3 / (iw - b3)
+    return gw.reshape((2 * n_max,) + rest)
+
+
+def chi_tr_from_chi_wr(chi_wr: np.ndarray, beta: float, n_tau: int = -1, moments=None) -> np.ndarray:
+    """Bosonic i omega -> tau per r and element (``chi_imtime.cpp:284-287`` ->
+    ``lattice/fourier.hpp:99-130`` -> ``fourier_matsubara.cpp:218-308``, boson branch).
+
+    Moments m1..m3 from the tail fit on the bosonic mesh (or given); b = (-1/2, -1, 1),
+    a1 = 4(m1-m3)/3, a2 = m3-(m1+m2)/2, a3 = m1/6+m2/2+m3/3; the difference
+    (1/beta)(chi - model) at row (m+L)%L, FFTW_FORWARD; chi(tau_t) = out[t] +
+    sum_j oneBoson(a_j, b_j, tau_t); chi[L] = +(chi[0] + m1).
+    """
+    nwt = chi_wr.shape[0]
+    nw = (nwt + 1) // 2
+    if n_tau < 0:
+        n_tau = 6 * nw + 1
+    L = n_tau - 1
+    if L < 2 * nw:
+        raise RuntimeError("Inverse Fourier: the time mesh must be at least twice as long as the freq mesh")
+    rest = chi_wr.shape[1:]
+    g = chi_wr.reshape(nwt, -1)
+    if moments is None:
+        c, err = tail_fit(g, beta, nw, "Boson")
+        if err > 1e-3:
+            raise RuntimeError(f"High frequency moments have an error greater than 1e-3: {err}")
+        if c.shape[0] < 4:
+            raise RuntimeError("Inverse Fourier requires at least a proper 3rd high-frequency moment")
+        m1, m2, m3 = c[1], c[2], c[3]
+    else:
+        mm = np.asarray(moments).reshape(3, -1)
+        m1, m2, m3 = mm[0], mm[1], mm[2]
+    b1, b2, b3 = -0.5, -1.0, 1.0
+    a1 = 4 * (m1 - m3) / 3
+    a2 = m3 - (m1 + m2) / 2
+    a3 = m1 / 6 + m2 / 2 + m3 / 3
+    iw = bosonic_iw(beta, nw)[:, None]
+    m = np.arange(-(nw - 1), nw)
+    gin = np.zeros((L, g.shape[1]), dtype=complex)
+    gin[(m + L) % L] = (1.0 / beta) * (g - (a1 / (iw - b1) + a2 / (iw - b2) + a3 / (iw - b3)))
+    out = np.fft.fft(gin, axis=0)
+    tau = tau_points(beta, n_tau)[:L]
+    gt = np.empty((n_tau, g.shape[1]), dtype=complex)
+    gt[:L] = out + _one_boson(a1, b1, tau, beta) + _one_boson(a2, b2, tau, beta) + _one_boson(a3, b3, tau, beta)
+    gt[L] = gt[0] + m1
+    return gt.reshape((n_tau,) + rest)
 
 
 # ----------------------------------------------------------------------------

@@ -56,6 +56,22 @@ def test_tail_fit_matrix_matches_oracle(lib):
         assert np.abs(Fc - Fo).max() <= 1e-10 * np.abs(Fo).max()
 
 
+def test_bosonic_tail_fit_matrix_matches_oracle(lib):
+    """The bosonic mesh's fit (chi_tr_from_chi_wr) follows the same definition in both."""
+    for beta, nw in [(10.0, 64), (20.0, 256), (5.0, 33), (40.0, 128), (2.0, 12)]:
+        nf, nm = ctypes.c_int(), ctypes.c_int()
+        assert lib.tprf_tail_fit_matrix_stat(beta, nw, 0, 0, ctypes.byref(nf), ctypes.byref(nm), None, None) == 0
+        rows = (ctypes.c_int * nf.value)()
+        F = (ctypes.c_double * (2 * nf.value * nm.value))()
+        assert lib.tprf_tail_fit_matrix_stat(beta, nw, 0, nf.value * nm.value, ctypes.byref(nf), ctypes.byref(nm),
+                                             rows, F) == 0
+        idx, Fo, _ = O.tail_fit_matrix(beta, nw, "Boson")
+        assert np.array_equal(np.array(rows[:]), idx)
+        assert 0 not in idx - (nw - 1)  # iw = 0 is never a fit point
+        Fc = np.frombuffer(F, dtype=np.complex128).reshape(nm.value, nf.value)
+        assert np.abs(Fc - Fo).max() <= 1e-10 * np.abs(Fo).max()
+
+
 def test_vandermonde_inverse_bitwise(lib):
     v = (ctypes.c_double * 64)()
     lib.tprf_vandermonde_inverse8(v)

@@ -188,6 +188,57 @@ def test_tau_to_w(cuda_lib, nw, n_tau):
     assert rel_err(T.chi_w0r_from_chi_tr(chi_tr).data, O.chi_w0r_from_chi_tr(chi_tr_ref, beta)) < PARITY_RTOL
 
 
+@pytest.mark.parametrize("n_iw,n_tau", [(64, -1), (40, 385), (17, 131)])  # 131: L = 2 5 13 (generic radix)
+def test_fourier_tr_to_wr(cuda_lib, n_iw, n_tau):
+    """Fermionic tau -> i nu (the inverse of fourier_wr_to_tr): G(tau, r) of the
+    square lattice to G(i nu, r), against the oracle."""
+    T = tp()
+    hopf, dims, beta, n_max = CASES[0]
+    _, _, g_wr, g_wr_ref = _g_wr(hopf(), dims, beta, n_max)
+    g_tr_ref = O.fourier_wr_to_tr(g_wr_ref, beta, n_tau)
+    tmesh = T.MeshImTime(beta, "Fermion", g_tr_ref.shape[0])
+    g_tr = T.Gf(mesh=T.MeshProduct(tmesh, T.MeshCycLat(dims=dims)), data=g_tr_ref)
+    nw = n_iw if n_tau > 0 else -1
+    out = T.fourier_tr_to_wr(g_tr, nw=nw)
+    n_expect = n_iw if n_tau > 0 else (g_tr_ref.shape[0] - 1) // 6
+    ref = O.fourier_tr_to_wr(g_tr_ref, beta, n_expect)
+    assert tuple(out.data.shape) == ref.shape == (2 * n_expect,) + g_tr_ref.shape[1:]
+    assert rel_err(out.data, ref) < PARITY_RTOL
+
+
+@pytest.mark.parametrize("nw,n_tau,mode", [(64, -1, "fit"), (40, 301, "fit"), (33, 250, "moments")])
+def test_chi_tr_from_chi_wr(cuda_lib, nw, n_tau, mode):
+    """Bosonic i omega -> tau (the inverse of chi_wr_from_chi_tr) with the tail fit on
+    the bosonic mesh or given moments, against the oracle."""
+    T = tp()
+    hopf, dims, beta, n_max = CASES[0]
+    _, _, _, g_wr_ref = _g_wr(hopf(), dims, beta, n_max)
+    chi_tr_ref = O.chi0_tr_from_grt_PH(O.fourier_wr_to_tr(g_wr_ref, beta), dims)
+    chi_wr_ref = O.chi_wr_from_chi_tr(chi_tr_ref, beta, nw)
+    mom = None
+    if mode == "moments":
+        rng = np.random.default_rng(nw)
+        mom = rand_c(rng, 3, *chi_wr_ref.shape[1:])
+    wmesh = T.MeshImFreq(beta, "Boson", nw)
+    chi_wr = T.Gf(mesh=T.MeshProduct(wmesh, T.MeshCycLat(dims=dims)), data=chi_wr_ref)
+    out = T.chi_tr_from_chi_wr(chi_wr, ntau=n_tau, moments=mom)
+    ref = O.chi_tr_from_chi_wr(chi_wr_ref, beta, n_tau, moments=mom)
+    assert tuple(out.data.shape) == ref.shape == ((6 * nw + 1) if n_tau < 0 else n_tau,) + chi_wr_ref.shape[1:]
+    assert rel_err(out.data, ref) < PARITY_RTOL
+
+
+def test_inverse_transforms_reject_short_time_mesh(cuda_lib):
+    T = tp()
+    g_tr = T.Gf(mesh=T.MeshProduct(T.MeshImTime(5.0, "Fermion", 41), T.MeshCycLat(dims=(2, 1, 1))),
+                data=np.zeros((41, 2, 1, 1), complex))
+    with pytest.raises(T.TprfError):
+        T.fourier_tr_to_wr(g_tr, nw=21)
+    chi_wr = T.Gf(mesh=T.MeshProduct(T.MeshImFreq(5.0, "Boson", 30), T.MeshCycLat(dims=(2, 1, 1))),
+                  data=np.zeros((59, 2, 1), complex))
+    with pytest.raises(T.TprfError):
+        T.chi_tr_from_chi_wr(chi_wr, ntau=50)
+
+
 # ---------------------------------------------------------------------------
 # (c) bubble
 

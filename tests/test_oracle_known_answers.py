@@ -138,3 +138,35 @@ def test_mesh_too_short_raises():
         O.fourier_wr_to_tr(g, 1.0, n_tau=20)
     with pytest.raises(RuntimeError):
         O.chi_wr_from_chi_tr(np.zeros((21, 1), complex), 1.0, nw=11)
+
+
+def test_inverse_transforms_known_answers():
+    """The inverse transforms (fourier_tr_to_wr, chi_tr_from_chi_wr) on analytic
+    one-pole functions and as round trips with the forward transforms; the GW
+    test of the reference (test/python/gw.py:88-103) uses both directions."""
+    beta, n_max = 10.0, 64
+    eps = np.array([-0.7, 0.3, 1.1])
+    iv = O.fermionic_iw(beta, n_max)[:, None]
+    g = 1.0 / (iv - eps[None])
+    tau = O.tau_points(beta, 6 * n_max + 1)[:, None]
+    g_tau = -np.exp(-eps[None] * tau) / (1 + np.exp(-beta * eps[None]))
+    # analytic G(tau) of a level -> 1/(iv - e), up to the time mesh's discretisation
+    assert np.abs(O.fourier_tr_to_wr(g_tau, beta, n_max) - g).max() < 1e-9
+    # iv -> tau -> iv
+    assert np.abs(O.fourier_tr_to_wr(O.fourier_wr_to_tr(g, beta), beta, n_max) - g).max() < 1e-10
+    # bosonic: chi(iw) = 1/(iw - w0) - 1/(iw + w0) and its tau form
+    nw = 64
+    w = O.bosonic_iw(beta, nw)[:, None]
+    w0 = np.array([0.5, 1.3])
+    chi = 1.0 / (w - w0[None]) - 1.0 / (w + w0[None])
+    taub = O.tau_points(beta, 6 * nw + 1)[:, None]
+
+    def bos(x):
+        return -np.exp(-x * taub) / (1 - np.exp(-beta * x))
+
+    chi_tau = bos(w0[None]) - bos(-w0[None])
+    ct = O.chi_tr_from_chi_wr(chi, beta)
+    assert np.abs(ct - chi_tau).max() < 1e-5 * np.abs(chi_tau).max()
+    assert np.abs(O.chi_wr_from_chi_tr(ct, beta, nw) - chi).max() < 1e-10 * np.abs(chi).max()
+    with pytest.raises(RuntimeError):
+        O.fourier_tr_to_wr(g_tau, beta, 200)  # time mesh shorter than 2 n_max

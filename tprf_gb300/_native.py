@@ -50,6 +50,11 @@ SIGNATURES = {
     "tprf_chi_wr_from_chi_tr": (c_int, [c_double, c_int, c_int, c_long, c_long, c_void_p, c_void_p, c_void_p]),
     "tprf_chi_w0r_from_chi_tr": (c_int, [c_double, c_int, c_long, c_long, c_void_p, c_void_p, c_void_p]),
     "tprf_solve_rpa_PH": (c_int, [c_long, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "tprf_fourier_tr_to_wr": (c_int, [c_double, c_int, c_int, c_long, c_long, c_void_p, c_void_p, c_void_p]),
+    "tprf_chi_tr_from_chi_wr": (c_int, [c_double, c_int, c_int, c_long, c_long, c_void_p, c_void_p, c_void_p,
+                                        c_void_p]),
+    "tprf_tail_fit_matrix_stat": (c_int, [c_double, c_int, c_int, c_int, ctypes.POINTER(c_int), ctypes.POINTER(c_int),
+                                          c_void_p, c_void_p]),
     "tprf_solve_rpa_PH_to_host_workspace_bytes": (c_size_t, [c_long, c_int, c_int]),
     "tprf_solve_rpa_PH_to_host": (c_int, [c_long, c_int, c_void_p, c_void_p, c_void_p, c_long, c_void_p, c_size_t,
                                           c_void_p]),

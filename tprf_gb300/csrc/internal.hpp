@@ -54,14 +54,17 @@ struct FftDesc {
 // Returns 0 or a status; fills *out. Cached per (device, n).
 int get_fft(int n, FftDesc *out);
 
-// iv -> tau (fermion) tables for one (beta, n_iw, n_tau).
+// Matsubara -> tau tables for one (beta, n, n_tau, statistic). Fermion: n = n_max,
+// inputs iv_n for n = -n_max .. n_max-1; boson: n = nw, inputs iw_m for
+// m = -(nw-1) .. nw-1.
 struct NuTauPlan {
   double beta;
   int n_iw, n_tau, L;
+  int fermion, n_in, in0;  // statistic, input count, frequency integer of input 0
   FftDesc fft;
-  const double2 *den;    // [3][2 n_iw]: 1/(iv_n - b_j), b = (0, 1, -1)
-  const double2 *phase;  // [L]: exp(-i pi tau_t / beta)
-  const double *ftail;   // [3][L]: oneFermion(1, b_j, tau_t)
+  const double2 *den;    // [3][n_in]: 1/(iw - b_j), b = (0, 1, -1) fermion, (-1/2, -1, 1) boson
+  const double2 *phase;  // [L]: exp(-i pi tau_t / beta) (fermion), 1 (boson)
+  const double *ftail;   // [3][L]: oneFermion / oneBoson(1, b_j, tau_t)
   int n_fit, n_mom;      // fit points, number of fitted moments (P+1)
   const int *fit_row;    // [n_fit]: data index of each fit point
   const double2 *fitF;   // [n_mom][n_fit]: moments = F g
@@ -74,17 +77,21 @@ struct NuTauPlan {
   const float4 *fitFf, *fitGf;
 };
 int get_nu_tau_plan(double beta, int n_iw, int n_tau, const NuTauPlan **out);
+int get_nu_tau_plan_stat(double beta, int n, int n_tau, bool fermion, const NuTauPlan **out);
 
-// tau -> i omega (boson) tables for one (beta, n_tau, nw).
+// tau -> Matsubara tables for one (beta, n_tau, n, statistic). Boson: n = nw,
+// outputs m = -(nw-1) .. nw-1; fermion: n = n_max, outputs n = -n_max .. n_max-1.
 struct TauWPlan {
   double beta;
   int n_tau, nw, L;
+  int fermion, n_out, out0;  // statistic, output count, frequency integer of output 0
   FftDesc fft;
-  const double *btail;   // [3][L]: oneBoson(1, b_j, tau_t), b = (-1/2, -1, 1)
-  const double2 *den;    // [3][2 nw - 1]: 1/(i w_m - b_j)
-  // Tail model folded after the FFT: chi(i w_m) = (beta/L) FFT(chi)[k_m] + sum_j a_j K[j][m],
-  //   K[j][m] = den[j][m] - (beta/L) FFT(btail[j])[k_m],  k_m = (m + L) % L.
-  const double2 *K;      // [3][2 nw - 1]
+  const double *btail;   // [3][L]: oneBoson / oneFermion(1, b_j, tau_t)
+  const double2 *den;    // [3][n_out]: 1/(i w_m - b_j)
+  const double2 *ph;     // [L]: input phase exp(i pi tau_t / beta) (fermion), 1 (boson)
+  // Tail model folded after the FFT: chi(i w_m) = (beta/L) FFT(ph chi)[k_m] + sum_j a_j K[j][m],
+  //   K[j][m] = den[j][m] - (beta/L) FFT(ph btail[j])[k_m],  k_m = (m + L) % L.
+  const double2 *K;      // [3][n_out]
   const float4 *Kf;
 };
 
@@ -93,6 +100,7 @@ struct TauWPlan {
 enum Arith : int { kArithDF64 = 0, kArithFP64 = 1, kArithDF64All = 2 };
 int arith_mode();
 int get_tau_w_plan(double beta, int n_tau, int nw, const TauWPlan **out);
+int get_tau_w_plan_stat(double beta, int n_tau, int n, bool fermion, const TauWPlan **out);
 
 // Exact inverse of the 8x8 Vandermonde V[m][j] = m^j (m = 1..8), uploaded to
 // __constant__ memory of the TU that needs it.

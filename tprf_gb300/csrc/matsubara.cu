@@ -1,10 +1,12 @@
 // Kernel (b), Matsubara part, and kernel (c), the particle-hole bubble.
 //
-//  * iv -> tau (fermion) with the three-pole tail model and the tail fit:
+//  * Matsubara -> tau with the three-pole tail model and the tail fit:
 //    restates c++/triqs_tprf/fourier/fourier_matsubara.cpp:218-308 as driven
-//    per r by lattice/fourier.hpp:99-130.
-//  * tau -> i omega (boson) with the fit_derivatives moments: restates
-//    fourier_matsubara.cpp:42-97 and :123-184, driven by lattice/fourier.hpp:133-163.
+//    per r by lattice/fourier.hpp:99-130; fermionic (fourier_wr_to_tr) and
+//    bosonic (chi_tr_from_chi_wr).
+//  * tau -> Matsubara with the fit_derivatives moments: restates
+//    fourier_matsubara.cpp:42-97 and :123-184, driven by lattice/fourier.hpp:133-163;
+//    bosonic (chi_wr_from_chi_tr, the bubble) and fermionic (fourier_tr_to_wr).
 //  * bubble chi0_abcd(tau_i, r) = G_da(tau_i, r) G_bc(tau_{N-1-i}, -r):
 //    restates lattice/chi_imtime.cpp:88-136 (product at :127); the fused
 //    bubble + tau -> w of chi_imtime.cpp:139-182; the trapezoid branch of
@@ -24,6 +26,8 @@
 // arithmetic run in double-float pairs on the FP32 pipe by default
 // (tprf_set_arithmetic), with inputs and outputs in complex128.
 #include <algorithm>
+
+#include <type_traits>
 
 #include "common.cuh"
 
@@ -69,10 +73,29 @@ __device__ __forceinline__ float cabsf_approx(cdf z) {
   return sqrtf(x * x + y * y);
 }
 
+// The three-pole tail amplitudes a_j from the moments m1..m3
+// (fourier_matsubara.cpp:156-171 and 268-284): fermion b = (0, 1, -1),
+// a = (m1-m3, (m2+m3)/2, (m3-m2)/2); boson b = (-1/2, -1, 1),
+// a = (4(m1-m3)/3, m3-(m1+m2)/2, m1/6+m2/2+m3/3). am[3] keeps m1.
+template <class C>
+__device__ __forceinline__ void tail_amplitudes(int fermion, double2 m1, double2 m2, double2 m3, C *am, int ic,
+                                                int c) {
+  if (fermion) {
+    am[0 * ic + c] = from_d2<C>(csub(m1, m3));
+    am[1 * ic + c] = from_d2<C>(cscale(cadd(m2, m3), 0.5));
+    am[2 * ic + c] = from_d2<C>(cscale(csub(m3, m2), 0.5));
+  } else {
+    am[0 * ic + c] = from_d2<C>(cscale(csub(m1, m3), 4.0 / 3.0));
+    am[1 * ic + c] = from_d2<C>(csub(m3, cscale(cadd(m1, m2), 0.5)));
+    am[2 * ic + c] = from_d2<C>(cadd(cadd(cscale(m1, 1.0 / 6.0), cscale(m2, 0.5)), cscale(m3, 1.0 / 3.0)));
+  }
+  am[3 * ic + c] = from_d2<C>(m1);
+}
+
 // ---------------------------------------------------------------------------
-// iv -> tau. The tail model enters after the FFT through the folded tables
-// (exactly the reference's model subtracted before and added after the FFT,
-// by linearity): G(tau_t) = P[t] FFT(g)[t] + sum_j a_j Q[j][t].
+// Matsubara -> tau. The tail model enters after the FFT through the folded
+// tables (exactly the reference's model subtracted before and added after the
+// FFT, by linearity): G(tau_t) = P[t] FFT(g)[t] + sum_j a_j Q[j][t].
 
 template <class C>
 __global__ void __launch_bounds__(kMatsubaraThreads, 2) nu_to_tau_kernel(NuTauPlan p, const double2 *__restrict__ gw,
@@ -81,7 +104,7 @@ __global__ void __launch_bounds__(kMatsubaraThreads, 2) nu_to_tau_kernel(NuTauPl
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ unsigned s_res;
   C *a = reinterpret_cast<C *>(smem_raw);
-  const int L = p.L, n_iw = p.n_iw, nnu = 2 * p.n_iw;
+  const int L = p.L, nnu = p.n_in;
   const int *rev = p.fft.rev;
   C *b = p.fft.has_generic ? a + (size_t)L * ic : nullptr;
   C *am = a + (size_t)(p.fft.has_generic ? 2 : 1) * L * ic;  // [4][ic]: a1, a2, a3, m1; then the fit coefficients
@@ -95,7 +118,7 @@ __global__ void __launch_bounds__(kMatsubaraThreads, 2) nu_to_tau_kernel(NuTauPl
   // frequency n sits at FFT row (n + L) % L, stored at its digit-reversed position
   for (int w = tid; w < nnu * ic; w += nthr) {
     const int c = w & (ic - 1), n = w >> lg;
-    if (c < ncol) a[rev[(n - n_iw + L) % L] * ic + c] = from_d2<C>(gw[(long)n * Ccols + col0 + c]);
+    if (c < ncol) a[rev[(n + p.in0 + L) % L] * ic + c] = from_d2<C>(gw[(long)n * Ccols + col0 + c]);
   }
   __syncthreads();
   if (mom == nullptr) {
@@ -119,13 +142,8 @@ __global__ void __launch_bounds__(kMatsubaraThreads, 2) nu_to_tau_kernel(NuTauPl
       const double2 d = csub(model, gw[(long)p.fit_row[i] * Ccols + col0 + c]);
       atomicMax(&s_res, __float_as_uint((float)sqrt(cabs2(d))));
     }
-    for (int c = tid; c < ic; c += nthr) {
-      const double2 m1 = coef[1 * ic + c], m2 = coef[2 * ic + c], m3 = coef[3 * ic + c];
-      am[0 * ic + c] = from_d2<C>(csub(m1, m3));
-      am[1 * ic + c] = from_d2<C>(cscale(cadd(m2, m3), 0.5));
-      am[2 * ic + c] = from_d2<C>(cscale(csub(m3, m2), 0.5));
-      am[3 * ic + c] = from_d2<C>(m1);
-    }
+    for (int c = tid; c < ic; c += nthr)
+      tail_amplitudes(p.fermion, coef[1 * ic + c], coef[2 * ic + c], coef[3 * ic + c], am, ic, c);
   } else {
     for (int c = tid; c < ic; c += nthr) {
       double2 m1 = make_double2(0.0, 0.0), m2 = m1, m3 = m1;
@@ -134,10 +152,7 @@ __global__ void __launch_bounds__(kMatsubaraThreads, 2) nu_to_tau_kernel(NuTauPl
         m2 = mom[1 * Ccols + col0 + c];
         m3 = mom[2 * Ccols + col0 + c];
       }
-      am[0 * ic + c] = from_d2<C>(csub(m1, m3));
-      am[1 * ic + c] = from_d2<C>(cscale(cadd(m2, m3), 0.5));
-      am[2 * ic + c] = from_d2<C>(cscale(csub(m3, m2), 0.5));
-      am[3 * ic + c] = from_d2<C>(m1);
+      tail_amplitudes(p.fermion, m1, m2, m3, am, ic, c);
     }
   }
   __syncthreads();
@@ -150,7 +165,8 @@ __global__ void __launch_bounds__(kMatsubaraThreads, 2) nu_to_tau_kernel(NuTauPl
     C v = cmul(table<C>(p.P, p.Pf, tt), r[tt * ic + c]);
 #pragma unroll
     for (int j = 0; j < 3; ++j) v = cadd(v, cmul(am[j * ic + c], table<C>(p.Q, p.Qf, (long)j * L + tt)));
-    if (t == L) v = csub(czero<C>(), cadd(v, am[3 * ic + c]));  // G[L] = -(G[0] + m1)
+    // G[L] = -(G[0] + m1) for fermions, +(G[0] + m1) for bosons
+    if (t == L) v = p.fermion ? csub(czero<C>(), cadd(v, am[3 * ic + c])) : cadd(v, am[3 * ic + c]);
     gt[(long)t * Ccols + col0 + c] = as_d2(v);
   }
 }
@@ -223,17 +239,19 @@ struct BubbleLoader {  // chi0 columns computed from G(tau, r): col = r * nb^4 +
 
 // tau -> i omega. fit_derivatives moments in FP64 from the end rows; the tail
 // model enters after the FFT: chi(i w_m) = (beta/L) FFT(chi)[k_m] + sum_j a_j K[j][m].
-template <class Loader, class C>
+// FERM: the fermionic transform (input phase, fermion moments); a template
+// parameter so that the bosonic bubble path carries no branch for it.
+template <class Loader, class C, bool FERM>
 __global__ void __launch_bounds__(kMatsubaraThreads, 2) tau_to_w_kernel(TauWPlan p, Loader ld, VinvRows vr, double2 *__restrict__ out,
                                                        long Ccols, int ic, int lg) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C *a = reinterpret_cast<C *>(smem_raw);
-  const int L = p.L, nw = p.nw, nwt = 2 * p.nw - 1;
+  const int L = p.L, nwt = p.n_out;
   const int *rev = p.fft.rev;
   C *b = p.fft.has_generic ? a + (size_t)L * ic : nullptr;
   C *last = a + (size_t)(p.fft.has_generic ? 2 : 1) * L * ic;  // [ic] row L
-  C *am = last + ic;                                            // [3][ic]
-  long *soff = reinterpret_cast<long *>(am + 3 * ic);           // [2][ic] loader offsets
+  C *am = last + ic;                                            // [4][ic] a1, a2, a3, m1
+  long *soff = reinterpret_cast<long *>(am + 4 * ic);           // [2][ic] loader offsets
   double2 *smp = reinterpret_cast<double2 *>(soff + 2 * ic);    // [18][ic] FP64 rows 0..8, L-8..L
   const int tid = threadIdx.x, nthr = blockDim.x;
   const long col0 = blockIdx.x * (long)ic;
@@ -259,7 +277,8 @@ __global__ void __launch_bounds__(kMatsubaraThreads, 2) tau_to_w_kernel(TauWPlan
         const int c = w & (ic - 1), t = w >> lg;
         if (t <= 8) smp[t * ic + c] = v[u];
         if (t >= L - 8) smp[(t - L + 17) * ic + c] = v[u];
-        const C x = from_d2<C>(v[u]);
+        // the fermionic transform takes exp(i pi tau / beta) g(tau) (fourier_matsubara.cpp:164)
+        const C x = from_d2<C>(FERM && t < L ? cmul(v[u], p.ph[t]) : v[u]);
         if (t < L)
           a[rev[t] * ic + c] = x;
         else
@@ -291,20 +310,27 @@ __global__ void __launch_bounds__(kMatsubaraThreads, 2) tau_to_w_kernel(TauWPlan
       gr0 = make_double2(fma(vr.r0[m], dr.x, gr0.x), fma(vr.r0[m], dr.y, gr0.y));
       gr1 = make_double2(fma(vr.r1[m], dr.x, gr1.x), fma(vr.r1[m], dr.y, gr1.y));
     }
-    const double2 m1 = make_double2(-(g0.x - gL.x), -(g0.y - gL.y));
-    const double2 m2 = csub(gl0, gr0);  // sign = +1 (boson)
-    const double2 m3 = cscale(cadd(gl1, gr1), -2.0 / dtau);
-    am[0 * ic + c] = from_d2<C>(cscale(csub(m1, m3), 4.0 / 3.0));
-    am[1 * ic + c] = from_d2<C>(csub(m3, cscale(cadd(m1, m2), 0.5)));
-    am[2 * ic + c] = from_d2<C>(cadd(cadd(cscale(m1, 1.0 / 6.0), cscale(m2, 0.5)), cscale(m3, 1.0 / 3.0)));
+    // m1 = -(g[0] -+ g[L]); m2 = gl0 - s gr0; m3 = -(gl1 + s gr1) 2 / dtau with
+    // s = +1 (boson), -1 (fermion) (fourier_matsubara.cpp:87-90, 153, 166)
+    double2 m1, m2, m3;
+    if (FERM) {
+      m1 = make_double2(-(g0.x + gL.x), -(g0.y + gL.y));
+      m2 = cadd(gl0, gr0);
+      m3 = cscale(csub(gl1, gr1), -2.0 / dtau);
+    } else {
+      m1 = make_double2(-(g0.x - gL.x), -(g0.y - gL.y));
+      m2 = csub(gl0, gr0);
+      m3 = cscale(cadd(gl1, gr1), -2.0 / dtau);
+    }
+    tail_amplitudes(FERM, m1, m2, m3, am, ic, c);
   }
-  // all stages but the last; the last is evaluated only at the 2 nw - 1 kept frequencies
+  // all stages but the last; the last is evaluated only at the kept frequencies
   C *r = fft_smem<false>(a, b, p.fft, ic, p.fft.nst - 1);
   const auto fact = real_of<C>(p.beta / (double)L);
   for (int w = tid; w < nwt * ic; w += nthr) {
     const int c = w & (ic - 1), mi = w >> lg;
     if (c >= ncol) continue;
-    const int m = mi - (nw - 1);
+    const int m = mi + p.out0;
     C v = cscale(last_stage_output<false>(r, p.fft, ic, c, m < 0 ? m + L : m), fact);
 #pragma unroll
     for (int j = 0; j < 3; ++j) v = cadd(v, cmul(am[j * ic + c], table<C>(p.K, p.Kf, (long)j * nwt + mi)));
@@ -366,11 +392,24 @@ template <class Loader, class E>
 int launch_tau_to_w_as(const TauWPlan *p, Loader ld, double2 *out, long C, cudaStream_t stream) {
   int ic, lg;
   size_t smem;
-  int st = pick_ic(p->fft, 4 * sizeof(double2) + 2 * sizeof(long) + 18 * sizeof(double2), &ic, &lg, &smem);
+  int st = pick_ic(p->fft, 5 * sizeof(double2) + 2 * sizeof(long) + 18 * sizeof(double2), &ic, &lg, &smem);
   if (st) return st;
-  TPRF_CUDA(cudaFuncSetAttribute(tau_to_w_kernel<Loader, E>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const long blocks = (C + ic - 1) / ic;
-  tau_to_w_kernel<Loader, E><<<(unsigned)blocks, kMatsubaraThreads, smem, stream>>>(*p, ld, make_vinv_rows(), out, C, ic, lg);
+  if constexpr (std::is_same<Loader, ArrayLoader>::value) {
+    if (p->fermion) {
+      TPRF_CUDA(cudaFuncSetAttribute(tau_to_w_kernel<Loader, E, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem));
+      tau_to_w_kernel<Loader, E, true><<<(unsigned)blocks, kMatsubaraThreads, smem, stream>>>(*p, ld, make_vinv_rows(),
+                                                                                             out, C, ic, lg);
+      TPRF_LAUNCH_CHECK("tau_to_w_kernel");
+      return TPRF_OK;
+    }
+  }
+  if (p->fermion) return set_error(TPRF_ERR_INVALID_ARGUMENT, "tau -> w: fermionic transform of a bubble");
+  TPRF_CUDA(cudaFuncSetAttribute(tau_to_w_kernel<Loader, E, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem));
+  tau_to_w_kernel<Loader, E, false><<<(unsigned)blocks, kMatsubaraThreads, smem, stream>>>(*p, ld, make_vinv_rows(), out,
+                                                                                          C, ic, lg);
   TPRF_LAUNCH_CHECK("tau_to_w_kernel");
   return TPRF_OK;
 }
@@ -570,16 +609,26 @@ __global__ void __launch_bounds__(256) bubble_adjoint_kernel(BubbleLoader ld, co
 
 // ---- internal launchers (no synchronisation) --------------------------------
 
+int launch_nu_to_tau_stat(double beta, int n_iw, int n_tau, bool fermion, long C, const double2 *gw,
+                          const double2 *mom, double2 *gt, cudaStream_t stream);
+
 int launch_nu_to_tau(double beta, int n_iw, int n_tau, long C, const double2 *gw, const double2 *mom, double2 *gt,
                      cudaStream_t stream) {
+  return launch_nu_to_tau_stat(beta, n_iw, n_tau, true, C, gw, mom, gt, stream);
+}
+
+// n: fermionic n_max or bosonic nw; the time mesh must hold L >= 2 n points
+// (fourier_matsubara.cpp:250-254).
+int launch_nu_to_tau_stat(double beta, int n_iw, int n_tau, bool fermion, long C, const double2 *gw,
+                          const double2 *mom, double2 *gt, cudaStream_t stream) {
   if (n_tau < 0) n_tau = default_n_tau(n_iw);
-  if (!(beta > 0.0) || n_iw < 1 || n_tau < 2 || C < 1)
+  if (!(beta > 0.0) || n_iw < 1 || n_tau < 2 || C < 1 || (!fermion && n_iw < 2))
     return set_error(TPRF_ERR_INVALID_ARGUMENT, "fourier_wr_to_tr: bad mesh");
   if (n_tau - 1 < 2 * n_iw)
     return set_error(TPRF_ERR_MESH_TOO_SHORT,
                      "Inverse Fourier: the time mesh must be at least twice as long as the freq mesh");
   const NuTauPlan *p = nullptr;
-  int st = get_nu_tau_plan(beta, n_iw, n_tau, &p);
+  int st = get_nu_tau_plan_stat(beta, n_iw, n_tau, fermion, &p);
   if (st) return st;
   if (!mom && p->n_mom < 4)
     return set_error(TPRF_ERR_TAIL_FIT, "Inverse Fourier requires at least a proper 3rd high-frequency moment");
@@ -608,6 +657,17 @@ int launch_chi_wr_from_chi_tr(double beta, int n_tau, int nw, long C, const doub
   const TauWPlan *p = nullptr;
   if ((st = get_tau_w_plan(beta, n_tau, nw, &p))) return st;
   return launch_tau_to_w_with(p, ArrayLoader{chi_tr, C}, chi_wr, C, stream);
+}
+
+// fermionic tau -> i nu (fourier_matsubara.cpp:123-184, fermion branch): n_iw
+// positive frequencies, outputs n = -n_iw .. n_iw-1
+int launch_fourier_tr_to_wr(double beta, int n_tau, int n_iw, long C, const double2 *g_tr, double2 *g_wr,
+                            cudaStream_t stream) {
+  int st = check_tau_w(beta, n_tau, n_iw);
+  if (st) return st;
+  const TauWPlan *p = nullptr;
+  if ((st = get_tau_w_plan_stat(beta, n_tau, n_iw, true, &p))) return st;
+  return launch_tau_to_w_with(p, ArrayLoader{g_tr, C}, g_wr, C, stream);
 }
 
 int launch_chi0_wr_from_grt(double beta, int n_tau, int nw, const int dims[3], int nb, const double2 *g,
@@ -645,6 +705,30 @@ extern "C" int tprf_fourier_wr_to_tr(double beta, int n_iw, int n_tau, long n_r,
                             reinterpret_cast<const double2 *>(moments), reinterpret_cast<double2 *>(g_tr), s);
   if (st) return st;
   return finish_with_checks(s, "fourier_wr_to_tr");
+}
+
+extern "C" int tprf_fourier_tr_to_wr(double beta, int n_tau, int n_iw, long n_r, long n_target, const double *g_tr,
+                                     double *g_wr, void *stream) {
+  if (!g_tr || !g_wr || n_r < 1 || n_target < 1)
+    return set_error(TPRF_ERR_INVALID_ARGUMENT, "fourier_tr_to_wr: bad shape or null pointer");
+  if (n_iw < 0) n_iw = (n_tau - 1) / 6;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int st = launch_fourier_tr_to_wr(beta, n_tau, n_iw, n_r * n_target, reinterpret_cast<const double2 *>(g_tr),
+                                   reinterpret_cast<double2 *>(g_wr), s);
+  if (st) return st;
+  return finish_with_checks(s, "fourier_tr_to_wr");
+}
+
+extern "C" int tprf_chi_tr_from_chi_wr(double beta, int nw, int n_tau, long n_r, long n_target, const double *chi_wr,
+                                       const double *moments, double *chi_tr, void *stream) {
+  if (!chi_wr || !chi_tr || n_r < 1 || n_target < 1)
+    return set_error(TPRF_ERR_INVALID_ARGUMENT, "chi_tr_from_chi_wr: bad shape or null pointer");
+  if (n_tau < 0) n_tau = 6 * nw + 1;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int st = launch_nu_to_tau_stat(beta, nw, n_tau, false, n_r * n_target, reinterpret_cast<const double2 *>(chi_wr),
+                                 reinterpret_cast<const double2 *>(moments), reinterpret_cast<double2 *>(chi_tr), s);
+  if (st) return st;
+  return finish_with_checks(s, "chi_tr_from_chi_wr");
 }
 
 extern "C" int tprf_chi_wr_from_chi_tr(double beta, int n_tau, int nw, long n_r, long n_target, const double *chi_tr,

@@ -223,17 +223,21 @@ int get_fft(int n, FftDesc *out) {
 }
 
 // ---------------------------------------------------------------------------
-// Tail fit: a linear least-squares fit of g(iv) ~ sum_{p<=P} c_p (iv)^-p on
-// the outer 20% of the fermionic mesh (at most 30 points a side, both signs),
-// frequencies normalised by omega_max; the order P is the largest with
-// omega_max^P <= 1e16, at most 9. This restates the method of TRIQS's
-// fit_tail (called at fourier_matsubara.cpp:226); the TRIQS code itself is not
-// part of the reference tree.
+// Tail fit: a linear least-squares fit of g(iw) ~ sum_{p<=P} c_p (iw)^-p on
+// the outer 20% of the mesh's positive frequency indices (at most 30 points a
+// side, both signs), frequencies normalised by omega_max; the order P is the
+// largest with omega_max^P <= 1e16, at most 9. This restates the method of
+// TRIQS's fit_tail (called at fourier_matsubara.cpp:226); the TRIQS code
+// itself is not part of the reference tree. A fermionic mesh (n = n_freq)
+// holds iv_n for n = -n .. n-1 and fits the indices 0 .. n-1; a bosonic one
+// (n = nw) holds iw_m for m = -(nw-1) .. nw-1 and fits the indices 1 .. nw-1.
 
-static void tail_fit_points(int n_max, std::vector<int> *rows) {
-  int n_pts = std::max(1, std::min((2 * n_max + 5) / 10, 30));
-  int n_hi = n_max - 1;
-  int n_lo = std::min(n_hi, (8 * n_max + 5) / 10);
+static void tail_fit_points(int n, bool fermion, std::vector<int> *rows) {
+  const int i_min = fermion ? 0 : 1, i_max = n - 1;
+  const int count = i_max - i_min + 1;
+  int n_pts = std::max(1, std::min((2 * count + 5) / 10, 30));
+  int n_hi = i_max;
+  int n_lo = std::min(n_hi, i_min + (8 * count + 5) / 10);
   std::vector<int> pos;
   if (n_pts == 1) {
     pos.push_back(n_hi);
@@ -242,12 +246,25 @@ static void tail_fit_points(int n_max, std::vector<int> *rows) {
     for (int j = 0; j < n_pts; ++j) pos.push_back(n_lo + (2 * j * span + (n_pts - 1)) / (2 * (n_pts - 1)));
   }
   rows->clear();
-  for (int i = (int)pos.size() - 1; i >= 0; --i) rows->push_back(-pos[i] - 1 + n_max);
-  for (int p : pos) rows->push_back(p + n_max);
+  if (fermion) {
+    for (int i = (int)pos.size() - 1; i >= 0; --i) rows->push_back(-pos[i] - 1 + n);
+    for (int p : pos) rows->push_back(p + n);
+  } else {
+    for (int i = (int)pos.size() - 1; i >= 0; --i) rows->push_back(-pos[i] + n - 1);
+    for (int p : pos) rows->push_back(p + n - 1);
+  }
 }
 
-static int tail_order(double beta, int n_max, int n_eq) {
-  const double omega_max = (2.0 * n_max - 1.0) * M_PI / beta;
+static double mesh_omega_max(double beta, int n, bool fermion) {
+  return fermion ? (2.0 * n - 1.0) * M_PI / beta : 2.0 * (n - 1) * M_PI / beta;
+}
+
+// the Matsubara frequency of data index i of a mesh
+static cd mesh_freq(double beta, int n, bool fermion, int i) {
+  return fermion ? cd(0.0, (2.0 * (i - n) + 1.0) * M_PI / beta) : cd(0.0, 2.0 * (i - (n - 1)) * M_PI / beta);
+}
+
+static int tail_order(double omega_max, int n_eq) {
   int order = 9;
   if (omega_max > 1.0) order = (int)std::floor(16.0 * std::log(10.0) / std::log(omega_max));
   order = std::min(order, 9);
@@ -310,20 +327,21 @@ static double one_boson(double b, double tau, double beta) {
                  : std::exp(b * (beta - tau)) / (1 - std::exp(b * beta)));
 }
 
-// Host-side definition of the tail fit for a fermionic mesh (beta, n_iw):
-// the data rows of the fit points, F (moments = F g[rows], [n_mom][n_fit])
-// and G (model value at fit point i = sum_p c_p G[i][p], G = (iv_i)^-p).
-int build_tail_fit(double beta, int n_iw, std::vector<int> *rows, std::vector<double2> *F,
+// Host-side definition of the tail fit for a mesh (beta, n, statistic): the
+// data rows of the fit points, F (moments = F g[rows], [n_mom][n_fit]) and G
+// (model value at fit point i = sum_p c_p G[i][p], G = (iw_i)^-p).
+int build_tail_fit(double beta, int n, bool fermion, std::vector<int> *rows, std::vector<double2> *F,
                    std::vector<double2> *G, int *n_mom_out) {
-  tail_fit_points(n_iw, rows);
+  tail_fit_points(n, fermion, rows);
   const int n_fit = (int)rows->size();
-  const int P = tail_order(beta, n_iw, n_fit);
+  const double omega_max = mesh_omega_max(beta, n, fermion);
+  const int P = tail_order(omega_max, n_fit);
   const int n_mom = P + 1;
-  const double omega_max = (2.0 * n_iw - 1.0) * M_PI / beta;
   std::vector<cd> A(n_fit * n_mom);
   G->assign(n_fit * n_mom, make_double2(0, 0));
   for (int i = 0; i < n_fit; ++i) {
-    const cd iw(0.0, (2.0 * ((*rows)[i] - n_iw) + 1.0) * M_PI / beta);
+    const cd iw = mesh_freq(beta, n, fermion, (*rows)[i]);
+    if (std::abs(iw) == 0.0) return set_error(TPRF_ERR_TAIL_FIT, "tail fit: bosonic mesh too short");
     const cd z = omega_max / iw;
     cd zp = 1.0, wp = 1.0;
     for (int q = 0; q < n_mom; ++q) {
@@ -347,13 +365,19 @@ int build_tail_fit(double beta, int n_iw, std::vector<int> *rows, std::vector<do
 }
 
 int get_nu_tau_plan(double beta, int n_iw, int n_tau, const NuTauPlan **out) {
+  return get_nu_tau_plan_stat(beta, n_iw, n_tau, true, out);
+}
+
+// Matsubara -> tau for either statistic (fourier_matsubara.cpp:218-308): n is
+// the fermionic n_max or the bosonic nw.
+int get_nu_tau_plan_stat(double beta, int n, int n_tau, bool fermion, const NuTauPlan **out) {
   int dev = 0;
   int st = current_device(&dev);
   if (st) return st;
-  static std::map<std::tuple<int, uint64_t, int, int>, std::unique_ptr<NuTauPlan>> cache;
+  static std::map<std::tuple<int, uint64_t, int, int, int>, std::unique_ptr<NuTauPlan>> cache;
   uint64_t bbits;
   std::memcpy(&bbits, &beta, 8);
-  auto key = std::make_tuple(dev, bbits, n_iw, n_tau);
+  auto key = std::make_tuple(dev, bbits, n, n_tau, fermion ? 1 : 0);
   {
     std::lock_guard<std::mutex> lock(g_mutex);
     auto it = cache.find(key);
@@ -364,37 +388,38 @@ int get_nu_tau_plan(double beta, int n_iw, int n_tau, const NuTauPlan **out) {
   }
   auto p = std::make_unique<NuTauPlan>();
   p->beta = beta;
-  p->n_iw = n_iw;
+  p->n_iw = n;
   p->n_tau = n_tau;
   p->L = n_tau - 1;
-  const int L = p->L, nnu = 2 * n_iw;
+  p->fermion = fermion ? 1 : 0;
+  p->n_in = fermion ? 2 * n : 2 * n - 1;
+  p->in0 = fermion ? -n : -(n - 1);
+  const int L = p->L, nnu = p->n_in;
   st = get_fft(L, &p->fft);
   if (st) return st;
-  const double bj[3] = {0.0, 1.0, -1.0};
+  const double bf[3] = {0.0, 1.0, -1.0}, bb[3] = {-0.5, -1.0, 1.0};
+  const double *bj = fermion ? bf : bb;
   std::vector<double2> den(3 * nnu);
   for (int j = 0; j < 3; ++j)
-    for (int n = 0; n < nnu; ++n) {
-      const cd iw(0.0, (2.0 * (n - n_iw) + 1.0) * M_PI / beta);
-      den[j * nnu + n] = to_d2(1.0 / (iw - bj[j]));
-    }
+    for (int i = 0; i < nnu; ++i) den[j * nnu + i] = to_d2(1.0 / (mesh_freq(beta, n, fermion, i) - bj[j]));
   std::vector<double2> phase(L);
   std::vector<double> ftail(3 * L);
   const double dtau = beta / (double)(n_tau - 1);
   for (int t = 0; t < L; ++t) {
     const double tau = (double)t * dtau;
-    phase[t] = to_d2(std::exp(cd(0.0, -M_PI * tau / beta)));
-    for (int j = 0; j < 3; ++j) ftail[j * L + t] = one_fermion(bj[j], tau, beta);
+    phase[t] = fermion ? to_d2(std::exp(cd(0.0, -M_PI * tau / beta))) : make_double2(1.0, 0.0);
+    for (int j = 0; j < 3; ++j) ftail[j * L + t] = fermion ? one_fermion(bj[j], tau, beta) : one_boson(bj[j], tau, beta);
   }
   // tail fit
   std::vector<int> rows;
   std::vector<double2> F, G;
   int n_mom = 0;
-  st = build_tail_fit(beta, n_iw, &rows, &F, &G, &n_mom);
+  st = build_tail_fit(beta, n, fermion, &rows, &F, &G, &n_mom);
   if (st) return st;
   const int n_fit = (int)rows.size();
   p->n_fit = n_fit;
   p->n_mom = n_mom;
-  // folded tail tables: FFT_FORWARD of each pole column, placed at rows (n+L)%L
+  // folded tail tables: FFT_FORWARD of each pole column, placed at rows (m+L)%L
   const std::vector<cd> wr = unit_roots(L, -1.0);
   std::vector<double2> P(L), Q(3 * L);
   for (int t = 0; t < L; ++t) {
@@ -402,9 +427,9 @@ int get_nu_tau_plan(double beta, int n_iw, int n_tau, const NuTauPlan **out) {
     P[t] = to_d2(Pt);
     for (int j = 0; j < 3; ++j) {
       cd acc = 0.0;
-      for (int n = 0; n < nnu; ++n) {
-        const long row = ((long)(n - n_iw) + L) % L;
-        acc += cd(den[j * nnu + n].x, den[j * nnu + n].y) * wr[(row * t) % L];
+      for (int i = 0; i < nnu; ++i) {
+        const long row = ((long)(i + p->in0) + L) % L;
+        acc += cd(den[j * nnu + i].x, den[j * nnu + i].y) * wr[(row * t) % L];
       }
       Q[j * L + t] = to_d2(ftail[j * L + t] - Pt * acc);
     }
@@ -422,13 +447,20 @@ int get_nu_tau_plan(double beta, int n_iw, int n_tau, const NuTauPlan **out) {
 }
 
 int get_tau_w_plan(double beta, int n_tau, int nw, const TauWPlan **out) {
+  return get_tau_w_plan_stat(beta, n_tau, nw, false, out);
+}
+
+// tau -> Matsubara for either statistic (fourier_matsubara.cpp:123-184): n is
+// the bosonic nw (outputs m = -(nw-1) .. nw-1) or the fermionic n_max
+// (outputs n = -n_max .. n_max-1).
+int get_tau_w_plan_stat(double beta, int n_tau, int n, bool fermion, const TauWPlan **out) {
   int dev = 0;
   int st = current_device(&dev);
   if (st) return st;
-  static std::map<std::tuple<int, uint64_t, int, int>, std::unique_ptr<TauWPlan>> cache;
+  static std::map<std::tuple<int, uint64_t, int, int, int>, std::unique_ptr<TauWPlan>> cache;
   uint64_t bbits;
   std::memcpy(&bbits, &beta, 8);
-  auto key = std::make_tuple(dev, bbits, n_tau, nw);
+  auto key = std::make_tuple(dev, bbits, n_tau, n, fermion ? 1 : 0);
   {
     std::lock_guard<std::mutex> lock(g_mutex);
     auto it = cache.find(key);
@@ -440,35 +472,46 @@ int get_tau_w_plan(double beta, int n_tau, int nw, const TauWPlan **out) {
   auto p = std::make_unique<TauWPlan>();
   p->beta = beta;
   p->n_tau = n_tau;
-  p->nw = nw;
+  p->nw = n;
   p->L = n_tau - 1;
-  const int L = p->L, nwt = 2 * nw - 1;
+  p->fermion = fermion ? 1 : 0;
+  p->n_out = fermion ? 2 * n : 2 * n - 1;
+  p->out0 = fermion ? -n : -(n - 1);
+  const int L = p->L, nwt = p->n_out;
   st = get_fft(L, &p->fft);
   if (st) return st;
-  const double bj[3] = {-0.5, -1.0, 1.0};
-  std::vector<double> btail(3 * L);
+  const double bf[3] = {0.0, 1.0, -1.0}, bb[3] = {-0.5, -1.0, 1.0};
+  const double *bj = fermion ? bf : bb;
+  // the input phase exp(i pi tau / beta) of the fermionic transform, and the
+  // one-pole tau functions with that phase applied
+  std::vector<double2> ph(L);
+  std::vector<cd> tailt(3 * L);
   const double dtau = beta / (double)(n_tau - 1);
-  for (int t = 0; t < L; ++t)
-    for (int j = 0; j < 3; ++j) btail[j * L + t] = one_boson(bj[j], (double)t * dtau, beta);
+  for (int t = 0; t < L; ++t) {
+    const double tau = (double)t * dtau;
+    const cd e = fermion ? std::exp(cd(0.0, M_PI * tau / beta)) : cd(1.0);
+    ph[t] = to_d2(e);
+    for (int j = 0; j < 3; ++j)
+      tailt[j * L + t] = e * (fermion ? one_fermion(bj[j], tau, beta) : one_boson(bj[j], tau, beta));
+  }
   std::vector<double2> den(3 * nwt);
   for (int j = 0; j < 3; ++j)
-    for (int m = 0; m < nwt; ++m) {
-      const cd iw(0.0, 2.0 * (m - (nw - 1)) * M_PI / beta);
-      den[j * nwt + m] = to_d2(1.0 / (iw - bj[j]));
-    }
+    for (int m = 0; m < nwt; ++m) den[j * nwt + m] = to_d2(1.0 / (mesh_freq(beta, n, fermion, m) - bj[j]));
   // folded tail tables: FFT_BACKWARD of each one-pole tau function, at the output rows
   const std::vector<cd> wb = unit_roots(L, +1.0);
   const double fact = beta / (double)L;
   std::vector<double2> K(3 * nwt);
   for (int j = 0; j < 3; ++j)
     for (int m = 0; m < nwt; ++m) {
-      const long k = ((long)(m - (nw - 1)) + L) % L;
+      const long k = ((long)(m + p->out0) + L) % L;
       cd acc = 0.0;
-      for (int t = 0; t < L; ++t) acc += btail[j * L + t] * wb[(k * t) % L];
+      for (int t = 0; t < L; ++t) acc += tailt[j * L + t] * wb[(k * t) % L];
       K[j * nwt + m] = to_d2(cd(den[j * nwt + m].x, den[j * nwt + m].y) - fact * acc);
     }
+  std::vector<double> btail(3 * L);
+  for (int i = 0; i < 3 * L; ++i) btail[i] = std::real(tailt[i] / cd(ph[i % L].x, ph[i % L].y));
   if ((st = upload(btail, &p->btail)) || (st = upload(den, &p->den)) || (st = upload(K, &p->K)) ||
-      (st = upload(to_df(K), &p->Kf)))
+      (st = upload(to_df(K), &p->Kf)) || (st = upload(ph, &p->ph)))
     return st;
   std::lock_guard<std::mutex> lock(g_mutex);
   auto &slot = cache[key];
@@ -541,12 +584,17 @@ extern "C" int tprf_check_device_status(void *stream) {
 
 extern "C" int tprf_tail_fit_matrix(double beta, int n_iw, int capacity, int *n_fit, int *n_mom, int *rows,
                                     double *F) {
-  if (!(beta > 0.0) || n_iw < 1 || !n_fit || !n_mom)
+  return ::tprf_tail_fit_matrix_stat(beta, n_iw, 1, capacity, n_fit, n_mom, rows, F);
+}
+
+extern "C" int tprf_tail_fit_matrix_stat(double beta, int n, int fermion, int capacity, int *n_fit, int *n_mom,
+                                         int *rows, double *F) {
+  if (!(beta > 0.0) || n < 1 || !n_fit || !n_mom)
     return tprf::set_error(TPRF_ERR_INVALID_ARGUMENT, "tail_fit_matrix: bad mesh or null pointer");
   std::vector<int> r;
   std::vector<double2> f, g;
   int nm = 0;
-  int st = tprf::build_tail_fit(beta, n_iw, &r, &f, &g, &nm);
+  int st = tprf::build_tail_fit(beta, n, fermion != 0, &r, &f, &g, &nm);
   if (st) return st;
   *n_fit = (int)r.size();
   *n_mom = nm;

@@ -20,7 +20,7 @@ __all__ = [
     "lattice_dyson_g0_wk", "lattice_dyson_g_wk", "fourier_wk_to_wr", "fourier_wr_to_wk",
     "fourier_wr_to_tr", "chi0_tr_from_grt_PH", "chi0_wr_from_grt_PH", "chi0_w0r_from_grt_PH",
     "chi_wr_from_chi_tr", "chi_w0r_from_chi_tr", "chi_wk_from_chi_wr", "chi_wr_from_chi_wk",
-    "solve_rpa_PH", "default_n_tau",
+    "solve_rpa_PH", "default_n_tau", "fourier_tr_to_wr", "chi_tr_from_chi_wr",
 ]
 
 
@@ -209,6 +209,43 @@ def chi_wr_from_chi_tr(chi_tr, nw):
     src = chi_tr.data.contiguous()
     check(_native.lib().tprf_chi_wr_from_chi_tr(tmesh.beta, tmesh.n_tau, int(nw), len(rmesh), _ntarget(chi_tr),
                                                 _ptr(src), _ptr(out.data), _stream()), "chi_wr_from_chi_tr")
+    return out
+
+
+def fourier_tr_to_wr(g_tr, nw=-1):
+    """Fermionic G(tau, r) -> G(iv, r) with fit_derivatives tails (lattice_desc.py:325,
+    gf.cpp:257-260). nw < 0: (n_tau - 1) / 6 positive frequencies."""
+    tmesh, rmesh = _components(g_tr, (MeshImTime, MeshCycLat), "fourier_tr_to_wr")
+    if tmesh.statistic != "Fermion":
+        raise TypeError("fourier_tr_to_wr: needs a fermionic time mesh")
+    n_iw = (tmesh.n_tau - 1) // 6 if nw is None or nw < 0 else int(nw)
+    out = Gf(mesh=MeshProduct(MeshImFreq(tmesh.beta, "Fermion", n_iw), rmesh), target_shape=g_tr.target_shape,
+             device=g_tr.data.device)
+    src = g_tr.data.contiguous()
+    check(_native.lib().tprf_fourier_tr_to_wr(tmesh.beta, tmesh.n_tau, n_iw, len(rmesh), _ntarget(g_tr), _ptr(src),
+                                              _ptr(out.data), _stream()), "fourier_tr_to_wr")
+    return out
+
+
+def chi_tr_from_chi_wr(chi_wr, ntau=-1, moments=None):
+    """Bosonic chi(iw, r) -> chi(tau, r) with the tail fit (lattice_desc.py:1426,
+    chi_imtime.cpp:284-287). ntau < 0: 6 nw + 1 points; ``moments`` (an extension)
+    may hold m1..m3 with shape (3, N_r) + target_shape."""
+    wmesh, rmesh = _components(chi_wr, (MeshImFreq, MeshCycLat), "chi_tr_from_chi_wr")
+    if wmesh.statistic != "Boson":
+        raise TypeError("chi_tr_from_chi_wr: needs a bosonic frequency mesh")
+    n_tau = 6 * wmesh.n_max + 1 if ntau is None or ntau < 0 else int(ntau)
+    out = Gf(mesh=MeshProduct(MeshImTime(wmesh.beta, "Boson", n_tau), rmesh), target_shape=chi_wr.target_shape,
+             device=chi_wr.data.device)
+    mom = None
+    if moments is not None:
+        mom = as_device_c128(moments, chi_wr.data.device)
+        if mom.numel() != 3 * len(rmesh) * _ntarget(chi_wr):
+            raise ValueError("chi_tr_from_chi_wr: moments must have shape (3, N_r) + target_shape")
+    src = chi_wr.data.contiguous()
+    check(_native.lib().tprf_chi_tr_from_chi_wr(wmesh.beta, wmesh.n_max, n_tau, len(rmesh), _ntarget(chi_wr),
+                                                _ptr(src), _ptr(mom), _ptr(out.data), _stream()),
+          "chi_tr_from_chi_wr")
     return out
 
 
