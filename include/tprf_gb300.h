@@ -242,6 +242,37 @@ int tprf_imtime_bubble_chi0_wk(double beta, int n_iw, int n_tau, int nw, const i
                                double *chi0_wk, void *workspace, size_t workspace_bytes,
                                void *stream);
 
+/* ---- GW consumers of the chain ----------------------------------------------------
+ * bubble_PI_wk (python/triqs_tprf/gw.py:56-91) is tprf_imtime_bubble_chi0_wk
+ * with nw = n_iw.
+ *
+ * Dynamic GW self energy sigma_ab(tau, r) = - sum_cd W_acdb(tau, r) G_cd(tau, r).
+ * Replaces triqs_tprf::gw_dynamic_sigma(chi_tr_cvt W_tr, g_tr_cvt g_tr)
+ *   (gw.hpp:158, gw.cpp:66-84).
+ * W_tr [n_tau, n_r, nb, nb, nb, nb], g_tr [n_tau, n_r, nb, nb] -> sigma_tr (as g_tr). */
+int tprf_gw_dynamic_sigma(long n_tau, long n_r, int nb, const double *W_tr, const double *g_tr,
+                          double *sigma_tr, void *stream);
+
+/* Screened interaction W(iw, k) from the bubble PI(iw, k).
+ * v_kind 0: static V [n_k, nb^4]; replaces
+ *   triqs_tprf::dynamical_screened_interaction_W(chi_wk_cvt PI_wk, chi_k_cvt V_k)
+ *   (dynamical_screened_interaction.hpp:44, .cpp:85-124):
+ *   W = sum_ef V(a,b,e,f) D^-1(e,f,c,d), D = delta_ad delta_bc - sum_ef PI(a,b,e,f) V(e,f,c,d).
+ * v_kind 1: dynamic V [n_w, n_k, nb^4]; replaces the chi_wk_cvt V_wk overload
+ *   (.cpp:30-80): W = V [I - PI V]^-1 on PH-grouped matrices.
+ * PI_wk, W_wk [n_w, n_k, nb, nb, nb, nb]; nb <= 8; FP64. */
+int tprf_dynamical_screened_interaction_W(long n_w, long n_k, int nb, const double *PI_wk,
+                                          const double *V, int v_kind, double *W_wk, void *stream);
+
+/* chi_const(k) = the constant (0th) moment of the tail fit of chi(iw, k) on the
+ * bosonic mesh (the fit of tprf_tail_fit_matrix_stat), chi_dyn = chi - chi_const.
+ * Replaces triqs_tprf::split_into_dynamic_wk_and_constant_k(chi_wk_cvt)
+ *   (lattice_utility.hpp:47, lattice_utility.cpp:57-85).
+ * chi_wk, chi_dyn_wk [2 nw - 1, n_k, n_target], chi_const_k [n_k, n_target]. */
+int tprf_split_into_dynamic_wk_and_constant_k(double beta, int nw, long n_k, long n_target,
+                                              const double *chi_wk, double *chi_dyn_wk,
+                                              double *chi_const_k, void *stream);
+
 /* ---- adjoints (differentiable path) ---------------------------------------------
  * Gradients for a real loss, in the conjugate-Wirtinger convention (for a
  * linear map y = M x, x_grad = M^H y_grad), used by the torch.autograd

@@ -28,6 +28,8 @@ __all__ = [
     "g0_tail_moments_wr",
     "fourier_wr_to_tr", "fit_derivatives", "vandermonde_inverse",
     "fourier_tr_to_wr", "chi_tr_from_chi_wr", "default_n_iw", "tail_order",
+    "bubble_PI_wk", "dynamical_screened_interaction_W", "dynamical_screened_interaction_W_wk",
+    "gw_dynamic_sigma", "split_into_dynamic_wk_and_constant_k",
     "chi0_tr_from_grt_PH", "chi_wr_from_chi_tr", "chi_wk_from_chi_wr",
     "chi_wr_from_chi_wk", "chi_trapz_tau", "chi_w0r_from_chi_tr",
     "chi0_w0r_from_grt_PH", "chi0_wr_from_grt_PH",
@@ -595,6 +597,55 @@ def imtime_bubble_chi0_wk(g_wk, beta, dims, nw=1, save_memory=False, n_tau=-1, m
     else:
         chi0_wr = chi0_wr_from_grt_PH(g_tr, beta, dims, nw)
     return chi_wk_from_chi_wr(chi0_wr, dims)
+
+
+# ----------------------------------------------------------------------------
+# GW consumers of the chain (python/triqs_tprf/gw.py, lattice/gw.cpp,
+# lattice/dynamical_screened_interaction.cpp, lattice/lattice_utility.cpp)
+# ----------------------------------------------------------------------------
+
+
+def bubble_PI_wk(g_wk, beta, dims):
+    """``gw.py:56-91``: the imaginary-time bubble with nw = n_max bosonic frequencies."""
+    return imtime_bubble_chi0_wk(g_wk, beta, dims, nw=g_wk.shape[0] // 2)
+
+
+def dynamical_screened_interaction_W(PI_wk, V_k):
+    """W(iw, k) for a static V(k): ``dynamical_screened_interaction.cpp:85-124``.
+
+    denom(a,b,c,d) = delta_ad delta_bc - sum_ef PI(a,b,e,f) V(e,f,c,d) (the
+    identity of the PH-grouped view, the natural (e,f) contraction); inverted
+    in the PH grouping; W(a,b,c,d) = sum_ef V(a,b,e,f) inv(e,f,c,d).
+    PI_wk [n_w, N_k, nb, nb, nb, nb], V_k [N_k, nb, nb, nb, nb].
+    """
+    nb = V_k.shape[-1]
+    eye = np.einsum("ad,bc->abcd", np.eye(nb), np.eye(nb))
+    denom = eye[None, None] - np.einsum("wkabef,kefcd->wkabcd", PI_wk, V_k)
+    inv = _ph_ungroup(np.linalg.inv(_ph_group(denom)), nb)
+    return np.einsum("kabef,wkefcd->wkabcd", V_k, inv)
+
+
+def dynamical_screened_interaction_W_wk(PI_wk, V_wk):
+    """W(iw, k) for a dynamic V(iw, k): ``dynamical_screened_interaction.cpp:30-80``
+    (W = V [I - PI V]^-1 on PH-grouped matrices)."""
+    nb = V_wk.shape[-1]
+    P, V = _ph_group(PI_wk), _ph_group(V_wk)
+    return _ph_ungroup(V @ np.linalg.inv(np.eye(nb * nb) - P @ V), nb)
+
+
+def gw_dynamic_sigma(W_tr, g_tr):
+    """``gw.cpp:66-84``: sigma_ab(tau, r) = - sum_cd W_acdb(tau, r) G_cd(tau, r)."""
+    return -np.einsum("tracdb,trcd->trab", W_tr, g_tr)
+
+
+def split_into_dynamic_wk_and_constant_k(chi_wk, beta):
+    """``lattice_utility.cpp:57-85``: chi_const(k) = the constant (0th) moment of the
+    tail fit of chi(iw, k) on the bosonic mesh; chi_dyn = chi - chi_const."""
+    nwt = chi_wk.shape[0]
+    nw = (nwt + 1) // 2
+    c, _ = tail_fit(chi_wk, beta, nw, "Boson")
+    const = c[0]
+    return chi_wk - const[None], const
 
 
 # ----------------------------------------------------------------------------

@@ -170,3 +170,52 @@ def test_inverse_transforms_known_answers():
     assert np.abs(O.chi_wr_from_chi_tr(ct, beta, nw) - chi).max() < 1e-10 * np.abs(chi).max()
     with pytest.raises(RuntimeError):
         O.fourier_tr_to_wr(g_tau, beta, 200)  # time mesh shorter than 2 n_max
+
+
+def _gw_chain_1d(beta=5.0, nk=8, n_max=64):
+    dims = (nk, 1, 1)
+    ek = O.ek_from_hoppings({(1, 0, 0): -np.eye(1), (-1, 0, 0): -np.eye(1)}, dims)
+    return dims, ek, O.lattice_dyson_g0_wk(0.0, ek, beta, n_max)
+
+
+def test_gw_tau_route_equals_matsubara_convolution():
+    """GW self energy of the 1D Hubbard chain (the setting of test/python/gw.py:36-103):
+    Sigma(k, iv) by the imaginary-time route (W(iw) -> W(tau), Sigma = -W G,
+    Sigma(tau) -> Sigma(iv)) against the direct Matsubara convolution
+    -1/(beta N) sum_{q, m} W(q, iw_m) G(k - q, iv - iw_m). The single-band W is
+    V / (1 - PI V)."""
+    beta, nk, n_max, V = 5.0, 8, 64, 1.0
+    dims, ek, g_wk = _gw_chain_1d(beta, nk, n_max)
+    PI = O.bubble_PI_wk(g_wk, beta, dims)
+    assert PI.shape[0] == 2 * n_max - 1
+    V_k = np.full((nk, 1, 1, 1, 1), V, complex)
+    W = O.dynamical_screened_interaction_W(PI, V_k)
+    assert np.abs(W[..., 0, 0, 0, 0] - V / (1 - PI[..., 0, 0, 0, 0] * V)).max() < 1e-14
+    W_dyn, W_const = O.split_into_dynamic_wk_and_constant_k(W, beta)
+    assert np.abs(W_const - V).max() < 1e-4  # W -> V at high frequency
+    g_tr = O.fourier_wr_to_tr(O.fourier_wk_to_wr(g_wk, dims), beta)
+    W_tr = O.chi_tr_from_chi_wr(O.chi_wr_from_chi_wk(W_dyn, dims), beta, g_tr.shape[0])
+    sig = O.fourier_wr_to_wk(O.fourier_tr_to_wr(O.gw_dynamic_sigma(W_tr, g_tr), beta, n_max), dims)
+    nv = np.arange(-n_max, n_max)
+    direct = np.zeros((2 * n_max, nk), complex)
+    for k in range(nk):
+        for q in range(nk):
+            for mi, m in enumerate(range(-(n_max - 1), n_max)):
+                n2 = nv - m
+                ok = (n2 >= -n_max) & (n2 < n_max)
+                direct[ok, k] += W_dyn[mi, q, 0, 0, 0, 0] * g_wk[n2[ok] + n_max, (k - q) % nk, 0, 0]
+    direct *= -1.0 / (beta * nk)
+    low = slice(n_max - 8, n_max + 8)  # the truncated direct sum is exact only away from the mesh edge
+    assert np.abs(sig[low, :, 0, 0] - direct[low]).max() < 1e-4 * np.abs(direct[low]).max()
+
+
+def test_screened_interaction_index_conventions():
+    """dynamical_screened_interaction.cpp:85-124 with PI = 0 gives W(a,b,c,d) = V(a,b,d,c)
+    (the PH-grouped identity is delta_ad delta_bc); the dynamic-V form gives W = V."""
+    rng = np.random.default_rng(5)
+    nb, nk = 2, 3
+    V = rng.standard_normal((nk,) + (nb,) * 4) + 1j * rng.standard_normal((nk,) + (nb,) * 4)
+    W = O.dynamical_screened_interaction_W(np.zeros((2, nk) + (nb,) * 4, complex), V)
+    assert np.allclose(W[0], np.swapaxes(V, -1, -2))
+    Wd = O.dynamical_screened_interaction_W_wk(np.zeros((2, nk) + (nb,) * 4, complex), np.stack([V, V]))
+    assert np.allclose(Wd[1], V)

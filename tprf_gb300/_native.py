@@ -50,6 +50,11 @@ SIGNATURES = {
     "tprf_chi_wr_from_chi_tr": (c_int, [c_double, c_int, c_int, c_long, c_long, c_void_p, c_void_p, c_void_p]),
     "tprf_chi_w0r_from_chi_tr": (c_int, [c_double, c_int, c_long, c_long, c_void_p, c_void_p, c_void_p]),
     "tprf_solve_rpa_PH": (c_int, [c_long, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "tprf_gw_dynamic_sigma": (c_int, [c_long, c_long, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "tprf_dynamical_screened_interaction_W": (c_int, [c_long, c_long, c_int, c_void_p, c_void_p, c_int, c_void_p,
+                                                      c_void_p]),
+    "tprf_split_into_dynamic_wk_and_constant_k": (c_int, [c_double, c_int, c_long, c_long, c_void_p, c_void_p,
+                                                          c_void_p, c_void_p]),
     "tprf_fourier_tr_to_wr": (c_int, [c_double, c_int, c_int, c_long, c_long, c_void_p, c_void_p, c_void_p]),
     "tprf_chi_tr_from_chi_wr": (c_int, [c_double, c_int, c_int, c_long, c_long, c_void_p, c_void_p, c_void_p,
                                         c_void_p]),

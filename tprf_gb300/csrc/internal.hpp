@@ -102,6 +102,14 @@ int arith_mode();
 int get_tau_w_plan(double beta, int n_tau, int nw, const TauWPlan **out);
 int get_tau_w_plan_stat(double beta, int n_tau, int n, bool fermion, const TauWPlan **out);
 
+// The tail-fit definition of one mesh on the device: moments c = F g[rows].
+struct TailFitPlan {
+  int n_fit, n_mom;
+  const int *rows;      // [n_fit]
+  const double2 *F;     // [n_mom][n_fit]
+};
+int get_tail_fit_plan(double beta, int n, bool fermion, const TailFitPlan **out);
+
 // Exact inverse of the 8x8 Vandermonde V[m][j] = m^j (m = 1..8), uploaded to
 // __constant__ memory of the TU that needs it.
 void vandermonde_inverse8(double out[64]);

@@ -520,6 +520,37 @@ int get_tau_w_plan_stat(double beta, int n_tau, int n, bool fermion, const TauWP
   return TPRF_OK;
 }
 
+int get_tail_fit_plan(double beta, int n, bool fermion, const TailFitPlan **out) {
+  int dev = 0;
+  int st = current_device(&dev);
+  if (st) return st;
+  static std::map<std::tuple<int, uint64_t, int, int>, std::unique_ptr<TailFitPlan>> cache;
+  uint64_t bbits;
+  std::memcpy(&bbits, &beta, 8);
+  auto key = std::make_tuple(dev, bbits, n, fermion ? 1 : 0);
+  {
+    std::lock_guard<std::mutex> lock(g_mutex);
+    auto it = cache.find(key);
+    if (it != cache.end()) {
+      *out = it->second.get();
+      return TPRF_OK;
+    }
+  }
+  std::vector<int> rows;
+  std::vector<double2> F, G;
+  int n_mom = 0;
+  if ((st = build_tail_fit(beta, n, fermion, &rows, &F, &G, &n_mom))) return st;
+  auto p = std::make_unique<TailFitPlan>();
+  p->n_fit = (int)rows.size();
+  p->n_mom = n_mom;
+  if ((st = upload(rows, &p->rows)) || (st = upload(F, &p->F))) return st;
+  std::lock_guard<std::mutex> lock(g_mutex);
+  auto &slot = cache[key];
+  if (!slot) slot = std::move(p);
+  *out = slot.get();
+  return TPRF_OK;
+}
+
 void vandermonde_inverse8(double out[64]) {
   // Column m of the inverse holds the coefficients of the Lagrange basis
   // polynomial through nodes 1..8 that is 1 at node m+1: integer polynomial

@@ -44,33 +44,17 @@ template <> struct Mag<cdf> {
 __device__ __forceinline__ double mag2(double2 z) { return cabs2(z); }
 __device__ __forceinline__ float mag2(cdf z) { return __fmaf_rn(z.x.hi, z.x.hi, z.y.hi * z.y.hi); }
 
+// Gaussian elimination with partial pivoting on the group's augmented matrix
+// M = [A | B] (N x 2N, row major, shared memory), then back substitution: on
+// return the right half holds A^-1 B and the left half the LU factors.
+// Lanes own columns; the pivot search is a shuffle argmax inside the group.
+// Returns the smallest squared pivot magnitude; sets `sing` on a zero pivot.
 template <class E, int G>
-__device__ double rpa_point_warp(const double2 *__restrict__ x, double2 *__restrict__ y, E *M, int N, int nb,
-                                 const SparseU &u, int lane, unsigned gmask, bool &singular) {
+__device__ __forceinline__ typename Mag<E>::type solve_augmented(E *M, int N, int lane, unsigned gmask, bool &sing) {
   const int W = 2 * N;
 #define MM(i, c) M[(i) * W + (c)]
-  // B = chi0 in the grouped layout (coalesced global reads)
-  for (int o = lane; o < N * N; o += G) MM(o / N, N + col_of_offset(o % N, nb)) = el_from(x[o], (E *)nullptr);
-  __syncwarp(gmask);
-  // A = I - X U from the non-zeros of U; the size of the terms bounds cancellation
-  float amax = 0.f;
-  for (int e = lane; e < N * N; e += G) {
-    const int r = e / N, c = e % N;
-    E s = (r == c) ? el_one((E *)nullptr) : el_zero((E *)nullptr);
-    float mag = (r == c) ? 1.f : 0.f;
-    for (int t = u.cs[c]; t < u.cs[c + 1]; ++t) {
-      const E xv = MM(r, N + u.row[t]);
-      const E uv = el_from(u.val[t], (E *)nullptr);
-      s = el_fms(xv, uv, s);
-      mag = fmaf(el_absf(xv), el_absf(uv), mag);
-    }
-    amax = fmaxf(amax, mag);
-    MM(r, c) = s;
-  }
-  __syncwarp(gmask);
   using MagT = typename Mag<E>::type;
   MagT pmin = Mag<E>::big;
-  bool sing = false;
   for (int j = 0; j < N; ++j) {
     int p = j;
     MagT best = -1;
@@ -112,8 +96,7 @@ __device__ double rpa_point_warp(const double2 *__restrict__ x, double2 *__restr
     if (lane == 0) MM(j, j) = inv;
     __syncwarp(gmask);
   }
-  singular = sing;
-  // back substitution, one B column per lane, then the grouped -> memory store
+  // back substitution, one B column per lane
   for (int c = N + lane; c < W; c += G) {
     for (int j = N - 1; j >= 0; --j) {
       const E xj = cmul(MM(j, c), MM(j, j));
@@ -123,14 +106,46 @@ __device__ double rpa_point_warp(const double2 *__restrict__ x, double2 *__restr
     }
   }
   __syncwarp(gmask);
-  for (int o = lane; o < N * N; o += G) y[o] = el_to(MM(o / N, N + col_of_offset(o % N, nb)));
+#undef MM
+  return pmin;
+}
+
+template <class E, int G>
+__device__ double rpa_point_warp(const double2 *__restrict__ x, double2 *__restrict__ y, E *M, int N, int nb,
+                                 const SparseU &u, int lane, unsigned gmask, bool &singular) {
+  const int W = 2 * N;
+#define MM(i, c) M[(i) * W + (c)]
+  // B = chi0 in the grouped layout (coalesced global reads)
+  for (int o = lane; o < N * N; o += G) MM(o / N, N + col_of_offset(o % N, nb)) = el_from(x[o], (E *)nullptr);
+  __syncwarp(gmask);
+  // A = I - X U from the non-zeros of U; the size of the terms bounds cancellation
+  float amax = 0.f;
+  for (int e = lane; e < N * N; e += G) {
+    const int r = e / N, c = e % N;
+    E s = (r == c) ? el_one((E *)nullptr) : el_zero((E *)nullptr);
+    float mag = (r == c) ? 1.f : 0.f;
+    for (int t = u.cs[c]; t < u.cs[c + 1]; ++t) {
+      const E xv = MM(r, N + u.row[t]);
+      const E uv = el_from(u.val[t], (E *)nullptr);
+      s = el_fms(xv, uv, s);
+      mag = fmaf(el_absf(xv), el_absf(uv), mag);
+    }
+    amax = fmaxf(amax, mag);
+    MM(r, c) = s;
+  }
+  __syncwarp(gmask);
+#undef MM
+  bool sing = false;
+  const auto pmin = solve_augmented<E, G>(M, N, lane, gmask, sing);
+  singular = sing;
+  for (int o = lane; o < N * N; o += G) y[o] = el_to(M[(o / N) * 2 * N + N + col_of_offset(o % N, nb)]);
 #pragma unroll
   for (int o = G / 2; o > 0; o >>= 1) amax = fmaxf(amax, __shfl_xor_sync(gmask, amax, o));
   __syncwarp(gmask);
-#undef MM
   const double am = (double)amax * (double)amax;
   return pmin > 0 ? am / (double)pmin : 1e300;
 }
+
 
 template <class E, int G>
 __global__ void __launch_bounds__(512) rpa_warp_kernel(long n_points, int nb, const double2 *__restrict__ chi0,
@@ -212,6 +227,54 @@ int launch_g(long n_points, int nb, const double2 *chi0, const double2 *U, doubl
              unsigned *status) {
   if (arith_mode() == kArithFP64) return launch_as<double2, G>(n_points, nb, chi0, U, chi, stream, status);
   return launch_as<cdf, G>(n_points, nb, chi0, U, chi, stream, status);
+}
+
+// ---- screened interaction W ---------------------------------------------------------
+// dynamical_screened_interaction.cpp, per (w, k) point, on PH-grouped matrices
+// (rows (a,b), columns (d,c)) with S the pair swap (e,f) <-> (f,e):
+//   static V(k) (:85-124): D(a,b,c,d) = delta_ad delta_bc - sum_ef PI(a,b,e,f) V(e,f,c,d)
+//     is D = I - PI S V, and W(a,b,c,d) = sum_ef V(a,b,e,f) D^-1(e,f,c,d) is W = V S D^-1;
+//   dynamic V(w, k) (:30-80): W = V (I - PI V)^-1, the same with S = I.
+// W D = V S, so the group solves D^T W^T = S V^T: [D^T | S V^T] in shared memory,
+// FP64, then stores W transposed back. One warp per point.
+__device__ __forceinline__ int pair_swap(int m, int nb) { return (m % nb) * nb + m / nb; }
+
+__global__ void __launch_bounds__(256) screened_w_kernel(long n_points, long nk, int nb, int swap, int v_per_point,
+                                                         const double2 *__restrict__ PI,
+                                                         const double2 *__restrict__ V, double2 *__restrict__ Wout,
+                                                         unsigned *status) {
+  const int N = nb * nb;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, n_warps = blockDim.x >> 5;
+  double2 *M = reinterpret_cast<double2 *>(smem_raw) + (size_t)warp * 4 * N * N;
+  double2 *P = M + 2 * N * N, *Vg = P + N * N;  // PI and V in the grouped layout
+  for (long pt = (long)blockIdx.x * n_warps + warp; pt < n_points; pt += (long)gridDim.x * n_warps) {
+    const double2 *pi = PI + pt * N * N;
+    const double2 *v = V + (v_per_point ? pt : pt % nk) * N * N;
+    for (int o = lane; o < N * N; o += 32) {
+      const int r = o / N, gc = col_of_offset(o % N, nb);
+      P[r * N + gc] = pi[o];
+      Vg[r * N + gc] = v[o];
+    }
+    __syncwarp();
+    for (int e = lane; e < N * N; e += 32) {
+      const int i = e / N, j = e % N;
+      double2 s = make_double2(i == j ? 1.0 : 0.0, 0.0);
+      for (int m = 0; m < N; ++m) s = cfms(P[j * N + (swap ? pair_swap(m, nb) : m)], Vg[m * N + i], s);
+      M[i * 2 * N + j] = s;                                                // D^T[i][j]
+      M[i * 2 * N + N + j] = Vg[j * N + (swap ? pair_swap(i, nb) : i)];  // (S V^T)[i][j]
+    }
+    __syncwarp();
+    bool sing = false;
+    solve_augmented<double2, 32>(M, N, lane, 0xffffffffu, sing);
+    if (sing && lane == 0) atomicOr(status, kDevErrSingular);
+    double2 *w = Wout + pt * N * N;
+    for (int o = lane; o < N * N; o += 32) {
+      const int r = o / N, gc = col_of_offset(o % N, nb);
+      w[o] = M[gc * 2 * N + N + r];  // W[r][gc] = (W^T)[gc][r]
+    }
+    __syncwarp();
+  }
 }
 
 // ---- adjoint -------------------------------------------------------------------
@@ -415,6 +478,23 @@ int launch_rpa_adjoint_warp(long n_points, int nb, const double2 *chi0, const do
   rpa_adjoint_warp_kernel<<<(unsigned)blocks, 32 * best_w, smem, stream>>>(n_points, nb, chi0, U, chi, chig, chi0g,
                                                                           Ug, status);
   TPRF_LAUNCH_CHECK("rpa_adjoint_warp_kernel");
+  return TPRF_OK;
+}
+
+int launch_screened_w(long n_points, long nk, int nb, bool swap, bool v_per_point, const double2 *PI, const double2 *V,
+                      double2 *W, cudaStream_t stream, unsigned *status) {
+  const int N = nb * nb;
+  const size_t per_warp = (size_t)4 * N * N * sizeof(double2);
+  const size_t limit = (size_t)max_smem_optin();
+  if (per_warp > limit) return set_error(TPRF_ERR_INVALID_ARGUMENT, "dynamical_screened_interaction_W: nb too large");
+  const int warps = (int)std::max<size_t>(1, std::min<size_t>(8, limit / per_warp));
+  const size_t smem = (size_t)warps * per_warp;
+  TPRF_CUDA(cudaFuncSetAttribute(screened_w_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  long blocks = (n_points + warps - 1) / warps;
+  blocks = std::max(1L, std::min(blocks, (long)num_sms() * 16));
+  screened_w_kernel<<<(unsigned)blocks, 32 * warps, smem, stream>>>(n_points, nk, nb, swap ? 1 : 0,
+                                                                     v_per_point ? 1 : 0, PI, V, W, status);
+  TPRF_LAUNCH_CHECK("screened_w_kernel");
   return TPRF_OK;
 }
 

@@ -21,6 +21,7 @@ __all__ = [
     "fourier_wr_to_tr", "chi0_tr_from_grt_PH", "chi0_wr_from_grt_PH", "chi0_w0r_from_grt_PH",
     "chi_wr_from_chi_tr", "chi_w0r_from_chi_tr", "chi_wk_from_chi_wr", "chi_wr_from_chi_wk",
     "solve_rpa_PH", "default_n_tau", "fourier_tr_to_wr", "chi_tr_from_chi_wr",
+    "split_into_dynamic_wk_and_constant_k",
 ]
 
 
@@ -247,6 +248,24 @@ def chi_tr_from_chi_wr(chi_wr, ntau=-1, moments=None):
                                                 _ptr(src), _ptr(mom), _ptr(out.data), _stream()),
           "chi_tr_from_chi_wr")
     return out
+
+
+def split_into_dynamic_wk_and_constant_k(chi_wk):
+    """(chi_dyn_wk, chi_const_k): chi_const(k) is the constant tail moment of
+    chi(iw, k) on the bosonic mesh, chi_dyn = chi - chi_const (lattice_desc.py:598,
+    lattice_utility.cpp:57-85)."""
+    wmesh, kmesh = _components(chi_wk, (MeshImFreq, MeshBrZone), "split_into_dynamic_wk_and_constant_k")
+    if wmesh.statistic != "Boson":
+        raise TypeError("split_into_dynamic_wk_and_constant_k: needs a bosonic frequency mesh")
+    dev = chi_wk.data.device
+    dyn = Gf(mesh=chi_wk.mesh, data=torch.empty_like(chi_wk.data))
+    const = Gf(mesh=kmesh, target_shape=chi_wk.target_shape, device=dev)
+    src = chi_wk.data.contiguous()
+    check(_native.lib().tprf_split_into_dynamic_wk_and_constant_k(wmesh.beta, wmesh.n_max, len(kmesh),
+                                                                  _ntarget(chi_wk), _ptr(src), _ptr(dyn.data),
+                                                                  _ptr(const.data), _stream()),
+          "split_into_dynamic_wk_and_constant_k")
+    return dyn, const
 
 
 def chi_w0r_from_chi_tr(chi_tr):
