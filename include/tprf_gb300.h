@@ -273,6 +273,18 @@ int tprf_split_into_dynamic_wk_and_constant_k(double beta, int nw, long n_k, lon
                                               const double *chi_wk, double *chi_dyn_wk,
                                               double *chi_const_k, void *stream);
 
+/* ---- analytic Lindhard bubble (validation) ------------------------------------------
+ * chi00_abcd(iw, q) = 1/N_k sum_k sum_ij U_k(a,i) U_k^*(d,i) U_k+q(c,j) U_k+q^*(b,j)
+ *   (f(e_ki) - f(e_k+q,j)) / (iw + e_k+q,j - e_ki), with the eigen-decomposition of
+ *   e(k) - mu and the w = 0 degenerate limit beta / (4 cosh^2(beta e / 2)).
+ * Replaces triqs_tprf::lindhard_chi00(e_k_cvt, mesh::imfreq, double mu)
+ *   (lindhard_chi00.hpp:97, lindhard_chi00.cpp:34-100). Cost O(N_k^2 nb^6 nw).
+ * e_k [n_k, nb, nb] (dims[0] dims[1] dims[2] = n_k) -> chi_wk [2 nw - 1, n_k, nb^4];
+ * workspace: tprf_lindhard_chi00_workspace_bytes(n_k, nb) bytes of device memory. */
+size_t tprf_lindhard_chi00_workspace_bytes(long n_k, int nb);
+int tprf_lindhard_chi00(long n_k, const int dims[3], int nb, const double *e_k, double beta, double mu,
+                        int nw, double *chi_wk, void *workspace, size_t workspace_bytes, void *stream);
+
 /* ---- adjoints (differentiable path) ---------------------------------------------
  * Gradients for a real loss, in the conjugate-Wirtinger convention (for a
  * linear map y = M x, x_grad = M^H y_grad), used by the torch.autograd

@@ -376,6 +376,40 @@ def test_lindhard_square_lattice_known_answer(cuda_lib):
                                          .data.cpu().numpy()[0], decimal=4)
 
 
+@pytest.mark.parametrize("nb,dims,nw", [(1, (6, 6, 1), 8), (2, (4, 4, 2), 70), (3, (3, 3, 3), 5)])
+def test_lindhard_chi00_on_gpu(cuda_lib, nb, dims, nw):
+    """Analytic Lindhard bubble (lindhard_chi00.cpp:34-94) on the GPU against the
+    oracle; (2, 70) spans several output chunks per q."""
+    T = tp()
+    rng = np.random.default_rng(nb)
+    hop = {}
+    for R in [(1, 0, 0), (0, 1, 0), (0, 0, 1)]:
+        t = -np.eye(nb) + 0.3 * (rng.standard_normal((nb, nb)) + 1j * rng.standard_normal((nb, nb)))
+        hop[R] = t
+        hop[tuple(-x for x in R)] = t.conj().T
+    ek = O.ek_from_hoppings(hop, dims)
+    beta, mu = 4.0, 0.2
+    chi = T.lindhard_chi00(T.Gf(mesh=T.MeshBrZone(dims=dims), data=ek), T.MeshImFreq(beta, "Boson", nw), mu)
+    ref = O.lindhard_chi00(ek, dims, beta, mu, nw)
+    assert tuple(chi.data.shape) == ref.shape
+    assert rel_err(chi.data, ref) < PARITY_RTOL
+
+
+def test_lindhard_gpu_matches_imtime_chain(cuda_lib):
+    """The known answer of test/python/chi00_square_lattice.py:90-180 with both sides on
+    the GPU: the analytic Lindhard bubble against the imaginary-time chain."""
+    import os
+    T = tp()
+    f = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "lindhard_square_2orb.npz")))
+    dims, beta = tuple(int(x) for x in f["dims"]), float(f["beta"])
+    e_k = T.Gf(mesh=T.MeshBrZone(dims=dims), data=f["e_k"])
+    lin = T.lindhard_chi00(e_k, T.MeshImFreq(beta, "Boson", 4), float(f["mu"]))
+    assert rel_err(lin.data, f["chi00_wk_nw4"]) < PARITY_RTOL
+    g0 = T.lattice_dyson_g0_wk(float(f["mu"]), e_k, T.MeshImFreq(beta, "Fermion", 500))
+    chi_wk = T.imtime_bubble_chi0_wk(g0, nw=4, verbose=False)
+    np.testing.assert_array_almost_equal(lin.data.cpu().numpy(), chi_wk.data.cpu().numpy(), decimal=7)
+
+
 def test_kanamori_rpa_closed_form(cuda_lib):
     """test/python/mean_field_kanamori.py:52-162 through the CUDA path."""
     import os

@@ -9,7 +9,7 @@ from .mesh import MeshBrZone, MeshCycLat, MeshImFreq, MeshImTime, MeshProduct
 from .lattice import (chi0_tr_from_grt_PH, chi0_w0r_from_grt_PH, chi0_wr_from_grt_PH, chi_tr_from_chi_wr,
                       chi_w0r_from_chi_tr, chi_wk_from_chi_wr, chi_wr_from_chi_tr, chi_wr_from_chi_wk, fourier_tr_to_wr,
                       fourier_wk_to_wr, fourier_wr_to_tr, fourier_wr_to_wk, lattice_dyson_g0_wk, lattice_dyson_g_wk,
-                      solve_rpa_PH, split_into_dynamic_wk_and_constant_k)
+                      lindhard_chi00, solve_rpa_PH, split_into_dynamic_wk_and_constant_k)
 from .gw import bubble_PI_wk, dynamical_screened_interaction_W, gw_dynamic_sigma
 from .lattice_utils import imtime_bubble_chi0_wk
 from ._native import TprfError

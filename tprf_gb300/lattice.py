@@ -21,7 +21,7 @@ __all__ = [
     "fourier_wr_to_tr", "chi0_tr_from_grt_PH", "chi0_wr_from_grt_PH", "chi0_w0r_from_grt_PH",
     "chi_wr_from_chi_tr", "chi_w0r_from_chi_tr", "chi_wk_from_chi_wr", "chi_wr_from_chi_wk",
     "solve_rpa_PH", "default_n_tau", "fourier_tr_to_wr", "chi_tr_from_chi_wr",
-    "split_into_dynamic_wk_and_constant_k",
+    "split_into_dynamic_wk_and_constant_k", "lindhard_chi00",
 ]
 
 
@@ -247,6 +247,25 @@ def chi_tr_from_chi_wr(chi_wr, ntau=-1, moments=None):
     check(_native.lib().tprf_chi_tr_from_chi_wr(wmesh.beta, wmesh.n_max, n_tau, len(rmesh), _ntarget(chi_wr),
                                                 _ptr(src), _ptr(mom), _ptr(out.data), _stream()),
           "chi_tr_from_chi_wr")
+    return out
+
+
+def lindhard_chi00(e_k, mesh, mu):
+    """Analytic band-basis bubble chi00(iw, q) on a bosonic MeshImFreq (lattice_desc.py:411,
+    lindhard_chi00.cpp:34-100). Cost O(N_k^2): a validation tool for small meshes."""
+    if not isinstance(e_k, Gf) or not isinstance(e_k.mesh, MeshBrZone):
+        raise TypeError("lindhard_chi00: e_k must be a Gf on a MeshBrZone")
+    if not isinstance(mesh, MeshImFreq) or mesh.statistic != "Boson":
+        raise RuntimeError("lindhard_chi00: statistic is incorrect.")
+    nb = e_k.target_shape[0]
+    nk = len(e_k.mesh)
+    dev = e_k.data.device
+    lib = _native.lib()
+    out = Gf(mesh=MeshProduct(mesh, e_k.mesh), target_shape=(nb,) * 4, device=dev)
+    ws = torch.empty(lib.tprf_lindhard_chi00_workspace_bytes(nk, nb), dtype=torch.uint8, device=dev)
+    ek = e_k.data.contiguous()
+    check(lib.tprf_lindhard_chi00(nk, dims3(e_k.mesh.dims), nb, _ptr(ek), mesh.beta, float(mu), mesh.n_max,
+                                  _ptr(out.data), _ptr(ws), ws.numel(), _stream()), "lindhard_chi00")
     return out
 
 
