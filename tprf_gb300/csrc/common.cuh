@@ -12,6 +12,10 @@ namespace tprf {
 
 __device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+// FP64 forms of the double-float butterfly adds (dfloat.cuh): plain adds, no renormalisation
+__device__ __forceinline__ double2 cadd_lz(double2 a, double2 b) { return cadd(a, b); }
+__device__ __forceinline__ double2 csub_lz(double2 a, double2 b) { return csub(a, b); }
+__device__ __forceinline__ double2 cnorm(double2 a) { return a; }
 __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
   return make_double2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
 }
@@ -71,13 +75,19 @@ __device__ __forceinline__ C root(const C *tw, int idx) {
 
 // ---------------------------------------------------------------------------
 // Small DFTs, y_q = sum_r v_r exp(-+ 2 pi i r q / R) (FWD: minus sign).
+template <class C, class K>
+__device__ __forceinline__ C caxpy_lz(K k, C x, C y) {  // y + k x inside a butterfly
+  return cadd_lz(y, cscale(x, k));
+}
+__device__ __forceinline__ double2 caxpy_lz(double k, double2 x, double2 y) { return caxpy(k, x, y); }
+
 template <int R, bool FWD, class C> struct Dft;
 
 template <bool FWD, class C> struct Dft<2, FWD, C> {
   static __device__ __forceinline__ void run(C *v) {
     const C a = v[0], b = v[1];
-    v[0] = cadd(a, b);
-    v[1] = csub(a, b);
+    v[0] = cadd_lz(a, b);
+    v[1] = csub_lz(a, b);
   }
 };
 
@@ -85,23 +95,23 @@ template <bool FWD, class C> struct Dft<3, FWD, C> {
   static __device__ __forceinline__ void run(C *v) {
     constexpr auto s3 = kc<C>(0.86602540378443864676);  // sin(2 pi / 3)
     constexpr auto mh = kc<C>(-0.5);
-    const C t1 = cadd(v[1], v[2]);
-    const C t2 = caxpy(mh, t1, v[0]);
-    const C t4 = mul_mi<FWD>(cscale(csub(v[1], v[2]), s3));
-    v[0] = cadd(v[0], t1);
-    v[1] = cadd(t2, t4);
-    v[2] = csub(t2, t4);
+    const C t1 = cadd_lz(v[1], v[2]);
+    const C t2 = caxpy_lz(mh, t1, v[0]);
+    const C t4 = mul_mi<FWD>(cscale(csub_lz(v[1], v[2]), s3));
+    v[0] = cadd_lz(v[0], t1);
+    v[1] = cadd_lz(t2, t4);
+    v[2] = csub_lz(t2, t4);
   }
 };
 
 template <bool FWD, class C> struct Dft<4, FWD, C> {
   static __device__ __forceinline__ void run(C *v) {
-    const C a = cadd(v[0], v[2]), b = csub(v[0], v[2]);
-    const C c = cadd(v[1], v[3]), d = mul_mi<FWD>(csub(v[1], v[3]));
-    v[0] = cadd(a, c);
-    v[2] = csub(a, c);
-    v[1] = cadd(b, d);
-    v[3] = csub(b, d);
+    const C a = cadd_lz(v[0], v[2]), b = csub_lz(v[0], v[2]);
+    const C c = cadd_lz(v[1], v[3]), d = mul_mi<FWD>(csub_lz(v[1], v[3]));
+    v[0] = cadd_lz(a, c);
+    v[2] = csub_lz(a, c);
+    v[1] = cadd_lz(b, d);
+    v[3] = csub_lz(b, d);
   }
 };
 
@@ -112,19 +122,19 @@ template <bool FWD, class C> struct Dft<5, FWD, C> {
     constexpr auto s1 = kc<C>(0.95105651629515357212);   // sin(2 pi / 5)
     constexpr auto s2 = kc<C>(0.58778525229247312917);   // sin(4 pi / 5)
     constexpr auto ms1 = kc<C>(-0.95105651629515357212);
-    const C a1 = cadd(v[1], v[4]), b1 = csub(v[1], v[4]);
-    const C a2 = cadd(v[2], v[3]), b2 = csub(v[2], v[3]);
+    const C a1 = cadd_lz(v[1], v[4]), b1 = csub_lz(v[1], v[4]);
+    const C a2 = cadd_lz(v[2], v[3]), b2 = csub_lz(v[2], v[3]);
     const C x0 = v[0];
-    const C r1 = caxpy(c2, a2, caxpy(c1, a1, x0));
-    const C r2 = caxpy(c1, a2, caxpy(c2, a1, x0));
+    const C r1 = caxpy_lz(c2, a2, caxpy_lz(c1, a1, x0));
+    const C r2 = caxpy_lz(c1, a2, caxpy_lz(c2, a1, x0));
     // q = 1: -i (s1 b1 + s2 b2), q = 2: -i (s2 b1 - s1 b2)  (FWD)
-    const C i1 = mul_mi<FWD>(caxpy(s2, b2, cscale(b1, s1)));
-    const C i2 = mul_mi<FWD>(caxpy(ms1, b2, cscale(b1, s2)));
-    v[0] = cadd(x0, cadd(a1, a2));
-    v[1] = cadd(r1, i1);
-    v[4] = csub(r1, i1);
-    v[2] = cadd(r2, i2);
-    v[3] = csub(r2, i2);
+    const C i1 = mul_mi<FWD>(caxpy_lz(s2, b2, cscale(b1, s1)));
+    const C i2 = mul_mi<FWD>(caxpy_lz(ms1, b2, cscale(b1, s2)));
+    v[0] = cadd_lz(x0, cadd_lz(a1, a2));
+    v[1] = cadd_lz(r1, i1);
+    v[4] = csub_lz(r1, i1);
+    v[2] = cadd_lz(r2, i2);
+    v[3] = csub_lz(r2, i2);
   }
 };
 
@@ -138,23 +148,23 @@ template <bool FWD, class C> struct Dft<7, FWD, C> {
     C a[3], b[3];
 #pragma unroll
     for (int q = 0; q < 3; ++q) {
-      a[q] = cadd(v[q + 1], v[6 - q]);
-      b[q] = csub(v[q + 1], v[6 - q]);
+      a[q] = cadd_lz(v[q + 1], v[6 - q]);
+      b[q] = csub_lz(v[q + 1], v[6 - q]);
     }
     const C x0 = v[0];
-    v[0] = cadd(x0, cadd(a[0], cadd(a[1], a[2])));
+    v[0] = cadd_lz(x0, cadd_lz(a[0], cadd_lz(a[1], a[2])));
 #pragma unroll
     for (int q = 1; q <= 3; ++q) {
       C re = x0, im = czero<C>();
 #pragma unroll
       for (int r = 1; r <= 3; ++r) {
         const int m = (q * r) % 7;
-        re = caxpy(kc<C>(cs[m - 1]), a[r - 1], re);
-        im = caxpy(kc<C>(sn[m - 1]), b[r - 1], im);
+        re = caxpy_lz(kc<C>(cs[m - 1]), a[r - 1], re);
+        im = caxpy_lz(kc<C>(sn[m - 1]), b[r - 1], im);
       }
       im = mul_mi<FWD>(im);
-      v[q] = cadd(re, im);
-      v[7 - q] = csub(re, im);
+      v[q] = cadd_lz(re, im);
+      v[7 - q] = csub_lz(re, im);
     }
   }
 };
@@ -167,17 +177,17 @@ template <bool FWD, class C> struct Dft<8, FWD, C> {
     Dft<4, FWD, C>::run(e);
     Dft<4, FWD, C>::run(o);
     // W8^1 o1 = h (o1 + mul_mi(o1)),  W8^2 o2 = mul_mi(o2),  W8^3 o3 = h (mul_mi(o3) - o3)
-    const C t1 = cscale(cadd(o[1], mul_mi<FWD>(o[1])), h);
+    const C t1 = cscale(cadd_lz(o[1], mul_mi<FWD>(o[1])), h);
     const C t2 = mul_mi<FWD>(o[2]);
-    const C t3 = cscale(csub(mul_mi<FWD>(o[3]), o[3]), h);
-    v[0] = cadd(e[0], o[0]);
-    v[4] = csub(e[0], o[0]);
-    v[1] = cadd(e[1], t1);
-    v[5] = csub(e[1], t1);
-    v[2] = cadd(e[2], t2);
-    v[6] = csub(e[2], t2);
-    v[3] = cadd(e[3], t3);
-    v[7] = csub(e[3], t3);
+    const C t3 = cscale(csub_lz(mul_mi<FWD>(o[3]), o[3]), h);
+    v[0] = cadd_lz(e[0], o[0]);
+    v[4] = csub_lz(e[0], o[0]);
+    v[1] = cadd_lz(e[1], t1);
+    v[5] = csub_lz(e[1], t1);
+    v[2] = cadd_lz(e[2], t2);
+    v[6] = csub_lz(e[2], t2);
+    v[3] = cadd_lz(e[3], t3);
+    v[7] = csub_lz(e[3], t3);
   }
 };
 
@@ -224,7 +234,7 @@ __device__ __forceinline__ void fft_stage(C *__restrict__ a, int n, int Ns, int 
     }
     Dft<R, FWD, C>::run(v);
 #pragma unroll
-    for (int r = 0; r < R; ++r) a[(base + r * Ns) * lay.stride + cb] = v[r];
+    for (int r = 0; r < R; ++r) a[(base + r * Ns) * lay.stride + cb] = cnorm(v[r]);
     k += kstep;
     if (k >= Ns) k -= Ns;
   }

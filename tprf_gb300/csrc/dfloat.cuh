@@ -51,6 +51,18 @@ __device__ __forceinline__ dfl dadd(dfl a, dfl b) {
 
 __device__ __forceinline__ dfl dsub(dfl a, dfl b) { return dadd(a, dneg(b)); }
 
+// a + b without the closing Fast2Sum: hi + lo carries the sum to the same
+// accuracy as dadd, but |lo| may exceed half an ulp of hi. TwoSum is exact for
+// any inputs and dmul keeps a.lo in full, so a short chain of these adds (the
+// levels of one butterfly) followed by one renorm() keeps the error bounded
+// relative to the magnitudes of the inputs, as the sloppy dadd does.
+__device__ __forceinline__ dfl dadd_lazy(dfl a, dfl b) {
+  float s, e;
+  two_sum(a.hi, b.hi, s, e);
+  return dfl{s, __fadd_rn(e, __fadd_rn(a.lo, b.lo))};
+}
+__device__ __forceinline__ dfl renorm(dfl a) { return fast_two_sum(a.hi, a.lo); }
+
 __device__ __forceinline__ dfl dmul(dfl a, dfl b) {
   const float p = __fmul_rn(a.hi, b.hi);
   float e = __fmaf_rn(a.hi, b.hi, -p);
@@ -81,6 +93,10 @@ __device__ __forceinline__ dfl ddot_add(dfl a1, dfl b1, dfl a2, dfl b2) { return
 // ---- complex ----------------------------------------------------------------
 __device__ __forceinline__ cdf cadd(cdf a, cdf b) { return cdf{dadd(a.x, b.x), dadd(a.y, b.y)}; }
 __device__ __forceinline__ cdf csub(cdf a, cdf b) { return cdf{dsub(a.x, b.x), dsub(a.y, b.y)}; }
+// butterfly-internal adds (see dadd_lazy) and the renormalisation before a store
+__device__ __forceinline__ cdf cadd_lz(cdf a, cdf b) { return cdf{dadd_lazy(a.x, b.x), dadd_lazy(a.y, b.y)}; }
+__device__ __forceinline__ cdf csub_lz(cdf a, cdf b) { return cdf{dadd_lazy(a.x, dneg(b.x)), dadd_lazy(a.y, dneg(b.y))}; }
+__device__ __forceinline__ cdf cnorm(cdf a) { return cdf{renorm(a.x), renorm(a.y)}; }
 __device__ __forceinline__ cdf cmul(cdf a, cdf b) { return cdf{ddot_sub(a.x, b.x, a.y, b.y), ddot_add(a.x, b.y, a.y, b.x)}; }
 __device__ __forceinline__ cdf cscale(cdf a, dfl s) { return cdf{dmul(a.x, s), dmul(a.y, s)}; }
 __device__ __forceinline__ cdf cconj(cdf a) { return cdf{a.x, dneg(a.y)}; }
