@@ -52,6 +52,28 @@ VinvRows make_vinv_rows() {
   return r;
 }
 
+// fit_derivatives with the divisions folded into constants: the moments need
+// sum_m r[m] (g[m] - g[0]) / tau_m, computed as sum_m (r[m] / tau_m) (g[m] - g[0])
+// (the same algebra; FP64 divisions are slow on this GPU), and m3 carries -2 / dtau.
+struct FitRows {
+  double c0[8], c1[8];
+  double k3;
+};
+
+FitRows make_fit_rows(double beta, int n_tau) {
+  double v[64];
+  vandermonde_inverse8(v);
+  const double dtau = beta / (double)(n_tau - 1);
+  FitRows f;
+  for (int m = 0; m < 8; ++m) {
+    const double tau = (double)(m + 1) * dtau;
+    f.c0[m] = v[0 * 8 + m] / tau;
+    f.c1[m] = v[1 * 8 + m] / tau;
+  }
+  f.k3 = -2.0 / dtau;
+  return f;
+}
+
 // element-type plumbing: double2 (FP64) or cdf (double-float)
 template <class C> __device__ __forceinline__ C from_d2(double2 z);
 template <> __device__ __forceinline__ double2 from_d2<double2>(double2 z) { return z; }
@@ -140,7 +162,7 @@ __global__ void __launch_bounds__(kMatsubaraThreads, 2) nu_to_tau_kernel(NuTauPl
       double2 model = make_double2(0.0, 0.0);
       for (int q = 0; q < nm; ++q) model = cfma(p.fitG[i * nm + q], coef[q * ic + c], model);
       const double2 d = csub(model, gw[(long)p.fit_row[i] * Ccols + col0 + c]);
-      atomicMax(&s_res, __float_as_uint((float)sqrt(cabs2(d))));
+      atomicMax(&s_res, __float_as_uint(sqrtf((float)cabs2(d))));  // compared with 1e-3
     }
     for (int c = tid; c < ic; c += nthr)
       tail_amplitudes(p.fermion, coef[1 * ic + c], coef[2 * ic + c], coef[3 * ic + c], am, ic, c);
@@ -194,21 +216,23 @@ struct BubbleLoader {  // chi0 columns computed from G(tau, r): col = r * nb^4 +
   int nb, n_tau;
   int d0, d1, d2;
   // offsets of G_da(., r) and G_bc(., -r) within one tau slice of G
+  // 32-bit index arithmetic: N_r nb^4 < 2^31 is checked at launch (bubble_columns)
   __device__ __forceinline__ void offsets(long col, long &ox, long &oy) const {
     const int nb2 = nb * nb, nb4 = nb2 * nb2;
-    const long r = col / nb4;
-    int e = (int)(col - r * nb4);
+    const int ci = (int)col;
+    const int r = ci / nb4;
+    int e = ci - r * nb4;
     const int d = e % nb;
     e /= nb;
     const int c = e % nb;
     e /= nb;
     const int b = e % nb;
     const int a = e / nb;
-    const int i2 = (int)(r % d2);
-    const int i1 = (int)((r / d2) % d1);
-    const int i0 = (int)(r / ((long)d2 * d1));
+    const int i2 = r % d2;
+    const int i1 = (r / d2) % d1;
+    const int i0 = r / (d2 * d1);
     const long mr = ((long)((d0 - i0) % d0) * d1 + (d1 - i1) % d1) * d2 + (d2 - i2) % d2;
-    ox = r * nb2 + d * nb + a;
+    ox = (long)r * nb2 + d * nb + a;
     oy = mr * nb2 + b * nb + c;
   }
   __device__ __forceinline__ double2 operator()(int t, long col) const {
@@ -242,7 +266,7 @@ struct BubbleLoader {  // chi0 columns computed from G(tau, r): col = r * nb^4 +
 // FERM: the fermionic transform (input phase, fermion moments); a template
 // parameter so that the bosonic bubble path carries no branch for it.
 template <class Loader, class C, bool FERM>
-__global__ void __launch_bounds__(kMatsubaraThreads, 2) tau_to_w_kernel(TauWPlan p, Loader ld, VinvRows vr, double2 *__restrict__ out,
+__global__ void __launch_bounds__(kMatsubaraThreads, 2) tau_to_w_kernel(TauWPlan p, Loader ld, FitRows fr, double2 *__restrict__ out,
                                                        long Ccols, int ic, int lg) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C *a = reinterpret_cast<C *>(smem_raw);
@@ -287,7 +311,6 @@ __global__ void __launch_bounds__(kMatsubaraThreads, 2) tau_to_w_kernel(TauWPlan
     }
   }
   __syncthreads();
-  const double dtau = p.beta / (double)(p.n_tau - 1);
   // fit_derivatives differentiates and then applies the inverse Vandermonde
   // matrix, which amplifies rounding: its 18 samples are the FP64 values, not
   // the double-float copy in the FFT buffer.
@@ -300,15 +323,14 @@ __global__ void __launch_bounds__(kMatsubaraThreads, 2) tau_to_w_kernel(TauWPlan
     double2 gl0 = make_double2(0.0, 0.0), gl1 = gl0, gr0 = gl0, gr1 = gl0;
 #pragma unroll
     for (int m = 0; m < 8; ++m) {
-      const double tau_m = (double)(m + 1) * dtau;
       const double2 xl = smp[(m + 1) * ic + c];
-      const double2 dl = make_double2((xl.x - g0.x) / tau_m, (xl.y - g0.y) / tau_m);
+      const double2 dl = make_double2(xl.x - g0.x, xl.y - g0.y);
       const double2 xr = smp[(16 - m) * ic + c];
-      const double2 dr = make_double2((gL.x - xr.x) / tau_m, (gL.y - xr.y) / tau_m);
-      gl0 = make_double2(fma(vr.r0[m], dl.x, gl0.x), fma(vr.r0[m], dl.y, gl0.y));
-      gl1 = make_double2(fma(vr.r1[m], dl.x, gl1.x), fma(vr.r1[m], dl.y, gl1.y));
-      gr0 = make_double2(fma(vr.r0[m], dr.x, gr0.x), fma(vr.r0[m], dr.y, gr0.y));
-      gr1 = make_double2(fma(vr.r1[m], dr.x, gr1.x), fma(vr.r1[m], dr.y, gr1.y));
+      const double2 dr = make_double2(gL.x - xr.x, gL.y - xr.y);
+      gl0 = make_double2(fma(fr.c0[m], dl.x, gl0.x), fma(fr.c0[m], dl.y, gl0.y));
+      gl1 = make_double2(fma(fr.c1[m], dl.x, gl1.x), fma(fr.c1[m], dl.y, gl1.y));
+      gr0 = make_double2(fma(fr.c0[m], dr.x, gr0.x), fma(fr.c0[m], dr.y, gr0.y));
+      gr1 = make_double2(fma(fr.c1[m], dr.x, gr1.x), fma(fr.c1[m], dr.y, gr1.y));
     }
     // m1 = -(g[0] -+ g[L]); m2 = gl0 - s gr0; m3 = -(gl1 + s gr1) 2 / dtau with
     // s = +1 (boson), -1 (fermion) (fourier_matsubara.cpp:87-90, 153, 166)
@@ -316,11 +338,11 @@ __global__ void __launch_bounds__(kMatsubaraThreads, 2) tau_to_w_kernel(TauWPlan
     if (FERM) {
       m1 = make_double2(-(g0.x + gL.x), -(g0.y + gL.y));
       m2 = cadd(gl0, gr0);
-      m3 = cscale(csub(gl1, gr1), -2.0 / dtau);
+      m3 = cscale(csub(gl1, gr1), fr.k3);
     } else {
       m1 = make_double2(-(g0.x - gL.x), -(g0.y - gL.y));
       m2 = csub(gl0, gr0);
-      m3 = cscale(cadd(gl1, gr1), -2.0 / dtau);
+      m3 = cscale(cadd(gl1, gr1), fr.k3);
     }
     tail_amplitudes(FERM, m1, m2, m3, am, ic, c);
   }
@@ -399,7 +421,8 @@ int launch_tau_to_w_as(const TauWPlan *p, Loader ld, double2 *out, long C, cudaS
     if (p->fermion) {
       TPRF_CUDA(cudaFuncSetAttribute(tau_to_w_kernel<Loader, E, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)smem));
-      tau_to_w_kernel<Loader, E, true><<<(unsigned)blocks, kMatsubaraThreads, smem, stream>>>(*p, ld, make_vinv_rows(),
+      tau_to_w_kernel<Loader, E, true><<<(unsigned)blocks, kMatsubaraThreads, smem, stream>>>(*p, ld,
+                                                                                             make_fit_rows(p->beta, p->n_tau),
                                                                                              out, C, ic, lg);
       TPRF_LAUNCH_CHECK("tau_to_w_kernel");
       return TPRF_OK;
@@ -408,7 +431,8 @@ int launch_tau_to_w_as(const TauWPlan *p, Loader ld, double2 *out, long C, cudaS
   if (p->fermion) return set_error(TPRF_ERR_INVALID_ARGUMENT, "tau -> w: fermionic transform of a bubble");
   TPRF_CUDA(cudaFuncSetAttribute(tau_to_w_kernel<Loader, E, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)smem));
-  tau_to_w_kernel<Loader, E, false><<<(unsigned)blocks, kMatsubaraThreads, smem, stream>>>(*p, ld, make_vinv_rows(), out,
+  tau_to_w_kernel<Loader, E, false><<<(unsigned)blocks, kMatsubaraThreads, smem, stream>>>(*p, ld,
+                                                                                          make_fit_rows(p->beta, p->n_tau), out,
                                                                                           C, ic, lg);
   TPRF_LAUNCH_CHECK("tau_to_w_kernel");
   return TPRF_OK;
@@ -441,12 +465,19 @@ BubbleLoader make_bubble(const double2 *g, int n_tau, const int dims[3], int nb)
   return ld;
 }
 
+// the bubble's column index (r, abcd) must fit the loaders' 32-bit arithmetic
+int bubble_columns(const int dims[3], int nb) {
+  const long long cols = (long long)dims[0] * dims[1] * dims[2] * nb * nb * nb * nb;
+  if (cols >= (1LL << 31)) return set_error(TPRF_ERR_UNSUPPORTED_SIZE, "bubble: N_r nb^4 must be below 2^31");
+  return TPRF_OK;
+}
+
 int check_bubble(int n_tau, const int dims[3], int nb, const void *g, const void *out) {
   if (!dims || !g || !out || n_tau < 2 || nb < 1 || nb > 8)
     return set_error(TPRF_ERR_INVALID_ARGUMENT, "bubble: bad shape (nb 1..8, n_tau >= 2) or null pointer");
   for (int a = 0; a < 3; ++a)
     if (dims[a] < 1) return set_error(TPRF_ERR_INVALID_ARGUMENT, "bubble: mesh dims must be >= 1");
-  return TPRF_OK;
+  return bubble_columns(dims, nb);
 }
 
 // ---------------------------------------------------------------------------
@@ -674,6 +705,7 @@ int launch_chi0_wr_from_grt(double beta, int n_tau, int nw, const int dims[3], i
                             double2 *chi0_wr, cudaStream_t stream) {
   int st = check_tau_w(beta, n_tau, nw);
   if (st) return st;
+  if ((st = bubble_columns(dims, nb))) return st;
   const TauWPlan *p = nullptr;
   if ((st = get_tau_w_plan(beta, n_tau, nw, &p))) return st;
   const BubbleLoader ld = make_bubble(g, n_tau, dims, nb);
@@ -683,6 +715,7 @@ int launch_chi0_wr_from_grt(double beta, int n_tau, int nw, const int dims[3], i
 
 int launch_chi0_w0r_from_grt(double beta, int n_tau, const int dims[3], int nb, const double2 *g, double2 *chi0_wr,
                              cudaStream_t stream) {
+  if (int st = bubble_columns(dims, nb)) return st;
   const BubbleLoader ld = make_bubble(g, n_tau, dims, nb);
   const long C = ld.Nr * nb * nb * nb * nb;
   trapz_kernel<BubbleLoader><<<(unsigned)grid_for(C, 256), 256, 0, stream>>>(ld, chi0_wr, C, n_tau, beta);
