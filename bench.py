@@ -18,6 +18,7 @@ replica (the path has no cross-instance exchange): weak scaling.
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import math
 import os
@@ -266,8 +267,6 @@ def run_gpu(args):
     points = nwt * nk
     U = torch.as_tensor(cfg["U"], dtype=torch.complex128, device=dev).contiguous()
     g_wk = torch.empty(n_nu, nk, nb, nb, dtype=torch.complex128, device=dev)
-    g_wr = torch.empty_like(g_wk)
-    g_tr = torch.empty(n_tau, nk, nb, nb, dtype=torch.complex128, device=dev)
     chi0 = torch.empty(nwt, nk, nb4, dtype=torch.complex128, device=dev)
     chi = torch.empty_like(chi0)
     d3 = dims3(dims)
@@ -276,31 +275,35 @@ def run_gpu(args):
     lib.tprf_set_sync_checks(0)
     launches_per_step = 1 + lattice_passes(dims) + 1 + 1 + lattice_passes(dims) + 1
 
+    ws_bytes = lib.tprf_imtime_bubble_workspace_bytes(n_max, n_tau, d3, nb)
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
     stages = ["dyson", "fft_k_to_r", "nu_to_tau", "bubble_tau_to_w", "fft_r_to_q", "rpa"]
+    no_events = (ctypes.c_void_p * 5)()
 
     def step(ev=None):
-        def mark(i):
-            if ev is not None:
-                ev[i].record(stream)
-        mark(0)
+        # Dyson, then the bubble chain through its own entry point (k->r, iv->tau,
+        # bubble + tau->iw, r->q; stage events recorded by the library), then the RPA
+        if ev is not None:
+            ev[0][0].record(stream)
         check(lib.tprf_lattice_dyson_g_wk(beta, n_max, nk, nb, mu, e_k.data_ptr(), None, 0, g_wk.data_ptr(), sh))
-        mark(1)
-        check(lib.tprf_fourier_wk_to_wr(n_nu, d3, nb2, g_wk.data_ptr(), g_wr.data_ptr(), sh))
-        mark(2)
-        check(lib.tprf_fourier_wr_to_tr(beta, n_max, n_tau, nk, nb2, g_wr.data_ptr(), None, g_tr.data_ptr(), sh))
-        mark(3)
-        check(lib.tprf_chi0_wr_from_grt_PH(beta, n_tau, nw, d3, nb, g_tr.data_ptr(), chi0.data_ptr(), sh))
-        mark(4)
-        check(lib.tprf_fourier_wr_to_wk(nwt, d3, nb4, chi0.data_ptr(), chi0.data_ptr(), sh))
-        mark(5)
+        check(lib.tprf_imtime_bubble_chi0_wk_timed(beta, n_max, n_tau, nw, d3, nb, g_wk.data_ptr(), None,
+                                                   chi0.data_ptr(), ws.data_ptr(), ws_bytes,
+                                                   ev[1] if ev is not None else no_events, sh))
         check(lib.tprf_solve_rpa_PH(points, nb, chi0.data_ptr(), U.data_ptr(), chi.data_ptr(), sh))
-        mark(6)
+        if ev is not None:
+            ev[0][6].record(stream)
 
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
     check(lib.tprf_check_device_status(sh), "warm-up")
     evs = [[torch.cuda.Event(enable_timing=True) for _ in range(7)] for _ in range(args.steps)]
+    for row in evs:  # torch creates an event's handle at its first record
+        for e in row:
+            e.record(stream)
+    torch.cuda.synchronize()
+    handles = [(ctypes.c_void_p * 5)(*[row[i].cuda_event for i in range(1, 6)]) for row in evs]
+    assert all(h for row in handles for h in row)
     clocks = ClockSampler(local)
     barrier(world, dev)
     torch.cuda.synchronize()
@@ -309,7 +312,7 @@ def run_gpu(args):
         t_end = torch.cuda.Event(enable_timing=True)
         t_start.record(stream)
         for k in range(args.steps):
-            step(evs[k])
+            step((evs[k], handles[k]))
         t_end.record(stream)
         torch.cuda.synchronize()
     barrier(world, dev)
@@ -330,7 +333,7 @@ def run_gpu(args):
         kmesh = T.MeshBrZone(dims=dims)
         ws = torch.empty(T.lattice_utils.bubble_workspace_bytes(n_max, n_tau, dims, nb), dtype=torch.uint8,
                          device=dev)
-        del g_wk, g_wr, g_tr, chi0, chi
+        del g_wk, ws, chi0, chi
         torch.cuda.empty_cache()
         lib.tprf_set_sync_checks(1)
 

@@ -234,13 +234,22 @@ int tprf_solve_rpa_PH_to_host(long n_points, int nb, const double *chi0, const d
  * g_wk -> chi0_wk as triqs_tprf.lattice_utils.imtime_bubble_chi0_wk
  * (python/triqs_tprf/lattice_utils.py:191-269): k->r, iv->tau, bubble, tau->iw
  * (nw > 1) or trapezoid (nw == 1), r->q. chi0(tau, r) is never stored.
- * Intermediate G(iv, r) and G(tau, r) live in the caller's workspace, whose
- * size tprf_imtime_bubble_workspace_bytes returns. chi0_wk [2nw-1, N_k, nb^4]. */
+ * Intermediate G(iv, r), G(tau, r) and a double-float copy of G(tau, r) (the
+ * bubble's FFT input is formed from the copy; the tail-fit samples from the
+ * complex128 values) live in the caller's workspace, whose size
+ * tprf_imtime_bubble_workspace_bytes returns. chi0_wk [2nw-1, N_k, nb^4]. */
 size_t tprf_imtime_bubble_workspace_bytes(int n_iw, int n_tau, const int dims[3], int nb);
 int tprf_imtime_bubble_chi0_wk(double beta, int n_iw, int n_tau, int nw, const int dims[3],
                                int nb, const double *g_wk, const double *moments,
                                double *chi0_wk, void *workspace, size_t workspace_bytes,
                                void *stream);
+/* The same, recording events[0..4] (cudaEvent_t, each may be NULL) on `stream`
+ * before k->r and after k->r, iv->tau, the bubble + tau->iw and r->q: the
+ * per-stage timing of the benchmark. No reference counterpart. */
+int tprf_imtime_bubble_chi0_wk_timed(double beta, int n_iw, int n_tau, int nw, const int dims[3],
+                                     int nb, const double *g_wk, const double *moments,
+                                     double *chi0_wk, void *workspace, size_t workspace_bytes,
+                                     void *const *events, void *stream);
 
 /* ---- GW consumers of the chain ----------------------------------------------------
  * bubble_PI_wk (python/triqs_tprf/gw.py:56-91) is tprf_imtime_bubble_chi0_wk

@@ -83,6 +83,8 @@ SIGNATURES = {
     "tprf_imtime_bubble_workspace_bytes": (c_size_t, [c_int, c_int, c_int3, c_int]),
     "tprf_imtime_bubble_chi0_wk": (c_int, [c_double, c_int, c_int, c_int, c_int3, c_int, c_void_p, c_void_p,
                                            c_void_p, c_void_p, c_size_t, c_void_p]),
+    "tprf_imtime_bubble_chi0_wk_timed": (c_int, [c_double, c_int, c_int, c_int, c_int3, c_int, c_void_p, c_void_p,
+                                                 c_void_p, c_void_p, c_size_t, ctypes.POINTER(c_void_p), c_void_p]),
 }
 
 

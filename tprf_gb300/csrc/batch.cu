@@ -28,6 +28,10 @@ int launch_chi0_wr_from_grt(double beta, int n_tau, int nw, const int dims[3], i
                             double2 *chi0_wr, cudaStream_t stream);
 int launch_chi0_w0r_from_grt(double beta, int n_tau, const int dims[3], int nb, const double2 *g, double2 *chi0_wr,
                              cudaStream_t stream);
+int launch_nu_to_tau_df(double beta, int n_iw, int n_tau, long C, const double2 *gw, const double2 *mom, double2 *gt,
+                        void *gt_df, cudaStream_t stream);
+int launch_chi0_wr_from_grt_df(double beta, int n_tau, int nw, const int dims[3], int nb, const double2 *g,
+                               const void *g_df, double2 *chi0_wr, cudaStream_t stream);
 int launch_rpa(long n_points, int nb, const double2 *chi0, const double2 *U, double2 *chi, cudaStream_t stream);
 }  // namespace tprf
 
@@ -55,7 +59,7 @@ size_t inst_scratch(const tprf_instance &a) {
   const size_t g = 2ull * a.n_iw * nk * nb2, gt = (size_t)inst_ntau(a) * nk * nb2;
   const size_t c = (size_t)(2 * a.nw - 1) * nk * nb4;
   auto al = [](size_t n) { return (n * sizeof(double2) + 255) & ~size_t(255); };
-  return 2 * al(g) + al(gt) + al(c);
+  return 2 * al(g) + 2 * al(gt) + al(c);  // G(iv, k), G(iv, r), G(tau, r) and its double-float copy, chi0
 }
 
 // Relative cost used to balance the streams: FFT work plus the RPA solves.
@@ -88,15 +92,16 @@ int enqueue_instance(const tprf_instance &a, unsigned char *scratch, cudaStream_
   double2 *g_wk = reinterpret_cast<double2 *>(scratch);
   double2 *g_wr = reinterpret_cast<double2 *>(scratch + al(g));
   double2 *g_tr = reinterpret_cast<double2 *>(scratch + 2 * al(g));
-  double2 *chi0 = reinterpret_cast<double2 *>(scratch + 2 * al(g) + al(gt));
+  void *g_tr_df = scratch + 2 * al(g) + al(gt);
+  double2 *chi0 = reinterpret_cast<double2 *>(scratch + 2 * al(g) + 2 * al(gt));
   int st = launch_dyson(a.beta, a.n_iw, nk, a.nb, a.mu, reinterpret_cast<const double2 *>(a.e_k), nullptr, 0, g_wk, s);
   if (st) return st;
   if ((st = launch_lattice_fft(true, 2L * a.n_iw, a.dims, nb2, g_wk, g_wr, s))) return st;
-  if ((st = launch_nu_to_tau(a.beta, a.n_iw, nt, nk * nb2, g_wr, nullptr, g_tr, s))) return st;
+  if ((st = launch_nu_to_tau_df(a.beta, a.n_iw, nt, nk * nb2, g_wr, nullptr, g_tr, g_tr_df, s))) return st;
   if (a.nw == 1)
     st = launch_chi0_w0r_from_grt(a.beta, nt, a.dims, a.nb, g_tr, chi0, s);
   else
-    st = launch_chi0_wr_from_grt(a.beta, nt, a.nw, a.dims, a.nb, g_tr, chi0, s);
+    st = launch_chi0_wr_from_grt_df(a.beta, nt, a.nw, a.dims, a.nb, g_tr, g_tr_df, chi0, s);
   if (st) return st;
   if ((st = launch_lattice_fft(false, 2L * a.nw - 1, a.dims, nb4, chi0, chi0, s))) return st;
   return launch_rpa((2L * a.nw - 1) * nk, a.nb, chi0, reinterpret_cast<const double2 *>(a.U),

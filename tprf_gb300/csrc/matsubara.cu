@@ -75,6 +75,8 @@ FitRows make_fit_rows(double beta, int n_tau) {
 }
 
 // element-type plumbing: double2 (FP64) or cdf (double-float)
+template <class C> struct IsDfElem { static constexpr bool value = false; };
+template <> struct IsDfElem<cdf> { static constexpr bool value = true; };
 template <class C> __device__ __forceinline__ C from_d2(double2 z);
 template <> __device__ __forceinline__ double2 from_d2<double2>(double2 z) { return z; }
 template <> __device__ __forceinline__ cdf from_d2<cdf>(double2 z) { return to_cdf(z); }
@@ -122,7 +124,8 @@ __device__ __forceinline__ void tail_amplitudes(int fermion, double2 m1, double2
 template <class C>
 __global__ void __launch_bounds__(kMatsubaraThreads, 2) nu_to_tau_kernel(NuTauPlan p, const double2 *__restrict__ gw,
                                                         const double2 *__restrict__ mom, double2 *__restrict__ gt,
-                                                        long Ccols, int ic, int lg, unsigned *status) {
+                                                        long Ccols, int ic, int lg, unsigned *status,
+                                                        cdf *__restrict__ gt_df) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ unsigned s_res;
   C *a = reinterpret_cast<C *>(smem_raw);
@@ -190,6 +193,9 @@ __global__ void __launch_bounds__(kMatsubaraThreads, 2) nu_to_tau_kernel(NuTauPl
     // G[L] = -(G[0] + m1) for fermions, +(G[0] + m1) for bosons
     if (t == L) v = p.fermion ? csub(czero<C>(), cadd(v, am[3 * ic + c])) : cadd(v, am[3 * ic + c]);
     gt[(long)t * Ccols + col0 + c] = as_d2(v);
+    if constexpr (IsDfElem<C>::value) {
+      if (gt_df) gt_df[(long)t * Ccols + col0 + c] = v;  // the value before rounding to complex128
+    }
   }
 }
 
@@ -261,6 +267,23 @@ struct BubbleLoader {  // chi0 columns computed from G(tau, r): col = r * nb^4 +
   }
 };
 
+// The fused bubble with a double-float copy of G(tau, r) beside the complex128
+// one: the FFT input is the double-float product of the copies (FP32 pipe, no
+// conversion), and only the rows fit_derivatives samples take the FP64
+// product of the complex128 values (get64).
+struct BubbleLoaderDF : BubbleLoader {
+  const cdf *gdf;
+  template <class E>
+  __device__ __forceinline__ E get(int t, int c, long col0, int ic, const long *s) const {
+    if constexpr (IsDfElem<E>::value) {
+      const long slice = Nr * nb * nb;
+      return cmul(gdf[(long)t * slice + s[c]], gdf[(long)(n_tau - 1 - t) * slice + s[ic + c]]);
+    } else {
+      return get64(t, c, col0, ic, s);
+    }
+  }
+};
+
 // tau -> i omega. fit_derivatives moments in FP64 from the end rows; the tail
 // model enters after the FFT: chi(i w_m) = (beta/L) FFT(chi)[k_m] + sum_j a_j K[j][m].
 // FERM: the fermionic transform (input phase, fermion moments); a template
@@ -288,21 +311,27 @@ __global__ void __launch_bounds__(kMatsubaraThreads, 2) tau_to_w_kernel(TauWPlan
   const int total = (L + 1) * ic;
   for (int w0 = tid; w0 < total; w0 += 4 * nthr) {
     double2 v[4];
+    C e[4];
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       const int w = w0 + u * nthr;
       const int c = w & (ic - 1), t = w >> lg;
-      v[u] = (w < total && c < ncol) ? ld.get64(t, c, col0, ic, soff) : make_double2(0.0, 0.0);
+      const bool live = w < total && c < ncol;
+      // the sampled rows (and every row of the fermionic transform) in FP64
+      const bool in64 = FERM || t <= 8 || t >= L - 8;
+      v[u] = (live && in64) ? ld.get64(t, c, col0, ic, soff) : make_double2(0.0, 0.0);
+      e[u] = (live && !in64) ? ld.template get<C>(t, c, col0, ic, soff) : czero<C>();
     }
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       const int w = w0 + u * nthr;
       if (w < total) {
         const int c = w & (ic - 1), t = w >> lg;
+        const bool in64 = FERM || t <= 8 || t >= L - 8;
         if (t <= 8) smp[t * ic + c] = v[u];
         if (t >= L - 8) smp[(t - L + 17) * ic + c] = v[u];
         // the fermionic transform takes exp(i pi tau / beta) g(tau) (fourier_matsubara.cpp:164)
-        const C x = from_d2<C>(FERM && t < L ? cmul(v[u], p.ph[t]) : v[u]);
+        const C x = in64 ? from_d2<C>(FERM && t < L ? cmul(v[u], p.ph[t]) : v[u]) : e[u];
         if (t < L)
           a[rev[t] * ic + c] = x;
         else
@@ -314,37 +343,42 @@ __global__ void __launch_bounds__(kMatsubaraThreads, 2) tau_to_w_kernel(TauWPlan
   // fit_derivatives differentiates and then applies the inverse Vandermonde
   // matrix, which amplifies rounding: its 18 samples are the FP64 values, not
   // the double-float copy in the FFT buffer.
-  for (int c = tid; c < ic; c += nthr) {
-    if (c >= ncol) {
-      am[c] = am[ic + c] = am[2 * ic + c] = czero<C>();
-      continue;
-    }
-    const double2 g0 = smp[c], gL = smp[17 * ic + c];
-    double2 gl0 = make_double2(0.0, 0.0), gl1 = gl0, gr0 = gl0, gr1 = gl0;
+  // The four 8-term sums of a column (gl0, gl1, gr0, gr1) run on four adjacent
+  // lanes and meet by shuffles: 4 ic lanes work instead of ic, and no barrier
+  // is added (the FFT's own barrier orders am before the epilogue).
+  if (tid < ((4 * ic + 31) & ~31)) {
+    const int c = tid >> 2, q = tid & 3;
+    const int cc = c < ic ? c : 0;  // lanes past the tile read column 0 and store nothing
+    const double2 g0 = smp[cc], gL = smp[17 * ic + cc];
+    double2 sum = make_double2(0.0, 0.0);
 #pragma unroll
     for (int m = 0; m < 8; ++m) {
-      const double2 xl = smp[(m + 1) * ic + c];
-      const double2 dl = make_double2(xl.x - g0.x, xl.y - g0.y);
-      const double2 xr = smp[(16 - m) * ic + c];
-      const double2 dr = make_double2(gL.x - xr.x, gL.y - xr.y);
-      gl0 = make_double2(fma(fr.c0[m], dl.x, gl0.x), fma(fr.c0[m], dl.y, gl0.y));
-      gl1 = make_double2(fma(fr.c1[m], dl.x, gl1.x), fma(fr.c1[m], dl.y, gl1.y));
-      gr0 = make_double2(fma(fr.c0[m], dr.x, gr0.x), fma(fr.c0[m], dr.y, gr0.y));
-      gr1 = make_double2(fma(fr.c1[m], dr.x, gr1.x), fma(fr.c1[m], dr.y, gr1.y));
+      const double w = (q & 1) ? fr.c1[m] : fr.c0[m];
+      const double2 x = smp[(q < 2 ? m + 1 : 16 - m) * ic + cc];
+      const double2 d = q < 2 ? make_double2(x.x - g0.x, x.y - g0.y) : make_double2(gL.x - x.x, gL.y - x.y);
+      sum = make_double2(fma(w, d.x, sum.x), fma(w, d.y, sum.y));
     }
-    // m1 = -(g[0] -+ g[L]); m2 = gl0 - s gr0; m3 = -(gl1 + s gr1) 2 / dtau with
-    // s = +1 (boson), -1 (fermion) (fourier_matsubara.cpp:87-90, 153, 166)
-    double2 m1, m2, m3;
-    if (FERM) {
-      m1 = make_double2(-(g0.x + gL.x), -(g0.y + gL.y));
-      m2 = cadd(gl0, gr0);
-      m3 = cscale(csub(gl1, gr1), fr.k3);
-    } else {
-      m1 = make_double2(-(g0.x - gL.x), -(g0.y - gL.y));
-      m2 = csub(gl0, gr0);
-      m3 = cscale(cadd(gl1, gr1), fr.k3);
+    const int l0 = (tid & 31) & ~3;
+    const double2 gl0 = make_double2(__shfl_sync(0xffffffffu, sum.x, l0), __shfl_sync(0xffffffffu, sum.y, l0));
+    const double2 gl1 = make_double2(__shfl_sync(0xffffffffu, sum.x, l0 + 1), __shfl_sync(0xffffffffu, sum.y, l0 + 1));
+    const double2 gr0 = make_double2(__shfl_sync(0xffffffffu, sum.x, l0 + 2), __shfl_sync(0xffffffffu, sum.y, l0 + 2));
+    const double2 gr1 = make_double2(__shfl_sync(0xffffffffu, sum.x, l0 + 3), __shfl_sync(0xffffffffu, sum.y, l0 + 3));
+    if (q == 0 && c < ic && c >= ncol) am[c] = am[ic + c] = am[2 * ic + c] = czero<C>();
+    if (q == 0 && c < ncol) {
+      // m1 = -(g[0] -+ g[L]); m2 = gl0 - s gr0; m3 = -(gl1 + s gr1) 2 / dtau with
+      // s = +1 (boson), -1 (fermion) (fourier_matsubara.cpp:87-90, 153, 166)
+      double2 m1, m2, m3;
+      if (FERM) {
+        m1 = make_double2(-(g0.x + gL.x), -(g0.y + gL.y));
+        m2 = cadd(gl0, gr0);
+        m3 = cscale(csub(gl1, gr1), fr.k3);
+      } else {
+        m1 = make_double2(-(g0.x - gL.x), -(g0.y - gL.y));
+        m2 = csub(gl0, gr0);
+        m3 = cscale(cadd(gl1, gr1), fr.k3);
+      }
+      tail_amplitudes(FERM, m1, m2, m3, am, ic, c);
     }
-    tail_amplitudes(FERM, m1, m2, m3, am, ic, c);
   }
   // all stages but the last; the last is evaluated only at the kept frequencies
   C *r = fft_smem<false>(a, b, p.fft, ic, p.fft.nst - 1);
@@ -641,7 +675,15 @@ __global__ void __launch_bounds__(256) bubble_adjoint_kernel(BubbleLoader ld, co
 // ---- internal launchers (no synchronisation) --------------------------------
 
 int launch_nu_to_tau_stat(double beta, int n_iw, int n_tau, bool fermion, long C, const double2 *gw,
-                          const double2 *mom, double2 *gt, cudaStream_t stream);
+                          const double2 *mom, double2 *gt, cudaStream_t stream, cdf *gt_df = nullptr);
+
+// The fermionic transform that also writes G(tau) as double-float pairs into
+// gt_df (left untouched in the FP64 arithmetic mode), for the fused bubble's
+// double-float product.
+int launch_nu_to_tau_df(double beta, int n_iw, int n_tau, long C, const double2 *gw, const double2 *mom, double2 *gt,
+                        void *gt_df, cudaStream_t stream) {
+  return launch_nu_to_tau_stat(beta, n_iw, n_tau, true, C, gw, mom, gt, stream, reinterpret_cast<cdf *>(gt_df));
+}
 
 int launch_nu_to_tau(double beta, int n_iw, int n_tau, long C, const double2 *gw, const double2 *mom, double2 *gt,
                      cudaStream_t stream) {
@@ -651,7 +693,7 @@ int launch_nu_to_tau(double beta, int n_iw, int n_tau, long C, const double2 *gw
 // n: fermionic n_max or bosonic nw; the time mesh must hold L >= 2 n points
 // (fourier_matsubara.cpp:250-254).
 int launch_nu_to_tau_stat(double beta, int n_iw, int n_tau, bool fermion, long C, const double2 *gw,
-                          const double2 *mom, double2 *gt, cudaStream_t stream) {
+                          const double2 *mom, double2 *gt, cudaStream_t stream, cdf *gt_df) {
   if (n_tau < 0) n_tau = default_n_tau(n_iw);
   if (!(beta > 0.0) || n_iw < 1 || n_tau < 2 || C < 1 || (!fermion && n_iw < 2))
     return set_error(TPRF_ERR_INVALID_ARGUMENT, "fourier_wr_to_tr: bad mesh");
@@ -672,10 +714,12 @@ int launch_nu_to_tau_stat(double beta, int n_iw, int n_tau, bool fermion, long C
   const long blocks = (C + ic - 1) / ic;
   if (arith_mode() == kArithFP64) {
     TPRF_CUDA(cudaFuncSetAttribute(nu_to_tau_kernel<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    nu_to_tau_kernel<double2><<<(unsigned)blocks, kMatsubaraThreads, smem, stream>>>(*p, gw, mom, gt, C, ic, lg, status);
+    nu_to_tau_kernel<double2><<<(unsigned)blocks, kMatsubaraThreads, smem, stream>>>(*p, gw, mom, gt, C, ic, lg, status,
+                                                                                      nullptr);
   } else {
     TPRF_CUDA(cudaFuncSetAttribute(nu_to_tau_kernel<cdf>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    nu_to_tau_kernel<cdf><<<(unsigned)blocks, kMatsubaraThreads, smem, stream>>>(*p, gw, mom, gt, C, ic, lg, status);
+    nu_to_tau_kernel<cdf><<<(unsigned)blocks, kMatsubaraThreads, smem, stream>>>(*p, gw, mom, gt, C, ic, lg, status,
+                                                                                  gt_df);
   }
   TPRF_LAUNCH_CHECK("nu_to_tau_kernel");
   return TPRF_OK;
@@ -711,6 +755,24 @@ int launch_chi0_wr_from_grt(double beta, int n_tau, int nw, const int dims[3], i
   const BubbleLoader ld = make_bubble(g, n_tau, dims, nb);
   const long C = ld.Nr * nb * nb * nb * nb;
   return launch_tau_to_w_with(p, ld, chi0_wr, C, stream);
+}
+
+// The fused bubble + tau -> w reading a double-float copy of G(tau, r) as well
+// (written by launch_nu_to_tau_df); g_df == NULL or the FP64 arithmetic mode
+// takes the complex128 path.
+int launch_chi0_wr_from_grt_df(double beta, int n_tau, int nw, const int dims[3], int nb, const double2 *g,
+                               const void *g_df, double2 *chi0_wr, cudaStream_t stream) {
+  if (!g_df || arith_mode() == kArithFP64) return launch_chi0_wr_from_grt(beta, n_tau, nw, dims, nb, g, chi0_wr, stream);
+  int st = check_tau_w(beta, n_tau, nw);
+  if (st) return st;
+  if ((st = bubble_columns(dims, nb))) return st;
+  const TauWPlan *p = nullptr;
+  if ((st = get_tau_w_plan(beta, n_tau, nw, &p))) return st;
+  BubbleLoaderDF ld;
+  static_cast<BubbleLoader &>(ld) = make_bubble(g, n_tau, dims, nb);
+  ld.gdf = reinterpret_cast<const cdf *>(g_df);
+  const long C = ld.Nr * nb * nb * nb * nb;
+  return launch_tau_to_w_as<BubbleLoaderDF, cdf>(p, ld, chi0_wr, C, stream);
 }
 
 int launch_chi0_w0r_from_grt(double beta, int n_tau, const int dims[3], int nb, const double2 *g, double2 *chi0_wr,

@@ -20,6 +20,10 @@ int launch_chi0_wr_from_grt(double beta, int n_tau, int nw, const int dims[3], i
                             double2 *chi0_wr, cudaStream_t stream);
 int launch_chi0_w0r_from_grt(double beta, int n_tau, const int dims[3], int nb, const double2 *g, double2 *chi0_wr,
                              cudaStream_t stream);
+int launch_nu_to_tau_df(double beta, int n_iw, int n_tau, long C, const double2 *gw, const double2 *mom, double2 *gt,
+                        void *gt_df, cudaStream_t stream);
+int launch_chi0_wr_from_grt_df(double beta, int n_tau, int nw, const int dims[3], int nb, const double2 *g,
+                               const void *g_df, double2 *chi0_wr, cudaStream_t stream);
 }  // namespace tprf
 
 using namespace tprf;
@@ -29,12 +33,21 @@ extern "C" size_t tprf_imtime_bubble_workspace_bytes(int n_iw, int n_tau, const 
   const size_t nk = (size_t)dims[0] * dims[1] * dims[2];
   const size_t t = (size_t)nb * nb * nk;
   const size_t g_wr = 2ull * n_iw * t, g_tr = (size_t)n_tau * t;
-  return (g_wr + g_tr) * sizeof(double2) + 256;
+  // G(iv, r), G(tau, r) and its double-float copy (16 bytes per element each)
+  return (g_wr + 2 * g_tr) * sizeof(double2) + 256;
 }
 
 extern "C" int tprf_imtime_bubble_chi0_wk(double beta, int n_iw, int n_tau, int nw, const int dims[3], int nb,
                                           const double *g_wk, const double *moments, double *chi0_wk,
                                           void *workspace, size_t workspace_bytes, void *stream) {
+  return tprf_imtime_bubble_chi0_wk_timed(beta, n_iw, n_tau, nw, dims, nb, g_wk, moments, chi0_wk, workspace,
+                                          workspace_bytes, nullptr, stream);
+}
+
+extern "C" int tprf_imtime_bubble_chi0_wk_timed(double beta, int n_iw, int n_tau, int nw, const int dims[3], int nb,
+                                                const double *g_wk, const double *moments, double *chi0_wk,
+                                                void *workspace, size_t workspace_bytes, void *const *events,
+                                                void *stream) {
   if (!dims || !g_wk || !chi0_wk || !workspace || nb < 1 || nb > 8 || nw < 1 || n_iw < 1)
     return set_error(TPRF_ERR_INVALID_ARGUMENT, "imtime_bubble_chi0_wk: bad shape or null pointer");
   if (n_tau < 0) n_tau = default_n_tau(n_iw);
@@ -47,17 +60,25 @@ extern "C" int tprf_imtime_bubble_chi0_wk(double beta, int n_iw, int n_tau, int 
   uintptr_t ws = (reinterpret_cast<uintptr_t>(workspace) + 255) & ~uintptr_t(255);
   double2 *g_wr = reinterpret_cast<double2 *>(ws);
   double2 *g_tr = g_wr + 2L * n_iw * nk * nb2;
+  double2 *g_tr_df = g_tr + (long)n_tau * nk * nb2;  // double-float copy, same element size
   double2 *out = reinterpret_cast<double2 *>(chi0_wk);
-  int st = launch_lattice_fft(true, 2L * n_iw, dims, nb2, reinterpret_cast<const double2 *>(g_wk), g_wr, s);
-  if (st) return st;
-  st = launch_nu_to_tau(beta, n_iw, n_tau, nk * nb2, g_wr, reinterpret_cast<const double2 *>(moments), g_tr, s);
-  if (st) return st;
+  auto mark = [&](int i) -> int {
+    if (events && events[i]) TPRF_CUDA(cudaEventRecord(static_cast<cudaEvent_t>(events[i]), s));
+    return TPRF_OK;
+  };
+  int st;
+  if ((st = mark(0))) return st;
+  st = launch_lattice_fft(true, 2L * n_iw, dims, nb2, reinterpret_cast<const double2 *>(g_wk), g_wr, s);
+  if (st || (st = mark(1))) return st;
+  st = launch_nu_to_tau_df(beta, n_iw, n_tau, nk * nb2, g_wr, reinterpret_cast<const double2 *>(moments), g_tr,
+                           g_tr_df, s);
+  if (st || (st = mark(2))) return st;
   if (nw == 1)
     st = launch_chi0_w0r_from_grt(beta, n_tau, dims, nb, g_tr, out, s);
   else
-    st = launch_chi0_wr_from_grt(beta, n_tau, nw, dims, nb, g_tr, out, s);
-  if (st) return st;
+    st = launch_chi0_wr_from_grt_df(beta, n_tau, nw, dims, nb, g_tr, g_tr_df, out, s);
+  if (st || (st = mark(3))) return st;
   st = launch_lattice_fft(false, 2L * nw - 1, dims, nb4, out, out, s);
-  if (st) return st;
+  if (st || (st = mark(4))) return st;
   return finish_with_checks(s, "imtime_bubble_chi0_wk");
 }
