@@ -331,10 +331,10 @@ def run_gpu(args):
         out_host = torch.empty((nwt, nk) + (nb,) * 4, dtype=torch.complex128, pin_memory=True)
         wmesh = T.MeshImFreq(beta, "Fermion", n_max)
         kmesh = T.MeshBrZone(dims=dims)
-        ws = torch.empty(T.lattice_utils.bubble_workspace_bytes(n_max, n_tau, dims, nb), dtype=torch.uint8,
-                         device=dev)
         del g_wk, ws, chi0, chi
         torch.cuda.empty_cache()
+        ws = torch.empty(T.lattice_utils.bubble_workspace_bytes(n_max, n_tau, dims, nb), dtype=torch.uint8,
+                         device=dev)
         lib.tprf_set_sync_checks(1)
 
         chunk = -(-points // 32)
@@ -483,6 +483,113 @@ def run_gpu_batched(args):
                    "parallelism": f"replicas x{world}"},
         "plain_single_instance": {"value": plain, "unit": UNIT, "instances_timed": n_plain,
                                   "path": "lattice_dyson_g0_wk -> imtime_bubble_chi0_wk -> solve_rpa_PH per instance"},
+        "speedup_vs_plain_single_instance": value / plain,
+        "gpu_launches": None,
+        "clocks": clocks.summary(),
+    }
+    batch.close()
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def run_gpu_batched_grad(args):
+    """cfg2 with gradients: the 512 uneven instances of cfg2, forward graph then
+    backward graph (tprf_batch_grad_*) per step, giving chi of every instance and
+    the gradient of L = sum_i sum |chi_i|^2 with respect to every instance's U,
+    e(k) and hoppings t(R). The plain single-instance differentiable path
+    (tprf_gb300.autodiff, one instance after the other) is timed beside it."""
+    import numpy as np
+    import torch
+
+    from tprf_gb300 import _native, workloads
+    from tprf_gb300.autodiff import HoppingModel, chi_rpa
+    from tprf_gb300.batch import BatchedRPAGrad, RPAInstance
+    from tprf_gb300.tight_binding import ek_tensor
+
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    lib = _native.lib()
+    specs = workloads.batched_instances(512, seed=0)
+    insts = [RPAInstance(e_k=ek_tensor(d["hoppings"], d["dims"], device=dev), U=d["U"], dims=d["dims"],
+                         beta=d["beta"], mu=d["mu"], n_max=d["n_max"], nw=d["nw"]) for d in specs]
+    lib.tprf_set_sync_checks(0)
+    batch = BatchedRPAGrad(insts, n_streams=args.streams, device=dev)
+    points = batch.points
+    stream = torch.cuda.current_stream()
+
+    def step():
+        batch.forward()
+        torch.mul(batch.chi_flat, 2.0, out=batch.chi_grad_flat)  # dL/d conj(chi) of sum |chi|^2
+        batch.backward()
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    _native.check(lib.tprf_check_device_status(stream.cuda_stream), "warm-up")
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler(local)
+    barrier(world, dev)
+    torch.cuda.synchronize()
+    with clocks:
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+    barrier(world, dev)
+    _native.check(lib.tprf_check_device_status(stream.cuda_stream), "timed steps")
+    ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, world, dev)
+    value = world * points / (ms / 1e3)
+    # forward graph alone
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        batch.forward()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    fwd_ms = e0.elapsed_time(e1) / args.steps
+    # the plain single-instance differentiable path, one instance after the other
+    lib.tprf_set_sync_checks(1)
+    n_plain = min(len(insts), 64)
+    plain_pts = sum(a.points for a in insts[:n_plain])
+    models = []
+    for d in specs[:n_plain]:
+        nb = d["nb"]
+        pat = {(1, 0): np.eye(nb), (-1, 0): np.eye(nb)}
+        models.append(HoppingModel(base=d["hoppings"], patterns=[pat], dims=d["dims"], beta=d["beta"], mu=d["mu"],
+                                   n_max=d["n_max"], nw=d["nw"]))
+    Us = [torch.as_tensor(d["U"], dtype=torch.complex128, device=dev) for d in specs[:n_plain]]
+    theta0 = torch.zeros(1, dtype=torch.float64, device=dev)
+
+    def plain_pass():
+        for m, U in zip(models, Us):
+            th = theta0.clone().requires_grad_(True)
+            u = U.clone().requires_grad_(True)
+            (chi_rpa(th, u, m).abs() ** 2).sum().backward()
+
+    plain_pass()  # plans
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    plain_pass()
+    torch.cuda.synchronize()
+    plain = plain_pts / (time.perf_counter() - t0)
+    line = {
+        "metric": "RPA chi(q,iw) + dL/dU, dL/de(k), dL/dt(R) points/s (complex128)", "value": value, "unit": UNIT,
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic (seeded tight-binding models)",
+        "config": {"workload": "batched_512_square_lattice_instances_with_gradients", "instances": len(insts),
+                   "points_per_step": points, "loss": "sum_i sum |chi_i|^2", "streams": args.streams,
+                   "launch": "forward graph + backward graph per step", "parallelism": f"replicas x{world}"},
+        "forward_only": {"value": world * points / (fwd_ms / 1e3), "unit": UNIT, "ms_per_step": fwd_ms},
+        "plain_single_instance": {"value": plain, "unit": UNIT, "instances_timed": n_plain,
+                                  "path": "tprf_gb300.autodiff.chi_rpa forward + backward per instance"},
         "speedup_vs_plain_single_instance": value / plain,
         "gpu_launches": None,
         "clocks": clocks.summary(),
@@ -647,11 +754,14 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     ap.add_argument("--streams", type=int, default=32, help="concurrent streams of the batched graph (cfg2)")
+    ap.add_argument("--grad", action="store_true", help="cfg2: forward + gradient graphs per step")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.config == "cfg2" and args.grad:
+        run_gpu_batched_grad(args)
     elif args.config == "cfg2":
         run_gpu_batched(args)
     elif args.config == "cfg3":

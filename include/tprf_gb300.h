@@ -358,6 +358,38 @@ int tprf_batch_run(tprf_batch *batch, void *stream);
 int tprf_batch_size(const tprf_batch *batch);
 int tprf_batch_destroy(tprf_batch *batch);
 
+/* ---- batched forward + gradient ---------------------------------------------------
+ * The differentiable form of the batch: the forward graph also keeps each
+ * instance's chi0 (in the caller's buffer) and a second graph runs every
+ * instance's adjoint chain (RPA adjoint, r->q, tau->iw, G recomputed, bubble,
+ * iv->tau, k->r, Dyson). Gradients follow the conjugate-Wirtinger convention of
+ * torch: given chi_grad = dL/d conj(chi), the backward graph writes
+ *   U_grad [nb^4]            dL/d conj(U)
+ *   e_grad [N_k, nb, nb]     dL/d conj(e(k))                        (nullable)
+ *   t_grad [N_k, nb, nb]     dL/d conj(t(R)) for every lattice vector R of the
+ *                            periodic mesh, row-major R index like k, with
+ *                            e(k) = sum_R t(R) e^{i k.R}: t_grad(R) =
+ *                            sum_k e_grad(k) e^{-i k.R}             (nullable)
+ * No reference counterpart (the reference has no gradients); the single-instance
+ * adjoints above are the same maps. nw must be >= 2 (the trapezoid branch has no
+ * adjoint here). All buffers are device memory and must outlive the batch. */
+typedef struct {
+  tprf_instance inst;
+  double *chi0;            /* [2nw-1, N_k, nb^4], written by the forward graph */
+  const double *chi_grad;  /* same shape as chi, read by the backward graph */
+  double *U_grad;
+  double *e_grad;
+  double *t_grad;
+} tprf_grad_instance;
+
+size_t tprf_batch_grad_workspace_bytes(const tprf_grad_instance *inst, int n, int n_streams);
+/* Plans, runs forward and backward once eagerly, then captures both graphs.
+ * tprf_batch_run launches the forward graph of the returned batch. */
+int tprf_batch_grad_create(const tprf_grad_instance *inst, int n, int n_streams, void *workspace,
+                           size_t workspace_bytes, tprf_batch **out);
+/* One graph launch computing every instance's gradients from its chi_grad. */
+int tprf_batch_backward(tprf_batch *batch, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

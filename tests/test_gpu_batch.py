@@ -53,3 +53,35 @@ def test_batch_rejects_bad_instance(cuda_lib):
                       dims=(4, 4, 1), beta=1.0, mu=0.0, n_max=8, nw=8, n_tau=10)  # time mesh too short
     with pytest.raises(RuntimeError, match="time mesh"):
         BatchedRPA([bad])
+
+
+def test_batch_gradients_match_dense_cpu_autograd(cuda_lib):
+    """tprf_batch_grad_*: every instance's U, e(k) and t(R) gradients from one
+    backward graph launch against torch.autograd through the dense FP64 CPU
+    restatement, on two runs in a row (graph replay)."""
+    from oracle import torch_chain as TC
+    from tprf_gb300 import workloads
+    from tprf_gb300.batch import BatchedRPAGrad
+    specs = workloads.batched_instances(6, seed=5)
+    for i, d in enumerate(specs):  # small meshes keep the dense reference fast
+        d["dims"] = ((4, 6, 8)[i % 3], 6, 1)
+        d["n_max"] = (16, 20, 24)[i % 3]
+        d["nw"] = (2, 5, 8)[i % 3]
+    batch = BatchedRPAGrad(_make(specs), n_streams=3)
+    rng = np.random.default_rng(11)
+    for rep in range(2):
+        w = rng.standard_normal(batch.chi_grad_flat.numel()) + 1j * rng.standard_normal(batch.chi_grad_flat.numel())
+        batch.forward()
+        batch.backward(torch.as_tensor(w, device="cuda"))
+        torch.cuda.synchronize()
+        for i, (a, d) in enumerate(zip(batch.instances, specs)):
+            e_k = a.e_k.detach().cpu().clone().requires_grad_(True)
+            U = torch.as_tensor(d["U"], dtype=torch.complex128).clone().requires_grad_(True)
+            chi = TC.chi_rpa(e_k, U, d["dims"], d["beta"], d["mu"], d["n_max"], d["nw"])
+            assert rel_err(a.chi, chi.detach().reshape(a.chi.shape).numpy()) < PARITY_RTOL
+            chi.backward(batch.chi_grad[i].cpu().reshape(chi.shape))
+            assert rel_err(batch.U_grad[i], U.grad.numpy()) < 1e-9, i
+            assert rel_err(batch.e_grad[i], e_k.grad.numpy()) < 1e-9, i
+            t_ref = np.fft.fftn(e_k.grad.numpy().reshape(tuple(d["dims"]) + e_k.shape[1:]), axes=(0, 1, 2))
+            assert rel_err(batch.t_grad[i], t_ref.reshape(e_k.shape)) < 1e-9, i
+    batch.close()

@@ -24,6 +24,12 @@ class Instance(ctypes.Structure):
                 ("U", ctypes.c_void_p), ("chi", ctypes.c_void_p)]
 
 
+class GradInstance(ctypes.Structure):
+    """C layout of tprf_grad_instance (include/tprf_gb300.h)."""
+    _fields_ = [("inst", Instance), ("chi0", ctypes.c_void_p), ("chi_grad", ctypes.c_void_p),
+                ("U_grad", ctypes.c_void_p), ("e_grad", ctypes.c_void_p), ("t_grad", ctypes.c_void_p)]
+
+
 # name -> (restype, argtypes); mirrors include/tprf_gb300.h
 SIGNATURES = {
     "tprf_status_string": (ctypes.c_char_p, [c_int]),
@@ -80,6 +86,10 @@ SIGNATURES = {
     "tprf_batch_run": (c_int, [c_void_p, c_void_p]),
     "tprf_batch_size": (c_int, [c_void_p]),
     "tprf_batch_destroy": (c_int, [c_void_p]),
+    "tprf_batch_grad_workspace_bytes": (c_size_t, [ctypes.POINTER(GradInstance), c_int, c_int]),
+    "tprf_batch_grad_create": (c_int, [ctypes.POINTER(GradInstance), c_int, c_int, c_void_p, c_size_t,
+                                       ctypes.POINTER(c_void_p)]),
+    "tprf_batch_backward": (c_int, [c_void_p, c_void_p]),
     "tprf_imtime_bubble_workspace_bytes": (c_size_t, [c_int, c_int, c_int3, c_int]),
     "tprf_imtime_bubble_chi0_wk": (c_int, [c_double, c_int, c_int, c_int, c_int3, c_int, c_void_p, c_void_p,
                                            c_void_p, c_void_p, c_size_t, c_void_p]),

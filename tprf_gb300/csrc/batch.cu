@@ -9,6 +9,8 @@
 // stream that its instances reuse in turn, and captures all of it into one
 // CUDA graph; tprf_batch_run is then a single graph launch, so hundreds of
 // small instances run concurrently without per-kernel host overhead.
+// tprf_batch_grad_create adds a second graph with every instance's adjoint
+// chain (gradients with respect to U, e(k) and the hoppings t(R)).
 #include <algorithm>
 #include <cmath>
 #include <memory>
@@ -39,28 +41,43 @@ using namespace tprf;
 
 struct tprf_batch {
   std::vector<tprf_instance> inst;
-  std::vector<int> stream_of;        // instance -> stream slot
-  std::vector<size_t> slot_offset;   // stream slot -> offset in the workspace
+  std::vector<tprf_grad_instance> grad;  // empty unless made by tprf_batch_grad_create
+  std::vector<int> stream_of;            // instance -> stream slot
+  std::vector<size_t> slot_offset;       // stream slot -> offset in the workspace
   int n_streams = 0;
   std::vector<cudaStream_t> streams;
   std::vector<cudaEvent_t> events;
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t exec = nullptr;
+  cudaGraph_t graph = nullptr, graph_bwd = nullptr;
+  cudaGraphExec_t exec = nullptr, exec_bwd = nullptr;
 };
 
 namespace {
 
 long inst_nk(const tprf_instance &a) { return (long)a.dims[0] * a.dims[1] * a.dims[2]; }
 int inst_ntau(const tprf_instance &a) { return a.n_tau < 0 ? default_n_tau(a.n_iw) : a.n_tau; }
+size_t al16(size_t n) { return (n * sizeof(double2) + 255) & ~size_t(255); }
 
-// Scratch of one instance: G(iv, k), G(iv, r), G(tau, r) and chi0(w, q).
-size_t inst_scratch(const tprf_instance &a) {
-  const size_t nk = inst_nk(a), nb2 = (size_t)a.nb * a.nb, nb4 = nb2 * nb2;
-  const size_t g = 2ull * a.n_iw * nk * nb2, gt = (size_t)inst_ntau(a) * nk * nb2;
-  const size_t c = (size_t)(2 * a.nw - 1) * nk * nb4;
-  auto al = [](size_t n) { return (n * sizeof(double2) + 255) & ~size_t(255); };
-  return 2 * al(g) + 2 * al(gt) + al(c);  // G(iv, k), G(iv, r), G(tau, r) and its double-float copy, chi0
-}
+// Scratch layout of one instance (element counts; every part 256-byte aligned):
+//   G(iv, k) | G(iv, r) | G(tau, r) | double-float G(tau, r) | chi0(w, q) | chi0(tau, r) gradient
+// The forward pass uses the first five (chi0 only when the caller does not keep
+// it); the backward pass reuses them for the gradients of the same shapes.
+struct Layout {
+  size_t g, gt, c, ct;
+  Layout(const tprf_instance &a) {
+    const size_t nk = inst_nk(a), nb2 = (size_t)a.nb * a.nb, nb4 = nb2 * nb2;
+    g = 2ull * a.n_iw * nk * nb2;
+    gt = (size_t)inst_ntau(a) * nk * nb2;
+    c = (size_t)(2 * a.nw - 1) * nk * nb4;
+    ct = (size_t)inst_ntau(a) * nk * nb4;
+  }
+  size_t off_gwr() const { return al16(g); }
+  size_t off_gtr() const { return 2 * al16(g); }
+  size_t off_gdf() const { return 2 * al16(g) + al16(gt); }
+  size_t off_c() const { return 2 * al16(g) + 2 * al16(gt); }
+  size_t off_ct() const { return off_c() + al16(c); }
+  size_t forward_bytes() const { return off_c() + al16(c); }
+  size_t grad_bytes() const { return off_ct() + al16(ct); }
+};
 
 // Relative cost used to balance the streams: FFT work plus the RPA solves.
 double inst_cost(const tprf_instance &a) {
@@ -83,17 +100,61 @@ int check_instance(const tprf_instance &a, int i) {
   return TPRF_OK;
 }
 
-// The whole chain of one instance on one stream, into the slot's scratch.
-int enqueue_instance(const tprf_instance &a, unsigned char *scratch, cudaStream_t s) {
+int check_grad_instance(const tprf_grad_instance &g, int i) {
+  int st = check_instance(g.inst, i);
+  if (st) return st;
+  if (!g.chi0 || !g.chi_grad || !g.U_grad)
+    return set_error(TPRF_ERR_INVALID_ARGUMENT, "batch instance " + std::to_string(i) + ": null chi0, chi_grad or U_grad");
+  if (g.inst.nw < 2)
+    return set_error(TPRF_ERR_INVALID_ARGUMENT, "batch instance " + std::to_string(i) + ": the gradient needs nw >= 2");
+  return TPRF_OK;
+}
+
+// Longest-processing-time assignment of the instances to K stream slots; each
+// slot is sized for the largest scratch among its instances.
+struct Assignment {
+  std::vector<int> stream_of;
+  std::vector<std::vector<int>> per;
+  std::vector<size_t> slot;
+};
+Assignment assign(const tprf_instance *inst, int n, int n_streams, bool grad) {
+  std::vector<int> order(n);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return inst_cost(inst[x]) > inst_cost(inst[y]); });
+  const int K = std::min(n_streams, n);
+  Assignment A;
+  A.stream_of.assign(n, 0);
+  A.per.assign(K, {});
+  A.slot.assign(K, 0);
+  std::vector<double> load(K, 0.0);
+  for (int i : order) {
+    const int k = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+    load[k] += inst_cost(inst[i]) * (grad ? 3.0 : 1.0);
+    const Layout L(inst[i]);
+    A.slot[k] = std::max(A.slot[k], grad ? L.grad_bytes() : L.forward_bytes());
+    A.stream_of[i] = k;
+    A.per[k].push_back(i);
+  }
+  return A;
+}
+
+size_t workspace_total(const Assignment &A) {
+  size_t total = 256;
+  for (size_t x : A.slot) total += (x + 255) & ~size_t(255);
+  return total;
+}
+
+// The whole chain of one instance on one stream, into the slot's scratch;
+// chi0 goes to chi0_out when given (kept for the backward pass).
+int enqueue_instance(const tprf_instance &a, unsigned char *scratch, cudaStream_t s, double2 *chi0_out = nullptr) {
   const long nk = inst_nk(a), nb2 = (long)a.nb * a.nb, nb4 = nb2 * nb2;
   const int nt = inst_ntau(a);
-  auto al = [](size_t n) { return (n * sizeof(double2) + 255) & ~size_t(255); };
-  const size_t g = 2ull * a.n_iw * nk * nb2, gt = (size_t)nt * nk * nb2;
+  const Layout L(a);
   double2 *g_wk = reinterpret_cast<double2 *>(scratch);
-  double2 *g_wr = reinterpret_cast<double2 *>(scratch + al(g));
-  double2 *g_tr = reinterpret_cast<double2 *>(scratch + 2 * al(g));
-  void *g_tr_df = scratch + 2 * al(g) + al(gt);
-  double2 *chi0 = reinterpret_cast<double2 *>(scratch + 2 * al(g) + 2 * al(gt));
+  double2 *g_wr = reinterpret_cast<double2 *>(scratch + L.off_gwr());
+  double2 *g_tr = reinterpret_cast<double2 *>(scratch + L.off_gtr());
+  void *g_tr_df = scratch + L.off_gdf();
+  double2 *chi0 = chi0_out ? chi0_out : reinterpret_cast<double2 *>(scratch + L.off_c());
   int st = launch_dyson(a.beta, a.n_iw, nk, a.nb, a.mu, reinterpret_cast<const double2 *>(a.e_k), nullptr, 0, g_wk, s);
   if (st) return st;
   if ((st = launch_lattice_fft(true, 2L * a.n_iw, a.dims, nb2, g_wk, g_wr, s))) return st;
@@ -108,33 +169,154 @@ int enqueue_instance(const tprf_instance &a, unsigned char *scratch, cudaStream_
                     reinterpret_cast<double2 *>(a.chi), s);
 }
 
+// The adjoint chain of one instance (the transposes of enqueue_instance's
+// stages in reverse order, G recomputed). The r->q transform is unscaled
+// FFTW_BACKWARD, so its transpose is the unscaled forward transform; k->r is
+// (1/N_k) FFTW_FORWARD, whose transpose is (1/N_k) FFTW_BACKWARD.
+int enqueue_backward(const tprf_grad_instance &gi, unsigned char *scratch, cudaStream_t s, unsigned *status) {
+  const tprf_instance &a = gi.inst;
+  const long nk = inst_nk(a), nb2 = (long)a.nb * a.nb, nb4 = nb2 * nb2;
+  const int nt = inst_ntau(a), nwt = 2 * a.nw - 1;
+  const Layout L(a);
+  auto at = [&](size_t off) { return reinterpret_cast<double2 *>(scratch + off); };
+  double2 *g_wk = at(0), *g_wr = at(L.off_gwr()), *g_tr = at(L.off_gtr());
+  double2 *g_tr_grad = at(L.off_gdf());  // the double-float slot is not needed here
+  double2 *chi0_grad = at(L.off_c()), *chi0tr_grad = at(L.off_ct());
+  double2 *g_wr_grad = g_wr;        // G(iv, r) is dead once G(tau, r) is recomputed
+  double2 *g_wk_grad = chi0tr_grad;  // n_tau nb^4 >= 2 n_iw nb^2
+  double2 *e_grad = gi.e_grad ? reinterpret_cast<double2 *>(gi.e_grad) : chi0_grad;
+  double2 *U_grad = reinterpret_cast<double2 *>(gi.U_grad);
+  auto cd = [](const double *p) { return reinterpret_cast<const double2 *>(p); };
+  TPRF_CUDA(cudaMemsetAsync(U_grad, 0, nb4 * sizeof(double2), s));
+  int st = launch_rpa_adjoint_warp((long)nwt * nk, a.nb, cd(gi.chi0), cd(a.U), cd(a.chi), cd(gi.chi_grad), chi0_grad,
+                                   U_grad, s, status);
+  if (st) return st;
+  if ((st = launch_lattice_fft_scaled(true, nwt, a.dims, nb4, chi0_grad, chi0_grad, 1.0, s))) return st;
+  if ((st = launch_tau_to_w_adjoint(a.beta, nt, a.nw, nk * nb4, chi0_grad, chi0tr_grad, s))) return st;
+  if ((st = launch_dyson(a.beta, a.n_iw, nk, a.nb, a.mu, cd(a.e_k), nullptr, 0, g_wk, s))) return st;
+  if ((st = launch_lattice_fft(true, 2L * a.n_iw, a.dims, nb2, g_wk, g_wr, s))) return st;
+  if ((st = launch_nu_to_tau(a.beta, a.n_iw, nt, nk * nb2, g_wr, nullptr, g_tr, s))) return st;
+  if ((st = launch_bubble_adjoint(nt, a.dims, a.nb, g_tr, chi0tr_grad, g_tr_grad, s))) return st;
+  if ((st = launch_nu_to_tau_adjoint(a.beta, a.n_iw, nt, nk * nb2, g_tr_grad, g_wr_grad, true, s))) return st;
+  if ((st = launch_lattice_fft_scaled(false, 2L * a.n_iw, a.dims, nb2, g_wr_grad, g_wk_grad, 1.0 / (double)nk, s)))
+    return st;
+  if ((st = launch_dyson_adjoint(a.n_iw, nk, a.nb, g_wk, g_wk_grad, e_grad, s))) return st;
+  if (gi.t_grad)
+    st = launch_lattice_fft_scaled(true, 1, a.dims, nb2, e_grad, reinterpret_cast<double2 *>(gi.t_grad), 1.0, s);
+  return st;
+}
+
 void destroy_parts(tprf_batch *b) {
+  if (b->exec_bwd) cudaGraphExecDestroy(b->exec_bwd);
+  if (b->graph_bwd) cudaGraphDestroy(b->graph_bwd);
   if (b->exec) cudaGraphExecDestroy(b->exec);
   if (b->graph) cudaGraphDestroy(b->graph);
   for (auto e : b->events) cudaEventDestroy(e);
   for (auto s : b->streams) cudaStreamDestroy(s);
 }
 
+// Captures `body(i, scratch, stream)` for every instance, each on its slot's
+// stream, forked from and joined into streams[0], into one graph.
+template <class Body>
+int capture(tprf_batch *b, const std::vector<std::vector<int>> &per, uintptr_t base, Body body, cudaGraph_t *graph,
+            cudaGraphExec_t *exec) {
+  const int K = b->n_streams;
+  cudaStream_t s0 = b->streams[0];
+  TPRF_CUDA(cudaStreamBeginCapture(s0, cudaStreamCaptureModeThreadLocal));
+  int st = TPRF_OK;
+  cudaEventRecord(b->events[K], s0);
+  for (int k = 1; k < K; ++k) cudaStreamWaitEvent(b->streams[k], b->events[K], 0);
+  for (int k = 0; k < K && st == TPRF_OK; ++k)
+    for (int i : per[k]) {
+      st = body(i, reinterpret_cast<unsigned char *>(base + b->slot_offset[k]), b->streams[k]);
+      if (st) break;
+    }
+  for (int k = 1; k < K; ++k) {
+    cudaEventRecord(b->events[k], b->streams[k]);
+    cudaStreamWaitEvent(s0, b->events[k], 0);
+  }
+  cudaError_t e = cudaStreamEndCapture(s0, graph);
+  if (st == TPRF_OK && e != cudaSuccess) st = cuda_status(e, "batch_create: capture");
+  if (st == TPRF_OK) {
+    e = cudaGraphInstantiate(exec, *graph, 0);
+    if (e != cudaSuccess) st = cuda_status(e, "batch_create: graph instantiate");
+  }
+  return st;
+}
+
+// Shared by tprf_batch_create and tprf_batch_grad_create (grad != nullptr).
+int create_batch(const tprf_instance *inst, const tprf_grad_instance *grad, int n, int n_streams, void *workspace,
+                 size_t workspace_bytes, tprf_batch **out) {
+  const Assignment A = assign(inst, n, n_streams, grad != nullptr);
+  if (workspace_bytes < workspace_total(A))
+    return set_error(TPRF_ERR_ALLOC, "batch_create: workspace smaller than the workspace-bytes query");
+  auto b = std::make_unique<tprf_batch>();
+  b->inst.assign(inst, inst + n);
+  if (grad) b->grad.assign(grad, grad + n);
+  const int K = (int)A.per.size();
+  b->n_streams = K;
+  b->stream_of = A.stream_of;
+  const uintptr_t base = (reinterpret_cast<uintptr_t>(workspace) + 255) & ~uintptr_t(255);
+  size_t off = 0;
+  b->slot_offset.assign(K, 0);
+  for (int k = 0; k < K; ++k) {
+    b->slot_offset[k] = off;
+    off += (A.slot[k] + 255) & ~size_t(255);
+  }
+  auto fail = [&](int st) {
+    destroy_parts(b.get());
+    return st;
+  };
+  for (int k = 0; k < K; ++k) {
+    cudaStream_t s;
+    cudaError_t e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return fail(cuda_status(e, "batch_create: stream"));
+    b->streams.push_back(s);
+  }
+  b->events.resize(K + 1, nullptr);
+  for (auto &ev : b->events) {
+    cudaError_t e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    if (e != cudaSuccess) return fail(cuda_status(e, "batch_create: event"));
+  }
+  unsigned *status = device_status_word();
+  if (!status) return fail(TPRF_ERR_CUDA);
+  auto fwd = [&](int i, unsigned char *scratch, cudaStream_t s) {
+    return enqueue_instance(b->inst[i], scratch, s, grad ? reinterpret_cast<double2 *>(b->grad[i].chi0) : nullptr);
+  };
+  auto bwd = [&](int i, unsigned char *scratch, cudaStream_t s) {
+    return enqueue_backward(b->grad[i], scratch, s, status);
+  };
+  // Plans upload their tables synchronously, so every instance runs once,
+  // eagerly, on one stream before the capture (the backward pass reads whatever
+  // chi_grad holds; its outputs are overwritten by every later run).
+  cudaStream_t s0 = b->streams[0];
+  for (int i = 0; i < n; ++i) {
+    unsigned char *scratch = reinterpret_cast<unsigned char *>(base + b->slot_offset[A.stream_of[i]]);
+    int st = fwd(i, scratch, s0);
+    if (!st && grad) st = bwd(i, scratch, s0);
+    if (st) return fail(st);
+  }
+  cudaError_t e = cudaStreamSynchronize(s0);
+  if (e != cudaSuccess) return fail(cuda_status(e, "batch_create: first run"));
+  int st = capture(b.get(), A.per, base, fwd, &b->graph, &b->exec);
+  if (!st && grad) st = capture(b.get(), A.per, base, bwd, &b->graph_bwd, &b->exec_bwd);
+  if (st) return fail(st);
+  *out = b.release();
+  return TPRF_OK;
+}
+
 }  // namespace
 
 extern "C" size_t tprf_batch_workspace_bytes(const tprf_instance *inst, int n, int n_streams) {
   if (!inst || n < 1 || n_streams < 1) return 0;
-  // same greedy assignment as tprf_batch_create: every stream slot holds the
-  // largest scratch among its instances
-  std::vector<int> order(n);
-  std::iota(order.begin(), order.end(), 0);
-  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return inst_cost(inst[x]) > inst_cost(inst[y]); });
-  const int K = std::min(n_streams, n);
-  std::vector<double> load(K, 0.0);
-  std::vector<size_t> slot(K, 0);
-  for (int i : order) {
-    const int k = (int)(std::min_element(load.begin(), load.end()) - load.begin());
-    load[k] += inst_cost(inst[i]);
-    slot[k] = std::max(slot[k], inst_scratch(inst[i]));
-  }
-  size_t total = 256;
-  for (size_t x : slot) total += (x + 255) & ~size_t(255);
-  return total;
+  return workspace_total(assign(inst, n, n_streams, false));
+}
+
+extern "C" size_t tprf_batch_grad_workspace_bytes(const tprf_grad_instance *inst, int n, int n_streams) {
+  if (!inst || n < 1 || n_streams < 1) return 0;
+  std::vector<tprf_instance> base(n);
+  for (int i = 0; i < n; ++i) base[i] = inst[i].inst;
+  return workspace_total(assign(base.data(), n, n_streams, true));
 }
 
 extern "C" int tprf_batch_create(const tprf_instance *inst, int n, int n_streams, void *workspace,
@@ -145,88 +327,27 @@ extern "C" int tprf_batch_create(const tprf_instance *inst, int n, int n_streams
     int st = check_instance(inst[i], i);
     if (st) return st;
   }
-  if (workspace_bytes < tprf_batch_workspace_bytes(inst, n, n_streams))
-    return set_error(TPRF_ERR_ALLOC, "batch_create: workspace smaller than tprf_batch_workspace_bytes");
-  auto b = std::make_unique<tprf_batch>();
-  b->inst.assign(inst, inst + n);
-  // longest-processing-time assignment to streams
-  std::vector<int> order(n);
-  std::iota(order.begin(), order.end(), 0);
-  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return inst_cost(inst[x]) > inst_cost(inst[y]); });
-  const int K = std::min(n_streams, n);
-  b->n_streams = K;
-  b->stream_of.assign(n, 0);
-  std::vector<double> load(K, 0.0);
-  std::vector<size_t> slot(K, 0);
-  std::vector<std::vector<int>> per(K);
-  for (int i : order) {
-    const int k = (int)(std::min_element(load.begin(), load.end()) - load.begin());
-    load[k] += inst_cost(inst[i]);
-    slot[k] = std::max(slot[k], inst_scratch(inst[i]));
-    b->stream_of[i] = k;
-    per[k].push_back(i);
-  }
-  const uintptr_t base = (reinterpret_cast<uintptr_t>(workspace) + 255) & ~uintptr_t(255);
-  size_t off = 0;
-  b->slot_offset.assign(K, 0);
-  for (int k = 0; k < K; ++k) {
-    b->slot_offset[k] = off;
-    off += (slot[k] + 255) & ~size_t(255);
-  }
-  // Plans and the device error word are built before capture (they upload
-  // tables synchronously): run every instance once, eagerly, on one stream.
-  cudaStream_t s0 = nullptr;
-  TPRF_CUDA(cudaStreamCreateWithFlags(&s0, cudaStreamNonBlocking));
-  b->streams.push_back(s0);
-  if (!device_status_word()) {
-    destroy_parts(b.get());
-    return TPRF_ERR_CUDA;
-  }
+  return create_batch(inst, nullptr, n, n_streams, workspace, workspace_bytes, out);
+}
+
+extern "C" int tprf_batch_grad_create(const tprf_grad_instance *inst, int n, int n_streams, void *workspace,
+                                      size_t workspace_bytes, tprf_batch **out) {
+  if (!inst || n < 1 || n_streams < 1 || !workspace || !out)
+    return set_error(TPRF_ERR_INVALID_ARGUMENT, "batch_grad_create: bad arguments");
+  std::vector<tprf_instance> base(n);
   for (int i = 0; i < n; ++i) {
-    int st = enqueue_instance(b->inst[i], reinterpret_cast<unsigned char *>(base + b->slot_offset[b->stream_of[i]]), s0);
-    if (st) {
-      destroy_parts(b.get());
-      return st;
-    }
+    int st = check_grad_instance(inst[i], i);
+    if (st) return st;
+    base[i] = inst[i].inst;
   }
-  cudaError_t e = cudaStreamSynchronize(s0);
-  if (e != cudaSuccess) {
-    destroy_parts(b.get());
-    return cuda_status(e, "batch_create: first run");
-  }
-  // capture: fork K streams from s0, one chain of instances each, join
-  for (int k = 1; k < K; ++k) {
-    cudaStream_t s;
-    TPRF_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
-    b->streams.push_back(s);
-  }
-  b->events.resize(K + 1);
-  for (auto &ev : b->events) TPRF_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
-  TPRF_CUDA(cudaStreamBeginCapture(s0, cudaStreamCaptureModeThreadLocal));
-  int st = TPRF_OK;
-  cudaEventRecord(b->events[K], s0);
-  for (int k = 1; k < K; ++k) cudaStreamWaitEvent(b->streams[k], b->events[K], 0);
-  for (int k = 0; k < K && st == TPRF_OK; ++k)
-    for (int i : per[k]) {
-      st = enqueue_instance(b->inst[i], reinterpret_cast<unsigned char *>(base + b->slot_offset[k]), b->streams[k]);
-      if (st) break;
-    }
-  for (int k = 1; k < K; ++k) {
-    cudaEventRecord(b->events[k], b->streams[k]);
-    cudaStreamWaitEvent(s0, b->events[k], 0);
-  }
-  e = cudaStreamEndCapture(s0, &b->graph);
-  if (st == TPRF_OK && e != cudaSuccess) st = cuda_status(e, "batch_create: capture");
-  if (st == TPRF_OK) {
-    e = cudaGraphInstantiate(&b->exec, b->graph, 0);
-    if (e != cudaSuccess) st = cuda_status(e, "batch_create: graph instantiate");
-  }
-  if (st) {
-    destroy_parts(b.get());
-    return st;
-  }
-  *out = b.release();
-  return TPRF_OK;
+  return create_batch(base.data(), inst, n, n_streams, workspace, workspace_bytes, out);
+}
+
+extern "C" int tprf_batch_backward(tprf_batch *b, void *stream) {
+  if (!b || !b->exec_bwd) return set_error(TPRF_ERR_INVALID_ARGUMENT, "batch_backward: not a gradient batch");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  TPRF_CUDA(cudaGraphLaunch(b->exec_bwd, s));
+  return finish_with_checks(s, "batch_backward");
 }
 
 extern "C" int tprf_batch_run(tprf_batch *b, void *stream) {

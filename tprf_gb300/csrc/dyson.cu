@@ -229,16 +229,9 @@ int launch_dyson_adjoint_nb(int n_nu, long n_k, const double2 *g, const double2 
 }
 
 }  // namespace
-}  // namespace tprf
 
-extern "C" int tprf_lattice_dyson_g_wk_adjoint(int n_iw, long n_k, int nb, const double *g_wk, const double *g_wk_grad,
-                                               double *e_k_grad, void *stream) {
-  using namespace tprf;
-  if (n_iw < 1 || n_k < 1 || !g_wk || !g_wk_grad || !e_k_grad)
-    return set_error(TPRF_ERR_INVALID_ARGUMENT, "lattice_dyson_g_wk_adjoint: bad shape or null pointer");
-  const double2 *g = reinterpret_cast<const double2 *>(g_wk), *gg = reinterpret_cast<const double2 *>(g_wk_grad);
-  double2 *out = reinterpret_cast<double2 *>(e_k_grad);
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
+int launch_dyson_adjoint(int n_iw, long n_k, int nb, const double2 *g, const double2 *gg, double2 *out,
+                         cudaStream_t s) {
   switch (nb) {
     case 1: return launch_dyson_adjoint_nb<1>(2 * n_iw, n_k, g, gg, out, s);
     case 2: return launch_dyson_adjoint_nb<2>(2 * n_iw, n_k, g, gg, out, s);
@@ -247,4 +240,16 @@ extern "C" int tprf_lattice_dyson_g_wk_adjoint(int n_iw, long n_k, int nb, const
     case 5: return launch_dyson_adjoint_nb<5>(2 * n_iw, n_k, g, gg, out, s);
     default: return set_error(TPRF_ERR_INVALID_ARGUMENT, "lattice_dyson_g_wk_adjoint: nb must be 1..5");
   }
+}
+
+}  // namespace tprf
+
+extern "C" int tprf_lattice_dyson_g_wk_adjoint(int n_iw, long n_k, int nb, const double *g_wk, const double *g_wk_grad,
+                                               double *e_k_grad, void *stream) {
+  using namespace tprf;
+  if (n_iw < 1 || n_k < 1 || !g_wk || !g_wk_grad || !e_k_grad)
+    return set_error(TPRF_ERR_INVALID_ARGUMENT, "lattice_dyson_g_wk_adjoint: bad shape or null pointer");
+  return launch_dyson_adjoint(n_iw, n_k, nb, reinterpret_cast<const double2 *>(g_wk),
+                              reinterpret_cast<const double2 *>(g_wk_grad), reinterpret_cast<double2 *>(e_k_grad),
+                              static_cast<cudaStream_t>(stream));
 }

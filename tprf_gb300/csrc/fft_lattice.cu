@@ -184,17 +184,36 @@ int launch_plane(const double2 *in, double2 *out, long outer, int n1, int n2, lo
 }  // namespace
 
 // Transform over the 3 mesh dims of [n_w, dims..., n_target]; in == out allowed.
+__global__ void __launch_bounds__(256) scale_copy_kernel(const double2 *__restrict__ in, double2 *__restrict__ out,
+                                                         long n, double s) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    out[i] = cscale(in[i], s);
+}
+
 int launch_lattice_fft(bool forward, long n_w, const int dims[3], long n_target, const double2 *in, double2 *out,
                        cudaStream_t stream) {
   const long nk = (long)dims[0] * dims[1] * dims[2];
+  return launch_lattice_fft_scaled(forward, n_w, dims, n_target, in, out, forward ? 1.0 / (double)nk : 1.0, stream);
+}
+
+// The lattice transform with an explicit overall factor (the adjoints use the
+// unscaled forward and the 1/N_k-scaled backward transforms).
+int launch_lattice_fft_scaled(bool forward, long n_w, const int dims[3], long n_target, const double2 *in,
+                              double2 *out, double scale_last, cudaStream_t stream) {
   int last = -1;
   for (int ax = 0; ax < 3; ++ax)
     if (dims[ax] > 1) last = ax;
-  if (last < 0) {  // a single k point: the transform is the identity
-    if (in != out) TPRF_CUDA(cudaMemcpyAsync(out, in, n_w * n_target * sizeof(double2), cudaMemcpyDeviceToDevice, stream));
+  if (last < 0) {  // a single k point: the transform is the identity (times the factor)
+    const long n = n_w * n_target;
+    if (scale_last == 1.0) {
+      if (in != out) TPRF_CUDA(cudaMemcpyAsync(out, in, n * sizeof(double2), cudaMemcpyDeviceToDevice, stream));
+    } else {
+      scale_copy_kernel<<<(unsigned)std::min((n + 255) / 256, (long)num_sms() * 8), 256, 0, stream>>>(in, out, n,
+                                                                                                    scale_last);
+      TPRF_LAUNCH_CHECK("scale_copy_kernel");
+    }
     return TPRF_OK;
   }
-  const double scale_last = forward ? 1.0 / (double)nk : 1.0;
   const double2 *src = in;
   // The two fastest-varying non-trivial axes in one pass where they are powers
   // of two; the remaining axis (if any) in a one-axis pass, which then scales.

@@ -121,4 +121,21 @@ inline int default_n_tau(int n_iw) { return 6 * n_iw + 1; }
 int max_smem_optin();
 int num_sms();
 
+// Stream-ordered launchers shared by the C-ABI entry points and the batched
+// graphs (no synchronisation; plans must exist before a graph capture).
+int launch_lattice_fft(bool forward, long n_w, const int dims[3], long n_target, const double2 *in, double2 *out,
+                       cudaStream_t stream);
+int launch_lattice_fft_scaled(bool forward, long n_w, const int dims[3], long n_target, const double2 *in,
+                              double2 *out, double scale, cudaStream_t stream);
+int launch_tau_to_w_adjoint(double beta, int n_tau, int nw, long C, const double2 *yg, double2 *xg,
+                            cudaStream_t stream);
+int launch_nu_to_tau_adjoint(double beta, int n_iw, int n_tau, long C, const double2 *yg, double2 *gg, bool fitted,
+                             cudaStream_t stream);
+int launch_bubble_adjoint(int n_tau, const int dims[3], int nb, const double2 *g_tr, const double2 *chig,
+                          double2 *gg, cudaStream_t stream);
+int launch_dyson_adjoint(int n_iw, long n_k, int nb, const double2 *g, const double2 *gg, double2 *e_grad,
+                         cudaStream_t stream);
+int launch_rpa_adjoint_warp(long n_points, int nb, const double2 *chi0, const double2 *U, const double2 *chi,
+                            const double2 *chig, double2 *chi0g, double2 *Ug, cudaStream_t stream, unsigned *status);
+
 }  // namespace tprf

@@ -91,11 +91,6 @@ template <> __device__ __forceinline__ cdf table<cdf>(const double2 *, const flo
 template <class C> __device__ __forceinline__ typename RealT<C>::type real_of(double v);
 template <> __device__ __forceinline__ double real_of<double2>(double v) { return v; }
 template <> __device__ __forceinline__ dfl real_of<cdf>(double v) { return split_double(v); }
-__device__ __forceinline__ float cabsf_approx(double2 z) { return (float)sqrt(cabs2(z)); }
-__device__ __forceinline__ float cabsf_approx(cdf z) {
-  const float x = __fadd_rn(z.x.hi, z.x.lo), y = __fadd_rn(z.y.hi, z.y.lo);
-  return sqrtf(x * x + y * y);
-}
 
 // The three-pole tail amplitudes a_j from the moments m1..m3
 // (fourier_matsubara.cpp:156-171 and 268-284): fermion b = (0, 1, -1),
@@ -886,24 +881,63 @@ extern "C" int tprf_chi0_w0r_from_grt_PH(double beta, int n_tau, const int dims[
 
 // ---- adjoints (differentiable path) -------------------------------------------
 
-extern "C" int tprf_chi_wr_from_chi_tr_adjoint(double beta, int n_tau, int nw, long n_r, long n_target,
-                                               const double *chi_wr_grad, double *chi_tr_grad, void *stream) {
-  if (!chi_wr_grad || !chi_tr_grad || n_r < 1 || n_target < 1)
-    return set_error(TPRF_ERR_INVALID_ARGUMENT, "chi_wr_from_chi_tr_adjoint: bad shape or null pointer");
+namespace tprf {
+
+// Internal launchers of the adjoints (no synchronisation; also used inside
+// the batched gradient's graph capture once their plans exist).
+int launch_tau_to_w_adjoint(double beta, int n_tau, int nw, long C, const double2 *yg, double2 *xg,
+                            cudaStream_t stream) {
   int st = check_tau_w(beta, n_tau, nw);
   if (st) return st;
   const TauWPlan *p = nullptr;
   if ((st = get_tau_w_plan(beta, n_tau, nw, &p))) return st;
-  const long C = n_r * n_target;
   int ic, lg;
   size_t smem;
   if ((st = pick_ic(p->fft, 18 * sizeof(double2), &ic, &lg, &smem))) return st;
   TPRF_CUDA(cudaFuncSetAttribute(tau_to_w_adjoint_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  tau_to_w_adjoint_kernel<<<(unsigned)((C + ic - 1) / ic), 256, smem, static_cast<cudaStream_t>(stream)>>>(
-      *p, make_vinv_rows(), reinterpret_cast<const double2 *>(chi_wr_grad), reinterpret_cast<double2 *>(chi_tr_grad),
-      C, ic, lg);
+  tau_to_w_adjoint_kernel<<<(unsigned)((C + ic - 1) / ic), 256, smem, stream>>>(*p, make_vinv_rows(), yg, xg, C, ic,
+                                                                               lg);
   TPRF_LAUNCH_CHECK("tau_to_w_adjoint_kernel");
   return TPRF_OK;
+}
+
+int launch_nu_to_tau_adjoint(double beta, int n_iw, int n_tau, long C, const double2 *yg, double2 *gg, bool fitted,
+                             cudaStream_t stream) {
+  if (n_tau - 1 < 2 * n_iw)
+    return set_error(TPRF_ERR_MESH_TOO_SHORT, "Inverse Fourier: the time mesh must be at least twice as long as the freq mesh");
+  const NuTauPlan *p = nullptr;
+  int st = get_nu_tau_plan(beta, n_iw, n_tau, &p);
+  if (st) return st;
+  int ic, lg;
+  size_t smem;
+  if ((st = pick_ic(p->fft, 3 * sizeof(double2), &ic, &lg, &smem))) return st;
+  TPRF_CUDA(cudaFuncSetAttribute(nu_to_tau_adjoint_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  nu_to_tau_adjoint_kernel<<<(unsigned)((C + ic - 1) / ic), 256, smem, stream>>>(*p, yg, gg, C, ic, lg,
+                                                                                fitted ? 1 : 0);
+  TPRF_LAUNCH_CHECK("nu_to_tau_adjoint_kernel");
+  return TPRF_OK;
+}
+
+int launch_bubble_adjoint(int n_tau, const int dims[3], int nb, const double2 *g_tr, const double2 *chig,
+                          double2 *gg, cudaStream_t stream) {
+  int st = check_bubble(n_tau, dims, nb, g_tr, gg);
+  if (st) return st;
+  if (!chig) return set_error(TPRF_ERR_INVALID_ARGUMENT, "bubble adjoint: null gradient");
+  const BubbleLoader ld = make_bubble(g_tr, n_tau, dims, nb);
+  const long total = (long)n_tau * ld.Nr * nb * nb;
+  bubble_adjoint_kernel<<<(unsigned)grid_for(total, 256), 256, 0, stream>>>(ld, chig, gg);
+  TPRF_LAUNCH_CHECK("bubble_adjoint_kernel");
+  return TPRF_OK;
+}
+
+}  // namespace tprf
+
+extern "C" int tprf_chi_wr_from_chi_tr_adjoint(double beta, int n_tau, int nw, long n_r, long n_target,
+                                               const double *chi_wr_grad, double *chi_tr_grad, void *stream) {
+  if (!chi_wr_grad || !chi_tr_grad || n_r < 1 || n_target < 1)
+    return set_error(TPRF_ERR_INVALID_ARGUMENT, "chi_wr_from_chi_tr_adjoint: bad shape or null pointer");
+  return launch_tau_to_w_adjoint(beta, n_tau, nw, n_r * n_target, reinterpret_cast<const double2 *>(chi_wr_grad),
+                                 reinterpret_cast<double2 *>(chi_tr_grad), static_cast<cudaStream_t>(stream));
 }
 
 extern "C" int tprf_fourier_wr_to_tr_adjoint(double beta, int n_iw, int n_tau, long n_r, long n_target,
@@ -911,32 +945,14 @@ extern "C" int tprf_fourier_wr_to_tr_adjoint(double beta, int n_iw, int n_tau, l
   if (!g_tr_grad || !g_wr_grad || n_r < 1 || n_target < 1 || n_iw < 1 || !(beta > 0.0))
     return set_error(TPRF_ERR_INVALID_ARGUMENT, "fourier_wr_to_tr_adjoint: bad shape or null pointer");
   if (n_tau < 0) n_tau = default_n_tau(n_iw);
-  if (n_tau - 1 < 2 * n_iw)
-    return set_error(TPRF_ERR_MESH_TOO_SHORT, "Inverse Fourier: the time mesh must be at least twice as long as the freq mesh");
-  const NuTauPlan *p = nullptr;
-  int st = get_nu_tau_plan(beta, n_iw, n_tau, &p);
-  if (st) return st;
-  const long C = n_r * n_target;
-  int ic, lg;
-  size_t smem;
-  if ((st = pick_ic(p->fft, 3 * sizeof(double2), &ic, &lg, &smem))) return st;
-  TPRF_CUDA(cudaFuncSetAttribute(nu_to_tau_adjoint_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  nu_to_tau_adjoint_kernel<<<(unsigned)((C + ic - 1) / ic), 256, smem, static_cast<cudaStream_t>(stream)>>>(
-      *p, reinterpret_cast<const double2 *>(g_tr_grad), reinterpret_cast<double2 *>(g_wr_grad), C, ic, lg,
-      fitted ? 1 : 0);
-  TPRF_LAUNCH_CHECK("nu_to_tau_adjoint_kernel");
-  return TPRF_OK;
+  return launch_nu_to_tau_adjoint(beta, n_iw, n_tau, n_r * n_target, reinterpret_cast<const double2 *>(g_tr_grad),
+                                  reinterpret_cast<double2 *>(g_wr_grad), fitted != 0,
+                                  static_cast<cudaStream_t>(stream));
 }
 
 extern "C" int tprf_chi0_tr_from_grt_PH_adjoint(int n_tau, const int dims[3], int nb, const double *g_tr,
                                                 const double *chi0_tr_grad, double *g_tr_grad, void *stream) {
-  int st = check_bubble(n_tau, dims, nb, g_tr, g_tr_grad);
-  if (st) return st;
-  if (!chi0_tr_grad) return set_error(TPRF_ERR_INVALID_ARGUMENT, "bubble adjoint: null gradient");
-  const BubbleLoader ld = make_bubble(reinterpret_cast<const double2 *>(g_tr), n_tau, dims, nb);
-  const long total = (long)n_tau * ld.Nr * nb * nb;
-  bubble_adjoint_kernel<<<(unsigned)grid_for(total, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
-      ld, reinterpret_cast<const double2 *>(chi0_tr_grad), reinterpret_cast<double2 *>(g_tr_grad));
-  TPRF_LAUNCH_CHECK("bubble_adjoint_kernel");
-  return TPRF_OK;
+  return launch_bubble_adjoint(n_tau, dims, nb, reinterpret_cast<const double2 *>(g_tr),
+                               reinterpret_cast<const double2 *>(chi0_tr_grad), reinterpret_cast<double2 *>(g_tr_grad),
+                               static_cast<cudaStream_t>(stream));
 }
