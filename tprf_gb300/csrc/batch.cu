@@ -188,7 +188,7 @@ int enqueue_backward(const tprf_grad_instance &gi, unsigned char *scratch, cudaS
   double2 *U_grad = reinterpret_cast<double2 *>(gi.U_grad);
   auto cd = [](const double *p) { return reinterpret_cast<const double2 *>(p); };
   TPRF_CUDA(cudaMemsetAsync(U_grad, 0, nb4 * sizeof(double2), s));
-  int st = launch_rpa_adjoint_warp((long)nwt * nk, a.nb, cd(gi.chi0), cd(a.U), cd(a.chi), cd(gi.chi_grad), chi0_grad,
+  int st = launch_rpa_adjoint((long)nwt * nk, a.nb, cd(gi.chi0), cd(a.U), cd(a.chi), cd(gi.chi_grad), chi0_grad,
                                    U_grad, s, status);
   if (st) return st;
   if ((st = launch_lattice_fft_scaled(true, nwt, a.dims, nb4, chi0_grad, chi0_grad, 1.0, s))) return st;

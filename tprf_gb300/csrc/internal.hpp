@@ -135,7 +135,7 @@ int launch_bubble_adjoint(int n_tau, const int dims[3], int nb, const double2 *g
                           double2 *gg, cudaStream_t stream);
 int launch_dyson_adjoint(int n_iw, long n_k, int nb, const double2 *g, const double2 *gg, double2 *e_grad,
                          cudaStream_t stream);
-int launch_rpa_adjoint_warp(long n_points, int nb, const double2 *chi0, const double2 *U, const double2 *chi,
-                            const double2 *chig, double2 *chi0g, double2 *Ug, cudaStream_t stream, unsigned *status);
+int launch_rpa_adjoint(long n_points, int nb, const double2 *chi0, const double2 *U, const double2 *chi,
+                       const double2 *chig, double2 *chi0g, double2 *Ug, cudaStream_t stream, unsigned *status);
 
 }  // namespace tprf

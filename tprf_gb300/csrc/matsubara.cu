@@ -512,11 +512,38 @@ int check_bubble(int n_tau, const int dims[3], int nb, const void *g, const void
 // ---------------------------------------------------------------------------
 // Adjoints (transposed linear maps) for the differentiable path, in FP64.
 
+// Sum over the threads of a CTA that share a column (c = tid & (ic - 1),
+// ic a power of two <= 32) of three complex partials: shuffles inside a warp
+// over the lanes that differ in the bits above c, then the warps' results
+// through red ([n_warps][3][ic]). The sums end in the threads tid < ic; every
+// thread of the CTA must call it.
+__device__ __forceinline__ void column_sum3(double2 v[3], double2 *red, int ic) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, n_warps = blockDim.x >> 5;
+#pragma unroll
+  for (int j = 0; j < 3; ++j)
+    for (int off = 16; off >= ic; off >>= 1) {
+      v[j].x += __shfl_xor_sync(0xffffffffu, v[j].x, off);
+      v[j].y += __shfl_xor_sync(0xffffffffu, v[j].y, off);
+    }
+  if (lane < ic)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) red[(warp * 3 + j) * ic + lane] = v[j];
+  __syncthreads();
+  if (tid < ic)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      double2 s = make_double2(0.0, 0.0);
+      for (int w = 0; w < n_warps; ++w) s = cadd(s, red[(w * 3 + j) * ic + tid]);
+      v[j] = s;
+    }
+}
+
 // tau -> i omega is linear in chi(tau): chi(i w_m) = (beta/L) sum_{t<L} g_t e^{+2 pi i t k_m / L}
 // + sum_j a_j K[j][m], with a = C m and the moments m linear in the 18 end samples
 // (m1 = -(g_0 - g_L), m2/m3 from fit_derivatives). Its transpose maps the output
 // gradient y to: (beta/L) FFT_FORWARD(y placed at rows k_m)[t] for t < L, plus
-// the moment terms D^T C^T (K^H y) on the end samples.
+// the moment terms D^T C^T (K^H y) on the end samples. K^H y is summed by all
+// threads of the CTA while y is placed.
 __global__ void __launch_bounds__(256) tau_to_w_adjoint_kernel(TauWPlan p, VinvRows vr, const double2 *__restrict__ yg,
                                                                double2 *__restrict__ xg, long Ccols, int ic, int lg) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -525,27 +552,30 @@ __global__ void __launch_bounds__(256) tau_to_w_adjoint_kernel(TauWPlan p, VinvR
   const int *rev = p.fft.rev;
   double2 *b = p.fft.has_generic ? a + (size_t)L * ic : nullptr;
   double2 *ends = a + (size_t)(p.fft.has_generic ? 2 : 1) * L * ic;  // [18][ic]: rows 0..8 and L-8..L
+  double2 *red = ends + 18 * ic;                                      // [8][3][ic]
   const int tid = threadIdx.x, nthr = blockDim.x;
   const long col0 = blockIdx.x * (long)ic;
   const int ncol = (int)min((long)ic, Ccols - col0);
   for (int w = tid; w < L * ic; w += nthr) a[w] = make_double2(0.0, 0.0);
   __syncthreads();
+  double2 v[3] = {make_double2(0.0, 0.0), make_double2(0.0, 0.0), make_double2(0.0, 0.0)};
   for (int w = tid; w < nwt * ic; w += nthr) {
     const int c = w & (ic - 1), mi = w >> lg;
-    if (c < ncol) a[rev[(mi - (nw - 1) + L) % L] * ic + c] = yg[(long)mi * Ccols + col0 + c];
+    if (c < ncol) {
+      const double2 y = yg[(long)mi * Ccols + col0 + c];
+      a[rev[(mi - (nw - 1) + L) % L] * ic + c] = y;
+#pragma unroll
+      for (int j = 0; j < 3; ++j) v[j] = cfma(cconj(p.K[j * nwt + mi]), y, v[j]);
+    }
   }
+  column_sum3(v, red, ic);
   const double dtau = p.beta / (double)(p.n_tau - 1);
-  for (int c = tid; c < ic; c += nthr) {
+  if (tid < ic) {
+    const int c = tid;
     double2 e[18];
 #pragma unroll
     for (int q = 0; q < 18; ++q) e[q] = make_double2(0.0, 0.0);
     if (c < ncol) {
-      double2 v[3] = {make_double2(0.0, 0.0), make_double2(0.0, 0.0), make_double2(0.0, 0.0)};
-      for (int mi = 0; mi < nwt; ++mi) {
-        const double2 y = yg[(long)mi * Ccols + col0 + c];
-#pragma unroll
-        for (int j = 0; j < 3; ++j) v[j] = cfma(cconj(p.K[j * nwt + mi]), y, v[j]);
-      }
       // a1 = 4(m1 - m3)/3, a2 = m3 - (m1 + m2)/2, a3 = m1/6 + m2/2 + m3/3: transpose
       const double2 m1g = cadd(cadd(cscale(v[0], 4.0 / 3.0), cscale(v[1], -0.5)), cscale(v[2], 1.0 / 6.0));
       const double2 m2g = cadd(cscale(v[1], -0.5), cscale(v[2], 0.5));
@@ -569,7 +599,7 @@ __global__ void __launch_bounds__(256) tau_to_w_adjoint_kernel(TauWPlan p, VinvR
 #pragma unroll
     for (int q = 0; q < 18; ++q) ends[q * ic + c] = e[q];
   }
-  double2 *r = fft_smem<true>(a, b, p.fft, ic);
+  double2 *r = fft_smem<true>(a, b, p.fft, ic);  // its first barrier orders the ends writes
   const double fact = p.beta / (double)L;
   for (int w = tid; w < (L + 1) * ic; w += nthr) {
     const int c = w & (ic - 1), t = w >> lg;
@@ -584,7 +614,9 @@ __global__ void __launch_bounds__(256) tau_to_w_adjoint_kernel(TauWPlan p, VinvR
 // iv -> tau is linear in G(iv): G(tau_t) = P[t] F[t] + sum_j a_j Q[j][t] (t < L),
 // G[L] = -(G[0] + m1), F = FFT_FORWARD of g placed at rows (n+L)%L, a = Cf m,
 // m = Fit g[fit rows] (when fitted). Transpose: y_0 -= y_L; BACKWARD FFT of
-// conj(P) y at rows (n+L)%L; plus Fit^H Cf^T (Q^H y) on the fit rows.
+// conj(P) y at rows (n+L)%L; plus Fit^H Cf^T (Q^H y) on the fit rows. Q^H y is
+// summed by all threads of the CTA while y is placed; the fit terms are added
+// to the transformed rows in shared memory (each fit row once per column).
 __global__ void __launch_bounds__(256) nu_to_tau_adjoint_kernel(NuTauPlan p, const double2 *__restrict__ yg,
                                                                 double2 *__restrict__ gg, long Ccols, int ic, int lg,
                                                                 int fitted) {
@@ -594,45 +626,47 @@ __global__ void __launch_bounds__(256) nu_to_tau_adjoint_kernel(NuTauPlan p, con
   const int *rev = p.fft.rev;
   double2 *b = p.fft.has_generic ? a + (size_t)L * ic : nullptr;
   double2 *mg = a + (size_t)(p.fft.has_generic ? 2 : 1) * L * ic;  // [3][ic] moment gradients
+  double2 *red = mg + 3 * ic;                                       // [8][3][ic]
   const int tid = threadIdx.x, nthr = blockDim.x;
   const long col0 = blockIdx.x * (long)ic;
   const int ncol = (int)min((long)ic, Ccols - col0);
+  double2 v[3] = {make_double2(0.0, 0.0), make_double2(0.0, 0.0), make_double2(0.0, 0.0)};
   for (int w = tid; w < L * ic; w += nthr) {
     const int c = w & (ic - 1), t = w >> lg;
     double2 y = make_double2(0.0, 0.0);
     if (c < ncol) {
       y = yg[(long)t * Ccols + col0 + c];
       if (t == 0) y = csub(y, yg[(long)L * Ccols + col0 + c]);
+      if (fitted)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) v[j] = cfma(cconj(p.Q[j * L + t]), y, v[j]);
     }
     a[rev[t] * ic + c] = cmul(cconj(p.P[t]), y);
   }
-  for (int c = tid; c < ic; c += nthr) {
-    double2 v[3] = {make_double2(0.0, 0.0), make_double2(0.0, 0.0), make_double2(0.0, 0.0)};
-    double2 yL = make_double2(0.0, 0.0);
-    if (c < ncol && fitted) {
-      yL = yg[(long)L * Ccols + col0 + c];
-      for (int t = 0; t < L; ++t) {
-        double2 y = yg[(long)t * Ccols + col0 + c];
-        if (t == 0) y = csub(y, yL);
-#pragma unroll
-        for (int j = 0; j < 3; ++j) v[j] = cfma(cconj(p.Q[j * L + t]), y, v[j]);
-      }
-    }
+  column_sum3(v, red, ic);
+  if (tid < ic) {
+    const int c = tid;
+    const double2 yL = (c < ncol && fitted) ? yg[(long)L * Ccols + col0 + c] : make_double2(0.0, 0.0);
     // a1 = m1 - m3, a2 = (m2 + m3)/2, a3 = (m3 - m2)/2; G[L] adds -m1
     mg[0 * ic + c] = csub(v[0], yL);
     mg[1 * ic + c] = cscale(csub(v[1], v[2]), 0.5);
     mg[2 * ic + c] = cadd(cscale(v[0], -1.0), cscale(cadd(v[1], v[2]), 0.5));
   }
-  double2 *r = fft_smem<false>(a, b, p.fft, ic);
+  double2 *r = fft_smem<false>(a, b, p.fft, ic);  // its first barrier orders the mg writes
+  if (fitted) {
+    for (int w = tid; w < p.n_fit * ic; w += nthr) {
+      const int c = w & (ic - 1), i = w >> lg;
+      const int row = (p.fit_row[i] - n_iw + L) % L;
+      double2 s = r[row * ic + c];
+      for (int q = 1; q <= 3; ++q) s = cfma(cconj(p.fitF[q * p.n_fit + i]), mg[(q - 1) * ic + c], s);
+      r[row * ic + c] = s;
+    }
+    __syncthreads();
+  }
   for (int w = tid; w < nnu * ic; w += nthr) {
     const int c = w & (ic - 1), n = w >> lg;
     if (c >= ncol) continue;
-    double2 v = r[((n - n_iw + L) % L) * ic + c];
-    if (fitted)
-      for (int i = 0; i < p.n_fit; ++i)
-        if (p.fit_row[i] == n)
-          for (int q = 1; q <= 3; ++q) v = cfma(cconj(p.fitF[q * p.n_fit + i]), mg[(q - 1) * ic + c], v);
-    gg[(long)n * Ccols + col0 + c] = v;
+    gg[(long)n * Ccols + col0 + c] = r[((n - n_iw + L) % L) * ic + c];
   }
 }
 
@@ -893,7 +927,7 @@ int launch_tau_to_w_adjoint(double beta, int n_tau, int nw, long C, const double
   if ((st = get_tau_w_plan(beta, n_tau, nw, &p))) return st;
   int ic, lg;
   size_t smem;
-  if ((st = pick_ic(p->fft, 18 * sizeof(double2), &ic, &lg, &smem))) return st;
+  if ((st = pick_ic(p->fft, (18 + 24) * sizeof(double2), &ic, &lg, &smem))) return st;
   TPRF_CUDA(cudaFuncSetAttribute(tau_to_w_adjoint_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   tau_to_w_adjoint_kernel<<<(unsigned)((C + ic - 1) / ic), 256, smem, stream>>>(*p, make_vinv_rows(), yg, xg, C, ic,
                                                                                lg);
@@ -910,7 +944,7 @@ int launch_nu_to_tau_adjoint(double beta, int n_iw, int n_tau, long C, const dou
   if (st) return st;
   int ic, lg;
   size_t smem;
-  if ((st = pick_ic(p->fft, 3 * sizeof(double2), &ic, &lg, &smem))) return st;
+  if ((st = pick_ic(p->fft, (3 + 24) * sizeof(double2), &ic, &lg, &smem))) return st;
   TPRF_CUDA(cudaFuncSetAttribute(nu_to_tau_adjoint_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   nu_to_tau_adjoint_kernel<<<(unsigned)((C + ic - 1) / ic), 256, smem, stream>>>(*p, yg, gg, C, ic, lg,
                                                                                 fitted ? 1 : 0);

@@ -335,10 +335,202 @@ extern "C" int tprf_solve_rpa_PH_to_host(long n_points, int nb, const double *ch
   return finish_with_checks(s, "solve_rpa_PH_to_host");
 }
 
-// ---- adjoint (differentiable path): the warp-per-point kernel of rpa_warp.cu ----
+// ---- adjoint (differentiable path) ------------------------------------------------
+// nb = 1, 2: one thread per point (below); nb >= 3: the warp-per-point kernel of
+// rpa_warp.cu. With the grouped matrices X0 (chi0), X (chi), Y (the gradient
+// dL/d conj(chi)) and Ug, and A = I - X0 Ug (so X = A^-1 X0):
+//   Z = A^-H Y,  P = Z X^H,
+//   chi0_grad = Z (I + Ug X)^H = Z + P Ug^H,
+//   U_grad    = sum over points of X0^H P  (= X^H Y X^H).
 namespace tprf {
+namespace {
+
+template <int NB, int NT>
+__global__ void __launch_bounds__(NT) rpa_adjoint_point_kernel(long n_points, const double2 *chi0,
+                                                               const double2 *__restrict__ U, const double2 *chi,
+                                                               const double2 *chig, double2 *chi0g, double2 *Ug_out,
+                                                               unsigned *status) {
+  constexpr int N = NB * NB;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  // Layout: [N*N] grouped U, [N*N][NT] LU of A^H, [N*N][NT] U_grad partial sums
+  // (both [element][thread]: conflict-free), [N][NT] row permutations.
+  double2 *ug = reinterpret_cast<double2 *>(smem_raw);
+  double2 *A = ug + N * N;
+  double2 *acc = A + N * N * NT;
+  int *perm = reinterpret_cast<int *>(acc + N * N * NT) + threadIdx.x;
+  const int tid = threadIdx.x;
+  for (int e = tid; e < N * N; e += NT) ug[e] = U[(e / N) * N + colmap<NB>(e % N)];
+#pragma unroll
+  for (int e = 0; e < N * N; ++e) acc[e * NT + tid] = make_double2(0.0, 0.0);
+  __syncthreads();
+#define AE(i, k) A[((i) * N + (k)) * NT + tid]
+#define ACC(i, k) acc[((i) * N + (k)) * NT + tid]
+  bool singular = false;
+  for (long pt = blockIdx.x * (long)NT + tid; pt < n_points; pt += (long)gridDim.x * NT) {
+    const double2 *x0 = chi0 + pt * N * N, *x = chi + pt * N * N, *y = chig + pt * N * N;
+    // A^H[i][j] = delta_ij - sum_m conj(Ug[m][i]) conj(X0[j][m]), one row of X0 at a time
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+      double2 xr[N];
+#pragma unroll
+      for (int m = 0; m < N; ++m) xr[m] = x0[j * N + colmap<NB>(m)];
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        double2 s = make_double2(i == j ? 1.0 : 0.0, 0.0);
+#pragma unroll
+        for (int m = 0; m < N; ++m) s = cfms(cconj(ug[m * N + i]), cconj(xr[m]), s);
+        AE(i, j) = s;
+      }
+      perm[j * NT] = j;
+    }
+    // LU of A^H with partial pivoting
+#pragma unroll 1
+    for (int j = 0; j < N; ++j) {
+      int p = j;
+      double best = cabs2(AE(j, j));
+#pragma unroll
+      for (int i = 0; i < N; ++i)
+        if (i > j) {
+          const double v = cabs2(AE(i, j));
+          if (v > best) {
+            best = v;
+            p = i;
+          }
+        }
+      if (best == 0.0) singular = true;
+      if (p != j) {
+#pragma unroll
+        for (int k = 0; k < N; ++k) {
+          const double2 t = AE(j, k);
+          AE(j, k) = AE(p, k);
+          AE(p, k) = t;
+        }
+        const int t = perm[j * NT];
+        perm[j * NT] = perm[p * NT];
+        perm[p * NT] = t;
+      }
+      const double2 inv = crecip(AE(j, j));
+      AE(j, j) = inv;
+#pragma unroll
+      for (int i = 0; i < N; ++i)
+        if (i > j) {
+          const double2 f = cmul(AE(i, j), inv);
+          AE(i, j) = f;
+#pragma unroll
+          for (int k = 0; k < N; ++k)
+            if (k > j) AE(i, k) = cfms(f, AE(j, k), AE(i, k));
+        }
+    }
+    // Z = A^-H Y, column by column, in registers
+    double2 Z[N][N];
+#pragma unroll
+    for (int c = 0; c < N; ++c) {
+      const int cm = colmap<NB>(c);
+      double2 b[N];
+#pragma unroll
+      for (int r = 0; r < N; ++r) b[r] = y[perm[r * NT] * N + cm];
+#pragma unroll
+      for (int r = 1; r < N; ++r)
+#pragma unroll
+        for (int l = 0; l < r; ++l) b[r] = cfms(AE(r, l), b[l], b[r]);
+#pragma unroll
+      for (int rr = 0; rr < N; ++rr) {
+        const int r = N - 1 - rr;
+#pragma unroll
+        for (int l = r + 1; l < N; ++l) b[r] = cfms(AE(r, l), b[l], b[r]);
+        b[r] = cmul(b[r], AE(r, r));
+      }
+#pragma unroll
+      for (int r = 0; r < N; ++r) Z[r][c] = b[r];
+    }
+    // P = Z X^H, one row of X at a time
+    double2 P[N][N];
+#pragma unroll
+    for (int m = 0; m < N; ++m) {
+      double2 xr[N];
+#pragma unroll
+      for (int l = 0; l < N; ++l) xr[l] = cconj(x[m * N + colmap<NB>(l)]);
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        double2 s = make_double2(0.0, 0.0);
+#pragma unroll
+        for (int l = 0; l < N; ++l) s = cfma(Z[i][l], xr[l], s);
+        P[i][m] = s;
+      }
+    }
+    // chi0_grad = Z + P Ug^H
+    double2 *g = chi0g + pt * N * N;
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+#pragma unroll
+      for (int j = 0; j < N; ++j) {
+        double2 s = Z[i][j];
+#pragma unroll
+        for (int m = 0; m < N; ++m) s = cfma(P[i][m], cconj(ug[j * N + m]), s);
+        g[i * N + colmap<NB>(j)] = s;
+      }
+    // U_grad += X0^H P, one column of X0 at a time
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      double2 xc[N];
+#pragma unroll
+      for (int l = 0; l < N; ++l) xc[l] = cconj(x0[l * N + colmap<NB>(i)]);
+#pragma unroll
+      for (int j = 0; j < N; ++j) {
+        double2 s = ACC(i, j);
+#pragma unroll
+        for (int l = 0; l < N; ++l) s = cfma(xc[l], P[l][j], s);
+        ACC(i, j) = s;
+      }
+    }
+  }
+#undef AE
+#undef ACC
+  if (singular) atomicOr(status, kDevErrSingular);
+  __syncthreads();
+  // CTA sum of the partials, one atomic per entry: grouped (m, c) -> offset m * N + colmap(c)
+  for (int e = tid; e < N * N; e += NT) {
+    double2 s = make_double2(0.0, 0.0);
+    for (int t = 0; t < NT; ++t) s = cadd(s, acc[e * NT + t]);
+    const int off = (e / N) * N + colmap<NB>(e % N);
+    atomicAdd(&reinterpret_cast<double *>(Ug_out)[2 * off], s.x);
+    atomicAdd(&reinterpret_cast<double *>(Ug_out)[2 * off + 1], s.y);
+  }
+}
+
+template <int NB>
+int launch_rpa_adjoint_point(long n_points, const double2 *chi0, const double2 *U, const double2 *chi,
+                             const double2 *chig, double2 *chi0g, double2 *Ug, cudaStream_t stream, unsigned *status) {
+  constexpr int N = NB * NB, NT = 128;
+  const size_t smem = (size_t)N * N * 16 * (1 + 2 * NT) + (size_t)N * NT * sizeof(int);
+  auto kern = rpa_adjoint_point_kernel<NB, NT>;
+  TPRF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0;
+  TPRF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, smem));
+  long blocks = (n_points + NT - 1) / NT;
+  blocks = std::max(1L, std::min(blocks, (long)num_sms() * std::max(1, per_sm)));
+  kern<<<(unsigned)blocks, NT, smem, stream>>>(n_points, chi0, U, chi, chig, chi0g, Ug, status);
+  TPRF_LAUNCH_CHECK("rpa_adjoint_point_kernel");
+  return TPRF_OK;
+}
+
+}  // namespace
+
 int launch_rpa_adjoint_warp(long n_points, int nb, const double2 *chi0, const double2 *U, const double2 *chi,
                             const double2 *chig, double2 *chi0g, double2 *Ug, cudaStream_t stream, unsigned *status);
+
+// The RPA adjoint by vertex size (U_grad is accumulated: the caller zeroes it).
+int launch_rpa_adjoint(long n_points, int nb, const double2 *chi0, const double2 *U, const double2 *chi,
+                       const double2 *chig, double2 *chi0g, double2 *Ug, cudaStream_t stream, unsigned *status) {
+  switch (nb) {
+    case 1: return launch_rpa_adjoint_point<1>(n_points, chi0, U, chi, chig, chi0g, Ug, stream, status);
+    case 2: return launch_rpa_adjoint_point<2>(n_points, chi0, U, chi, chig, chi0g, Ug, stream, status);
+    default:
+      if (nb < 1 || nb > 8) return set_error(TPRF_ERR_INVALID_ARGUMENT, "solve_rpa_PH_adjoint: nb must be 1..8");
+      return launch_rpa_adjoint_warp(n_points, nb, chi0, U, chi, chig, chi0g, Ug, stream, status);
+  }
+}
+
 }  // namespace tprf
 
 extern "C" int tprf_solve_rpa_PH_adjoint(long n_points, int nb, const double *chi0, const double *U, const double *chi,
@@ -351,8 +543,7 @@ extern "C" int tprf_solve_rpa_PH_adjoint(long n_points, int nb, const double *ch
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   auto c = [](const double *p) { return reinterpret_cast<const double2 *>(p); };
   double2 *g0 = reinterpret_cast<double2 *>(chi0_grad), *ug = reinterpret_cast<double2 *>(U_grad);
-  if (nb < 1 || nb > 8) return set_error(TPRF_ERR_INVALID_ARGUMENT, "solve_rpa_PH_adjoint: nb must be 1..8");
-  const int st = launch_rpa_adjoint_warp(n_points, nb, c(chi0), c(U), c(chi), c(chi_grad), g0, ug, s, status);
+  const int st = launch_rpa_adjoint(n_points, nb, c(chi0), c(U), c(chi), c(chi_grad), g0, ug, s, status);
   if (st) return st;
   return finish_with_checks(s, "solve_rpa_PH_adjoint");
 }
