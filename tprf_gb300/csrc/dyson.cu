@@ -177,53 +177,66 @@ extern "C" int tprf_lattice_dyson_g_wk(double beta, int n_iw, long n_k, int nb, 
 // ---- adjoint (differentiable path) ----------------------------------------------
 // G = [(iv + mu) I - e(k)]^-1 gives dG = G de G, so for a real loss with gradient
 // Gg = dL/dG (conjugate Wirtinger convention, as torch uses) the gradient of e(k)
-// is sum_v G^H Gg G^H. One thread per k sums over the frequencies.
+// is sum_v G^H Gg G^H. A CTA takes 32 consecutive k (one per lane) and a slice
+// of the frequencies (every warp of the grid's slices a different frequency,
+// so a warp's loads are 32 consecutive k of one frequency); the partial sums
+// meet in e_grad through FP64 atomics (the launcher zeroes it first).
 
 namespace tprf {
 namespace {
 
 template <int NB>
-__global__ void __launch_bounds__(128) dyson_adjoint_kernel(int n_nu, long n_k, const double2 *__restrict__ g,
+__global__ void __launch_bounds__(256) dyson_adjoint_kernel(int n_nu, long n_k, const double2 *__restrict__ g,
                                                             const double2 *__restrict__ gg, double2 *__restrict__ ekg) {
-  for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n_k; k += (long)gridDim.x * blockDim.x) {
-    double2 acc[NB][NB];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, n_warps = blockDim.x >> 5;
+  const long k = blockIdx.x * 32L + lane;
+  if (k >= n_k) return;
+  const int stride = gridDim.y * n_warps;
+  double2 acc[NB][NB];
+#pragma unroll
+  for (int i = 0; i < NB; ++i)
+#pragma unroll
+    for (int j = 0; j < NB; ++j) acc[i][j] = make_double2(0.0, 0.0);
+  for (int n = blockIdx.y * n_warps + warp; n < n_nu; n += stride) {
+    const double2 *G = g + ((long)n * n_k + k) * NB * NB;
+    const double2 *Y = gg + ((long)n * n_k + k) * NB * NB;
+    // T = Gg G^H, then acc += G^H T
+    double2 T[NB][NB];
 #pragma unroll
     for (int i = 0; i < NB; ++i)
 #pragma unroll
-      for (int j = 0; j < NB; ++j) acc[i][j] = make_double2(0.0, 0.0);
-    for (int n = 0; n < n_nu; ++n) {
-      const double2 *G = g + ((long)n * n_k + k) * NB * NB;
-      const double2 *Y = gg + ((long)n * n_k + k) * NB * NB;
-      // T = Gg G^H, then acc += G^H T
-      double2 T[NB][NB];
+      for (int j = 0; j < NB; ++j) {
+        double2 s = make_double2(0.0, 0.0);
 #pragma unroll
-      for (int i = 0; i < NB; ++i)
-#pragma unroll
-        for (int j = 0; j < NB; ++j) {
-          double2 s = make_double2(0.0, 0.0);
-#pragma unroll
-          for (int l = 0; l < NB; ++l) s = cfma(Y[i * NB + l], cconj(G[j * NB + l]), s);
-          T[i][j] = s;
-        }
-#pragma unroll
-      for (int i = 0; i < NB; ++i)
-#pragma unroll
-        for (int j = 0; j < NB; ++j)
-#pragma unroll
-          for (int l = 0; l < NB; ++l) acc[i][j] = cfma(cconj(G[l * NB + i]), T[l][j], acc[i][j]);
-    }
+        for (int l = 0; l < NB; ++l) s = cfma(Y[i * NB + l], cconj(G[j * NB + l]), s);
+        T[i][j] = s;
+      }
 #pragma unroll
     for (int i = 0; i < NB; ++i)
 #pragma unroll
-      for (int j = 0; j < NB; ++j) ekg[k * NB * NB + i * NB + j] = acc[i][j];
+      for (int j = 0; j < NB; ++j)
+#pragma unroll
+        for (int l = 0; l < NB; ++l) acc[i][j] = cfma(cconj(G[l * NB + i]), T[l][j], acc[i][j]);
   }
+  double *out = reinterpret_cast<double *>(ekg + k * NB * NB);
+#pragma unroll
+  for (int i = 0; i < NB; ++i)
+#pragma unroll
+    for (int j = 0; j < NB; ++j) {
+      atomicAdd(out + 2 * (i * NB + j), acc[i][j].x);
+      atomicAdd(out + 2 * (i * NB + j) + 1, acc[i][j].y);
+    }
 }
 
 template <int NB>
 int launch_dyson_adjoint_nb(int n_nu, long n_k, const double2 *g, const double2 *gg, double2 *ekg, cudaStream_t s) {
-  long blocks = (n_k + 127) / 128;
-  blocks = std::max(1L, std::min(blocks, (long)num_sms() * 16));
-  dyson_adjoint_kernel<NB><<<(unsigned)blocks, 128, 0, s>>>(n_nu, n_k, g, gg, ekg);
+  TPRF_CUDA(cudaMemsetAsync(ekg, 0, (size_t)n_k * NB * NB * sizeof(double2), s));
+  const long k_tiles = (n_k + 31) / 32;
+  constexpr int kWarps = 8;
+  const long target = (long)num_sms() * 8;  // CTAs for a full GPU
+  const long slices = std::max(1L, std::min((long)((n_nu + kWarps - 1) / kWarps), (target + k_tiles - 1) / k_tiles));
+  if (k_tiles > 0x7fffffffL) return set_error(TPRF_ERR_UNSUPPORTED_SIZE, "lattice_dyson_g_wk_adjoint: too many k");
+  dyson_adjoint_kernel<NB><<<dim3((unsigned)k_tiles, (unsigned)slices), 32 * kWarps, 0, s>>>(n_nu, n_k, g, gg, ekg);
   TPRF_LAUNCH_CHECK("dyson_adjoint_kernel");
   return TPRF_OK;
 }

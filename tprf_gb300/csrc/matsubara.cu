@@ -510,7 +510,9 @@ int check_bubble(int n_tau, const int dims[3], int nb, const void *g, const void
 }
 
 // ---------------------------------------------------------------------------
-// Adjoints (transposed linear maps) for the differentiable path, in FP64.
+// Adjoints (transposed linear maps) for the differentiable path: tail terms
+// and sums in FP64, the FFT butterflies in double-float (FP64 in the FP64
+// arithmetic mode), as in the forward transforms.
 
 // Sum over the threads of a CTA that share a column (c = tid & (ic - 1),
 // ic a power of two <= 32) of three complex partials: shuffles inside a warp
@@ -544,26 +546,27 @@ __device__ __forceinline__ void column_sum3(double2 v[3], double2 *red, int ic) 
 // gradient y to: (beta/L) FFT_FORWARD(y placed at rows k_m)[t] for t < L, plus
 // the moment terms D^T C^T (K^H y) on the end samples. K^H y is summed by all
 // threads of the CTA while y is placed.
+template <class C>
 __global__ void __launch_bounds__(256) tau_to_w_adjoint_kernel(TauWPlan p, VinvRows vr, const double2 *__restrict__ yg,
                                                                double2 *__restrict__ xg, long Ccols, int ic, int lg) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  double2 *a = reinterpret_cast<double2 *>(smem_raw);
+  C *a = reinterpret_cast<C *>(smem_raw);
   const int L = p.L, nw = p.nw, nwt = 2 * p.nw - 1;
   const int *rev = p.fft.rev;
-  double2 *b = p.fft.has_generic ? a + (size_t)L * ic : nullptr;
-  double2 *ends = a + (size_t)(p.fft.has_generic ? 2 : 1) * L * ic;  // [18][ic]: rows 0..8 and L-8..L
+  C *b = p.fft.has_generic ? a + (size_t)L * ic : nullptr;
+  double2 *ends = reinterpret_cast<double2 *>(a + (size_t)(p.fft.has_generic ? 2 : 1) * L * ic);  // [18][ic]
   double2 *red = ends + 18 * ic;                                      // [8][3][ic]
   const int tid = threadIdx.x, nthr = blockDim.x;
   const long col0 = blockIdx.x * (long)ic;
   const int ncol = (int)min((long)ic, Ccols - col0);
-  for (int w = tid; w < L * ic; w += nthr) a[w] = make_double2(0.0, 0.0);
+  for (int w = tid; w < L * ic; w += nthr) a[w] = from_d2<C>(make_double2(0.0, 0.0));
   __syncthreads();
   double2 v[3] = {make_double2(0.0, 0.0), make_double2(0.0, 0.0), make_double2(0.0, 0.0)};
   for (int w = tid; w < nwt * ic; w += nthr) {
     const int c = w & (ic - 1), mi = w >> lg;
     if (c < ncol) {
       const double2 y = yg[(long)mi * Ccols + col0 + c];
-      a[rev[(mi - (nw - 1) + L) % L] * ic + c] = y;
+      a[rev[(mi - (nw - 1) + L) % L] * ic + c] = from_d2<C>(y);
 #pragma unroll
       for (int j = 0; j < 3; ++j) v[j] = cfma(cconj(p.K[j * nwt + mi]), y, v[j]);
     }
@@ -599,12 +602,12 @@ __global__ void __launch_bounds__(256) tau_to_w_adjoint_kernel(TauWPlan p, VinvR
 #pragma unroll
     for (int q = 0; q < 18; ++q) ends[q * ic + c] = e[q];
   }
-  double2 *r = fft_smem<true>(a, b, p.fft, ic);  // its first barrier orders the ends writes
+  C *r = fft_smem<true>(a, b, p.fft, ic);  // its first barrier orders the ends writes
   const double fact = p.beta / (double)L;
   for (int w = tid; w < (L + 1) * ic; w += nthr) {
     const int c = w & (ic - 1), t = w >> lg;
     if (c >= ncol) continue;
-    double2 v = (t < L) ? cscale(r[t * ic + c], fact) : make_double2(0.0, 0.0);
+    double2 v = (t < L) ? cscale(as_d2(r[t * ic + c]), fact) : make_double2(0.0, 0.0);
     if (t <= 8) v = cadd(v, ends[t * ic + c]);
     if (t >= L - 8) v = cadd(v, ends[(9 + t - (L - 8)) * ic + c]);
     xg[(long)t * Ccols + col0 + c] = v;
@@ -617,15 +620,16 @@ __global__ void __launch_bounds__(256) tau_to_w_adjoint_kernel(TauWPlan p, VinvR
 // conj(P) y at rows (n+L)%L; plus Fit^H Cf^T (Q^H y) on the fit rows. Q^H y is
 // summed by all threads of the CTA while y is placed; the fit terms are added
 // to the transformed rows in shared memory (each fit row once per column).
+template <class C>
 __global__ void __launch_bounds__(256) nu_to_tau_adjoint_kernel(NuTauPlan p, const double2 *__restrict__ yg,
                                                                 double2 *__restrict__ gg, long Ccols, int ic, int lg,
                                                                 int fitted) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  double2 *a = reinterpret_cast<double2 *>(smem_raw);
+  C *a = reinterpret_cast<C *>(smem_raw);
   const int L = p.L, n_iw = p.n_iw, nnu = 2 * p.n_iw;
   const int *rev = p.fft.rev;
-  double2 *b = p.fft.has_generic ? a + (size_t)L * ic : nullptr;
-  double2 *mg = a + (size_t)(p.fft.has_generic ? 2 : 1) * L * ic;  // [3][ic] moment gradients
+  C *b = p.fft.has_generic ? a + (size_t)L * ic : nullptr;
+  double2 *mg = reinterpret_cast<double2 *>(a + (size_t)(p.fft.has_generic ? 2 : 1) * L * ic);  // [3][ic]
   double2 *red = mg + 3 * ic;                                       // [8][3][ic]
   const int tid = threadIdx.x, nthr = blockDim.x;
   const long col0 = blockIdx.x * (long)ic;
@@ -641,7 +645,7 @@ __global__ void __launch_bounds__(256) nu_to_tau_adjoint_kernel(NuTauPlan p, con
 #pragma unroll
         for (int j = 0; j < 3; ++j) v[j] = cfma(cconj(p.Q[j * L + t]), y, v[j]);
     }
-    a[rev[t] * ic + c] = cmul(cconj(p.P[t]), y);
+    a[rev[t] * ic + c] = from_d2<C>(cmul(cconj(p.P[t]), y));
   }
   column_sum3(v, red, ic);
   if (tid < ic) {
@@ -652,21 +656,21 @@ __global__ void __launch_bounds__(256) nu_to_tau_adjoint_kernel(NuTauPlan p, con
     mg[1 * ic + c] = cscale(csub(v[1], v[2]), 0.5);
     mg[2 * ic + c] = cadd(cscale(v[0], -1.0), cscale(cadd(v[1], v[2]), 0.5));
   }
-  double2 *r = fft_smem<false>(a, b, p.fft, ic);  // its first barrier orders the mg writes
+  C *r = fft_smem<false>(a, b, p.fft, ic);  // its first barrier orders the mg writes
   if (fitted) {
     for (int w = tid; w < p.n_fit * ic; w += nthr) {
       const int c = w & (ic - 1), i = w >> lg;
       const int row = (p.fit_row[i] - n_iw + L) % L;
-      double2 s = r[row * ic + c];
+      double2 s = as_d2(r[row * ic + c]);
       for (int q = 1; q <= 3; ++q) s = cfma(cconj(p.fitF[q * p.n_fit + i]), mg[(q - 1) * ic + c], s);
-      r[row * ic + c] = s;
+      r[row * ic + c] = from_d2<C>(s);
     }
     __syncthreads();
   }
   for (int w = tid; w < nnu * ic; w += nthr) {
     const int c = w & (ic - 1), n = w >> lg;
     if (c >= ncol) continue;
-    gg[(long)n * Ccols + col0 + c] = r[((n - n_iw + L) % L) * ic + c];
+    gg[(long)n * Ccols + col0 + c] = as_d2(r[((n - n_iw + L) % L) * ic + c]);
   }
 }
 
@@ -928,9 +932,10 @@ int launch_tau_to_w_adjoint(double beta, int n_tau, int nw, long C, const double
   int ic, lg;
   size_t smem;
   if ((st = pick_ic(p->fft, (18 + 24) * sizeof(double2), &ic, &lg, &smem))) return st;
-  TPRF_CUDA(cudaFuncSetAttribute(tau_to_w_adjoint_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  tau_to_w_adjoint_kernel<<<(unsigned)((C + ic - 1) / ic), 256, smem, stream>>>(*p, make_vinv_rows(), yg, xg, C, ic,
-                                                                               lg);
+  // double-float butterflies unless the FP64 arithmetic mode is set
+  auto kern = arith_mode() == kArithFP64 ? tau_to_w_adjoint_kernel<double2> : tau_to_w_adjoint_kernel<cdf>;
+  TPRF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  kern<<<(unsigned)((C + ic - 1) / ic), 256, smem, stream>>>(*p, make_vinv_rows(), yg, xg, C, ic, lg);
   TPRF_LAUNCH_CHECK("tau_to_w_adjoint_kernel");
   return TPRF_OK;
 }
@@ -945,9 +950,9 @@ int launch_nu_to_tau_adjoint(double beta, int n_iw, int n_tau, long C, const dou
   int ic, lg;
   size_t smem;
   if ((st = pick_ic(p->fft, (3 + 24) * sizeof(double2), &ic, &lg, &smem))) return st;
-  TPRF_CUDA(cudaFuncSetAttribute(nu_to_tau_adjoint_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  nu_to_tau_adjoint_kernel<<<(unsigned)((C + ic - 1) / ic), 256, smem, stream>>>(*p, yg, gg, C, ic, lg,
-                                                                                fitted ? 1 : 0);
+  auto kern = arith_mode() == kArithFP64 ? nu_to_tau_adjoint_kernel<double2> : nu_to_tau_adjoint_kernel<cdf>;
+  TPRF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  kern<<<(unsigned)((C + ic - 1) / ic), 256, smem, stream>>>(*p, yg, gg, C, ic, lg, fitted ? 1 : 0);
   TPRF_LAUNCH_CHECK("nu_to_tau_adjoint_kernel");
   return TPRF_OK;
 }
