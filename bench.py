@@ -228,6 +228,17 @@ def cpu_throughput(cfg_key, procs: int, scale=1.0, pool=None):
 # ---------------------------------------------------------------------------
 # GPU arm
 
+def setup_autotune(lib, args):
+    """Measure mode of the library's autotuner unless --no-autotune: the first
+    (warm-up) call of each shape times the candidate launch shapes."""
+    lib.tprf_set_autotune(0 if args.no_autotune else 1)
+
+
+def autotune_info(lib, args):
+    return {"mode": "fixed heuristics" if args.no_autotune else "measure (tuned during warm-up)",
+            "wisdom_entries": int(lib.tprf_autotune_entries())}
+
+
 def lattice_passes(dims) -> int:
     """Kernel launches of one lattice FFT over `dims`: the two fastest non-trivial axes
     share one pass when both are powers of two (at most 256, plane at most 4096 points),
@@ -257,6 +268,7 @@ def run_gpu(args):
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=dev)
     lib = _native.lib()
+    setup_autotune(lib, args)
     cfg = workloads.config(args.config)
     dims, beta, mu, n_max, nw = cfg["dims"], cfg["beta"], cfg["mu"], cfg["n_max"], cfg["nw"]
     nk = int(math.prod(dims))
@@ -401,6 +413,7 @@ def run_gpu(args):
         "gpu_launches": launches_per_step * args.steps,
         "roofline": roofline,
         "clocks": clocks.summary(),
+        "autotune": autotune_info(lib, args),
     }
     if rank == 0 and not args.no_cpu_baseline:
         v, cores, wall = cpu_throughput(args.config, 1, scale=40)
@@ -434,6 +447,7 @@ def run_gpu_batched(args):
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=dev)
     lib = _native.lib()
+    setup_autotune(lib, args)
     specs = workloads.batched_instances(512, seed=0)
     insts = [RPAInstance(e_k=ek_tensor(d["hoppings"], d["dims"], device=dev), U=d["U"], dims=d["dims"],
                          beta=d["beta"], mu=d["mu"], n_max=d["n_max"], nw=d["nw"]) for d in specs]
@@ -486,6 +500,7 @@ def run_gpu_batched(args):
         "speedup_vs_plain_single_instance": value / plain,
         "gpu_launches": None,
         "clocks": clocks.summary(),
+        "autotune": autotune_info(lib, args),
     }
     batch.close()
     if world > 1:
@@ -516,6 +531,7 @@ def run_gpu_batched_grad(args):
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=dev)
     lib = _native.lib()
+    setup_autotune(lib, args)
     specs = workloads.batched_instances(512, seed=0)
     insts = [RPAInstance(e_k=ek_tensor(d["hoppings"], d["dims"], device=dev), U=d["U"], dims=d["dims"],
                          beta=d["beta"], mu=d["mu"], n_max=d["n_max"], nw=d["nw"]) for d in specs]
@@ -593,6 +609,7 @@ def run_gpu_batched_grad(args):
         "speedup_vs_plain_single_instance": value / plain,
         "gpu_launches": None,
         "clocks": clocks.summary(),
+        "autotune": autotune_info(lib, args),
     }
     batch.close()
     if world > 1:
@@ -620,6 +637,7 @@ def run_gpu_grad(args):
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=dev)
     lib = _native.lib()
+    setup_autotune(lib, args)
     lib.tprf_set_sync_checks(0)
     model, theta0, U0 = cfg3_model()
     nk = int(math.prod(model.dims))
@@ -676,6 +694,7 @@ def run_gpu_grad(args):
                 "d2h_bytes_per_step": int(grads_h.numel() * 8 + 8)},
         "gpu_launches": None,
         "clocks": clocks.summary(),
+        "autotune": autotune_info(lib, args),
     }
     if world > 1:
         import torch.distributed as dist
@@ -755,6 +774,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     ap.add_argument("--streams", type=int, default=32, help="concurrent streams of the batched graph (cfg2)")
     ap.add_argument("--grad", action="store_true", help="cfg2: forward + gradient graphs per step")
+    ap.add_argument("--no-autotune", action="store_true", help="fixed launch-shape heuristics instead of measure mode")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

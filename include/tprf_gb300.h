@@ -72,6 +72,24 @@ int tprf_check_device_status(void *stream);
 int tprf_set_arithmetic(int mode);
 int tprf_get_arithmetic(void);
 
+/* Autotuner of launch shapes. The reference plans its FFTs with FFTW_ESTIMATE
+ * (c++/triqs_tprf/fourier/fourier_common.cpp:32-43): a fixed heuristic. Mode 0
+ * (default) uses fixed heuristics here too; mode 1 ("measure", as FFTW_MEASURE)
+ * times every candidate on the first call of each shape and keeps the fastest:
+ * columns per CTA of the iv -> tau and tau -> i omega kernels (fused bubble
+ * included), lanes per point of the RPA group kernel (nb >= 3). Candidates run
+ * on a prefix of the call's own columns or points (out-of-place kernels only),
+ * so results do not depend on the mode. A tuning call waits for its stream;
+ * tuning is skipped while the stream is being captured. The choices ("wisdom")
+ * are process-wide, keyed by GPU, arithmetic mode, kernel and shape, and can be
+ * saved to and loaded from a text file ("key value" per line). */
+int tprf_set_autotune(int mode);
+int tprf_get_autotune(void);
+int tprf_autotune_entries(void);
+void tprf_autotune_clear(void);
+int tprf_autotune_save(const char *path);
+int tprf_autotune_load(const char *path);
+
 /* Device capability: sustained FP64 FMA throughput (TFLOP/s) of the current
  * GPU, best of three timed runs of a fixed-length FMA loop; synchronises
  * `stream`. The path's kernels are bound by this pipe on GB300, so the

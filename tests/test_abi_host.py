@@ -118,3 +118,31 @@ def test_meshes():
     assert k.dims == (4, 2, 1) and len(k) == 8
     np.testing.assert_allclose(k.values(), O.kpoints((4, 2, 1)))
     assert len(MeshProduct(wf, k)) == 128 * 8
+
+
+def test_autotune_wisdom_file_round_trip(lib, tmp_path):
+    """Wisdom files (host-only): load, count, save, reload; malformed files are refused."""
+    from tprf_gb300 import tuning
+    from tprf_gb300._native import TprfError
+    tuning.clear_wisdom()
+    src = tmp_path / "w.txt"
+    src.write_text("# comment\nsm103x152/tau_to_w/0/1536/256/0/13 4\nsm103x152/rpa_group/0/3 8\n")
+    tuning.load_wisdom(src)
+    assert tuning.wisdom_entries() == 2
+    out = tmp_path / "out.txt"
+    tuning.save_wisdom(out)
+    lines = [ln for ln in out.read_text().splitlines() if not ln.startswith("#")]
+    assert sorted(lines) == ["sm103x152/rpa_group/0/3 8", "sm103x152/tau_to_w/0/1536/256/0/13 4"]
+    tuning.clear_wisdom()
+    assert tuning.wisdom_entries() == 0
+    tuning.load_wisdom(out)
+    assert tuning.wisdom_entries() == 2
+    bad = tmp_path / "bad.txt"
+    bad.write_text("only_a_key\n")
+    with pytest.raises(TprfError, match="malformed line 1"):
+        tuning.load_wisdom(bad)
+    with pytest.raises(TprfError, match="cannot read"):
+        tuning.load_wisdom(tmp_path / "missing.txt")
+    assert lib.tprf_set_autotune(2) != 0
+    assert not tuning.autotune_enabled()
+    tuning.clear_wisdom()

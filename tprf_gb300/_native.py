@@ -86,6 +86,12 @@ SIGNATURES = {
     "tprf_batch_run": (c_int, [c_void_p, c_void_p]),
     "tprf_batch_size": (c_int, [c_void_p]),
     "tprf_batch_destroy": (c_int, [c_void_p]),
+    "tprf_set_autotune": (c_int, [c_int]),
+    "tprf_get_autotune": (c_int, []),
+    "tprf_autotune_entries": (c_int, []),
+    "tprf_autotune_clear": (None, []),
+    "tprf_autotune_save": (c_int, [ctypes.c_char_p]),
+    "tprf_autotune_load": (c_int, [ctypes.c_char_p]),
     "tprf_batch_grad_workspace_bytes": (c_size_t, [ctypes.POINTER(GradInstance), c_int, c_int]),
     "tprf_batch_grad_create": (c_int, [ctypes.POINTER(GradInstance), c_int, c_int, c_void_p, c_size_t,
                                        ctypes.POINTER(c_void_p)]),

@@ -3,7 +3,10 @@
 
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <functional>
+#include <initializer_list>
 #include <string>
+#include <vector>
 
 #include "../../include/tprf_gb300.h"
 
@@ -137,5 +140,14 @@ int launch_dyson_adjoint(int n_iw, long n_k, int nb, const double2 *g, const dou
                          cudaStream_t stream);
 int launch_rpa_adjoint(long n_points, int nb, const double2 *chi0, const double2 *U, const double2 *chi,
                        const double2 *chig, double2 *chi0g, double2 *Ug, cudaStream_t stream, unsigned *status);
+
+// Autotuner (tune.cu): the wisdom value of `key` if one is recorded and is
+// among the candidates; else, in measure mode and outside a stream capture,
+// times launch(v) for every candidate on `s` and records the fastest; else the
+// fallback.
+int tune_mode();
+std::string tune_key(const char *kernel, std::initializer_list<long> shape);
+int tune_pick(const std::string &key, const std::vector<int> &candidates, int fallback, cudaStream_t s,
+              const std::function<int(int)> &launch, int *choice);
 
 }  // namespace tprf

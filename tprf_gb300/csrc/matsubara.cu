@@ -26,6 +26,7 @@
 // arithmetic run in double-float pairs on the FP32 pipe by default
 // (tprf_set_arithmetic), with inputs and outputs in complex128.
 #include <algorithm>
+#include <vector>
 
 #include <type_traits>
 
@@ -433,38 +434,77 @@ int pick_ic(const FftDesc &fft, size_t extra_per_col, int *ic_out, int *lg_out, 
   return TPRF_OK;
 }
 
+// Every power-of-two column count up to 32 whose tile fits one CTA (the
+// autotuner's candidates; pick_ic gives the heuristic one), and the shared
+// memory of a tile.
+size_t ic_smem(const FftDesc &fft, size_t extra_per_col, int ic) {
+  return (fft.has_generic ? 2 : 1) * (size_t)fft.n * ic * sizeof(double2) + extra_per_col * ic;
+}
+std::vector<int> ic_candidates(const FftDesc &fft, size_t extra_per_col) {
+  const size_t full = (size_t)std::min(max_smem_optin(), 220 * 1024);
+  std::vector<int> out;
+  for (int ic = 1; ic <= 32; ic *= 2)
+    if (ic_smem(fft, extra_per_col, ic) <= full) out.push_back(ic);
+  return out;
+}
+int log2_ic(int ic) {
+  int lg = 0;
+  while ((1 << lg) < ic) ++lg;
+  return lg;
+}
+// Columns timed per candidate: enough CTAs to fill the GPU several times.
+long tune_columns(long C) { return std::min(C, (long)num_sms() * 8 * 32); }
+
 long grid_for(long work, int threads) {
   long blocks = (work + threads - 1) / threads;
   const long cap = (long)num_sms() * 32;
   return std::max(1L, std::min(blocks, cap));
 }
 
+// Tuning reruns a prefix of the columns, so it needs the input apart from the output.
+bool aliases(const ArrayLoader &l, const double2 *out) { return (const void *)l.x == (const void *)out; }
+bool aliases(const BubbleLoader &l, const double2 *out) { return (const void *)l.g == (const void *)out; }
+int tune_tag(const ArrayLoader &) { return 0; }
+int tune_tag(const BubbleLoader &l) { return 10 + l.nb; }
+int tune_tag(const BubbleLoaderDF &l) { return 20 + l.nb; }
+
 template <class Loader, class E>
 int launch_tau_to_w_as(const TauWPlan *p, Loader ld, double2 *out, long C, cudaStream_t stream) {
+  const size_t extra = 5 * sizeof(double2) + 2 * sizeof(long) + 18 * sizeof(double2);
   int ic, lg;
   size_t smem;
-  int st = pick_ic(p->fft, 5 * sizeof(double2) + 2 * sizeof(long) + 18 * sizeof(double2), &ic, &lg, &smem);
+  int st = pick_ic(p->fft, extra, &ic, &lg, &smem);
   if (st) return st;
-  const long blocks = (C + ic - 1) / ic;
-  if constexpr (std::is_same<Loader, ArrayLoader>::value) {
-    if (p->fermion) {
-      TPRF_CUDA(cudaFuncSetAttribute(tau_to_w_kernel<Loader, E, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)smem));
-      tau_to_w_kernel<Loader, E, true><<<(unsigned)blocks, kMatsubaraThreads, smem, stream>>>(*p, ld,
-                                                                                             make_fit_rows(p->beta, p->n_tau),
-                                                                                             out, C, ic, lg);
-      TPRF_LAUNCH_CHECK("tau_to_w_kernel");
-      return TPRF_OK;
+  if (p->fermion && !std::is_same<Loader, ArrayLoader>::value)
+    return set_error(TPRF_ERR_INVALID_ARGUMENT, "tau -> w: fermionic transform of a bubble");
+  const FitRows fr = make_fit_rows(p->beta, p->n_tau);
+  // columns [0, n_cols) of the C columns with icv columns per CTA
+  auto launch = [&](int icv, long n_cols) -> int {
+    const size_t sm = ic_smem(p->fft, extra, icv);
+    const long blocks = (n_cols + icv - 1) / icv;
+    if constexpr (std::is_same<Loader, ArrayLoader>::value) {
+      if (p->fermion) {
+        TPRF_CUDA(cudaFuncSetAttribute(tau_to_w_kernel<Loader, E, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)sm));
+        tau_to_w_kernel<Loader, E, true><<<(unsigned)blocks, kMatsubaraThreads, sm, stream>>>(*p, ld, fr, out, C, icv,
+                                                                                              log2_ic(icv));
+        TPRF_LAUNCH_CHECK("tau_to_w_kernel");
+        return TPRF_OK;
+      }
     }
-  }
-  if (p->fermion) return set_error(TPRF_ERR_INVALID_ARGUMENT, "tau -> w: fermionic transform of a bubble");
-  TPRF_CUDA(cudaFuncSetAttribute(tau_to_w_kernel<Loader, E, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem));
-  tau_to_w_kernel<Loader, E, false><<<(unsigned)blocks, kMatsubaraThreads, smem, stream>>>(*p, ld,
-                                                                                          make_fit_rows(p->beta, p->n_tau), out,
-                                                                                          C, ic, lg);
-  TPRF_LAUNCH_CHECK("tau_to_w_kernel");
-  return TPRF_OK;
+    TPRF_CUDA(cudaFuncSetAttribute(tau_to_w_kernel<Loader, E, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)sm));
+    tau_to_w_kernel<Loader, E, false><<<(unsigned)blocks, kMatsubaraThreads, sm, stream>>>(*p, ld, fr, out, C, icv,
+                                                                                           log2_ic(icv));
+    TPRF_LAUNCH_CHECK("tau_to_w_kernel");
+    return TPRF_OK;
+  };
+  const long Ct = tune_columns(C);
+  if (!aliases(ld, out) &&
+      (st = tune_pick(tune_key("tau_to_w", {p->L, p->nw, p->fermion, tune_tag(ld)}), ic_candidates(p->fft, extra),
+                      ic, stream, [&](int v) { return launch(v, Ct); }, &ic)))
+    return st;
+  return launch(ic, C);
 }
 
 template <class Loader>
@@ -740,22 +780,33 @@ int launch_nu_to_tau_stat(double beta, int n_iw, int n_tau, bool fermion, long C
     return set_error(TPRF_ERR_TAIL_FIT, "Inverse Fourier requires at least a proper 3rd high-frequency moment");
   unsigned *status = device_status_word();
   if (!status) return TPRF_ERR_CUDA;
+  const size_t extra = 14 * sizeof(double2);
   int ic, lg;
   size_t smem;
-  st = pick_ic(p->fft, 14 * sizeof(double2), &ic, &lg, &smem);
+  st = pick_ic(p->fft, extra, &ic, &lg, &smem);
   if (st) return st;
-  const long blocks = (C + ic - 1) / ic;
-  if (arith_mode() == kArithFP64) {
-    TPRF_CUDA(cudaFuncSetAttribute(nu_to_tau_kernel<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    nu_to_tau_kernel<double2><<<(unsigned)blocks, kMatsubaraThreads, smem, stream>>>(*p, gw, mom, gt, C, ic, lg, status,
-                                                                                      nullptr);
-  } else {
-    TPRF_CUDA(cudaFuncSetAttribute(nu_to_tau_kernel<cdf>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    nu_to_tau_kernel<cdf><<<(unsigned)blocks, kMatsubaraThreads, smem, stream>>>(*p, gw, mom, gt, C, ic, lg, status,
-                                                                                  gt_df);
-  }
-  TPRF_LAUNCH_CHECK("nu_to_tau_kernel");
-  return TPRF_OK;
+  const bool fp64 = arith_mode() == kArithFP64;
+  auto launch = [&](int icv, long n_cols) -> int {  // columns [0, n_cols), icv per CTA
+    const size_t sm = ic_smem(p->fft, extra, icv);
+    const long blocks = (n_cols + icv - 1) / icv;
+    if (fp64) {
+      TPRF_CUDA(cudaFuncSetAttribute(nu_to_tau_kernel<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+      nu_to_tau_kernel<double2><<<(unsigned)blocks, kMatsubaraThreads, sm, stream>>>(*p, gw, mom, gt, C, icv,
+                                                                                      log2_ic(icv), status, nullptr);
+    } else {
+      TPRF_CUDA(cudaFuncSetAttribute(nu_to_tau_kernel<cdf>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+      nu_to_tau_kernel<cdf><<<(unsigned)blocks, kMatsubaraThreads, sm, stream>>>(*p, gw, mom, gt, C, icv, log2_ic(icv),
+                                                                                  status, gt_df);
+    }
+    TPRF_LAUNCH_CHECK("nu_to_tau_kernel");
+    return TPRF_OK;
+  };
+  const long Ct = tune_columns(C);
+  if ((const void *)gw != (const void *)gt &&
+      (st = tune_pick(tune_key("nu_to_tau", {p->L, p->n_iw, p->fermion, mom != nullptr, gt_df != nullptr}),
+                      ic_candidates(p->fft, extra), ic, stream, [&](int v) { return launch(v, Ct); }, &ic)))
+    return st;
+  return launch(ic, C);
 }
 
 int launch_chi_wr_from_chi_tr(double beta, int n_tau, int nw, long C, const double2 *chi_tr, double2 *chi_wr,

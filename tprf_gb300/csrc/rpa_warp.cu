@@ -16,6 +16,8 @@
 // limit (the estimate of rpa.cu).
 #include <algorithm>
 
+#include <vector>
+
 #include "rpa_common.cuh"
 
 namespace tprf {
@@ -444,11 +446,27 @@ int rpa_group_lanes(int nb) { return nb <= 3 ? 8 : 32; }
 
 int launch_rpa_warp(long n_points, int nb, const double2 *chi0, const double2 *U, double2 *chi, cudaStream_t stream,
                     unsigned *status) {
-  switch (rpa_group_lanes(nb)) {
-    case 8: return launch_g<8>(n_points, nb, chi0, U, chi, stream, status);
-    case 16: return launch_g<16>(n_points, nb, chi0, U, chi, stream, status);
-    default: return launch_g<32>(n_points, nb, chi0, U, chi, stream, status);
+  auto launch = [&](int lanes, long n) -> int {
+    switch (lanes) {
+      case 8: return launch_g<8>(n, nb, chi0, U, chi, stream, status);
+      case 16: return launch_g<16>(n, nb, chi0, U, chi, stream, status);
+      default: return launch_g<32>(n, nb, chi0, U, chi, stream, status);
+    }
+  };
+  // candidates: the group sizes whose per-warp tiles fit one CTA (as launch_as sizes them)
+  const int N = nb * nb;
+  const size_t u_bytes = ((size_t)N * N * (sizeof(double2) + sizeof(int)) + (N + 1) * sizeof(int) + 15) & ~(size_t)15;
+  std::vector<int> cands;
+  for (int g : {8, 16, 32})
+    if (u_bytes + (size_t)(32 / g) * 2 * N * N * 16 <= (size_t)max_smem_optin()) cands.push_back(g);
+  int lanes = rpa_group_lanes(nb);
+  const long n_tune = std::min(n_points, (long)num_sms() * 2048);
+  if ((const void *)chi0 != (const void *)chi) {
+    int st = tune_pick(tune_key("rpa_group", {nb}), cands, lanes, stream, [&](int v) { return launch(v, n_tune); },
+                       &lanes);
+    if (st) return st;
   }
+  return launch(lanes, n_points);
 }
 
 int launch_rpa_adjoint_warp(long n_points, int nb, const double2 *chi0, const double2 *U, const double2 *chi,
