@@ -32,8 +32,6 @@ int launch_chi0_w0r_from_grt(double beta, int n_tau, const int dims[3], int nb, 
                              cudaStream_t stream);
 int launch_nu_to_tau_df(double beta, int n_iw, int n_tau, long C, const double2 *gw, const double2 *mom, double2 *gt,
                         void *gt_df, cudaStream_t stream);
-int launch_chi0_wr_from_grt_df(double beta, int n_tau, int nw, const int dims[3], int nb, const double2 *g,
-                               const void *g_df, double2 *chi0_wr, cudaStream_t stream);
 int launch_rpa(long n_points, int nb, const double2 *chi0, const double2 *U, double2 *chi, cudaStream_t stream);
 }  // namespace tprf
 
@@ -159,12 +157,13 @@ int enqueue_instance(const tprf_instance &a, unsigned char *scratch, cudaStream_
   if (st) return st;
   if ((st = launch_lattice_fft(true, 2L * a.n_iw, a.dims, nb2, g_wk, g_wr, s))) return st;
   if ((st = launch_nu_to_tau_df(a.beta, a.n_iw, nt, nk * nb2, g_wr, nullptr, g_tr, g_tr_df, s))) return st;
+  bool chi_df = false;  // chi0(w, r) handed to r -> q as double-float pairs (as the single-instance chain)
   if (a.nw == 1)
     st = launch_chi0_w0r_from_grt(a.beta, nt, a.dims, a.nb, g_tr, chi0, s);
   else
-    st = launch_chi0_wr_from_grt_df(a.beta, nt, a.nw, a.dims, a.nb, g_tr, g_tr_df, chi0, s);
+    st = launch_chi0_wr_from_grt_df(a.beta, nt, a.nw, a.dims, a.nb, g_tr, g_tr_df, chi0, s, nk > 1, &chi_df);
   if (st) return st;
-  if ((st = launch_lattice_fft(false, 2L * a.nw - 1, a.dims, nb4, chi0, chi0, s))) return st;
+  if ((st = launch_lattice_fft_fmt(false, 2L * a.nw - 1, a.dims, nb4, chi0, chi_df, chi0, false, 1.0, s))) return st;
   return launch_rpa((2L * a.nw - 1) * nk, a.nb, chi0, reinterpret_cast<const double2 *>(a.U),
                     reinterpret_cast<double2 *>(a.chi), s);
 }

@@ -18,6 +18,7 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <type_traits>
 
 #include "common.cuh"
 
@@ -32,8 +33,33 @@ __device__ __forceinline__ double2 store_el(cdf z, double, dfl sd, bool scaled) 
   return to_double2(scaled ? cscale(z, sd) : z);
 }
 
-template <bool FWD, class E>
-__global__ void __launch_bounds__(256) lattice_axis_kernel(const double2 *in, double2 *out, long ncols_total,
+// Element i of a pass's input or output in either storage format: complex128,
+// or (DF) double-float pairs (re.hi, re.lo, im.hi, im.lo), the same 16 bytes.
+// Passes of one transform hand each other double-float pairs, so only the
+// transform's own input and output are converted.
+template <class E, bool DF>
+__device__ __forceinline__ E load_in(const void *p, long i) {
+  if constexpr (DF) {
+    static_assert(std::is_same<E, cdf>::value, "double-float storage needs double-float arithmetic");
+    return reinterpret_cast<const cdf *>(p)[i];
+  } else {
+    return load_el<E>(reinterpret_cast<const double2 *>(p)[i]);
+  }
+}
+template <class E> __device__ __forceinline__ E zero_el();
+template <> __device__ __forceinline__ double2 zero_el<double2>() { return make_double2(0.0, 0.0); }
+template <> __device__ __forceinline__ cdf zero_el<cdf>() { return cdf{dfl{0.f, 0.f}, dfl{0.f, 0.f}}; }
+template <class E, bool DF>
+__device__ __forceinline__ void store_out(void *p, long i, E z, double s, dfl sd, bool scaled) {
+  if constexpr (DF) {
+    reinterpret_cast<cdf *>(p)[i] = scaled ? cscale(z, sd) : cnorm(z);
+  } else {
+    reinterpret_cast<double2 *>(p)[i] = store_el(z, s, sd, scaled);
+  }
+}
+
+template <bool FWD, class E, bool IN_DF, bool OUT_DF>
+__global__ void __launch_bounds__(256) lattice_axis_kernel(const void *in, void *out, long ncols_total,
                                                            long inner, int ncol, int lgcol, FftDesc d, double scale) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int n = d.n;
@@ -53,8 +79,7 @@ __global__ void __launch_bounds__(256) lattice_axis_kernel(const double2 *in, do
   for (int w = threadIdx.x; w < tile; w += blockDim.x) {
     const int c = w & (ncol - 1), row = w >> lgcol;
     const long bs = base[c];
-    const double2 v = bs >= 0 ? in[bs + (long)row * inner] : make_double2(0.0, 0.0);
-    a[d.rev[row] * ncol + c] = load_el<E>(v);
+    a[d.rev[row] * ncol + c] = bs >= 0 ? load_in<E, IN_DF>(in, bs + (long)row * inner) : zero_el<E>();
   }
   E *r = fft_smem<FWD>(a, b, d, ncol);
   const bool scaled = scale != 1.0;
@@ -62,12 +87,12 @@ __global__ void __launch_bounds__(256) lattice_axis_kernel(const double2 *in, do
   for (int w = threadIdx.x; w < tile; w += blockDim.x) {
     const int c = w & (ncol - 1), row = w >> lgcol;
     const long bs = base[c];
-    if (bs >= 0) out[bs + (long)row * inner] = store_el(r[row * ncol + c], scale, sd, scaled);
+    if (bs >= 0) store_out<E, OUT_DF>(out, bs + (long)row * inner, r[row * ncol + c], scale, sd, scaled);
   }
 }
 
-template <bool FWD, class E>
-int launch_axis_as(const double2 *in, double2 *out, long outer, int n, long inner, double scale, cudaStream_t stream) {
+template <bool FWD, class E, bool IN_DF, bool OUT_DF>
+int launch_axis_as(const void *in, void *out, long outer, int n, long inner, double scale, cudaStream_t stream) {
   FftDesc d;
   int st = get_fft(n, &d);
   if (st) return st;
@@ -85,16 +110,26 @@ int launch_axis_as(const double2 *in, double2 *out, long outer, int n, long inne
   while ((1 << lg) < ncol) ++lg;
   const long blocks = (ncols_total + ncol - 1) / ncol;
   if (blocks > 0x7fffffffL) return set_error(TPRF_ERR_INVALID_ARGUMENT, "lattice FFT: too many tiles");
-  TPRF_CUDA(cudaFuncSetAttribute(lattice_axis_kernel<FWD, E>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  lattice_axis_kernel<FWD, E><<<(unsigned)blocks, 256, smem, stream>>>(in, out, ncols_total, inner, ncol, lg, d, scale);
+  auto kern = lattice_axis_kernel<FWD, E, IN_DF, OUT_DF>;
+  TPRF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  kern<<<(unsigned)blocks, 256, smem, stream>>>(in, out, ncols_total, inner, ncol, lg, d, scale);
   TPRF_LAUNCH_CHECK("lattice_axis_kernel");
   return TPRF_OK;
 }
 
+// Storage formats of a pass: complex128 (0) or double-float pairs (1) for its
+// input and output; double-float only with double-float arithmetic.
 template <bool FWD>
-int launch_axis(const double2 *in, double2 *out, long outer, int n, long inner, double scale, cudaStream_t stream) {
-  if (arith_mode() == kArithFP64) return launch_axis_as<FWD, double2>(in, out, outer, n, inner, scale, stream);
-  return launch_axis_as<FWD, cdf>(in, out, outer, n, inner, scale, stream);
+int launch_axis(const void *in, bool in_df, void *out, bool out_df, long outer, int n, long inner, double scale,
+                cudaStream_t stream) {
+  if (arith_mode() == kArithFP64) {
+    if (in_df || out_df) return set_error(TPRF_ERR_INVALID_ARGUMENT, "lattice FFT: double-float storage in FP64 mode");
+    return launch_axis_as<FWD, double2, false, false>(in, out, outer, n, inner, scale, stream);
+  }
+  if (in_df && out_df) return launch_axis_as<FWD, cdf, true, true>(in, out, outer, n, inner, scale, stream);
+  if (in_df) return launch_axis_as<FWD, cdf, true, false>(in, out, outer, n, inner, scale, stream);
+  if (out_df) return launch_axis_as<FWD, cdf, false, true>(in, out, outer, n, inner, scale, stream);
+  return launch_axis_as<FWD, cdf, false, false>(in, out, outer, n, inner, scale, stream);
 }
 
 // Two adjacent mesh axes in one pass: the array is [outer, n1, n2, n_target]
@@ -104,8 +139,8 @@ int launch_axis(const double2 *in, double2 *out, long outer, int n, long inner, 
 // n1-point ones columns (i2, t) with stride n2 * nt. Each element is read,
 // converted, written and converted back once for both axes. n1, n2 and nt are
 // powers of two with n1 * nt and n2 * nt dividing the 256 threads.
-template <bool FWD, class E>
-__global__ void __launch_bounds__(256) lattice_plane_kernel(const double2 *in, double2 *out, long outer, long n_target,
+template <bool FWD, class E, bool IN_DF, bool OUT_DF>
+__global__ void __launch_bounds__(256) lattice_plane_kernel(const void *in, void *out, long outer, long n_target,
                                                             int nt, int lgt, FftDesc d1, FftDesc d2, int lg2,
                                                             double scale) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -119,8 +154,8 @@ __global__ void __launch_bounds__(256) lattice_plane_kernel(const double2 *in, d
   for (int w = threadIdx.x; w < P * nt; w += blockDim.x) {
     const int t = w & (nt - 1), p = w >> lgt;
     const int i1 = p >> lg2, i2 = p & (n2 - 1);
-    const double2 v = t < ntv ? in[gbase + (long)p * n_target + t] : make_double2(0.0, 0.0);
-    a[((d1.rev[i1] << lg2) + d2.rev[i2]) * nt + t] = load_el<E>(v);
+    a[((d1.rev[i1] << lg2) + d2.rev[i2]) * nt + t] =
+        t < ntv ? load_in<E, IN_DF>(in, gbase + (long)p * n_target + t) : zero_el<E>();
   }
   // axis 2: columns (i1, t), element i2 at i1 * n2 * nt + i2 * nt + t
   fft_smem<FWD>(a, (E *)nullptr, d2, n1 * nt, -1, ColLayout{nt, n2 * nt, lgt});
@@ -130,7 +165,7 @@ __global__ void __launch_bounds__(256) lattice_plane_kernel(const double2 *in, d
   const dfl sd = split_double(scale);
   for (int w = threadIdx.x; w < P * nt; w += blockDim.x) {
     const int t = w & (nt - 1), p = w >> lgt;
-    if (t < ntv) out[gbase + (long)p * n_target + t] = store_el(r[p * nt + t], scale, sd, scaled);
+    if (t < ntv) store_out<E, OUT_DF>(out, gbase + (long)p * n_target + t, r[p * nt + t], scale, sd, scaled);
   }
 }
 
@@ -155,8 +190,8 @@ int plane_targets(int n1, int n2, long n_target) {
   return nt;
 }
 
-template <bool FWD, class E>
-int launch_plane_as(const double2 *in, double2 *out, long outer, int n1, int n2, long n_target, double scale,
+template <bool FWD, class E, bool IN_DF, bool OUT_DF>
+int launch_plane_as(const void *in, void *out, long outer, int n1, int n2, long n_target, double scale,
                     cudaStream_t stream) {
   FftDesc d1, d2;
   int st = get_fft(n1, &d1);
@@ -167,18 +202,24 @@ int launch_plane_as(const double2 *in, double2 *out, long outer, int n1, int n2,
   const size_t smem = (size_t)n1 * n2 * nt * sizeof(E);
   const long tiles = outer * ((n_target + nt - 1) / nt);
   if (tiles > 0x7fffffffL) return set_error(TPRF_ERR_INVALID_ARGUMENT, "lattice FFT: too many tiles");
-  TPRF_CUDA(cudaFuncSetAttribute(lattice_plane_kernel<FWD, E>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  lattice_plane_kernel<FWD, E><<<(unsigned)tiles, 256, smem, stream>>>(in, out, outer, n_target, nt, log2i(nt), d1, d2,
-                                                                     log2i(n2), scale);
+  auto kern = lattice_plane_kernel<FWD, E, IN_DF, OUT_DF>;
+  TPRF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  kern<<<(unsigned)tiles, 256, smem, stream>>>(in, out, outer, n_target, nt, log2i(nt), d1, d2, log2i(n2), scale);
   TPRF_LAUNCH_CHECK("lattice_plane_kernel");
   return TPRF_OK;
 }
 
 template <bool FWD>
-int launch_plane(const double2 *in, double2 *out, long outer, int n1, int n2, long n_target, double scale,
-                 cudaStream_t stream) {
-  if (arith_mode() == kArithFP64) return launch_plane_as<FWD, double2>(in, out, outer, n1, n2, n_target, scale, stream);
-  return launch_plane_as<FWD, cdf>(in, out, outer, n1, n2, n_target, scale, stream);
+int launch_plane(const void *in, bool in_df, void *out, bool out_df, long outer, int n1, int n2, long n_target,
+                 double scale, cudaStream_t stream) {
+  if (arith_mode() == kArithFP64) {
+    if (in_df || out_df) return set_error(TPRF_ERR_INVALID_ARGUMENT, "lattice FFT: double-float storage in FP64 mode");
+    return launch_plane_as<FWD, double2, false, false>(in, out, outer, n1, n2, n_target, scale, stream);
+  }
+  if (in_df && out_df) return launch_plane_as<FWD, cdf, true, true>(in, out, outer, n1, n2, n_target, scale, stream);
+  if (in_df) return launch_plane_as<FWD, cdf, true, false>(in, out, outer, n1, n2, n_target, scale, stream);
+  if (out_df) return launch_plane_as<FWD, cdf, false, true>(in, out, outer, n1, n2, n_target, scale, stream);
+  return launch_plane_as<FWD, cdf, false, false>(in, out, outer, n1, n2, n_target, scale, stream);
 }
 
 }  // namespace
@@ -200,64 +241,76 @@ int launch_lattice_fft(bool forward, long n_w, const int dims[3], long n_target,
 // unscaled forward and the 1/N_k-scaled backward transforms).
 int launch_lattice_fft_scaled(bool forward, long n_w, const int dims[3], long n_target, const double2 *in,
                               double2 *out, double scale_last, cudaStream_t stream) {
-  int last = -1;
+  return launch_lattice_fft_fmt(forward, n_w, dims, n_target, in, false, out, false, scale_last, stream);
+}
+
+// The general form: input and output each stored as complex128 or (with
+// double-float arithmetic) as double-float pairs; the passes in between hand
+// each other double-float pairs whenever the arithmetic is double-float.
+int launch_lattice_fft_fmt(bool forward, long n_w, const int dims[3], long n_target, const void *in, bool in_df,
+                           void *out, bool out_df, double scale_last, cudaStream_t stream) {
+  const bool mid_df = arith_mode() != kArithFP64;
+  int nontriv[3], nn = 0;
   for (int ax = 0; ax < 3; ++ax)
-    if (dims[ax] > 1) last = ax;
-  if (last < 0) {  // a single k point: the transform is the identity (times the factor)
+    if (dims[ax] > 1) nontriv[nn++] = ax;
+  if (nn == 0) {  // a single k point: the transform is the identity (times the factor)
+    if (in_df || out_df)
+      return set_error(TPRF_ERR_INVALID_ARGUMENT, "lattice FFT: double-float storage needs a mesh with N_k > 1");
     const long n = n_w * n_target;
+    const double2 *src = static_cast<const double2 *>(in);
+    double2 *dst = static_cast<double2 *>(out);
     if (scale_last == 1.0) {
-      if (in != out) TPRF_CUDA(cudaMemcpyAsync(out, in, n * sizeof(double2), cudaMemcpyDeviceToDevice, stream));
+      if (src != dst) TPRF_CUDA(cudaMemcpyAsync(dst, src, n * sizeof(double2), cudaMemcpyDeviceToDevice, stream));
     } else {
-      scale_copy_kernel<<<(unsigned)std::min((n + 255) / 256, (long)num_sms() * 8), 256, 0, stream>>>(in, out, n,
-                                                                                                    scale_last);
+      scale_copy_kernel<<<(unsigned)std::min((n + 255) / 256, (long)num_sms() * 8), 256, 0, stream>>>(src, dst, n,
+                                                                                                      scale_last);
       TPRF_LAUNCH_CHECK("scale_copy_kernel");
     }
     return TPRF_OK;
   }
-  const double2 *src = in;
   // The two fastest-varying non-trivial axes in one pass where they are powers
   // of two; the remaining axis (if any) in a one-axis pass, which then scales.
-  int nontriv[3], nn = 0;
-  for (int ax = 0; ax < 3; ++ax)
-    if (dims[ax] > 1) nontriv[nn++] = ax;
   if (nn >= 2) {
     const int A = nontriv[nn - 2], B = nontriv[nn - 1];
     if (plane_targets(dims[A], dims[B], n_target) > 0) {
       long outer = n_w;
       for (int a2 = 0; a2 < A; ++a2) outer *= dims[a2];
       const double scale = (nn == 2) ? scale_last : 1.0;
-      int st = forward ? launch_plane<true>(src, out, outer, dims[A], dims[B], n_target, scale, stream)
-                       : launch_plane<false>(src, out, outer, dims[A], dims[B], n_target, scale, stream);
+      const bool plane_out_df = (nn == 3) ? mid_df : out_df;
+      int st = forward ? launch_plane<true>(in, in_df, out, plane_out_df, outer, dims[A], dims[B], n_target, scale, stream)
+                       : launch_plane<false>(in, in_df, out, plane_out_df, outer, dims[A], dims[B], n_target, scale,
+                                             stream);
       if (st) return st;
       if (nn == 3) {
         const int ax = nontriv[0];
         long outer0 = n_w, inner0 = n_target;
         for (int a2 = 0; a2 < ax; ++a2) outer0 *= dims[a2];
         for (int a2 = ax + 1; a2 < 3; ++a2) inner0 *= dims[a2];
-        st = forward ? launch_axis<true>(out, out, outer0, dims[ax], inner0, scale_last, stream)
-                     : launch_axis<false>(out, out, outer0, dims[ax], inner0, scale_last, stream);
+        st = forward ? launch_axis<true>(out, mid_df, out, out_df, outer0, dims[ax], inner0, scale_last, stream)
+                     : launch_axis<false>(out, mid_df, out, out_df, outer0, dims[ax], inner0, scale_last, stream);
         if (st) return st;
       }
       return TPRF_OK;
     }
   }
-  // fastest-varying mesh dimension first: its pass has the longest contiguous rows
-  for (int ax = 2; ax >= 0; --ax) {
-    const int n = dims[ax];
-    if (n <= 1) continue;
+  // fastest-varying mesh dimension first: its pass has the longest contiguous rows;
+  // the factor on the last pass (the slowest dimension with n > 1)
+  const void *src = in;
+  bool src_df = in_df;
+  for (int i = nn - 1; i >= 0; --i) {
+    const int ax = nontriv[i], n = dims[ax];
     long outer = n_w, inner = n_target;
     for (int a2 = 0; a2 < ax; ++a2) outer *= dims[a2];
     for (int a2 = ax + 1; a2 < 3; ++a2) inner *= dims[a2];
-    // scale once, on the last pass issued (the slowest dimension with n > 1)
-    int first_nontrivial = 0;
-    while (dims[first_nontrivial] <= 1) ++first_nontrivial;
-    const double scale = (ax == first_nontrivial) ? scale_last : 1.0;
-    int st = forward ? launch_axis<true>(src, out, outer, n, inner, scale, stream)
-                     : launch_axis<false>(src, out, outer, n, inner, scale, stream);
+    const bool last_pass = (i == 0);
+    const double scale = last_pass ? scale_last : 1.0;
+    const bool dst_df = last_pass ? out_df : mid_df;
+    int st = forward ? launch_axis<true>(src, src_df, out, dst_df, outer, n, inner, scale, stream)
+                     : launch_axis<false>(src, src_df, out, dst_df, outer, n, inner, scale, stream);
     if (st) return st;
     src = out;
+    src_df = dst_df;
   }
-  (void)last;
   return TPRF_OK;
 }
 
@@ -407,8 +460,9 @@ int noalloc_axis(const double2 *in, double2 *out, long outer, long inner, const 
   int lg = 0;
   while ((1 << lg) < ncol) ++lg;
   const long blocks = (ncols_total + ncol - 1) / ncol;
-  TPRF_CUDA(cudaFuncSetAttribute(lattice_axis_kernel<FWD, E>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  lattice_axis_kernel<FWD, E><<<(unsigned)blocks, 256, smem, stream>>>(in, out, ncols_total, inner, ncol, lg, d, scale);
+  auto kern = lattice_axis_kernel<FWD, E, false, false>;
+  TPRF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  kern<<<(unsigned)blocks, 256, smem, stream>>>(in, out, ncols_total, inner, ncol, lg, d, scale);
   TPRF_LAUNCH_CHECK("lattice_axis_kernel (no-alloc)");
   return TPRF_OK;
 }

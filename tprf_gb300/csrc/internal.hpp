@@ -130,6 +130,14 @@ int launch_lattice_fft(bool forward, long n_w, const int dims[3], long n_target,
                        cudaStream_t stream);
 int launch_lattice_fft_scaled(bool forward, long n_w, const int dims[3], long n_target, const double2 *in,
                               double2 *out, double scale, cudaStream_t stream);
+// Input / output stored as complex128 or (in_df / out_df, double-float
+// arithmetic only, N_k > 1) as double-float pairs of the same 16 bytes.
+int launch_lattice_fft_fmt(bool forward, long n_w, const int dims[3], long n_target, const void *in, bool in_df,
+                           void *out, bool out_df, double scale, cudaStream_t stream);
+// The fused bubble + tau -> iw, writing chi0(iw, r) as double-float pairs when
+// want_df and the double-float path runs (*wrote_df tells which).
+int launch_chi0_wr_from_grt_df(double beta, int n_tau, int nw, const int dims[3], int nb, const double2 *g,
+                               const void *g_df, double2 *chi0_wr, cudaStream_t stream, bool want_df, bool *wrote_df);
 int launch_tau_to_w_adjoint(double beta, int n_tau, int nw, long C, const double2 *yg, double2 *xg,
                             cudaStream_t stream);
 int launch_nu_to_tau_adjoint(double beta, int n_iw, int n_tau, long C, const double2 *yg, double2 *gg, bool fitted,

@@ -286,7 +286,7 @@ struct BubbleLoaderDF : BubbleLoader {
 // parameter so that the bosonic bubble path carries no branch for it.
 template <class Loader, class C, bool FERM>
 __global__ void __launch_bounds__(kMatsubaraThreads, 2) tau_to_w_kernel(TauWPlan p, Loader ld, FitRows fr, double2 *__restrict__ out,
-                                                       long Ccols, int ic, int lg) {
+                                                       long Ccols, int ic, int lg, int out_df) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C *a = reinterpret_cast<C *>(smem_raw);
   const int L = p.L, nwt = p.n_out;
@@ -386,7 +386,11 @@ __global__ void __launch_bounds__(kMatsubaraThreads, 2) tau_to_w_kernel(TauWPlan
     C v = cscale(last_stage_output<false>(r, p.fft, ic, c, m < 0 ? m + L : m), fact);
 #pragma unroll
     for (int j = 0; j < 3; ++j) v = cadd(v, cmul(am[j * ic + c], table<C>(p.K, p.Kf, (long)j * nwt + mi)));
-    out[(long)mi * Ccols + col0 + c] = as_d2(v);
+    // complex128, or the element type itself for a following double-float pass
+    if (out_df)
+      reinterpret_cast<C *>(out)[(long)mi * Ccols + col0 + c] = v;
+    else
+      out[(long)mi * Ccols + col0 + c] = as_d2(v);
   }
 }
 
@@ -469,7 +473,8 @@ int tune_tag(const BubbleLoader &l) { return 10 + l.nb; }
 int tune_tag(const BubbleLoaderDF &l) { return 20 + l.nb; }
 
 template <class Loader, class E>
-int launch_tau_to_w_as(const TauWPlan *p, Loader ld, double2 *out, long C, cudaStream_t stream) {
+int launch_tau_to_w_as(const TauWPlan *p, Loader ld, double2 *out, long C, cudaStream_t stream,
+                       bool out_df = false) {
   const size_t extra = 5 * sizeof(double2) + 2 * sizeof(long) + 18 * sizeof(double2);
   int ic, lg;
   size_t smem;
@@ -487,7 +492,7 @@ int launch_tau_to_w_as(const TauWPlan *p, Loader ld, double2 *out, long C, cudaS
         TPRF_CUDA(cudaFuncSetAttribute(tau_to_w_kernel<Loader, E, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)sm));
         tau_to_w_kernel<Loader, E, true><<<(unsigned)blocks, kMatsubaraThreads, sm, stream>>>(*p, ld, fr, out, C, icv,
-                                                                                              log2_ic(icv));
+                                                                                              log2_ic(icv), out_df);
         TPRF_LAUNCH_CHECK("tau_to_w_kernel");
         return TPRF_OK;
       }
@@ -495,13 +500,13 @@ int launch_tau_to_w_as(const TauWPlan *p, Loader ld, double2 *out, long C, cudaS
     TPRF_CUDA(cudaFuncSetAttribute(tau_to_w_kernel<Loader, E, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)sm));
     tau_to_w_kernel<Loader, E, false><<<(unsigned)blocks, kMatsubaraThreads, sm, stream>>>(*p, ld, fr, out, C, icv,
-                                                                                           log2_ic(icv));
+                                                                                           log2_ic(icv), out_df);
     TPRF_LAUNCH_CHECK("tau_to_w_kernel");
     return TPRF_OK;
   };
   const long Ct = tune_columns(C);
   if (!aliases(ld, out) &&
-      (st = tune_pick(tune_key("tau_to_w", {p->L, p->nw, p->fermion, tune_tag(ld)}), ic_candidates(p->fft, extra),
+      (st = tune_pick(tune_key("tau_to_w", {p->L, p->nw, p->fermion, tune_tag(ld), out_df}), ic_candidates(p->fft, extra),
                       ic, stream, [&](int v) { return launch(v, Ct); }, &ic)))
     return st;
   return launch(ic, C);
@@ -845,7 +850,8 @@ int launch_chi0_wr_from_grt(double beta, int n_tau, int nw, const int dims[3], i
 // (written by launch_nu_to_tau_df); g_df == NULL or the FP64 arithmetic mode
 // takes the complex128 path.
 int launch_chi0_wr_from_grt_df(double beta, int n_tau, int nw, const int dims[3], int nb, const double2 *g,
-                               const void *g_df, double2 *chi0_wr, cudaStream_t stream) {
+                               const void *g_df, double2 *chi0_wr, cudaStream_t stream, bool want_df, bool *wrote_df) {
+  if (wrote_df) *wrote_df = false;
   if (!g_df || arith_mode() == kArithFP64) return launch_chi0_wr_from_grt(beta, n_tau, nw, dims, nb, g, chi0_wr, stream);
   int st = check_tau_w(beta, n_tau, nw);
   if (st) return st;
@@ -856,7 +862,9 @@ int launch_chi0_wr_from_grt_df(double beta, int n_tau, int nw, const int dims[3]
   static_cast<BubbleLoader &>(ld) = make_bubble(g, n_tau, dims, nb);
   ld.gdf = reinterpret_cast<const cdf *>(g_df);
   const long C = ld.Nr * nb * nb * nb * nb;
-  return launch_tau_to_w_as<BubbleLoaderDF, cdf>(p, ld, chi0_wr, C, stream);
+  st = launch_tau_to_w_as<BubbleLoaderDF, cdf>(p, ld, chi0_wr, C, stream, want_df);
+  if (!st && wrote_df) *wrote_df = want_df;
+  return st;
 }
 
 int launch_chi0_w0r_from_grt(double beta, int n_tau, const int dims[3], int nb, const double2 *g, double2 *chi0_wr,

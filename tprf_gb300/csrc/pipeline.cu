@@ -22,8 +22,6 @@ int launch_chi0_w0r_from_grt(double beta, int n_tau, const int dims[3], int nb, 
                              cudaStream_t stream);
 int launch_nu_to_tau_df(double beta, int n_iw, int n_tau, long C, const double2 *gw, const double2 *mom, double2 *gt,
                         void *gt_df, cudaStream_t stream);
-int launch_chi0_wr_from_grt_df(double beta, int n_tau, int nw, const int dims[3], int nb, const double2 *g,
-                               const void *g_df, double2 *chi0_wr, cudaStream_t stream);
 }  // namespace tprf
 
 using namespace tprf;
@@ -73,12 +71,15 @@ extern "C" int tprf_imtime_bubble_chi0_wk_timed(double beta, int n_iw, int n_tau
   st = launch_nu_to_tau_df(beta, n_iw, n_tau, nk * nb2, g_wr, reinterpret_cast<const double2 *>(moments), g_tr,
                            g_tr_df, s);
   if (st || (st = mark(2))) return st;
+  // chi0(w, r) goes from the bubble to the r -> q transform as double-float
+  // pairs (same bytes) on the double-float path: no conversion in between
+  bool chi_df = false;
   if (nw == 1)
     st = launch_chi0_w0r_from_grt(beta, n_tau, dims, nb, g_tr, out, s);
   else
-    st = launch_chi0_wr_from_grt_df(beta, n_tau, nw, dims, nb, g_tr, g_tr_df, out, s);
+    st = launch_chi0_wr_from_grt_df(beta, n_tau, nw, dims, nb, g_tr, g_tr_df, out, s, nk > 1, &chi_df);
   if (st || (st = mark(3))) return st;
-  st = launch_lattice_fft(false, 2L * nw - 1, dims, nb4, out, out, s);
+  st = launch_lattice_fft_fmt(false, 2L * nw - 1, dims, nb4, out, chi_df, out, false, 1.0, s);
   if (st || (st = mark(4))) return st;
   return finish_with_checks(s, "imtime_bubble_chi0_wk");
 }
