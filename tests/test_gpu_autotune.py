@@ -49,3 +49,50 @@ def test_measure_mode_records_wisdom_and_keeps_results(cuda_lib, tmp_path):
     finally:
         tuning.set_autotune(False)
         tuning.clear_wisdom()
+
+
+def _device_prefix():
+    p = torch.cuda.get_device_properties(0)
+    return f"sm{p.major}{p.minor}x{p.multi_processor_count}"
+
+
+def test_every_rpa_group_size_gives_the_same_chi(cuda_lib, tmp_path):
+    """The RPA group kernel with 8, 9, 16 and 32 lanes per point (forced through
+    wisdom files) gives the same chi, in double-float and in FP64 arithmetic,
+    including points re-solved in FP64 (a near-singular subset)."""
+    from tprf_gb300 import _native, tuning
+    from tprf_gb300.workloads import kanamori_spin_vertex
+    nb, n = 3, 20000
+    rng = np.random.default_rng(7)
+    chi0 = 0.2 * (rng.standard_normal((n, nb ** 4)) + 1j * rng.standard_normal((n, nb ** 4)))
+    U = kanamori_spin_vertex(nb, 2.3, 0.4)
+    Ug = U.reshape(nb, nb, nb, nb).transpose(0, 1, 3, 2).reshape(nb * nb, nb * nb)
+    # points 0..99: chi0 = (I - eps) Ug^-1 grouped, so I - chi0 Ug is nearly singular
+    inv = np.linalg.inv(Ug)
+    for i in range(100):
+        m = (np.eye(nb * nb) - 1e-3 * rng.standard_normal((nb * nb, nb * nb))) @ inv
+        chi0[i] = m.reshape(nb, nb, nb, nb).transpose(0, 1, 3, 2).reshape(-1)
+    x = torch.as_tensor(chi0, device="cuda").contiguous()
+    u = torch.as_tensor(U, dtype=torch.complex128, device="cuda").contiguous()
+    lib = cuda_lib
+    out = {}
+    try:
+        for arith in (0, 1):
+            _native.check(lib.tprf_set_arithmetic(arith))
+            for lanes in (8, 9, 16, 32):
+                tuning.set_autotune(False)
+                tuning.clear_wisdom()
+                w = tmp_path / f"w{lanes}.txt"
+                w.write_text(f"{_device_prefix()}/rpa_group/{arith}/{nb} {lanes}\n")
+                tuning.load_wisdom(w)
+                chi = torch.empty_like(x)
+                _native.check(lib.tprf_solve_rpa_PH(n, nb, x.data_ptr(), u.data_ptr(), chi.data_ptr(), None))
+                torch.cuda.synchronize()
+                out[(arith, lanes)] = chi.cpu().numpy()
+    finally:
+        lib.tprf_set_arithmetic(0)
+        tuning.clear_wisdom()
+    ref = out[(1, 8)]
+    for key, chi in out.items():
+        assert rel_err(chi, ref) < 1e-11, key
+        assert rel_err(chi, out[(key[0], 8)]) < 1e-14, key

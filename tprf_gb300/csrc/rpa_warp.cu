@@ -46,6 +46,52 @@ template <> struct Mag<cdf> {
 __device__ __forceinline__ double mag2(double2 z) { return cabs2(z); }
 __device__ __forceinline__ float mag2(cdf z) { return __fmaf_rn(z.x.hi, z.x.hi, z.y.hi * z.y.hi); }
 
+// Reductions inside a group of G lanes (gmask): xor shuffles when G is a
+// power of two, else the warp reduce instructions on order-preserving integer
+// keys (non-negative floats and doubles order as their bit patterns). The
+// argmax keeps the smallest row index among equal magnitudes; a lane without
+// candidate rows (best < 0) takes part with magnitude zero and row j.
+constexpr bool pow2_lanes(int g) { return (g & (g - 1)) == 0; }
+
+template <int G>
+__device__ __forceinline__ float group_max(float v, unsigned gmask) {
+  if constexpr (pow2_lanes(G)) {
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(gmask, v, o));
+    return v;
+  } else {
+    return __uint_as_float(__reduce_max_sync(gmask, __float_as_uint(fmaxf(v, 0.f))));
+  }
+}
+
+template <int G, class MagT>
+__device__ __forceinline__ void group_argmax(MagT &best, int &p, unsigned gmask) {
+  if constexpr (pow2_lanes(G)) {
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) {
+      const MagT ob = __shfl_xor_sync(gmask, best, o);
+      const int op = __shfl_xor_sync(gmask, p, o);
+      if (ob > best || (ob == best && op < p)) {
+        best = ob;
+        p = op;
+      }
+    }
+  } else if constexpr (sizeof(MagT) == 4) {
+    const unsigned key = best > 0 ? __float_as_uint(best) : 0u;
+    const unsigned kmax = __reduce_max_sync(gmask, key);
+    p = (int)__reduce_min_sync(gmask, key == kmax ? (unsigned)p : 0xffffffffu);
+    best = __uint_as_float(kmax);
+  } else {
+    const unsigned long long key = best > 0 ? (unsigned long long)__double_as_longlong(best) : 0ull;
+    const unsigned hi = (unsigned)(key >> 32), lo = (unsigned)key;
+    const unsigned hmax = __reduce_max_sync(gmask, hi);
+    const unsigned lmax = __reduce_max_sync(gmask, hi == hmax ? lo : 0u);
+    const unsigned long long kmax = ((unsigned long long)hmax << 32) | lmax;
+    p = (int)__reduce_min_sync(gmask, key == kmax ? (unsigned)p : 0xffffffffu);
+    best = __longlong_as_double((long long)kmax);
+  }
+}
+
 // Gaussian elimination with partial pivoting on the group's augmented matrix
 // M = [A | B] (N x 2N, row major, shared memory), then back substitution: on
 // return the right half holds A^-1 B and the left half the LU factors.
@@ -67,15 +113,7 @@ __device__ __forceinline__ typename Mag<E>::type solve_augmented(E *M, int N, in
         p = i;
       }
     }
-#pragma unroll
-    for (int o = G / 2; o > 0; o >>= 1) {
-      const MagT ob = __shfl_xor_sync(gmask, best, o);
-      const int op = __shfl_xor_sync(gmask, p, o);
-      if (ob > best || (ob == best && op < p)) {
-        best = ob;
-        p = op;
-      }
-    }
+    group_argmax<G>(best, p, gmask);
     if (best == 0) sing = true;
     pmin = pmin < best ? pmin : best;
     if (p != j) {
@@ -141,8 +179,7 @@ __device__ double rpa_point_warp(const double2 *__restrict__ x, double2 *__restr
   const auto pmin = solve_augmented<E, G>(M, N, lane, gmask, sing);
   singular = sing;
   for (int o = lane; o < N * N; o += G) y[o] = el_to(M[(o / N) * 2 * N + N + col_of_offset(o % N, nb)]);
-#pragma unroll
-  for (int o = G / 2; o > 0; o >>= 1) amax = fmaxf(amax, __shfl_xor_sync(gmask, amax, o));
+  amax = group_max<G>(amax, gmask);
   __syncwarp(gmask);
   const double am = (double)amax * (double)amax;
   return pmin > 0 ? am / (double)pmin : 1e300;
@@ -159,10 +196,14 @@ __global__ void __launch_bounds__(512) rpa_warp_kernel(long n_points, int nb, co
   int *s_row = reinterpret_cast<int *>(s_val + N * N);
   int *s_cs = s_row + N * N;
   const size_t u_bytes = ((size_t)N * N * (sizeof(double2) + sizeof(int)) + (N + 1) * sizeof(int) + 15) & ~(size_t)15;
-  // groups of G lanes, one point per group
-  const int grp = threadIdx.x / G, lane = threadIdx.x & (G - 1), n_grp = blockDim.x / G;
-  const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (threadIdx.x & 31 & ~(G - 1)));
-  E *M = reinterpret_cast<E *>(smem_raw + u_bytes) + (size_t)grp * 2 * N * N;
+  // groups of G lanes, one point per group, 32 / G groups in each warp (the
+  // lanes past the last whole group of a warp stay idle)
+  constexpr int GPW = 32 / G;
+  const int wl = threadIdx.x & 31, gw = wl / G;
+  const int grp = (threadIdx.x >> 5) * GPW + gw, lane = wl - gw * G, n_grp = (blockDim.x >> 5) * GPW;
+  const bool active = gw < GPW;
+  const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (gw * G));
+  E *M = reinterpret_cast<E *>(smem_raw + u_bytes) + (size_t)(active ? grp : 0) * 2 * N * N;
   if (threadIdx.x == 0) {
     int t = 0;
     for (int c = 0; c < N; ++c) {
@@ -181,6 +222,7 @@ __global__ void __launch_bounds__(512) rpa_warp_kernel(long n_points, int nb, co
   }
   __syncthreads();
   const SparseU u{s_val, s_row, s_cs};
+  if (!active) return;
   for (long pt = (long)blockIdx.x * n_grp + grp; pt < n_points; pt += (long)gridDim.x * n_grp) {
     const double2 *x = chi0 + pt * N * N;
     double2 *y = chi + pt * N * N;
@@ -449,6 +491,7 @@ int launch_rpa_warp(long n_points, int nb, const double2 *chi0, const double2 *U
   auto launch = [&](int lanes, long n) -> int {
     switch (lanes) {
       case 8: return launch_g<8>(n, nb, chi0, U, chi, stream, status);
+      case 9: return launch_g<9>(n, nb, chi0, U, chi, stream, status);
       case 16: return launch_g<16>(n, nb, chi0, U, chi, stream, status);
       default: return launch_g<32>(n, nb, chi0, U, chi, stream, status);
     }
@@ -457,8 +500,10 @@ int launch_rpa_warp(long n_points, int nb, const double2 *chi0, const double2 *U
   const int N = nb * nb;
   const size_t u_bytes = ((size_t)N * N * (sizeof(double2) + sizeof(int)) + (N + 1) * sizeof(int) + 15) & ~(size_t)15;
   std::vector<int> cands;
-  for (int g : {8, 16, 32})
-    if (u_bytes + (size_t)(32 / g) * 2 * N * N * 16 <= (size_t)max_smem_optin()) cands.push_back(g);
+  // 9 lanes (three groups per warp) own two of the 18 columns of a 9 x 9 system each
+  for (int g : {8, 9, 16, 32})
+    if ((g != 9 || N == 9) && u_bytes + (size_t)(32 / g) * 2 * N * N * 16 <= (size_t)max_smem_optin())
+      cands.push_back(g);
   int lanes = rpa_group_lanes(nb);
   const long n_tune = std::min(n_points, (long)num_sms() * 2048);
   if ((const void *)chi0 != (const void *)chi) {
