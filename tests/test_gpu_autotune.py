@@ -96,3 +96,4 @@ def test_every_rpa_group_size_gives_the_same_chi(cuda_lib, tmp_path):
     for key, chi in out.items():
         assert rel_err(chi, ref) < 1e-11, key
         assert rel_err(chi, out[(key[0], 8)]) < 1e-14, key
+

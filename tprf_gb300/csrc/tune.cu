@@ -147,7 +147,7 @@ extern "C" int tprf_autotune_load(const char *path) {
     std::istringstream ls(line);
     std::string key, extra;
     long v = 0;
-    if (!(ls >> key >> v) || (ls >> extra) || v < 1 || v > (1 << 20))
+    if (!(ls >> key >> v) || (ls >> extra) || v < 0 || v > (1 << 20))
       return tprf::set_error(TPRF_ERR_INVALID_ARGUMENT,
                              "autotune_load: malformed line " + std::to_string(n) + " of " + path);
     read[key] = (int)v;
