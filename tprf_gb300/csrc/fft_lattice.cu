@@ -25,6 +25,8 @@
 namespace tprf {
 namespace {
 
+constexpr int kLoadBatch = 4;  // tile loads per thread issued together
+
 template <class E> __device__ __forceinline__ E load_el(double2 z);
 template <> __device__ __forceinline__ double2 load_el<double2>(double2 z) { return z; }
 template <> __device__ __forceinline__ cdf load_el<cdf>(double2 z) { return to_cdf(z); }
@@ -46,6 +48,16 @@ __device__ __forceinline__ E load_in(const void *p, long i) {
     return load_el<E>(reinterpret_cast<const double2 *>(p)[i]);
   }
 }
+// The same in two steps, so that a batch of loads can be in flight before any
+// is converted: the raw 16 bytes, then the element.
+template <bool DF> struct RawOf { using type = double2; };
+template <> struct RawOf<true> { using type = cdf; };
+template <class E, bool DF>
+__device__ __forceinline__ typename RawOf<DF>::type load_raw(const void *p, long i) {
+  return reinterpret_cast<const typename RawOf<DF>::type *>(p)[i];
+}
+template <class E> __device__ __forceinline__ E from_raw(double2 z) { return load_el<E>(z); }
+template <class E> __device__ __forceinline__ E from_raw(cdf z) { return z; }
 template <class E> __device__ __forceinline__ E zero_el();
 template <> __device__ __forceinline__ double2 zero_el<double2>() { return make_double2(0.0, 0.0); }
 template <> __device__ __forceinline__ cdf zero_el<cdf>() { return cdf{dfl{0.f, 0.f}, dfl{0.f, 0.f}}; }
@@ -76,10 +88,23 @@ __global__ void __launch_bounds__(256) lattice_axis_kernel(const void *in, void 
   }
   __syncthreads();
   const int tile = n * ncol;
-  for (int w = threadIdx.x; w < tile; w += blockDim.x) {
-    const int c = w & (ncol - 1), row = w >> lgcol;
-    const long bs = base[c];
-    a[d.rev[row] * ncol + c] = bs >= 0 ? load_in<E, IN_DF>(in, bs + (long)row * inner) : zero_el<E>();
+  // kLoadBatch loads per thread in flight before the first is converted and stored
+  for (int w0 = threadIdx.x; w0 < tile; w0 += kLoadBatch * blockDim.x) {
+    typename RawOf<IN_DF>::type v[kLoadBatch];
+#pragma unroll
+    for (int u = 0; u < kLoadBatch; ++u) {
+      const int w = w0 + u * blockDim.x;
+      const int c = w & (ncol - 1), row = w >> lgcol;
+      const long bs = w < tile ? base[c] : -1;
+      if (bs >= 0) v[u] = load_raw<E, IN_DF>(in, bs + (long)row * inner);
+    }
+#pragma unroll
+    for (int u = 0; u < kLoadBatch; ++u) {
+      const int w = w0 + u * blockDim.x;
+      if (w >= tile) break;
+      const int c = w & (ncol - 1), row = w >> lgcol;
+      a[d.rev[row] * ncol + c] = base[c] >= 0 ? from_raw<E>(v[u]) : zero_el<E>();
+    }
   }
   E *r = fft_smem<FWD>(a, b, d, ncol);
   const bool scaled = scale != 1.0;
@@ -151,11 +176,22 @@ __global__ void __launch_bounds__(256) lattice_plane_kernel(const void *in, void
   const long t0 = (blockIdx.x - o * tiles_t) * (long)nt;
   const int ntv = (int)min((long)nt, n_target - t0);
   const long gbase = o * P * n_target + t0;
-  for (int w = threadIdx.x; w < P * nt; w += blockDim.x) {
-    const int t = w & (nt - 1), p = w >> lgt;
-    const int i1 = p >> lg2, i2 = p & (n2 - 1);
-    a[((d1.rev[i1] << lg2) + d2.rev[i2]) * nt + t] =
-        t < ntv ? load_in<E, IN_DF>(in, gbase + (long)p * n_target + t) : zero_el<E>();
+  for (int w0 = threadIdx.x; w0 < P * nt; w0 += kLoadBatch * blockDim.x) {
+    typename RawOf<IN_DF>::type v[kLoadBatch];
+#pragma unroll
+    for (int u = 0; u < kLoadBatch; ++u) {
+      const int w = w0 + u * blockDim.x;
+      const int t = w & (nt - 1), p = w >> lgt;
+      if (w < P * nt && t < ntv) v[u] = load_raw<E, IN_DF>(in, gbase + (long)p * n_target + t);
+    }
+#pragma unroll
+    for (int u = 0; u < kLoadBatch; ++u) {
+      const int w = w0 + u * blockDim.x;
+      if (w >= P * nt) break;
+      const int t = w & (nt - 1), p = w >> lgt;
+      const int i1 = p >> lg2, i2 = p & (n2 - 1);
+      a[((d1.rev[i1] << lg2) + d2.rev[i2]) * nt + t] = t < ntv ? from_raw<E>(v[u]) : zero_el<E>();
+    }
   }
   // axis 2: columns (i1, t), element i2 at i1 * n2 * nt + i2 * nt + t
   fft_smem<FWD>(a, (E *)nullptr, d2, n1 * nt, -1, ColLayout{nt, n2 * nt, lgt});
