@@ -136,10 +136,22 @@ __global__ void __launch_bounds__(kMatsubaraThreads, 2) nu_to_tau_kernel(NuTauPl
   for (int w = tid; w < L * ic; w += nthr) a[w] = czero<C>();
   if (tid == 0) s_res = 0u;
   __syncthreads();
-  // frequency n sits at FFT row (n + L) % L, stored at its digit-reversed position
-  for (int w = tid; w < nnu * ic; w += nthr) {
-    const int c = w & (ic - 1), n = w >> lg;
-    if (c < ncol) a[rev[(n + p.in0 + L) % L] * ic + c] = from_d2<C>(gw[(long)n * Ccols + col0 + c]);
+  // frequency n sits at FFT row (n + L) % L, stored at its digit-reversed
+  // position; four loads per thread are in flight before the first is stored
+  for (int w0 = tid; w0 < nnu * ic; w0 += 4 * nthr) {
+    double2 v[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int w = w0 + u * nthr;
+      const int c = w & (ic - 1), n = w >> lg;
+      if (w < nnu * ic && c < ncol) v[u] = gw[(long)n * Ccols + col0 + c];
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int w = w0 + u * nthr;
+      const int c = w & (ic - 1), n = w >> lg;
+      if (w < nnu * ic && c < ncol) a[rev[(n + p.in0 + L) % L] * ic + c] = from_d2<C>(v[u]);
+    }
   }
   __syncthreads();
   if (mom == nullptr) {
