@@ -97,3 +97,37 @@ def test_every_rpa_group_size_gives_the_same_chi(cuda_lib, tmp_path):
         assert rel_err(chi, ref) < 1e-11, key
         assert rel_err(chi, out[(key[0], 8)]) < 1e-14, key
 
+
+
+@pytest.mark.parametrize("dims,n_target", [((32, 32, 4), 9), ((16, 8, 1), 81), ((8, 8, 2), 1), ((4, 8, 1), 5)])
+def test_tma_plane_pass_matches_the_plain_pass_and_numpy(cuda_lib, tmp_path, dims, n_target):
+    """The TMA-staged plane pass of the lattice FFT (forced through wisdom with
+    each tile size it accepts) gives the plain pass's transform, in place and out
+    of place, both directions, against numpy."""
+    from tprf_gb300 import _native, tuning
+    rng = np.random.default_rng(3)
+    n_w, nk = 3, int(np.prod(dims))
+    x = rng.standard_normal((n_w, nk, n_target)) + 1j * rng.standard_normal((n_w, nk, n_target))
+    xd = torch.as_tensor(x, device="cuda").contiguous()
+    nontriv = [d for d in dims if d > 1]
+    n1, n2 = nontriv[-2], nontriv[-1]
+    lib = cuda_lib
+    ref_f = np.fft.fftn(x.reshape((n_w,) + dims + (n_target,)), axes=(1, 2, 3)).reshape(x.shape) / nk
+    ref_b = np.fft.ifftn(x.reshape((n_w,) + dims + (n_target,)), axes=(1, 2, 3)).reshape(x.shape) * nk
+    try:
+        for nt in (0, 1, 2, 4, 8, 16):
+            tuning.set_autotune(False)
+            tuning.clear_wisdom()
+            w = tmp_path / f"p{nt}.txt"
+            w.write_text(f"{_device_prefix()}/lattice_plane_tma/0/{n1}/{n2}/{n_target} {nt}\n")
+            tuning.load_wisdom(w)
+            for fn, ref in ((lib.tprf_fourier_wk_to_wr, ref_f), (lib.tprf_fourier_wr_to_wk, ref_b)):
+                out = torch.empty_like(xd)
+                _native.check(fn(n_w, _native.dims3(dims), n_target, xd.data_ptr(), out.data_ptr(), None))
+                inplace = xd.clone()
+                _native.check(fn(n_w, _native.dims3(dims), n_target, inplace.data_ptr(), inplace.data_ptr(), None))
+                torch.cuda.synchronize()
+                assert rel_err(out, ref) < 1e-13, (nt, fn)
+                assert rel_err(inplace, ref) < 1e-13, (nt, fn)
+    finally:
+        tuning.clear_wisdom()

@@ -298,6 +298,63 @@ __device__ C *fft_smem(C *a, C *b, const FftDesc &d, int ncol, int n_stages = -1
   return a;
 }
 
+// Decimation in frequency: natural order in, digit-reversed order out (output
+// t at position FftDesc::rev[t]). The DFT matrix is symmetric, so transposing
+// the DIT factorisation F = S_last ... S_0 P (S_s = butterflies after
+// twiddles) gives F = P^T (T_0 B_0) ... (T_last B_last): the same stages in
+// reverse order, each butterfly first and its twiddles after. Lets a tile be
+// loaded in natural order (bulk copies) and permuted on the way out instead.
+template <int R, bool FWD, class C>
+__device__ __forceinline__ void fft_stage_dif(C *__restrict__ a, int n, int Ns, int ncol, const C *__restrict__ tw,
+                                              ColLayout lay) {
+  const int nbf = n / R;
+  const int tws = n / (Ns * R);
+  const int cb = lay.cbase(threadIdx.x % ncol);
+  const int j0 = threadIdx.x / ncol;
+  const int step = blockDim.x / ncol;
+  const int kstep = step % Ns;
+  int k = j0 % Ns;
+  for (int j = j0; j < nbf; j += step) {
+    const int base = (j - k) * R + k;
+    C v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = a[(base + r * Ns) * lay.stride + cb];
+    Dft<R, FWD, C>::run(v);
+    if (Ns > 1) {
+#pragma unroll
+      for (int r = 1; r < R; ++r) v[r] = cmul(v[r], root<FWD>(tw, k * r * tws));
+    }
+#pragma unroll
+    for (int r = 0; r < R; ++r) a[(base + r * Ns) * lay.stride + cb] = cnorm(v[r]);
+    k += kstep;
+    if (k >= Ns) k -= Ns;
+  }
+}
+
+// The full DIF transform of the `ncol` columns of buffer a, in place; plans
+// with a generic-radix stage are not supported here (use fft_smem). Starts and
+// ends with a barrier.
+template <bool FWD, class C>
+__device__ void fft_smem_dif(C *a, const FftDesc &d, int ncol, ColLayout lay = ColLayout{0, 0, 30}) {
+  __syncthreads();
+  const C *tw = twiddles<C>(d);
+  if (lay.stride == 0) lay = interleaved(ncol);
+  int Ns = d.n;
+  for (int s = d.nst - 1; s >= 0; --s) {
+    const int R = d.radix[s];
+    Ns /= R;
+    switch (R) {
+      case 2: fft_stage_dif<2, FWD>(a, d.n, Ns, ncol, tw, lay); break;
+      case 3: fft_stage_dif<3, FWD>(a, d.n, Ns, ncol, tw, lay); break;
+      case 4: fft_stage_dif<4, FWD>(a, d.n, Ns, ncol, tw, lay); break;
+      case 5: fft_stage_dif<5, FWD>(a, d.n, Ns, ncol, tw, lay); break;
+      case 7: fft_stage_dif<7, FWD>(a, d.n, Ns, ncol, tw, lay); break;
+      default: fft_stage_dif<8, FWD>(a, d.n, Ns, ncol, tw, lay); break;
+    }
+    __syncthreads();
+  }
+}
+
 // One output i of the last DIT stage (radix R, Ns = n / R) computed directly
 // from the buffer left by the other stages: X[i] = sum_r W_n^{r i} v[i mod Ns + r Ns]
 // (the butterfly k = i mod Ns, its output q = i / Ns, with the twiddle and the

@@ -21,6 +21,9 @@
 #include <type_traits>
 
 #include "common.cuh"
+#include "tma.cuh"
+
+#include <cudaTypedefs.h>
 
 namespace tprf {
 namespace {
@@ -205,6 +208,84 @@ __global__ void __launch_bounds__(256) lattice_plane_kernel(const void *in, void
   }
 }
 
+// TMA-staged form of the plane pass (double-float arithmetic): persistent CTAs
+// with two tile buffers. While the transforms of one tile run, the TMA unit
+// copies the CTA's next tile into the other buffer (one 4-D box per tile,
+// [i1][i2][t] in natural order as the box lays it out), so the tile loads no
+// longer wait on DRAM latency. The transforms run decimation-in-frequency on
+// the natural-order tile and the store reads the digit-reversed positions.
+// Double-float input lands as it is; complex128 input is converted in place.
+constexpr long kTmaMaxTries = 1L << 22;  // mbarrier probes before a wait gives up
+
+template <bool FWD, bool IN_DF, bool OUT_DF>
+__global__ void __launch_bounds__(256) lattice_plane_tma_kernel(const __grid_constant__ CUtensorMap map, void *out,
+                                                                long outer, long n_target, int nt, int lgt, FftDesc d1,
+                                                                FftDesc d2, int lg2, double scale, unsigned *status) {
+  using E = cdf;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  const int n1 = d1.n, n2 = d2.n, P = n1 * n2, tile_elems = P * nt;
+  E *buf0 = reinterpret_cast<E *>(smem_raw);
+  E *buf1 = buf0 + tile_elems;
+  uint64_t *bar = reinterpret_cast<uint64_t *>(buf1 + tile_elems);
+  const long tiles_t = (n_target + nt - 1) / nt;
+  const long n_tiles = outer * tiles_t;
+  const uint32_t tile_bytes = (uint32_t)tile_elems * 16u;
+  auto issue = [&](long tile, int b) {
+    const long o = tile / tiles_t;
+    const int t0 = (int)((tile - o * tiles_t) * nt);
+    mbar_arrive_expect_tx(&bar[b], tile_bytes);
+    tma_load_4d(b ? buf1 : buf0, &map, 2 * t0, 0, 0, (int)o, &bar[b]);
+  };
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_mbar_init();
+    fence_async_shared();
+    if ((long)blockIdx.x < n_tiles) issue(blockIdx.x, 0);
+  }
+  __syncthreads();
+  const bool scaled = scale != 1.0;
+  const dfl sd = split_double(scale);
+  int k = 0;
+  for (long tile = blockIdx.x; tile < n_tiles; tile += gridDim.x, ++k) {
+    const int b = k & 1;
+    const long nxt = tile + gridDim.x;
+    if (threadIdx.x == 0 && nxt < n_tiles) {
+      fence_async_shared();  // this CTA's earlier accesses to that buffer precede the copy
+      issue(nxt, b ^ 1);
+    }
+    const bool ok = mbar_wait_bounded(&bar[b], (uint32_t)((k >> 1) & 1), kTmaMaxTries);
+    if (__syncthreads_or(!ok)) {
+      // give the copy in flight a bounded chance to land before leaving
+      if (threadIdx.x == 0) {
+        atomicOr(status, kDevErrTimeout);
+        if (nxt < n_tiles) mbar_wait_bounded(&bar[b ^ 1], (uint32_t)(((k + 1) >> 1) & 1), kTmaMaxTries);
+      }
+      return;
+    }
+    E *a = b ? buf1 : buf0;
+    if constexpr (!IN_DF) {
+      for (int w = threadIdx.x; w < tile_elems; w += blockDim.x) a[w] = to_cdf(reinterpret_cast<const double2 *>(a)[w]);
+    }
+    // axis 2: columns (i1, t), element i2 at i1 * n2 * nt + i2 * nt + t
+    fft_smem_dif<FWD>(a, d2, n1 * nt, ColLayout{nt, n2 * nt, lgt});
+    // axis 1: columns (i2, t), element i1 at i1 * n2 * nt + (i2 * nt + t)
+    fft_smem_dif<FWD>(a, d1, n2 * nt);
+    const long o = tile / tiles_t;
+    const long t0 = (tile - o * tiles_t) * (long)nt;
+    const int ntv = (int)min((long)nt, n_target - t0);
+    const long gbase = o * P * n_target + t0;
+    for (int w = threadIdx.x; w < tile_elems; w += blockDim.x) {
+      const int t = w & (nt - 1), p = w >> lgt;
+      const int i1 = p >> lg2, i2 = p & (n2 - 1);
+      if (t < ntv)
+        store_out<E, OUT_DF>(out, gbase + (long)p * n_target + t, a[((d1.rev[i1] << lg2) + d2.rev[i2]) * nt + t],
+                             scale, sd, scaled);
+    }
+    __syncthreads();  // the buffer is free for the tile after next
+  }
+}
+
 bool pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
 int log2i(int n) {
   int l = 0;
@@ -256,6 +337,77 @@ int launch_plane(const void *in, bool in_df, void *out, bool out_df, long outer,
   if (in_df) return launch_plane_as<FWD, cdf, true, false>(in, out, outer, n1, n2, n_target, scale, stream);
   if (out_df) return launch_plane_as<FWD, cdf, false, true>(in, out, outer, n1, n2, n_target, scale, stream);
   return launch_plane_as<FWD, cdf, false, false>(in, out, outer, n1, n2, n_target, scale, stream);
+}
+
+// The TMA-staged plane pass with nt targets per tile (two tiles per CTA).
+constexpr int kNotApplicable = 1;
+
+template <bool FWD>
+int launch_plane_tma_nt(const void *in, bool in_df, void *out, bool out_df, long outer, int n1, int n2,
+                        long n_target, double scale, cudaStream_t stream, int nt) {
+  const int P = n1 * n2;
+  FftDesc d1, d2;
+  int st = get_fft(n1, &d1);
+  if (st) return st;
+  if ((st = get_fft(n2, &d2))) return st;
+  unsigned *status = device_status_word();
+  if (!status) return TPRF_ERR_CUDA;
+  // the array as FP64 words: [outer][n1][n2][n_target][2]
+  const uint64_t dims[4] = {2 * (uint64_t)n_target, (uint64_t)n2, (uint64_t)n1, (uint64_t)outer};
+  const uint64_t strides[3] = {16 * (uint64_t)n_target, 16 * (uint64_t)n_target * n2,
+                               16 * (uint64_t)n_target * n2 * n1};
+  const uint32_t box[4] = {2 * (uint32_t)nt, (uint32_t)n2, (uint32_t)n1, 1};
+  CUtensorMap map;
+  if ((st = encode_tensor_map_f64(&map, in, 4, dims, strides, box))) return st;
+  const size_t smem = 2 * (size_t)P * nt * 16 + 16;
+  const long tiles = outer * ((n_target + nt - 1) / nt);
+  void (*kern)(const CUtensorMap, void *, long, long, int, int, FftDesc, FftDesc, int, double, unsigned *);
+  if (in_df)
+    kern = out_df ? lattice_plane_tma_kernel<FWD, true, true> : lattice_plane_tma_kernel<FWD, true, false>;
+  else
+    kern = out_df ? lattice_plane_tma_kernel<FWD, false, true> : lattice_plane_tma_kernel<FWD, false, false>;
+  TPRF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0;
+  TPRF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, smem));
+  const long grid = std::max(1L, std::min(tiles, (long)num_sms() * std::max(1, per_sm)));
+  kern<<<(unsigned)grid, 256, smem, stream>>>(map, out, outer, n_target, nt, log2i(nt), d1, d2, log2i(n2), scale,
+                                              status);
+  TPRF_LAUNCH_CHECK("lattice_plane_tma_kernel");
+  return TPRF_OK;
+}
+
+// The plane pass: the TMA-staged form with the tile size the wisdom names
+// (autotuner: measure mode on an out-of-place call, or tprf_autotune_load),
+// else the plain form (kNotApplicable tells the caller to run it).
+template <bool FWD>
+int launch_plane_tma(const void *in, bool in_df, void *out, bool out_df, long outer, int n1, int n2, long n_target,
+                     double scale, cudaStream_t stream) {
+  if (arith_mode() == kArithFP64 || (reinterpret_cast<uintptr_t>(in) & 15) || outer > 0x7fffffffL ||
+      2 * n_target > 0x7fffffffL || plane_targets(n1, n2, n_target) < 1)
+    return kNotApplicable;
+  const int P = n1 * n2;
+  auto fits = [&](int nt) {
+    return n1 * nt <= 256 && n2 * nt <= 256 && 256 % (n1 * nt) == 0 && 256 % (n2 * nt) == 0 &&
+           ((size_t)P * nt * 16) % 128 == 0 && 2 * (size_t)P * nt * 16 + 16 <= (size_t)max_smem_optin() &&
+           (nt == 1 || nt / 2 < n_target);
+  };
+  std::vector<int> cands = {0};  // 0: the plain pass
+  for (int c = 1; c <= 16; c *= 2)
+    if (fits(c)) cands.push_back(c);
+  const std::string key = tune_key("lattice_plane_tma", {n1, n2, n_target});
+  int nt = 0, st;
+  if (in != (const void *)out) {
+    auto trial = [&](int v) -> int {
+      return v == 0 ? launch_plane<FWD>(in, in_df, out, out_df, outer, n1, n2, n_target, scale, stream)
+                    : launch_plane_tma_nt<FWD>(in, in_df, out, out_df, outer, n1, n2, n_target, scale, stream, v);
+    };
+    st = tune_pick(key, cands, 0, stream, trial, &nt);
+  } else {
+    st = tune_lookup(key, cands, 0, &nt);  // in place: a trial would transform the data twice
+  }
+  if (st) return st;
+  if (nt == 0) return kNotApplicable;
+  return launch_plane_tma_nt<FWD>(in, in_df, out, out_df, outer, n1, n2, n_target, scale, stream, nt);
 }
 
 }  // namespace
@@ -313,9 +465,14 @@ int launch_lattice_fft_fmt(bool forward, long n_w, const int dims[3], long n_tar
       for (int a2 = 0; a2 < A; ++a2) outer *= dims[a2];
       const double scale = (nn == 2) ? scale_last : 1.0;
       const bool plane_out_df = (nn == 3) ? mid_df : out_df;
-      int st = forward ? launch_plane<true>(in, in_df, out, plane_out_df, outer, dims[A], dims[B], n_target, scale, stream)
-                       : launch_plane<false>(in, in_df, out, plane_out_df, outer, dims[A], dims[B], n_target, scale,
-                                             stream);
+      int st = forward ? launch_plane_tma<true>(in, in_df, out, plane_out_df, outer, dims[A], dims[B], n_target, scale,
+                                                stream)
+                       : launch_plane_tma<false>(in, in_df, out, plane_out_df, outer, dims[A], dims[B], n_target, scale,
+                                                 stream);
+      if (st == kNotApplicable)
+        st = forward ? launch_plane<true>(in, in_df, out, plane_out_df, outer, dims[A], dims[B], n_target, scale, stream)
+                     : launch_plane<false>(in, in_df, out, plane_out_df, outer, dims[A], dims[B], n_target, scale,
+                                           stream);
       if (st) return st;
       if (nn == 3) {
         const int ax = nontriv[0];
@@ -347,6 +504,39 @@ int launch_lattice_fft_fmt(bool forward, long n_w, const int dims[3], long n_tar
     src = out;
     src_df = dst_df;
   }
+  return TPRF_OK;
+}
+
+int encode_tensor_map_f64(CUtensorMap *map, const void *base, int rank, const uint64_t *dims,
+                          const uint64_t *strides_bytes, const uint32_t *box) {
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  });
+  if (!encode) return set_error(TPRF_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
+  if (rank < 1 || rank > 5 || (reinterpret_cast<uintptr_t>(base) & 15) || (box[0] * 8u) % 16u)
+    return set_error(TPRF_ERR_INVALID_ARGUMENT, "tensor map: bad rank, base alignment or inner box");
+  cuuint64_t gd[5], gs[4];
+  cuuint32_t bx[5], es[5];
+  for (int i = 0; i < rank; ++i) {
+    if (box[i] < 1 || box[i] > 256 || dims[i] < 1) return set_error(TPRF_ERR_INVALID_ARGUMENT, "tensor map: box");
+    gd[i] = dims[i];
+    bx[i] = box[i];
+    es[i] = 1;
+  }
+  for (int i = 0; i + 1 < rank; ++i) {
+    if (strides_bytes[i] % 16) return set_error(TPRF_ERR_INVALID_ARGUMENT, "tensor map: stride not a multiple of 16");
+    gs[i] = strides_bytes[i];
+  }
+  const CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, (cuuint32_t)rank, const_cast<void *>(base), gd, gs,
+                            bx, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return set_error(TPRF_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
   return TPRF_OK;
 }
 

@@ -155,6 +155,8 @@ int launch_rpa_adjoint(long n_points, int nb, const double2 *chi0, const double2
 // fallback.
 int tune_mode();
 std::string tune_key(const char *kernel, std::initializer_list<long> shape);
+// The wisdom value of `key` among the candidates, else the fallback; never times anything.
+int tune_lookup(const std::string &key, const std::vector<int> &candidates, int fallback, int *choice);
 int tune_pick(const std::string &key, const std::vector<int> &candidates, int fallback, cudaStream_t s,
               const std::function<int(int)> &launch, int *choice);
 

@@ -61,6 +61,15 @@ std::string tune_key(const char *kernel, std::initializer_list<long> shape) {
   return k.str();
 }
 
+int tune_lookup(const std::string &key, const std::vector<int> &candidates, int fallback, int *choice) {
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  auto it = g_wisdom.find(key);
+  const bool hit =
+      it != g_wisdom.end() && std::find(candidates.begin(), candidates.end(), it->second) != candidates.end();
+  *choice = hit ? it->second : fallback;
+  return TPRF_OK;
+}
+
 int tune_pick(const std::string &key, const std::vector<int> &candidates, int fallback, cudaStream_t s,
               const std::function<int(int)> &launch, int *choice) {
   {
