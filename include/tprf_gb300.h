@@ -77,9 +77,12 @@ int tprf_get_arithmetic(void);
  * (default) uses fixed heuristics here too; mode 1 ("measure", as FFTW_MEASURE)
  * times every candidate on the first call of each shape and keeps the fastest:
  * columns per CTA of the iv -> tau and tau -> i omega kernels (fused bubble
- * included), lanes per point of the RPA group kernel (nb >= 3). Candidates run
- * on a prefix of the call's own columns or points (out-of-place kernels only),
- * so results do not depend on the mode. A tuning call waits for its stream;
+ * included), lanes per point of the RPA group kernel (nb >= 3), threads per
+ * CTA of the Dyson kernel, and the tile size of the TMA-staged lattice plane
+ * pass (0 = the plain pass; in-place calls only read it from wisdom).
+ * Candidates run on a prefix of the call's own columns or points, or on the
+ * whole call (out-of-place kernels only), so results do not depend on the mode
+ * beyond rounding (the TMA plane pass rounds as a decimation-in-frequency FFT). A tuning call waits for its stream;
  * tuning is skipped while the stream is being captured. The choices ("wisdom")
  * are process-wide, keyed by GPU, arithmetic mode, kernel and shape, and can be
  * saved to and loaded from a text file ("key value" per line). */

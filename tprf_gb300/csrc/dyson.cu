@@ -130,13 +130,23 @@ template <int NB>
 int launch_dyson_nb(double beta, int n_iw, long n_k, double mu, const double2 *e_k, const double2 *sigma,
                     int sigma_kind, double2 *g, cudaStream_t stream, unsigned *status) {
   const long total = 2L * n_iw * n_k;
-  const int threads = 128;
-  long blocks = (total + threads - 1) / threads;
-  const long cap = (long)num_sms() * 16;
-  if (blocks > cap) blocks = cap;
-  dyson_kernel<NB><<<(unsigned)blocks, threads, 0, stream>>>(beta, n_iw, n_k, mu, e_k, sigma, sigma_kind, g, status);
-  TPRF_LAUNCH_CHECK("dyson_kernel");
-  return TPRF_OK;
+  // threads per CTA (at most the kernel's bound of 128): 128 unless the
+  // autotuner measured another (the kernel is out of place, so a trial run
+  // recomputes the same G)
+  auto launch = [&](int threads) -> int {
+    long blocks = (total + threads - 1) / threads;
+    const long cap = (long)num_sms() * 2048 / threads;
+    if (blocks > cap) blocks = cap;
+    dyson_kernel<NB><<<(unsigned)blocks, threads, 0, stream>>>(beta, n_iw, n_k, mu, e_k, sigma, sigma_kind, g, status);
+    TPRF_LAUNCH_CHECK("dyson_kernel");
+    return TPRF_OK;
+  };
+  int threads = 128;
+  if ((const void *)e_k != (const void *)g && (const void *)sigma != (const void *)g) {
+    int st = tune_pick(tune_key("dyson", {NB, sigma_kind}), {32, 64, 128}, 128, stream, launch, &threads);
+    if (st) return st;
+  }
+  return launch(threads);
 }
 
 }  // namespace
