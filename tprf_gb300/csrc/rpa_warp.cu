@@ -97,8 +97,9 @@ __device__ __forceinline__ void group_argmax(MagT &best, int &p, unsigned gmask)
 // return the right half holds A^-1 B and the left half the LU factors.
 // Lanes own columns; the pivot search is a shuffle argmax inside the group.
 // Returns the smallest squared pivot magnitude; sets `sing` on a zero pivot.
-template <class E, int G>
-__device__ __forceinline__ typename Mag<E>::type solve_augmented(E *M, int N, int lane, unsigned gmask, bool &sing) {
+template <class E, int G, int NC = 0>
+__device__ __forceinline__ typename Mag<E>::type solve_augmented(E *M, int N_in, int lane, unsigned gmask, bool &sing) {
+  const int N = NC > 0 ? NC : N_in;  // a compile-time size when NC > 0
   const int W = 2 * N;
 #define MM(i, c) M[(i) * W + (c)]
   using MagT = typename Mag<E>::type;
@@ -150,9 +151,11 @@ __device__ __forceinline__ typename Mag<E>::type solve_augmented(E *M, int N, in
   return pmin;
 }
 
-template <class E, int G>
-__device__ double rpa_point_warp(const double2 *__restrict__ x, double2 *__restrict__ y, E *M, int N, int nb,
+template <class E, int G, int NBC = 0>
+__device__ double rpa_point_warp(const double2 *__restrict__ x, double2 *__restrict__ y, E *M, int N_in, int nb_in,
                                  const SparseU &u, int lane, unsigned gmask, bool &singular) {
+  const int nb = NBC > 0 ? NBC : nb_in;  // a compile-time size when NBC > 0
+  const int N = NBC > 0 ? NBC * NBC : N_in;
   const int W = 2 * N;
 #define MM(i, c) M[(i) * W + (c)]
   // B = chi0 in the grouped layout (coalesced global reads)
@@ -176,7 +179,7 @@ __device__ double rpa_point_warp(const double2 *__restrict__ x, double2 *__restr
   __syncwarp(gmask);
 #undef MM
   bool sing = false;
-  const auto pmin = solve_augmented<E, G>(M, N, lane, gmask, sing);
+  const auto pmin = solve_augmented<E, G, NBC * NBC>(M, N, lane, gmask, sing);
   singular = sing;
   for (int o = lane; o < N * N; o += G) y[o] = el_to(M[(o / N) * 2 * N + N + col_of_offset(o % N, nb)]);
   amax = group_max<G>(amax, gmask);
@@ -186,10 +189,11 @@ __device__ double rpa_point_warp(const double2 *__restrict__ x, double2 *__restr
 }
 
 
-template <class E, int G>
-__global__ void __launch_bounds__(512) rpa_warp_kernel(long n_points, int nb, const double2 *__restrict__ chi0,
+template <class E, int G, int NBC = 0>
+__global__ void __launch_bounds__(512) rpa_warp_kernel(long n_points, int nb_in, const double2 *__restrict__ chi0,
                                                        const double2 *__restrict__ U, double2 *__restrict__ chi,
                                                        unsigned *status) {
+  const int nb = NBC > 0 ? NBC : nb_in;
   const int N = nb * nb;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   double2 *s_val = reinterpret_cast<double2 *>(smem_raw);
@@ -227,14 +231,14 @@ __global__ void __launch_bounds__(512) rpa_warp_kernel(long n_points, int nb, co
     const double2 *x = chi0 + pt * N * N;
     double2 *y = chi + pt * N * N;
     bool singular = false;
-    const double cond2 = rpa_point_warp<E, G>(x, y, M, N, nb, u, lane, gmask, singular);
+    const double cond2 = rpa_point_warp<E, G, NBC>(x, y, M, N, nb, u, lane, gmask, singular);
     if (IsDf<E>::value && !(cond2 <= kDf64CondLimit2))
-      rpa_point_warp<double2, G>(x, y, reinterpret_cast<double2 *>(M), N, nb, u, lane, gmask, singular);
+      rpa_point_warp<double2, G, NBC>(x, y, reinterpret_cast<double2 *>(M), N, nb, u, lane, gmask, singular);
     if (singular && lane == 0) atomicOr(status, kDevErrSingular);
   }
 }
 
-template <class E, int G>
+template <class E, int G, int NBC = 0>
 int launch_as(long n_points, int nb, const double2 *chi0, const double2 *U, double2 *chi, cudaStream_t stream,
               unsigned *status) {
   const int N = nb * nb;
@@ -243,14 +247,14 @@ int launch_as(long n_points, int nb, const double2 *chi0, const double2 *U, doub
   const int ppw = 32 / G;  // points per warp
   const size_t limit = (size_t)max_smem_optin();
   if (u_bytes + ppw * per_point > limit) return set_error(TPRF_ERR_INVALID_ARGUMENT, "solve_rpa_PH: nb too large");
-  TPRF_CUDA(cudaFuncSetAttribute(rpa_warp_kernel<E, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)limit));
+  TPRF_CUDA(cudaFuncSetAttribute(rpa_warp_kernel<E, G, NBC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)limit));
   // the number of warps per CTA that puts the most warps on an SM
   int best_w = 1, best_total = 0;
   for (int w = 1; w <= 16; ++w) {
     const size_t smem = u_bytes + (size_t)w * ppw * per_point;
     if (smem > limit) break;
     int per_sm = 0;
-    TPRF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, rpa_warp_kernel<E, G>, 32 * w, smem));
+    TPRF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, rpa_warp_kernel<E, G, NBC>, 32 * w, smem));
     if (per_sm * w >= best_total) {
       best_total = per_sm * w;
       best_w = w;
@@ -261,16 +265,25 @@ int launch_as(long n_points, int nb, const double2 *chi0, const double2 *U, doub
   const long per_block = (long)best_w * ppw;
   long blocks = (n_points + per_block - 1) / per_block;
   blocks = std::max(1L, std::min(blocks, (long)num_sms() * (best_total / best_w) * 8));
-  rpa_warp_kernel<E, G><<<(unsigned)blocks, 32 * best_w, smem, stream>>>(n_points, nb, chi0, U, chi, status);
+  rpa_warp_kernel<E, G, NBC><<<(unsigned)blocks, 32 * best_w, smem, stream>>>(n_points, nb, chi0, U, chi, status);
   TPRF_LAUNCH_CHECK("rpa_warp_kernel");
   return TPRF_OK;
 }
 
+// Sizes compiled in full: nb = 3 (9 x 9) and nb = 5 (25 x 25); other vertex
+// sizes run the runtime-sized form of the same kernel.
 template <int G>
 int launch_g(long n_points, int nb, const double2 *chi0, const double2 *U, double2 *chi, cudaStream_t stream,
              unsigned *status) {
-  if (arith_mode() == kArithFP64) return launch_as<double2, G>(n_points, nb, chi0, U, chi, stream, status);
-  return launch_as<cdf, G>(n_points, nb, chi0, U, chi, stream, status);
+  const bool fp64 = arith_mode() == kArithFP64;
+  if (nb == 3)
+    return fp64 ? launch_as<double2, G, 3>(n_points, nb, chi0, U, chi, stream, status)
+                : launch_as<cdf, G, 3>(n_points, nb, chi0, U, chi, stream, status);
+  if (nb == 5 && G >= 16)
+    return fp64 ? launch_as<double2, G, 5>(n_points, nb, chi0, U, chi, stream, status)
+                : launch_as<cdf, G, 5>(n_points, nb, chi0, U, chi, stream, status);
+  return fp64 ? launch_as<double2, G>(n_points, nb, chi0, U, chi, stream, status)
+              : launch_as<cdf, G>(n_points, nb, chi0, U, chi, stream, status);
 }
 
 // ---- screened interaction W ---------------------------------------------------------
@@ -481,10 +494,10 @@ __global__ void __launch_bounds__(512) rpa_adjoint_warp_kernel(long n_points, in
 
 }  // namespace
 
-// lanes per point (measured on GB300: nb = 3 8 lanes, 102 ms for 16.7 M points,
-// against 109 ms with 16 lanes; nb = 5 32 lanes, 1.08 s for 8.4 M points,
-// against 1.61 s with 16)
-int rpa_group_lanes(int nb) { return nb <= 3 ? 8 : 32; }
+// lanes per point (measured on GB300 with the compiled sizes: nb = 3 9 lanes,
+// 90.2 ms for 16.7 M points, against 92.9 ms with 8 and 97.1 ms with 16;
+// nb = 5 32 lanes, 248 ms for 2.1 M points, against 376 ms with 16)
+int rpa_group_lanes(int nb) { return nb <= 2 ? 8 : nb == 3 ? 9 : 32; }
 
 int launch_rpa_warp(long n_points, int nb, const double2 *chi0, const double2 *U, double2 *chi, cudaStream_t stream,
                     unsigned *status) {
