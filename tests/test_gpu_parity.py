@@ -136,6 +136,12 @@ CASES = [
     (lambda: {(0, 1): -np.eye(1), (0, -1): -np.eye(1), (1, 0): -np.eye(1), (-1, 0): -np.eye(1)}, (8, 8, 1), 10.0, 64),
     (lambda: __import__("tprf_gb300.workloads", fromlist=["x"]).cubic_3orb(0), (4, 4, 4), 20.0, 32),
     (lambda: __import__("tprf_gb300.workloads", fromlist=["x"]).square_2orb(1), (6, 6, 1), 5.0, 45),
+    # complex hoppings: G(tau, r) is complex, the bubble keeps one FFT per column
+    (lambda: {(1, 0): np.array([[-1.0, 0.3j], [0.2j, -0.8]]), (-1, 0): np.array([[-1.0, 0.3j], [0.2j, -0.8]]).conj().T,
+              (0, 1): np.array([[-0.5, 0.1], [-0.4j, -1.0]]), (0, -1): np.array([[-0.5, 0.1], [-0.4j, -1.0]]).conj().T},
+     (6, 4, 1), 8.0, 40),
+    # real hoppings with an odd number of bubble columns (25 x 81): the last real pair has one column
+    (lambda: __import__("tprf_gb300.workloads", fromlist=["x"]).cubic_3orb(2), (5, 5, 1), 6.0, 30),
 ]
 
 

@@ -30,8 +30,6 @@ int launch_chi0_wr_from_grt(double beta, int n_tau, int nw, const int dims[3], i
                             double2 *chi0_wr, cudaStream_t stream);
 int launch_chi0_w0r_from_grt(double beta, int n_tau, const int dims[3], int nb, const double2 *g, double2 *chi0_wr,
                              cudaStream_t stream);
-int launch_nu_to_tau_df(double beta, int n_iw, int n_tau, long C, const double2 *gw, const double2 *mom, double2 *gt,
-                        void *gt_df, cudaStream_t stream);
 int launch_rpa(long n_points, int nb, const double2 *chi0, const double2 *U, double2 *chi, cudaStream_t stream);
 }  // namespace tprf
 
@@ -56,7 +54,7 @@ int inst_ntau(const tprf_instance &a) { return a.n_tau < 0 ? default_n_tau(a.n_i
 size_t al16(size_t n) { return (n * sizeof(double2) + 255) & ~size_t(255); }
 
 // Scratch layout of one instance (element counts; every part 256-byte aligned):
-//   G(iv, k) | G(iv, r) | G(tau, r) | double-float G(tau, r) | chi0(w, q) | chi0(tau, r) gradient
+//   256 B | G(iv, k) | G(iv, r) | G(tau, r) | double-float G(tau, r) | chi0(w, q) | chi0(tau, r) gradient
 // The forward pass uses the first five (chi0 only when the caller does not keep
 // it); the backward pass reuses them for the gradients of the same shapes.
 struct Layout {
@@ -68,10 +66,13 @@ struct Layout {
     c = (size_t)(2 * a.nw - 1) * nk * nb4;
     ct = (size_t)inst_ntau(a) * nk * nb4;
   }
-  size_t off_gwr() const { return al16(g); }
-  size_t off_gtr() const { return 2 * al16(g); }
-  size_t off_gdf() const { return 2 * al16(g) + al16(gt); }
-  size_t off_c() const { return 2 * al16(g) + 2 * al16(gt); }
+  // 256 bytes first: the max |G|, max |Im G| words of the real-pair test
+  static constexpr size_t kHdr = 256;
+  size_t off_gwk() const { return kHdr; }
+  size_t off_gwr() const { return kHdr + al16(g); }
+  size_t off_gtr() const { return kHdr + 2 * al16(g); }
+  size_t off_gdf() const { return kHdr + 2 * al16(g) + al16(gt); }
+  size_t off_c() const { return kHdr + 2 * al16(g) + 2 * al16(gt); }
   size_t off_ct() const { return off_c() + al16(c); }
   size_t forward_bytes() const { return off_c() + al16(c); }
   size_t grad_bytes() const { return off_ct() + al16(ct); }
@@ -148,7 +149,8 @@ int enqueue_instance(const tprf_instance &a, unsigned char *scratch, cudaStream_
   const long nk = inst_nk(a), nb2 = (long)a.nb * a.nb, nb4 = nb2 * nb2;
   const int nt = inst_ntau(a);
   const Layout L(a);
-  double2 *g_wk = reinterpret_cast<double2 *>(scratch);
+  unsigned *gmax = reinterpret_cast<unsigned *>(scratch);
+  double2 *g_wk = reinterpret_cast<double2 *>(scratch + L.off_gwk());
   double2 *g_wr = reinterpret_cast<double2 *>(scratch + L.off_gwr());
   double2 *g_tr = reinterpret_cast<double2 *>(scratch + L.off_gtr());
   void *g_tr_df = scratch + L.off_gdf();
@@ -156,12 +158,13 @@ int enqueue_instance(const tprf_instance &a, unsigned char *scratch, cudaStream_
   int st = launch_dyson(a.beta, a.n_iw, nk, a.nb, a.mu, reinterpret_cast<const double2 *>(a.e_k), nullptr, 0, g_wk, s);
   if (st) return st;
   if ((st = launch_lattice_fft(true, 2L * a.n_iw, a.dims, nb2, g_wk, g_wr, s))) return st;
-  if ((st = launch_nu_to_tau_df(a.beta, a.n_iw, nt, nk * nb2, g_wr, nullptr, g_tr, g_tr_df, s))) return st;
+  TPRF_CUDA(cudaMemsetAsync(gmax, 0, 2 * sizeof(unsigned), s));
+  if ((st = launch_nu_to_tau_df(a.beta, a.n_iw, nt, nk * nb2, g_wr, nullptr, g_tr, g_tr_df, s, gmax))) return st;
   bool chi_df = false;  // chi0(w, r) handed to r -> q as double-float pairs (as the single-instance chain)
   if (a.nw == 1)
     st = launch_chi0_w0r_from_grt(a.beta, nt, a.dims, a.nb, g_tr, chi0, s);
   else
-    st = launch_chi0_wr_from_grt_df(a.beta, nt, a.nw, a.dims, a.nb, g_tr, g_tr_df, chi0, s, nk > 1, &chi_df);
+    st = launch_chi0_wr_from_grt_df(a.beta, nt, a.nw, a.dims, a.nb, g_tr, g_tr_df, chi0, s, nk > 1, &chi_df, gmax);
   if (st) return st;
   if ((st = launch_lattice_fft_fmt(false, 2L * a.nw - 1, a.dims, nb4, chi0, chi_df, chi0, false, 1.0, s))) return st;
   return launch_rpa((2L * a.nw - 1) * nk, a.nb, chi0, reinterpret_cast<const double2 *>(a.U),
@@ -178,7 +181,7 @@ int enqueue_backward(const tprf_grad_instance &gi, unsigned char *scratch, cudaS
   const int nt = inst_ntau(a), nwt = 2 * a.nw - 1;
   const Layout L(a);
   auto at = [&](size_t off) { return reinterpret_cast<double2 *>(scratch + off); };
-  double2 *g_wk = at(0), *g_wr = at(L.off_gwr()), *g_tr = at(L.off_gtr());
+  double2 *g_wk = at(L.off_gwk()), *g_wr = at(L.off_gwr()), *g_tr = at(L.off_gtr());
   double2 *g_tr_grad = at(L.off_gdf());  // the double-float slot is not needed here
   double2 *chi0_grad = at(L.off_c()), *chi0tr_grad = at(L.off_ct());
   double2 *g_wr_grad = g_wr;        // G(iv, r) is dead once G(tau, r) is recomputed

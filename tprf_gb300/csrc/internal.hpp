@@ -137,7 +137,13 @@ int launch_lattice_fft_fmt(bool forward, long n_w, const int dims[3], long n_tar
 // The fused bubble + tau -> iw, writing chi0(iw, r) as double-float pairs when
 // want_df and the double-float path runs (*wrote_df tells which).
 int launch_chi0_wr_from_grt_df(double beta, int n_tau, int nw, const int dims[3], int nb, const double2 *g,
-                               const void *g_df, double2 *chi0_wr, cudaStream_t stream, bool want_df, bool *wrote_df);
+                               const void *g_df, double2 *chi0_wr, cudaStream_t stream, bool want_df, bool *wrote_df,
+                               const unsigned *gmax = nullptr);
+// iv -> tau writing the double-float copy as well; gmax (nullable, zeroed by
+// the caller) receives max |G| and max |Im G| for launch_chi0_wr_from_grt_df,
+// which pairs real bubble columns when G is real.
+int launch_nu_to_tau_df(double beta, int n_iw, int n_tau, long C, const double2 *gw, const double2 *mom, double2 *gt,
+                        void *gt_df, cudaStream_t stream, unsigned *gmax = nullptr);
 int launch_tau_to_w_adjoint(double beta, int n_tau, int nw, long C, const double2 *yg, double2 *xg,
                             cudaStream_t stream);
 int launch_nu_to_tau_adjoint(double beta, int n_iw, int n_tau, long C, const double2 *yg, double2 *gg, bool fitted,

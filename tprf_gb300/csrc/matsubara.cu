@@ -80,6 +80,14 @@ template <class C> struct IsDfElem { static constexpr bool value = false; };
 template <> struct IsDfElem<cdf> { static constexpr bool value = true; };
 template <class C> __device__ __forceinline__ C from_d2(double2 z);
 template <> __device__ __forceinline__ double2 from_d2<double2>(double2 z) { return z; }
+__device__ __forceinline__ double2 hi_parts(double2 z) { return z; }
+__device__ __forceinline__ double2 hi_parts(cdf z) { return make_double2(z.x.hi, z.y.hi); }
+__device__ __forceinline__ double2 conj_el(double2 z) { return cconj(z); }
+__device__ __forceinline__ cdf conj_el(cdf z) { return cconj(z); }
+__device__ __forceinline__ double2 half_el(double2 z) { return make_double2(0.5 * z.x, 0.5 * z.y); }
+__device__ __forceinline__ cdf half_el(cdf z) {  // exact: scales both words by 1/2
+  return cdf{dfl{0.5f * z.x.hi, 0.5f * z.x.lo}, dfl{0.5f * z.y.hi, 0.5f * z.y.lo}};
+}
 template <> __device__ __forceinline__ cdf from_d2<cdf>(double2 z) { return to_cdf(z); }
 __device__ __forceinline__ double2 as_d2(double2 z) { return z; }
 __device__ __forceinline__ double2 as_d2(cdf z) { return to_double2(z); }
@@ -121,7 +129,7 @@ template <class C>
 __global__ void __launch_bounds__(kMatsubaraThreads, 2) nu_to_tau_kernel(NuTauPlan p, const double2 *__restrict__ gw,
                                                         const double2 *__restrict__ mom, double2 *__restrict__ gt,
                                                         long Ccols, int ic, int lg, unsigned *status,
-                                                        cdf *__restrict__ gt_df) {
+                                                        cdf *__restrict__ gt_df, unsigned *gmax) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ unsigned s_res;
   C *a = reinterpret_cast<C *>(smem_raw);
@@ -191,6 +199,7 @@ __global__ void __launch_bounds__(kMatsubaraThreads, 2) nu_to_tau_kernel(NuTauPl
   __syncthreads();
   if (tid == 0 && __uint_as_float(s_res) > 1e-3f) atomicOr(status, kDevErrTailFit);
   C *r = fft_smem<true>(a, b, p.fft, ic);
+  float g_abs = 0.f, g_im = 0.f;
   for (int w = tid; w < (L + 1) * ic; w += nthr) {
     const int c = w & (ic - 1), t = w >> lg;
     if (c >= ncol) continue;
@@ -203,6 +212,23 @@ __global__ void __launch_bounds__(kMatsubaraThreads, 2) nu_to_tau_kernel(NuTauPl
     gt[(long)t * Ccols + col0 + c] = as_d2(v);
     if constexpr (IsDfElem<C>::value) {
       if (gt_df) gt_df[(long)t * Ccols + col0 + c] = v;  // the value before rounding to complex128
+    }
+    if (gmax) {
+      const double2 h = hi_parts(v);
+      g_abs = fmaxf(g_abs, fmaxf(fabsf((float)h.x), fabsf((float)h.y)));
+      g_im = fmaxf(g_im, fabsf((float)h.y));
+    }
+  }
+  // max |G| and max |Im G| of the whole transform, for the real-pair bubble
+  if (gmax) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      g_abs = fmaxf(g_abs, __shfl_xor_sync(0xffffffffu, g_abs, o));
+      g_im = fmaxf(g_im, __shfl_xor_sync(0xffffffffu, g_im, o));
+    }
+    if ((tid & 31) == 0) {
+      atomicMax(gmax, __float_as_uint(g_abs));
+      atomicMax(gmax + 1, __float_as_uint(g_im));
     }
   }
 }
@@ -292,13 +318,73 @@ struct BubbleLoaderDF : BubbleLoader {
   }
 };
 
+// Real pairs. When G(tau, r) is real (Hermitian hoppings that are real in
+// real space: the iv -> tau pass records max |G| and max |Im G| in gmax and
+// the data count as real when the second is at most 1e-11 of the first: the
+// transforms leave an imaginary residue of about 1e-12 on a real G, and 1e-11
+// is a tenth of the 1e-10 accuracy bar of the path), every
+// bubble column chi0(tau) is real, and two of them, f and h, go through one
+// complex transform as z = f + i h. The tau -> i omega map T is complex-linear
+// and T(f)(-m) = conj(T(f)(m)) for real f, so T(f)(m) = (T(z)(m) + conj(T(z)(-m)))/2
+// and T(h)(m) = (T(z)(m) - conj(T(z)(-m)))/(2i): half the transforms. The
+// moments of z are the moments of f plus i times those of h (the fit is
+// linear with real coefficients), so the tail works unchanged on z. The
+// imaginary parts of G (rounding residue, below the bound) are dropped.
+constexpr float kRealInputTol = 1e-11f;
+
+struct BubblePairLoaderDF : BubbleLoaderDF {
+  const unsigned *gmax;  // [max |G|, max |Im G|] as float bits, or null: no pairs
+  bool pairs = false;
+  __device__ __forceinline__ void init() {
+    pairs = gmax != nullptr && __uint_as_float(gmax[1]) <= kRealInputTol * __uint_as_float(gmax[0]);
+  }
+  // offsets of the two real columns 2 (col0 + c) and 2 (col0 + c) + 1 (the
+  // second past the last column reads the first: its results are not stored)
+  __device__ __forceinline__ void setup(long col0, int ic, int ncol, long *s) const {
+    if (!pairs) return BubbleLoader::setup(col0, ic, ncol, s);
+    const long nreal = Nr * nb * nb * nb * nb;
+    for (int c = threadIdx.x; c < ic; c += blockDim.x) {
+      long o[4] = {0, 0, 0, 0};
+      if (c < ncol) {
+        const long f = 2 * (col0 + c);
+        offsets(f, o[0], o[1]);
+        offsets(f + 1 < nreal ? f + 1 : f, o[2], o[3]);
+      }
+      for (int q = 0; q < 4; ++q) s[q * ic + c] = o[q];
+    }
+  }
+  template <class E>
+  __device__ __forceinline__ E get(int t, int c, long col0, int ic, const long *s) const {
+    if (!pairs) return BubbleLoaderDF::template get<E>(t, c, col0, ic, s);
+    if constexpr (IsDfElem<E>::value) {
+      const long slice = Nr * nb * nb, t1 = (long)t * slice, t2 = (long)(n_tau - 1 - t) * slice;
+      return cdf{dmul(gdf[t1 + s[c]].x, gdf[t2 + s[ic + c]].x), dmul(gdf[t1 + s[2 * ic + c]].x, gdf[t2 + s[3 * ic + c]].x)};
+    } else {
+      return get64(t, c, col0, ic, s);
+    }
+  }
+  __device__ __forceinline__ double2 get64(int t, int c, long col0, int ic, const long *s) const {
+    if (!pairs) return BubbleLoader::get64(t, c, col0, ic, s);
+    const long slice = Nr * nb * nb, t1 = (long)t * slice, t2 = (long)(n_tau - 1 - t) * slice;
+    return make_double2(g[t1 + s[c]].x * g[t2 + s[ic + c]].x, g[t1 + s[2 * ic + c]].x * g[t2 + s[3 * ic + c]].x);
+  }
+};
+template <class L> struct HasPairs { static constexpr bool value = false; };
+template <> struct HasPairs<BubblePairLoaderDF> { static constexpr bool value = true; };
+
 // tau -> i omega. fit_derivatives moments in FP64 from the end rows; the tail
 // model enters after the FFT: chi(i w_m) = (beta/L) FFT(chi)[k_m] + sum_j a_j K[j][m].
 // FERM: the fermionic transform (input phase, fermion moments); a template
 // parameter so that the bosonic bubble path carries no branch for it.
 template <class Loader, class C, bool FERM>
-__global__ void __launch_bounds__(kMatsubaraThreads, 2) tau_to_w_kernel(TauWPlan p, Loader ld, FitRows fr, double2 *__restrict__ out,
+__global__ void __launch_bounds__(kMatsubaraThreads, 2) tau_to_w_kernel(TauWPlan p, Loader ld_in, FitRows fr, double2 *__restrict__ out,
                                                        long Ccols, int ic, int lg, int out_df) {
+  Loader ld = ld_in;
+  bool pairs = false;  // real pairs (BubblePairLoaderDF on real input): Ccols real columns, half as many FFT columns
+  if constexpr (HasPairs<Loader>::value) {
+    ld.init();
+    pairs = ld.pairs;
+  }
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C *a = reinterpret_cast<C *>(smem_raw);
   const int L = p.L, nwt = p.n_out;
@@ -306,11 +392,13 @@ __global__ void __launch_bounds__(kMatsubaraThreads, 2) tau_to_w_kernel(TauWPlan
   C *b = p.fft.has_generic ? a + (size_t)L * ic : nullptr;
   C *last = a + (size_t)(p.fft.has_generic ? 2 : 1) * L * ic;  // [ic] row L
   C *am = last + ic;                                            // [4][ic] a1, a2, a3, m1
-  long *soff = reinterpret_cast<long *>(am + 4 * ic);           // [2][ic] loader offsets
-  double2 *smp = reinterpret_cast<double2 *>(soff + 2 * ic);    // [18][ic] FP64 rows 0..8, L-8..L
+  long *soff = reinterpret_cast<long *>(am + 4 * ic);           // [4][ic] loader offsets
+  double2 *smp = reinterpret_cast<double2 *>(soff + 4 * ic);    // [18][ic] FP64 rows 0..8, L-8..L
   const int tid = threadIdx.x, nthr = blockDim.x;
+  const long n_fft_cols = pairs ? (Ccols + 1) / 2 : Ccols;
   const long col0 = blockIdx.x * (long)ic;
-  const int ncol = (int)min((long)ic, Ccols - col0);
+  if (col0 >= n_fft_cols) return;  // the second half of the grid in pair mode
+  const int ncol = (int)min((long)ic, n_fft_cols - col0);
   ld.setup(col0, ic, ncol, soff);
   __syncthreads();
   // Rows t < L go to their digit-reversed FFT positions, row L aside. The loads
@@ -391,18 +479,46 @@ __global__ void __launch_bounds__(kMatsubaraThreads, 2) tau_to_w_kernel(TauWPlan
   // all stages but the last; the last is evaluated only at the kept frequencies
   C *r = fft_smem<false>(a, b, p.fft, ic, p.fft.nst - 1);
   const auto fact = real_of<C>(p.beta / (double)L);
-  for (int w = tid; w < nwt * ic; w += nthr) {
-    const int c = w & (ic - 1), mi = w >> lg;
-    if (c >= ncol) continue;
+  auto value = [&](int c, int mi) {  // T(column c) at output mi: FFT term and tail
     const int m = mi + p.out0;
     C v = cscale(last_stage_output<false>(r, p.fft, ic, c, m < 0 ? m + L : m), fact);
 #pragma unroll
     for (int j = 0; j < 3; ++j) v = cadd(v, cmul(am[j * ic + c], table<C>(p.K, p.Kf, (long)j * nwt + mi)));
-    // complex128, or the element type itself for a following double-float pass
+    return v;
+  };
+  auto store = [&](long idx, C v) {  // complex128, or the element type itself for a following double-float pass
     if (out_df)
-      reinterpret_cast<C *>(out)[(long)mi * Ccols + col0 + c] = v;
+      reinterpret_cast<C *>(out)[idx] = v;
     else
-      out[(long)mi * Ccols + col0 + c] = as_d2(v);
+      out[idx] = as_d2(v);
+  };
+  if constexpr (HasPairs<Loader>::value && !FERM) {
+    if (pairs) {
+      // bosonic outputs m = -(nw-1) .. nw-1 at mi = m + nw - 1: the pair (m, -m)
+      // from T(z)(m) and T(z)(-m); column 2q gets F, column 2q + 1 gets H
+      const int nw = (nwt + 1) / 2;
+      for (int w = tid; w < nw * ic; w += nthr) {
+        const int c = w & (ic - 1), mh = w >> lg;
+        if (c >= ncol) continue;
+        const int mp = nw - 1 + mh, mn = nw - 1 - mh;
+        const C vp = value(c, mp), vn = conj_el(value(c, mn));
+        const C F = half_el(cadd(vp, vn)), D = half_el(csub(vp, vn));
+        const C H = mul_mi<true>(D);  // (vp - conj(vn)) / (2 i)
+        const long f = 2 * (col0 + c);
+        store((long)mp * Ccols + f, F);
+        if (mh > 0) store((long)mn * Ccols + f, conj_el(F));
+        if (f + 1 < Ccols) {
+          store((long)mp * Ccols + f + 1, H);
+          if (mh > 0) store((long)mn * Ccols + f + 1, conj_el(H));
+        }
+      }
+      return;
+    }
+  }
+  for (int w = tid; w < nwt * ic; w += nthr) {
+    const int c = w & (ic - 1), mi = w >> lg;
+    if (c >= ncol) continue;
+    store((long)mi * Ccols + col0 + c, value(c, mi));
   }
 }
 
@@ -483,11 +599,12 @@ bool aliases(const BubbleLoader &l, const double2 *out) { return (const void *)l
 int tune_tag(const ArrayLoader &) { return 0; }
 int tune_tag(const BubbleLoader &l) { return 10 + l.nb; }
 int tune_tag(const BubbleLoaderDF &l) { return 20 + l.nb; }
+int tune_tag(const BubblePairLoaderDF &l) { return 30 + l.nb; }
 
 template <class Loader, class E>
 int launch_tau_to_w_as(const TauWPlan *p, Loader ld, double2 *out, long C, cudaStream_t stream,
                        bool out_df = false) {
-  const size_t extra = 5 * sizeof(double2) + 2 * sizeof(long) + 18 * sizeof(double2);
+  const size_t extra = 5 * sizeof(double2) + 4 * sizeof(long) + 18 * sizeof(double2);
   int ic, lg;
   size_t smem;
   int st = pick_ic(p->fft, extra, &ic, &lg, &smem);
@@ -765,14 +882,17 @@ __global__ void __launch_bounds__(256) bubble_adjoint_kernel(BubbleLoader ld, co
 // ---- internal launchers (no synchronisation) --------------------------------
 
 int launch_nu_to_tau_stat(double beta, int n_iw, int n_tau, bool fermion, long C, const double2 *gw,
-                          const double2 *mom, double2 *gt, cudaStream_t stream, cdf *gt_df = nullptr);
+                          const double2 *mom, double2 *gt, cudaStream_t stream, cdf *gt_df = nullptr,
+                          unsigned *gmax = nullptr);
 
 // The fermionic transform that also writes G(tau) as double-float pairs into
 // gt_df (left untouched in the FP64 arithmetic mode), for the fused bubble's
 // double-float product.
+// gmax (nullable, two words the caller zeroed): max |G| and max |Im G| of the
+// result as float bits, which decide whether the bubble can pair real columns.
 int launch_nu_to_tau_df(double beta, int n_iw, int n_tau, long C, const double2 *gw, const double2 *mom, double2 *gt,
-                        void *gt_df, cudaStream_t stream) {
-  return launch_nu_to_tau_stat(beta, n_iw, n_tau, true, C, gw, mom, gt, stream, reinterpret_cast<cdf *>(gt_df));
+                        void *gt_df, cudaStream_t stream, unsigned *gmax) {
+  return launch_nu_to_tau_stat(beta, n_iw, n_tau, true, C, gw, mom, gt, stream, reinterpret_cast<cdf *>(gt_df), gmax);
 }
 
 int launch_nu_to_tau(double beta, int n_iw, int n_tau, long C, const double2 *gw, const double2 *mom, double2 *gt,
@@ -783,7 +903,7 @@ int launch_nu_to_tau(double beta, int n_iw, int n_tau, long C, const double2 *gw
 // n: fermionic n_max or bosonic nw; the time mesh must hold L >= 2 n points
 // (fourier_matsubara.cpp:250-254).
 int launch_nu_to_tau_stat(double beta, int n_iw, int n_tau, bool fermion, long C, const double2 *gw,
-                          const double2 *mom, double2 *gt, cudaStream_t stream, cdf *gt_df) {
+                          const double2 *mom, double2 *gt, cudaStream_t stream, cdf *gt_df, unsigned *gmax) {
   if (n_tau < 0) n_tau = default_n_tau(n_iw);
   if (!(beta > 0.0) || n_iw < 1 || n_tau < 2 || C < 1 || (!fermion && n_iw < 2))
     return set_error(TPRF_ERR_INVALID_ARGUMENT, "fourier_wr_to_tr: bad mesh");
@@ -809,11 +929,12 @@ int launch_nu_to_tau_stat(double beta, int n_iw, int n_tau, bool fermion, long C
     if (fp64) {
       TPRF_CUDA(cudaFuncSetAttribute(nu_to_tau_kernel<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
       nu_to_tau_kernel<double2><<<(unsigned)blocks, kMatsubaraThreads, sm, stream>>>(*p, gw, mom, gt, C, icv,
-                                                                                      log2_ic(icv), status, nullptr);
+                                                                                      log2_ic(icv), status, nullptr,
+                                                                                      gmax);
     } else {
       TPRF_CUDA(cudaFuncSetAttribute(nu_to_tau_kernel<cdf>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
       nu_to_tau_kernel<cdf><<<(unsigned)blocks, kMatsubaraThreads, sm, stream>>>(*p, gw, mom, gt, C, icv, log2_ic(icv),
-                                                                                  status, gt_df);
+                                                                                  status, gt_df, gmax);
     }
     TPRF_LAUNCH_CHECK("nu_to_tau_kernel");
     return TPRF_OK;
@@ -862,7 +983,8 @@ int launch_chi0_wr_from_grt(double beta, int n_tau, int nw, const int dims[3], i
 // (written by launch_nu_to_tau_df); g_df == NULL or the FP64 arithmetic mode
 // takes the complex128 path.
 int launch_chi0_wr_from_grt_df(double beta, int n_tau, int nw, const int dims[3], int nb, const double2 *g,
-                               const void *g_df, double2 *chi0_wr, cudaStream_t stream, bool want_df, bool *wrote_df) {
+                               const void *g_df, double2 *chi0_wr, cudaStream_t stream, bool want_df, bool *wrote_df,
+                               const unsigned *gmax) {
   if (wrote_df) *wrote_df = false;
   if (!g_df || arith_mode() == kArithFP64) return launch_chi0_wr_from_grt(beta, n_tau, nw, dims, nb, g, chi0_wr, stream);
   int st = check_tau_w(beta, n_tau, nw);
@@ -870,11 +992,14 @@ int launch_chi0_wr_from_grt_df(double beta, int n_tau, int nw, const int dims[3]
   if ((st = bubble_columns(dims, nb))) return st;
   const TauWPlan *p = nullptr;
   if ((st = get_tau_w_plan(beta, n_tau, nw, &p))) return st;
-  BubbleLoaderDF ld;
+  BubblePairLoaderDF ld;
   static_cast<BubbleLoader &>(ld) = make_bubble(g, n_tau, dims, nb);
   ld.gdf = reinterpret_cast<const cdf *>(g_df);
+  ld.gmax = gmax;
   const long C = ld.Nr * nb * nb * nb * nb;
-  st = launch_tau_to_w_as<BubbleLoaderDF, cdf>(p, ld, chi0_wr, C, stream, want_df);
+  st = gmax ? launch_tau_to_w_as<BubblePairLoaderDF, cdf>(p, ld, chi0_wr, C, stream, want_df)
+            : launch_tau_to_w_as<BubbleLoaderDF, cdf>(p, static_cast<const BubbleLoaderDF &>(ld), chi0_wr, C, stream,
+                                                       want_df);
   if (!st && wrote_df) *wrote_df = want_df;
   return st;
 }

@@ -20,8 +20,6 @@ int launch_chi0_wr_from_grt(double beta, int n_tau, int nw, const int dims[3], i
                             double2 *chi0_wr, cudaStream_t stream);
 int launch_chi0_w0r_from_grt(double beta, int n_tau, const int dims[3], int nb, const double2 *g, double2 *chi0_wr,
                              cudaStream_t stream);
-int launch_nu_to_tau_df(double beta, int n_iw, int n_tau, long C, const double2 *gw, const double2 *mom, double2 *gt,
-                        void *gt_df, cudaStream_t stream);
 }  // namespace tprf
 
 using namespace tprf;
@@ -31,8 +29,9 @@ extern "C" size_t tprf_imtime_bubble_workspace_bytes(int n_iw, int n_tau, const 
   const size_t nk = (size_t)dims[0] * dims[1] * dims[2];
   const size_t t = (size_t)nb * nb * nk;
   const size_t g_wr = 2ull * n_iw * t, g_tr = (size_t)n_tau * t;
-  // G(iv, r), G(tau, r) and its double-float copy (16 bytes per element each)
-  return (g_wr + 2 * g_tr) * sizeof(double2) + 256;
+  // G(iv, r), G(tau, r) and its double-float copy (16 bytes per element each),
+  // then 256 bytes for the max |G|, max |Im G| words of the real-pair test
+  return (g_wr + 2 * g_tr) * sizeof(double2) + 512;
 }
 
 extern "C" int tprf_imtime_bubble_chi0_wk(double beta, int n_iw, int n_tau, int nw, const int dims[3], int nb,
@@ -59,6 +58,7 @@ extern "C" int tprf_imtime_bubble_chi0_wk_timed(double beta, int n_iw, int n_tau
   double2 *g_wr = reinterpret_cast<double2 *>(ws);
   double2 *g_tr = g_wr + 2L * n_iw * nk * nb2;
   double2 *g_tr_df = g_tr + (long)n_tau * nk * nb2;  // double-float copy, same element size
+  unsigned *gmax = reinterpret_cast<unsigned *>(g_tr_df + (long)n_tau * nk * nb2);
   double2 *out = reinterpret_cast<double2 *>(chi0_wk);
   auto mark = [&](int i) -> int {
     if (events && events[i]) TPRF_CUDA(cudaEventRecord(static_cast<cudaEvent_t>(events[i]), s));
@@ -68,8 +68,9 @@ extern "C" int tprf_imtime_bubble_chi0_wk_timed(double beta, int n_iw, int n_tau
   if ((st = mark(0))) return st;
   st = launch_lattice_fft(true, 2L * n_iw, dims, nb2, reinterpret_cast<const double2 *>(g_wk), g_wr, s);
   if (st || (st = mark(1))) return st;
+  TPRF_CUDA(cudaMemsetAsync(gmax, 0, 2 * sizeof(unsigned), s));
   st = launch_nu_to_tau_df(beta, n_iw, n_tau, nk * nb2, g_wr, reinterpret_cast<const double2 *>(moments), g_tr,
-                           g_tr_df, s);
+                           g_tr_df, s, gmax);
   if (st || (st = mark(2))) return st;
   // chi0(w, r) goes from the bubble to the r -> q transform as double-float
   // pairs (same bytes) on the double-float path: no conversion in between
@@ -77,7 +78,7 @@ extern "C" int tprf_imtime_bubble_chi0_wk_timed(double beta, int n_iw, int n_tau
   if (nw == 1)
     st = launch_chi0_w0r_from_grt(beta, n_tau, dims, nb, g_tr, out, s);
   else
-    st = launch_chi0_wr_from_grt_df(beta, n_tau, nw, dims, nb, g_tr, g_tr_df, out, s, nk > 1, &chi_df);
+    st = launch_chi0_wr_from_grt_df(beta, n_tau, nw, dims, nb, g_tr, g_tr_df, out, s, nk > 1, &chi_df, gmax);
   if (st || (st = mark(3))) return st;
   st = launch_lattice_fft_fmt(false, 2L * nw - 1, dims, nb4, out, chi_df, out, false, 1.0, s);
   if (st || (st = mark(4))) return st;
