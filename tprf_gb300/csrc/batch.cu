@@ -166,7 +166,9 @@ int enqueue_instance(const tprf_instance &a, unsigned char *scratch, cudaStream_
   else
     st = launch_chi0_wr_from_grt_df(a.beta, nt, a.nw, a.dims, a.nb, g_tr, g_tr_df, chi0, s, nk > 1, &chi_df, gmax);
   if (st) return st;
-  if ((st = launch_lattice_fft_fmt(false, 2L * a.nw - 1, a.dims, nb4, chi0, chi_df, chi0, false, 1.0, s))) return st;
+  if ((st = launch_lattice_fft_fmt(false, 2L * a.nw - 1, a.dims, nb4, chi0, chi_df, chi0, false, 1.0, s,
+                                   chi_df ? gmax : nullptr)))
+    return st;
   return launch_rpa((2L * a.nw - 1) * nk, a.nb, chi0, reinterpret_cast<const double2 *>(a.U),
                     reinterpret_cast<double2 *>(a.chi), s);
 }

@@ -30,6 +30,15 @@ namespace {
 
 constexpr int kLoadBatch = 4;  // tile loads per thread issued together
 
+// Leading part of a pass to leave out when the bubble's input was real
+// (gmax, see gmax_says_real): the negative bosonic frequencies, which the
+// mirror kernel fills afterwards. `columns` counts the pass's own units (the
+// axis pass: flattened columns; the plane pass: outer indices); 0 = none.
+struct SkipRows {
+  const unsigned *gmax;
+  long columns;
+};
+
 template <class E> __device__ __forceinline__ E load_el(double2 z);
 template <> __device__ __forceinline__ double2 load_el<double2>(double2 z) { return z; }
 template <> __device__ __forceinline__ cdf load_el<cdf>(double2 z) { return to_cdf(z); }
@@ -75,7 +84,8 @@ __device__ __forceinline__ void store_out(void *p, long i, E z, double s, dfl sd
 
 template <bool FWD, class E, bool IN_DF, bool OUT_DF>
 __global__ void __launch_bounds__(256) lattice_axis_kernel(const void *in, void *out, long ncols_total,
-                                                           long inner, int ncol, int lgcol, FftDesc d, double scale) {
+                                                           long inner, int ncol, int lgcol, FftDesc d, double scale,
+                                                           SkipRows skip) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int n = d.n;
   E *a = reinterpret_cast<E *>(smem_raw);
@@ -84,6 +94,7 @@ __global__ void __launch_bounds__(256) lattice_axis_kernel(const void *in, void 
   // The tile is ncol consecutive columns of the flattened (outer, inner) index;
   // element (row, column f) sits at (f / inner) * n * inner + row * inner + f % inner.
   const long f0 = blockIdx.x * (long)ncol;
+  if (f0 + ncol <= skip.columns && gmax_says_real(skip.gmax)) return;  // rows the mirror fills
   for (int c = threadIdx.x; c < ncol; c += blockDim.x) {
     const long f = f0 + c;
     const long o = f / inner;
@@ -120,7 +131,8 @@ __global__ void __launch_bounds__(256) lattice_axis_kernel(const void *in, void 
 }
 
 template <bool FWD, class E, bool IN_DF, bool OUT_DF>
-int launch_axis_as(const void *in, void *out, long outer, int n, long inner, double scale, cudaStream_t stream) {
+int launch_axis_as(const void *in, void *out, long outer, int n, long inner, double scale, cudaStream_t stream,
+                   SkipRows skip = SkipRows{nullptr, 0}) {
   FftDesc d;
   int st = get_fft(n, &d);
   if (st) return st;
@@ -140,7 +152,7 @@ int launch_axis_as(const void *in, void *out, long outer, int n, long inner, dou
   if (blocks > 0x7fffffffL) return set_error(TPRF_ERR_INVALID_ARGUMENT, "lattice FFT: too many tiles");
   auto kern = lattice_axis_kernel<FWD, E, IN_DF, OUT_DF>;
   TPRF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  kern<<<(unsigned)blocks, 256, smem, stream>>>(in, out, ncols_total, inner, ncol, lg, d, scale);
+  kern<<<(unsigned)blocks, 256, smem, stream>>>(in, out, ncols_total, inner, ncol, lg, d, scale, skip);
   TPRF_LAUNCH_CHECK("lattice_axis_kernel");
   return TPRF_OK;
 }
@@ -149,15 +161,15 @@ int launch_axis_as(const void *in, void *out, long outer, int n, long inner, dou
 // input and output; double-float only with double-float arithmetic.
 template <bool FWD>
 int launch_axis(const void *in, bool in_df, void *out, bool out_df, long outer, int n, long inner, double scale,
-                cudaStream_t stream) {
+                cudaStream_t stream, SkipRows skip = SkipRows{nullptr, 0}) {
   if (arith_mode() == kArithFP64) {
     if (in_df || out_df) return set_error(TPRF_ERR_INVALID_ARGUMENT, "lattice FFT: double-float storage in FP64 mode");
-    return launch_axis_as<FWD, double2, false, false>(in, out, outer, n, inner, scale, stream);
+    return launch_axis_as<FWD, double2, false, false>(in, out, outer, n, inner, scale, stream, skip);
   }
-  if (in_df && out_df) return launch_axis_as<FWD, cdf, true, true>(in, out, outer, n, inner, scale, stream);
-  if (in_df) return launch_axis_as<FWD, cdf, true, false>(in, out, outer, n, inner, scale, stream);
-  if (out_df) return launch_axis_as<FWD, cdf, false, true>(in, out, outer, n, inner, scale, stream);
-  return launch_axis_as<FWD, cdf, false, false>(in, out, outer, n, inner, scale, stream);
+  if (in_df && out_df) return launch_axis_as<FWD, cdf, true, true>(in, out, outer, n, inner, scale, stream, skip);
+  if (in_df) return launch_axis_as<FWD, cdf, true, false>(in, out, outer, n, inner, scale, stream, skip);
+  if (out_df) return launch_axis_as<FWD, cdf, false, true>(in, out, outer, n, inner, scale, stream, skip);
+  return launch_axis_as<FWD, cdf, false, false>(in, out, outer, n, inner, scale, stream, skip);
 }
 
 // Two adjacent mesh axes in one pass: the array is [outer, n1, n2, n_target]
@@ -170,12 +182,13 @@ int launch_axis(const void *in, bool in_df, void *out, bool out_df, long outer, 
 template <bool FWD, class E, bool IN_DF, bool OUT_DF>
 __global__ void __launch_bounds__(256) lattice_plane_kernel(const void *in, void *out, long outer, long n_target,
                                                             int nt, int lgt, FftDesc d1, FftDesc d2, int lg2,
-                                                            double scale) {
+                                                            double scale, SkipRows skip) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   E *a = reinterpret_cast<E *>(smem_raw);
   const int n1 = d1.n, n2 = d2.n, P = n1 * n2;
   const long tiles_t = (n_target + nt - 1) / nt;
   const long o = blockIdx.x / tiles_t;
+  if (o < skip.columns && gmax_says_real(skip.gmax)) return;  // rows the mirror fills
   const long t0 = (blockIdx.x - o * tiles_t) * (long)nt;
   const int ntv = (int)min((long)nt, n_target - t0);
   const long gbase = o * P * n_target + t0;
@@ -309,7 +322,7 @@ int plane_targets(int n1, int n2, long n_target) {
 
 template <bool FWD, class E, bool IN_DF, bool OUT_DF>
 int launch_plane_as(const void *in, void *out, long outer, int n1, int n2, long n_target, double scale,
-                    cudaStream_t stream) {
+                    cudaStream_t stream, SkipRows skip) {
   FftDesc d1, d2;
   int st = get_fft(n1, &d1);
   if (st) return st;
@@ -321,22 +334,51 @@ int launch_plane_as(const void *in, void *out, long outer, int n1, int n2, long 
   if (tiles > 0x7fffffffL) return set_error(TPRF_ERR_INVALID_ARGUMENT, "lattice FFT: too many tiles");
   auto kern = lattice_plane_kernel<FWD, E, IN_DF, OUT_DF>;
   TPRF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  kern<<<(unsigned)tiles, 256, smem, stream>>>(in, out, outer, n_target, nt, log2i(nt), d1, d2, log2i(n2), scale);
+  kern<<<(unsigned)tiles, 256, smem, stream>>>(in, out, outer, n_target, nt, log2i(nt), d1, d2, log2i(n2), scale,
+                                               skip);
   TPRF_LAUNCH_CHECK("lattice_plane_kernel");
   return TPRF_OK;
 }
 
 template <bool FWD>
 int launch_plane(const void *in, bool in_df, void *out, bool out_df, long outer, int n1, int n2, long n_target,
-                 double scale, cudaStream_t stream) {
+                 double scale, cudaStream_t stream, SkipRows skip = SkipRows{nullptr, 0}) {
   if (arith_mode() == kArithFP64) {
     if (in_df || out_df) return set_error(TPRF_ERR_INVALID_ARGUMENT, "lattice FFT: double-float storage in FP64 mode");
-    return launch_plane_as<FWD, double2, false, false>(in, out, outer, n1, n2, n_target, scale, stream);
+    return launch_plane_as<FWD, double2, false, false>(in, out, outer, n1, n2, n_target, scale, stream, skip);
   }
-  if (in_df && out_df) return launch_plane_as<FWD, cdf, true, true>(in, out, outer, n1, n2, n_target, scale, stream);
-  if (in_df) return launch_plane_as<FWD, cdf, true, false>(in, out, outer, n1, n2, n_target, scale, stream);
-  if (out_df) return launch_plane_as<FWD, cdf, false, true>(in, out, outer, n1, n2, n_target, scale, stream);
-  return launch_plane_as<FWD, cdf, false, false>(in, out, outer, n1, n2, n_target, scale, stream);
+  if (in_df && out_df) return launch_plane_as<FWD, cdf, true, true>(in, out, outer, n1, n2, n_target, scale, stream, skip);
+  if (in_df) return launch_plane_as<FWD, cdf, true, false>(in, out, outer, n1, n2, n_target, scale, stream, skip);
+  if (out_df) return launch_plane_as<FWD, cdf, false, true>(in, out, outer, n1, n2, n_target, scale, stream, skip);
+  return launch_plane_as<FWD, cdf, false, false>(in, out, outer, n1, n2, n_target, scale, stream, skip);
+}
+
+// Negative frequencies by symmetry: when the bubble's input was real
+// (gmax_says_real), its rows satisfy x(-w, r) = conj(x(w, r)) exactly, so after a
+// lattice transform of the non-negative rows x(-w, q) = conj(x(w, -q)), with
+// -q = (N_a - q_a) mod N_a on every axis. Rows are [n_w = 2 nw - 1][N_k][n_target],
+// row w - (nw - 1) = m; elements stored as complex128 or double-float pairs
+// (the conjugate negates the imaginary words in both).
+template <class T>
+__global__ void __launch_bounds__(256) mirror_neg_freq_kernel(T *x, int nw, int d0, int d1, int d2, long n_target,
+                                                              const unsigned *gmax) {
+  if (!gmax_says_real(gmax)) return;
+  const long nk = (long)d0 * d1 * d2, total = (long)(nw - 1) * nk * n_target;
+  for (long idx = blockIdx.x * (long)blockDim.x + threadIdx.x; idx < total; idx += (long)gridDim.x * blockDim.x) {
+    const long e = idx % n_target, k = (idx / n_target) % nk;
+    const int mi = (int)(idx / (n_target * nk));  // m = mi - (nw - 1) < 0
+    const int k2 = (int)(k % d2), k1 = (int)((k / d2) % d1), k0 = (int)(k / ((long)d2 * d1));
+    const long mk = ((long)((d0 - k0) % d0) * d1 + (d1 - k1) % d1) * d2 + (d2 - k2) % d2;
+    const long src = ((long)(2 * (nw - 1) - mi) * nk + mk) * n_target + e;
+    T v = x[src];
+    if constexpr (std::is_same<T, double2>::value) {
+      v.y = -v.y;
+    } else {
+      v.y.hi = -v.y.hi;
+      v.y.lo = -v.y.lo;
+    }
+    x[idx] = v;
+  }
 }
 
 // The TMA-staged plane pass with nt targets per tile (two tiles per CTA).
@@ -436,8 +478,24 @@ int launch_lattice_fft_scaled(bool forward, long n_w, const int dims[3], long n_
 // double-float arithmetic) as double-float pairs; the passes in between hand
 // each other double-float pairs whenever the arithmetic is double-float.
 int launch_lattice_fft_fmt(bool forward, long n_w, const int dims[3], long n_target, const void *in, bool in_df,
-                           void *out, bool out_df, double scale_last, cudaStream_t stream) {
+                           void *out, bool out_df, double scale_last, cudaStream_t stream, const unsigned *gmax) {
   const bool mid_df = arith_mode() != kArithFP64;
+  // with gmax: the n_w = 2 nw - 1 bosonic rows of a real bubble; the first nw - 1
+  // (negative frequencies) are left out of the passes and mirrored at the end
+  const long n_skip = (gmax && n_w >= 3 && (n_w & 1)) ? (n_w - 1) / 2 : 0;
+  auto mirror = [&]() -> int {
+    if (n_skip == 0) return TPRF_OK;
+    const long total = n_skip * (long)dims[0] * dims[1] * dims[2] * n_target;
+    const unsigned blocks = (unsigned)std::min((total + 255) / 256, (long)num_sms() * 16);
+    if (out_df)
+      mirror_neg_freq_kernel<cdf><<<blocks, 256, 0, stream>>>(static_cast<cdf *>(out), (int)(n_skip + 1), dims[0],
+                                                              dims[1], dims[2], n_target, gmax);
+    else
+      mirror_neg_freq_kernel<double2><<<blocks, 256, 0, stream>>>(static_cast<double2 *>(out), (int)(n_skip + 1),
+                                                                  dims[0], dims[1], dims[2], n_target, gmax);
+    TPRF_LAUNCH_CHECK("mirror_neg_freq_kernel");
+    return TPRF_OK;
+  };
   int nontriv[3], nn = 0;
   for (int ax = 0; ax < 3; ++ax)
     if (dims[ax] > 1) nontriv[nn++] = ax;
@@ -465,25 +523,30 @@ int launch_lattice_fft_fmt(bool forward, long n_w, const int dims[3], long n_tar
       for (int a2 = 0; a2 < A; ++a2) outer *= dims[a2];
       const double scale = (nn == 2) ? scale_last : 1.0;
       const bool plane_out_df = (nn == 3) ? mid_df : out_df;
-      int st = forward ? launch_plane_tma<true>(in, in_df, out, plane_out_df, outer, dims[A], dims[B], n_target, scale,
-                                                stream)
-                       : launch_plane_tma<false>(in, in_df, out, plane_out_df, outer, dims[A], dims[B], n_target, scale,
-                                                 stream);
+      const SkipRows pskip{gmax, n_skip * (outer / n_w)};
+      int st = kNotApplicable;
+      if (n_skip == 0)  // the TMA form has no row skip
+        st = forward ? launch_plane_tma<true>(in, in_df, out, plane_out_df, outer, dims[A], dims[B], n_target, scale,
+                                              stream)
+                     : launch_plane_tma<false>(in, in_df, out, plane_out_df, outer, dims[A], dims[B], n_target, scale,
+                                               stream);
       if (st == kNotApplicable)
-        st = forward ? launch_plane<true>(in, in_df, out, plane_out_df, outer, dims[A], dims[B], n_target, scale, stream)
+        st = forward ? launch_plane<true>(in, in_df, out, plane_out_df, outer, dims[A], dims[B], n_target, scale,
+                                          stream, pskip)
                      : launch_plane<false>(in, in_df, out, plane_out_df, outer, dims[A], dims[B], n_target, scale,
-                                           stream);
+                                           stream, pskip);
       if (st) return st;
       if (nn == 3) {
         const int ax = nontriv[0];
         long outer0 = n_w, inner0 = n_target;
         for (int a2 = 0; a2 < ax; ++a2) outer0 *= dims[a2];
         for (int a2 = ax + 1; a2 < 3; ++a2) inner0 *= dims[a2];
-        st = forward ? launch_axis<true>(out, mid_df, out, out_df, outer0, dims[ax], inner0, scale_last, stream)
-                     : launch_axis<false>(out, mid_df, out, out_df, outer0, dims[ax], inner0, scale_last, stream);
+        const SkipRows askip{gmax, n_skip * (outer0 / n_w) * inner0};
+        st = forward ? launch_axis<true>(out, mid_df, out, out_df, outer0, dims[ax], inner0, scale_last, stream, askip)
+                     : launch_axis<false>(out, mid_df, out, out_df, outer0, dims[ax], inner0, scale_last, stream, askip);
         if (st) return st;
       }
-      return TPRF_OK;
+      return mirror();
     }
   }
   // fastest-varying mesh dimension first: its pass has the longest contiguous rows;
@@ -498,13 +561,14 @@ int launch_lattice_fft_fmt(bool forward, long n_w, const int dims[3], long n_tar
     const bool last_pass = (i == 0);
     const double scale = last_pass ? scale_last : 1.0;
     const bool dst_df = last_pass ? out_df : mid_df;
-    int st = forward ? launch_axis<true>(src, src_df, out, dst_df, outer, n, inner, scale, stream)
-                     : launch_axis<false>(src, src_df, out, dst_df, outer, n, inner, scale, stream);
+    const SkipRows askip{gmax, n_skip * (outer / n_w) * inner};
+    int st = forward ? launch_axis<true>(src, src_df, out, dst_df, outer, n, inner, scale, stream, askip)
+                     : launch_axis<false>(src, src_df, out, dst_df, outer, n, inner, scale, stream, askip);
     if (st) return st;
     src = out;
     src_df = dst_df;
   }
-  return TPRF_OK;
+  return mirror();
 }
 
 int encode_tensor_map_f64(CUtensorMap *map, const void *base, int rank, const uint64_t *dims,
@@ -688,7 +752,7 @@ int noalloc_axis(const double2 *in, double2 *out, long outer, long inner, const 
   const long blocks = (ncols_total + ncol - 1) / ncol;
   auto kern = lattice_axis_kernel<FWD, E, false, false>;
   TPRF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  kern<<<(unsigned)blocks, 256, smem, stream>>>(in, out, ncols_total, inner, ncol, lg, d, scale);
+  kern<<<(unsigned)blocks, 256, smem, stream>>>(in, out, ncols_total, inner, ncol, lg, d, scale, SkipRows{nullptr, 0});
   TPRF_LAUNCH_CHECK("lattice_axis_kernel (no-alloc)");
   return TPRF_OK;
 }

@@ -124,6 +124,16 @@ inline int default_n_tau(int n_iw) { return 6 * n_iw + 1; }
 int max_smem_optin();
 int num_sms();
 
+// Real-input test of the bubble chain: G(tau, r) counts as real when
+// max |Im G| <= kRealInputTol max |G| (both recorded by the iv -> tau pass as
+// float bits in two words); see the real-pair bubble in matsubara.cu.
+constexpr float kRealInputTol = 1e-11f;
+#ifdef __CUDACC__
+__device__ __forceinline__ bool gmax_says_real(const unsigned *gmax) {
+  return gmax != nullptr && __uint_as_float(gmax[1]) <= kRealInputTol * __uint_as_float(gmax[0]);
+}
+#endif
+
 // Stream-ordered launchers shared by the C-ABI entry points and the batched
 // graphs (no synchronisation; plans must exist before a graph capture).
 int launch_lattice_fft(bool forward, long n_w, const int dims[3], long n_target, const double2 *in, double2 *out,
@@ -132,8 +142,12 @@ int launch_lattice_fft_scaled(bool forward, long n_w, const int dims[3], long n_
                               double2 *out, double scale, cudaStream_t stream);
 // Input / output stored as complex128 or (in_df / out_df, double-float
 // arithmetic only, N_k > 1) as double-float pairs of the same 16 bytes.
+// gmax (nullable): the rows are the 2 nw - 1 bosonic frequencies of a real
+// bubble (launch_chi0_wr_from_grt_df with the same words); when the words say
+// real, the negative frequencies are skipped and filled by symmetry,
+// x(-w, q) = conj(x(w, -q)). With in != out the skipped input rows are not read.
 int launch_lattice_fft_fmt(bool forward, long n_w, const int dims[3], long n_target, const void *in, bool in_df,
-                           void *out, bool out_df, double scale, cudaStream_t stream);
+                           void *out, bool out_df, double scale, cudaStream_t stream, const unsigned *gmax = nullptr);
 // The fused bubble + tau -> iw, writing chi0(iw, r) as double-float pairs when
 // want_df and the double-float path runs (*wrote_df tells which).
 int launch_chi0_wr_from_grt_df(double beta, int n_tau, int nw, const int dims[3], int nb, const double2 *g,

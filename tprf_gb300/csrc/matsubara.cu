@@ -330,14 +330,11 @@ struct BubbleLoaderDF : BubbleLoader {
 // moments of z are the moments of f plus i times those of h (the fit is
 // linear with real coefficients), so the tail works unchanged on z. The
 // imaginary parts of G (rounding residue, below the bound) are dropped.
-constexpr float kRealInputTol = 1e-11f;
 
 struct BubblePairLoaderDF : BubbleLoaderDF {
   const unsigned *gmax;  // [max |G|, max |Im G|] as float bits, or null: no pairs
   bool pairs = false;
-  __device__ __forceinline__ void init() {
-    pairs = gmax != nullptr && __uint_as_float(gmax[1]) <= kRealInputTol * __uint_as_float(gmax[0]);
-  }
+  __device__ __forceinline__ void init() { pairs = gmax_says_real(gmax); }
   // offsets of the two real columns 2 (col0 + c) and 2 (col0 + c) + 1 (the
   // second past the last column reads the first: its results are not stored)
   __device__ __forceinline__ void setup(long col0, int ic, int ncol, long *s) const {

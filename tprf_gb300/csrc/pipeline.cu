@@ -80,7 +80,9 @@ extern "C" int tprf_imtime_bubble_chi0_wk_timed(double beta, int n_iw, int n_tau
   else
     st = launch_chi0_wr_from_grt_df(beta, n_tau, nw, dims, nb, g_tr, g_tr_df, out, s, nk > 1, &chi_df, gmax);
   if (st || (st = mark(3))) return st;
-  st = launch_lattice_fft_fmt(false, 2L * nw - 1, dims, nb4, out, chi_df, out, false, 1.0, s);
+  // on a real bubble (the same words) only the non-negative frequencies are
+  // transformed; the others follow by symmetry
+  st = launch_lattice_fft_fmt(false, 2L * nw - 1, dims, nb4, out, chi_df, out, false, 1.0, s, chi_df ? gmax : nullptr);
   if (st || (st = mark(4))) return st;
   return finish_with_checks(s, "imtime_bubble_chi0_wk");
 }
