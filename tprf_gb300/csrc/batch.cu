@@ -164,7 +164,8 @@ int enqueue_instance(const tprf_instance &a, unsigned char *scratch, cudaStream_
   if (a.nw == 1)
     st = launch_chi0_w0r_from_grt(a.beta, nt, a.dims, a.nb, g_tr, chi0, s);
   else
-    st = launch_chi0_wr_from_grt_df(a.beta, nt, a.nw, a.dims, a.nb, g_tr, g_tr_df, chi0, s, nk > 1, &chi_df, gmax);
+    st = launch_chi0_wr_from_grt_df(a.beta, nt, a.nw, a.dims, a.nb, g_tr, g_tr_df, chi0, s, nk > 1, &chi_df, gmax,
+                                    nk > 1);
   if (st) return st;
   if ((st = launch_lattice_fft_fmt(false, 2L * a.nw - 1, a.dims, nb4, chi0, chi_df, chi0, false, 1.0, s,
                                    chi_df ? gmax : nullptr)))

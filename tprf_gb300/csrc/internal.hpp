@@ -149,10 +149,12 @@ int launch_lattice_fft_scaled(bool forward, long n_w, const int dims[3], long n_
 int launch_lattice_fft_fmt(bool forward, long n_w, const int dims[3], long n_target, const void *in, bool in_df,
                            void *out, bool out_df, double scale, cudaStream_t stream, const unsigned *gmax = nullptr);
 // The fused bubble + tau -> iw, writing chi0(iw, r) as double-float pairs when
-// want_df and the double-float path runs (*wrote_df tells which).
+// want_df and the double-float path runs (*wrote_df tells which). skip_neg:
+// on a real bubble (gmax words), the negative frequencies are left unwritten
+// for a following launch_lattice_fft_fmt with the same words, which fills them.
 int launch_chi0_wr_from_grt_df(double beta, int n_tau, int nw, const int dims[3], int nb, const double2 *g,
                                const void *g_df, double2 *chi0_wr, cudaStream_t stream, bool want_df, bool *wrote_df,
-                               const unsigned *gmax = nullptr);
+                               const unsigned *gmax = nullptr, bool skip_neg = false);
 // iv -> tau writing the double-float copy as well; gmax (nullable, zeroed by
 // the caller) receives max |G| and max |Im G| for launch_chi0_wr_from_grt_df,
 // which pairs real bubble columns when G is real.

@@ -375,7 +375,7 @@ template <> struct HasPairs<BubblePairLoaderDF> { static constexpr bool value = 
 // parameter so that the bosonic bubble path carries no branch for it.
 template <class Loader, class C, bool FERM>
 __global__ void __launch_bounds__(kMatsubaraThreads, 2) tau_to_w_kernel(TauWPlan p, Loader ld_in, FitRows fr, double2 *__restrict__ out,
-                                                       long Ccols, int ic, int lg, int out_df) {
+                                                       long Ccols, int ic, int lg, int out_df, int skip_neg) {
   Loader ld = ld_in;
   bool pairs = false;  // real pairs (BubblePairLoaderDF on real input): Ccols real columns, half as many FFT columns
   if constexpr (HasPairs<Loader>::value) {
@@ -502,11 +502,13 @@ __global__ void __launch_bounds__(kMatsubaraThreads, 2) tau_to_w_kernel(TauWPlan
         const C F = half_el(cadd(vp, vn)), D = half_el(csub(vp, vn));
         const C H = mul_mi<true>(D);  // (vp - conj(vn)) / (2 i)
         const long f = 2 * (col0 + c);
+        // the negative frequencies only when the caller does not fill them by symmetry
+        const bool neg = mh > 0 && !skip_neg;
         store((long)mp * Ccols + f, F);
-        if (mh > 0) store((long)mn * Ccols + f, conj_el(F));
+        if (neg) store((long)mn * Ccols + f, conj_el(F));
         if (f + 1 < Ccols) {
           store((long)mp * Ccols + f + 1, H);
-          if (mh > 0) store((long)mn * Ccols + f + 1, conj_el(H));
+          if (neg) store((long)mn * Ccols + f + 1, conj_el(H));
         }
       }
       return;
@@ -600,7 +602,7 @@ int tune_tag(const BubblePairLoaderDF &l) { return 30 + l.nb; }
 
 template <class Loader, class E>
 int launch_tau_to_w_as(const TauWPlan *p, Loader ld, double2 *out, long C, cudaStream_t stream,
-                       bool out_df = false) {
+                       bool out_df = false, bool skip_neg = false) {
   const size_t extra = 5 * sizeof(double2) + 4 * sizeof(long) + 18 * sizeof(double2);
   int ic, lg;
   size_t smem;
@@ -618,7 +620,7 @@ int launch_tau_to_w_as(const TauWPlan *p, Loader ld, double2 *out, long C, cudaS
         TPRF_CUDA(cudaFuncSetAttribute(tau_to_w_kernel<Loader, E, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)sm));
         tau_to_w_kernel<Loader, E, true><<<(unsigned)blocks, kMatsubaraThreads, sm, stream>>>(*p, ld, fr, out, C, icv,
-                                                                                              log2_ic(icv), out_df);
+                                                                                              log2_ic(icv), out_df, skip_neg);
         TPRF_LAUNCH_CHECK("tau_to_w_kernel");
         return TPRF_OK;
       }
@@ -626,7 +628,7 @@ int launch_tau_to_w_as(const TauWPlan *p, Loader ld, double2 *out, long C, cudaS
     TPRF_CUDA(cudaFuncSetAttribute(tau_to_w_kernel<Loader, E, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)sm));
     tau_to_w_kernel<Loader, E, false><<<(unsigned)blocks, kMatsubaraThreads, sm, stream>>>(*p, ld, fr, out, C, icv,
-                                                                                           log2_ic(icv), out_df);
+                                                                                           log2_ic(icv), out_df, skip_neg);
     TPRF_LAUNCH_CHECK("tau_to_w_kernel");
     return TPRF_OK;
   };
@@ -981,7 +983,7 @@ int launch_chi0_wr_from_grt(double beta, int n_tau, int nw, const int dims[3], i
 // takes the complex128 path.
 int launch_chi0_wr_from_grt_df(double beta, int n_tau, int nw, const int dims[3], int nb, const double2 *g,
                                const void *g_df, double2 *chi0_wr, cudaStream_t stream, bool want_df, bool *wrote_df,
-                               const unsigned *gmax) {
+                               const unsigned *gmax, bool skip_neg) {
   if (wrote_df) *wrote_df = false;
   if (!g_df || arith_mode() == kArithFP64) return launch_chi0_wr_from_grt(beta, n_tau, nw, dims, nb, g, chi0_wr, stream);
   int st = check_tau_w(beta, n_tau, nw);
@@ -994,7 +996,7 @@ int launch_chi0_wr_from_grt_df(double beta, int n_tau, int nw, const int dims[3]
   ld.gdf = reinterpret_cast<const cdf *>(g_df);
   ld.gmax = gmax;
   const long C = ld.Nr * nb * nb * nb * nb;
-  st = gmax ? launch_tau_to_w_as<BubblePairLoaderDF, cdf>(p, ld, chi0_wr, C, stream, want_df)
+  st = gmax ? launch_tau_to_w_as<BubblePairLoaderDF, cdf>(p, ld, chi0_wr, C, stream, want_df, skip_neg)
             : launch_tau_to_w_as<BubbleLoaderDF, cdf>(p, static_cast<const BubbleLoaderDF &>(ld), chi0_wr, C, stream,
                                                        want_df);
   if (!st && wrote_df) *wrote_df = want_df;

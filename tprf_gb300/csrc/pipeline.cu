@@ -78,7 +78,8 @@ extern "C" int tprf_imtime_bubble_chi0_wk_timed(double beta, int n_iw, int n_tau
   if (nw == 1)
     st = launch_chi0_w0r_from_grt(beta, n_tau, dims, nb, g_tr, out, s);
   else
-    st = launch_chi0_wr_from_grt_df(beta, n_tau, nw, dims, nb, g_tr, g_tr_df, out, s, nk > 1, &chi_df, gmax);
+    st = launch_chi0_wr_from_grt_df(beta, n_tau, nw, dims, nb, g_tr, g_tr_df, out, s, nk > 1, &chi_df, gmax,
+                                    nk > 1);
   if (st || (st = mark(3))) return st;
   // on a real bubble (the same words) only the non-negative frequencies are
   // transformed; the others follow by symmetry
