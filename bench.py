@@ -301,7 +301,7 @@ def run_gpu(args):
         check(lib.tprf_imtime_bubble_chi0_wk_timed(beta, n_max, n_tau, nw, d3, nb, g_wk.data_ptr(), None,
                                                    chi0.data_ptr(), ws.data_ptr(), ws_bytes,
                                                    ev[1] if ev is not None else no_events, sh))
-        check(lib.tprf_solve_rpa_PH(points, nb, chi0.data_ptr(), U.data_ptr(), chi.data_ptr(), sh))
+        check(lib.tprf_solve_rpa_PH_wk(nw, d3, nb, chi0.data_ptr(), U.data_ptr(), chi.data_ptr(), sh))
         if ev is not None:
             ev[0][6].record(stream)
 

@@ -237,6 +237,16 @@ int tprf_chi_w0r_from_chi_tr(double beta, int n_tau, long n_r, long n_target,
  * nb <= 8. */
 int tprf_solve_rpa_PH(long n_points, int nb, const double *chi0, const double *U,
                       double *chi, void *stream);
+/* solve_rpa_PH on a (bosonic i omega, q) mesh: chi0 and chi are
+ * [2 nw - 1][dims[0] dims[1] dims[2]][nb^4], frequencies -(nw-1) .. nw-1 and q
+ * row-major over dims, as the reference's chi_wk. Same result as
+ * tprf_solve_rpa_PH; knowing the mesh, it solves a point pair (w, q), (-w, -q)
+ * once where U is real and chi0(-w, -q) is bit for bit conj(chi0(w, q)) (a
+ * bubble of real hoppings from tprf_imtime_bubble_chi0_wk is), since the
+ * elimination then gives the conjugate result bit for bit (up to the signs of
+ * zeros). In place (chi == chi0) allowed. Reference: rpa.cpp:29-68 (solve_rpa_PH). */
+int tprf_solve_rpa_PH_wk(int nw, const int dims[3], int nb, const double *chi0, const double *U, double *chi,
+                         void *stream);
 
 /* solve_rpa_PH with chi written to HOST memory, as the reference's C++ function
  * returns it (rpa.cpp:29-68 returns a host gf). The points are solved in chunks

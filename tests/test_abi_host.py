@@ -102,7 +102,8 @@ def test_argument_errors_are_reported_without_a_gpu(lib):
 def test_workspace_size(lib):
     from tprf_gb300 import _native
     n = lib.tprf_imtime_bubble_workspace_bytes(256, -1, _native.dims3((32, 32, 32)), 3)
-    expect = (512 + 2 * 1537) * 32768 * 9 * 16 + 256  # G(iv, r), G(tau, r) and its double-float copy
+    # G(iv, r), G(tau, r) and its double-float copy, the real-input test words, alignment
+    expect = (512 + 2 * 1537) * 32768 * 9 * 16 + 512
     assert n == expect
 
 

@@ -432,3 +432,28 @@ def test_kanamori_rpa_closed_form(cuda_lib):
     Sz = 0.5 * np.diag([1.0, -1.0, 1.0, -1.0])
     szsz = np.einsum("wkabcd,ab,cd->wk", chi, Sz, Sz)
     np.testing.assert_array_almost_equal(szsz[0, 0].real, f["chi_szsz_q0"])
+
+
+@pytest.mark.parametrize("case", range(len(CASES)))
+@pytest.mark.parametrize("u_kind", ["real", "complex"])
+def test_rpa_on_the_wk_mesh_equals_the_point_solve(cuda_lib, case, u_kind):
+    """solve_rpa_PH on a chi0 Gf (mesh-aware C ABI, conjugate point pairs solved
+    once where chi0 and U allow) gives exactly the point-by-point solve
+    (tprf_solve_rpa_PH), and the oracle's chi."""
+    T = tp()
+    from tprf_gb300 import _native
+    hopf, dims, beta, n_max = CASES[case]
+    ek, g_wk, _, _ = _g_wr(hopf(), dims, beta, n_max)
+    chi0 = T.imtime_bubble_chi0_wk(g_wk, nw=6, verbose=False)
+    nb = ek.shape[-1]
+    rng = np.random.default_rng(10 + case)
+    U = 0.3 * rng.standard_normal((nb,) * 4) + (0.1j * rng.standard_normal((nb,) * 4) if u_kind == "complex" else 0j)
+    chi = T.solve_rpa_PH(chi0, U)
+    flat = torch.empty_like(chi0.data)
+    Ud = torch.as_tensor(U, dtype=torch.complex128, device="cuda").contiguous()
+    n_points = chi0.data.numel() // nb ** 4
+    _native.check(cuda_lib.tprf_solve_rpa_PH(n_points, nb, chi0.data.data_ptr(), Ud.data_ptr(), flat.data_ptr(), None))
+    torch.cuda.synchronize()
+    assert torch.equal(chi.data, flat)
+    ref0 = O.imtime_bubble_chi0_wk(O.lattice_dyson_g0_wk(0.0, ek, beta, n_max), beta, dims, nw=6)
+    assert rel_err(chi.data, O.solve_rpa_PH(ref0, U)) < PARITY_RTOL

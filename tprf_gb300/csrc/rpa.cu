@@ -245,6 +245,33 @@ extern "C" int tprf_solve_rpa_PH(long n_points, int nb, const double *chi0, cons
   return finish_with_checks(s, "solve_rpa_PH");
 }
 
+// ---- RPA on a (w, q) mesh with conjugate pairs ----------------------------------------
+namespace tprf {
+int launch_rpa_warp_pairs(int nw, const int dims[3], int nb, const double2 *chi0, const double2 *U, double2 *chi,
+                          cudaStream_t stream, unsigned *status);
+
+int launch_rpa_wk(int nw, const int dims[3], int nb, const double2 *chi0, const double2 *U, double2 *chi,
+                  cudaStream_t stream) {
+  if (nb < 3 || nw < 1) return launch_rpa((2L * nw - 1) * dims[0] * dims[1] * dims[2], nb, chi0, U, chi, stream);
+  unsigned *status = device_status_word();
+  if (!status) return TPRF_ERR_CUDA;
+  if (nb > 8) return set_error(TPRF_ERR_INVALID_ARGUMENT, "solve_rpa_PH: nb must be 1..8");
+  return launch_rpa_warp_pairs(nw, dims, nb, chi0, U, chi, stream, status);
+}
+}  // namespace tprf
+
+extern "C" int tprf_solve_rpa_PH_wk(int nw, const int dims[3], int nb, const double *chi0, const double *U,
+                                    double *chi, void *stream) {
+  using namespace tprf;
+  if (nw < 1 || !dims || dims[0] < 1 || dims[1] < 1 || dims[2] < 1 || !chi0 || !U || !chi)
+    return set_error(TPRF_ERR_INVALID_ARGUMENT, "solve_rpa_PH_wk: bad mesh or null pointer");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int st = launch_rpa_wk(nw, dims, nb, reinterpret_cast<const double2 *>(chi0), reinterpret_cast<const double2 *>(U),
+                         reinterpret_cast<double2 *>(chi), s);
+  if (st) return st;
+  return finish_with_checks(s, "solve_rpa_PH");
+}
+
 // ---- RPA with the result streamed to host memory -----------------------------------
 // The reference returns chi as a host-side gf. Here the points are solved in chunks
 // into a small device ring (the caller's workspace) and each chunk is copied to the

@@ -153,7 +153,8 @@ __device__ __forceinline__ typename Mag<E>::type solve_augmented(E *M, int N_in,
 
 template <class E, int G, int NBC = 0>
 __device__ double rpa_point_warp(const double2 *__restrict__ x, double2 *__restrict__ y, E *M, int N_in, int nb_in,
-                                 const SparseU &u, int lane, unsigned gmask, bool &singular) {
+                                 const SparseU &u, int lane, unsigned gmask, bool &singular,
+                                 double2 *__restrict__ y_conj = nullptr) {
   const int nb = NBC > 0 ? NBC : nb_in;  // a compile-time size when NBC > 0
   const int N = NBC > 0 ? NBC * NBC : N_in;
   const int W = 2 * N;
@@ -181,7 +182,11 @@ __device__ double rpa_point_warp(const double2 *__restrict__ x, double2 *__restr
   bool sing = false;
   const auto pmin = solve_augmented<E, G, NBC * NBC>(M, N, lane, gmask, sing);
   singular = sing;
-  for (int o = lane; o < N * N; o += G) y[o] = el_to(M[(o / N) * 2 * N + N + col_of_offset(o % N, nb)]);
+  for (int o = lane; o < N * N; o += G) {
+    const double2 v = el_to(M[(o / N) * 2 * N + N + col_of_offset(o % N, nb)]);
+    y[o] = v;
+    if (y_conj) y_conj[o] = make_double2(v.x, -v.y);  // the solve of the conjugate system, bit for bit
+  }
   amax = group_max<G>(amax, gmask);
   __syncwarp(gmask);
   const double am = (double)amax * (double)amax;
@@ -235,6 +240,85 @@ __global__ void __launch_bounds__(512) rpa_warp_kernel(long n_points, int nb_in,
     if (IsDf<E>::value && !(cond2 <= kDf64CondLimit2))
       rpa_point_warp<double2, G, NBC>(x, y, reinterpret_cast<double2 *>(M), N, nb, u, lane, gmask, singular);
     if (singular && lane == 0) atomicOr(status, kDevErrSingular);
+  }
+}
+
+// Conjugate pairs on a bosonic (w, q) mesh: with U real, chi0(-w, q) =
+// conj(chi0(w, -q)) (a real bubble gives this exactly) makes A(-w, q) the
+// conjugate of A(w, -q), and the elimination (conjugation only flips signs,
+// which every step preserves) gives chi(-w, q) = conj(chi(w, -q)) bit for bit.
+// A group takes a unit (w >= 0, q) with its partner (-w, -q); if the partner's
+// chi0 is that conjugate, bit for bit, it solves once and stores both, else it
+// solves both. Units: the nw x N_k points with w >= 0 (at w = 0 only q <= -q).
+template <class E, int G, int NBC = 0>
+__global__ void __launch_bounds__(512) rpa_pair_kernel(int nw, int d0, int d1, int d2, int nb_in,
+                                                       const double2 *__restrict__ chi0, const double2 *__restrict__ U,
+                                                       double2 *__restrict__ chi, unsigned *status) {
+  const int nb = NBC > 0 ? NBC : nb_in;
+  const int N = nb * nb;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double2 *s_val = reinterpret_cast<double2 *>(smem_raw);
+  int *s_row = reinterpret_cast<int *>(s_val + N * N);
+  int *s_cs = s_row + N * N;
+  __shared__ int s_ureal;
+  const size_t u_bytes = ((size_t)N * N * (sizeof(double2) + sizeof(int)) + (N + 1) * sizeof(int) + 15) & ~(size_t)15;
+  constexpr int GPW = 32 / G;
+  const int wl = threadIdx.x & 31, gw = wl / G;
+  const int grp = (threadIdx.x >> 5) * GPW + gw, lane = wl - gw * G, n_grp = (blockDim.x >> 5) * GPW;
+  const bool active = gw < GPW;
+  const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (gw * G));
+  E *M = reinterpret_cast<E *>(smem_raw + u_bytes) + (size_t)(active ? grp : 0) * 2 * N * N;
+  if (threadIdx.x == 0) {
+    int t = 0, ureal = 1;
+    for (int c = 0; c < N; ++c) {
+      s_cs[c] = t;
+      for (int m = 0; m < N; ++m) {
+        const double2 v = U[m * N + (c % nb) * nb + c / nb];
+        if (v.y != 0.0) ureal = 0;
+        if (v.x != 0.0 || v.y != 0.0) {
+          s_row[t] = m;
+          s_val[t] = v;
+          ++t;
+        }
+      }
+    }
+    s_cs[N] = t;
+    s_ureal = ureal;
+  }
+  __syncthreads();
+  const SparseU u{s_val, s_row, s_cs};
+  const bool ureal = s_ureal != 0;
+  if (!active) return;
+  const long nk = (long)d0 * d1 * d2, units = (long)nw * nk;
+  for (long un = (long)blockIdx.x * n_grp + grp; un < units; un += (long)gridDim.x * n_grp) {
+    const int mh = (int)(un / nk);
+    const long q = un - (long)mh * nk;
+    const int q2 = (int)(q % d2), q1 = (int)((q / d2) % d1), q0 = (int)(q / ((long)d2 * d1));
+    const long mq = ((long)((d0 - q0) % d0) * d1 + (d1 - q1) % d1) * d2 + (d2 - q2) % d2;
+    if (mh == 0 && q > mq) continue;  // its partner (0, -q) holds this unit
+    const long p = (long)(nw - 1 + mh) * nk + q, pm = (long)(nw - 1 - mh) * nk + mq;
+    const double2 *x = chi0 + p * N * N, *xm = chi0 + pm * N * N;
+    bool sym = ureal;
+    if (pm != p) {
+      for (int o = lane; o < N * N; o += G) {
+        const double2 a = x[o], b = xm[o];
+        sym = sym && __double_as_longlong(a.x) == __double_as_longlong(b.x) &&
+              __double_as_longlong(a.y) == __double_as_longlong(-b.y);
+      }
+      sym = __all_sync(gmask, sym);
+    }
+    double2 *y = chi + p * N * N, *ym = chi + pm * N * N;
+    for (int k = 0; k < 2; ++k) {
+      if (k == 1 && (pm == p || sym)) break;
+      const double2 *xs = k ? xm : x;
+      double2 *ys = k ? ym : y;
+      double2 *yc = (k == 0 && sym && pm != p) ? ym : nullptr;
+      bool singular = false;
+      const double cond2 = rpa_point_warp<E, G, NBC>(xs, ys, M, N, nb, u, lane, gmask, singular, yc);
+      if (IsDf<E>::value && !(cond2 <= kDf64CondLimit2))
+        rpa_point_warp<double2, G, NBC>(xs, ys, reinterpret_cast<double2 *>(M), N, nb, u, lane, gmask, singular, yc);
+      if (singular && lane == 0) atomicOr(status, kDevErrSingular);
+    }
   }
 }
 
@@ -499,6 +583,52 @@ __global__ void __launch_bounds__(512) rpa_adjoint_warp_kernel(long n_points, in
 // nb = 5 32 lanes, 248 ms for 2.1 M points, against 376 ms with 16)
 int rpa_group_lanes(int nb) { return nb <= 2 ? 8 : nb == 3 ? 9 : 32; }
 
+template <class E, int G, int NBC>
+int launch_pair_as(int nw, const int dims[3], int nb, const double2 *chi0, const double2 *U, double2 *chi,
+                   cudaStream_t stream, unsigned *status) {
+  const int N = nb * nb;
+  const size_t u_bytes = ((size_t)N * N * (sizeof(double2) + sizeof(int)) + (N + 1) * sizeof(int) + 15) & ~(size_t)15;
+  const size_t per_point = (size_t)2 * N * N * 16;
+  const int ppw = 32 / G;
+  const size_t limit = (size_t)max_smem_optin() - 64;  // the kernel's static word
+  if (u_bytes + ppw * per_point > limit) return set_error(TPRF_ERR_INVALID_ARGUMENT, "solve_rpa_PH: nb too large");
+  auto kern = rpa_pair_kernel<E, G, NBC>;
+  TPRF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)limit));
+  int best_w = 1, best_total = 0;
+  for (int w = 1; w <= 16; ++w) {
+    const size_t smem = u_bytes + (size_t)w * ppw * per_point;
+    if (smem > limit) break;
+    int per_sm = 0;
+    TPRF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * w, smem));
+    if (per_sm * w >= best_total) {
+      best_total = per_sm * w;
+      best_w = w;
+    }
+  }
+  if (best_total == 0) return set_error(TPRF_ERR_INVALID_ARGUMENT, "solve_rpa_PH: nb too large");
+  const size_t smem = u_bytes + (size_t)best_w * ppw * per_point;
+  const long units = (long)nw * dims[0] * dims[1] * dims[2], per_block = (long)best_w * ppw;
+  long blocks = (units + per_block - 1) / per_block;
+  blocks = std::max(1L, std::min(blocks, (long)num_sms() * (best_total / best_w) * 8));
+  kern<<<(unsigned)blocks, 32 * best_w, smem, stream>>>(nw, dims[0], dims[1], dims[2], nb, chi0, U, chi, status);
+  TPRF_LAUNCH_CHECK("rpa_pair_kernel");
+  return TPRF_OK;
+}
+
+template <int G>
+int launch_pair_g(int nw, const int dims[3], int nb, const double2 *chi0, const double2 *U, double2 *chi,
+                  cudaStream_t stream, unsigned *status) {
+  const bool fp64 = arith_mode() == kArithFP64;
+  if (nb == 3)
+    return fp64 ? launch_pair_as<double2, G, 3>(nw, dims, nb, chi0, U, chi, stream, status)
+                : launch_pair_as<cdf, G, 3>(nw, dims, nb, chi0, U, chi, stream, status);
+  if (nb == 5 && G >= 16)
+    return fp64 ? launch_pair_as<double2, G, 5>(nw, dims, nb, chi0, U, chi, stream, status)
+                : launch_pair_as<cdf, G, 5>(nw, dims, nb, chi0, U, chi, stream, status);
+  return fp64 ? launch_pair_as<double2, G, 0>(nw, dims, nb, chi0, U, chi, stream, status)
+              : launch_pair_as<cdf, G, 0>(nw, dims, nb, chi0, U, chi, stream, status);
+}
+
 int launch_rpa_warp(long n_points, int nb, const double2 *chi0, const double2 *U, double2 *chi, cudaStream_t stream,
                     unsigned *status) {
   auto launch = [&](int lanes, long n) -> int {
@@ -525,6 +655,38 @@ int launch_rpa_warp(long n_points, int nb, const double2 *chi0, const double2 *U
     if (st) return st;
   }
   return launch(lanes, n_points);
+}
+
+// The RPA on a bosonic (w, q) mesh (2 nw - 1 frequencies, k mesh dims) with
+// conjugate pairs solved once (rpa_pair_kernel); lanes per point as the point
+// form uses (the autotuner's rpa_group wisdom, else the heuristic).
+int launch_rpa_warp_pairs(int nw, const int dims[3], int nb, const double2 *chi0, const double2 *U, double2 *chi,
+                          cudaStream_t stream, unsigned *status) {
+  const int N = nb * nb;
+  const size_t u_bytes = ((size_t)N * N * (sizeof(double2) + sizeof(int)) + (N + 1) * sizeof(int) + 15) & ~(size_t)15;
+  std::vector<int> cands;
+  for (int g : {8, 9, 16, 32})
+    if ((g != 9 || N == 9) && u_bytes + (size_t)(32 / g) * 2 * N * N * 16 <= (size_t)max_smem_optin() - 64)
+      cands.push_back(g);
+  auto launch = [&](int lanes, int nw_run) -> int {
+    switch (lanes) {
+      case 8: return launch_pair_g<8>(nw_run, dims, nb, chi0, U, chi, stream, status);
+      case 9: return launch_pair_g<9>(nw_run, dims, nb, chi0, U, chi, stream, status);
+      case 16: return launch_pair_g<16>(nw_run, dims, nb, chi0, U, chi, stream, status);
+      default: return launch_pair_g<32>(nw_run, dims, nb, chi0, U, chi, stream, status);
+    }
+  };
+  int lanes = rpa_group_lanes(nb);
+  int st;
+  if ((const void *)chi0 != (const void *)chi) {
+    // a trial solves the units of the first frequencies; an unpaired trial over
+    // 1 frequency (nw_run = 1: w = 0 only) writes the same values as the full run
+    st = tune_pick(tune_key("rpa_group", {nb}), cands, lanes, stream, [&](int v) { return launch(v, 1); }, &lanes);
+  } else {
+    st = tune_lookup(tune_key("rpa_group", {nb}), cands, lanes, &lanes);
+  }
+  if (st) return st;
+  return launch(lanes, nw);
 }
 
 int launch_rpa_adjoint_warp(long n_points, int nb, const double2 *chi0, const double2 *U, const double2 *chi,

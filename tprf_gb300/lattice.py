@@ -25,6 +25,17 @@ __all__ = [
 ]
 
 
+def _bosonic_wk_mesh(g):
+    """(nw, dims) when g lives on (bosonic MeshImFreq, MeshBrZone), else None."""
+    m = g.mesh
+    if not isinstance(m, MeshProduct) or len(m.components) != 2:
+        return None
+    w, k = m.components
+    if not isinstance(w, MeshImFreq) or w.statistic != "Boson" or not isinstance(k, MeshBrZone):
+        return None
+    return w.n_max, tuple(k.dims)
+
+
 def _stream() -> int:
     return torch.cuda.current_stream().cuda_stream
 
@@ -322,7 +333,13 @@ def solve_rpa_PH(chi0, U, out=None, chunk_points=None, workspace=None):
     lib = _native.lib()
     if out is None:
         res = Gf(mesh=chi0.mesh, data=torch.empty_like(chi0.data))
-        check(lib.tprf_solve_rpa_PH(n_points, nb, _ptr(src), _ptr(Ud), _ptr(res.data), _stream()), "solve_rpa_PH")
+        wk = _bosonic_wk_mesh(chi0)
+        if wk is not None:  # the mesh-aware solve: conjugate point pairs solved once
+            nw, dims = wk
+            check(lib.tprf_solve_rpa_PH_wk(nw, dims3(dims), nb, _ptr(src), _ptr(Ud), _ptr(res.data), _stream()),
+                  "solve_rpa_PH")
+        else:
+            check(lib.tprf_solve_rpa_PH(n_points, nb, _ptr(src), _ptr(Ud), _ptr(res.data), _stream()), "solve_rpa_PH")
         return res
     if out.device.type != "cpu" or out.dtype != torch.complex128 or tuple(out.shape) != tuple(chi0.data.shape) \
             or not out.is_contiguous():
