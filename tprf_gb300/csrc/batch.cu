@@ -170,8 +170,8 @@ int enqueue_instance(const tprf_instance &a, unsigned char *scratch, cudaStream_
   if ((st = launch_lattice_fft_fmt(false, 2L * a.nw - 1, a.dims, nb4, chi0, chi_df, chi0, false, 1.0, s,
                                    chi_df ? gmax : nullptr)))
     return st;
-  return launch_rpa((2L * a.nw - 1) * nk, a.nb, chi0, reinterpret_cast<const double2 *>(a.U),
-                    reinterpret_cast<double2 *>(a.chi), s);
+  return launch_rpa_wk(a.nw, a.dims, a.nb, chi0, reinterpret_cast<const double2 *>(a.U),
+                       reinterpret_cast<double2 *>(a.chi), s);
 }
 
 // The adjoint chain of one instance (the transposes of enqueue_instance's

@@ -171,6 +171,11 @@ int launch_dyson_adjoint(int n_iw, long n_k, int nb, const double2 *g, const dou
 int launch_rpa_adjoint(long n_points, int nb, const double2 *chi0, const double2 *U, const double2 *chi,
                        const double2 *chig, double2 *chi0g, double2 *Ug, cudaStream_t stream, unsigned *status);
 
+// The RPA on a bosonic (w, q) mesh: conjugate point pairs solved once where
+// U is real and chi0 is bit for bit conjugate-symmetric (rpa.cu).
+int launch_rpa_wk(int nw, const int dims[3], int nb, const double2 *chi0, const double2 *U, double2 *chi,
+                  cudaStream_t stream);
+
 // Autotuner (tune.cu): the wisdom value of `key` if one is recorded and is
 // among the candidates; else, in measure mode and outside a stream capture,
 // times launch(v) for every candidate on `s` and records the fastest; else the

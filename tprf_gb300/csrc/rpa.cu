@@ -36,7 +36,7 @@ namespace {
 // from double-float to FP64.
 template <int NB, int NT, class E>
 __device__ double rpa_point(const double2 *x, double2 *y, E *A, int *perm, const E *s_val, const int *s_off,
-                            const int *s_cs, bool &singular) {
+                            const int *s_cs, bool &singular, double2 *y_conj = nullptr) {
   constexpr int N = NB * NB;
 #define AE(i, k) A[((i) * N + (k)) * NT]
   double amax = 0.0;
@@ -125,7 +125,11 @@ __device__ double rpa_point(const double2 *x, double2 *y, E *A, int *perm, const
       b[r] = cmul(b[r], F[(r * N + r) * NT]);
     }
 #pragma unroll
-    for (int r = 0; r < N; ++r) y[r * N + cm] = el_to(b[r]);
+    for (int r = 0; r < N; ++r) {
+      const double2 v = el_to(b[r]);
+      y[r * N + cm] = v;
+      if (y_conj) y_conj[r * N + cm] = make_double2(v.x, -v.y);  // the conjugate system's solve
+    }
   }
 #undef AE
   return pmin > 0.0 ? amax / pmin : 1e300;
@@ -186,6 +190,95 @@ __global__ void __launch_bounds__(NT) rpa_lu_kernel(long n_points, const double2
     }
     if (singular) atomicOr(status, kDevErrSingular);
   }
+}
+
+// Conjugate point pairs on a bosonic (w, q) mesh, one thread per unit (the
+// pairing of rpa_pair_kernel in rpa_warp.cu): with U real and chi0(-w, -q) bit
+// for bit conj(chi0(w, q)), the pair is solved once and both results stored.
+template <int NB, int NT, class E>
+__global__ void __launch_bounds__(NT) rpa_lu_pair_kernel(int nw, int d0, int d1, int d2, const double2 *chi0,
+                                                         const double2 *__restrict__ U, double2 *chi,
+                                                         unsigned *status) {
+  constexpr int N = NB * NB;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  E *s_val = reinterpret_cast<E *>(smem_raw);
+  unsigned char *lu_base = smem_raw + (size_t)N * N * sizeof(E);
+  int *s_off = reinterpret_cast<int *>(lu_base + (size_t)N * N * NT * 16);
+  int *s_cs = s_off + N * N;
+  int *perm = s_cs + N + 1 + threadIdx.x;
+  __shared__ int s_ureal;
+  if (threadIdx.x == 0) {
+    int t = 0, ureal = 1;
+    for (int c = 0; c < N; ++c) {
+      s_cs[c] = t;
+      for (int m = 0; m < N; ++m) {
+        const double2 u = U[m * N + colmap<NB>(c)];
+        if (u.y != 0.0) ureal = 0;
+        if (u.x != 0.0 || u.y != 0.0) {
+          s_off[t] = colmap<NB>(m);
+          s_val[t] = el_from(u, (E *)nullptr);
+          ++t;
+        }
+      }
+    }
+    s_cs[N] = t;
+    s_ureal = ureal;
+  }
+  __syncthreads();
+  const bool ureal = s_ureal != 0;
+  const long nk = (long)d0 * d1 * d2, units = (long)nw * nk;
+  for (long un = blockIdx.x * (long)NT + threadIdx.x; un < units; un += (long)gridDim.x * NT) {
+    const int mh = (int)(un / nk);
+    const long q = un - (long)mh * nk;
+    const int q2 = (int)(q % d2), q1 = (int)((q / d2) % d1), q0 = (int)(q / ((long)d2 * d1));
+    const long mq = ((long)((d0 - q0) % d0) * d1 + (d1 - q1) % d1) * d2 + (d2 - q2) % d2;
+    if (mh == 0 && q > mq) continue;  // its partner (0, -q) holds this unit
+    const long p = (long)(nw - 1 + mh) * nk + q, pm = (long)(nw - 1 - mh) * nk + mq;
+    bool sym = ureal && pm != p;
+    for (int o = 0; o < N * N && sym; ++o) {
+      const double2 a = chi0[p * N * N + o], b = chi0[pm * N * N + o];
+      sym = __double_as_longlong(a.x) == __double_as_longlong(b.x) &&
+            __double_as_longlong(a.y) == __double_as_longlong(-b.y);
+    }
+    for (int k = 0; k < 2; ++k) {
+      if (k == 1 && (pm == p || sym)) break;
+      const long pt = k ? pm : p;
+      const double2 *x = chi0 + pt * N * N;
+      double2 *y = chi + pt * N * N;
+      double2 *yc = (k == 0 && sym) ? chi + pm * N * N : nullptr;
+      bool singular = false;
+      const double cond2 = rpa_point<NB, NT, E>(x, y, reinterpret_cast<E *>(lu_base) + threadIdx.x, perm, s_val,
+                                                s_off, s_cs, singular, yc);
+      if (IsDf<E>::value && !(cond2 <= kDf64CondLimit2)) {
+        double2 uval[N * N];
+        for (int t = 0; t < s_cs[N]; ++t) {
+          int c = 0;
+          while (s_cs[c + 1] <= t) ++c;
+          const int m = (s_off[t] % NB) * NB + s_off[t] / NB;
+          uval[t] = U[m * N + colmap<NB>(c)];
+        }
+        rpa_point<NB, NT, double2>(x, y, reinterpret_cast<double2 *>(lu_base) + threadIdx.x, perm, uval, s_off, s_cs,
+                                   singular, yc);
+      }
+      if (singular) atomicOr(status, kDevErrSingular);
+    }
+  }
+}
+
+template <int NB, int NT, class E>
+int launch_rpa_pair_as(int nw, const int dims[3], const double2 *chi0, const double2 *U, double2 *chi,
+                       cudaStream_t stream, unsigned *status) {
+  constexpr int N = NB * NB;
+  const size_t smem = (size_t)N * N * 16 * (1 + NT) + (size_t)(N * N + N + 1) * sizeof(int) +
+                      (size_t)N * NT * sizeof(int);
+  auto kern = rpa_lu_pair_kernel<NB, NT, E>;
+  TPRF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const long units = (long)nw * dims[0] * dims[1] * dims[2];
+  long blocks = (units + NT - 1) / NT;
+  blocks = std::max(1L, std::min(blocks, (long)num_sms() * 64));
+  kern<<<(unsigned)blocks, NT, smem, stream>>>(nw, dims[0], dims[1], dims[2], chi0, U, chi, status);
+  TPRF_LAUNCH_CHECK("rpa_lu_pair_kernel");
+  return TPRF_OK;
 }
 
 template <int NB, int NT, class E>
@@ -252,9 +345,15 @@ int launch_rpa_warp_pairs(int nw, const int dims[3], int nb, const double2 *chi0
 
 int launch_rpa_wk(int nw, const int dims[3], int nb, const double2 *chi0, const double2 *U, double2 *chi,
                   cudaStream_t stream) {
-  if (nb < 3 || nw < 1) return launch_rpa((2L * nw - 1) * dims[0] * dims[1] * dims[2], nb, chi0, U, chi, stream);
   unsigned *status = device_status_word();
   if (!status) return TPRF_ERR_CUDA;
+  const bool df = arith_mode() == kArithDF64All;  // as the point form: FP64 unless double-float everywhere
+  if (nb == 1)
+    return df ? launch_rpa_pair_as<1, 256, cdf>(nw, dims, chi0, U, chi, stream, status)
+              : launch_rpa_pair_as<1, 256, double2>(nw, dims, chi0, U, chi, stream, status);
+  if (nb == 2)
+    return df ? launch_rpa_pair_as<2, 256, cdf>(nw, dims, chi0, U, chi, stream, status)
+              : launch_rpa_pair_as<2, 256, double2>(nw, dims, chi0, U, chi, stream, status);
   if (nb > 8) return set_error(TPRF_ERR_INVALID_ARGUMENT, "solve_rpa_PH: nb must be 1..8");
   return launch_rpa_warp_pairs(nw, dims, nb, chi0, U, chi, stream, status);
 }
