@@ -132,6 +132,9 @@ constexpr float kRealInputTol = 1e-11f;
 __device__ __forceinline__ bool gmax_says_real(const unsigned *gmax) {
   return gmax != nullptr && __uint_as_float(gmax[1]) <= kRealInputTol * __uint_as_float(gmax[0]);
 }
+// The same test on G(iv, r): words [max |G|, max |G(iv) - conj(G(-iv))|]
+// (hermitian_check_kernel); Hermitian in iv means G(tau, r) is real.
+__device__ __forceinline__ bool hermitian_says_yes(const unsigned *hw) { return gmax_says_real(hw); }
 #endif
 
 // Stream-ordered launchers shared by the C-ABI entry points and the batched
@@ -159,7 +162,11 @@ int launch_chi0_wr_from_grt_df(double beta, int n_tau, int nw, const int dims[3]
 // the caller) receives max |G| and max |Im G| for launch_chi0_wr_from_grt_df,
 // which pairs real bubble columns when G is real.
 int launch_nu_to_tau_df(double beta, int n_iw, int n_tau, long C, const double2 *gw, const double2 *mom, double2 *gt,
-                        void *gt_df, cudaStream_t stream, unsigned *gmax = nullptr);
+                        void *gt_df, cudaStream_t stream, unsigned *gmax = nullptr, const unsigned *hwords = nullptr);
+// hwords (two words the caller zeroed) <- max |G(iv, r)|, max |G(iv) - conj(G(-iv))|
+// over the 2 n_iw fermionic rows of C columns; launch_nu_to_tau_df with them
+// pairs columns when G(iv, r) is Hermitian in iv.
+int launch_hermitian_check(int n_iw, long C, const double2 *gw, unsigned *hwords, cudaStream_t stream);
 int launch_tau_to_w_adjoint(double beta, int n_tau, int nw, long C, const double2 *yg, double2 *xg,
                             cudaStream_t stream);
 int launch_nu_to_tau_adjoint(double beta, int n_iw, int n_tau, long C, const double2 *yg, double2 *gg, bool fitted,

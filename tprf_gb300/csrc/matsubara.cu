@@ -129,7 +129,8 @@ template <class C>
 __global__ void __launch_bounds__(kMatsubaraThreads, 2) nu_to_tau_kernel(NuTauPlan p, const double2 *__restrict__ gw,
                                                         const double2 *__restrict__ mom, double2 *__restrict__ gt,
                                                         long Ccols, int ic, int lg, unsigned *status,
-                                                        cdf *__restrict__ gt_df, unsigned *gmax) {
+                                                        cdf *__restrict__ gt_df, unsigned *gmax,
+                                                        const unsigned *hwords) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ unsigned s_res;
   C *a = reinterpret_cast<C *>(smem_raw);
@@ -138,8 +139,25 @@ __global__ void __launch_bounds__(kMatsubaraThreads, 2) nu_to_tau_kernel(NuTauPl
   C *b = p.fft.has_generic ? a + (size_t)L * ic : nullptr;
   C *am = a + (size_t)(p.fft.has_generic ? 2 : 1) * L * ic;  // [4][ic]: a1, a2, a3, m1; then the fit coefficients
   const int tid = threadIdx.x, nthr = blockDim.x;
+  // Real pairs (double-float path, hwords saying G(iv, r) is Hermitian in iv,
+  // so G(tau, r) is real): two columns g1, g2 go through one transform as
+  // z = g1 + i g2 and G1(tau) = Re T(z), G2(tau) = Im T(z) (T is complex-linear;
+  // the fit coefficients and tail moments of such data are real). Column c of
+  // the CTA is then the pair of real columns 2 (col0 + c) and 2 (col0 + c) + 1.
+  bool pairs = false;
+  if constexpr (IsDfElem<C>::value) pairs = hermitian_says_yes(hwords);
+  const long n_units = pairs ? (Ccols + 1) / 2 : Ccols;
   const long col0 = blockIdx.x * (long)ic;
-  const int ncol = (int)min((long)ic, Ccols - col0);
+  if (col0 >= n_units) return;  // the second half of the grid in pair mode
+  const int ncol = (int)min((long)ic, n_units - col0);
+  // input of unit c at frequency row n: the column, or z of the pair
+  auto in_at = [&](long n, int c) -> double2 {
+    if (!pairs) return gw[n * Ccols + col0 + c];
+    const long f = 2 * (col0 + c);
+    const double2 g1 = gw[n * Ccols + f];
+    const double2 g2 = f + 1 < Ccols ? gw[n * Ccols + f + 1] : make_double2(0.0, 0.0);
+    return make_double2(g1.x - g2.y, g1.y + g2.x);
+  };
 
   for (int w = tid; w < L * ic; w += nthr) a[w] = czero<C>();
   if (tid == 0) s_res = 0u;
@@ -152,7 +170,7 @@ __global__ void __launch_bounds__(kMatsubaraThreads, 2) nu_to_tau_kernel(NuTauPl
     for (int u = 0; u < 4; ++u) {
       const int w = w0 + u * nthr;
       const int c = w & (ic - 1), n = w >> lg;
-      if (w < nnu * ic && c < ncol) v[u] = gw[(long)n * Ccols + col0 + c];
+      if (w < nnu * ic && c < ncol) v[u] = in_at(n, c);
     }
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
@@ -171,27 +189,52 @@ __global__ void __launch_bounds__(kMatsubaraThreads, 2) nu_to_tau_kernel(NuTauPl
       const int c = w & (ic - 1), q = w >> lg;
       double2 acc = make_double2(0.0, 0.0);
       if (c < ncol)
-        for (int i = 0; i < nf; ++i) acc = cfma(p.fitF[q * nf + i], gw[(long)p.fit_row[i] * Ccols + col0 + c], acc);
+        for (int i = 0; i < nf; ++i) acc = cfma(p.fitF[q * nf + i], in_at(p.fit_row[i], c), acc);
       coef[q * ic + c] = acc;
     }
     __syncthreads();
     for (int w = tid; w < nf * ic; w += nthr) {
       const int c = w & (ic - 1), i = w >> lg;
       if (c >= ncol) continue;
-      double2 model = make_double2(0.0, 0.0);
-      for (int q = 0; q < nm; ++q) model = cfma(p.fitG[i * nm + q], coef[q * ic + c], model);
-      const double2 d = csub(model, gw[(long)p.fit_row[i] * Ccols + col0 + c]);
-      atomicMax(&s_res, __float_as_uint(sqrtf((float)cabs2(d))));  // compared with 1e-3
+      if (!pairs) {
+        double2 model = make_double2(0.0, 0.0);
+        for (int q = 0; q < nm; ++q) model = cfma(p.fitG[i * nm + q], coef[q * ic + c], model);
+        const double2 d = csub(model, gw[(long)p.fit_row[i] * Ccols + col0 + c]);
+        atomicMax(&s_res, __float_as_uint(sqrtf((float)cabs2(d))));  // compared with 1e-3
+      } else {
+        // each real column of the pair against its own model (real and imaginary
+        // parts of the pair's coefficients)
+        const long f = 2 * (col0 + c);
+        for (int h = 0; h < 2 && f + h < Ccols; ++h) {
+          double2 model = make_double2(0.0, 0.0);
+          for (int q = 0; q < nm; ++q) {
+            const double2 cq = coef[q * ic + c];
+            model = cfma(p.fitG[i * nm + q], make_double2(h ? cq.y : cq.x, 0.0), model);
+          }
+          const double2 d = csub(model, gw[(long)p.fit_row[i] * Ccols + f + h]);
+          atomicMax(&s_res, __float_as_uint(sqrtf((float)cabs2(d))));
+        }
+      }
     }
     for (int c = tid; c < ic; c += nthr)
       tail_amplitudes(p.fermion, coef[1 * ic + c], coef[2 * ic + c], coef[3 * ic + c], am, ic, c);
   } else {
     for (int c = tid; c < ic; c += nthr) {
       double2 m1 = make_double2(0.0, 0.0), m2 = m1, m3 = m1;
-      if (c < ncol) {
+      if (c < ncol && !pairs) {
         m1 = mom[0 * Ccols + col0 + c];
         m2 = mom[1 * Ccols + col0 + c];
         m3 = mom[2 * Ccols + col0 + c];
+      } else if (c < ncol) {  // z = g1 + i g2: moments likewise
+        const long f = 2 * (col0 + c);
+        const bool two = f + 1 < Ccols;
+        auto zm = [&](int q) {
+          const double2 a1 = mom[q * Ccols + f], a2 = two ? mom[q * Ccols + f + 1] : make_double2(0.0, 0.0);
+          return make_double2(a1.x - a2.y, a1.y + a2.x);
+        };
+        m1 = zm(0);
+        m2 = zm(1);
+        m3 = zm(2);
       }
       tail_amplitudes(p.fermion, m1, m2, m3, am, ic, c);
     }
@@ -209,6 +252,20 @@ __global__ void __launch_bounds__(kMatsubaraThreads, 2) nu_to_tau_kernel(NuTauPl
     for (int j = 0; j < 3; ++j) v = cadd(v, cmul(am[j * ic + c], table<C>(p.Q, p.Qf, (long)j * L + tt)));
     // G[L] = -(G[0] + m1) for fermions, +(G[0] + m1) for bosons
     if (t == L) v = p.fermion ? csub(czero<C>(), cadd(v, am[3 * ic + c])) : cadd(v, am[3 * ic + c]);
+    if (pairs) {
+      if constexpr (IsDfElem<C>::value) {
+        const long f = 2 * (col0 + c);
+        const cdf v1 = cdf{v.x, dfl{0.f, 0.f}}, v2 = cdf{v.y, dfl{0.f, 0.f}};
+        gt[(long)t * Ccols + f] = as_d2(v1);
+        if (gt_df) gt_df[(long)t * Ccols + f] = v1;
+        if (f + 1 < Ccols) {
+          gt[(long)t * Ccols + f + 1] = as_d2(v2);
+          if (gt_df) gt_df[(long)t * Ccols + f + 1] = v2;
+        }
+        if (gmax) g_abs = fmaxf(g_abs, fmaxf(fabsf(v.x.hi), fabsf(v.y.hi)));  // both parts are real columns
+      }
+      continue;
+    }
     gt[(long)t * Ccols + col0 + c] = as_d2(v);
     if constexpr (IsDfElem<C>::value) {
       if (gt_df) gt_df[(long)t * Ccols + col0 + c] = v;  // the value before rounding to complex128
@@ -882,7 +939,7 @@ __global__ void __launch_bounds__(256) bubble_adjoint_kernel(BubbleLoader ld, co
 
 int launch_nu_to_tau_stat(double beta, int n_iw, int n_tau, bool fermion, long C, const double2 *gw,
                           const double2 *mom, double2 *gt, cudaStream_t stream, cdf *gt_df = nullptr,
-                          unsigned *gmax = nullptr);
+                          unsigned *gmax = nullptr, const unsigned *hwords = nullptr);
 
 // The fermionic transform that also writes G(tau) as double-float pairs into
 // gt_df (left untouched in the FP64 arithmetic mode), for the fused bubble's
@@ -890,8 +947,38 @@ int launch_nu_to_tau_stat(double beta, int n_iw, int n_tau, bool fermion, long C
 // gmax (nullable, two words the caller zeroed): max |G| and max |Im G| of the
 // result as float bits, which decide whether the bubble can pair real columns.
 int launch_nu_to_tau_df(double beta, int n_iw, int n_tau, long C, const double2 *gw, const double2 *mom, double2 *gt,
-                        void *gt_df, cudaStream_t stream, unsigned *gmax) {
-  return launch_nu_to_tau_stat(beta, n_iw, n_tau, true, C, gw, mom, gt, stream, reinterpret_cast<cdf *>(gt_df), gmax);
+                        void *gt_df, cudaStream_t stream, unsigned *gmax, const unsigned *hwords) {
+  return launch_nu_to_tau_stat(beta, n_iw, n_tau, true, C, gw, mom, gt, stream, reinterpret_cast<cdf *>(gt_df), gmax,
+                               hwords);
+}
+
+__global__ void __launch_bounds__(256) hermitian_check_kernel(const double2 *__restrict__ gw, int n_iw, long C,
+                                                              unsigned *hw) {
+  float g_abs = 0.f, g_dev = 0.f;
+  const long total = (long)n_iw * C;  // rows i < n_iw against rows 2 n_iw - 1 - i
+  for (long idx = blockIdx.x * (long)blockDim.x + threadIdx.x; idx < total; idx += (long)gridDim.x * blockDim.x) {
+    const long i = idx / C, c = idx - i * C;
+    const double2 a = gw[i * C + c], b = gw[(2L * n_iw - 1 - i) * C + c];
+    g_abs = fmaxf(g_abs, (float)fmax(sqrt(cabs2(a)), sqrt(cabs2(b))));
+    g_dev = fmaxf(g_dev, (float)sqrt(cabs2(make_double2(a.x - b.x, a.y + b.y))));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    g_abs = fmaxf(g_abs, __shfl_xor_sync(0xffffffffu, g_abs, o));
+    g_dev = fmaxf(g_dev, __shfl_xor_sync(0xffffffffu, g_dev, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(hw, __float_as_uint(g_abs));
+    atomicMax(hw + 1, __float_as_uint(g_dev));
+  }
+}
+
+int launch_hermitian_check(int n_iw, long C, const double2 *gw, unsigned *hwords, cudaStream_t stream) {
+  const long total = (long)n_iw * C;
+  const unsigned blocks = (unsigned)std::max(1L, std::min((total + 255) / 256, (long)num_sms() * 8));
+  hermitian_check_kernel<<<blocks, 256, 0, stream>>>(gw, n_iw, C, hwords);
+  TPRF_LAUNCH_CHECK("hermitian_check_kernel");
+  return TPRF_OK;
 }
 
 int launch_nu_to_tau(double beta, int n_iw, int n_tau, long C, const double2 *gw, const double2 *mom, double2 *gt,
@@ -902,7 +989,8 @@ int launch_nu_to_tau(double beta, int n_iw, int n_tau, long C, const double2 *gw
 // n: fermionic n_max or bosonic nw; the time mesh must hold L >= 2 n points
 // (fourier_matsubara.cpp:250-254).
 int launch_nu_to_tau_stat(double beta, int n_iw, int n_tau, bool fermion, long C, const double2 *gw,
-                          const double2 *mom, double2 *gt, cudaStream_t stream, cdf *gt_df, unsigned *gmax) {
+                          const double2 *mom, double2 *gt, cudaStream_t stream, cdf *gt_df, unsigned *gmax,
+                          const unsigned *hwords) {
   if (n_tau < 0) n_tau = default_n_tau(n_iw);
   if (!(beta > 0.0) || n_iw < 1 || n_tau < 2 || C < 1 || (!fermion && n_iw < 2))
     return set_error(TPRF_ERR_INVALID_ARGUMENT, "fourier_wr_to_tr: bad mesh");
@@ -929,11 +1017,11 @@ int launch_nu_to_tau_stat(double beta, int n_iw, int n_tau, bool fermion, long C
       TPRF_CUDA(cudaFuncSetAttribute(nu_to_tau_kernel<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
       nu_to_tau_kernel<double2><<<(unsigned)blocks, kMatsubaraThreads, sm, stream>>>(*p, gw, mom, gt, C, icv,
                                                                                       log2_ic(icv), status, nullptr,
-                                                                                      gmax);
+                                                                                      gmax, nullptr);
     } else {
       TPRF_CUDA(cudaFuncSetAttribute(nu_to_tau_kernel<cdf>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
       nu_to_tau_kernel<cdf><<<(unsigned)blocks, kMatsubaraThreads, sm, stream>>>(*p, gw, mom, gt, C, icv, log2_ic(icv),
-                                                                                  status, gt_df, gmax);
+                                                                                  status, gt_df, gmax, hwords);
     }
     TPRF_LAUNCH_CHECK("nu_to_tau_kernel");
     return TPRF_OK;

@@ -68,9 +68,12 @@ extern "C" int tprf_imtime_bubble_chi0_wk_timed(double beta, int n_iw, int n_tau
   if ((st = mark(0))) return st;
   st = launch_lattice_fft(true, 2L * n_iw, dims, nb2, reinterpret_cast<const double2 *>(g_wk), g_wr, s);
   if (st || (st = mark(1))) return st;
-  TPRF_CUDA(cudaMemsetAsync(gmax, 0, 2 * sizeof(unsigned), s));
+  // gmax[0..1]: the real-input test of G(tau, r); gmax[2..3]: the Hermitian
+  // test of G(iv, r), which lets iv -> tau pair real columns
+  TPRF_CUDA(cudaMemsetAsync(gmax, 0, 4 * sizeof(unsigned), s));
+  if ((st = launch_hermitian_check(n_iw, nk * nb2, g_wr, gmax + 2, s))) return st;
   st = launch_nu_to_tau_df(beta, n_iw, n_tau, nk * nb2, g_wr, reinterpret_cast<const double2 *>(moments), g_tr,
-                           g_tr_df, s, gmax);
+                           g_tr_df, s, gmax, gmax + 2);
   if (st || (st = mark(2))) return st;
   // chi0(w, r) goes from the bubble to the r -> q transform as double-float
   // pairs (same bytes) on the double-float path: no conversion in between
