@@ -345,21 +345,21 @@ def run_gpu(args):
         kmesh = T.MeshBrZone(dims=dims)
         del g_wk, ws, chi0, chi
         torch.cuda.empty_cache()
-        ws = torch.empty(T.lattice_utils.bubble_workspace_bytes(n_max, n_tau, dims, nb), dtype=torch.uint8,
-                         device=dev)
         lib.tprf_set_sync_checks(1)
-
-        chunk = -(-points // 32)
-        ring = torch.empty(lib.tprf_solve_rpa_PH_to_host_workspace_bytes(chunk, nb, 3), dtype=torch.uint8, device=dev)
+        from tprf_gb300.lattice_utils import imtime_bubble_rpa_wk
+        block = max(1, -(-nw // 16))
+        fws = torch.empty(lib.tprf_imtime_bubble_rpa_to_host_workspace_bytes(n_max, n_tau, nw, d3, nb, block, 3),
+                          dtype=torch.uint8, device=dev)
+        chi0_buf = torch.empty((nwt, nk) + (nb,) * 4, dtype=torch.complex128, device=dev)
 
         def e2e_step():
-            # chi is streamed into the pinned host buffer while the RPA solves (out=)
+            # the public API: Dyson, then the bubble chain and the RPA in one call with chi
+            # copied to the pinned host buffer in frequency blocks while later blocks solve
             ekd = ek_host.to(dev, non_blocking=True)
             g = T.lattice_dyson_g0_wk(mu, T.Gf(mesh=kmesh, data=ekd), wmesh)
-            c0 = T.imtime_bubble_chi0_wk(g, nw=nw, verbose=False, workspace=ws)
+            imtime_bubble_rpa_wk(g, cfg["U"], nw, out=out_host, block_freqs=block, slots=3, chi0=chi0_buf,
+                                 workspace=fws)
             del g
-            T.solve_rpa_PH(c0, cfg["U"], out=out_host, chunk_points=chunk, workspace=ring)
-            del c0
 
         e2e_steps = max(1, min(args.steps, 3))
         e2e_step()
@@ -371,7 +371,8 @@ def run_gpu(args):
         torch.cuda.synchronize()
         e2e_s = max_over_ranks((time.perf_counter() - t0) / e2e_steps, world, dev)
         e2e = {"value": world * points / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(ek_host.numel() * C16),
-               "d2h_bytes_per_step": int(out_host.numel() * C16)}
+               "d2h_bytes_per_step": int(out_host.numel() * C16),
+               "path": "lattice_dyson_g0_wk -> imtime_bubble_rpa_wk (chain + RPA, chi to pinned host memory)"}
 
     # ---- roofline of the dominant kernel
     model = stage_model(nb, nk, n_nu, n_tau, nw)

@@ -248,6 +248,21 @@ int tprf_solve_rpa_PH(long n_points, int nb, const double *chi0, const double *U
 int tprf_solve_rpa_PH_wk(int nw, const int dims[3], int nb, const double *chi0, const double *U, double *chi,
                          void *stream);
 
+/* imtime_bubble_chi0_wk followed by solve_rpa_PH (lattice_utils.py:191-269,
+ * rpa.cpp:29-68) with chi written to host memory (chi_host: pinned, shape of
+ * chi_wk). chi0_wk is a device buffer of chi_wk's shape, used as scratch (it
+ * ends holding chi0 for the frequencies the blocks transformed). The r -> q
+ * transform, the RPA and the copies to the host run in blocks of block_freqs
+ * bosonic frequencies with `slots` device buffers (1..8), so that the copy of
+ * one block overlaps the solve of the next. Same chi as the two calls.
+ * Returns when chi is on the host. No reference counterpart as one call. */
+size_t tprf_imtime_bubble_rpa_to_host_workspace_bytes(int n_iw, int n_tau, int nw, const int dims[3], int nb,
+                                                      int block_freqs, int slots);
+int tprf_imtime_bubble_rpa_to_host(double beta, int n_iw, int n_tau, int nw, const int dims[3], int nb,
+                                   const double *g_wk, const double *moments, const double *U, double *chi0_wk,
+                                   double *chi_host, int block_freqs, int slots, void *workspace,
+                                   size_t workspace_bytes, void *stream);
+
 /* solve_rpa_PH with chi written to HOST memory, as the reference's C++ function
  * returns it (rpa.cpp:29-68 returns a host gf). The points are solved in chunks
  * of `chunk_points` into a device ring held in `workspace` (one slot per chunk of

@@ -457,3 +457,22 @@ def test_rpa_on_the_wk_mesh_equals_the_point_solve(cuda_lib, case, u_kind):
     assert torch.equal(chi.data, flat)
     ref0 = O.imtime_bubble_chi0_wk(O.lattice_dyson_g0_wk(0.0, ek, beta, n_max), beta, dims, nw=6)
     assert rel_err(chi.data, O.solve_rpa_PH(ref0, U)) < PARITY_RTOL
+
+
+@pytest.mark.parametrize("case", range(len(CASES)))
+@pytest.mark.parametrize("block_freqs,slots", [(2, 2), (1, 3), (8, 1)])
+def test_fused_chain_and_rpa_to_host_equals_the_two_calls(cuda_lib, case, block_freqs, slots):
+    """imtime_bubble_rpa_wk (r -> q, RPA and host copies in frequency blocks)
+    gives exactly solve_rpa_PH(imtime_bubble_chi0_wk(...)), real and complex U."""
+    T = tp()
+    from tprf_gb300.lattice_utils import imtime_bubble_rpa_wk
+    hopf, dims, beta, n_max = CASES[case]
+    ek, g_wk, _, _ = _g_wr(hopf(), dims, beta, n_max)
+    nb = ek.shape[-1]
+    rng = np.random.default_rng(20 + case)
+    for U in (0.3 * rng.standard_normal((nb,) * 4) + 0j,
+              0.3 * rng.standard_normal((nb,) * 4) + 0.05j * rng.standard_normal((nb,) * 4)):
+        two = T.solve_rpa_PH(T.imtime_bubble_chi0_wk(g_wk, nw=5, verbose=False), U)
+        fused = imtime_bubble_rpa_wk(g_wk, U, 5, block_freqs=block_freqs, slots=slots)
+        torch.cuda.synchronize()
+        assert torch.equal(fused.data, two.data.cpu())

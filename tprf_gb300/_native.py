@@ -57,6 +57,10 @@ SIGNATURES = {
     "tprf_chi_w0r_from_chi_tr": (c_int, [c_double, c_int, c_long, c_long, c_void_p, c_void_p, c_void_p]),
     "tprf_solve_rpa_PH": (c_int, [c_long, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
     "tprf_solve_rpa_PH_wk": (c_int, [c_int, c_int3, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "tprf_imtime_bubble_rpa_to_host_workspace_bytes": (c_size_t, [c_int, c_int, c_int, c_int3, c_int, c_int, c_int]),
+    "tprf_imtime_bubble_rpa_to_host": (c_int, [c_double, c_int, c_int, c_int, c_int3, c_int, c_void_p, c_void_p,
+                                               c_void_p, c_void_p, c_void_p, c_int, c_int, c_void_p, c_size_t,
+                                               c_void_p]),
     "tprf_lindhard_chi00_workspace_bytes": (c_size_t, [c_long, c_int]),
     "tprf_lindhard_chi00": (c_int, [c_long, c_int3, c_int, c_void_p, c_double, c_double, c_int, c_void_p, c_void_p,
                                     c_size_t, c_void_p]),

@@ -1,0 +1,171 @@
+// The bubble chain and the RPA in one call, with chi streamed to host memory:
+// imtime_bubble_chi0_wk (lattice_utils.py:191-269) followed by solve_rpa_PH
+// (rpa.cpp:29-68) as a TPRF user chains them, for callers that want chi on the
+// host. Copying chi to the host (21.7 GB for the 3-orbital 32^3 case at about
+// 193 GB/s on GB300) takes longer than the RPA itself, so the r -> q transform,
+// the RPA and the copies run block by block over the bosonic frequencies: the
+// copy of one block overlaps the transform and solve of the next, and the copy
+// starts as soon as the first block is solved rather than after all of chi0.
+//
+// On a real bubble (the chain's real-input words) a block holds the
+// frequencies m = m0 .. m1-1 >= 0: r -> q on those rows, the rows -m filled by
+// symmetry, chi0(-w, q) = conj(chi0(w, -q)), and the conjugate-pair solve,
+// which writes both signs. Otherwise a block is a range of rows of the whole
+// mesh, transformed and solved point by point.
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <vector>
+
+#include "common.cuh"
+
+namespace tprf {
+int bubble_to_wr(double beta, int n_iw, int n_tau, int nw, const int dims[3], int nb, const double *g_wk,
+                 const double *moments, double2 *out, void *workspace, size_t workspace_bytes, void *const *events,
+                 cudaStream_t s, bool *chi_df, unsigned **gmax_out);
+int launch_rpa(long n_points, int nb, const double2 *chi0, const double2 *U, double2 *chi, cudaStream_t stream);
+
+namespace {
+
+constexpr int kMaxSlots = 8;
+
+// rows -m for m in [m_lo, m_hi) of x [2 nw - 1][N_k][n_target] from rows m:
+// x(-m, q) = conj(x(m, -q)), complex128
+__global__ void __launch_bounds__(256) mirror_rows_kernel(double2 *x, int nw, int m_lo, int m_hi, int d0, int d1,
+                                                          int d2, long n_target) {
+  const long nk = (long)d0 * d1 * d2, per = nk * n_target, total = (long)(m_hi - m_lo) * per;
+  for (long idx = blockIdx.x * (long)blockDim.x + threadIdx.x; idx < total; idx += (long)gridDim.x * blockDim.x) {
+    const int m = m_lo + (int)(idx / per);
+    const long rem = idx - (long)(m - m_lo) * per;
+    const long k = rem / n_target, e = rem - k * n_target;
+    const int k2 = (int)(k % d2), k1 = (int)((k / d2) % d1), k0 = (int)(k / ((long)d2 * d1));
+    const long mk = ((long)((d0 - k0) % d0) * d1 + (d1 - k1) % d1) * d2 + (d2 - k2) % d2;
+    const double2 v = x[((long)(nw - 1 + m) * nk + mk) * n_target + e];
+    x[((long)(nw - 1 - m) * nk + k) * n_target + e] = make_double2(v.x, -v.y);
+  }
+}
+
+// One copy stream and its events per device, created on first use.
+struct CopyCtx {
+  bool ready = false;
+  cudaStream_t copy = nullptr;
+  cudaEvent_t computed[kMaxSlots], copied[kMaxSlots], done;
+};
+std::mutex g_copy_mu;
+std::map<int, CopyCtx> g_copy;
+
+int copy_ctx(CopyCtx **out) {
+  int dev = 0;
+  TPRF_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lock(g_copy_mu);
+  CopyCtx &c = g_copy[dev];
+  if (!c.ready) {
+    TPRF_CUDA(cudaStreamCreateWithFlags(&c.copy, cudaStreamNonBlocking));
+    for (int i = 0; i < kMaxSlots; ++i) {
+      TPRF_CUDA(cudaEventCreateWithFlags(&c.computed[i], cudaEventDisableTiming));
+      TPRF_CUDA(cudaEventCreateWithFlags(&c.copied[i], cudaEventDisableTiming));
+    }
+    TPRF_CUDA(cudaEventCreateWithFlags(&c.done, cudaEventDisableTiming));
+    c.ready = true;
+  }
+  *out = &c;
+  return TPRF_OK;
+}
+
+size_t slot_bytes(int block_freqs, long row) { return (2 * (size_t)block_freqs * row * sizeof(double2) + 255) & ~size_t(255); }
+
+}  // namespace
+}  // namespace tprf
+
+using namespace tprf;
+
+extern "C" size_t tprf_imtime_bubble_rpa_to_host_workspace_bytes(int n_iw, int n_tau, int nw, const int dims[3], int nb,
+                                                                 int block_freqs, int slots) {
+  if (!dims || nb < 1 || block_freqs < 1 || slots < 1) return 0;
+  if (n_tau < 0) n_tau = default_n_tau(n_iw);
+  const long row = (long)dims[0] * dims[1] * dims[2] * nb * nb * nb * nb;
+  return tprf_imtime_bubble_workspace_bytes(n_iw, n_tau, dims, nb) + (size_t)slots * slot_bytes(block_freqs, row) + 256;
+}
+
+extern "C" int tprf_imtime_bubble_rpa_to_host(double beta, int n_iw, int n_tau, int nw, const int dims[3], int nb,
+                                              const double *g_wk, const double *moments, const double *U,
+                                              double *chi0_wk, double *chi_host, int block_freqs, int slots,
+                                              void *workspace, size_t workspace_bytes, void *stream) {
+  if (!dims || !g_wk || !U || !chi0_wk || !chi_host || !workspace || nb < 1 || nb > 8 || nw < 1 || n_iw < 1 ||
+      block_freqs < 1 || slots < 1 || slots > kMaxSlots)
+    return set_error(TPRF_ERR_INVALID_ARGUMENT, "imtime_bubble_rpa_to_host: bad shape, slots or null pointer");
+  if (n_tau < 0) n_tau = default_n_tau(n_iw);
+  if (workspace_bytes < tprf_imtime_bubble_rpa_to_host_workspace_bytes(n_iw, n_tau, nw, dims, nb, block_freqs, slots))
+    return set_error(TPRF_ERR_ALLOC, "imtime_bubble_rpa_to_host: workspace smaller than its workspace-bytes query");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const long nk = (long)dims[0] * dims[1] * dims[2], nb4 = (long)nb * nb * nb * nb, row = nk * nb4;
+  const size_t chain_bytes = tprf_imtime_bubble_workspace_bytes(n_iw, n_tau, dims, nb);
+  double2 *chi0 = reinterpret_cast<double2 *>(chi0_wk);
+  double2 *host = reinterpret_cast<double2 *>(chi_host);
+  const double2 *Ud = reinterpret_cast<const double2 *>(U);
+  bool chi_df = false;
+  unsigned *gmax = nullptr;
+  int st = bubble_to_wr(beta, n_iw, n_tau, nw, dims, nb, g_wk, moments, chi0, workspace, chain_bytes, nullptr, s,
+                        &chi_df, &gmax);
+  if (st) return st;
+  // the plan depends on whether the bubble was real: read its two words
+  bool real = false;
+  if (chi_df && nw >= 2) {
+    unsigned w[2];
+    TPRF_CUDA(cudaMemcpyAsync(w, gmax, sizeof(w), cudaMemcpyDeviceToHost, s));
+    TPRF_CUDA(cudaStreamSynchronize(s));
+    float a, b;
+    memcpy(&a, &w[0], 4);
+    memcpy(&b, &w[1], 4);
+    real = b <= kRealInputTol * a;
+  }
+  const uintptr_t ring0 = (reinterpret_cast<uintptr_t>(workspace) + chain_bytes + 255) & ~uintptr_t(255);
+  const size_t sb = slot_bytes(block_freqs, row);
+  CopyCtx *c = nullptr;
+  if ((st = copy_ctx(&c))) return st;
+  TPRF_CUDA(cudaEventRecord(c->done, s));  // the copy stream starts after the chain
+  TPRF_CUDA(cudaStreamWaitEvent(c->copy, c->done, 0));
+  const int n_w = 2 * nw - 1;
+  const int n_blocks = real ? (nw + block_freqs - 1) / block_freqs : (n_w + block_freqs - 1) / block_freqs;
+  for (int k = 0; k < n_blocks; ++k) {
+    const int slot = k % slots;
+    double2 *pos = reinterpret_cast<double2 *>(ring0 + (size_t)slot * sb);
+    double2 *neg = pos + (long)block_freqs * row;
+    if (k >= slots) TPRF_CUDA(cudaStreamWaitEvent(s, c->copied[slot], 0));
+    if (real) {
+      const int m0 = k * block_freqs, m1 = std::min(nw, m0 + block_freqs), m_lo = std::max(m0, 1);
+      double2 *rows = chi0 + (long)(nw - 1 + m0) * row;
+      if ((st = launch_lattice_fft_fmt(false, m1 - m0, dims, nb4, rows, chi_df, rows, false, 1.0, s))) return st;
+      if (m_lo < m1) {
+        const long total = (long)(m1 - m_lo) * row;
+        const unsigned blocks = (unsigned)std::min((total + 255) / 256, (long)num_sms() * 16);
+        mirror_rows_kernel<<<blocks, 256, 0, s>>>(chi0, nw, m_lo, m1, dims[0], dims[1], dims[2], nb4);
+        TPRF_LAUNCH_CHECK("mirror_rows_kernel");
+      }
+      // frequency m at pos row m - m0; frequency -m (m >= m_lo) at neg row m1 - 1 - m
+      const PairOut out{pos, neg + (long)(m1 - 1 - m0) * row, row, -row, m0, m1};
+      if ((st = launch_rpa_wk_block(nw, dims, nb, chi0, Ud, out, s))) return st;
+      TPRF_CUDA(cudaEventRecord(c->computed[slot], s));
+      TPRF_CUDA(cudaStreamWaitEvent(c->copy, c->computed[slot], 0));
+      TPRF_CUDA(cudaMemcpyAsync(host + (long)(nw - 1 + m0) * row, pos, (size_t)(m1 - m0) * row * sizeof(double2),
+                                cudaMemcpyDeviceToHost, c->copy));
+      if (m_lo < m1)
+        TPRF_CUDA(cudaMemcpyAsync(host + (long)(nw - m1) * row, neg, (size_t)(m1 - m_lo) * row * sizeof(double2),
+                                  cudaMemcpyDeviceToHost, c->copy));
+    } else {
+      const int r0 = k * block_freqs, r1 = std::min(n_w, r0 + block_freqs);
+      double2 *rows = chi0 + (long)r0 * row;
+      if ((st = launch_lattice_fft_fmt(false, r1 - r0, dims, nb4, rows, chi_df, rows, false, 1.0, s))) return st;
+      if ((st = launch_rpa((long)(r1 - r0) * nk, nb, rows, Ud, pos, s))) return st;
+      TPRF_CUDA(cudaEventRecord(c->computed[slot], s));
+      TPRF_CUDA(cudaStreamWaitEvent(c->copy, c->computed[slot], 0));
+      TPRF_CUDA(cudaMemcpyAsync(host + (long)r0 * row, pos, (size_t)(r1 - r0) * row * sizeof(double2),
+                                cudaMemcpyDeviceToHost, c->copy));
+    }
+    TPRF_CUDA(cudaEventRecord(c->copied[slot], c->copy));
+  }
+  TPRF_CUDA(cudaEventRecord(c->done, c->copy));
+  TPRF_CUDA(cudaStreamWaitEvent(s, c->done, 0));
+  return finish_with_checks(s, "imtime_bubble_rpa_to_host");
+}

@@ -182,6 +182,17 @@ int launch_rpa_adjoint(long n_points, int nb, const double2 *chi0, const double2
 // U is real and chi0 is bit for bit conjugate-symmetric (rpa.cu).
 int launch_rpa_wk(int nw, const int dims[3], int nb, const double2 *chi0, const double2 *U, double2 *chi,
                   cudaStream_t stream);
+// Where the pair solves of the frequencies m = mh0 .. mh1-1 (and -m) put chi:
+// frequency m >= 0 at pos + (m - mh0) row, frequency -m (m > 0) at
+// neg + (m - mh0) neg_step (element offsets; row = N_k nb^4). The whole mesh in
+// place: pos = neg = chi + (nw - 1) row, neg_step = -row, mh0 = 0, mh1 = nw.
+struct PairOut {
+  double2 *pos, *neg;
+  long row, neg_step;
+  int mh0, mh1;
+};
+int launch_rpa_wk_block(int nw, const int dims[3], int nb, const double2 *chi0, const double2 *U, PairOut out,
+                        cudaStream_t stream);
 
 // Autotuner (tune.cu): the wisdom value of `key` if one is recorded and is
 // among the candidates; else, in measure mode and outside a stream capture,

@@ -41,25 +41,29 @@ extern "C" int tprf_imtime_bubble_chi0_wk(double beta, int n_iw, int n_tau, int 
                                           workspace_bytes, nullptr, stream);
 }
 
-extern "C" int tprf_imtime_bubble_chi0_wk_timed(double beta, int n_iw, int n_tau, int nw, const int dims[3], int nb,
-                                                const double *g_wk, const double *moments, double *chi0_wk,
-                                                void *workspace, size_t workspace_bytes, void *const *events,
-                                                void *stream) {
-  if (!dims || !g_wk || !chi0_wk || !workspace || nb < 1 || nb > 8 || nw < 1 || n_iw < 1)
+namespace tprf {
+
+// The chain up to chi0(w, r) in `out` (k -> r, iv -> tau, the fused bubble);
+// events[0..3] (nullable) are recorded before and after each stage. *chi_df:
+// chi0(w, r) was written as double-float pairs; *gmax_out: the real-input words
+// of the bubble, which the r -> q mirror and the pair solves use.
+int bubble_to_wr(double beta, int n_iw, int n_tau, int nw, const int dims[3], int nb, const double *g_wk,
+                 const double *moments, double2 *out, void *workspace, size_t workspace_bytes, void *const *events,
+                 cudaStream_t s, bool *chi_df, unsigned **gmax_out) {
+  if (!dims || !g_wk || !out || !workspace || nb < 1 || nb > 8 || nw < 1 || n_iw < 1)
     return set_error(TPRF_ERR_INVALID_ARGUMENT, "imtime_bubble_chi0_wk: bad shape or null pointer");
   if (n_tau < 0) n_tau = default_n_tau(n_iw);
   const size_t need = tprf_imtime_bubble_workspace_bytes(n_iw, n_tau, dims, nb);
   if (workspace_bytes < need)
     return set_error(TPRF_ERR_ALLOC, "imtime_bubble_chi0_wk: workspace smaller than tprf_imtime_bubble_workspace_bytes");
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
   const long nk = (long)dims[0] * dims[1] * dims[2];
-  const long nb2 = (long)nb * nb, nb4 = nb2 * nb2;
+  const long nb2 = (long)nb * nb;
   uintptr_t ws = (reinterpret_cast<uintptr_t>(workspace) + 255) & ~uintptr_t(255);
   double2 *g_wr = reinterpret_cast<double2 *>(ws);
   double2 *g_tr = g_wr + 2L * n_iw * nk * nb2;
   double2 *g_tr_df = g_tr + (long)n_tau * nk * nb2;  // double-float copy, same element size
   unsigned *gmax = reinterpret_cast<unsigned *>(g_tr_df + (long)n_tau * nk * nb2);
-  double2 *out = reinterpret_cast<double2 *>(chi0_wk);
+  *gmax_out = gmax;
   auto mark = [&](int i) -> int {
     if (events && events[i]) TPRF_CUDA(cudaEventRecord(static_cast<cudaEvent_t>(events[i]), s));
     return TPRF_OK;
@@ -77,16 +81,33 @@ extern "C" int tprf_imtime_bubble_chi0_wk_timed(double beta, int n_iw, int n_tau
   if (st || (st = mark(2))) return st;
   // chi0(w, r) goes from the bubble to the r -> q transform as double-float
   // pairs (same bytes) on the double-float path: no conversion in between
-  bool chi_df = false;
+  *chi_df = false;
   if (nw == 1)
     st = launch_chi0_w0r_from_grt(beta, n_tau, dims, nb, g_tr, out, s);
   else
-    st = launch_chi0_wr_from_grt_df(beta, n_tau, nw, dims, nb, g_tr, g_tr_df, out, s, nk > 1, &chi_df, gmax,
-                                    nk > 1);
+    st = launch_chi0_wr_from_grt_df(beta, n_tau, nw, dims, nb, g_tr, g_tr_df, out, s, nk > 1, chi_df, gmax, nk > 1);
   if (st || (st = mark(3))) return st;
+  return TPRF_OK;
+}
+
+}  // namespace tprf
+
+extern "C" int tprf_imtime_bubble_chi0_wk_timed(double beta, int n_iw, int n_tau, int nw, const int dims[3], int nb,
+                                                const double *g_wk, const double *moments, double *chi0_wk,
+                                                void *workspace, size_t workspace_bytes, void *const *events,
+                                                void *stream) {
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  double2 *out = reinterpret_cast<double2 *>(chi0_wk);
+  bool chi_df = false;
+  unsigned *gmax = nullptr;
+  int st = bubble_to_wr(beta, n_iw, n_tau, nw, dims, nb, g_wk, moments, out, workspace, workspace_bytes, events, s,
+                        &chi_df, &gmax);
+  if (st) return st;
+  const long nb4 = (long)nb * nb * nb * nb;
   // on a real bubble (the same words) only the non-negative frequencies are
   // transformed; the others follow by symmetry
   st = launch_lattice_fft_fmt(false, 2L * nw - 1, dims, nb4, out, chi_df, out, false, 1.0, s, chi_df ? gmax : nullptr);
-  if (st || (st = mark(4))) return st;
+  if (st) return st;
+  if (events && events[4]) TPRF_CUDA(cudaEventRecord(static_cast<cudaEvent_t>(events[4]), s));
   return finish_with_checks(s, "imtime_bubble_chi0_wk");
 }

@@ -197,7 +197,7 @@ __global__ void __launch_bounds__(NT) rpa_lu_kernel(long n_points, const double2
 // for bit conj(chi0(w, q)), the pair is solved once and both results stored.
 template <int NB, int NT, class E>
 __global__ void __launch_bounds__(NT) rpa_lu_pair_kernel(int nw, int d0, int d1, int d2, const double2 *chi0,
-                                                         const double2 *__restrict__ U, double2 *chi,
+                                                         const double2 *__restrict__ U, PairOut out,
                                                          unsigned *status) {
   constexpr int N = NB * NB;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -226,10 +226,10 @@ __global__ void __launch_bounds__(NT) rpa_lu_pair_kernel(int nw, int d0, int d1,
   }
   __syncthreads();
   const bool ureal = s_ureal != 0;
-  const long nk = (long)d0 * d1 * d2, units = (long)nw * nk;
+  const long nk = (long)d0 * d1 * d2, units = (long)(out.mh1 - out.mh0) * nk;
   for (long un = blockIdx.x * (long)NT + threadIdx.x; un < units; un += (long)gridDim.x * NT) {
-    const int mh = (int)(un / nk);
-    const long q = un - (long)mh * nk;
+    const int mh = out.mh0 + (int)(un / nk);
+    const long q = un - (long)(mh - out.mh0) * nk;
     const int q2 = (int)(q % d2), q1 = (int)((q / d2) % d1), q0 = (int)(q / ((long)d2 * d1));
     const long mq = ((long)((d0 - q0) % d0) * d1 + (d1 - q1) % d1) * d2 + (d2 - q2) % d2;
     if (mh == 0 && q > mq) continue;  // its partner (0, -q) holds this unit
@@ -240,12 +240,15 @@ __global__ void __launch_bounds__(NT) rpa_lu_pair_kernel(int nw, int d0, int d1,
       sym = __double_as_longlong(a.x) == __double_as_longlong(b.x) &&
             __double_as_longlong(a.y) == __double_as_longlong(-b.y);
     }
+    double2 *yp = out.pos + (long)(mh - out.mh0) * out.row + q * N * N;
+    double2 *ypm = (mh == 0 ? out.pos + (long)(mh - out.mh0) * out.row : out.neg + (long)(mh - out.mh0) * out.neg_step) +
+                   mq * N * N;
     for (int k = 0; k < 2; ++k) {
       if (k == 1 && (pm == p || sym)) break;
       const long pt = k ? pm : p;
       const double2 *x = chi0 + pt * N * N;
-      double2 *y = chi + pt * N * N;
-      double2 *yc = (k == 0 && sym) ? chi + pm * N * N : nullptr;
+      double2 *y = k ? ypm : yp;
+      double2 *yc = (k == 0 && sym) ? ypm : nullptr;
       bool singular = false;
       const double cond2 = rpa_point<NB, NT, E>(x, y, reinterpret_cast<E *>(lu_base) + threadIdx.x, perm, s_val,
                                                 s_off, s_cs, singular, yc);
@@ -266,17 +269,17 @@ __global__ void __launch_bounds__(NT) rpa_lu_pair_kernel(int nw, int d0, int d1,
 }
 
 template <int NB, int NT, class E>
-int launch_rpa_pair_as(int nw, const int dims[3], const double2 *chi0, const double2 *U, double2 *chi,
+int launch_rpa_pair_as(int nw, const int dims[3], const double2 *chi0, const double2 *U, PairOut out,
                        cudaStream_t stream, unsigned *status) {
   constexpr int N = NB * NB;
   const size_t smem = (size_t)N * N * 16 * (1 + NT) + (size_t)(N * N + N + 1) * sizeof(int) +
                       (size_t)N * NT * sizeof(int);
   auto kern = rpa_lu_pair_kernel<NB, NT, E>;
   TPRF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  const long units = (long)nw * dims[0] * dims[1] * dims[2];
+  const long units = (long)(out.mh1 - out.mh0) * dims[0] * dims[1] * dims[2];
   long blocks = (units + NT - 1) / NT;
   blocks = std::max(1L, std::min(blocks, (long)num_sms() * 64));
-  kern<<<(unsigned)blocks, NT, smem, stream>>>(nw, dims[0], dims[1], dims[2], chi0, U, chi, status);
+  kern<<<(unsigned)blocks, NT, smem, stream>>>(nw, dims[0], dims[1], dims[2], chi0, U, out, status);
   TPRF_LAUNCH_CHECK("rpa_lu_pair_kernel");
   return TPRF_OK;
 }
@@ -340,22 +343,31 @@ extern "C" int tprf_solve_rpa_PH(long n_points, int nb, const double *chi0, cons
 
 // ---- RPA on a (w, q) mesh with conjugate pairs ----------------------------------------
 namespace tprf {
-int launch_rpa_warp_pairs(int nw, const int dims[3], int nb, const double2 *chi0, const double2 *U, double2 *chi,
+int launch_rpa_warp_pairs(int nw, const int dims[3], int nb, const double2 *chi0, const double2 *U, PairOut out,
                           cudaStream_t stream, unsigned *status);
+
+int launch_rpa_wk_block(int nw, const int dims[3], int nb, const double2 *chi0, const double2 *U, PairOut out,
+                        cudaStream_t stream) {
+  unsigned *status = device_status_word();
+  if (!status) return TPRF_ERR_CUDA;
+  if (nb < 1 || nb > 8) return set_error(TPRF_ERR_INVALID_ARGUMENT, "solve_rpa_PH: nb must be 1..8");
+  if (out.mh0 < 0 || out.mh1 > nw || out.mh0 >= out.mh1)
+    return set_error(TPRF_ERR_INVALID_ARGUMENT, "solve_rpa_PH: bad frequency range");
+  const bool df = arith_mode() == kArithDF64All;  // as the point form: FP64 unless double-float everywhere
+  if (nb == 1)
+    return df ? launch_rpa_pair_as<1, 256, cdf>(nw, dims, chi0, U, out, stream, status)
+              : launch_rpa_pair_as<1, 256, double2>(nw, dims, chi0, U, out, stream, status);
+  if (nb == 2)
+    return df ? launch_rpa_pair_as<2, 256, cdf>(nw, dims, chi0, U, out, stream, status)
+              : launch_rpa_pair_as<2, 256, double2>(nw, dims, chi0, U, out, stream, status);
+  return launch_rpa_warp_pairs(nw, dims, nb, chi0, U, out, stream, status);
+}
 
 int launch_rpa_wk(int nw, const int dims[3], int nb, const double2 *chi0, const double2 *U, double2 *chi,
                   cudaStream_t stream) {
-  unsigned *status = device_status_word();
-  if (!status) return TPRF_ERR_CUDA;
-  const bool df = arith_mode() == kArithDF64All;  // as the point form: FP64 unless double-float everywhere
-  if (nb == 1)
-    return df ? launch_rpa_pair_as<1, 256, cdf>(nw, dims, chi0, U, chi, stream, status)
-              : launch_rpa_pair_as<1, 256, double2>(nw, dims, chi0, U, chi, stream, status);
-  if (nb == 2)
-    return df ? launch_rpa_pair_as<2, 256, cdf>(nw, dims, chi0, U, chi, stream, status)
-              : launch_rpa_pair_as<2, 256, double2>(nw, dims, chi0, U, chi, stream, status);
-  if (nb > 8) return set_error(TPRF_ERR_INVALID_ARGUMENT, "solve_rpa_PH: nb must be 1..8");
-  return launch_rpa_warp_pairs(nw, dims, nb, chi0, U, chi, stream, status);
+  const long row = (long)dims[0] * dims[1] * dims[2] * nb * nb * nb * nb;
+  const PairOut out{chi + (long)(nw - 1) * row, chi + (long)(nw - 1) * row, row, -row, 0, nw};
+  return launch_rpa_wk_block(nw, dims, nb, chi0, U, out, stream);
 }
 }  // namespace tprf
 

@@ -253,7 +253,7 @@ __global__ void __launch_bounds__(512) rpa_warp_kernel(long n_points, int nb_in,
 template <class E, int G, int NBC = 0>
 __global__ void __launch_bounds__(512) rpa_pair_kernel(int nw, int d0, int d1, int d2, int nb_in,
                                                        const double2 *__restrict__ chi0, const double2 *__restrict__ U,
-                                                       double2 *__restrict__ chi, unsigned *status) {
+                                                       PairOut out, unsigned *status) {
   const int nb = NBC > 0 ? NBC : nb_in;
   const int N = nb * nb;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -289,10 +289,10 @@ __global__ void __launch_bounds__(512) rpa_pair_kernel(int nw, int d0, int d1, i
   const SparseU u{s_val, s_row, s_cs};
   const bool ureal = s_ureal != 0;
   if (!active) return;
-  const long nk = (long)d0 * d1 * d2, units = (long)nw * nk;
+  const long nk = (long)d0 * d1 * d2, units = (long)(out.mh1 - out.mh0) * nk;
   for (long un = (long)blockIdx.x * n_grp + grp; un < units; un += (long)gridDim.x * n_grp) {
-    const int mh = (int)(un / nk);
-    const long q = un - (long)mh * nk;
+    const int mh = out.mh0 + (int)(un / nk);
+    const long q = un - (long)(mh - out.mh0) * nk;
     const int q2 = (int)(q % d2), q1 = (int)((q / d2) % d1), q0 = (int)(q / ((long)d2 * d1));
     const long mq = ((long)((d0 - q0) % d0) * d1 + (d1 - q1) % d1) * d2 + (d2 - q2) % d2;
     if (mh == 0 && q > mq) continue;  // its partner (0, -q) holds this unit
@@ -307,7 +307,9 @@ __global__ void __launch_bounds__(512) rpa_pair_kernel(int nw, int d0, int d1, i
       }
       sym = __all_sync(gmask, sym);
     }
-    double2 *y = chi + p * N * N, *ym = chi + pm * N * N;
+    double2 *y = out.pos + (long)(mh - out.mh0) * out.row + q * N * N;
+    double2 *ym = (mh == 0 ? out.pos + (long)(mh - out.mh0) * out.row : out.neg + (long)(mh - out.mh0) * out.neg_step) +
+                  mq * N * N;
     for (int k = 0; k < 2; ++k) {
       if (k == 1 && (pm == p || sym)) break;
       const double2 *xs = k ? xm : x;
@@ -584,7 +586,7 @@ __global__ void __launch_bounds__(512) rpa_adjoint_warp_kernel(long n_points, in
 int rpa_group_lanes(int nb) { return nb <= 2 ? 8 : nb == 3 ? 9 : 32; }
 
 template <class E, int G, int NBC>
-int launch_pair_as(int nw, const int dims[3], int nb, const double2 *chi0, const double2 *U, double2 *chi,
+int launch_pair_as(int nw, const int dims[3], int nb, const double2 *chi0, const double2 *U, PairOut out,
                    cudaStream_t stream, unsigned *status) {
   const int N = nb * nb;
   const size_t u_bytes = ((size_t)N * N * (sizeof(double2) + sizeof(int)) + (N + 1) * sizeof(int) + 15) & ~(size_t)15;
@@ -607,16 +609,16 @@ int launch_pair_as(int nw, const int dims[3], int nb, const double2 *chi0, const
   }
   if (best_total == 0) return set_error(TPRF_ERR_INVALID_ARGUMENT, "solve_rpa_PH: nb too large");
   const size_t smem = u_bytes + (size_t)best_w * ppw * per_point;
-  const long units = (long)nw * dims[0] * dims[1] * dims[2], per_block = (long)best_w * ppw;
+  const long units = (long)(out.mh1 - out.mh0) * dims[0] * dims[1] * dims[2], per_block = (long)best_w * ppw;
   long blocks = (units + per_block - 1) / per_block;
   blocks = std::max(1L, std::min(blocks, (long)num_sms() * (best_total / best_w) * 8));
-  kern<<<(unsigned)blocks, 32 * best_w, smem, stream>>>(nw, dims[0], dims[1], dims[2], nb, chi0, U, chi, status);
+  kern<<<(unsigned)blocks, 32 * best_w, smem, stream>>>(nw, dims[0], dims[1], dims[2], nb, chi0, U, out, status);
   TPRF_LAUNCH_CHECK("rpa_pair_kernel");
   return TPRF_OK;
 }
 
 template <int G>
-int launch_pair_g(int nw, const int dims[3], int nb, const double2 *chi0, const double2 *U, double2 *chi,
+int launch_pair_g(int nw, const int dims[3], int nb, const double2 *chi0, const double2 *U, PairOut chi,
                   cudaStream_t stream, unsigned *status) {
   const bool fp64 = arith_mode() == kArithFP64;
   if (nb == 3)
@@ -660,7 +662,7 @@ int launch_rpa_warp(long n_points, int nb, const double2 *chi0, const double2 *U
 // The RPA on a bosonic (w, q) mesh (2 nw - 1 frequencies, k mesh dims) with
 // conjugate pairs solved once (rpa_pair_kernel); lanes per point as the point
 // form uses (the autotuner's rpa_group wisdom, else the heuristic).
-int launch_rpa_warp_pairs(int nw, const int dims[3], int nb, const double2 *chi0, const double2 *U, double2 *chi,
+int launch_rpa_warp_pairs(int nw, const int dims[3], int nb, const double2 *chi0, const double2 *U, PairOut out,
                           cudaStream_t stream, unsigned *status) {
   const int N = nb * nb;
   const size_t u_bytes = ((size_t)N * N * (sizeof(double2) + sizeof(int)) + (N + 1) * sizeof(int) + 15) & ~(size_t)15;
@@ -668,25 +670,28 @@ int launch_rpa_warp_pairs(int nw, const int dims[3], int nb, const double2 *chi0
   for (int g : {8, 9, 16, 32})
     if ((g != 9 || N == 9) && u_bytes + (size_t)(32 / g) * 2 * N * N * 16 <= (size_t)max_smem_optin() - 64)
       cands.push_back(g);
-  auto launch = [&](int lanes, int nw_run) -> int {
+  auto launch = [&](int lanes, PairOut o) -> int {
     switch (lanes) {
-      case 8: return launch_pair_g<8>(nw_run, dims, nb, chi0, U, chi, stream, status);
-      case 9: return launch_pair_g<9>(nw_run, dims, nb, chi0, U, chi, stream, status);
-      case 16: return launch_pair_g<16>(nw_run, dims, nb, chi0, U, chi, stream, status);
-      default: return launch_pair_g<32>(nw_run, dims, nb, chi0, U, chi, stream, status);
+      case 8: return launch_pair_g<8>(nw, dims, nb, chi0, U, o, stream, status);
+      case 9: return launch_pair_g<9>(nw, dims, nb, chi0, U, o, stream, status);
+      case 16: return launch_pair_g<16>(nw, dims, nb, chi0, U, o, stream, status);
+      default: return launch_pair_g<32>(nw, dims, nb, chi0, U, o, stream, status);
     }
   };
   int lanes = rpa_group_lanes(nb);
   int st;
-  if ((const void *)chi0 != (const void *)chi) {
-    // a trial solves the units of the first frequencies; an unpaired trial over
-    // 1 frequency (nw_run = 1: w = 0 only) writes the same values as the full run
-    st = tune_pick(tune_key("rpa_group", {nb}), cands, lanes, stream, [&](int v) { return launch(v, 1); }, &lanes);
+  if ((const void *)chi0 != (const void *)(out.pos - (long)(nw - 1 - out.mh0) * out.row)) {
+    // a trial solves the units of the first frequency of the range, the same
+    // values the full run writes there
+    PairOut first = out;
+    first.mh1 = out.mh0 + 1;
+    st = tune_pick(tune_key("rpa_group", {nb}), cands, lanes, stream, [&](int v) { return launch(v, first); },
+                   &lanes);
   } else {
     st = tune_lookup(tune_key("rpa_group", {nb}), cands, lanes, &lanes);
   }
   if (st) return st;
-  return launch(lanes, nw);
+  return launch(lanes, out);
 }
 
 int launch_rpa_adjoint_warp(long n_points, int nb, const double2 *chi0, const double2 *U, const double2 *chi,

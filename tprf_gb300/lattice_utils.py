@@ -54,3 +54,46 @@ def imtime_bubble_chi0_wk(g_wk, nw=1, save_memory=False, verbose=True, nt=-1, mo
         mom.data_ptr() if mom is not None else None, out.data.data_ptr(), workspace.data_ptr(), workspace.numel(),
         _stream()), "imtime_bubble_chi0_wk")
     return out
+
+
+def imtime_bubble_rpa_wk(g_wk, U, nw, out=None, nt=-1, moments=None, block_freqs=None, slots=3, chi0=None,
+                         workspace=None):
+    """chi(iw, q) = solve_rpa_PH(imtime_bubble_chi0_wk(g_wk, nw), U) with chi written
+    to host memory (``out``: a pinned complex128 host tensor of chi's shape,
+    allocated if None), the two reference calls in one: the r -> q transform,
+    the RPA and the copies to the host run in blocks of ``block_freqs`` bosonic
+    frequencies, the copy of one block overlapping the solve of the next.
+    ``chi0`` (device tensor of chi's shape) and ``workspace`` (uint8 device
+    tensor) may be given to avoid allocations. Returns a host Gf."""
+    wmesh, kmesh = _components(g_wk, (MeshImFreq, MeshBrZone), "imtime_bubble_rpa_wk")
+    nb = g_wk.target_shape[0]
+    nw = int(nw)
+    n_tau = default_n_tau(wmesh.n_max) if nt is None or nt < 0 else int(nt)
+    dev = g_wk.data.device
+    lib = _native.lib()
+    shape = (2 * nw - 1, len(kmesh)) + (nb,) * 4
+    if block_freqs is None:
+        block_freqs = max(1, -(-nw // 16))
+    need = lib.tprf_imtime_bubble_rpa_to_host_workspace_bytes(wmesh.n_max, n_tau, nw, dims3(kmesh.dims), nb,
+                                                              int(block_freqs), int(slots))
+    if workspace is None:
+        workspace = torch.empty(int(need), dtype=torch.uint8, device=dev)
+    elif workspace.numel() < need:
+        raise ValueError(f"imtime_bubble_rpa_wk: workspace needs {need} bytes")
+    if chi0 is None:
+        chi0 = torch.empty(shape, dtype=torch.complex128, device=dev)
+    if out is None:
+        out = torch.empty(shape, dtype=torch.complex128, pin_memory=True)
+    if tuple(out.shape) != shape or out.dtype != torch.complex128 or out.device.type != "cpu" or not out.is_contiguous():
+        raise ValueError("imtime_bubble_rpa_wk: out must be a contiguous complex128 host tensor of chi's shape")
+    Ud = as_device_c128(U, dev)
+    if tuple(Ud.shape) != (nb,) * 4:
+        raise ValueError(f"imtime_bubble_rpa_wk: U must have shape {(nb,) * 4}")
+    mom = as_device_c128(moments, dev) if moments is not None else None
+    src = g_wk.data.contiguous()
+    check(lib.tprf_imtime_bubble_rpa_to_host(
+        wmesh.beta, wmesh.n_max, n_tau, nw, dims3(kmesh.dims), nb, src.data_ptr(),
+        mom.data_ptr() if mom is not None else None, Ud.data_ptr(), chi0.data_ptr(), out.data_ptr(), int(block_freqs),
+        int(slots), workspace.data_ptr(), workspace.numel(), _stream()), "imtime_bubble_rpa_wk")
+    return Gf(mesh=MeshProduct(MeshImFreq(wmesh.beta, "Boson", nw), kmesh), data=out, device=torch.device("cpu"))
+
