@@ -31,18 +31,23 @@ namespace {
 constexpr int kMaxSlots = 8;
 
 // rows -m for m in [m_lo, m_hi) of x [2 nw - 1][N_k][n_target] from rows m:
-// x(-m, q) = conj(x(m, -q)), complex128
+// x(-m, q) = conj(x(m, -q)), complex128; one warp per (m, q) block
 __global__ void __launch_bounds__(256) mirror_rows_kernel(double2 *x, int nw, int m_lo, int m_hi, int d0, int d1,
                                                           int d2, long n_target) {
-  const long nk = (long)d0 * d1 * d2, per = nk * n_target, total = (long)(m_hi - m_lo) * per;
-  for (long idx = blockIdx.x * (long)blockDim.x + threadIdx.x; idx < total; idx += (long)gridDim.x * blockDim.x) {
-    const int m = m_lo + (int)(idx / per);
-    const long rem = idx - (long)(m - m_lo) * per;
-    const long k = rem / n_target, e = rem - k * n_target;
+  const long nk = (long)d0 * d1 * d2, blocks = (long)(m_hi - m_lo) * nk;
+  const int lane = threadIdx.x & 31;
+  const long warps = (long)gridDim.x * (blockDim.x >> 5);
+  for (long wb = blockIdx.x * (long)(blockDim.x >> 5) + (threadIdx.x >> 5); wb < blocks; wb += warps) {
+    const int m = m_lo + (int)(wb / nk);
+    const long k = wb - (long)(m - m_lo) * nk;
     const int k2 = (int)(k % d2), k1 = (int)((k / d2) % d1), k0 = (int)(k / ((long)d2 * d1));
     const long mk = ((long)((d0 - k0) % d0) * d1 + (d1 - k1) % d1) * d2 + (d2 - k2) % d2;
-    const double2 v = x[((long)(nw - 1 + m) * nk + mk) * n_target + e];
-    x[((long)(nw - 1 - m) * nk + k) * n_target + e] = make_double2(v.x, -v.y);
+    const double2 *src = x + ((long)(nw - 1 + m) * nk + mk) * n_target;
+    double2 *dst = x + ((long)(nw - 1 - m) * nk + k) * n_target;
+    for (long e = lane; e < n_target; e += 32) {
+      const double2 v = src[e];
+      dst[e] = make_double2(v.x, -v.y);
+    }
   }
 }
 
@@ -138,8 +143,8 @@ extern "C" int tprf_imtime_bubble_rpa_to_host(double beta, int n_iw, int n_tau, 
       double2 *rows = chi0 + (long)(nw - 1 + m0) * row;
       if ((st = launch_lattice_fft_fmt(false, m1 - m0, dims, nb4, rows, chi_df, rows, false, 1.0, s))) return st;
       if (m_lo < m1) {
-        const long total = (long)(m1 - m_lo) * row;
-        const unsigned blocks = (unsigned)std::min((total + 255) / 256, (long)num_sms() * 16);
+        const long total = (long)(m1 - m_lo) * nk;  // (m, q) blocks, a warp each
+        const unsigned blocks = (unsigned)std::min((total + 7) / 8, (long)num_sms() * 16);
         mirror_rows_kernel<<<blocks, 256, 0, s>>>(chi0, nw, m_lo, m1, dims[0], dims[1], dims[2], nb4);
         TPRF_LAUNCH_CHECK("mirror_rows_kernel");
       }

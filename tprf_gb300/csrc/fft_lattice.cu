@@ -363,21 +363,28 @@ template <class T>
 __global__ void __launch_bounds__(256) mirror_neg_freq_kernel(T *x, int nw, int d0, int d1, int d2, long n_target,
                                                               const unsigned *gmax) {
   if (!gmax_says_real(gmax)) return;
-  const long nk = (long)d0 * d1 * d2, total = (long)(nw - 1) * nk * n_target;
-  for (long idx = blockIdx.x * (long)blockDim.x + threadIdx.x; idx < total; idx += (long)gridDim.x * blockDim.x) {
-    const long e = idx % n_target, k = (idx / n_target) % nk;
-    const int mi = (int)(idx / (n_target * nk));  // m = mi - (nw - 1) < 0
+  // one warp per (m, k) block of n_target contiguous elements: the index
+  // arithmetic once per block, the copy coalesced on both sides
+  const long nk = (long)d0 * d1 * d2, blocks = (long)(nw - 1) * nk;
+  const int lane = threadIdx.x & 31;
+  const long warps = (long)gridDim.x * (blockDim.x >> 5);
+  for (long wb = blockIdx.x * (long)(blockDim.x >> 5) + (threadIdx.x >> 5); wb < blocks; wb += warps) {
+    const int mi = (int)(wb / nk);  // m = mi - (nw - 1) < 0
+    const long k = wb - (long)mi * nk;
     const int k2 = (int)(k % d2), k1 = (int)((k / d2) % d1), k0 = (int)(k / ((long)d2 * d1));
     const long mk = ((long)((d0 - k0) % d0) * d1 + (d1 - k1) % d1) * d2 + (d2 - k2) % d2;
-    const long src = ((long)(2 * (nw - 1) - mi) * nk + mk) * n_target + e;
-    T v = x[src];
-    if constexpr (std::is_same<T, double2>::value) {
-      v.y = -v.y;
-    } else {
-      v.y.hi = -v.y.hi;
-      v.y.lo = -v.y.lo;
+    const T *src = x + ((long)(2 * (nw - 1) - mi) * nk + mk) * n_target;
+    T *dst = x + wb * n_target;
+    for (long e = lane; e < n_target; e += 32) {
+      T v = src[e];
+      if constexpr (std::is_same<T, double2>::value) {
+        v.y = -v.y;
+      } else {
+        v.y.hi = -v.y.hi;
+        v.y.lo = -v.y.lo;
+      }
+      dst[e] = v;
     }
-    x[idx] = v;
   }
 }
 
@@ -485,8 +492,8 @@ int launch_lattice_fft_fmt(bool forward, long n_w, const int dims[3], long n_tar
   const long n_skip = (gmax && n_w >= 3 && (n_w & 1)) ? (n_w - 1) / 2 : 0;
   auto mirror = [&]() -> int {
     if (n_skip == 0) return TPRF_OK;
-    const long total = n_skip * (long)dims[0] * dims[1] * dims[2] * n_target;
-    const unsigned blocks = (unsigned)std::min((total + 255) / 256, (long)num_sms() * 16);
+    const long total = n_skip * (long)dims[0] * dims[1] * dims[2];  // (m, k) blocks, a warp each
+    const unsigned blocks = (unsigned)std::min((total + 7) / 8, (long)num_sms() * 16);
     if (out_df)
       mirror_neg_freq_kernel<cdf><<<blocks, 256, 0, stream>>>(static_cast<cdf *>(out), (int)(n_skip + 1), dims[0],
                                                               dims[1], dims[2], n_target, gmax);

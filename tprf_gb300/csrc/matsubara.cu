@@ -954,22 +954,26 @@ int launch_nu_to_tau_df(double beta, int n_iw, int n_tau, long C, const double2 
 
 __global__ void __launch_bounds__(256) hermitian_check_kernel(const double2 *__restrict__ gw, int n_iw, long C,
                                                               unsigned *hw) {
-  float g_abs = 0.f, g_dev = 0.f;
+  // squared magnitudes: the difference in FP64 (it cancels), everything else in
+  // FP32 (the FP64 pipe is the scarce one); the words hold the square roots
+  float g_abs2 = 0.f, g_dev2 = 0.f;
   const long total = (long)n_iw * C;  // rows i < n_iw against rows 2 n_iw - 1 - i
   for (long idx = blockIdx.x * (long)blockDim.x + threadIdx.x; idx < total; idx += (long)gridDim.x * blockDim.x) {
     const long i = idx / C, c = idx - i * C;
     const double2 a = gw[i * C + c], b = gw[(2L * n_iw - 1 - i) * C + c];
-    g_abs = fmaxf(g_abs, (float)fmax(sqrt(cabs2(a)), sqrt(cabs2(b))));
-    g_dev = fmaxf(g_dev, (float)sqrt(cabs2(make_double2(a.x - b.x, a.y + b.y))));
+    const float ax = (float)a.x, ay = (float)a.y, bx = (float)b.x, by = (float)b.y;
+    const float dx = (float)(a.x - b.x), dy = (float)(a.y + b.y);
+    g_abs2 = fmaxf(g_abs2, fmaxf(fmaf(ax, ax, ay * ay), fmaf(bx, bx, by * by)));
+    g_dev2 = fmaxf(g_dev2, fmaf(dx, dx, dy * dy));
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-    g_abs = fmaxf(g_abs, __shfl_xor_sync(0xffffffffu, g_abs, o));
-    g_dev = fmaxf(g_dev, __shfl_xor_sync(0xffffffffu, g_dev, o));
+    g_abs2 = fmaxf(g_abs2, __shfl_xor_sync(0xffffffffu, g_abs2, o));
+    g_dev2 = fmaxf(g_dev2, __shfl_xor_sync(0xffffffffu, g_dev2, o));
   }
   if ((threadIdx.x & 31) == 0) {
-    atomicMax(hw, __float_as_uint(g_abs));
-    atomicMax(hw + 1, __float_as_uint(g_dev));
+    atomicMax(hw, __float_as_uint(sqrtf(g_abs2)));
+    atomicMax(hw + 1, __float_as_uint(sqrtf(g_dev2)));
   }
 }
 
