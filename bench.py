@@ -285,7 +285,9 @@ def run_gpu(args):
     stream = torch.cuda.current_stream()
     sh = stream.cuda_stream
     lib.tprf_set_sync_checks(0)
-    launches_per_step = 1 + lattice_passes(dims) + 1 + 1 + lattice_passes(dims) + 1
+    # Dyson, k->r passes, Hermitian test, iv->tau, bubble + tau->iw, r->q passes, the
+    # negative-frequency mirror (a no-op launch on complex input), RPA
+    launches_per_step = 1 + lattice_passes(dims) + 1 + 1 + 1 + lattice_passes(dims) + 1 + 1
 
     ws_bytes = lib.tprf_imtime_bubble_workspace_bytes(n_max, n_tau, d3, nb)
     ws = torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
@@ -721,10 +723,10 @@ def measure_fp64_peak(lib, dev) -> float:
 # profiles/ (16x16x8 case, 2048 r points), scaled to 32^3 (x16) by the number of r
 # points: the kernels stream their columns, so traffic grows in proportion.
 TRAFFIC = {
-    ("cfg1", "bubble_tau_to_w"): 16 * 2.179e9,  # profiles/tau_to_w_bubble_cubic3orb_16x16x8.md
-    ("cfg1", "rpa"): 16 * 2.664e9,              # profiles/rpa_warp_cubic3orb_16x16x8.md
-    # plane pass + one-axis pass: profiles/lattice_plane_r_to_q_*.md, lattice_axis_r_to_q_*.md
-    ("cfg1", "fft_r_to_q"): 16 * (2.655e9 + 2.653e9),
+    # DRAM bytes of one launch from an ncu capture of the kernel on the 16x16x8 case,
+    # scaled to 32^3 by the columns (points) processed
+    ("cfg1", "bubble_tau_to_w"): 16 * 1.487e9,
+    ("cfg1", "rpa"): 16 * 2.727e9,
 }
 
 
