@@ -160,7 +160,8 @@ int enqueue_instance(const tprf_instance &a, unsigned char *scratch, cudaStream_
   if ((st = launch_lattice_fft(true, 2L * a.n_iw, a.dims, nb2, g_wk, g_wr, s))) return st;
   TPRF_CUDA(cudaMemsetAsync(gmax, 0, 4 * sizeof(unsigned), s));  // real-input and Hermitian tests
   if ((st = launch_hermitian_check(a.n_iw, nk * nb2, g_wr, gmax + 2, s))) return st;
-  if ((st = launch_nu_to_tau_df(a.beta, a.n_iw, nt, nk * nb2, g_wr, nullptr, g_tr, g_tr_df, s, gmax, gmax + 2)))
+  if ((st = launch_nu_to_tau_df(a.beta, a.n_iw, nt, nk * nb2, g_wr, nullptr, g_tr, g_tr_df, s, gmax, gmax + 2,
+                                a.nw > 1)))
     return st;
   bool chi_df = false;  // chi0(w, r) handed to r -> q as double-float pairs (as the single-instance chain)
   if (a.nw == 1)

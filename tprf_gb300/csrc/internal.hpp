@@ -161,8 +161,13 @@ int launch_chi0_wr_from_grt_df(double beta, int n_tau, int nw, const int dims[3]
 // iv -> tau writing the double-float copy as well; gmax (nullable, zeroed by
 // the caller) receives max |G| and max |Im G| for launch_chi0_wr_from_grt_df,
 // which pairs real bubble columns when G is real.
+// When hwords say G(iv, r) is Hermitian (G(tau, r) real), gt_df holds the real
+// parts only, one dfl (8 bytes) per element, and with fit_rows_only the
+// complex128 gt holds only the rows t <= 8 and t >= n_tau - 9 that the
+// bubble's fit samples (the fused bubble reads nothing else of it).
 int launch_nu_to_tau_df(double beta, int n_iw, int n_tau, long C, const double2 *gw, const double2 *mom, double2 *gt,
-                        void *gt_df, cudaStream_t stream, unsigned *gmax = nullptr, const unsigned *hwords = nullptr);
+                        void *gt_df, cudaStream_t stream, unsigned *gmax = nullptr, const unsigned *hwords = nullptr,
+                        bool fit_rows_only = false);
 // hwords (two words the caller zeroed) <- max |G(iv, r)|, max |G(iv) - conj(G(-iv))|
 // over the 2 n_iw fermionic rows of C columns; launch_nu_to_tau_df with them
 // pairs columns when G(iv, r) is Hermitian in iv.

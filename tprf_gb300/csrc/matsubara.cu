@@ -130,7 +130,7 @@ __global__ void __launch_bounds__(kMatsubaraThreads, 2) nu_to_tau_kernel(NuTauPl
                                                         const double2 *__restrict__ mom, double2 *__restrict__ gt,
                                                         long Ccols, int ic, int lg, unsigned *status,
                                                         cdf *__restrict__ gt_df, unsigned *gmax,
-                                                        const unsigned *hwords) {
+                                                        const unsigned *hwords, int fit_rows_only) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ unsigned s_res;
   C *a = reinterpret_cast<C *>(smem_raw);
@@ -254,13 +254,16 @@ __global__ void __launch_bounds__(kMatsubaraThreads, 2) nu_to_tau_kernel(NuTauPl
     if (t == L) v = p.fermion ? csub(czero<C>(), cadd(v, am[3 * ic + c])) : cadd(v, am[3 * ic + c]);
     if (pairs) {
       if constexpr (IsDfElem<C>::value) {
+        // real results: the double-float copy keeps the real parts only (dfl,
+        // 8 bytes), the complex128 copy all rows or the fit rows only
         const long f = 2 * (col0 + c);
-        const cdf v1 = cdf{v.x, dfl{0.f, 0.f}}, v2 = cdf{v.y, dfl{0.f, 0.f}};
-        gt[(long)t * Ccols + f] = as_d2(v1);
-        if (gt_df) gt_df[(long)t * Ccols + f] = v1;
+        const bool keep = !fit_rows_only || t <= 8 || t >= L - 8;
+        dfl *gre = reinterpret_cast<dfl *>(gt_df);
+        if (keep) gt[(long)t * Ccols + f] = as_d2(cdf{v.x, dfl{0.f, 0.f}});
+        if (gt_df) gre[(long)t * Ccols + f] = v.x;
         if (f + 1 < Ccols) {
-          gt[(long)t * Ccols + f + 1] = as_d2(v2);
-          if (gt_df) gt_df[(long)t * Ccols + f + 1] = v2;
+          if (keep) gt[(long)t * Ccols + f + 1] = as_d2(cdf{v.y, dfl{0.f, 0.f}});
+          if (gt_df) gre[(long)t * Ccols + f + 1] = v.y;
         }
         if (gmax) g_abs = fmaxf(g_abs, fmaxf(fabsf(v.x.hi), fabsf(v.y.hi)));  // both parts are real columns
       }
@@ -389,9 +392,15 @@ struct BubbleLoaderDF : BubbleLoader {
 // imaginary parts of G (rounding residue, below the bound) are dropped.
 
 struct BubblePairLoaderDF : BubbleLoaderDF {
-  const unsigned *gmax;  // [max |G|, max |Im G|] as float bits, or null: no pairs
+  // the four words of launch_nu_to_tau_df: [max |G|, max |Im G|] of G(tau, r),
+  // then the Hermitian words of G(iv, r), as float bits; null: no pairs
+  const unsigned *gmax;
   bool pairs = false;
-  __device__ __forceinline__ void init() { pairs = gmax_says_real(gmax); }
+  bool compact = false;  // gdf holds real parts only (dfl per element): iv -> tau ran on real pairs
+  __device__ __forceinline__ void init() {
+    pairs = gmax_says_real(gmax);
+    compact = pairs && hermitian_says_yes(gmax + 2);
+  }
   // offsets of the two real columns 2 (col0 + c) and 2 (col0 + c) + 1 (the
   // second past the last column reads the first: its results are not stored)
   __device__ __forceinline__ void setup(long col0, int ic, int ncol, long *s) const {
@@ -412,6 +421,10 @@ struct BubblePairLoaderDF : BubbleLoaderDF {
     if (!pairs) return BubbleLoaderDF::template get<E>(t, c, col0, ic, s);
     if constexpr (IsDfElem<E>::value) {
       const long slice = Nr * nb * nb, t1 = (long)t * slice, t2 = (long)(n_tau - 1 - t) * slice;
+      if (compact) {
+        const dfl *gre = reinterpret_cast<const dfl *>(gdf);
+        return cdf{dmul(gre[t1 + s[c]], gre[t2 + s[ic + c]]), dmul(gre[t1 + s[2 * ic + c]], gre[t2 + s[3 * ic + c]])};
+      }
       return cdf{dmul(gdf[t1 + s[c]].x, gdf[t2 + s[ic + c]].x), dmul(gdf[t1 + s[2 * ic + c]].x, gdf[t2 + s[3 * ic + c]].x)};
     } else {
       return get64(t, c, col0, ic, s);
@@ -939,7 +952,7 @@ __global__ void __launch_bounds__(256) bubble_adjoint_kernel(BubbleLoader ld, co
 
 int launch_nu_to_tau_stat(double beta, int n_iw, int n_tau, bool fermion, long C, const double2 *gw,
                           const double2 *mom, double2 *gt, cudaStream_t stream, cdf *gt_df = nullptr,
-                          unsigned *gmax = nullptr, const unsigned *hwords = nullptr);
+                          unsigned *gmax = nullptr, const unsigned *hwords = nullptr, bool fit_rows_only = false);
 
 // The fermionic transform that also writes G(tau) as double-float pairs into
 // gt_df (left untouched in the FP64 arithmetic mode), for the fused bubble's
@@ -947,9 +960,9 @@ int launch_nu_to_tau_stat(double beta, int n_iw, int n_tau, bool fermion, long C
 // gmax (nullable, two words the caller zeroed): max |G| and max |Im G| of the
 // result as float bits, which decide whether the bubble can pair real columns.
 int launch_nu_to_tau_df(double beta, int n_iw, int n_tau, long C, const double2 *gw, const double2 *mom, double2 *gt,
-                        void *gt_df, cudaStream_t stream, unsigned *gmax, const unsigned *hwords) {
+                        void *gt_df, cudaStream_t stream, unsigned *gmax, const unsigned *hwords, bool fit_rows_only) {
   return launch_nu_to_tau_stat(beta, n_iw, n_tau, true, C, gw, mom, gt, stream, reinterpret_cast<cdf *>(gt_df), gmax,
-                               hwords);
+                               hwords, fit_rows_only);
 }
 
 __global__ void __launch_bounds__(256) hermitian_check_kernel(const double2 *__restrict__ gw, int n_iw, long C,
@@ -994,7 +1007,7 @@ int launch_nu_to_tau(double beta, int n_iw, int n_tau, long C, const double2 *gw
 // (fourier_matsubara.cpp:250-254).
 int launch_nu_to_tau_stat(double beta, int n_iw, int n_tau, bool fermion, long C, const double2 *gw,
                           const double2 *mom, double2 *gt, cudaStream_t stream, cdf *gt_df, unsigned *gmax,
-                          const unsigned *hwords) {
+                          const unsigned *hwords, bool fit_rows_only) {
   if (n_tau < 0) n_tau = default_n_tau(n_iw);
   if (!(beta > 0.0) || n_iw < 1 || n_tau < 2 || C < 1 || (!fermion && n_iw < 2))
     return set_error(TPRF_ERR_INVALID_ARGUMENT, "fourier_wr_to_tr: bad mesh");
@@ -1021,11 +1034,12 @@ int launch_nu_to_tau_stat(double beta, int n_iw, int n_tau, bool fermion, long C
       TPRF_CUDA(cudaFuncSetAttribute(nu_to_tau_kernel<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
       nu_to_tau_kernel<double2><<<(unsigned)blocks, kMatsubaraThreads, sm, stream>>>(*p, gw, mom, gt, C, icv,
                                                                                       log2_ic(icv), status, nullptr,
-                                                                                      gmax, nullptr);
+                                                                                      gmax, nullptr, 0);
     } else {
       TPRF_CUDA(cudaFuncSetAttribute(nu_to_tau_kernel<cdf>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
       nu_to_tau_kernel<cdf><<<(unsigned)blocks, kMatsubaraThreads, sm, stream>>>(*p, gw, mom, gt, C, icv, log2_ic(icv),
-                                                                                  status, gt_df, gmax, hwords);
+                                                                                  status, gt_df, gmax, hwords,
+                                                                                  fit_rows_only ? 1 : 0);
     }
     TPRF_LAUNCH_CHECK("nu_to_tau_kernel");
     return TPRF_OK;

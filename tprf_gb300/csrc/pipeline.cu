@@ -77,7 +77,7 @@ int bubble_to_wr(double beta, int n_iw, int n_tau, int nw, const int dims[3], in
   TPRF_CUDA(cudaMemsetAsync(gmax, 0, 4 * sizeof(unsigned), s));
   if ((st = launch_hermitian_check(n_iw, nk * nb2, g_wr, gmax + 2, s))) return st;
   st = launch_nu_to_tau_df(beta, n_iw, n_tau, nk * nb2, g_wr, reinterpret_cast<const double2 *>(moments), g_tr,
-                           g_tr_df, s, gmax, gmax + 2);
+                           g_tr_df, s, gmax, gmax + 2, nw > 1);
   if (st || (st = mark(2))) return st;
   // chi0(w, r) goes from the bubble to the r -> q transform as double-float
   // pairs (same bytes) on the double-float path: no conversion in between
