@@ -255,13 +255,28 @@ int tprf_solve_rpa_PH_wk(int nw, const int dims[3], int nb, const double *chi0, 
  * transform, the RPA and the copies to the host run in blocks of block_freqs
  * bosonic frequencies with `slots` device buffers (1..8), so that the copy of
  * one block overlaps the solve of the next. Same chi as the two calls.
- * Returns when chi is on the host. No reference counterpart as one call. */
+ * Stream-ordered: `stream` waits for the last copy, and with sync checks on
+ * (tprf_set_sync_checks) the call returns when chi is on the host. No
+ * reference counterpart as one call. */
 size_t tprf_imtime_bubble_rpa_to_host_workspace_bytes(int n_iw, int n_tau, int nw, const int dims[3], int nb,
                                                       int block_freqs, int slots);
 int tprf_imtime_bubble_rpa_to_host(double beta, int n_iw, int n_tau, int nw, const int dims[3], int nb,
                                    const double *g_wk, const double *moments, const double *U, double *chi0_wk,
                                    double *chi_host, int block_freqs, int slots, void *workspace,
                                    size_t workspace_bytes, void *stream);
+/* The same call without the final wait: the copies of chi keep running on the
+ * library's copy stream of the device after the compute on `stream` is done,
+ * so that the next call's chain overlaps them (a pipeline over many inputs;
+ * that call's solves wait for the device buffers they reuse). chi_host is
+ * complete after tprf_imtime_bubble_rpa_to_host_join(stream) once `stream`
+ * gets there, or after a device-wide synchronisation. Do not reuse chi_host or
+ * chi0_wk before then. */
+int tprf_imtime_bubble_rpa_to_host_async(double beta, int n_iw, int n_tau, int nw, const int dims[3], int nb,
+                                         const double *g_wk, const double *moments, const double *U,
+                                         double *chi0_wk, double *chi_host, int block_freqs, int slots,
+                                         void *workspace, size_t workspace_bytes, void *stream);
+/* `stream` waits for every copy the calls above have enqueued on this device. */
+int tprf_imtime_bubble_rpa_to_host_join(void *stream);
 
 /* solve_rpa_PH with chi written to HOST memory, as the reference's C++ function
  * returns it (rpa.cpp:29-68 returns a host gf). The points are solved in chunks

@@ -476,3 +476,40 @@ def test_fused_chain_and_rpa_to_host_equals_the_two_calls(cuda_lib, case, block_
         fused = imtime_bubble_rpa_wk(g_wk, U, 5, block_freqs=block_freqs, slots=slots)
         torch.cuda.synchronize()
         assert torch.equal(fused.data, two.data.cpu())
+
+
+@pytest.mark.parametrize("case", [0, 3, len(CASES) - 1])
+def test_pipelined_fused_calls_equal_the_waiting_call(cuda_lib, case):
+    """imtime_bubble_rpa_wk(wait=False) back to back on several inputs sharing
+    one workspace (the copies of a call running behind the next call's chain,
+    whose solves wait for the ring slots they reuse), then join_host_copies:
+    every output equals the waiting call's chi."""
+    T = tp()
+    from tprf_gb300 import _native
+    from tprf_gb300.lattice_utils import imtime_bubble_rpa_wk, join_host_copies
+    hopf, dims, beta, n_max = CASES[case]
+    ek, g_wk, _, _ = _g_wr(hopf(), dims, beta, n_max)
+    nb = ek.shape[-1]
+    rng = np.random.default_rng(40 + case)
+    Us = [0.3 * rng.standard_normal((nb,) * 4) + 0j for _ in range(3)]
+    nw, block, slots = 5, 1, 2
+    lib = _native.lib()
+    need = lib.tprf_imtime_bubble_rpa_to_host_workspace_bytes(n_max, -1, nw, _native.dims3(dims), nb, block, slots)
+    ws = torch.empty(int(need), dtype=torch.uint8, device="cuda")
+    chi0 = torch.empty((2 * nw - 1, int(np.prod(dims))) + (nb,) * 4, dtype=torch.complex128, device="cuda")
+    expect = [imtime_bubble_rpa_wk(g_wk, U, nw, block_freqs=block, slots=slots).data.clone() for U in Us]
+    outs = [torch.empty_like(e).pin_memory() for e in expect]
+    lib.tprf_set_sync_checks(0)
+    try:
+        for U, out in zip(Us, outs):
+            imtime_bubble_rpa_wk(g_wk, U, nw, out=out, block_freqs=block, slots=slots, chi0=chi0, workspace=ws,
+                                 wait=False)
+        join_host_copies()
+        torch.cuda.synchronize()
+        _native.check(lib.tprf_check_device_status(None), "pipelined calls")
+    finally:
+        lib.tprf_set_sync_checks(1)
+    for e, out in zip(expect, outs):
+        assert torch.equal(out, e)
+    with pytest.raises(ValueError):
+        imtime_bubble_rpa_wk(g_wk, Us[0], nw, wait=False)

@@ -51,11 +51,16 @@ __global__ void __launch_bounds__(256) mirror_rows_kernel(double2 *x, int nw, in
   }
 }
 
-// One copy stream and its events per device, created on first use.
+// One copy stream and its events per device, created on first use. copied[i]
+// marks the last copy out of ring slot i (of this call or an earlier one: a
+// call that does not wait for its copies leaves them running while the next
+// call computes, and that call's solves wait for the slot they reuse).
 struct CopyCtx {
   bool ready = false;
   cudaStream_t copy = nullptr;
   cudaEvent_t computed[kMaxSlots], copied[kMaxSlots], done;
+  bool pending[kMaxSlots] = {};
+  std::mutex mu;  // one call at a time enqueues on this device's copy stream
 };
 std::mutex g_copy_mu;
 std::map<int, CopyCtx> g_copy;
@@ -93,10 +98,12 @@ extern "C" size_t tprf_imtime_bubble_rpa_to_host_workspace_bytes(int n_iw, int n
   return tprf_imtime_bubble_workspace_bytes(n_iw, n_tau, dims, nb) + (size_t)slots * slot_bytes(block_freqs, row) + 256;
 }
 
-extern "C" int tprf_imtime_bubble_rpa_to_host(double beta, int n_iw, int n_tau, int nw, const int dims[3], int nb,
-                                              const double *g_wk, const double *moments, const double *U,
-                                              double *chi0_wk, double *chi_host, int block_freqs, int slots,
-                                              void *workspace, size_t workspace_bytes, void *stream) {
+namespace {
+// join: `stream` waits for the last copy (chi is on the host once the stream
+// gets there); otherwise the copies run on past the call, behind its compute.
+int bubble_rpa_to_host(double beta, int n_iw, int n_tau, int nw, const int dims[3], int nb, const double *g_wk,
+                       const double *moments, const double *U, double *chi0_wk, double *chi_host, int block_freqs,
+                       int slots, void *workspace, size_t workspace_bytes, void *stream, bool join) {
   if (!dims || !g_wk || !U || !chi0_wk || !chi_host || !workspace || nb < 1 || nb > 8 || nw < 1 || n_iw < 1 ||
       block_freqs < 1 || slots < 1 || slots > kMaxSlots)
     return set_error(TPRF_ERR_INVALID_ARGUMENT, "imtime_bubble_rpa_to_host: bad shape, slots or null pointer");
@@ -129,6 +136,7 @@ extern "C" int tprf_imtime_bubble_rpa_to_host(double beta, int n_iw, int n_tau, 
   const size_t sb = slot_bytes(block_freqs, row);
   CopyCtx *c = nullptr;
   if ((st = copy_ctx(&c))) return st;
+  std::lock_guard<std::mutex> lock(c->mu);
   TPRF_CUDA(cudaEventRecord(c->done, s));  // the copy stream starts after the chain
   TPRF_CUDA(cudaStreamWaitEvent(c->copy, c->done, 0));
   const int n_w = 2 * nw - 1;
@@ -137,7 +145,7 @@ extern "C" int tprf_imtime_bubble_rpa_to_host(double beta, int n_iw, int n_tau, 
     const int slot = k % slots;
     double2 *pos = reinterpret_cast<double2 *>(ring0 + (size_t)slot * sb);
     double2 *neg = pos + (long)block_freqs * row;
-    if (k >= slots) TPRF_CUDA(cudaStreamWaitEvent(s, c->copied[slot], 0));
+    if (c->pending[slot]) TPRF_CUDA(cudaStreamWaitEvent(s, c->copied[slot], 0));
     if (real) {
       const int m0 = k * block_freqs, m1 = std::min(nw, m0 + block_freqs), m_lo = std::max(m0, 1);
       double2 *rows = chi0 + (long)(nw - 1 + m0) * row;
@@ -169,8 +177,36 @@ extern "C" int tprf_imtime_bubble_rpa_to_host(double beta, int n_iw, int n_tau, 
                                 cudaMemcpyDeviceToHost, c->copy));
     }
     TPRF_CUDA(cudaEventRecord(c->copied[slot], c->copy));
+    c->pending[slot] = true;
   }
   TPRF_CUDA(cudaEventRecord(c->done, c->copy));
-  TPRF_CUDA(cudaStreamWaitEvent(s, c->done, 0));
+  if (join) TPRF_CUDA(cudaStreamWaitEvent(s, c->done, 0));
   return finish_with_checks(s, "imtime_bubble_rpa_to_host");
+}
+}  // namespace
+
+extern "C" int tprf_imtime_bubble_rpa_to_host(double beta, int n_iw, int n_tau, int nw, const int dims[3], int nb,
+                                              const double *g_wk, const double *moments, const double *U,
+                                              double *chi0_wk, double *chi_host, int block_freqs, int slots,
+                                              void *workspace, size_t workspace_bytes, void *stream) {
+  return bubble_rpa_to_host(beta, n_iw, n_tau, nw, dims, nb, g_wk, moments, U, chi0_wk, chi_host, block_freqs, slots,
+                            workspace, workspace_bytes, stream, true);
+}
+
+extern "C" int tprf_imtime_bubble_rpa_to_host_async(double beta, int n_iw, int n_tau, int nw, const int dims[3],
+                                                    int nb, const double *g_wk, const double *moments,
+                                                    const double *U, double *chi0_wk, double *chi_host,
+                                                    int block_freqs, int slots, void *workspace,
+                                                    size_t workspace_bytes, void *stream) {
+  return bubble_rpa_to_host(beta, n_iw, n_tau, nw, dims, nb, g_wk, moments, U, chi0_wk, chi_host, block_freqs, slots,
+                            workspace, workspace_bytes, stream, false);
+}
+
+extern "C" int tprf_imtime_bubble_rpa_to_host_join(void *stream) {
+  CopyCtx *c = nullptr;
+  if (int st = copy_ctx(&c)) return st;
+  std::lock_guard<std::mutex> lock(c->mu);
+  TPRF_CUDA(cudaEventRecord(c->done, c->copy));
+  TPRF_CUDA(cudaStreamWaitEvent(static_cast<cudaStream_t>(stream), c->done, 0));
+  return TPRF_OK;
 }

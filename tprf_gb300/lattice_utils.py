@@ -57,14 +57,23 @@ def imtime_bubble_chi0_wk(g_wk, nw=1, save_memory=False, verbose=True, nt=-1, mo
 
 
 def imtime_bubble_rpa_wk(g_wk, U, nw, out=None, nt=-1, moments=None, block_freqs=None, slots=3, chi0=None,
-                         workspace=None):
+                         workspace=None, wait=True):
     """chi(iw, q) = solve_rpa_PH(imtime_bubble_chi0_wk(g_wk, nw), U) with chi written
     to host memory (``out``: a pinned complex128 host tensor of chi's shape,
     allocated if None), the two reference calls in one: the r -> q transform,
     the RPA and the copies to the host run in blocks of ``block_freqs`` bosonic
     frequencies, the copy of one block overlapping the solve of the next.
     ``chi0`` (device tensor of chi's shape) and ``workspace`` (uint8 device
-    tensor) may be given to avoid allocations. Returns a host Gf."""
+    tensor) may be given to avoid allocations. Returns a host Gf.
+
+    ``wait=False`` returns without waiting for the copies: they run on behind
+    the compute, so that the next call's chain overlaps them (a pipeline over
+    many inputs). ``out`` is then complete after :func:`join_host_copies` and a
+    synchronisation of the current stream (or of the device); ``out`` and
+    ``chi0`` must not be reused before, and ``workspace`` (whose ring buffers
+    the copies read) must be given and held by the caller."""
+    if not wait and workspace is None:
+        raise ValueError("imtime_bubble_rpa_wk: wait=False needs a workspace held by the caller")
     wmesh, kmesh = _components(g_wk, (MeshImFreq, MeshBrZone), "imtime_bubble_rpa_wk")
     nb = g_wk.target_shape[0]
     nw = int(nw)
@@ -91,9 +100,16 @@ def imtime_bubble_rpa_wk(g_wk, U, nw, out=None, nt=-1, moments=None, block_freqs
         raise ValueError(f"imtime_bubble_rpa_wk: U must have shape {(nb,) * 4}")
     mom = as_device_c128(moments, dev) if moments is not None else None
     src = g_wk.data.contiguous()
-    check(lib.tprf_imtime_bubble_rpa_to_host(
+    fn = lib.tprf_imtime_bubble_rpa_to_host if wait else lib.tprf_imtime_bubble_rpa_to_host_async
+    check(fn(
         wmesh.beta, wmesh.n_max, n_tau, nw, dims3(kmesh.dims), nb, src.data_ptr(),
         mom.data_ptr() if mom is not None else None, Ud.data_ptr(), chi0.data_ptr(), out.data_ptr(), int(block_freqs),
         int(slots), workspace.data_ptr(), workspace.numel(), _stream()), "imtime_bubble_rpa_wk")
     return Gf(mesh=MeshProduct(MeshImFreq(wmesh.beta, "Boson", nw), kmesh), data=out, device=torch.device("cpu"))
+
+
+def join_host_copies():
+    """Make the current stream wait for every copy to host memory that
+    ``imtime_bubble_rpa_wk(..., wait=False)`` has started on this device."""
+    check(_native.lib().tprf_imtime_bubble_rpa_to_host_join(_stream()), "join_host_copies")
 
