@@ -384,10 +384,14 @@ def run_gpu(args):
         # one call at a time: each returns when its chi is on the host
         lib.tprf_set_sync_checks(1)
         serial_s = e2e_run(max(1, min(args.steps, 2)), True)
+        # the bytes that crossed to the host: the frequencies w >= 0 when the host fills
+        # chi(-w, q) = conj(chi(w, -q)) (real bubble, real U), else all of chi
+        d2h = int(lib.tprf_imtime_bubble_rpa_to_host_last_d2h_bytes())
         e2e = {"value": world * points / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(ek_host.numel() * C16),
-               "d2h_bytes_per_step": int(out_host.numel() * C16),
+               "d2h_bytes_per_step": d2h, "result_bytes_per_step": int(out_host.numel() * C16),
                "path": "lattice_dyson_g0_wk -> imtime_bubble_rpa_wk(wait=False) (chain + RPA, chi to pinned host "
-                       "memory, the copies of a step overlapping the next step's chain)",
+                       "memory, the copies of a step overlapping the next step's chain; host threads fill "
+                       "chi(-w, q) = conj(chi(w, -q)) when only w >= 0 crossed)",
                "steps": e2e_steps, "ms_per_step": e2e_s * 1e3,
                "serial": {"value": world * points / serial_s, "ms_per_step": serial_s * 1e3,
                           "path": "imtime_bubble_rpa_wk(wait=True): each call returns with chi on the host"}}

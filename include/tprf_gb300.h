@@ -254,7 +254,9 @@ int tprf_solve_rpa_PH_wk(int nw, const int dims[3], int nb, const double *chi0, 
  * ends holding chi0 for the frequencies the blocks transformed). The r -> q
  * transform, the RPA and the copies to the host run in blocks of block_freqs
  * bosonic frequencies with `slots` device buffers (1..8), so that the copy of
- * one block overlaps the solve of the next. Same chi as the two calls.
+ * one block overlaps the solve of the next. Same chi as the two calls. With a
+ * real bubble and a real U, chi(-w, q) = conj(chi(w, -q)) exactly, and only the
+ * frequencies w >= 0 cross to the host: host threads fill the others there.
  * Stream-ordered: `stream` waits for the last copy, and with sync checks on
  * (tprf_set_sync_checks) the call returns when chi is on the host. No
  * reference counterpart as one call. */
@@ -277,6 +279,8 @@ int tprf_imtime_bubble_rpa_to_host_async(double beta, int n_iw, int n_tau, int n
                                          void *workspace, size_t workspace_bytes, void *stream);
 /* `stream` waits for every copy the calls above have enqueued on this device. */
 int tprf_imtime_bubble_rpa_to_host_join(void *stream);
+/* Bytes the last of these calls on this device copied from the device to the host. */
+size_t tprf_imtime_bubble_rpa_to_host_last_d2h_bytes(void);
 
 /* solve_rpa_PH with chi written to HOST memory, as the reference's C++ function
  * returns it (rpa.cpp:29-68 returns a host gf). The points are solved in chunks

@@ -479,7 +479,7 @@ def test_fused_chain_and_rpa_to_host_equals_the_two_calls(cuda_lib, case, block_
 
 
 @pytest.mark.parametrize("case", [0, 3, len(CASES) - 1])
-def test_pipelined_fused_calls_equal_the_waiting_call(cuda_lib, case):
+def test_pipelined_fused_calls_equal_the_waiting_call(cuda_lib, arithmetic, case):
     """imtime_bubble_rpa_wk(wait=False) back to back on several inputs sharing
     one workspace (the copies of a call running behind the next call's chain,
     whose solves wait for the ring slots they reuse), then join_host_copies:
@@ -511,5 +511,9 @@ def test_pipelined_fused_calls_equal_the_waiting_call(cuda_lib, case):
         lib.tprf_set_sync_checks(1)
     for e, out in zip(expect, outs):
         assert torch.equal(out, e)
+    # real hoppings and a real U on the double-float path (which records that the
+    # bubble is real): only the frequencies w >= 0 crossed to the host
+    rows = nw if case != 3 and arithmetic != "fp64" else 2 * nw - 1
+    assert lib.tprf_imtime_bubble_rpa_to_host_last_d2h_bytes() == rows * int(np.prod(dims)) * nb ** 4 * 16
     with pytest.raises(ValueError):
         imtime_bubble_rpa_wk(g_wk, Us[0], nw, wait=False)

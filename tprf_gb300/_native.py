@@ -65,6 +65,7 @@ SIGNATURES = {
                                                      c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int, c_void_p,
                                                      c_size_t, c_void_p]),
     "tprf_imtime_bubble_rpa_to_host_join": (c_int, [c_void_p]),
+    "tprf_imtime_bubble_rpa_to_host_last_d2h_bytes": (c_size_t, []),
     "tprf_lindhard_chi00_workspace_bytes": (c_size_t, [c_long, c_int]),
     "tprf_lindhard_chi00": (c_int, [c_long, c_int3, c_int, c_void_p, c_double, c_double, c_int, c_void_p, c_void_p,
                                     c_size_t, c_void_p]),

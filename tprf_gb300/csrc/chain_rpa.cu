@@ -13,9 +13,13 @@
 // which writes both signs. Otherwise a block is a range of rows of the whole
 // mesh, transformed and solved point by point.
 #include <algorithm>
+#include <condition_variable>
 #include <cstring>
+#include <deque>
+#include <functional>
 #include <map>
 #include <mutex>
+#include <thread>
 #include <vector>
 
 #include "common.cuh"
@@ -51,6 +55,97 @@ __global__ void __launch_bounds__(256) mirror_rows_kernel(double2 *x, int nw, in
   }
 }
 
+// Host threads that fill the negative frequencies of chi in host memory from
+// the non-negative ones already copied there, chi(-w, q) = conj(chi(w, -q)),
+// when the device solve gives exactly that (a real bubble and a real U: the
+// conjugate-pair solve stores the conjugate of the same values): half the
+// bytes cross the device-to-host link, which bounds the call. Jobs are
+// submitted by host functions on the copy stream once a block's copy has
+// landed; a last host function waits for them, so that the copy stream (and a
+// stream joined to it) passes only when chi is complete. No CUDA calls here.
+class HostPool {
+ public:
+  static HostPool &get() {
+    static HostPool *p = new HostPool();  // never destroyed: its threads sleep until exit
+    return *p;
+  }
+  int threads() const { return (int)n_; }
+  void submit(std::function<void()> f) {
+    {
+      std::lock_guard<std::mutex> l(mu_);
+      q_.push_back(std::move(f));
+      ++outstanding_;
+    }
+    cv_.notify_one();
+  }
+  void wait_idle() {
+    std::unique_lock<std::mutex> l(mu_);
+    idle_.wait(l, [&] { return outstanding_ == 0; });
+  }
+
+ private:
+  HostPool() {
+    const unsigned hw = std::thread::hardware_concurrency();
+    n_ = std::max(1u, std::min(hw ? hw : 4u, 16u));
+    for (unsigned i = 0; i < n_; ++i) std::thread([this] { run(); }).detach();
+  }
+  void run() {
+    for (;;) {
+      std::function<void()> f;
+      {
+        std::unique_lock<std::mutex> l(mu_);
+        cv_.wait(l, [&] { return !q_.empty(); });
+        f = std::move(q_.front());
+        q_.pop_front();
+      }
+      f();
+      std::lock_guard<std::mutex> l(mu_);
+      if (--outstanding_ == 0) idle_.notify_all();
+    }
+  }
+  unsigned n_ = 1;
+  std::mutex mu_;
+  std::condition_variable cv_, idle_;
+  std::deque<std::function<void()>> q_;
+  long outstanding_ = 0;
+};
+
+// rows -m for m in [m_lo, m_hi) of host chi [2 nw - 1][N_k][n_target] from rows
+// m, split over the pool's threads
+struct HostMirror {
+  double2 *host;
+  int nw, m_lo, m_hi, d0, d1, d2;
+  long n_target;
+};
+
+void host_mirror_range(const HostMirror &j, long b0, long b1) {
+  const long nk = (long)j.d0 * j.d1 * j.d2;
+  for (long b = b0; b < b1; ++b) {
+    const int m = j.m_lo + (int)(b / nk);
+    const long k = b - (long)(m - j.m_lo) * nk;
+    const int k2 = (int)(k % j.d2), k1 = (int)((k / j.d2) % j.d1), k0 = (int)(k / ((long)j.d2 * j.d1));
+    const long mk = ((long)((j.d0 - k0) % j.d0) * j.d1 + (j.d1 - k1) % j.d1) * j.d2 + (j.d2 - k2) % j.d2;
+    const double2 *src = j.host + ((long)(j.nw - 1 + m) * nk + mk) * j.n_target;
+    double2 *dst = j.host + ((long)(j.nw - 1 - m) * nk + k) * j.n_target;
+    for (long e = 0; e < j.n_target; ++e) dst[e] = make_double2(src[e].x, -src[e].y);
+  }
+}
+
+void CUDART_CB submit_host_mirror(void *data) {
+  const HostMirror *j = static_cast<const HostMirror *>(data);
+  HostPool &pool = HostPool::get();
+  const long blocks = (long)(j->m_hi - j->m_lo) * j->d0 * j->d1 * j->d2;
+  const long parts = std::min<long>(blocks, pool.threads());
+  for (long i = 0; i < parts; ++i) {
+    const long b0 = blocks * i / parts, b1 = blocks * (i + 1) / parts;
+    const HostMirror copy = *j;
+    pool.submit([copy, b0, b1] { host_mirror_range(copy, b0, b1); });
+  }
+  delete j;
+}
+
+void CUDART_CB wait_host_mirrors(void *) { HostPool::get().wait_idle(); }
+
 // One copy stream and its events per device, created on first use. copied[i]
 // marks the last copy out of ring slot i (of this call or an earlier one: a
 // call that does not wait for its copies leaves them running while the next
@@ -60,7 +155,8 @@ struct CopyCtx {
   cudaStream_t copy = nullptr;
   cudaEvent_t computed[kMaxSlots], copied[kMaxSlots], done;
   bool pending[kMaxSlots] = {};
-  std::mutex mu;  // one call at a time enqueues on this device's copy stream
+  size_t last_d2h = 0;  // bytes the last call copied to the host
+  std::mutex mu;        // one call at a time enqueues on this device's copy stream
 };
 std::mutex g_copy_mu;
 std::map<int, CopyCtx> g_copy;
@@ -121,17 +217,23 @@ int bubble_rpa_to_host(double beta, int n_iw, int n_tau, int nw, const int dims[
   int st = bubble_to_wr(beta, n_iw, n_tau, nw, dims, nb, g_wk, moments, chi0, workspace, chain_bytes, nullptr, s,
                         &chi_df, &gmax);
   if (st) return st;
-  // the plan depends on whether the bubble was real: read its two words
-  bool real = false;
+  // the plan depends on whether the bubble was real: read its two words (and
+  // U: with U real as well the host fills the negative frequencies)
+  bool real = false, u_real = false;
   if (chi_df && nw >= 2) {
     unsigned w[2];
+    std::vector<double2> uh((size_t)nb * nb * nb * nb);
     TPRF_CUDA(cudaMemcpyAsync(w, gmax, sizeof(w), cudaMemcpyDeviceToHost, s));
+    TPRF_CUDA(cudaMemcpyAsync(uh.data(), Ud, uh.size() * sizeof(double2), cudaMemcpyDeviceToHost, s));
     TPRF_CUDA(cudaStreamSynchronize(s));
     float a, b;
     memcpy(&a, &w[0], 4);
     memcpy(&b, &w[1], 4);
     real = b <= kRealInputTol * a;
+    u_real = std::all_of(uh.begin(), uh.end(), [](const double2 &v) { return v.y == 0.0; });
   }
+  const bool host_mirror = real && u_real;
+  size_t d2h = 0;
   const uintptr_t ring0 = (reinterpret_cast<uintptr_t>(workspace) + chain_bytes + 255) & ~uintptr_t(255);
   const size_t sb = slot_bytes(block_freqs, row);
   CopyCtx *c = nullptr;
@@ -163,9 +265,16 @@ int bubble_rpa_to_host(double beta, int n_iw, int n_tau, int nw, const int dims[
       TPRF_CUDA(cudaStreamWaitEvent(c->copy, c->computed[slot], 0));
       TPRF_CUDA(cudaMemcpyAsync(host + (long)(nw - 1 + m0) * row, pos, (size_t)(m1 - m0) * row * sizeof(double2),
                                 cudaMemcpyDeviceToHost, c->copy));
-      if (m_lo < m1)
+      d2h += (size_t)(m1 - m0) * row * sizeof(double2);
+      if (m_lo < m1 && host_mirror) {
+        // the partners' rows -m read rows m at every q: all in this block
+        TPRF_CUDA(cudaLaunchHostFunc(
+            c->copy, submit_host_mirror, new HostMirror{host, nw, m_lo, m1, dims[0], dims[1], dims[2], nb4}));
+      } else if (m_lo < m1) {
         TPRF_CUDA(cudaMemcpyAsync(host + (long)(nw - m1) * row, neg, (size_t)(m1 - m_lo) * row * sizeof(double2),
                                   cudaMemcpyDeviceToHost, c->copy));
+        d2h += (size_t)(m1 - m_lo) * row * sizeof(double2);
+      }
     } else {
       const int r0 = k * block_freqs, r1 = std::min(n_w, r0 + block_freqs);
       double2 *rows = chi0 + (long)r0 * row;
@@ -175,10 +284,13 @@ int bubble_rpa_to_host(double beta, int n_iw, int n_tau, int nw, const int dims[
       TPRF_CUDA(cudaStreamWaitEvent(c->copy, c->computed[slot], 0));
       TPRF_CUDA(cudaMemcpyAsync(host + (long)r0 * row, pos, (size_t)(r1 - r0) * row * sizeof(double2),
                                 cudaMemcpyDeviceToHost, c->copy));
+      d2h += (size_t)(r1 - r0) * row * sizeof(double2);
     }
     TPRF_CUDA(cudaEventRecord(c->copied[slot], c->copy));
     c->pending[slot] = true;
   }
+  if (host_mirror) TPRF_CUDA(cudaLaunchHostFunc(c->copy, wait_host_mirrors, nullptr));
+  c->last_d2h = d2h;
   TPRF_CUDA(cudaEventRecord(c->done, c->copy));
   if (join) TPRF_CUDA(cudaStreamWaitEvent(s, c->done, 0));
   return finish_with_checks(s, "imtime_bubble_rpa_to_host");
@@ -200,6 +312,13 @@ extern "C" int tprf_imtime_bubble_rpa_to_host_async(double beta, int n_iw, int n
                                                     size_t workspace_bytes, void *stream) {
   return bubble_rpa_to_host(beta, n_iw, n_tau, nw, dims, nb, g_wk, moments, U, chi0_wk, chi_host, block_freqs, slots,
                             workspace, workspace_bytes, stream, false);
+}
+
+extern "C" size_t tprf_imtime_bubble_rpa_to_host_last_d2h_bytes(void) {
+  CopyCtx *c = nullptr;
+  if (copy_ctx(&c)) return 0;
+  std::lock_guard<std::mutex> lock(c->mu);
+  return c->last_d2h;
 }
 
 extern "C" int tprf_imtime_bubble_rpa_to_host_join(void *stream) {
