@@ -364,24 +364,28 @@ __global__ void __launch_bounds__(256) mirror_neg_freq_kernel(T *x, int nw, int 
                                                               const unsigned *gmax) {
   if (!gmax_says_real(gmax)) return;
   // one warp per (m, k) block of n_target contiguous elements: the index
-  // arithmetic once per block, the copy coalesced on both sides
-  const long nk = (long)d0 * d1 * d2, blocks = (long)(nw - 1) * nk;
+  // arithmetic once per block (32-bit: the launcher checks the block count),
+  // the copy coalesced on both sides, the conjugation a sign-bit flip (integer
+  // pipe: a negation would run on the scarce FP64 pipe)
+  const unsigned nk = (unsigned)d0 * d1 * d2, blocks = (unsigned)(nw - 1) * nk;
   const int lane = threadIdx.x & 31;
-  const long warps = (long)gridDim.x * (blockDim.x >> 5);
-  for (long wb = blockIdx.x * (long)(blockDim.x >> 5) + (threadIdx.x >> 5); wb < blocks; wb += warps) {
-    const int mi = (int)(wb / nk);  // m = mi - (nw - 1) < 0
-    const long k = wb - (long)mi * nk;
-    const int k2 = (int)(k % d2), k1 = (int)((k / d2) % d1), k0 = (int)(k / ((long)d2 * d1));
-    const long mk = ((long)((d0 - k0) % d0) * d1 + (d1 - k1) % d1) * d2 + (d2 - k2) % d2;
-    const T *src = x + ((long)(2 * (nw - 1) - mi) * nk + mk) * n_target;
-    T *dst = x + wb * n_target;
+  const unsigned warps = gridDim.x * (blockDim.x >> 5);
+  for (unsigned wb = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); wb < blocks; wb += warps) {
+    const unsigned mi = wb / nk;  // m = mi - (nw - 1) < 0
+    const unsigned k = wb - mi * nk;
+    const unsigned k2 = k % d2, k12 = k / d2, k1 = k12 % d1, k0 = k12 / d1;
+    const unsigned mk = ((k0 ? d0 - k0 : 0) * d1 + (k1 ? d1 - k1 : 0)) * d2 + (k2 ? d2 - k2 : 0);
+    const int4 *src = reinterpret_cast<const int4 *>(x + ((long)(2 * (nw - 1) - mi) * nk + mk) * n_target);
+    int4 *dst = reinterpret_cast<int4 *>(x + (long)wb * n_target);
     for (long e = lane; e < n_target; e += 32) {
-      T v = src[e];
+      int4 v = src[e];
+      // double2 {x, y}: the sign of y is bit 31 of .w; cdf {x.hi, x.lo, y.hi, y.lo}:
+      // the signs of y.hi and y.lo are bit 31 of .z and .w
       if constexpr (std::is_same<T, double2>::value) {
-        v.y = -v.y;
+        v.w ^= (int)0x80000000u;
       } else {
-        v.y.hi = -v.y.hi;
-        v.y.lo = -v.y.lo;
+        v.z ^= (int)0x80000000u;
+        v.w ^= (int)0x80000000u;
       }
       dst[e] = v;
     }
@@ -493,6 +497,7 @@ int launch_lattice_fft_fmt(bool forward, long n_w, const int dims[3], long n_tar
   auto mirror = [&]() -> int {
     if (n_skip == 0) return TPRF_OK;
     const long total = n_skip * (long)dims[0] * dims[1] * dims[2];  // (m, k) blocks, a warp each
+    if (total >= (1L << 31)) return set_error(TPRF_ERR_INVALID_ARGUMENT, "lattice FFT: too many (w, q) blocks");
     const unsigned blocks = (unsigned)std::min((total + 7) / 8, (long)num_sms() * 16);
     if (out_df)
       mirror_neg_freq_kernel<cdf><<<blocks, 256, 0, stream>>>(static_cast<cdf *>(out), (int)(n_skip + 1), dims[0],

@@ -970,12 +970,24 @@ __global__ void __launch_bounds__(256) hermitian_check_kernel(const double2 *__r
   // squared magnitudes: the difference in FP64 (it cancels), everything else in
   // FP32 (the FP64 pipe is the scarce one); the words hold the square roots
   float g_abs2 = 0.f, g_dev2 = 0.f;
-  const long total = (long)n_iw * C;  // rows i < n_iw against rows 2 n_iw - 1 - i
-  for (long idx = blockIdx.x * (long)blockDim.x + threadIdx.x; idx < total; idx += (long)gridDim.x * blockDim.x) {
-    const long i = idx / C, c = idx - i * C;
+  // rows i < n_iw against rows 2 n_iw - 1 - i; the (row, column) of the
+  // grid-stride index advance without a division per element
+  const long stride = (long)gridDim.x * blockDim.x;
+  const long start = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const long dstep = stride / C, cstep = stride - dstep * C;
+  long i = start / C, c = start - i * C;
+  for (; i < n_iw; i += dstep, c += cstep) {
+    if (c >= C) {
+      c -= C;
+      ++i;
+      if (i >= n_iw) break;
+    }
     const double2 a = gw[i * C + c], b = gw[(2L * n_iw - 1 - i) * C + c];
-    const float ax = (float)a.x, ay = (float)a.y, bx = (float)b.x, by = (float)b.y;
-    const float dx = (float)(a.x - b.x), dy = (float)(a.y + b.y);
+    // FP32 values by truncating bit operations (a conversion instruction would
+    // run on the FP64 pipe): the tolerance test needs magnitudes to a few digits
+    const float ax = split_double(a.x).hi, ay = split_double(a.y).hi, bx = split_double(b.x).hi,
+                by = split_double(b.y).hi;
+    const float dx = split_double(a.x - b.x).hi, dy = split_double(a.y + b.y).hi;
     g_abs2 = fmaxf(g_abs2, fmaxf(fmaf(ax, ax, ay * ay), fmaf(bx, bx, by * by)));
     g_dev2 = fmaxf(g_dev2, fmaf(dx, dx, dy * dy));
   }
