@@ -285,9 +285,9 @@ def run_gpu(args):
     stream = torch.cuda.current_stream()
     sh = stream.cuda_stream
     lib.tprf_set_sync_checks(0)
-    # Dyson, k->r passes, Hermitian test, iv->tau, bubble + tau->iw, r->q passes, the
-    # negative-frequency mirror (a no-op launch on complex input), RPA
-    launches_per_step = 1 + lattice_passes(dims) + 1 + 1 + 1 + lattice_passes(dims) + 1 + 1
+    # Dyson, k->r passes, Hermitian test, iv->tau, bubble + tau->iw, r->q passes (the
+    # last one also stores the negative frequencies of a real bubble), RPA
+    launches_per_step = 1 + lattice_passes(dims) + 1 + 1 + 1 + lattice_passes(dims) + 1
 
     ws_bytes = lib.tprf_imtime_bubble_workspace_bytes(n_max, n_tau, d3, nb)
     ws = torch.empty(ws_bytes, dtype=torch.uint8, device=dev)

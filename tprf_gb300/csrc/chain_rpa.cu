@@ -34,30 +34,6 @@ namespace {
 
 constexpr int kMaxSlots = 8;
 
-// rows -m for m in [m_lo, m_hi) of x [2 nw - 1][N_k][n_target] from rows m:
-// x(-m, q) = conj(x(m, -q)), complex128; one warp per (m, q) block, 32-bit
-// block indices (the caller checks the count), the conjugation a sign-bit flip
-// on the integer pipe
-__global__ void __launch_bounds__(256) mirror_rows_kernel(double2 *x, int nw, int m_lo, int m_hi, int d0, int d1,
-                                                          int d2, long n_target) {
-  const unsigned nk = (unsigned)d0 * d1 * d2, blocks = (unsigned)(m_hi - m_lo) * nk;
-  const int lane = threadIdx.x & 31;
-  const unsigned warps = gridDim.x * (blockDim.x >> 5);
-  for (unsigned wb = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); wb < blocks; wb += warps) {
-    const unsigned mo = wb / nk, k = wb - mo * nk;
-    const int m = m_lo + (int)mo;
-    const unsigned k2 = k % d2, k12 = k / d2, k1 = k12 % d1, k0 = k12 / d1;
-    const unsigned mk = ((k0 ? d0 - k0 : 0) * d1 + (k1 ? d1 - k1 : 0)) * d2 + (k2 ? d2 - k2 : 0);
-    const int4 *src = reinterpret_cast<const int4 *>(x + ((long)(nw - 1 + m) * nk + mk) * n_target);
-    int4 *dst = reinterpret_cast<int4 *>(x + ((long)(nw - 1 - m) * nk + k) * n_target);
-    for (long e = lane; e < n_target; e += 32) {
-      int4 v = src[e];
-      v.w ^= (int)0x80000000u;  // the sign of the imaginary part
-      dst[e] = v;
-    }
-  }
-}
-
 // Host threads that fill the negative frequencies of chi in host memory from
 // the non-negative ones already copied there, chi(-w, q) = conj(chi(w, -q)),
 // when the device solve gives exactly that (a real bubble and a real U: the
@@ -254,15 +230,11 @@ int bubble_rpa_to_host(double beta, int n_iw, int n_tau, int nw, const int dims[
     if (real) {
       const int m0 = k * block_freqs, m1 = std::min(nw, m0 + block_freqs), m_lo = std::max(m0, 1);
       double2 *rows = chi0 + (long)(nw - 1 + m0) * row;
-      if ((st = launch_lattice_fft_fmt(false, m1 - m0, dims, nb4, rows, chi_df, rows, false, 1.0, s))) return st;
-      if (m_lo < m1) {
-        const long total = (long)(m1 - m_lo) * nk;  // (m, q) blocks, a warp each
-        if (total >= (1L << 31))
-          return set_error(TPRF_ERR_INVALID_ARGUMENT, "imtime_bubble_rpa_to_host: too many (w, q) blocks per block");
-        const unsigned blocks = (unsigned)std::min((total + 7) / 8, (long)num_sms() * 16);
-        mirror_rows_kernel<<<blocks, 256, 0, s>>>(chi0, nw, m_lo, m1, dims[0], dims[1], dims[2], nb4);
-        TPRF_LAUNCH_CHECK("mirror_rows_kernel");
-      }
+      // the r -> q pass also stores chi0(-m, -q) = conj(chi0(m, q)) for m in
+      // [max(m0, 1), m1): row j of the block (m = m0 + j) at row -2 m0 - j from `rows`
+      if ((st = launch_lattice_fft_fmt(false, m1 - m0, dims, nb4, rows, chi_df, rows, false, 1.0, s, nullptr, true,
+                                       -2L * m0)))
+        return st;
       // frequency m at pos row m - m0; frequency -m (m >= m_lo) at neg row m1 - 1 - m
       const PairOut out{pos, neg + (long)(m1 - 1 - m0) * row, row, -row, m0, m1};
       if ((st = launch_rpa_wk_block(nw, dims, nb, chi0, Ud, out, s))) return st;

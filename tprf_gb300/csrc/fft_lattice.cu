@@ -32,12 +32,34 @@ constexpr int kLoadBatch = 4;  // tile loads per thread issued together
 
 // Leading part of a pass to leave out when the bubble's input was real
 // (gmax, see gmax_says_real): the negative bosonic frequencies, which the
-// mirror kernel fills afterwards. `columns` counts the pass's own units (the
-// axis pass: flattened columns; the plane pass: outer indices); 0 = none.
+// last pass stores from their partner rows (RowMirror). `columns` counts the
+// pass's own units (the axis pass: flattened columns; the plane pass: outer
+// indices); 0 = none.
 struct SkipRows {
   const unsigned *gmax;
   long columns;
 };
+
+// The negative frequencies written by the last pass of a lattice transform.
+// On a real bubble the rows satisfy x(-w, q) = conj(x(w, -q)) exactly, so the
+// pass that finishes row j (counted from the pass's base pointer; its partner
+// is row c - j) also stores the conjugate at the partner row and the negated k
+// point. Rows with c - j > j belong to their partner and are not stored; the
+// row with c - j == j (w = 0) has none. The conjugate is the stored value with
+// the sign bits of its imaginary words flipped, so the pair is exact bit for
+// bit. e1, e2: the mesh dims after the transformed axis (1 where absent); the
+// dims before it are trivial, as the last pass transforms the slowest
+// non-trivial axis.
+struct RowMirror {
+  const unsigned *gmax;  // words of the real-input test (gmax_says_real); null: unconditional
+  long c;
+  int e1, e2;
+  int on;
+  __device__ __forceinline__ bool active() const { return on && (gmax == nullptr || gmax_says_real(gmax)); }
+};
+constexpr RowMirror kNoRowMirror{nullptr, 0, 1, 1, 0};
+constexpr long kNoPartner = -0x7fffffffffffffffL - 1;  // a column without a partner store
+
 
 template <class E> __device__ __forceinline__ E load_el(double2 z);
 template <> __device__ __forceinline__ double2 load_el<double2>(double2 z) { return z; }
@@ -82,23 +104,66 @@ __device__ __forceinline__ void store_out(void *p, long i, E z, double s, dfl sd
   }
 }
 
+// The 16 bytes a pass stores for element z, and the same with the imaginary
+// part's sign bits flipped: complex128 {x, y} has the sign of y in bit 31 of
+// .w; double-float {x.hi, x.lo, y.hi, y.lo} has those of y.hi and y.lo in .z
+// and .w (a negation would run on the FP64 pipe).
+union Bits16 {
+  int4 i;
+  double2 d;
+  cdf f;
+};
+template <class E, bool DF>
+__device__ __forceinline__ int4 stored_bits(E z, double s, dfl sd, bool scaled) {
+  Bits16 b;
+  if constexpr (DF)
+    b.f = scaled ? cscale(z, sd) : cnorm(z);
+  else
+    b.d = store_el(z, s, sd, scaled);
+  return b.i;
+}
+template <bool DF>
+__device__ __forceinline__ int4 conj_bits(int4 v) {
+  if constexpr (DF) v.z ^= (int)0x80000000u;
+  v.w ^= (int)0x80000000u;
+  return v;
+}
+
 template <bool FWD, class E, bool IN_DF, bool OUT_DF>
 __global__ void __launch_bounds__(256) lattice_axis_kernel(const void *in, void *out, long ncols_total,
                                                            long inner, int ncol, int lgcol, FftDesc d, double scale,
-                                                           SkipRows skip) {
+                                                           SkipRows skip, RowMirror mir) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int n = d.n;
   E *a = reinterpret_cast<E *>(smem_raw);
   E *b = d.has_generic ? a + (size_t)n * ncol : nullptr;
   long *base = reinterpret_cast<long *>(smem_raw + (size_t)(d.has_generic ? 2 : 1) * n * ncol * sizeof(E));
+  long *pbase = base + ncol;  // partner stores (the launcher sizes shared memory for them when mir.on)
   // The tile is ncol consecutive columns of the flattened (outer, inner) index;
   // element (row, column f) sits at (f / inner) * n * inner + row * inner + f % inner.
   const long f0 = blockIdx.x * (long)ncol;
-  if (f0 + ncol <= skip.columns && gmax_says_real(skip.gmax)) return;  // rows the mirror fills
+  if (f0 + ncol <= skip.columns && gmax_says_real(skip.gmax)) return;  // rows the partner rows fill
+  const bool mirror = mir.active();
   for (int c = threadIdx.x; c < ncol; c += blockDim.x) {
     const long f = f0 + c;
     const long o = f / inner;
-    base[c] = (f < ncols_total) ? o * n * inner + (f - o * inner) : -1;
+    long bs = (f < ncols_total) ? o * n * inner + (f - o * inner) : -1;
+    if (mirror) {
+      // outer index o is the row (the dims before the axis are trivial); the
+      // partner element of (row i, inner (k1, k2, t)) is (c - o, -i, -k1, -k2, t)
+      long pb = kNoPartner;
+      const long prow = mir.c - o;
+      if (bs >= 0 && prow > o) bs = -1;  // stored by the partner row's tile
+      if (bs >= 0 && prow < o) {
+        const long n_target = inner / ((long)mir.e1 * mir.e2);
+        const long rem = f - o * inner, kk = rem / n_target, t = rem - kk * n_target;
+        const long k1 = kk / mir.e2, k2 = kk - k1 * mir.e2;
+        const long mk = (k1 ? mir.e1 - k1 : 0) * (long)mir.e2 + (k2 ? mir.e2 - k2 : 0);
+        pb = prow * n * inner + mk * n_target + t;
+      }
+      pbase[c] = pb;
+    }
+    base[c] = bs;
   }
   __syncthreads();
   const int tile = n * ncol;
@@ -123,6 +188,19 @@ __global__ void __launch_bounds__(256) lattice_axis_kernel(const void *in, void 
   E *r = fft_smem<FWD>(a, b, d, ncol);
   const bool scaled = scale != 1.0;
   const dfl sd = split_double(scale);
+  if (mirror) {
+    int4 *o4 = reinterpret_cast<int4 *>(out);
+    for (int w = threadIdx.x; w < tile; w += blockDim.x) {
+      const int c = w & (ncol - 1), row = w >> lgcol;
+      const long bs = base[c];
+      if (bs < 0) continue;
+      const int4 v = stored_bits<E, OUT_DF>(r[row * ncol + c], scale, sd, scaled);
+      o4[bs + (long)row * inner] = v;
+      const long pb = pbase[c];
+      if (pb != kNoPartner) o4[pb + (long)(row ? n - row : 0) * inner] = conj_bits<OUT_DF>(v);
+    }
+    return;
+  }
   for (int w = threadIdx.x; w < tile; w += blockDim.x) {
     const int c = w & (ncol - 1), row = w >> lgcol;
     const long bs = base[c];
@@ -132,19 +210,21 @@ __global__ void __launch_bounds__(256) lattice_axis_kernel(const void *in, void 
 
 template <bool FWD, class E, bool IN_DF, bool OUT_DF>
 int launch_axis_as(const void *in, void *out, long outer, int n, long inner, double scale, cudaStream_t stream,
-                   SkipRows skip = SkipRows{nullptr, 0}) {
+                   SkipRows skip = SkipRows{nullptr, 0}, RowMirror mir = kNoRowMirror) {
   FftDesc d;
   int st = get_fft(n, &d);
   if (st) return st;
   // Tile of up to 64 columns (a power of two dividing the 256 threads), limited
-  // by shared memory: one buffer of n x ncol elements (two with a generic radix).
+  // by shared memory: one buffer of n x ncol elements (two with a generic radix)
+  // and the column offsets (twice with partner stores).
   const int bufs = d.has_generic ? 2 : 1;
+  const size_t offs = (mir.on ? 2 : 1) * sizeof(long);
   const size_t budget = (size_t)std::min(max_smem_optin(), 200 * 1024);
   int ncol = 64;
-  while (ncol > 1 && (size_t)bufs * n * ncol * sizeof(E) + ncol * sizeof(long) > budget) ncol /= 2;
+  while (ncol > 1 && (size_t)bufs * n * ncol * sizeof(E) + ncol * offs > budget) ncol /= 2;
   const long ncols_total = outer * inner;
   while (ncol > 8 && ncol / 2 >= ncols_total) ncol /= 2;
-  const size_t smem = (size_t)bufs * n * ncol * sizeof(E) + ncol * sizeof(long);
+  const size_t smem = (size_t)bufs * n * ncol * sizeof(E) + ncol * offs;
   if (smem > budget) return set_error(TPRF_ERR_UNSUPPORTED_SIZE, "lattice FFT: mesh dimension too long for one CTA");
   int lg = 0;
   while ((1 << lg) < ncol) ++lg;
@@ -152,7 +232,7 @@ int launch_axis_as(const void *in, void *out, long outer, int n, long inner, dou
   if (blocks > 0x7fffffffL) return set_error(TPRF_ERR_INVALID_ARGUMENT, "lattice FFT: too many tiles");
   auto kern = lattice_axis_kernel<FWD, E, IN_DF, OUT_DF>;
   TPRF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  kern<<<(unsigned)blocks, 256, smem, stream>>>(in, out, ncols_total, inner, ncol, lg, d, scale, skip);
+  kern<<<(unsigned)blocks, 256, smem, stream>>>(in, out, ncols_total, inner, ncol, lg, d, scale, skip, mir);
   TPRF_LAUNCH_CHECK("lattice_axis_kernel");
   return TPRF_OK;
 }
@@ -161,15 +241,15 @@ int launch_axis_as(const void *in, void *out, long outer, int n, long inner, dou
 // input and output; double-float only with double-float arithmetic.
 template <bool FWD>
 int launch_axis(const void *in, bool in_df, void *out, bool out_df, long outer, int n, long inner, double scale,
-                cudaStream_t stream, SkipRows skip = SkipRows{nullptr, 0}) {
+                cudaStream_t stream, SkipRows skip = SkipRows{nullptr, 0}, RowMirror mir = kNoRowMirror) {
   if (arith_mode() == kArithFP64) {
     if (in_df || out_df) return set_error(TPRF_ERR_INVALID_ARGUMENT, "lattice FFT: double-float storage in FP64 mode");
-    return launch_axis_as<FWD, double2, false, false>(in, out, outer, n, inner, scale, stream, skip);
+    return launch_axis_as<FWD, double2, false, false>(in, out, outer, n, inner, scale, stream, skip, mir);
   }
-  if (in_df && out_df) return launch_axis_as<FWD, cdf, true, true>(in, out, outer, n, inner, scale, stream, skip);
-  if (in_df) return launch_axis_as<FWD, cdf, true, false>(in, out, outer, n, inner, scale, stream, skip);
-  if (out_df) return launch_axis_as<FWD, cdf, false, true>(in, out, outer, n, inner, scale, stream, skip);
-  return launch_axis_as<FWD, cdf, false, false>(in, out, outer, n, inner, scale, stream, skip);
+  if (in_df && out_df) return launch_axis_as<FWD, cdf, true, true>(in, out, outer, n, inner, scale, stream, skip, mir);
+  if (in_df) return launch_axis_as<FWD, cdf, true, false>(in, out, outer, n, inner, scale, stream, skip, mir);
+  if (out_df) return launch_axis_as<FWD, cdf, false, true>(in, out, outer, n, inner, scale, stream, skip, mir);
+  return launch_axis_as<FWD, cdf, false, false>(in, out, outer, n, inner, scale, stream, skip, mir);
 }
 
 // Two adjacent mesh axes in one pass: the array is [outer, n1, n2, n_target]
@@ -182,13 +262,17 @@ int launch_axis(const void *in, bool in_df, void *out, bool out_df, long outer, 
 template <bool FWD, class E, bool IN_DF, bool OUT_DF>
 __global__ void __launch_bounds__(256) lattice_plane_kernel(const void *in, void *out, long outer, long n_target,
                                                             int nt, int lgt, FftDesc d1, FftDesc d2, int lg2,
-                                                            double scale, SkipRows skip) {
+                                                            double scale, SkipRows skip, RowMirror mir) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   E *a = reinterpret_cast<E *>(smem_raw);
   const int n1 = d1.n, n2 = d2.n, P = n1 * n2;
   const long tiles_t = (n_target + nt - 1) / nt;
   const long o = blockIdx.x / tiles_t;
-  if (o < skip.columns && gmax_says_real(skip.gmax)) return;  // rows the mirror fills
+  if (o < skip.columns && gmax_says_real(skip.gmax)) return;  // rows the partner rows fill
+  // partner stores: o is the row (the dims before the plane are trivial)
+  const bool mirror = mir.active();
+  const long prow = mir.c - o;
+  if (mirror && prow > o) return;  // stored by the partner row's tiles
   const long t0 = (blockIdx.x - o * tiles_t) * (long)nt;
   const int ntv = (int)min((long)nt, n_target - t0);
   const long gbase = o * P * n_target + t0;
@@ -215,6 +299,23 @@ __global__ void __launch_bounds__(256) lattice_plane_kernel(const void *in, void
   E *r = fft_smem<FWD>(a, (E *)nullptr, d1, n2 * nt);
   const bool scaled = scale != 1.0;
   const dfl sd = split_double(scale);
+  if (mirror) {
+    // element (i1, i2, t) of row o, and its conjugate at (prow, -i1, -i2, t) for w != 0
+    int4 *o4 = reinterpret_cast<int4 *>(out);
+    const long pbase = prow * P * n_target + t0;
+    for (int w = threadIdx.x; w < P * nt; w += blockDim.x) {
+      const int t = w & (nt - 1), p = w >> lgt;
+      if (t >= ntv) continue;
+      const int4 v = stored_bits<E, OUT_DF>(r[p * nt + t], scale, sd, scaled);
+      o4[gbase + (long)p * n_target + t] = v;
+      if (prow < o) {
+        const int i1 = p >> lg2, i2 = p & (n2 - 1);
+        const int pm = (((n1 - i1) & (n1 - 1)) << lg2) | ((n2 - i2) & (n2 - 1));
+        o4[pbase + (long)pm * n_target + t] = conj_bits<OUT_DF>(v);
+      }
+    }
+    return;
+  }
   for (int w = threadIdx.x; w < P * nt; w += blockDim.x) {
     const int t = w & (nt - 1), p = w >> lgt;
     if (t < ntv) store_out<E, OUT_DF>(out, gbase + (long)p * n_target + t, r[p * nt + t], scale, sd, scaled);
@@ -322,7 +423,7 @@ int plane_targets(int n1, int n2, long n_target) {
 
 template <bool FWD, class E, bool IN_DF, bool OUT_DF>
 int launch_plane_as(const void *in, void *out, long outer, int n1, int n2, long n_target, double scale,
-                    cudaStream_t stream, SkipRows skip) {
+                    cudaStream_t stream, SkipRows skip, RowMirror mir) {
   FftDesc d1, d2;
   int st = get_fft(n1, &d1);
   if (st) return st;
@@ -335,61 +436,24 @@ int launch_plane_as(const void *in, void *out, long outer, int n1, int n2, long 
   auto kern = lattice_plane_kernel<FWD, E, IN_DF, OUT_DF>;
   TPRF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   kern<<<(unsigned)tiles, 256, smem, stream>>>(in, out, outer, n_target, nt, log2i(nt), d1, d2, log2i(n2), scale,
-                                               skip);
+                                               skip, mir);
   TPRF_LAUNCH_CHECK("lattice_plane_kernel");
   return TPRF_OK;
 }
 
 template <bool FWD>
 int launch_plane(const void *in, bool in_df, void *out, bool out_df, long outer, int n1, int n2, long n_target,
-                 double scale, cudaStream_t stream, SkipRows skip = SkipRows{nullptr, 0}) {
+                 double scale, cudaStream_t stream, SkipRows skip = SkipRows{nullptr, 0},
+                 RowMirror mir = kNoRowMirror) {
   if (arith_mode() == kArithFP64) {
     if (in_df || out_df) return set_error(TPRF_ERR_INVALID_ARGUMENT, "lattice FFT: double-float storage in FP64 mode");
-    return launch_plane_as<FWD, double2, false, false>(in, out, outer, n1, n2, n_target, scale, stream, skip);
+    return launch_plane_as<FWD, double2, false, false>(in, out, outer, n1, n2, n_target, scale, stream, skip, mir);
   }
-  if (in_df && out_df) return launch_plane_as<FWD, cdf, true, true>(in, out, outer, n1, n2, n_target, scale, stream, skip);
-  if (in_df) return launch_plane_as<FWD, cdf, true, false>(in, out, outer, n1, n2, n_target, scale, stream, skip);
-  if (out_df) return launch_plane_as<FWD, cdf, false, true>(in, out, outer, n1, n2, n_target, scale, stream, skip);
-  return launch_plane_as<FWD, cdf, false, false>(in, out, outer, n1, n2, n_target, scale, stream, skip);
-}
-
-// Negative frequencies by symmetry: when the bubble's input was real
-// (gmax_says_real), its rows satisfy x(-w, r) = conj(x(w, r)) exactly, so after a
-// lattice transform of the non-negative rows x(-w, q) = conj(x(w, -q)), with
-// -q = (N_a - q_a) mod N_a on every axis. Rows are [n_w = 2 nw - 1][N_k][n_target],
-// row w - (nw - 1) = m; elements stored as complex128 or double-float pairs
-// (the conjugate negates the imaginary words in both).
-template <class T>
-__global__ void __launch_bounds__(256) mirror_neg_freq_kernel(T *x, int nw, int d0, int d1, int d2, long n_target,
-                                                              const unsigned *gmax) {
-  if (!gmax_says_real(gmax)) return;
-  // one warp per (m, k) block of n_target contiguous elements: the index
-  // arithmetic once per block (32-bit: the launcher checks the block count),
-  // the copy coalesced on both sides, the conjugation a sign-bit flip (integer
-  // pipe: a negation would run on the scarce FP64 pipe)
-  const unsigned nk = (unsigned)d0 * d1 * d2, blocks = (unsigned)(nw - 1) * nk;
-  const int lane = threadIdx.x & 31;
-  const unsigned warps = gridDim.x * (blockDim.x >> 5);
-  for (unsigned wb = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); wb < blocks; wb += warps) {
-    const unsigned mi = wb / nk;  // m = mi - (nw - 1) < 0
-    const unsigned k = wb - mi * nk;
-    const unsigned k2 = k % d2, k12 = k / d2, k1 = k12 % d1, k0 = k12 / d1;
-    const unsigned mk = ((k0 ? d0 - k0 : 0) * d1 + (k1 ? d1 - k1 : 0)) * d2 + (k2 ? d2 - k2 : 0);
-    const int4 *src = reinterpret_cast<const int4 *>(x + ((long)(2 * (nw - 1) - mi) * nk + mk) * n_target);
-    int4 *dst = reinterpret_cast<int4 *>(x + (long)wb * n_target);
-    for (long e = lane; e < n_target; e += 32) {
-      int4 v = src[e];
-      // double2 {x, y}: the sign of y is bit 31 of .w; cdf {x.hi, x.lo, y.hi, y.lo}:
-      // the signs of y.hi and y.lo are bit 31 of .z and .w
-      if constexpr (std::is_same<T, double2>::value) {
-        v.w ^= (int)0x80000000u;
-      } else {
-        v.z ^= (int)0x80000000u;
-        v.w ^= (int)0x80000000u;
-      }
-      dst[e] = v;
-    }
-  }
+  if (in_df && out_df)
+    return launch_plane_as<FWD, cdf, true, true>(in, out, outer, n1, n2, n_target, scale, stream, skip, mir);
+  if (in_df) return launch_plane_as<FWD, cdf, true, false>(in, out, outer, n1, n2, n_target, scale, stream, skip, mir);
+  if (out_df) return launch_plane_as<FWD, cdf, false, true>(in, out, outer, n1, n2, n_target, scale, stream, skip, mir);
+  return launch_plane_as<FWD, cdf, false, false>(in, out, outer, n1, n2, n_target, scale, stream, skip, mir);
 }
 
 // The TMA-staged plane pass with nt targets per tile (two tiles per CTA).
@@ -489,31 +553,31 @@ int launch_lattice_fft_scaled(bool forward, long n_w, const int dims[3], long n_
 // double-float arithmetic) as double-float pairs; the passes in between hand
 // each other double-float pairs whenever the arithmetic is double-float.
 int launch_lattice_fft_fmt(bool forward, long n_w, const int dims[3], long n_target, const void *in, bool in_df,
-                           void *out, bool out_df, double scale_last, cudaStream_t stream, const unsigned *gmax) {
+                           void *out, bool out_df, double scale_last, cudaStream_t stream, const unsigned *gmax,
+                           bool fill_partners, long partner_c) {
   const bool mid_df = arith_mode() != kArithFP64;
   // with gmax: the n_w = 2 nw - 1 bosonic rows of a real bubble; the first nw - 1
-  // (negative frequencies) are left out of the passes and mirrored at the end
+  // (negative frequencies) are left out of the passes, and the last pass stores
+  // them from their partners, row j of the others giving row 2 (nw - 1) - j
   const long n_skip = (gmax && n_w >= 3 && (n_w & 1)) ? (n_w - 1) / 2 : 0;
-  auto mirror = [&]() -> int {
-    if (n_skip == 0) return TPRF_OK;
-    const long total = n_skip * (long)dims[0] * dims[1] * dims[2];  // (m, k) blocks, a warp each
-    if (total >= (1L << 31)) return set_error(TPRF_ERR_INVALID_ARGUMENT, "lattice FFT: too many (w, q) blocks");
-    const unsigned blocks = (unsigned)std::min((total + 7) / 8, (long)num_sms() * 16);
-    if (out_df)
-      mirror_neg_freq_kernel<cdf><<<blocks, 256, 0, stream>>>(static_cast<cdf *>(out), (int)(n_skip + 1), dims[0],
-                                                              dims[1], dims[2], n_target, gmax);
-    else
-      mirror_neg_freq_kernel<double2><<<blocks, 256, 0, stream>>>(static_cast<double2 *>(out), (int)(n_skip + 1),
-                                                                  dims[0], dims[1], dims[2], n_target, gmax);
-    TPRF_LAUNCH_CHECK("mirror_neg_freq_kernel");
-    return TPRF_OK;
-  };
+  if (n_skip > 0) {
+    fill_partners = true;
+    partner_c = 2 * n_skip;
+  } else {
+    gmax = nullptr;  // partner stores as the caller asks, unconditionally
+  }
   int nontriv[3], nn = 0;
   for (int ax = 0; ax < 3; ++ax)
     if (dims[ax] > 1) nontriv[nn++] = ax;
+  // the partner stores of the last pass, which transforms axis nontriv[0]
+  auto mirror_for = [&](int ax) {
+    if (!fill_partners) return kNoRowMirror;
+    return RowMirror{gmax, partner_c, ax == 0 ? dims[1] : 1, ax <= 1 ? dims[2] : 1, 1};
+  };
   if (nn == 0) {  // a single k point: the transform is the identity (times the factor)
     if (in_df || out_df)
       return set_error(TPRF_ERR_INVALID_ARGUMENT, "lattice FFT: double-float storage needs a mesh with N_k > 1");
+    if (fill_partners) return set_error(TPRF_ERR_INVALID_ARGUMENT, "lattice FFT: partner rows need a mesh with N_k > 1");
     const long n = n_w * n_target;
     const double2 *src = static_cast<const double2 *>(in);
     double2 *dst = static_cast<double2 *>(out);
@@ -536,17 +600,18 @@ int launch_lattice_fft_fmt(bool forward, long n_w, const int dims[3], long n_tar
       const double scale = (nn == 2) ? scale_last : 1.0;
       const bool plane_out_df = (nn == 3) ? mid_df : out_df;
       const SkipRows pskip{gmax, n_skip * (outer / n_w)};
+      const RowMirror pmir = (nn == 2) ? mirror_for(A) : kNoRowMirror;
       int st = kNotApplicable;
-      if (n_skip == 0)  // the TMA form has no row skip
+      if (n_skip == 0 && !pmir.on)  // the TMA form has no row skip and no partner stores
         st = forward ? launch_plane_tma<true>(in, in_df, out, plane_out_df, outer, dims[A], dims[B], n_target, scale,
                                               stream)
                      : launch_plane_tma<false>(in, in_df, out, plane_out_df, outer, dims[A], dims[B], n_target, scale,
                                                stream);
       if (st == kNotApplicable)
         st = forward ? launch_plane<true>(in, in_df, out, plane_out_df, outer, dims[A], dims[B], n_target, scale,
-                                          stream, pskip)
+                                          stream, pskip, pmir)
                      : launch_plane<false>(in, in_df, out, plane_out_df, outer, dims[A], dims[B], n_target, scale,
-                                           stream, pskip);
+                                           stream, pskip, pmir);
       if (st) return st;
       if (nn == 3) {
         const int ax = nontriv[0];
@@ -554,11 +619,14 @@ int launch_lattice_fft_fmt(bool forward, long n_w, const int dims[3], long n_tar
         for (int a2 = 0; a2 < ax; ++a2) outer0 *= dims[a2];
         for (int a2 = ax + 1; a2 < 3; ++a2) inner0 *= dims[a2];
         const SkipRows askip{gmax, n_skip * (outer0 / n_w) * inner0};
-        st = forward ? launch_axis<true>(out, mid_df, out, out_df, outer0, dims[ax], inner0, scale_last, stream, askip)
-                     : launch_axis<false>(out, mid_df, out, out_df, outer0, dims[ax], inner0, scale_last, stream, askip);
+        const RowMirror amir = mirror_for(ax);
+        st = forward ? launch_axis<true>(out, mid_df, out, out_df, outer0, dims[ax], inner0, scale_last, stream, askip,
+                                         amir)
+                     : launch_axis<false>(out, mid_df, out, out_df, outer0, dims[ax], inner0, scale_last, stream,
+                                          askip, amir);
         if (st) return st;
       }
-      return mirror();
+      return TPRF_OK;
     }
   }
   // fastest-varying mesh dimension first: its pass has the longest contiguous rows;
@@ -574,13 +642,14 @@ int launch_lattice_fft_fmt(bool forward, long n_w, const int dims[3], long n_tar
     const double scale = last_pass ? scale_last : 1.0;
     const bool dst_df = last_pass ? out_df : mid_df;
     const SkipRows askip{gmax, n_skip * (outer / n_w) * inner};
-    int st = forward ? launch_axis<true>(src, src_df, out, dst_df, outer, n, inner, scale, stream, askip)
-                     : launch_axis<false>(src, src_df, out, dst_df, outer, n, inner, scale, stream, askip);
+    const RowMirror amir = last_pass ? mirror_for(ax) : kNoRowMirror;
+    int st = forward ? launch_axis<true>(src, src_df, out, dst_df, outer, n, inner, scale, stream, askip, amir)
+                     : launch_axis<false>(src, src_df, out, dst_df, outer, n, inner, scale, stream, askip, amir);
     if (st) return st;
     src = out;
     src_df = dst_df;
   }
-  return mirror();
+  return TPRF_OK;
 }
 
 int encode_tensor_map_f64(CUtensorMap *map, const void *base, int rank, const uint64_t *dims,
@@ -764,7 +833,8 @@ int noalloc_axis(const double2 *in, double2 *out, long outer, long inner, const 
   const long blocks = (ncols_total + ncol - 1) / ncol;
   auto kern = lattice_axis_kernel<FWD, E, false, false>;
   TPRF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  kern<<<(unsigned)blocks, 256, smem, stream>>>(in, out, ncols_total, inner, ncol, lg, d, scale, SkipRows{nullptr, 0});
+  kern<<<(unsigned)blocks, 256, smem, stream>>>(in, out, ncols_total, inner, ncol, lg, d, scale, SkipRows{nullptr, 0},
+                                                kNoRowMirror);
   TPRF_LAUNCH_CHECK("lattice_axis_kernel (no-alloc)");
   return TPRF_OK;
 }

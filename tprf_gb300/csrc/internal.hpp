@@ -148,9 +148,17 @@ int launch_lattice_fft_scaled(bool forward, long n_w, const int dims[3], long n_
 // gmax (nullable): the rows are the 2 nw - 1 bosonic frequencies of a real
 // bubble (launch_chi0_wr_from_grt_df with the same words); when the words say
 // real, the negative frequencies are skipped and filled by symmetry,
-// x(-w, q) = conj(x(w, -q)). With in != out the skipped input rows are not read.
+// x(-w, q) = conj(x(w, -q)), by the last pass, which stores each value of a
+// non-negative frequency a second time, conjugated, at its partner (the sign
+// bits of the imaginary words flipped: exact). With in != out the skipped
+// input rows are not read. fill_partners (without gmax): the same partner
+// stores unconditionally, row j of the call (counted from `out`) going to
+// row partner_c - j; rows with partner_c - j > j are then not stored, and the
+// row with partner_c - j == j has no partner (a frequency block m0 .. m1 - 1
+// of the non-negative rows, out at row nw - 1 + m0: partner_c = -2 m0).
 int launch_lattice_fft_fmt(bool forward, long n_w, const int dims[3], long n_target, const void *in, bool in_df,
-                           void *out, bool out_df, double scale, cudaStream_t stream, const unsigned *gmax = nullptr);
+                           void *out, bool out_df, double scale, cudaStream_t stream, const unsigned *gmax = nullptr,
+                           bool fill_partners = false, long partner_c = 0);
 // The fused bubble + tau -> iw, writing chi0(iw, r) as double-float pairs when
 // want_df and the double-float path runs (*wrote_df tells which). skip_neg:
 // on a real bubble (gmax words), the negative frequencies are left unwritten
