@@ -36,6 +36,7 @@ namespace tprf {
 namespace {
 
 constexpr int kMatsubaraThreads = 256;  // columns per CTA (<= 32) divide it
+constexpr int kMidBatch = 8;             // tau -> w: row loads per thread in flight
 
 struct VinvRows {
   double r0[8];  // row 0 of the inverse Vandermonde: first derivative
@@ -469,9 +470,39 @@ __global__ void __launch_bounds__(kMatsubaraThreads, 2) tau_to_w_kernel(TauWPlan
   ld.setup(col0, ic, ncol, soff);
   __syncthreads();
   // Rows t < L go to their digit-reversed FFT positions, row L aside. The loads
-  // of four iterations are issued before any is used (their latency overlaps),
-  // and the FP64 values of the 18 rows that fit_derivatives samples are kept.
-  const int total = (L + 1) * ic;
+  // of several iterations are issued before any is used (their latency
+  // overlaps), and the FP64 values of the 18 rows that fit_derivatives samples
+  // are kept. The bosonic transform loads its rows 9 .. L-9 through the
+  // element type (eight iterations in flight), then the 18 sampled rows in FP64.
+  if constexpr (!FERM) {
+    const int mid0 = 9 * ic, mid = (L - 17) * ic;
+    for (int w0 = tid; w0 < mid; w0 += kMidBatch * nthr) {
+      C e[kMidBatch];
+#pragma unroll
+      for (int u = 0; u < kMidBatch; ++u) {
+        const int w = mid0 + w0 + u * nthr;
+        const int c = w & (ic - 1), t = w >> lg;
+        e[u] = (w0 + u * nthr < mid && c < ncol) ? ld.template get<C>(t, c, col0, ic, soff) : czero<C>();
+      }
+#pragma unroll
+      for (int u = 0; u < kMidBatch; ++u) {
+        const int w = mid0 + w0 + u * nthr;
+        if (w0 + u * nthr < mid) a[rev[w >> lg] * ic + (w & (ic - 1))] = e[u];
+      }
+    }
+    // sampled row q: t = q for q <= 8, t = L - 17 + q (L - 8 .. L) for q >= 9
+    for (int w = tid; w < 18 * ic; w += nthr) {
+      const int c = w & (ic - 1), q = w >> lg;
+      const int t = q <= 8 ? q : L - 17 + q;
+      const double2 v = c < ncol ? ld.get64(t, c, col0, ic, soff) : make_double2(0.0, 0.0);
+      smp[q * ic + c] = v;
+      if (t < L)
+        a[rev[t] * ic + c] = from_d2<C>(v);
+      else
+        last[c] = from_d2<C>(v);
+    }
+  }
+  const int total = FERM ? (L + 1) * ic : 0;
   for (int w0 = tid; w0 < total; w0 += 4 * nthr) {
     double2 v[4];
     C e[4];
