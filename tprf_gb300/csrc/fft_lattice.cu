@@ -28,7 +28,7 @@
 namespace tprf {
 namespace {
 
-constexpr int kLoadBatch = 4;  // tile loads per thread issued together
+constexpr int kLoadBatch = 8;  // tile loads per thread issued together
 
 // Leading part of a pass to leave out when the bubble's input was real
 // (gmax, see gmax_says_real): the negative bosonic frequencies, which the

@@ -36,7 +36,7 @@ namespace tprf {
 namespace {
 
 constexpr int kMatsubaraThreads = 256;  // columns per CTA (<= 32) divide it
-constexpr int kMidBatch = 8;             // tau -> w: row loads per thread in flight
+constexpr int kMidBatch = 8;             // row loads per thread in flight (load phases)
 
 struct VinvRows {
   double r0[8];  // row 0 of the inverse Vandermonde: first derivative
@@ -164,17 +164,17 @@ __global__ void __launch_bounds__(kMatsubaraThreads, 2) nu_to_tau_kernel(NuTauPl
   if (tid == 0) s_res = 0u;
   __syncthreads();
   // frequency n sits at FFT row (n + L) % L, stored at its digit-reversed
-  // position; four loads per thread are in flight before the first is stored
-  for (int w0 = tid; w0 < nnu * ic; w0 += 4 * nthr) {
-    double2 v[4];
+  // position; kMidBatch loads per thread are in flight before the first is stored
+  for (int w0 = tid; w0 < nnu * ic; w0 += kMidBatch * nthr) {
+    double2 v[kMidBatch];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
+    for (int u = 0; u < kMidBatch; ++u) {
       const int w = w0 + u * nthr;
       const int c = w & (ic - 1), n = w >> lg;
       if (w < nnu * ic && c < ncol) v[u] = in_at(n, c);
     }
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
+    for (int u = 0; u < kMidBatch; ++u) {
       const int w = w0 + u * nthr;
       const int c = w & (ic - 1), n = w >> lg;
       if (w < nnu * ic && c < ncol) a[rev[(n + p.in0 + L) % L] * ic + c] = from_d2<C>(v[u]);
