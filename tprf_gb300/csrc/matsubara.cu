@@ -362,6 +362,18 @@ struct BubbleLoader {  // chi0 columns computed from G(tau, r): col = r * nb^4 +
   }
 };
 
+// Gathered reads of the double-float copy of G(tau, r) as single 8- and
+// 16-byte loads (dfl itself is only 4-byte aligned).
+__device__ __forceinline__ cdf ld_cdf(const cdf *p, long i) { return p[i]; }
+__device__ __forceinline__ dfl ld_dfl(const void *p, long i) {  // 8 bytes at element i of dfl[] p
+  const float2 v = reinterpret_cast<const float2 *>(p)[i];
+  return dfl{v.x, v.y};
+}
+__device__ __forceinline__ dfl ld_re(const cdf *p, long i) {  // the real part of element i of cdf[] p
+  const float2 v = reinterpret_cast<const float2 *>(p)[2 * i];
+  return dfl{v.x, v.y};
+}
+
 // The fused bubble with a double-float copy of G(tau, r) beside the complex128
 // one: the FFT input is the double-float product of the copies (FP32 pipe, no
 // conversion), and only the rows fit_derivatives samples take the FP64
@@ -372,7 +384,7 @@ struct BubbleLoaderDF : BubbleLoader {
   __device__ __forceinline__ E get(int t, int c, long col0, int ic, const long *s) const {
     if constexpr (IsDfElem<E>::value) {
       const long slice = Nr * nb * nb;
-      return cmul(gdf[(long)t * slice + s[c]], gdf[(long)(n_tau - 1 - t) * slice + s[ic + c]]);
+      return cmul(ld_cdf(gdf, (long)t * slice + s[c]), ld_cdf(gdf, (long)(n_tau - 1 - t) * slice + s[ic + c]));
     } else {
       return get64(t, c, col0, ic, s);
     }
@@ -422,11 +434,11 @@ struct BubblePairLoaderDF : BubbleLoaderDF {
     if (!pairs) return BubbleLoaderDF::template get<E>(t, c, col0, ic, s);
     if constexpr (IsDfElem<E>::value) {
       const long slice = Nr * nb * nb, t1 = (long)t * slice, t2 = (long)(n_tau - 1 - t) * slice;
-      if (compact) {
-        const dfl *gre = reinterpret_cast<const dfl *>(gdf);
-        return cdf{dmul(gre[t1 + s[c]], gre[t2 + s[ic + c]]), dmul(gre[t1 + s[2 * ic + c]], gre[t2 + s[3 * ic + c]])};
-      }
-      return cdf{dmul(gdf[t1 + s[c]].x, gdf[t2 + s[ic + c]].x), dmul(gdf[t1 + s[2 * ic + c]].x, gdf[t2 + s[3 * ic + c]].x)};
+      if (compact)
+        return cdf{dmul(ld_dfl(gdf, t1 + s[c]), ld_dfl(gdf, t2 + s[ic + c])),
+                   dmul(ld_dfl(gdf, t1 + s[2 * ic + c]), ld_dfl(gdf, t2 + s[3 * ic + c]))};
+      return cdf{dmul(ld_re(gdf, t1 + s[c]), ld_re(gdf, t2 + s[ic + c])),
+                 dmul(ld_re(gdf, t1 + s[2 * ic + c]), ld_re(gdf, t2 + s[3 * ic + c]))};
     } else {
       return get64(t, c, col0, ic, s);
     }

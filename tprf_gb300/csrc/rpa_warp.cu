@@ -151,16 +151,19 @@ __device__ __forceinline__ typename Mag<E>::type solve_augmented(E *M, int N_in,
   return pmin;
 }
 
+// b_ready: the caller has already written B = chi0 (from x) into M, with the
+// same lane of the group writing element o as the load loop here would.
 template <class E, int G, int NBC = 0>
 __device__ double rpa_point_warp(const double2 *__restrict__ x, double2 *__restrict__ y, E *M, int N_in, int nb_in,
                                  const SparseU &u, int lane, unsigned gmask, bool &singular,
-                                 double2 *__restrict__ y_conj = nullptr) {
+                                 double2 *__restrict__ y_conj = nullptr, bool b_ready = false) {
   const int nb = NBC > 0 ? NBC : nb_in;  // a compile-time size when NBC > 0
   const int N = NBC > 0 ? NBC * NBC : N_in;
   const int W = 2 * N;
 #define MM(i, c) M[(i) * W + (c)]
   // B = chi0 in the grouped layout (coalesced global reads)
-  for (int o = lane; o < N * N; o += G) MM(o / N, N + col_of_offset(o % N, nb)) = el_from(x[o], (E *)nullptr);
+  if (!b_ready)
+    for (int o = lane; o < N * N; o += G) MM(o / N, N + col_of_offset(o % N, nb)) = el_from(x[o], (E *)nullptr);
   __syncwarp(gmask);
   // A = I - X U from the non-zeros of U; the size of the terms bounds cancellation
   float amax = 0.f;
@@ -298,15 +301,20 @@ __global__ void __launch_bounds__(512) rpa_pair_kernel(int nw, int d0, int d1, i
     if (mh == 0 && q > mq) continue;  // its partner (0, -q) holds this unit
     const long p = (long)(nw - 1 + mh) * nk + q, pm = (long)(nw - 1 - mh) * nk + mq;
     const double2 *x = chi0 + p * N * N, *xm = chi0 + pm * N * N;
+    // one read of chi0(w, q): the symmetry test against the partner and B of
+    // the first solve (written to the group's matrix as rpa_point_warp would)
     bool sym = ureal;
-    if (pm != p) {
-      for (int o = lane; o < N * N; o += G) {
-        const double2 a = x[o], b = xm[o];
+    const bool partner = pm != p;
+    for (int o = lane; o < N * N; o += G) {
+      const double2 a = x[o];
+      M[(o / N) * 2 * N + N + col_of_offset(o % N, nb)] = el_from(a, (E *)nullptr);
+      if (partner) {
+        const double2 b = xm[o];
         sym = sym && __double_as_longlong(a.x) == __double_as_longlong(b.x) &&
               __double_as_longlong(a.y) == __double_as_longlong(-b.y);
       }
-      sym = __all_sync(gmask, sym);
     }
+    if (partner) sym = __all_sync(gmask, sym);
     double2 *y = out.pos + (long)(mh - out.mh0) * out.row + q * N * N;
     double2 *ym = (mh == 0 ? out.pos + (long)(mh - out.mh0) * out.row : out.neg + (long)(mh - out.mh0) * out.neg_step) +
                   mq * N * N;
@@ -316,7 +324,7 @@ __global__ void __launch_bounds__(512) rpa_pair_kernel(int nw, int d0, int d1, i
       double2 *ys = k ? ym : y;
       double2 *yc = (k == 0 && sym && pm != p) ? ym : nullptr;
       bool singular = false;
-      const double cond2 = rpa_point_warp<E, G, NBC>(xs, ys, M, N, nb, u, lane, gmask, singular, yc);
+      const double cond2 = rpa_point_warp<E, G, NBC>(xs, ys, M, N, nb, u, lane, gmask, singular, yc, k == 0);
       if (IsDf<E>::value && !(cond2 <= kDf64CondLimit2))
         rpa_point_warp<double2, G, NBC>(xs, ys, reinterpret_cast<double2 *>(M), N, nb, u, lane, gmask, singular, yc);
       if (singular && lane == 0) atomicOr(status, kDevErrSingular);
