@@ -36,7 +36,8 @@ namespace tprf {
 namespace {
 
 constexpr int kMatsubaraThreads = 256;  // columns per CTA (<= 32) divide it
-constexpr int kMidBatch = 8;             // row loads per thread in flight (load phases)
+constexpr int kMidBatch = 12;            // row loads per thread in flight (load phases)
+constexpr int kEpiBatch = 2;             // iv -> tau output rows whose tables are read together
 
 struct VinvRows {
   double r0[8];  // row 0 of the inverse Vandermonde: first derivative
@@ -244,40 +245,59 @@ __global__ void __launch_bounds__(kMatsubaraThreads, 2) nu_to_tau_kernel(NuTauPl
   if (tid == 0 && __uint_as_float(s_res) > 1e-3f) atomicOr(status, kDevErrTailFit);
   C *r = fft_smem<true>(a, b, p.fft, ic);
   float g_abs = 0.f, g_im = 0.f;
-  for (int w = tid; w < (L + 1) * ic; w += nthr) {
-    const int c = w & (ic - 1), t = w >> lg;
-    if (c >= ncol) continue;
-    const int tt = (t < L) ? t : 0;
-    C v = cmul(table<C>(p.P, p.Pf, tt), r[tt * ic + c]);
+  // the phase and tail tables (larger than what L1 keeps beside the FFT
+  // buffers) of kEpiBatch iterations are read before any is used
+  const int n_out = (L + 1) * ic;
+  for (int w0 = tid; w0 < n_out; w0 += kEpiBatch * nthr) {
+    C tp[kEpiBatch], tq[kEpiBatch][3];
 #pragma unroll
-    for (int j = 0; j < 3; ++j) v = cadd(v, cmul(am[j * ic + c], table<C>(p.Q, p.Qf, (long)j * L + tt)));
-    // G[L] = -(G[0] + m1) for fermions, +(G[0] + m1) for bosons
-    if (t == L) v = p.fermion ? csub(czero<C>(), cadd(v, am[3 * ic + c])) : cadd(v, am[3 * ic + c]);
-    if (pairs) {
-      if constexpr (IsDfElem<C>::value) {
-        // real results: the double-float copy keeps the real parts only (dfl,
-        // 8 bytes), the complex128 copy all rows or the fit rows only
-        const long f = 2 * (col0 + c);
-        const bool keep = !fit_rows_only || t <= 8 || t >= L - 8;
-        dfl *gre = reinterpret_cast<dfl *>(gt_df);
-        if (keep) gt[(long)t * Ccols + f] = as_d2(cdf{v.x, dfl{0.f, 0.f}});
-        if (gt_df) gre[(long)t * Ccols + f] = v.x;
-        if (f + 1 < Ccols) {
-          if (keep) gt[(long)t * Ccols + f + 1] = as_d2(cdf{v.y, dfl{0.f, 0.f}});
-          if (gt_df) gre[(long)t * Ccols + f + 1] = v.y;
-        }
-        if (gmax) g_abs = fmaxf(g_abs, fmaxf(fabsf(v.x.hi), fabsf(v.y.hi)));  // both parts are real columns
+    for (int u = 0; u < kEpiBatch; ++u) {
+      const int w = w0 + u * nthr, t = w >> lg;
+      const int tt = (t < L) ? t : 0;
+      if (w < n_out) {
+        tp[u] = table<C>(p.P, p.Pf, tt);
+#pragma unroll
+        for (int j = 0; j < 3; ++j) tq[u][j] = table<C>(p.Q, p.Qf, (long)j * L + tt);
       }
-      continue;
     }
-    gt[(long)t * Ccols + col0 + c] = as_d2(v);
-    if constexpr (IsDfElem<C>::value) {
-      if (gt_df) gt_df[(long)t * Ccols + col0 + c] = v;  // the value before rounding to complex128
-    }
-    if (gmax) {
-      const double2 h = hi_parts(v);
-      g_abs = fmaxf(g_abs, fmaxf(fabsf((float)h.x), fabsf((float)h.y)));
-      g_im = fmaxf(g_im, fabsf((float)h.y));
+#pragma unroll
+    for (int u = 0; u < kEpiBatch; ++u) {
+      const int w = w0 + u * nthr;
+      if (w >= n_out) break;
+      const int c = w & (ic - 1), t = w >> lg;
+      if (c >= ncol) continue;
+      const int tt = (t < L) ? t : 0;
+      C v = cmul(tp[u], r[tt * ic + c]);
+#pragma unroll
+      for (int j = 0; j < 3; ++j) v = cadd(v, cmul(am[j * ic + c], tq[u][j]));
+      // G[L] = -(G[0] + m1) for fermions, +(G[0] + m1) for bosons
+      if (t == L) v = p.fermion ? csub(czero<C>(), cadd(v, am[3 * ic + c])) : cadd(v, am[3 * ic + c]);
+      if (pairs) {
+        if constexpr (IsDfElem<C>::value) {
+          // real results: the double-float copy keeps the real parts only (dfl,
+          // 8 bytes), the complex128 copy all rows or the fit rows only
+          const long f = 2 * (col0 + c);
+          const bool keep = !fit_rows_only || t <= 8 || t >= L - 8;
+          dfl *gre = reinterpret_cast<dfl *>(gt_df);
+          if (keep) gt[(long)t * Ccols + f] = as_d2(cdf{v.x, dfl{0.f, 0.f}});
+          if (gt_df) gre[(long)t * Ccols + f] = v.x;
+          if (f + 1 < Ccols) {
+            if (keep) gt[(long)t * Ccols + f + 1] = as_d2(cdf{v.y, dfl{0.f, 0.f}});
+            if (gt_df) gre[(long)t * Ccols + f + 1] = v.y;
+          }
+          if (gmax) g_abs = fmaxf(g_abs, fmaxf(fabsf(v.x.hi), fabsf(v.y.hi)));  // both parts are real columns
+        }
+        continue;
+      }
+      gt[(long)t * Ccols + col0 + c] = as_d2(v);
+      if constexpr (IsDfElem<C>::value) {
+        if (gt_df) gt_df[(long)t * Ccols + col0 + c] = v;  // the value before rounding to complex128
+      }
+      if (gmax) {
+        const double2 h = hi_parts(v);
+        g_abs = fmaxf(g_abs, fmaxf(fabsf((float)h.x), fabsf((float)h.y)));
+        g_im = fmaxf(g_im, fabsf((float)h.y));
+      }
     }
   }
   // max |G| and max |Im G| of the whole transform, for the real-pair bubble
