@@ -745,8 +745,8 @@ def measure_fp64_peak(lib, dev) -> float:
 TRAFFIC = {
     # DRAM bytes of one launch from an ncu capture of the kernel on the 16x16x8 case,
     # scaled to 32^3 by the columns (points) processed
-    ("cfg1", "bubble_tau_to_w"): 16 * 1.487e9,
-    ("cfg1", "rpa"): 16 * 2.727e9,
+    ("cfg1", "bubble_tau_to_w"): 16 * 1.049e9,
+    ("cfg1", "rpa"): 16 * 2.685e9,
 }
 
 
