@@ -478,6 +478,58 @@ def test_fused_chain_and_rpa_to_host_equals_the_two_calls(cuda_lib, case, block_
         assert torch.equal(fused.data, two.data.cpu())
 
 
+# Layouts of the last r -> q pass, which stores a real bubble's negative
+# frequencies from their partners: the two-axis pass last (a trivial axis in
+# front or in the middle), one axis (the first or the last), and an axis
+# sequence ending on the middle axis (a length that is not a power of two).
+PARTNER_MESHES = [(1, 8, 8), (4, 1, 4), (1, 1, 8), (8, 1, 1), (1, 6, 6), (1, 6, 4)]
+
+
+def _real_nn_model(dims):
+    """Two bands, real nearest-neighbour hoppings along every non-trivial axis."""
+    t = np.array([[-1.0, 0.2], [0.2, -0.6]])
+    hop = {(0, 0, 0): np.diag([0.3, -0.2])}
+    for ax, d in enumerate(dims):
+        if d > 1:
+            R = [0, 0, 0]
+            R[ax] = 1
+            hop[tuple(R)] = t
+            hop[tuple(-x for x in R)] = t.T
+    return hop
+
+
+@pytest.mark.parametrize("dims", PARTNER_MESHES)
+def test_partner_stores_on_every_mesh_layout(cuda_lib, arithmetic, dims):
+    """On every layout of the last r -> q pass: chi0 matches the oracle, its
+    negative frequencies are exactly the partners' conjugates, chi0(-w, q) =
+    conj(chi0(w, -q)) (the native FP64 mode transforms every row and meets the
+    symmetry to the parity bar), and the fused call (partner stores per
+    frequency block) gives exactly the two calls' chi."""
+    T = tp()
+    from tprf_gb300.lattice_utils import imtime_bubble_rpa_wk
+    beta, n_max, nw = 8.0, 24, 5
+    ek, g_wk, _, _ = _g_wr(_real_nn_model(dims), dims, beta, n_max)
+    chi0 = T.imtime_bubble_chi0_wk(g_wk, nw=nw, verbose=False)
+    ref = O.imtime_bubble_chi0_wk(O.lattice_dyson_g0_wk(0.0, ek, beta, n_max), beta, dims, nw=nw)
+    assert rel_err(chi0.data, ref) < PARITY_RTOL
+    x = chi0.data.cpu().reshape((2 * nw - 1,) + tuple(dims) + (-1,))
+    partner = torch.conj(torch.flip(x, dims=[0]))  # row i <- row 2 (nw - 1) - i
+    for ax in (1, 2, 3):  # k -> (N - k) mod N along every mesh axis
+        partner = torch.roll(torch.flip(partner, dims=[ax]), shifts=1, dims=ax)
+    if arithmetic == "fp64":
+        assert rel_err(x[: nw - 1], partner[: nw - 1]) < PARITY_RTOL
+    else:
+        assert torch.equal(x[: nw - 1], partner[: nw - 1])
+    rng = np.random.default_rng(sum(dims))
+    U = 0.3 * rng.standard_normal((2,) * 4) + 0j
+    two = T.solve_rpa_PH(chi0, U)
+    assert rel_err(two.data, O.solve_rpa_PH(ref, U)) < PARITY_RTOL
+    for block_freqs in (1, 2):
+        fused = imtime_bubble_rpa_wk(g_wk, U, nw, block_freqs=block_freqs, slots=2)
+        torch.cuda.synchronize()
+        assert torch.equal(fused.data, two.data.cpu())
+
+
 @pytest.mark.parametrize("case", [0, 3, len(CASES) - 1])
 def test_pipelined_fused_calls_equal_the_waiting_call(cuda_lib, arithmetic, case):
     """imtime_bubble_rpa_wk(wait=False) back to back on several inputs sharing
