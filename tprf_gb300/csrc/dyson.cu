@@ -9,22 +9,26 @@
 // in place by Gauss-Jordan elimination with partial pivoting. Row swaps use
 // compile-time indices with predicated selects and the final column
 // permutation is folded into the store addresses, so the matrix stays in
-// registers (nb <= 5; larger nb spill but stay correct).
+// registers (nb <= 5; larger nb spill but stay correct). The elimination runs
+// in double-float on the FP32 pipe (about 48 significant bits; the matrix is
+// (iv + mu) I - e(k) - Sigma, whose inverse is well conditioned for the
+// Matsubara frequencies, |Im| >= pi / beta) and in FP64 in the FP64
+// arithmetic mode; the input is read and the output written as complex128.
 #include <algorithm>
 
-#include "common.cuh"
+#include "rpa_common.cuh"
 
 namespace tprf {
 namespace {
 
-template <int NB>
-__device__ __forceinline__ void swap_rows_if(double2 (&M)[NB][NB], int j, int p) {
+template <int NB, class E>
+__device__ __forceinline__ void swap_rows_if(E (&M)[NB][NB], int j, int p) {
 #pragma unroll
   for (int i = 0; i < NB; ++i) {
     if (i > j && i == p) {
 #pragma unroll
       for (int c = 0; c < NB; ++c) {
-        double2 t = M[i][c];
+        E t = M[i][c];
         M[i][c] = M[j][c];
         M[j][c] = t;
       }
@@ -37,17 +41,22 @@ __device__ __forceinline__ void swap_rows_if(double2 (&M)[NB][NB], int j, int p)
 // packed (destination column of column c in bits [4c, 4c+4)) and applied by
 // the caller when storing, so no register array is indexed at run time.
 // Returns false on an exactly zero pivot.
-template <int NB>
-__device__ __forceinline__ bool invert_in_place(double2 (&M)[NB][NB], unsigned &dest) {
+// Pivot magnitudes: |z|^2 in FP64, or from the high words of a double-float
+// element (the choice of pivot only needs the order of magnitudes).
+__device__ __forceinline__ double pivot_mag(double2 z) { return cabs2(z); }
+__device__ __forceinline__ float pivot_mag(cdf z) { return __fmaf_rn(z.x.hi, z.x.hi, z.y.hi * z.y.hi); }
+
+template <int NB, class E>
+__device__ __forceinline__ bool invert_in_place(E (&M)[NB][NB], unsigned &dest) {
   unsigned perm = 0u;  // pivot row of step j in bits [4j, 4j+4)
   bool ok = true;
 #pragma unroll
   for (int j = 0; j < NB; ++j) {
     int p = j;
-    double best = cabs2(M[j][j]);
+    auto best = pivot_mag(M[j][j]);
 #pragma unroll
     for (int i = j + 1; i < NB; ++i) {
-      const double v = cabs2(M[i][j]);
+      const auto v = pivot_mag(M[i][j]);
       if (v > best) {
         best = v;
         p = i;
@@ -55,18 +64,18 @@ __device__ __forceinline__ bool invert_in_place(double2 (&M)[NB][NB], unsigned &
     }
     perm |= (unsigned)p << (4 * j);
     swap_rows_if<NB>(M, j, p);
-    if (best == 0.0) ok = false;
-    const double2 inv = crecip(M[j][j]);
-    M[j][j] = make_double2(1.0, 0.0);
+    if (best == 0) ok = false;
+    const E inv = el_recip(M[j][j]);
+    M[j][j] = el_one((E *)nullptr);
 #pragma unroll
     for (int c = 0; c < NB; ++c) M[j][c] = cmul(M[j][c], inv);
 #pragma unroll
     for (int i = 0; i < NB; ++i) {
       if (i != j) {
-        const double2 f = M[i][j];
-        M[i][j] = make_double2(0.0, 0.0);
+        const E f = M[i][j];
+        M[i][j] = el_zero((E *)nullptr);
 #pragma unroll
-        for (int c = 0; c < NB; ++c) M[i][c] = cfms(f, M[j][c], M[i][c]);
+        for (int c = 0; c < NB; ++c) M[i][c] = el_fms(f, M[j][c], M[i][c]);
       }
     }
   }
@@ -88,7 +97,7 @@ __device__ __forceinline__ bool invert_in_place(double2 (&M)[NB][NB], unsigned &
   return ok;
 }
 
-template <int NB>
+template <int NB, class E>
 __global__ void __launch_bounds__(128) dyson_kernel(double beta, int n_iw, long n_k, double mu,
                                                     const double2 *__restrict__ e_k,
                                                     const double2 *__restrict__ sigma, int sigma_kind,
@@ -98,22 +107,21 @@ __global__ void __launch_bounds__(128) dyson_kernel(double beta, int n_iw, long 
     const int n = (int)(idx / n_k);
     const long k = idx - (long)n * n_k;
     const double nu = (2.0 * (n - n_iw) + 1.0) * M_PI / beta;
-    double2 M[NB][NB];
+    E M[NB][NB];
     const double2 *ek = e_k + k * NB * NB;
+    // the matrix in FP64 (the diagonal shift and Sigma), then one conversion
 #pragma unroll
     for (int i = 0; i < NB; ++i)
 #pragma unroll
       for (int j = 0; j < NB; ++j) {
         const double2 e = ek[i * NB + j];
-        M[i][j] = (i == j) ? make_double2(mu - e.x, nu - e.y) : make_double2(-e.x, -e.y);
+        double2 m = (i == j) ? make_double2(mu - e.x, nu - e.y) : make_double2(-e.x, -e.y);
+        if (sigma_kind != 0) {
+          const double2 *s = (sigma_kind == 1) ? sigma + (long)n * NB * NB : sigma + idx * NB * NB;
+          m = csub(m, s[i * NB + j]);
+        }
+        M[i][j] = el_from(m, (E *)nullptr);
       }
-    if (sigma_kind != 0) {
-      const double2 *s = (sigma_kind == 1) ? sigma + (long)n * NB * NB : sigma + idx * NB * NB;
-#pragma unroll
-      for (int i = 0; i < NB; ++i)
-#pragma unroll
-        for (int j = 0; j < NB; ++j) M[i][j] = csub(M[i][j], s[i * NB + j]);
-    }
     unsigned dest;
     if (!invert_in_place<NB>(M, dest)) atomicOr(status, kDevErrSingular);
     double2 *out = g + idx * NB * NB;
@@ -121,7 +129,7 @@ __global__ void __launch_bounds__(128) dyson_kernel(double beta, int n_iw, long 
     for (int j = 0; j < NB; ++j) {
       const int dj = (int)((dest >> (4 * j)) & 15u);
 #pragma unroll
-      for (int i = 0; i < NB; ++i) out[i * NB + dj] = M[i][j];
+      for (int i = 0; i < NB; ++i) out[i * NB + dj] = el_to(M[i][j]);
     }
   }
 }
@@ -133,11 +141,17 @@ int launch_dyson_nb(double beta, int n_iw, long n_k, double mu, const double2 *e
   // threads per CTA (at most the kernel's bound of 128): 128 unless the
   // autotuner measured another (the kernel is out of place, so a trial run
   // recomputes the same G)
+  const bool fp64 = arith_mode() == kArithFP64;
   auto launch = [&](int threads) -> int {
     long blocks = (total + threads - 1) / threads;
     const long cap = (long)num_sms() * 2048 / threads;
     if (blocks > cap) blocks = cap;
-    dyson_kernel<NB><<<(unsigned)blocks, threads, 0, stream>>>(beta, n_iw, n_k, mu, e_k, sigma, sigma_kind, g, status);
+    if (fp64)
+      dyson_kernel<NB, double2><<<(unsigned)blocks, threads, 0, stream>>>(beta, n_iw, n_k, mu, e_k, sigma, sigma_kind,
+                                                                          g, status);
+    else
+      dyson_kernel<NB, cdf><<<(unsigned)blocks, threads, 0, stream>>>(beta, n_iw, n_k, mu, e_k, sigma, sigma_kind, g,
+                                                                      status);
     TPRF_LAUNCH_CHECK("dyson_kernel");
     return TPRF_OK;
   };
