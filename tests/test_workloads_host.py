@@ -1,0 +1,79 @@
+"""Host checks of the synthetic workloads the benchmark runs (no GPU).
+
+The benchmark configs are seeded tight-binding models with the shapes of the
+reference's benchmark cases; these tests pin what they contain: Hermitian
+dispersions, the vertex shapes, the 5-orbital bandwidth, and the batched
+instances' ranges, frequency counts and determinism.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from tprf_gb300 import workloads as W
+
+
+def _is_smooth7(n):
+    for p in (2, 3, 5, 7):
+        while n % p == 0:
+            n //= p
+    return n == 1
+
+
+@pytest.mark.parametrize("key", ["cfg0", "cfg1", "cfg3", "cfg4"])
+def test_models_give_hermitian_dispersions(key):
+    c = W.config(key)
+    for R, t in c["hoppings"].items():
+        back = c["hoppings"][tuple(-x for x in R)]
+        assert np.array_equal(np.asarray(back), np.asarray(t).T)  # real t(R): t(-R) = t(R)^T
+    small = tuple(min(d, 6) for d in c["dims"])
+    ek = O.ek_from_hoppings(c["hoppings"], small)
+    assert np.abs(ek - np.conj(np.transpose(ek, (0, 2, 1)))).max() < 1e-14
+
+
+@pytest.mark.parametrize("key,nb", [("cfg0", 1), ("cfg1", 3), ("cfg3", 2), ("cfg4", 5)])
+def test_vertex_shapes(key, nb):
+    c = W.config(key)
+    U = np.asarray(c["U"])
+    assert U.shape == (nb,) * 4
+    assert np.all(U.imag == 0)
+    assert next(iter(c["hoppings"].values())).shape == (nb, nb)
+
+
+def test_layered_5orb_bandwidth_is_about_four():
+    """Each of the five bands is about 4 wide (nearest-neighbour -0.5 in the plane)."""
+    c = W.config("cfg4")
+    ek = O.ek_from_hoppings(c["hoppings"], (32, 32, 4))
+    ev = np.linalg.eigvalsh(ek)  # [N_k, 5], ascending per k
+    widths = ev.max(axis=0) - ev.min(axis=0)
+    assert np.all((widths > 3.0) & (widths < 5.0))
+
+
+def test_smooth7_near():
+    assert W.smooth7_near(12.8 * 5.0, 32, 512) == 64
+    assert W.smooth7_near(12.8 * 40.0, 32, 512) == 512
+    assert W.smooth7_near(1.0, 32, 512) == 32
+    for x in (100.3, 257.9, 333.0):
+        n = W.smooth7_near(x, 32, 512)
+        assert _is_smooth7(n)
+        assert all(abs(m - x) >= abs(n - x) for m in range(32, 513) if _is_smooth7(m))
+
+
+def test_batched_instances_follow_the_spec():
+    a = W.batched_instances(512, seed=0)
+    b = W.batched_instances(512, seed=0)
+    assert len(a) == 512
+    nbs = set()
+    for x, y in zip(a, b):
+        assert x["dims"] == y["dims"] and x["beta"] == y["beta"] and x["mu"] == y["mu"]
+        assert np.array_equal(x["U"], y["U"])
+        L0, L1, L2 = x["dims"]
+        assert L0 == L1 and L0 in (8, 16, 24, 32, 48) and L2 == 1
+        assert 5.0 <= x["beta"] <= 40.0 and -1.0 <= x["mu"] <= 1.0
+        assert x["nw"] == x["n_max"] and 32 <= x["n_max"] <= 512 and _is_smooth7(x["n_max"])
+        assert x["n_max"] == W.smooth7_near(12.8 * x["beta"], 32, 512)
+        assert np.asarray(x["U"]).shape == (x["nb"],) * 4
+        if x["nb"] == 1:
+            assert 0.5 <= float(np.asarray(x["U"]).real.ravel()[0]) <= 2.5
+        nbs.add(x["nb"])
+    assert nbs == {1, 2}
+    assert W.batched_instances(8, seed=1)[0]["beta"] != a[0]["beta"]
