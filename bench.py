@@ -32,7 +32,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
-METRIC = "RPA chi(q,iw) points/s (complex128, <=1e-10 rel err vs FP64 oracle)"
+METRIC = "RPA \u03c7(q,i\u03bd) points/s on 1 GB300 at \u22641e-10 rel err vs plain GPU path; % HBM peak"
 UNIT = "points/s"
 C16 = 16  # bytes per complex128
 
@@ -141,6 +141,99 @@ def barrier(world: int, device=None):
             dist.barrier(device_ids=[device.index])
         else:
             dist.barrier()
+
+
+# ---------------------------------------------------------------------------
+# host placement of the end-to-end leg (NUMA nodes of the pinned buffer, the GPU
+# and the library's host-fill threads), read from /proc and /sys
+
+def _cpulist(text):
+    out = []
+    for part in text.strip().split(","):
+        if "-" in part:
+            a, b = part.split("-")
+            out.extend(range(int(a), int(b) + 1))
+        elif part:
+            out.append(int(part))
+    return out
+
+
+def numa_nodes():
+    base = "/sys/devices/system/node"
+    nodes = {}
+    try:
+        for name in sorted(os.listdir(base)):
+            if name.startswith("node") and name[4:].isdigit():
+                with open(os.path.join(base, name, "cpulist")) as f:
+                    cpus = _cpulist(f.read())
+                if cpus:
+                    nodes[int(name[4:])] = cpus
+    except OSError:
+        pass
+    return nodes
+
+
+def buffer_numa_pages(ptr):
+    """{node: pages} of the mapping that holds host address `ptr` (/proc/self/numa_maps)."""
+    start = None
+    try:
+        with open("/proc/self/maps") as f:
+            for line in f:
+                lo, hi = (int(x, 16) for x in line.split()[0].split("-"))
+                if lo <= ptr < hi:
+                    start = lo
+                    break
+        if start is None:
+            return {}
+        with open("/proc/self/numa_maps") as f:
+            for line in f:
+                fields = line.split()
+                if int(fields[0], 16) == start:
+                    return {int(k[1:]): int(v) for k, v in (x.split("=") for x in fields[2:] if x[:1] == "N" and "=" in x)}
+    except (OSError, ValueError):
+        pass
+    return {}
+
+
+def thread_cpus(comm):
+    """Last CPU of each thread of this process named `comm`."""
+    cpus = []
+    try:
+        for tid in os.listdir("/proc/self/task"):
+            try:
+                with open(f"/proc/self/task/{tid}/comm") as f:
+                    if f.read().strip() != comm:
+                        continue
+                with open(f"/proc/self/task/{tid}/stat") as f:
+                    stat = f.read()
+                cpus.append(int(stat[stat.rindex(")") + 2:].split()[36]))
+            except (OSError, ValueError, IndexError):
+                continue
+    except OSError:
+        pass
+    return sorted(cpus)
+
+
+def gpu_numa_node(dev_index):
+    import torch
+    p = torch.cuda.get_device_properties(dev_index)
+    bus = f"{p.pci_domain_id:04x}:{p.pci_bus_id:02x}:{p.pci_device_id:02x}.0"
+    try:
+        with open(f"/sys/bus/pci/devices/{bus}/numa_node") as f:
+            return int(f.read().strip())
+    except (OSError, ValueError):
+        return None
+
+
+def host_placement(ptr, dev_index):
+    nodes = numa_nodes()
+    node_of = {c: n for n, cs in nodes.items() for c in cs}
+    fill = thread_cpus("tprf-host-fill")
+    allowed = sorted(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else []
+    return {"pinned_buffer_pages_by_node": buffer_numa_pages(ptr), "gpu_pci_numa_node": gpu_numa_node(dev_index),
+            "cpus_allowed": len(allowed), "cpus_allowed_by_node": {n: sum(1 for c in allowed if node_of.get(c) == n)
+                                                                   for n in nodes},
+            "fill_thread_cpus": fill, "fill_thread_nodes": sorted({node_of.get(c) for c in fill} - {None})}
 
 
 # ---------------------------------------------------------------------------
@@ -294,16 +387,17 @@ def run_gpu(args):
     stages = ["dyson", "fft_k_to_r", "nu_to_tau", "bubble_tau_to_w", "fft_r_to_q", "rpa"]
     no_events = (ctypes.c_void_p * 5)()
 
-    def step(ev=None):
+    def step(ev=None, out=None):
         # Dyson, then the bubble chain through its own entry point (k->r, iv->tau,
         # bubble + tau->iw, r->q; stage events recorded by the library), then the RPA
+        out = chi if out is None else out
         if ev is not None:
             ev[0][0].record(stream)
         check(lib.tprf_lattice_dyson_g_wk(beta, n_max, nk, nb, mu, e_k.data_ptr(), None, 0, g_wk.data_ptr(), sh))
         check(lib.tprf_imtime_bubble_chi0_wk_timed(beta, n_max, n_tau, nw, d3, nb, g_wk.data_ptr(), None,
                                                    chi0.data_ptr(), ws.data_ptr(), ws_bytes,
                                                    ev[1] if ev is not None else no_events, sh))
-        check(lib.tprf_solve_rpa_PH_wk(nw, d3, nb, chi0.data_ptr(), U.data_ptr(), chi.data_ptr(), sh))
+        check(lib.tprf_solve_rpa_PH_wk(nw, d3, nb, chi0.data_ptr(), U.data_ptr(), out.data_ptr(), sh))
         if ev is not None:
             ev[0][6].record(stream)
 
@@ -337,6 +431,42 @@ def run_gpu(args):
     stage_ms = {s: statistics.mean(evs[k][i].elapsed_time(evs[k][i + 1]) for k in range(args.steps))
                 for i, s in enumerate(stages)}
     value = world * points / (ms_per_step / 1e3)
+
+    # ---- the metric's accuracy clause: one more step with every stage in native
+    # FP64 (the plain GPU path: no double-float stage, every (w, q) point solved on
+    # its own), compared with the benched step's chi over the whole tensor
+    accuracy = None
+    if not args.no_accuracy:
+        chi_ref = torch.empty_like(chi)
+        mode0, tune0 = lib.tprf_get_arithmetic(), lib.tprf_get_autotune()
+        lib.tprf_set_autotune(0)
+        check(lib.tprf_set_arithmetic(1))
+        try:
+            a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a0.record(stream)
+            step(out=chi_ref)
+            a1.record(stream)
+            torch.cuda.synchronize()
+            check(lib.tprf_check_device_status(sh), "FP64 step")
+        finally:
+            lib.tprf_set_arithmetic(mode0)
+            lib.tprf_set_autotune(tune0)
+        fp64_ms = a0.elapsed_time(a1)
+        num = den = 0.0
+        for a in range(0, nwt, 32):  # chunks of frequencies bound the temporaries
+            b = min(nwt, a + 32)
+            num = max(num, float((chi[a:b] - chi_ref[a:b]).abs().max()))
+            den = max(den, float(chi_ref[a:b].abs().max()))
+        accuracy = {"max_rel_err_vs_fp64": num / den, "bar": 1e-10,
+                    "definition": "max |chi - chi_fp64| / max |chi_fp64| over the whole (iw, q, orbital) tensor",
+                    "arithmetic": {0: "df64", 1: "fp64", 2: "df64_all"}[mode0],
+                    "arithmetic_detail": "double-float (FP32 pairs) in the lattice FFTs, iv->tau, bubble + tau->iw, "
+                                         "the Dyson inversion and the nb >= 3 RPA (points with a conditioning "
+                                         "estimate above 100 re-solved in FP64); tail fits and fit_derivatives "
+                                         "samples in FP64" if mode0 == 0 else "see tprf_set_arithmetic",
+                    "fp64_path": {"value": world * points / (fp64_ms / 1e3), "unit": UNIT, "ms_per_step": fp64_ms}}
+        del chi_ref
+        torch.cuda.empty_cache()
 
     # ---- end to end through the public API, host buffers in and out
     e2e = None
@@ -374,6 +504,18 @@ def run_gpu(args):
             torch.cuda.synchronize()
             return max_over_ranks((time.perf_counter() - t0) / n, world, dev)
 
+        def host_record():
+            # the library's record of the last call: its device-to-host copies and the
+            # host threads' fill of the negative frequencies
+            st = (ctypes.c_double * 10)()
+            check(lib.tprf_imtime_bubble_rpa_to_host_last_stats(st, 10), "last_stats")
+            return {"d2h_gb": round(st[0] / 1e9, 3), "d2h_copy_ms": round(st[1], 2),
+                    "d2h_gbs": round(st[0] / (st[1] * 1e6), 1) if st[1] > 0 else None,
+                    "copy_span_ms": round(st[2], 2), "fill_span_ms": round(st[3], 2),
+                    "fill_job_ms": round(st[4], 1), "fill_cpus": int(st[5]), "copies": int(st[6]),
+                    "fill_threads": int(st[7]), "real_path": bool(st[8]),
+                    "blocks_with_negative_rows_over_link": round(st[9], 3)}
+
         e2e_steps = max(1, min(args.steps, 5))
         # pipelined: a step's chi copy (bound by the device-to-host link) runs behind the
         # next step's chain; device errors are read once, after the run
@@ -381,9 +523,23 @@ def run_gpu(args):
         e2e_step(False)
         e2e_s = e2e_run(e2e_steps, False)
         check(lib.tprf_check_device_status(sh), "e2e steps")
+        rec_pipelined = host_record()
+        placement = host_placement(out_host.data_ptr(), local)
         # one call at a time: each returns when its chi is on the host
         lib.tprf_set_sync_checks(1)
         serial_s = e2e_run(max(1, min(args.steps, 2)), True)
+        rec_serial = host_record()
+        # the link alone: one 4 GiB device-to-host copy into the same pinned buffer
+        probe = torch.empty(1 << 29, dtype=torch.float64, device=dev)
+        dst = out_host.view(torch.float64).reshape(-1)[: probe.numel()]
+        l0, l1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        dst.copy_(probe, non_blocking=True)
+        l0.record(stream)
+        dst.copy_(probe, non_blocking=True)
+        l1.record(stream)
+        torch.cuda.synchronize()
+        link_gbs = probe.numel() * 8 / (l0.elapsed_time(l1) * 1e6)
+        del probe
         # the bytes that crossed to the host: the frequencies w >= 0 when the host fills
         # chi(-w, q) = conj(chi(w, -q)) (real bubble, real U), else all of chi
         d2h = int(lib.tprf_imtime_bubble_rpa_to_host_last_d2h_bytes())
@@ -394,7 +550,10 @@ def run_gpu(args):
                        "chi(-w, q) = conj(chi(w, -q)) when only w >= 0 crossed)",
                "steps": e2e_steps, "ms_per_step": e2e_s * 1e3,
                "serial": {"value": world * points / serial_s, "ms_per_step": serial_s * 1e3,
-                          "path": "imtime_bubble_rpa_wk(wait=True): each call returns with chi on the host"}}
+                          "path": "imtime_bubble_rpa_wk(wait=True): each call returns with chi on the host",
+                          "host_side_last_step": rec_serial},
+               "host_side_last_step": rec_pipelined, "d2h_link_gbs_4gib_copy": round(link_gbs, 1),
+               "placement": placement}
 
     # ---- roofline of the dominant kernel
     model = stage_model(nb, nk, n_nu, n_tau, nw)
@@ -433,6 +592,7 @@ def run_gpu(args):
                          f"chi {points * nb4 * C16 / 1e9:.2f} GB per step)",
                    "parallelism": f"replicas x{world}"},
         "e2e": e2e,
+        "accuracy": accuracy,
         "gpu_launches": launches_per_step * args.steps,
         "roofline": roofline,
         "clocks": clocks.summary(),
@@ -771,13 +931,16 @@ def run_reference(args):
             walls.append(wall)
     from tprf_gb300 import workloads
     cfg = workloads.config(args.config)
+    nb = int(cfg["U"].shape[0])
     value = statistics.mean(vals)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(walls), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic (seeded tight-binding model)",
-        "config": {"workload": cfg["name"], "dims": list(cfg["dims"]), "beta": cfg["beta"], "n_max": cfg["n_max"],
-                   "nw": cfg["nw"]},
+        "config": {"workload": cfg["name"], "dims": list(cfg["dims"]), "nb": nb, "beta": cfg["beta"],
+                   "n_max": cfg["n_max"], "nw": cfg["nw"], "n_tau": 6 * cfg["n_max"] + 1,
+                   "points_per_step": (2 * cfg["nw"] - 1) * int(math.prod(cfg["dims"])),
+                   "vertex": cfg.get("vertex_label"), "parallelism": "host cores"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": procs, "kind": "port",
                          "sample": "FP64 restatement of the reference (numpy), one process per host core, each "
                                    "timing every stage on a slice (~2 s) and scaling it to one full step"},
@@ -795,6 +958,7 @@ def main():
     ap.add_argument("--config", default="cfg1")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
+    ap.add_argument("--no-accuracy", action="store_true", help="skip the FP64 comparison step (profiling runs)")
     ap.add_argument("--streams", type=int, default=32, help="concurrent streams of the batched graph (cfg2)")
     ap.add_argument("--grad", action="store_true", help="cfg2: forward + gradient graphs per step")
     ap.add_argument("--no-autotune", action="store_true", help="fixed launch-shape heuristics instead of measure mode")

@@ -59,13 +59,28 @@ const char *tprf_version(void);
 void tprf_set_sync_checks(int on);
 int tprf_check_device_status(void *stream);
 
-/* Arithmetic of the FFT stages (lattice FFTs, iv -> tau, tau -> i omega).
- * TPRF_ARITH_DF64 (default): butterflies in double-float pairs on the FP32
- * pipe (~48-bit significand; on GB300 FP32 runs ~70x faster than FP64);
- * TPRF_ARITH_FP64: native FP64; TPRF_ARITH_DF64_ALL: double-float also in the
- * RPA solve, where points whose conditioning estimate exceeds 100 are
- * re-solved in FP64. Inputs and outputs are complex128 in every mode.
- * Process-wide; no reference counterpart (the reference has one CPU path). */
+/* Bound of the device-side waits of the TMA-staged lattice pass on the tile
+ * copies it has in flight, in nanoseconds of the GPU's global timer (default
+ * 200 ms; 0 makes every such wait give up at once). A wait that runs out sets
+ * the device error word (reported as "device wait timed out" by the call's
+ * check or tprf_check_device_status); the block then waits up to 1 s for each
+ * of its copies in flight to land and leaves, so the context stays usable.
+ * Process-wide. No reference counterpart. */
+int tprf_set_device_wait_limit_ns(long long ns);
+
+/* Arithmetic of the path. Double-float means pairs of FP32 values (~48-bit
+ * significand, FP32 exponent range) on the FP32 pipe, which on GB300 runs ~70x
+ * faster than the FP64 pipe.
+ * TPRF_ARITH_DF64 (default): double-float in the lattice FFTs, iv -> tau, the
+ *   bubble + tau -> i omega, the Dyson inversion and the RPA solve of nb >= 3
+ *   (the warp-group kernels; a point whose conditioning estimate, largest term
+ *   over smallest pivot, exceeds 100 is re-solved in FP64); native FP64 in the
+ *   tail fits, the fit_derivatives samples and the thread-per-point RPA of
+ *   nb <= 2.
+ * TPRF_ARITH_FP64: native FP64 in every kernel (the plain GPU path).
+ * TPRF_ARITH_DF64_ALL: as DF64, with the nb <= 2 RPA in double-float as well.
+ * Inputs and outputs are complex128 in every mode. Process-wide; no reference
+ * counterpart (the reference has one CPU path). */
 #define TPRF_ARITH_DF64 0
 #define TPRF_ARITH_FP64 1
 #define TPRF_ARITH_DF64_ALL 2
@@ -115,9 +130,13 @@ int tprf_tail_fit_matrix_stat(double beta, int n, int fermion, int capacity, int
                               int *rows, double *F);
 
 /* Host-only: exact inverse of the 8x8 Vandermonde matrix V[m][j] = m^j
- * (m = 1..8), the matrix fourier_matsubara.cpp:56-71 approximates (used by
- * the fit_derivatives moments of the tau -> i omega transform). */
+ * (m = 1..8), the matrix fourier_matsubara.cpp:56-71 approximates. */
 void tprf_vandermonde_inverse8(double out[64]);
+/* Host-only: rows 0 and 1 of that inverse as TPRF hard-codes them in
+ * fit_derivatives (fourier_matsubara.cpp:56-71, up to ~5e-12 relative from
+ * the exact rationals): out[0..7] row 0 (first derivative), out[8..15] row 1.
+ * These are the constants the tau -> i omega kernels apply. */
+void tprf_fit_derivative_rows(double out[16]);
 
 /* ---- (a) Dyson equation -------------------------------------------------
  * G(iv_n, k) = [(iv_n + mu) I - e(k) - Sigma]^-1, per (v, k).
@@ -281,6 +300,26 @@ int tprf_imtime_bubble_rpa_to_host_async(double beta, int n_iw, int n_tau, int n
 int tprf_imtime_bubble_rpa_to_host_join(void *stream);
 /* Bytes the last of these calls on this device copied from the device to the host. */
 size_t tprf_imtime_bubble_rpa_to_host_last_d2h_bytes(void);
+/* Host-side record of the last of these calls on this device, for diagnosing
+ * the end-to-end time: out[0] bytes copied to the host, out[1] summed duration
+ * of its device-to-host copies (ms, CUDA events around each copy), out[2] span
+ * from the start of the first copy to the end of the last (ms), out[3] span of
+ * the host threads' fill of the negative frequencies (ms, 0 without a fill),
+ * out[4] summed fill-job time (ms), out[5] distinct host CPUs the fill jobs ran
+ * on, out[6] copies, out[7] fill threads of the pool, out[8] 1 when the call
+ * took the real-bubble path (conjugate pairs), out[9] fraction of the
+ * frequency blocks whose negative frequencies crossed the link (1 when the host
+ * filled none). Writes min(n, 10) values. Waits for that call's copies and
+ * fill to finish. No reference counterpart. */
+int tprf_imtime_bubble_rpa_to_host_last_stats(double *out, int n);
+/* Where the negative frequencies of a real chi come from when only some need to
+ * cross the link (a real bubble and a real U): mode 1 fills all of them on the
+ * host from the rows w >= 0 (half the link bytes, twice the host-memory traffic
+ * of a copy), mode 0 copies every row over the link, mode -1 (default) splits the
+ * frequency blocks between the two, moving the split on every completed call
+ * toward the point where the link's and the host threads' measured times meet.
+ * Per device, process-wide. No reference counterpart. */
+int tprf_set_host_fill(int mode);
 
 /* solve_rpa_PH with chi written to HOST memory, as the reference's C++ function
  * returns it (rpa.cpp:29-68 returns a host gf). The points are solved in chunks

@@ -83,7 +83,7 @@ def tau_to_w(chi_tr, beta, nw):
     rest = chi_tr.shape[1:]
     g = chi_tr.reshape(n_tau, -1)
     dtau = beta / (n_tau - 1)
-    V = _t(O.vandermonde_inverse(8))
+    V = _t(O.FIT_DERIVATIVE_ROWS)
     taus = torch.as_tensor(np.arange(1, 9) * dtau, dtype=torch.float64)[:, None]
     d_left = (g[1:9] - g[0][None]) / taus
     d_right = (g[n_tau - 1][None] - g[n_tau - 2 - torch.arange(8)]) / taus

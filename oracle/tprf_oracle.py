@@ -26,7 +26,7 @@ __all__ = [
     "fourier_wk_to_wr", "fourier_wr_to_wk",
     "tail_fit_indices", "tail_fit_matrix", "tail_fit",
     "g0_tail_moments_wr",
-    "fourier_wr_to_tr", "fit_derivatives", "vandermonde_inverse",
+    "fourier_wr_to_tr", "fit_derivatives", "vandermonde_inverse", "FIT_DERIVATIVE_ROWS",
     "fourier_tr_to_wr", "chi_tr_from_chi_wr", "default_n_iw", "tail_order",
     "bubble_PI_wk", "dynamical_screened_interaction_W", "dynamical_screened_interaction_W_wk",
     "gw_dynamic_sigma", "split_into_dynamic_wk_and_constant_k",
@@ -37,6 +37,10 @@ __all__ = [
     "lindhard_chi00", "kanamori_charge_and_spin_quartic_interaction_tensors",
     "quartic_tensor_from_charge_and_spin", "kanamori_quartic_tensor",
     "fermi", "chi0_q0_integral_1d",
+    "tprf_order_to_matrix_rpa_order", "lose_spin_degree_of_freedom", "rpa_us_tensor", "rpa_uc_tensor",
+    "tensor_to_matrix", "matrix_to_tensor", "matrix_rpa", "chi_rpa_spin", "chi_rpa_charge",
+    "split_quartic_tensor_in_charge_and_spin", "general_susceptibility_from_charge_and_spin",
+    "charge_and_spin_susceptibility_from_general", "hartree_response",
 ]
 
 # ----------------------------------------------------------------------------
@@ -366,14 +370,23 @@ def vandermonde_inverse(order: int = 8) -> np.ndarray:
     return np.array([[float(v) for v in row] for row in inv])
 
 
-_VINV = vandermonde_inverse(8)
+# Rows 0 and 1 of the inverse Vandermonde table exactly as fourier_matsubara.cpp:56-71
+# hard-codes them (the only rows fit_derivatives uses): the reference's own numbers,
+# up to ~5e-12 relative from the exact rationals above.
+FIT_DERIVATIVE_ROWS = np.array([
+    [8.000000000008853, -28.000000000055913, 56.000000000151815, -70.00000000021936,
+     56.00000000020795, -28.000000000115904, 8.00000000003683, -1.0000000000049232],
+    [-13.742857142879107, 62.10000000013776, -133.5333333337073, 172.75000000055635,
+     -141.00000000052023, 71.43333333362274, -20.600000000091182, 2.592857142869304]])
+_VINV = FIT_DERIVATIVE_ROWS
 
 
 def fit_derivatives(gt: np.ndarray, beta: float, statistic: str = "Boson"):
     """Moments m2, m3 of a tau function from 8-point one-sided differences.
 
     ``fourier_matsubara.cpp:42-97``: d_left[m-1] = (g[m]-g[0])/tau_m,
-    d_right[m-1] = (g[N-1]-g[N-1-m])/tau_m, g_vec = Vinv @ d; m2 = gl0 - s gr0,
+    d_right[m-1] = (g[N-1]-g[N-1-m])/tau_m, g_vec = Vinv @ d with the
+    reference's table rows (FIT_DERIVATIVE_ROWS); m2 = gl0 - s gr0,
     m3 = -(gl1 + s gr1) * 2 / dtau with s = -1 (Fermion) or +1 (Boson).
     gt: [N_tau, ncol]. Returns [2, ncol].
     """
@@ -749,3 +762,149 @@ def kanamori_quartic_tensor(norb, U, Up, J, Jp):
     """``rpa_tensor.py:198-233``."""
     U_c, U_s = kanamori_charge_and_spin_quartic_interaction_tensors(norb, U, Up, J, Jp)
     return quartic_tensor_from_charge_and_spin(U_c, U_s)
+
+
+# ---------------------------------------------------------------------------
+# Matrix RPA and the charge / spin channels (known answers of
+# test/python/compare_general_rpa_to_matrix_rpa.py:150-241)
+
+def tprf_order_to_matrix_rpa_order(x: np.ndarray) -> np.ndarray:
+    """Swap the last two target indices. ``python/triqs_tprf/matrix_rpa.py:42-48``."""
+    return np.swapaxes(x, -1, -2)
+
+
+def lose_spin_degree_of_freedom(x: np.ndarray, rank: int, spin_fast: bool = True) -> np.ndarray:
+    """One spin block of the last `rank` (spin, orbital) indices: every second index
+    (spin fast) or the second half (spin slow). ``matrix_rpa.py:51-76``, ``rpa_tensor.py:236-256``."""
+    norb = x.shape[-1] // 2
+    sl = slice(None, None, 2) if spin_fast else slice(norb, None)
+    return x[(Ellipsis,) + (sl,) * rank]
+
+
+def _kanamori_pattern(norb, v_diag, v_pair, v_dens, v_flip):
+    """The four Kanamori index patterns of ``matrix_rpa.py:79-142``: a=b=c=d, a=c!=b=d,
+    a=b!=c=d, a=d!=b=c, in the cc^+c^+c order of the matrix formalism."""
+    out = np.zeros([norb] * 4, dtype=complex)
+    for a, b, c, d in itertools.product(range(norb), repeat=4):
+        if a == b == c == d:
+            out[a, b, c, d] = v_diag
+        elif a == c != b == d:
+            out[a, b, c, d] = v_pair
+        elif a == b != c == d:
+            out[a, b, c, d] = v_dens
+        elif a == d != b == c:
+            out[a, b, c, d] = v_flip
+    return out
+
+
+def rpa_us_tensor(norb, U, Up, J, Jp):
+    """Spin-channel vertex of the matrix formalism. ``matrix_rpa.py:79-109``."""
+    return _kanamori_pattern(norb, U, Up, J, Jp)
+
+
+def rpa_uc_tensor(norb, U, Up, J, Jp):
+    """Charge-channel vertex of the matrix formalism. ``matrix_rpa.py:112-142``."""
+    return _kanamori_pattern(norb, U, -Up + 2 * J, 2 * Up - J, Jp)
+
+
+def _matrix_rpa_order(norb: int) -> np.ndarray:
+    """Row/column order of the matrix formalism: the pairs (a, a) first, then the
+    others ascending. ``matrix_rpa.py:145-191``."""
+    idx = list(range(norb * norb))
+    diag = idx[:: norb + 1]
+    return np.array(diag + sorted(set(idx) - set(diag)))
+
+
+def tensor_to_matrix(x: np.ndarray) -> np.ndarray:
+    norb = x.shape[-1]
+    o = _matrix_rpa_order(norb)
+    m = x.reshape(x.shape[:-4] + (norb * norb, norb * norb))
+    return m[..., o, :][..., :, o]
+
+
+def matrix_to_tensor(m: np.ndarray) -> np.ndarray:
+    norb = int(round(np.sqrt(m.shape[-1])))
+    inv = np.argsort(_matrix_rpa_order(norb))
+    return m[..., inv, :][..., :, inv].reshape(m.shape[:-2] + (norb,) * 4)
+
+
+def matrix_rpa(chi0_m: np.ndarray, u_m: np.ndarray) -> np.ndarray:
+    """[1 - chi0 u]^-1 chi0 on matrices. ``matrix_rpa.py:194-212``."""
+    n = chi0_m.shape[-1]
+    return np.linalg.solve(np.eye(n) - chi0_m @ u_m, chi0_m)
+
+
+def chi_rpa_spin(chi0: np.ndarray, us: np.ndarray) -> np.ndarray:
+    """``matrix_rpa.py:215-234``."""
+    return matrix_to_tensor(matrix_rpa(tensor_to_matrix(chi0), tensor_to_matrix(us)))
+
+
+def chi_rpa_charge(chi0: np.ndarray, uc: np.ndarray) -> np.ndarray:
+    """With -uc (the charge channel's sign). ``matrix_rpa.py:237-257``."""
+    return matrix_to_tensor(matrix_rpa(tensor_to_matrix(chi0), -tensor_to_matrix(uc)))
+
+
+def split_quartic_tensor_in_charge_and_spin(U_4: np.ndarray):
+    """(U_c, U_s) of a spin-slow quartic tensor: U_c = -U_uuuu - U_uudd,
+    U_s = U_uuuu - U_uudd, after checking that spin is conserved.
+    ``python/triqs_tprf/rpa_tensor.py:123-172``."""
+    n = U_4.shape[0] // 2
+    U_8 = U_4.reshape(2, n, 2, n, 2, n, 2, n).transpose(0, 2, 4, 6, 1, 3, 5, 7)
+    for s in itertools.product(range(2), repeat=4):
+        conserving = (s[0] == s[1] and s[2] == s[3]) or (s[0] == s[3] and s[1] == s[2])
+        if not conserving:
+            np.testing.assert_array_almost_equal(U_8[s], 0.0)
+    return -U_8[0, 0, 0, 0] - U_8[0, 0, 1, 1], U_8[0, 0, 0, 0] - U_8[0, 0, 1, 1]
+
+
+def _spin_slices(norb, spin_fast):
+    return (slice(None, None, 2), slice(1, None, 2)) if spin_fast else (slice(norb), slice(norb, None))
+
+
+def general_susceptibility_from_charge_and_spin(chi_c, chi_s, spin_fast=True):
+    """chi_uuuu = chi_dddd = (chi_c + chi_s)/2, chi_uudd = chi_dduu = (chi_c - chi_s)/2,
+    chi_uddu = chi_duud = chi_s. ``rpa_tensor.py:259-299``."""
+    norb = chi_c.shape[-1]
+    out = np.zeros(chi_c.shape[:-4] + (2 * norb,) * 4, dtype=complex)
+    up, dn = _spin_slices(norb, spin_fast)
+    e = (Ellipsis,)
+    out[e + (up, up, up, up)] = out[e + (dn, dn, dn, dn)] = 0.5 * (chi_c + chi_s)
+    out[e + (up, up, dn, dn)] = out[e + (dn, dn, up, up)] = 0.5 * (chi_c - chi_s)
+    out[e + (up, dn, dn, up)] = out[e + (dn, up, up, dn)] = chi_s
+    return out
+
+
+def charge_and_spin_susceptibility_from_general(chi, spin_fast=True):
+    """(chi_c, chi_s) = (chi_uuuu + chi_uudd, chi_uuuu - chi_uudd). ``rpa_tensor.py:302-340``."""
+    norb = chi.shape[-1] // 2
+    up, dn = _spin_slices(norb, spin_fast)
+    e = (Ellipsis,)
+    return chi[e + (up, up, up, up)] + chi[e + (up, up, dn, dn)], chi[e + (up, up, up, up)] - chi[e + (up, up, dn, dn)]
+
+
+# ---------------------------------------------------------------------------
+# Hartree linear response (known answer of test/python/hartree_response.py:123-176)
+
+def hartree_response(e_k: np.ndarray, beta: float, mu: float, U_abcd: np.ndarray, eps: float = 1e-9):
+    """Static uniform response of the mean-field (Hartree) lattice to a density field,
+    by central differences of the density matrix, as
+    ``python/triqs_tprf/hf_response.py:56-86, 254-290`` computes it:
+    chi0_ab = -(1/N_k) sum_k d rho_k,bb / d F_aa (field F_aa on orbital a, step eps)
+    and chi_ab = chi0 [1 - U_ab chi0]^-1 with U_ab = U_abcd[a, a, b, b]."""
+    nk, nb = e_k.shape[0], e_k.shape[-1]
+    E = e_k - mu * np.eye(nb)
+
+    def rho(H):
+        w, v = np.linalg.eigh(H)
+        f = 1.0 / (np.exp(beta * w) + 1.0)
+        return np.einsum("kab,kb,kcb->kac", v, f, v.conj())
+
+    chi0 = np.zeros((nb, nb), dtype=complex)
+    for a in range(nb):
+        F = np.zeros((nb, nb))
+        F[a, a] = 1.0
+        d = (rho(E + eps * F) - rho(E - eps * F)).sum(axis=0) / (2.0 * eps * nk)
+        chi0[a] = -np.diag(d)
+    U_ab = np.array([[U_abcd[a, a, b, b] for b in range(nb)] for a in range(nb)])
+    chi = chi0 @ np.linalg.inv(np.eye(nb) - U_ab @ chi0)
+    return chi0, chi

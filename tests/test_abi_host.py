@@ -78,6 +78,13 @@ def test_vandermonde_inverse_bitwise(lib):
     assert np.array_equal(np.array(v[:]).reshape(8, 8), O.vandermonde_inverse(8))
 
 
+def test_fit_derivative_rows_bitwise(lib):
+    """The kernels' fit_derivatives constants are the oracle's (the reference's table rows)."""
+    v = (ctypes.c_double * 16)()
+    lib.tprf_fit_derivative_rows(v)
+    assert np.array_equal(np.array(v[:]).reshape(2, 8), O.FIT_DERIVATIVE_ROWS)
+
+
 def test_argument_errors_are_reported_without_a_gpu(lib):
     from tprf_gb300 import _native
     fake = ctypes.c_void_p(0x1000)

@@ -131,3 +131,40 @@ def test_tma_plane_pass_matches_the_plain_pass_and_numpy(cuda_lib, tmp_path, dim
                 assert rel_err(inplace, ref) < 1e-13, (nt, fn)
     finally:
         tuning.clear_wisdom()
+
+
+def test_tma_plane_wait_that_runs_out_is_reported(cuda_lib, tmp_path):
+    """A wait of the TMA-staged plane pass on its tile copies that runs out (limit
+    0 ns: every wait gives up at its first check) sets the device error word, read
+    back as a timeout; the blocks let their copies in flight land before leaving,
+    so the context stays usable and the next call, with the default limit, is
+    correct."""
+    from tprf_gb300 import _native, tuning
+    dims, n_target, n_w = (16, 8, 1), 81, 2
+    rng = np.random.default_rng(9)
+    x = rng.standard_normal((n_w, 128, n_target)) + 1j * rng.standard_normal((n_w, 128, n_target))
+    xd = torch.as_tensor(x, device="cuda").contiguous()
+    ref = np.fft.fftn(x.reshape((n_w,) + dims + (n_target,)), axes=(1, 2, 3)).reshape(x.shape) / 128
+    lib = cuda_lib
+    try:
+        tuning.set_autotune(False)
+        tuning.clear_wisdom()
+        w = tmp_path / "tma.txt"
+        w.write_text(f"{_device_prefix()}/lattice_plane_tma/0/16/8/{n_target} 1\n")
+        tuning.load_wisdom(w)
+        out = torch.empty_like(xd)
+        _native.check(lib.tprf_set_device_wait_limit_ns(0))
+        _native.check(lib.tprf_fourier_wk_to_wr(n_w, _native.dims3(dims), n_target, xd.data_ptr(), out.data_ptr(),
+                                                None))
+        torch.cuda.synchronize()
+        st = lib.tprf_check_device_status(None)
+        assert st != 0 and "timed out" in lib.tprf_last_error().decode()
+        _native.check(lib.tprf_set_device_wait_limit_ns(200_000_000))
+        _native.check(lib.tprf_fourier_wk_to_wr(n_w, _native.dims3(dims), n_target, xd.data_ptr(), out.data_ptr(),
+                                                None))
+        torch.cuda.synchronize()
+        assert lib.tprf_check_device_status(None) == 0
+        assert rel_err(out, ref) < 1e-13
+    finally:
+        lib.tprf_set_device_wait_limit_ns(200_000_000)
+        tuning.clear_wisdom()

@@ -434,6 +434,67 @@ def test_kanamori_rpa_closed_form(cuda_lib):
     np.testing.assert_array_almost_equal(szsz[0, 0].real, f["chi_szsz_q0"])
 
 
+def test_general_rpa_equals_matrix_rpa_on_gpu(cuda_lib):
+    """test/python/compare_general_rpa_to_matrix_rpa.py:150-241 through the CUDA
+    path: the spin-resolved bubble (4 spin-orbitals) and RPA, and the spin and
+    charge channels solved on their own (2 orbitals), obey chi_uu = (chi_c +
+    chi_s)/2, chi_ud = (chi_c - chi_s)/2, chi_xud = chi_s and agree with the
+    matrix formalism, to 1e-10 (the reference asserts rtol 1e-7)."""
+    from test_oracle_known_answers import check_general_vs_matrix_rpa, general_vs_matrix_rpa_model
+    T = tp()
+    hop, dims, beta, n_max, (U, Up, J, Jp) = general_vs_matrix_rpa_model()
+    ek, e_k = gf_ek(hop, dims)
+    g0 = T.lattice_dyson_g0_wk(0.0, e_k, T.MeshImFreq(beta, "Fermion", n_max))
+    chi00 = T.imtime_bubble_chi0_wk(g0, nw=1, verbose=False)
+    U_abcd = O.kanamori_quartic_tensor(2, U, Up, J, Jp)
+    uc, us = O.split_quartic_tensor_in_charge_and_spin(U_abcd)
+    chi = T.solve_rpa_PH(chi00, U_abcd).data.cpu().numpy()
+    c0 = O.lose_spin_degree_of_freedom(chi00.data.cpu().numpy(), 4, spin_fast=False).copy()
+    c0g = T.Gf(mesh=chi00.mesh, data=c0)
+    chi_s = T.solve_rpa_PH(c0g, us).data.cpu().numpy()
+    chi_c = T.solve_rpa_PH(c0g, -uc).data.cpu().numpy()
+    ref00 = O.imtime_bubble_chi0_wk(O.lattice_dyson_g0_wk(0.0, ek, beta, n_max), beta, dims, nw=1)
+    assert rel_err(chi00.data, ref00) < PARITY_RTOL
+    check_general_vs_matrix_rpa(chi00.data.cpu().numpy(), chi, chi_s, chi_c, rtol=PARITY_RTOL)
+
+
+def test_hartree_linear_response_on_gpu(cuda_lib):
+    """test/python/hartree_response.py:123-176 through the CUDA path: the static
+    uniform bubble and RPA equal the Hartree linear response (finite differences
+    of the mean-field density) to the reference's decimal 7."""
+    from test_oracle_known_answers import check_hartree, hartree_model
+    T = tp()
+    hop, dims, beta, n_max, U, J = hartree_model()
+    ek, e_k = gf_ek(hop, dims)
+    U_abcd = O.kanamori_quartic_tensor(1, U, U - 2 * J, J, J)
+    chi0_ab, chi_ab = O.hartree_response(ek, beta, 0.0, U_abcd)
+    g0 = T.lattice_dyson_g0_wk(0.0, e_k, T.MeshImFreq(beta, "Fermion", n_max))
+    chi00 = T.imtime_bubble_chi0_wk(g0, nw=1, verbose=False)
+    chi = T.solve_rpa_PH(chi00, U_abcd)
+    check_hartree(chi00.data.cpu().numpy()[0, 0], chi.data.cpu().numpy()[0, 0], chi0_ab, chi_ab)
+
+
+def test_hubbard_1d_fazekas_rpa_on_gpu(cuda_lib):
+    """test/python/mean_field.py:295-351 through the CUDA path: the 1D chain's
+    static q = 0 bubble (imaginary-time chain and analytic Lindhard) and the RPA
+    Sz-Sz response against the fixture's density-of-states integral and Fazekas
+    closed form."""
+    import os
+    T = tp()
+    f = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "hubbard_1d_q0.npz")))
+    beta, U = float(f["beta"]), float(f["U"])
+    hop = {(0,): np.zeros((2, 2)), (1,): -np.eye(2), (-1,): -np.eye(2)}
+    _, e_k = gf_ek(hop, (128, 1, 1))
+    g0 = T.lattice_dyson_g0_wk(0.0, e_k, T.MeshImFreq(beta, "Fermion", 400))
+    chi00 = T.imtime_bubble_chi0_wk(g0, nw=1, verbose=False)
+    lin = T.lindhard_chi00(e_k, T.MeshImFreq(beta, "Boson", 1), 0.0).data.cpu().numpy()
+    np.testing.assert_almost_equal(chi00.data.cpu().numpy(), lin, decimal=5)
+    np.testing.assert_almost_equal(lin[0, 0, 0, 0, 0, 0], f["chi0_q0"])
+    chi = T.solve_rpa_PH(chi00, O.kanamori_quartic_tensor(1, U, 0.0, 0.0, 0.0)).data.cpu().numpy()
+    Sz = 0.5 * np.diag([1.0, -1.0])
+    np.testing.assert_almost_equal(np.einsum("wkabcd,ab,cd->wk", chi, Sz, Sz)[0, 0], f["chi_szsz_q0"])
+
+
 @pytest.mark.parametrize("case", range(len(CASES)))
 @pytest.mark.parametrize("u_kind", ["real", "complex"])
 def test_rpa_on_the_wk_mesh_equals_the_point_solve(cuda_lib, case, u_kind):
@@ -552,6 +613,7 @@ def test_pipelined_fused_calls_equal_the_waiting_call(cuda_lib, arithmetic, case
     expect = [imtime_bubble_rpa_wk(g_wk, U, nw, block_freqs=block, slots=slots).data.clone() for U in Us]
     outs = [torch.empty_like(e).pin_memory() for e in expect]
     lib.tprf_set_sync_checks(0)
+    lib.tprf_set_host_fill(1)  # every negative frequency of a real chi filled on the host
     try:
         for U, out in zip(Us, outs):
             imtime_bubble_rpa_wk(g_wk, U, nw, out=out, block_freqs=block, slots=slots, chi0=chi0, workspace=ws,
@@ -561,6 +623,7 @@ def test_pipelined_fused_calls_equal_the_waiting_call(cuda_lib, arithmetic, case
         _native.check(lib.tprf_check_device_status(None), "pipelined calls")
     finally:
         lib.tprf_set_sync_checks(1)
+        lib.tprf_set_host_fill(-1)
     for e, out in zip(expect, outs):
         assert torch.equal(out, e)
     # real hoppings and a real U on the double-float path (which records that the

@@ -59,6 +59,95 @@ def test_hubbard_1d_bubble_and_fazekas_rpa():
     np.testing.assert_almost_equal(szsz[0, 0], f["chi_szsz_q0"])
 
 
+def general_vs_matrix_rpa_model():
+    """The lattice of test/python/compare_general_rpa_to_matrix_rpa.py:18-60: two
+    orbitals x spin (spin slow), nearest-neighbour hopping -1 on the square lattice
+    with an inter-orbital part -0.1, 16 x 16 k, beta = 5, n_max = 30; Kanamori
+    U = 1, U' = 0.8, J = J' = 0.1."""
+    X = np.zeros((4, 4))
+    X[0, 1] = X[1, 0] = X[2, 3] = X[3, 2] = 1.0
+    T = -1.0 * np.eye(4) - 0.1 * X
+    hop = {(0, 1): T, (0, -1): T, (1, 0): T, (-1, 0): T}
+    return hop, (16, 16, 1), 5.0, 30, (1.0, 0.8, 0.1, 0.1)
+
+
+def check_general_vs_matrix_rpa(chi00, chi, chi_spin, chi_charge, rtol):
+    """The identities of compare_general_rpa_to_matrix_rpa.py:186-241, given the
+    spin-resolved bubble and RPA chi (TPRF order) and the TPRF solves of the spin
+    and charge channels: chi_uu = (chi_c + chi_s)/2, chi_ud = (chi_c - chi_s)/2,
+    chi_xud = chi_s against the matrix formalism, the channel solves against it,
+    and general -> charge/spin -> general."""
+    norb = 2
+    U, Up, J, Jp = general_vs_matrix_rpa_model()[-1]
+    c0 = O.tprf_order_to_matrix_rpa_order(O.lose_spin_degree_of_freedom(chi00, 4, spin_fast=False))
+    cs = O.chi_rpa_spin(c0, O.rpa_us_tensor(norb, U, Up, J, Jp))
+    cc = O.chi_rpa_charge(c0, O.rpa_uc_tensor(norb, U, Up, J, Jp))
+    m = O.tprf_order_to_matrix_rpa_order
+    chi_uu, chi_ud = m(chi[..., :norb, :norb, :norb, :norb]), m(chi[..., :norb, :norb, norb:, norb:])
+    chi_xud = m(chi[..., :norb, norb:, norb:, :norb])
+    np.testing.assert_allclose(chi_uu, 0.5 * (cc + cs), rtol=rtol, atol=rtol * np.abs(cs).max())
+    np.testing.assert_allclose(chi_ud, 0.5 * (cc - cs), rtol=rtol, atol=rtol * np.abs(cs).max())
+    np.testing.assert_allclose(cs, chi_uu - chi_ud, rtol=rtol, atol=rtol * np.abs(cs).max())
+    np.testing.assert_allclose(cc, chi_uu + chi_ud, rtol=rtol, atol=rtol * np.abs(cs).max())
+    np.testing.assert_allclose(cs, chi_xud, rtol=rtol, atol=rtol * np.abs(cs).max())
+    np.testing.assert_allclose(cs, m(chi_spin), rtol=rtol, atol=rtol * np.abs(cs).max())
+    np.testing.assert_allclose(cc, m(chi_charge), rtol=rtol, atol=rtol * np.abs(cs).max())
+    gen = O.general_susceptibility_from_charge_and_spin(chi_charge, chi_spin, spin_fast=False)
+    np.testing.assert_allclose(chi, gen, rtol=rtol, atol=rtol * np.abs(chi).max())
+    c, s = O.charge_and_spin_susceptibility_from_general(chi, spin_fast=False)
+    np.testing.assert_allclose(chi, O.general_susceptibility_from_charge_and_spin(c, s, spin_fast=False), rtol=rtol,
+                               atol=rtol * np.abs(chi).max())
+
+
+def test_general_rpa_equals_matrix_rpa():
+    """test/python/compare_general_rpa_to_matrix_rpa.py:150-241 on the oracle (the
+    reference's rtol 1e-7; the restatement meets ~1e-15)."""
+    hop, dims, beta, n_max, (U, Up, J, Jp) = general_vs_matrix_rpa_model()
+    ek = O.ek_from_hoppings(hop, dims)
+    chi00 = O.imtime_bubble_chi0_wk(O.lattice_dyson_g0_wk(0.0, ek, beta, n_max), beta, dims, nw=1)
+    U_abcd = O.kanamori_quartic_tensor(2, U, Up, J, Jp)
+    uc, us = O.split_quartic_tensor_in_charge_and_spin(U_abcd)
+    np.testing.assert_allclose(O.rpa_us_tensor(2, U, Up, J, Jp), O.tprf_order_to_matrix_rpa_order(us))
+    np.testing.assert_allclose(O.rpa_uc_tensor(2, U, Up, J, Jp), O.tprf_order_to_matrix_rpa_order(uc))
+    c0 = O.lose_spin_degree_of_freedom(chi00, 4, spin_fast=False)
+    check_general_vs_matrix_rpa(chi00, O.solve_rpa_PH(chi00, U_abcd), O.solve_rpa_PH(c0, us),
+                                O.solve_rpa_PH(c0, -uc), rtol=1e-12)
+    # the matrix-formalism index order is a permutation: tensor -> matrix -> tensor is exact
+    x = np.random.default_rng(0).standard_normal((3,) + (2,) * 4)
+    np.testing.assert_array_equal(O.matrix_to_tensor(O.tensor_to_matrix(x)), x)
+
+
+def hartree_model():
+    """test/python/hartree_response.py:33-85 (the branch it runs): one orbital x
+    spin on a 4-site chain, t = 1, beta = 1, mu = 0, 100 fermionic frequencies,
+    Kanamori U = 2.3, J = 0.4 (one orbital: the Hubbard U)."""
+    T = -1.0 * np.eye(2)
+    return {(0,): np.zeros((2, 2)), (1,): T, (-1,): T}, (4, 1, 1), 1.0, 100, 2.3, 0.4
+
+
+def test_hartree_linear_response():
+    """test/python/hartree_response.py:123-176 on the oracle: the static uniform
+    bubble and RPA of the imaginary-time chain equal the Hartree linear response
+    (finite differences of the mean-field density, eps = 1e-9) to the reference's
+    decimal 7, density-density parts and Sz-Sz."""
+    hop, dims, beta, n_max, U, J = hartree_model()
+    ek = O.ek_from_hoppings(hop, dims)
+    U_abcd = O.kanamori_quartic_tensor(1, U, U - 2 * J, J, J)
+    chi0_ab, chi_ab = O.hartree_response(ek, beta, 0.0, U_abcd)
+    chi00 = O.imtime_bubble_chi0_wk(O.lattice_dyson_g0_wk(0.0, ek, beta, n_max), beta, dims, nw=1)
+    chi = O.solve_rpa_PH(chi00, U_abcd)
+    check_hartree(chi00[0, 0], chi[0, 0], chi0_ab, chi_ab)
+
+
+def check_hartree(chi0_abcd, chi_abcd, chi0_ab, chi_ab):
+    dd = lambda x: np.array([[x[a, a, b, b] for b in range(2)] for a in range(2)])  # noqa: E731
+    Sz = np.diag([0.5, -0.5])
+    np.testing.assert_almost_equal(dd(chi0_abcd), chi0_ab)
+    np.testing.assert_almost_equal(np.einsum("ab,abcd,cd->", Sz, chi0_abcd, Sz), np.einsum("aa,ab,bb->", Sz, chi0_ab, Sz))
+    np.testing.assert_almost_equal(dd(chi_abcd), chi_ab)
+    np.testing.assert_almost_equal(np.einsum("ab,abcd,cd->", Sz, chi_abcd, Sz), np.einsum("aa,ab,bb->", Sz, chi_ab, Sz))
+
+
 def test_kanamori_1d_rpa_closed_form():
     """test/python/mean_field_kanamori.py:52-162 (2 orbitals x spin, spin fastest)."""
     f = _load("kanamori_1d_q0.npz")
@@ -101,11 +190,19 @@ def test_vandermonde_inverse_is_exact():
     assert Vi[1, 3] == 172.75 and Vi[0, 0] == 8.0
 
 
+def test_fit_derivative_rows_are_the_reference_table():
+    """The oracle and the CUDA path apply rows 0 and 1 of the reference's rounded
+    inverse Vandermonde table (fourier_matsubara.cpp:56-71); they lie within
+    ~5e-12 relative of the exact rationals (a transcription check)."""
+    exact = O.vandermonde_inverse(8)[:2]
+    rel = np.abs(O.FIT_DERIVATIVE_ROWS - exact) / np.abs(exact)
+    assert rel.max() < 6e-12 and rel.min() > 1e-13  # every entry rounded, none exact
+
+
 def test_fit_derivatives_table_sensitivity():
-    """The reference hard-codes a rounded copy of the 8x8 table
-    (fourier_matsubara.cpp:56-71; entries off by up to ~3.5e-12 relative), the
-    oracle and the CUDA path use the exact rationals. Perturbing the table by
-    1e-11 relative (about 3x that rounding) moves chi(i w) by < 1e-11 relative."""
+    """The table's rounding (up to ~5e-12 relative of the exact inverse) is far
+    below the accuracy bar: perturbing the rows by 1e-11 relative (about 3x that
+    rounding) moves chi(i w) by < 1e-11 relative."""
     f = _load("lindhard_square_2orb.npz")
     dims, beta, ek = tuple(f["dims"]), float(f["beta"]), f["e_k"]
     g0 = O.lattice_dyson_g0_wk(0.0, ek, beta, 64)

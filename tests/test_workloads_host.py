@@ -77,3 +77,16 @@ def test_batched_instances_follow_the_spec():
         nbs.add(x["nb"])
     assert nbs == {1, 2}
     assert W.batched_instances(8, seed=1)[0]["beta"] != a[0]["beta"]
+
+
+def test_vertex_builders_equal_the_oracle_restatement():
+    """tprf_gb300.rpa_tensor (delta-tensor form) gives the oracle's Kanamori tensors
+    (a loop restatement of python/triqs_tprf/rpa_tensor.py:87-233) exactly."""
+    import oracle as O
+    from tprf_gb300 import rpa_tensor as R
+    for norb, pars in [(1, (2.3, 1.5, 0.4, 0.4)), (2, (1.0, 0.8, 0.1, 0.1)), (3, (2.3, 1.5, 0.4, 0.3)),
+                       (5, (3.0, 2.0, 0.5, 0.5))]:
+        for a, b in zip(R.kanamori_charge_and_spin_quartic_interaction_tensors(norb, *pars),
+                        O.kanamori_charge_and_spin_quartic_interaction_tensors(norb, *pars)):
+            assert np.array_equal(a, b)
+        assert np.array_equal(R.kanamori_quartic_tensor(norb, *pars), O.kanamori_quartic_tensor(norb, *pars))

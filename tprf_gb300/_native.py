@@ -37,12 +37,14 @@ SIGNATURES = {
     "tprf_version": (ctypes.c_char_p, []),
     "tprf_set_sync_checks": (None, [c_int]),
     "tprf_check_device_status": (c_int, [c_void_p]),
+    "tprf_set_device_wait_limit_ns": (c_int, [ctypes.c_longlong]),
     "tprf_set_arithmetic": (c_int, [c_int]),
     "tprf_get_arithmetic": (c_int, []),
     "tprf_measure_fp64_tflops": (c_int, [ctypes.POINTER(c_double), c_void_p, c_size_t, c_void_p]),
     "tprf_tail_fit_matrix": (c_int, [c_double, c_int, c_int, ctypes.POINTER(c_int), ctypes.POINTER(c_int),
                                      ctypes.POINTER(c_int), ctypes.POINTER(c_double)]),
     "tprf_vandermonde_inverse8": (None, [ctypes.POINTER(c_double)]),
+    "tprf_fit_derivative_rows": (None, [ctypes.POINTER(c_double)]),
     "tprf_lattice_dyson_g_wk": (c_int, [c_double, c_int, c_long, c_int, c_double, c_void_p, c_void_p, c_int,
                                         c_void_p, c_void_p]),
     "tprf_fourier_wk_to_wr": (c_int, [c_long, c_int3, c_long, c_void_p, c_void_p, c_void_p]),
@@ -66,6 +68,8 @@ SIGNATURES = {
                                                      c_size_t, c_void_p]),
     "tprf_imtime_bubble_rpa_to_host_join": (c_int, [c_void_p]),
     "tprf_imtime_bubble_rpa_to_host_last_d2h_bytes": (c_size_t, []),
+    "tprf_imtime_bubble_rpa_to_host_last_stats": (c_int, [ctypes.POINTER(c_double), c_int]),
+    "tprf_set_host_fill": (c_int, [c_int]),
     "tprf_lindhard_chi00_workspace_bytes": (c_size_t, [c_long, c_int]),
     "tprf_lindhard_chi00": (c_int, [c_long, c_int3, c_int, c_void_p, c_double, c_double, c_int, c_void_p, c_void_p,
                                     c_size_t, c_void_p]),

@@ -19,6 +19,8 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB_DIR = os.path.join(HERE, "_lib")
 LIB_PATH = os.path.join(LIB_DIR, "libtprf_gb300.so")
+CXX_DIR = os.path.join(HERE, "cxx")
+CXX_LIB_PATH = os.path.join(LIB_DIR, "libtprf_gb300_cxx.so")
 
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH_FLAGS + [
@@ -36,6 +38,48 @@ def _nvcc() -> str:
 
 def sources():
     return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
+
+
+def cuda_root() -> str:
+    return os.path.dirname(os.path.dirname(os.path.realpath(_nvcc())))
+
+
+def _cxx() -> str:
+    for cand in (os.environ.get("CXX"), shutil.which("g++"), shutil.which("c++")):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("g++ not found: the C++ layer of tprf_gb300 cannot be built")
+
+
+def cxx_flags():
+    """Compile and link flags of a C++ program using the TPRF-signature layer."""
+    root = cuda_root()
+    return (["-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"), "-I", os.path.join(root, "include")],
+            ["-L", LIB_DIR, "-ltprf_gb300_cxx", "-ltprf_gb300", "-L", os.path.join(root, "lib64"), "-lcudart",
+             "-Wl,-rpath," + LIB_DIR, "-Wl,-rpath," + os.path.join(root, "lib64")])
+
+
+def build_cxx_layer(verbose: bool = False, force: bool = False) -> str:
+    """The C++ host layer with TPRF's signatures (include/triqs_tprf_gb300/triqs_tprf.hpp)
+    over the C ABI: one g++ translation unit, linked against libtprf_gb300.so."""
+    srcs = sorted(os.path.join(CXX_DIR, f) for f in os.listdir(CXX_DIR) if f.endswith(".cpp"))
+    hdrs = [os.path.join(ROOT, "include", "tprf_gb300.h"), os.path.join(ROOT, "include", "triqs_tprf_gb300",
+                                                                          "triqs_tprf.hpp")]
+    if not (force or _stale(CXX_LIB_PATH, srcs + hdrs + [LIB_PATH])):
+        return CXX_LIB_PATH
+    cflags, _ = cxx_flags()
+    root = cuda_root()
+    tmp = CXX_LIB_PATH + ".tmp"
+    cmd = [_cxx(), *cflags, "-fPIC", "-shared", "-Wall", "-o", tmp, *srcs, "-L", LIB_DIR, "-ltprf_gb300",
+           "-L", os.path.join(root, "lib64"), "-lcudart", "-Wl,-rpath," + LIB_DIR,
+           "-Wl,-rpath," + os.path.join(root, "lib64")]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"g++ failed for the C++ layer:\n{res.stdout}\n{res.stderr}")
+    os.replace(tmp, CXX_LIB_PATH)
+    return CXX_LIB_PATH
 
 
 def _stale(target: str, deps) -> bool:
@@ -79,6 +123,7 @@ def build_library(verbose: bool = False, force: bool = False, jobs: int | None =
         run([nvcc, *ARCH_FLAGS, "-shared", "-cudart", "shared", "-Xlinker", "-rpath", "-Xlinker", cuda_lib,
              "-o", tmp, *objs])
         os.replace(tmp, LIB_PATH)
+    build_cxx_layer(verbose=verbose, force=force)
     return LIB_PATH
 
 

@@ -12,12 +12,19 @@
 // symmetry, chi0(-w, q) = conj(chi0(w, -q)), and the conjugate-pair solve,
 // which writes both signs. Otherwise a block is a range of rows of the whole
 // mesh, transformed and solved point by point.
+#include <pthread.h>
+#include <sched.h>
+
 #include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
 #include <condition_variable>
 #include <cstring>
 #include <deque>
 #include <functional>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <thread>
 #include <vector>
@@ -66,7 +73,11 @@ class HostPool {
   HostPool() {
     const unsigned hw = std::thread::hardware_concurrency();
     n_ = std::max(1u, std::min(hw ? hw : 4u, 16u));
-    for (unsigned i = 0; i < n_; ++i) std::thread([this] { run(); }).detach();
+    for (unsigned i = 0; i < n_; ++i) {
+      std::thread t([this] { run(); });
+      pthread_setname_np(t.native_handle(), "tprf-host-fill");  // visible in /proc/<pid>/task/*/comm
+      t.detach();
+    }
   }
   void run() {
     for (;;) {
@@ -89,12 +100,40 @@ class HostPool {
   long outstanding_ = 0;
 };
 
+using Clock = std::chrono::steady_clock;
+
+// Host-side record of one call's fill of the negative frequencies: the span
+// from the first job's start to the last job's end, the summed job times and
+// the host CPUs the jobs ran on (sched_getcpu), read by
+// tprf_imtime_bubble_rpa_to_host_last_stats.
+struct FillStats {
+  std::mutex mu;
+  std::atomic<bool> complete{false};  // set once the call's last fill job has ended
+  bool any = false;
+  Clock::time_point first, last;
+  double job_ms = 0.0;
+  std::vector<int> cpus;
+  void add(Clock::time_point t0, Clock::time_point t1, int cpu) {
+    std::lock_guard<std::mutex> l(mu);
+    if (!any || t0 < first) first = t0;
+    if (!any || t1 > last) last = t1;
+    any = true;
+    job_ms += std::chrono::duration<double, std::milli>(t1 - t0).count();
+    if (cpu >= 0 && std::find(cpus.begin(), cpus.end(), cpu) == cpus.end()) cpus.push_back(cpu);
+  }
+  double span_ms() {
+    std::lock_guard<std::mutex> l(mu);
+    return any ? std::chrono::duration<double, std::milli>(last - first).count() : 0.0;
+  }
+};
+
 // rows -m for m in [m_lo, m_hi) of host chi [2 nw - 1][N_k][n_target] from rows
 // m, split over the pool's threads
 struct HostMirror {
   double2 *host;
   int nw, m_lo, m_hi, d0, d1, d2;
   long n_target;
+  std::shared_ptr<FillStats> stats;
 };
 
 void host_mirror_range(const HostMirror &j, long b0, long b1) {
@@ -118,12 +157,23 @@ void CUDART_CB submit_host_mirror(void *data) {
   for (long i = 0; i < parts; ++i) {
     const long b0 = blocks * i / parts, b1 = blocks * (i + 1) / parts;
     const HostMirror copy = *j;
-    pool.submit([copy, b0, b1] { host_mirror_range(copy, b0, b1); });
+    pool.submit([copy, b0, b1] {
+      const Clock::time_point t0 = Clock::now();
+      host_mirror_range(copy, b0, b1);
+      copy.stats->add(t0, Clock::now(), sched_getcpu());
+    });
   }
   delete j;
 }
 
-void CUDART_CB wait_host_mirrors(void *) { HostPool::get().wait_idle(); }
+// the copy stream's last host function of a call: waits for the call's fill jobs
+// (host functions of one stream run in order, so no later call's jobs are queued yet)
+void CUDART_CB wait_host_mirrors(void *data) {
+  auto *sp = static_cast<std::shared_ptr<FillStats> *>(data);
+  HostPool::get().wait_idle();
+  (*sp)->complete = true;
+  delete sp;
+}
 
 // One copy stream and its events per device, created on first use. copied[i]
 // marks the last copy out of ring slot i (of this call or an earlier one: a
@@ -135,8 +185,73 @@ struct CopyCtx {
   cudaEvent_t computed[kMaxSlots], copied[kMaxSlots], done;
   bool pending[kMaxSlots] = {};
   size_t last_d2h = 0;  // bytes the last call copied to the host
+  // timing events around every copy of the last call (grown on demand) and
+  // its host-fill record
+  std::vector<cudaEvent_t> copy_begin, copy_end;
+  int last_copies = 0;
+  std::shared_ptr<FillStats> last_fill;
+  // Split of the negative frequencies of a real chi between the link and the host
+  // threads: block k copies its rows -m over the link (both signs solved on the
+  // device) when floor((k + 1) f + 1/2) > floor(k f + 1/2), so a fraction f of the
+  // blocks does, spread evenly; the other blocks' rows -m are filled on the host.
+  // Both draw on host memory bandwidth (a DMA write of a row against a read, a
+  // write and a write-allocate read of the fill), so the best f balances the
+  // link's time (1 + f) B / R_link against the fill's (1 - f) B / R_fill.
+  // Adaptive mode measures both rates on each completed call and moves f halfway
+  // to the balance point (kept in [0, 0.9], so the fill rate stays measured).
+  int host_fill_mode = -1;  // -1 adaptive, 0 every row over the link, 1 every row -m filled on the host
+  double dma_frac = 0.4;    // current f of the adaptive mode
+  bool fold_pending = false;
+  bool last_real = false, last_mirror = false;
+  double last_frac = 0.0;
+  size_t last_filled = 0;   // bytes of rows -m the host filled in the last call
   std::mutex mu;        // one call at a time enqueues on this device's copy stream
 };
+
+// the i-th pair of timing events of a call (created on first use)
+int copy_events(CopyCtx *c, int i, cudaEvent_t *b, cudaEvent_t *e) {
+  while ((int)c->copy_begin.size() <= i) {
+    cudaEvent_t x, y;
+    TPRF_CUDA(cudaEventCreate(&x));
+    TPRF_CUDA(cudaEventCreate(&y));
+    c->copy_begin.push_back(x);
+    c->copy_end.push_back(y);
+  }
+  *b = c->copy_begin[i];
+  *e = c->copy_end[i];
+  return TPRF_OK;
+}
+
+// Adaptive split: fold the last call's rates into dma_frac once its copies and
+// fill have finished (checked without waiting; a call still in flight is folded
+// by a later call).
+void fold_split_rates(CopyCtx *c) {
+  if (!c->fold_pending || c->last_copies == 0 || !c->last_fill) return;
+  if (cudaEventQuery(c->copy_end[c->last_copies - 1]) != cudaSuccess) {
+    cudaGetLastError();  // a not-ready query is not an error of the next call
+    return;
+  }
+  if (!c->last_fill->complete.load()) return;
+  c->fold_pending = false;
+  double copy_ms = 0.0;
+  for (int i = 0; i < c->last_copies; ++i) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, c->copy_begin[i], c->copy_end[i]) != cudaSuccess) {
+      cudaGetLastError();
+      return;
+    }
+    copy_ms += ms;
+  }
+  double fill_busy_ms;
+  {
+    std::lock_guard<std::mutex> l(c->last_fill->mu);
+    fill_busy_ms = c->last_fill->job_ms / std::max(1, HostPool::get().threads());
+  }
+  if (copy_ms <= 0.0 || fill_busy_ms <= 0.0 || c->last_filled == 0) return;
+  const double r_link = (double)c->last_d2h / copy_ms, r_fill = (double)c->last_filled / fill_busy_ms;
+  const double target = std::min(0.9, std::max(0.0, (r_link - r_fill) / (r_link + r_fill)));
+  c->dma_frac = 0.5 * (c->dma_frac + target);
+}
 std::mutex g_copy_mu;
 std::map<int, CopyCtx> g_copy;
 
@@ -208,7 +323,7 @@ int bubble_rpa_to_host(double beta, int n_iw, int n_tau, int nw, const int dims[
     float a, b;
     memcpy(&a, &w[0], 4);
     memcpy(&b, &w[1], 4);
-    real = b <= kRealInputTol * a;
+    real = real_input_ratio(a, b);
     u_real = std::all_of(uh.begin(), uh.end(), [](const double2 &v) { return v.y == 0.0; });
   }
   const bool host_mirror = real && u_real;
@@ -218,10 +333,25 @@ int bubble_rpa_to_host(double beta, int n_iw, int n_tau, int nw, const int dims[
   CopyCtx *c = nullptr;
   if ((st = copy_ctx(&c))) return st;
   std::lock_guard<std::mutex> lock(c->mu);
+  fold_split_rates(c);
+  const double frac = !host_mirror ? 1.0 : c->host_fill_mode == 0 ? 1.0 : c->host_fill_mode == 1 ? 0.0 : c->dma_frac;
+  size_t filled = 0;
   TPRF_CUDA(cudaEventRecord(c->done, s));  // the copy stream starts after the chain
   TPRF_CUDA(cudaStreamWaitEvent(c->copy, c->done, 0));
   const int n_w = 2 * nw - 1;
   const int n_blocks = real ? (nw + block_freqs - 1) / block_freqs : (n_w + block_freqs - 1) / block_freqs;
+  auto fill = std::make_shared<FillStats>();
+  int n_copies = 0;
+  // one device-to-host copy on the copy stream, between this call's timing events
+  auto d2h_copy = [&](double2 *dst, const double2 *src, size_t bytes) -> int {
+    cudaEvent_t b, e;
+    if (int r = copy_events(c, n_copies++, &b, &e)) return r;
+    TPRF_CUDA(cudaEventRecord(b, c->copy));
+    TPRF_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->copy));
+    TPRF_CUDA(cudaEventRecord(e, c->copy));
+    d2h += bytes;
+    return TPRF_OK;
+  };
   for (int k = 0; k < n_blocks; ++k) {
     const int slot = k % slots;
     double2 *pos = reinterpret_cast<double2 *>(ring0 + (size_t)slot * sb);
@@ -240,17 +370,17 @@ int bubble_rpa_to_host(double beta, int n_iw, int n_tau, int nw, const int dims[
       if ((st = launch_rpa_wk_block(nw, dims, nb, chi0, Ud, out, s))) return st;
       TPRF_CUDA(cudaEventRecord(c->computed[slot], s));
       TPRF_CUDA(cudaStreamWaitEvent(c->copy, c->computed[slot], 0));
-      TPRF_CUDA(cudaMemcpyAsync(host + (long)(nw - 1 + m0) * row, pos, (size_t)(m1 - m0) * row * sizeof(double2),
-                                cudaMemcpyDeviceToHost, c->copy));
-      d2h += (size_t)(m1 - m0) * row * sizeof(double2);
-      if (m_lo < m1 && host_mirror) {
+      if ((st = d2h_copy(host + (long)(nw - 1 + m0) * row, pos, (size_t)(m1 - m0) * row * sizeof(double2))))
+        return st;
+      const bool by_link = std::floor((k + 1) * frac + 0.5) > std::floor(k * frac + 0.5);
+      if (m_lo < m1 && host_mirror && !by_link) {
         // the partners' rows -m read rows m at every q: all in this block
+        filled += (size_t)(m1 - m_lo) * row * sizeof(double2);
         TPRF_CUDA(cudaLaunchHostFunc(
-            c->copy, submit_host_mirror, new HostMirror{host, nw, m_lo, m1, dims[0], dims[1], dims[2], nb4}));
+            c->copy, submit_host_mirror, new HostMirror{host, nw, m_lo, m1, dims[0], dims[1], dims[2], nb4, fill}));
       } else if (m_lo < m1) {
-        TPRF_CUDA(cudaMemcpyAsync(host + (long)(nw - m1) * row, neg, (size_t)(m1 - m_lo) * row * sizeof(double2),
-                                  cudaMemcpyDeviceToHost, c->copy));
-        d2h += (size_t)(m1 - m_lo) * row * sizeof(double2);
+        if ((st = d2h_copy(host + (long)(nw - m1) * row, neg, (size_t)(m1 - m_lo) * row * sizeof(double2))))
+          return st;
       }
     } else {
       const int r0 = k * block_freqs, r1 = std::min(n_w, r0 + block_freqs);
@@ -259,15 +389,21 @@ int bubble_rpa_to_host(double beta, int n_iw, int n_tau, int nw, const int dims[
       if ((st = launch_rpa((long)(r1 - r0) * nk, nb, rows, Ud, pos, s))) return st;
       TPRF_CUDA(cudaEventRecord(c->computed[slot], s));
       TPRF_CUDA(cudaStreamWaitEvent(c->copy, c->computed[slot], 0));
-      TPRF_CUDA(cudaMemcpyAsync(host + (long)r0 * row, pos, (size_t)(r1 - r0) * row * sizeof(double2),
-                                cudaMemcpyDeviceToHost, c->copy));
-      d2h += (size_t)(r1 - r0) * row * sizeof(double2);
+      if ((st = d2h_copy(host + (long)r0 * row, pos, (size_t)(r1 - r0) * row * sizeof(double2)))) return st;
     }
     TPRF_CUDA(cudaEventRecord(c->copied[slot], c->copy));
     c->pending[slot] = true;
   }
-  if (host_mirror) TPRF_CUDA(cudaLaunchHostFunc(c->copy, wait_host_mirrors, nullptr));
+  if (host_mirror)
+    TPRF_CUDA(cudaLaunchHostFunc(c->copy, wait_host_mirrors, new std::shared_ptr<FillStats>(fill)));
   c->last_d2h = d2h;
+  c->last_copies = n_copies;
+  c->last_fill = fill;
+  c->last_real = real;
+  c->last_mirror = host_mirror;
+  c->last_frac = frac;
+  c->last_filled = filled;
+  c->fold_pending = host_mirror && filled > 0;
   TPRF_CUDA(cudaEventRecord(c->done, c->copy));
   if (join) TPRF_CUDA(cudaStreamWaitEvent(s, c->done, 0));
   return finish_with_checks(s, "imtime_bubble_rpa_to_host");
@@ -296,6 +432,51 @@ extern "C" size_t tprf_imtime_bubble_rpa_to_host_last_d2h_bytes(void) {
   if (copy_ctx(&c)) return 0;
   std::lock_guard<std::mutex> lock(c->mu);
   return c->last_d2h;
+}
+
+extern "C" int tprf_imtime_bubble_rpa_to_host_last_stats(double *out, int n) {
+  if (!out || n < 1) return set_error(TPRF_ERR_INVALID_ARGUMENT, "imtime_bubble_rpa_to_host_last_stats: no output");
+  CopyCtx *c = nullptr;
+  if (int st = copy_ctx(&c)) return st;
+  std::lock_guard<std::mutex> lock(c->mu);
+  double v[10] = {(double)c->last_d2h, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, (double)HostPool::get().threads(),
+                  c->last_real ? 1.0 : 0.0, c->last_mirror ? c->last_frac : 1.0};
+  if (c->last_copies > 0) {
+    TPRF_CUDA(cudaEventSynchronize(c->copy_end[c->last_copies - 1]));
+    float ms = 0.f;
+    for (int i = 0; i < c->last_copies; ++i) {
+      TPRF_CUDA(cudaEventElapsedTime(&ms, c->copy_begin[i], c->copy_end[i]));
+      v[1] += ms;
+    }
+    TPRF_CUDA(cudaEventElapsedTime(&ms, c->copy_begin[0], c->copy_end[c->last_copies - 1]));
+    v[2] = ms;
+  }
+  if (c->last_fill && c->last_mirror) {
+    // the copy stream's last host function sets the flag after the fill jobs (the
+    // copies above have finished, so it runs next); bounded wait
+    const Clock::time_point t0 = Clock::now();
+    while (!c->last_fill->complete.load()) {
+      if (Clock::now() - t0 > std::chrono::seconds(60))
+        return set_error(TPRF_ERR_CUDA, "imtime_bubble_rpa_to_host_last_stats: host fill did not finish in 60 s");
+      std::this_thread::sleep_for(std::chrono::microseconds(200));
+    }
+    v[3] = c->last_fill->span_ms();
+    std::lock_guard<std::mutex> l(c->last_fill->mu);
+    v[4] = c->last_fill->job_ms;
+    v[5] = (double)c->last_fill->cpus.size();
+  }
+  v[6] = (double)c->last_copies;
+  for (int i = 0; i < n && i < 10; ++i) out[i] = v[i];
+  return TPRF_OK;
+}
+
+extern "C" int tprf_set_host_fill(int mode) {
+  if (mode < -1 || mode > 1) return set_error(TPRF_ERR_INVALID_ARGUMENT, "set_host_fill: mode must be -1, 0 or 1");
+  CopyCtx *c = nullptr;
+  if (int st = copy_ctx(&c)) return st;
+  std::lock_guard<std::mutex> lock(c->mu);
+  c->host_fill_mode = mode;
+  return TPRF_OK;
 }
 
 extern "C" int tprf_imtime_bubble_rpa_to_host_join(void *stream) {

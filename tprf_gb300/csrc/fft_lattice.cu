@@ -329,12 +329,12 @@ __global__ void __launch_bounds__(256) lattice_plane_kernel(const void *in, void
 // longer wait on DRAM latency. The transforms run decimation-in-frequency on
 // the natural-order tile and the store reads the digit-reversed positions.
 // Double-float input lands as it is; complex128 input is converted in place.
-constexpr long kTmaMaxTries = 1L << 22;  // mbarrier probes before a wait gives up
 
 template <bool FWD, bool IN_DF, bool OUT_DF>
 __global__ void __launch_bounds__(256) lattice_plane_tma_kernel(const __grid_constant__ CUtensorMap map, void *out,
                                                                 long outer, long n_target, int nt, int lgt, FftDesc d1,
-                                                                FftDesc d2, int lg2, double scale, unsigned *status) {
+                                                                FftDesc d2, int lg2, double scale, unsigned *status,
+                                                                unsigned long long wait_ns) {
   using E = cdf;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const int n1 = d1.n, n2 = d2.n, P = n1 * n2, tile_elems = P * nt;
@@ -368,13 +368,17 @@ __global__ void __launch_bounds__(256) lattice_plane_tma_kernel(const __grid_con
       fence_async_shared();  // this CTA's earlier accesses to that buffer precede the copy
       issue(nxt, b ^ 1);
     }
-    const bool ok = mbar_wait_bounded(&bar[b], (uint32_t)((k >> 1) & 1), kTmaMaxTries);
+    const bool ok = mbar_wait_timed(&bar[b], (uint32_t)((k >> 1) & 1), wait_ns);
     if (__syncthreads_or(!ok)) {
-      // give the copy in flight a bounded chance to land before leaving
+      // the wait ran out: record it, then let both copies this block has in
+      // flight (this tile's and the next one's) land before leaving, each for at
+      // most kTmaDrainNs, since they write this block's shared memory
       if (threadIdx.x == 0) {
         atomicOr(status, kDevErrTimeout);
-        if (nxt < n_tiles) mbar_wait_bounded(&bar[b ^ 1], (uint32_t)(((k + 1) >> 1) & 1), kTmaMaxTries);
+        mbar_wait_timed(&bar[b], (uint32_t)((k >> 1) & 1), kTmaDrainNs);
+        if (nxt < n_tiles) mbar_wait_timed(&bar[b ^ 1], (uint32_t)(((k + 1) >> 1) & 1), kTmaDrainNs);
       }
+      __syncthreads();
       return;
     }
     E *a = b ? buf1 : buf0;
@@ -478,7 +482,8 @@ int launch_plane_tma_nt(const void *in, bool in_df, void *out, bool out_df, long
   if ((st = encode_tensor_map_f64(&map, in, 4, dims, strides, box))) return st;
   const size_t smem = 2 * (size_t)P * nt * 16 + 16;
   const long tiles = outer * ((n_target + nt - 1) / nt);
-  void (*kern)(const CUtensorMap, void *, long, long, int, int, FftDesc, FftDesc, int, double, unsigned *);
+  void (*kern)(const CUtensorMap, void *, long, long, int, int, FftDesc, FftDesc, int, double, unsigned *,
+               unsigned long long);
   if (in_df)
     kern = out_df ? lattice_plane_tma_kernel<FWD, true, true> : lattice_plane_tma_kernel<FWD, true, false>;
   else
@@ -488,7 +493,7 @@ int launch_plane_tma_nt(const void *in, bool in_df, void *out, bool out_df, long
   TPRF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, smem));
   const long grid = std::max(1L, std::min(tiles, (long)num_sms() * std::max(1, per_sm)));
   kern<<<(unsigned)grid, 256, smem, stream>>>(map, out, outer, n_target, nt, log2i(nt), d1, d2, log2i(n2), scale,
-                                              status);
+                                              status, device_wait_limit_ns());
   TPRF_LAUNCH_CHECK("lattice_plane_tma_kernel");
   return TPRF_OK;
 }

@@ -29,6 +29,9 @@ int cuda_status(cudaError_t e, const char *what);
   } while (0)
 
 bool sync_checks_enabled();
+// Bound (ns of the GPU's global timer) of the device-side waits on copies in
+// flight (the TMA-staged passes); tprf_set_device_wait_limit_ns.
+unsigned long long device_wait_limit_ns();
 
 // Device-side error word (one per device). Kernels OR flag bits into it.
 enum : unsigned {
@@ -98,8 +101,11 @@ struct TauWPlan {
   const float4 *Kf;
 };
 
-// Element type used by the FFT stages: double-float on the FP32 pipe (default)
-// or native FP64; kArithDF64All also runs the RPA solve in double-float.
+// Arithmetic mode. kArithDF64 (default): double-float on the FP32 pipe in the
+// FFT stages, the bubble, the Dyson inversion and the nb >= 3 (warp-group) RPA
+// solve, FP64 in the tail fits and the nb <= 2 thread-per-point RPA; kArithFP64:
+// native FP64 everywhere; kArithDF64All: kArithDF64 with the nb <= 2 RPA in
+// double-float as well.
 enum Arith : int { kArithDF64 = 0, kArithFP64 = 1, kArithDF64All = 2 };
 int arith_mode();
 int get_tau_w_plan(double beta, int n_tau, int nw, const TauWPlan **out);
@@ -116,6 +122,8 @@ int get_tail_fit_plan(double beta, int n, bool fermion, const TailFitPlan **out)
 // Exact inverse of the 8x8 Vandermonde V[m][j] = m^j (m = 1..8), uploaded to
 // __constant__ memory of the TU that needs it.
 void vandermonde_inverse8(double out[64]);
+// rows 0 and 1 of the inverse Vandermonde table as TPRF hard-codes it (fit_derivatives)
+void fit_derivative_rows(double r0[8], double r1[8]);
 
 // Default time mesh of the reference's make_adjoint_mesh for a fermionic
 // mesh with n_iw positive frequencies.
@@ -128,9 +136,16 @@ int num_sms();
 // max |Im G| <= kRealInputTol max |G| (both recorded by the iv -> tau pass as
 // float bits in two words); see the real-pair bubble in matsubara.cu.
 constexpr float kRealInputTol = 1e-11f;
+// Smallest max |G| for which the FP32 ratio test means something (kRealInputTol
+// times it is a normal float); the words of a G that is zero, tiny, infinite or
+// NaN never say real, so such inputs take the general complex path.
+constexpr float kRealInputMin = 1e-26f;
+__host__ __device__ __forceinline__ bool real_input_ratio(float max_abs, float max_im) {
+  return max_abs >= kRealInputMin && max_abs <= 3.4028234e38f && max_im <= kRealInputTol * max_abs;
+}
 #ifdef __CUDACC__
 __device__ __forceinline__ bool gmax_says_real(const unsigned *gmax) {
-  return gmax != nullptr && __uint_as_float(gmax[1]) <= kRealInputTol * __uint_as_float(gmax[0]);
+  return gmax != nullptr && real_input_ratio(__uint_as_float(gmax[0]), __uint_as_float(gmax[1]));
 }
 // The same test on G(iv, r): words [max |G|, max |G(iv) - conj(G(-iv))|]
 // (hermitian_check_kernel); Hermitian in iv means G(tau, r) is real.

@@ -45,13 +45,8 @@ struct VinvRows {
 };
 
 VinvRows make_vinv_rows() {
-  double v[64];
-  vandermonde_inverse8(v);
   VinvRows r;
-  for (int m = 0; m < 8; ++m) {
-    r.r0[m] = v[0 * 8 + m];
-    r.r1[m] = v[1 * 8 + m];
-  }
+  fit_derivative_rows(r.r0, r.r1);
   return r;
 }
 
@@ -64,14 +59,14 @@ struct FitRows {
 };
 
 FitRows make_fit_rows(double beta, int n_tau) {
-  double v[64];
-  vandermonde_inverse8(v);
+  double r0[8], r1[8];
+  fit_derivative_rows(r0, r1);
   const double dtau = beta / (double)(n_tau - 1);
   FitRows f;
   for (int m = 0; m < 8; ++m) {
     const double tau = (double)(m + 1) * dtau;
-    f.c0[m] = v[0 * 8 + m] / tau;
-    f.c1[m] = v[1 * 8 + m] / tau;
+    f.c0[m] = r0[m] / tau;
+    f.c1[m] = r1[m] / tau;
   }
   f.k3 = -2.0 / dtau;
   return f;
@@ -1030,9 +1025,10 @@ int launch_nu_to_tau_df(double beta, int n_iw, int n_tau, long C, const double2 
 
 __global__ void __launch_bounds__(256) hermitian_check_kernel(const double2 *__restrict__ gw, int n_iw, long C,
                                                               unsigned *hw) {
-  // squared magnitudes: the difference in FP64 (it cancels), everything else in
-  // FP32 (the FP64 pipe is the scarce one); the words hold the square roots
-  float g_abs2 = 0.f, g_dev2 = 0.f;
+  // magnitudes as the larger of |Re| and |Im| (within sqrt 2 of the modulus, and
+  // no squares that could overflow or underflow FP32): the difference in FP64 (it
+  // cancels), everything else in FP32 (the FP64 pipe is the scarce one)
+  float g_abs = 0.f, g_dev = 0.f;
   // rows i < n_iw against rows 2 n_iw - 1 - i; the (row, column) of the
   // grid-stride index advance without a division per element
   const long stride = (long)gridDim.x * blockDim.x;
@@ -1051,17 +1047,17 @@ __global__ void __launch_bounds__(256) hermitian_check_kernel(const double2 *__r
     const float ax = split_double(a.x).hi, ay = split_double(a.y).hi, bx = split_double(b.x).hi,
                 by = split_double(b.y).hi;
     const float dx = split_double(a.x - b.x).hi, dy = split_double(a.y + b.y).hi;
-    g_abs2 = fmaxf(g_abs2, fmaxf(fmaf(ax, ax, ay * ay), fmaf(bx, bx, by * by)));
-    g_dev2 = fmaxf(g_dev2, fmaf(dx, dx, dy * dy));
+    g_abs = fmaxf(g_abs, fmaxf(fmaxf(fabsf(ax), fabsf(ay)), fmaxf(fabsf(bx), fabsf(by))));
+    g_dev = fmaxf(g_dev, fmaxf(fabsf(dx), fabsf(dy)));
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-    g_abs2 = fmaxf(g_abs2, __shfl_xor_sync(0xffffffffu, g_abs2, o));
-    g_dev2 = fmaxf(g_dev2, __shfl_xor_sync(0xffffffffu, g_dev2, o));
+    g_abs = fmaxf(g_abs, __shfl_xor_sync(0xffffffffu, g_abs, o));
+    g_dev = fmaxf(g_dev, __shfl_xor_sync(0xffffffffu, g_dev, o));
   }
-  if ((threadIdx.x & 31) == 0) {
-    atomicMax(hw, __float_as_uint(sqrtf(g_abs2)));
-    atomicMax(hw + 1, __float_as_uint(sqrtf(g_dev2)));
+  if ((threadIdx.x & 31) == 0) {  // non-negative floats order as their bit patterns
+    atomicMax(hw, __float_as_uint(g_abs));
+    atomicMax(hw + 1, __float_as_uint(g_dev));
   }
 }
 

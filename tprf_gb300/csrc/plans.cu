@@ -85,6 +85,9 @@ bool sync_checks_enabled() { return g_sync_checks.load(); }
 
 int arith_mode() { return g_arith.load(); }
 
+std::atomic<unsigned long long> g_wait_limit_ns{200000000ull};  // 200 ms
+unsigned long long device_wait_limit_ns() { return g_wait_limit_ns.load(); }
+
 unsigned *device_status_word() {
   static std::map<int, unsigned *> words;
   int dev = 0;
@@ -551,6 +554,23 @@ int get_tail_fit_plan(double beta, int n, bool fermion, const TailFitPlan **out)
   return TPRF_OK;
 }
 
+// Rows 0 and 1 of the inverse of the Vandermonde matrix V[m][j] = m^j (m = 1..8)
+// exactly as TPRF hard-codes them in fit_derivatives
+// (c++/triqs_tprf/fourier/fourier_matsubara.cpp:56-71). They differ from the
+// exact rationals (vandermonde_inverse8) by up to ~5e-12 relative; using the
+// same constants keeps the tau -> i omega moments m2, m3 the reference's. Rows
+// 2..7 of the table never enter the moments.
+void fit_derivative_rows(double r0[8], double r1[8]) {
+  static const double row0[8] = {8.000000000008853,  -28.000000000055913, 56.000000000151815, -70.00000000021936,
+                                 56.00000000020795,  -28.000000000115904, 8.00000000003683,   -1.0000000000049232};
+  static const double row1[8] = {-13.742857142879107, 62.10000000013776,   -133.5333333337073, 172.75000000055635,
+                                 -141.00000000052023, 71.43333333362274,   -20.600000000091182, 2.592857142869304};
+  for (int m = 0; m < 8; ++m) {
+    r0[m] = row0[m];
+    r1[m] = row1[m];
+  }
+}
+
 void vandermonde_inverse8(double out[64]) {
   // Column m of the inverse holds the coefficients of the Lagrange basis
   // polynomial through nodes 1..8 that is 1 at node m+1: integer polynomial
@@ -606,6 +626,12 @@ extern "C" int tprf_set_arithmetic(int mode) {
 
 extern "C" int tprf_get_arithmetic(void) { return tprf::g_arith.load(); }
 
+extern "C" int tprf_set_device_wait_limit_ns(long long ns) {
+  if (ns < 0) return tprf::set_error(TPRF_ERR_INVALID_ARGUMENT, "set_device_wait_limit_ns: negative limit");
+  tprf::g_wait_limit_ns.store((unsigned long long)ns);
+  return TPRF_OK;
+}
+
 extern "C" int tprf_check_device_status(void *stream) {
   unsigned f = 0;
   int st = tprf::read_and_clear_status(static_cast<cudaStream_t>(stream), &f);
@@ -641,3 +667,4 @@ extern "C" int tprf_tail_fit_matrix_stat(double beta, int n, int fermion, int ca
 }
 
 extern "C" void tprf_vandermonde_inverse8(double out[64]) { tprf::vandermonde_inverse8(out); }
+extern "C" void tprf_fit_derivative_rows(double out[16]) { tprf::fit_derivative_rows(out, out + 8); }

@@ -45,13 +45,27 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
   return done != 0;
 }
 
-// Waits for the phase with the given parity, at most max_tries probes (each
-// probe itself suspends the thread for a while). False when the limit ran out.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, long max_tries) {
-  for (long i = 0; i < max_tries; ++i)
-    if (mbar_try_wait(bar, parity)) return true;
-  return false;
+// Nanoseconds of the GPU's global timer.
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
 }
+
+// Waits for the phase with the given parity for at most limit_ns nanoseconds of
+// the global timer (checked before every probe, so limit_ns = 0 gives up at once).
+// False when the limit ran out.
+__device__ __forceinline__ bool mbar_wait_timed(uint64_t *bar, uint32_t parity, unsigned long long limit_ns) {
+  const unsigned long long t0 = global_ns();
+  for (;;) {
+    if (global_ns() - t0 >= limit_ns) return false;
+    if (mbar_try_wait(bar, parity)) return true;
+  }
+}
+
+// Bound of the drain after a timed-out wait: a block waits this long for each
+// copy it has in flight before it leaves (the copies write its shared memory).
+constexpr unsigned long long kTmaDrainNs = 1000000000ull;
 
 // 4-D tiled bulk copy global -> shared, completing on the barrier (bytes counted
 // by the barrier's expect_tx). Coordinates innermost first, in elements.
