@@ -498,9 +498,12 @@ def test_hubbard_1d_fazekas_rpa_on_gpu(cuda_lib):
 @pytest.mark.parametrize("case", range(len(CASES)))
 @pytest.mark.parametrize("u_kind", ["real", "complex"])
 def test_rpa_on_the_wk_mesh_equals_the_point_solve(cuda_lib, case, u_kind):
-    """solve_rpa_PH on a chi0 Gf (mesh-aware C ABI, conjugate point pairs solved
-    once where chi0 and U allow) gives exactly the point-by-point solve
-    (tprf_solve_rpa_PH), and the oracle's chi."""
+    """solve_rpa_PH on a chi0 Gf (mesh-aware C ABI: conjugate point pairs solved
+    once where chi0 and U allow, and with a symmetric U the transposition
+    partner chi(w, -q) = chi(w, q)^T taken where chi0 is symmetric to within the
+    solve's conditioning) gives the point-by-point solve (tprf_solve_rpa_PH) to
+    rounding, and the oracle's chi. In the FP64 mode every point is solved on its
+    own: the two agree exactly."""
     T = tp()
     from tprf_gb300 import _native
     hopf, dims, beta, n_max = CASES[case]
@@ -515,7 +518,10 @@ def test_rpa_on_the_wk_mesh_equals_the_point_solve(cuda_lib, case, u_kind):
     n_points = chi0.data.numel() // nb ** 4
     _native.check(cuda_lib.tprf_solve_rpa_PH(n_points, nb, chi0.data.data_ptr(), Ud.data_ptr(), flat.data_ptr(), None))
     torch.cuda.synchronize()
-    assert torch.equal(chi.data, flat)
+    if cuda_lib.tprf_get_arithmetic() == 1:
+        assert torch.equal(chi.data, flat)
+    else:
+        assert rel_err(chi.data, flat) < 1e-12
     ref0 = O.imtime_bubble_chi0_wk(O.lattice_dyson_g0_wk(0.0, ek, beta, n_max), beta, dims, nw=6)
     assert rel_err(chi.data, O.solve_rpa_PH(ref0, U)) < PARITY_RTOL
 

@@ -158,10 +158,13 @@ int enqueue_instance(const tprf_instance &a, unsigned char *scratch, cudaStream_
   int st = launch_dyson(a.beta, a.n_iw, nk, a.nb, a.mu, reinterpret_cast<const double2 *>(a.e_k), nullptr, 0, g_wk, s);
   if (st) return st;
   if ((st = launch_lattice_fft(true, 2L * a.n_iw, a.dims, nb2, g_wk, g_wr, s))) return st;
-  TPRF_CUDA(cudaMemsetAsync(gmax, 0, 4 * sizeof(unsigned), s));  // real-input and Hermitian tests
-  if ((st = launch_hermitian_check(a.n_iw, nk * nb2, g_wr, gmax + 2, s))) return st;
+  // real-input, Hermitian and transposition tests
+  TPRF_CUDA(cudaMemsetAsync(gmax, 0, 8 * sizeof(unsigned), s));
+  if ((st = launch_hermitian_check(a.n_iw, nk * nb2, g_wr, gmax + 2, s, a.dims, a.nb))) return st;
+  const TransposePairs *tp2 = nullptr;
+  if ((st = get_transpose_pairs(a.dims, a.nb, 2, &tp2))) return st;
   if ((st = launch_nu_to_tau_df(a.beta, a.n_iw, nt, nk * nb2, g_wr, nullptr, g_tr, g_tr_df, s, gmax, gmax + 2,
-                                a.nw > 1)))
+                                a.nw > 1, tp2)))
     return st;
   bool chi_df = false;  // chi0(w, r) handed to r -> q as double-float pairs (as the single-instance chain)
   if (a.nw == 1)

@@ -125,6 +125,19 @@ void vandermonde_inverse8(double out[64]);
 // rows 0 and 1 of the inverse Vandermonde table as TPRF hard-codes it (fit_derivatives)
 void fit_derivative_rows(double r0[8], double r1[8]);
 
+// Transposition pairs of the columns (r, e) of a function on a periodic mesh
+// with nb^rank target elements e: column c = r * nb^rank + e and its partner
+// t(c) = (-r) * nb^rank + e', e' the element with its indices reversed (ab ->
+// ba for rank 2, abcd -> dcba for rank 4). With real hoppings G(tau, -r)_ab =
+// G(tau, r)_ba and chi0(tau, -r)_dcba = chi0(tau, r)_abcd, so a transform of the
+// canonical columns (c <= t(c)) stored at c and t(c) gives every column.
+// pairs[i] = {c, t(c)} for the n_can canonical columns in increasing order.
+struct TransposePairs {
+  long n_can;
+  const int2 *pairs;  // device
+};
+int get_transpose_pairs(const int dims[3], int nb, int rank, const TransposePairs **out);
+
 // Default time mesh of the reference's make_adjoint_mesh for a fermionic
 // mesh with n_iw positive frequencies.
 inline int default_n_tau(int n_iw) { return 6 * n_iw + 1; }
@@ -150,6 +163,12 @@ __device__ __forceinline__ bool gmax_says_real(const unsigned *gmax) {
 // The same test on G(iv, r): words [max |G|, max |G(iv) - conj(G(-iv))|]
 // (hermitian_check_kernel); Hermitian in iv means G(tau, r) is real.
 __device__ __forceinline__ bool hermitian_says_yes(const unsigned *hw) { return gmax_says_real(hw); }
+// And its third word, max |G_ab(iv, -r) - G_ba(iv, r)|: G(iv, -r) = G(iv, r)^T
+// (real hoppings), so that G(tau, -r) = G(tau, r)^T and the bubble columns
+// (r, abcd) and (-r, dcba) are equal (the transposition pairs below).
+__device__ __forceinline__ bool transpose_says_yes(const unsigned *hw) {
+  return hw != nullptr && real_input_ratio(__uint_as_float(hw[0]), __uint_as_float(hw[2]));
+}
 #endif
 
 // Stream-ordered launchers shared by the C-ABI entry points and the batched
@@ -178,6 +197,9 @@ int launch_lattice_fft_fmt(bool forward, long n_w, const int dims[3], long n_tar
 // want_df and the double-float path runs (*wrote_df tells which). skip_neg:
 // on a real bubble (gmax words), the negative frequencies are left unwritten
 // for a following launch_lattice_fft_fmt with the same words, which fills them.
+// With gmax and the transposition words (gmax[2], gmax[4]) saying yes, only the
+// canonical columns of the rank-4 transposition pairs are transformed, each
+// result stored at its column and its partner.
 int launch_chi0_wr_from_grt_df(double beta, int n_tau, int nw, const int dims[3], int nb, const double2 *g,
                                const void *g_df, double2 *chi0_wr, cudaStream_t stream, bool want_df, bool *wrote_df,
                                const unsigned *gmax = nullptr, bool skip_neg = false);
@@ -188,13 +210,20 @@ int launch_chi0_wr_from_grt_df(double beta, int n_tau, int nw, const int dims[3]
 // parts only, one dfl (8 bytes) per element, and with fit_rows_only the
 // complex128 gt holds only the rows t <= 8 and t >= n_tau - 9 that the
 // bubble's fit samples (the fused bubble reads nothing else of it).
+// tp (nullable): the rank-2 transposition pairs of the columns; with hwords'
+// transposition word saying yes, only the canonical columns are transformed and
+// each stored at its column and its partner (G(tau, r) then meets
+// G(tau, -r) = G(tau, r)^T bit for bit).
 int launch_nu_to_tau_df(double beta, int n_iw, int n_tau, long C, const double2 *gw, const double2 *mom, double2 *gt,
                         void *gt_df, cudaStream_t stream, unsigned *gmax = nullptr, const unsigned *hwords = nullptr,
-                        bool fit_rows_only = false);
-// hwords (two words the caller zeroed) <- max |G(iv, r)|, max |G(iv) - conj(G(-iv))|
-// over the 2 n_iw fermionic rows of C columns; launch_nu_to_tau_df with them
-// pairs columns when G(iv, r) is Hermitian in iv.
-int launch_hermitian_check(int n_iw, long C, const double2 *gw, unsigned *hwords, cudaStream_t stream);
+                        bool fit_rows_only = false, const TransposePairs *tp = nullptr);
+// hwords (three words the caller zeroed) <- max |G(iv, r)|, max |G(iv) - conj(G(-iv))|
+// over the 2 n_iw fermionic rows of C columns, and max |G_ab(iv, -r) - G_ba(iv, r)|
+// when dims and nb give the column layout (C = N_r nb^2; nb = 0: the third word
+// says no); launch_nu_to_tau_df with them pairs columns when G(iv, r) is
+// Hermitian in iv, and transposition partners when it is transpose-symmetric.
+int launch_hermitian_check(int n_iw, long C, const double2 *gw, unsigned *hwords, cudaStream_t stream,
+                           const int *dims = nullptr, int nb = 0);
 int launch_tau_to_w_adjoint(double beta, int n_tau, int nw, long C, const double2 *yg, double2 *xg,
                             cudaStream_t stream);
 int launch_nu_to_tau_adjoint(double beta, int n_iw, int n_tau, long C, const double2 *yg, double2 *gg, bool fitted,

@@ -127,7 +127,8 @@ __global__ void __launch_bounds__(kMatsubaraThreads, 2) nu_to_tau_kernel(NuTauPl
                                                         const double2 *__restrict__ mom, double2 *__restrict__ gt,
                                                         long Ccols, int ic, int lg, unsigned *status,
                                                         cdf *__restrict__ gt_df, unsigned *gmax,
-                                                        const unsigned *hwords, int fit_rows_only) {
+                                                        const unsigned *hwords, int fit_rows_only,
+                                                        const int2 *__restrict__ tpairs, long n_can) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ unsigned s_res;
   C *a = reinterpret_cast<C *>(smem_raw);
@@ -141,18 +142,37 @@ __global__ void __launch_bounds__(kMatsubaraThreads, 2) nu_to_tau_kernel(NuTauPl
   // z = g1 + i g2 and G1(tau) = Re T(z), G2(tau) = Im T(z) (T is complex-linear;
   // the fit coefficients and tail moments of such data are real). Column c of
   // the CTA is then the pair of real columns 2 (col0 + c) and 2 (col0 + c) + 1.
-  bool pairs = false;
-  if constexpr (IsDfElem<C>::value) pairs = hermitian_says_yes(hwords);
-  const long n_units = pairs ? (Ccols + 1) / 2 : Ccols;
+  // Transposition partners (real pairs with hwords saying G(iv, -r) =
+  // G(iv, r)^T, and the rank-2 pairs given): the units run over the canonical
+  // columns only, the f-th real column being tpairs[f].x, and each result is
+  // stored at that column and at its partner tpairs[f].y.
+  bool pairs = false, canon = false;
+  if constexpr (IsDfElem<C>::value) {
+    pairs = hermitian_says_yes(hwords);
+    canon = pairs && tpairs != nullptr && transpose_says_yes(hwords);
+  }
+  const long n_real = canon ? n_can : Ccols;  // real columns to transform
+  const long n_units = pairs ? (n_real + 1) / 2 : n_real;
   const long col0 = blockIdx.x * (long)ic;
-  if (col0 >= n_units) return;  // the second half of the grid in pair mode
+  if (col0 >= n_units) return;  // the rest of the grid in pair mode
   const int ncol = (int)min((long)ic, n_units - col0);
+  __shared__ int s_col[64], s_par[64];  // canonical mode: the CTA's real columns and partners (ic <= 32)
+  if (canon)
+    for (int k = tid; k < 2 * ic; k += nthr) {
+      const long f = 2 * col0 + k;
+      const int2 cp = f < n_real ? tpairs[f] : make_int2(0, 0);
+      s_col[k] = cp.x;
+      s_par[k] = cp.y;
+    }
+  __syncthreads();
+  // memory column of real column f of this CTA (f in [2 col0, 2 col0 + 2 ic))
+  auto rcol = [&](long f) -> long { return canon ? (long)s_col[f - 2 * col0] : f; };
   // input of unit c at frequency row n: the column, or z of the pair
   auto in_at = [&](long n, int c) -> double2 {
     if (!pairs) return gw[n * Ccols + col0 + c];
     const long f = 2 * (col0 + c);
-    const double2 g1 = gw[n * Ccols + f];
-    const double2 g2 = f + 1 < Ccols ? gw[n * Ccols + f + 1] : make_double2(0.0, 0.0);
+    const double2 g1 = gw[n * Ccols + rcol(f)];
+    const double2 g2 = f + 1 < n_real ? gw[n * Ccols + rcol(f + 1)] : make_double2(0.0, 0.0);
     return make_double2(g1.x - g2.y, g1.y + g2.x);
   };
 
@@ -202,13 +222,13 @@ __global__ void __launch_bounds__(kMatsubaraThreads, 2) nu_to_tau_kernel(NuTauPl
         // each real column of the pair against its own model (real and imaginary
         // parts of the pair's coefficients)
         const long f = 2 * (col0 + c);
-        for (int h = 0; h < 2 && f + h < Ccols; ++h) {
+        for (int h = 0; h < 2 && f + h < n_real; ++h) {
           double2 model = make_double2(0.0, 0.0);
           for (int q = 0; q < nm; ++q) {
             const double2 cq = coef[q * ic + c];
             model = cfma(p.fitG[i * nm + q], make_double2(h ? cq.y : cq.x, 0.0), model);
           }
-          const double2 d = csub(model, gw[(long)p.fit_row[i] * Ccols + f + h]);
+          const double2 d = csub(model, gw[(long)p.fit_row[i] * Ccols + rcol(f + h)]);
           atomicMax(&s_res, __float_as_uint(sqrtf((float)cabs2(d))));
         }
       }
@@ -224,9 +244,9 @@ __global__ void __launch_bounds__(kMatsubaraThreads, 2) nu_to_tau_kernel(NuTauPl
         m3 = mom[2 * Ccols + col0 + c];
       } else if (c < ncol) {  // z = g1 + i g2: moments likewise
         const long f = 2 * (col0 + c);
-        const bool two = f + 1 < Ccols;
+        const bool two = f + 1 < n_real;
         auto zm = [&](int q) {
-          const double2 a1 = mom[q * Ccols + f], a2 = two ? mom[q * Ccols + f + 1] : make_double2(0.0, 0.0);
+          const double2 a1 = mom[q * Ccols + rcol(f)], a2 = two ? mom[q * Ccols + rcol(f + 1)] : make_double2(0.0, 0.0);
           return make_double2(a1.x - a2.y, a1.y + a2.x);
         };
         m1 = zm(0);
@@ -274,12 +294,21 @@ __global__ void __launch_bounds__(kMatsubaraThreads, 2) nu_to_tau_kernel(NuTauPl
           const long f = 2 * (col0 + c);
           const bool keep = !fit_rows_only || t <= 8 || t >= L - 8;
           dfl *gre = reinterpret_cast<dfl *>(gt_df);
-          if (keep) gt[(long)t * Ccols + f] = as_d2(cdf{v.x, dfl{0.f, 0.f}});
-          if (gt_df) gre[(long)t * Ccols + f] = v.x;
-          if (f + 1 < Ccols) {
-            if (keep) gt[(long)t * Ccols + f + 1] = as_d2(cdf{v.y, dfl{0.f, 0.f}});
-            if (gt_df) gre[(long)t * Ccols + f + 1] = v.y;
-          }
+          // real column f + h gets x, and in the canonical mode its partner too
+          auto put = [&](long fh, dfl x) {
+            const long col = rcol(fh);
+            if (keep) gt[(long)t * Ccols + col] = as_d2(cdf{x, dfl{0.f, 0.f}});
+            if (gt_df) gre[(long)t * Ccols + col] = x;
+            if (canon) {
+              const long pc = s_par[fh - 2 * col0];
+              if (pc != col) {
+                if (keep) gt[(long)t * Ccols + pc] = as_d2(cdf{x, dfl{0.f, 0.f}});
+                if (gt_df) gre[(long)t * Ccols + pc] = x;
+              }
+            }
+          };
+          put(f, v.x);
+          if (f + 1 < n_real) put(f + 1, v.y);
           if (gmax) g_abs = fmaxf(g_abs, fmaxf(fabsf(v.x.hi), fabsf(v.y.hi)));  // both parts are real columns
         }
         continue;
@@ -419,27 +448,39 @@ struct BubbleLoaderDF : BubbleLoader {
 // linear with real coefficients), so the tail works unchanged on z. The
 // imaginary parts of G (rounding residue, below the bound) are dropped.
 
+// Transposition partners: when iv -> tau also ran on canonical columns (its
+// words say G(iv, -r) = G(iv, r)^T, and G(tau, -r) = G(tau, r)^T then holds bit
+// for bit), chi0(tau, -r)_dcba = G_ad(tau, -r) G_cb(beta - tau, r) is the same
+// product, in the same order, as chi0(tau, r)_abcd = G_da(tau, r) G_bc(beta - tau,
+// -r): the columns (r, abcd) and (-r, dcba) are equal, and only the canonical one
+// of each pair (tpairs, rank 4) is transformed, its result stored at both.
 struct BubblePairLoaderDF : BubbleLoaderDF {
-  // the four words of launch_nu_to_tau_df: [max |G|, max |Im G|] of G(tau, r),
-  // then the Hermitian words of G(iv, r), as float bits; null: no pairs
+  // the five words of the chain: [max |G|, max |Im G|] of G(tau, r), then the
+  // Hermitian and transposition words of G(iv, r), as float bits; null: no pairs
   const unsigned *gmax;
+  const int2 *tpairs = nullptr;  // rank-4 transposition pairs (nullable)
+  long n_can = 0;
   bool pairs = false;
   bool compact = false;  // gdf holds real parts only (dfl per element): iv -> tau ran on real pairs
+  bool canon = false;    // transform the canonical columns of tpairs only
   __device__ __forceinline__ void init() {
     pairs = gmax_says_real(gmax);
     compact = pairs && hermitian_says_yes(gmax + 2);
+    canon = compact && tpairs != nullptr && transpose_says_yes(gmax + 2);
   }
+  __device__ __forceinline__ long real_cols() const { return canon ? n_can : Nr * nb * nb * nb * nb; }
+  __device__ __forceinline__ long real_col(long f) const { return canon ? (long)tpairs[f].x : f; }
   // offsets of the two real columns 2 (col0 + c) and 2 (col0 + c) + 1 (the
   // second past the last column reads the first: its results are not stored)
   __device__ __forceinline__ void setup(long col0, int ic, int ncol, long *s) const {
     if (!pairs) return BubbleLoader::setup(col0, ic, ncol, s);
-    const long nreal = Nr * nb * nb * nb * nb;
+    const long nreal = real_cols();
     for (int c = threadIdx.x; c < ic; c += blockDim.x) {
       long o[4] = {0, 0, 0, 0};
       if (c < ncol) {
         const long f = 2 * (col0 + c);
-        offsets(f, o[0], o[1]);
-        offsets(f + 1 < nreal ? f + 1 : f, o[2], o[3]);
+        offsets(real_col(f), o[0], o[1]);
+        offsets(real_col(f + 1 < nreal ? f + 1 : f), o[2], o[3]);
       }
       for (int q = 0; q < 4; ++q) s[q * ic + c] = o[q];
     }
@@ -476,9 +517,13 @@ __global__ void __launch_bounds__(kMatsubaraThreads, 2) tau_to_w_kernel(TauWPlan
                                                        long Ccols, int ic, int lg, int out_df, int skip_neg) {
   Loader ld = ld_in;
   bool pairs = false;  // real pairs (BubblePairLoaderDF on real input): Ccols real columns, half as many FFT columns
+  bool canon = false;  // and only the canonical columns of the transposition pairs
+  long n_real = Ccols;
   if constexpr (HasPairs<Loader>::value) {
     ld.init();
     pairs = ld.pairs;
+    canon = ld.canon;
+    n_real = ld.real_cols();
   }
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C *a = reinterpret_cast<C *>(smem_raw);
@@ -490,11 +535,21 @@ __global__ void __launch_bounds__(kMatsubaraThreads, 2) tau_to_w_kernel(TauWPlan
   long *soff = reinterpret_cast<long *>(am + 4 * ic);           // [4][ic] loader offsets
   double2 *smp = reinterpret_cast<double2 *>(soff + 4 * ic);    // [18][ic] FP64 rows 0..8, L-8..L
   const int tid = threadIdx.x, nthr = blockDim.x;
-  const long n_fft_cols = pairs ? (Ccols + 1) / 2 : Ccols;
+  const long n_fft_cols = pairs ? (n_real + 1) / 2 : Ccols;
   const long col0 = blockIdx.x * (long)ic;
-  if (col0 >= n_fft_cols) return;  // the second half of the grid in pair mode
+  if (col0 >= n_fft_cols) return;  // the rest of the grid in pair mode
   const int ncol = (int)min((long)ic, n_fft_cols - col0);
   ld.setup(col0, ic, ncol, soff);
+  __shared__ int s_tcol[64], s_tpar[64];  // canonical mode: the CTA's real columns and partners (ic <= 32)
+  if constexpr (HasPairs<Loader>::value) {
+    if (canon)
+      for (int k = tid; k < 2 * ic; k += nthr) {
+        const long f = 2 * col0 + k;
+        const int2 cp = f < n_real ? ld.tpairs[f] : make_int2(0, 0);
+        s_tcol[k] = cp.x;
+        s_tpar[k] = cp.y;
+      }
+  }
   __syncthreads();
   // Rows t < L go to their digit-reversed FFT positions, row L aside. The loads
   // of several iterations are issued before any is used (their latency
@@ -632,12 +687,23 @@ __global__ void __launch_bounds__(kMatsubaraThreads, 2) tau_to_w_kernel(TauWPlan
         const long f = 2 * (col0 + c);
         // the negative frequencies only when the caller does not fill them by symmetry
         const bool neg = mh > 0 && !skip_neg;
-        store((long)mp * Ccols + f, F);
-        if (neg) store((long)mn * Ccols + f, conj_el(F));
-        if (f + 1 < Ccols) {
-          store((long)mp * Ccols + f + 1, H);
-          if (neg) store((long)mn * Ccols + f + 1, conj_el(H));
-        }
+        // real column fh gets val (its memory column, and in the canonical mode its partner)
+        auto put = [&](long fh, C val) {
+          long col = fh, pc = -1;
+          if (canon) {
+            col = s_tcol[fh - 2 * col0];
+            pc = s_tpar[fh - 2 * col0];
+            if (pc == col) pc = -1;
+          }
+          store((long)mp * Ccols + col, val);
+          if (neg) store((long)mn * Ccols + col, conj_el(val));
+          if (pc >= 0) {
+            store((long)mp * Ccols + pc, val);
+            if (neg) store((long)mn * Ccols + pc, conj_el(val));
+          }
+        };
+        put(f, F);
+        if (f + 1 < n_real) put(f + 1, H);
       }
       return;
     }
@@ -1010,7 +1076,8 @@ __global__ void __launch_bounds__(256) bubble_adjoint_kernel(BubbleLoader ld, co
 
 int launch_nu_to_tau_stat(double beta, int n_iw, int n_tau, bool fermion, long C, const double2 *gw,
                           const double2 *mom, double2 *gt, cudaStream_t stream, cdf *gt_df = nullptr,
-                          unsigned *gmax = nullptr, const unsigned *hwords = nullptr, bool fit_rows_only = false);
+                          unsigned *gmax = nullptr, const unsigned *hwords = nullptr, bool fit_rows_only = false,
+                          const TransposePairs *tp = nullptr);
 
 // The fermionic transform that also writes G(tau) as double-float pairs into
 // gt_df (left untouched in the FP64 arithmetic mode), for the fused bubble's
@@ -1018,17 +1085,23 @@ int launch_nu_to_tau_stat(double beta, int n_iw, int n_tau, bool fermion, long C
 // gmax (nullable, two words the caller zeroed): max |G| and max |Im G| of the
 // result as float bits, which decide whether the bubble can pair real columns.
 int launch_nu_to_tau_df(double beta, int n_iw, int n_tau, long C, const double2 *gw, const double2 *mom, double2 *gt,
-                        void *gt_df, cudaStream_t stream, unsigned *gmax, const unsigned *hwords, bool fit_rows_only) {
+                        void *gt_df, cudaStream_t stream, unsigned *gmax, const unsigned *hwords, bool fit_rows_only,
+                        const TransposePairs *tp) {
   return launch_nu_to_tau_stat(beta, n_iw, n_tau, true, C, gw, mom, gt, stream, reinterpret_cast<cdf *>(gt_df), gmax,
-                               hwords, fit_rows_only);
+                               hwords, fit_rows_only, tp);
 }
 
+// Words of G(iv, r): hw[0] = max |G|, hw[1] = max |G(iv) - conj(G(-iv))|
+// (Hermitian in iv: G(tau, r) is real) and, with the column layout (nb > 0,
+// C = N_r nb^2), hw[2] = max |G_ab(iv, -r) - G_ba(iv, r)| over all rows (the
+// transposition symmetry of real hoppings); nb = 0 marks hw[2] infinite (no).
 __global__ void __launch_bounds__(256) hermitian_check_kernel(const double2 *__restrict__ gw, int n_iw, long C,
-                                                              unsigned *hw) {
+                                                              unsigned *hw, int nb, int d0, int d1, int d2) {
   // magnitudes as the larger of |Re| and |Im| (within sqrt 2 of the modulus, and
   // no squares that could overflow or underflow FP32): the difference in FP64 (it
   // cancels), everything else in FP32 (the FP64 pipe is the scarce one)
-  float g_abs = 0.f, g_dev = 0.f;
+  float g_abs = 0.f, g_dev = 0.f, g_tdev = 0.f;
+  const int nb2 = nb * nb;
   // rows i < n_iw against rows 2 n_iw - 1 - i; the (row, column) of the
   // grid-stride index advance without a division per element
   const long stride = (long)gridDim.x * blockDim.x;
@@ -1049,22 +1122,37 @@ __global__ void __launch_bounds__(256) hermitian_check_kernel(const double2 *__r
     const float dx = split_double(a.x - b.x).hi, dy = split_double(a.y + b.y).hi;
     g_abs = fmaxf(g_abs, fmaxf(fmaxf(fabsf(ax), fabsf(ay)), fmaxf(fabsf(bx), fabsf(by))));
     g_dev = fmaxf(g_dev, fmaxf(fabsf(dx), fabsf(dy)));
+    if (nb > 0) {
+      // the partner column (-r, ba) of c = (r, ab), at both rows
+      const int ci = (int)c, r = ci / nb2, e = ci - r * nb2, ea = e / nb, eb = e - ea * nb;
+      const int i2 = r % d2, i1 = (r / d2) % d1, i0 = r / (d2 * d1);
+      const long mr = ((long)((d0 - i0) % d0) * d1 + (d1 - i1) % d1) * d2 + (d2 - i2) % d2;
+      const long tc = mr * nb2 + eb * nb + ea;
+      const double2 at = gw[i * C + tc], bt = gw[(2L * n_iw - 1 - i) * C + tc];
+      g_tdev = fmaxf(g_tdev, fmaxf(fmaxf(fabsf(split_double(a.x - at.x).hi), fabsf(split_double(a.y - at.y).hi)),
+                                   fmaxf(fabsf(split_double(b.x - bt.x).hi), fabsf(split_double(b.y - bt.y).hi))));
+    }
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     g_abs = fmaxf(g_abs, __shfl_xor_sync(0xffffffffu, g_abs, o));
     g_dev = fmaxf(g_dev, __shfl_xor_sync(0xffffffffu, g_dev, o));
+    g_tdev = fmaxf(g_tdev, __shfl_xor_sync(0xffffffffu, g_tdev, o));
   }
   if ((threadIdx.x & 31) == 0) {  // non-negative floats order as their bit patterns
     atomicMax(hw, __float_as_uint(g_abs));
     atomicMax(hw + 1, __float_as_uint(g_dev));
+    atomicMax(hw + 2, nb > 0 ? __float_as_uint(g_tdev) : 0x7f800000u);
   }
 }
 
-int launch_hermitian_check(int n_iw, long C, const double2 *gw, unsigned *hwords, cudaStream_t stream) {
+int launch_hermitian_check(int n_iw, long C, const double2 *gw, unsigned *hwords, cudaStream_t stream,
+                           const int *dims, int nb) {
   const long total = (long)n_iw * C;
   const unsigned blocks = (unsigned)std::max(1L, std::min((total + 255) / 256, (long)num_sms() * 8));
-  hermitian_check_kernel<<<blocks, 256, 0, stream>>>(gw, n_iw, C, hwords);
+  const bool layout = dims && nb > 0 && (long)dims[0] * dims[1] * dims[2] * nb * nb == C && C < 0x7fffffffL;
+  hermitian_check_kernel<<<blocks, 256, 0, stream>>>(gw, n_iw, C, hwords, layout ? nb : 0, layout ? dims[0] : 1,
+                                                     layout ? dims[1] : 1, layout ? dims[2] : 1);
   TPRF_LAUNCH_CHECK("hermitian_check_kernel");
   return TPRF_OK;
 }
@@ -1078,7 +1166,7 @@ int launch_nu_to_tau(double beta, int n_iw, int n_tau, long C, const double2 *gw
 // (fourier_matsubara.cpp:250-254).
 int launch_nu_to_tau_stat(double beta, int n_iw, int n_tau, bool fermion, long C, const double2 *gw,
                           const double2 *mom, double2 *gt, cudaStream_t stream, cdf *gt_df, unsigned *gmax,
-                          const unsigned *hwords, bool fit_rows_only) {
+                          const unsigned *hwords, bool fit_rows_only, const TransposePairs *tp) {
   if (n_tau < 0) n_tau = default_n_tau(n_iw);
   if (!(beta > 0.0) || n_iw < 1 || n_tau < 2 || C < 1 || (!fermion && n_iw < 2))
     return set_error(TPRF_ERR_INVALID_ARGUMENT, "fourier_wr_to_tr: bad mesh");
@@ -1105,12 +1193,14 @@ int launch_nu_to_tau_stat(double beta, int n_iw, int n_tau, bool fermion, long C
       TPRF_CUDA(cudaFuncSetAttribute(nu_to_tau_kernel<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
       nu_to_tau_kernel<double2><<<(unsigned)blocks, kMatsubaraThreads, sm, stream>>>(*p, gw, mom, gt, C, icv,
                                                                                       log2_ic(icv), status, nullptr,
-                                                                                      gmax, nullptr, 0);
+                                                                                      gmax, nullptr, 0, nullptr, 0L);
     } else {
       TPRF_CUDA(cudaFuncSetAttribute(nu_to_tau_kernel<cdf>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
       nu_to_tau_kernel<cdf><<<(unsigned)blocks, kMatsubaraThreads, sm, stream>>>(*p, gw, mom, gt, C, icv, log2_ic(icv),
                                                                                   status, gt_df, gmax, hwords,
-                                                                                  fit_rows_only ? 1 : 0);
+                                                                                  fit_rows_only ? 1 : 0,
+                                                                                  tp ? tp->pairs : nullptr,
+                                                                                  tp ? tp->n_can : 0L);
     }
     TPRF_LAUNCH_CHECK("nu_to_tau_kernel");
     return TPRF_OK;
@@ -1172,6 +1262,12 @@ int launch_chi0_wr_from_grt_df(double beta, int n_tau, int nw, const int dims[3]
   static_cast<BubbleLoader &>(ld) = make_bubble(g, n_tau, dims, nb);
   ld.gdf = reinterpret_cast<const cdf *>(g_df);
   ld.gmax = gmax;
+  if (gmax) {
+    const TransposePairs *tp = nullptr;
+    if ((st = get_transpose_pairs(dims, nb, 4, &tp))) return st;
+    ld.tpairs = tp->pairs;
+    ld.n_can = tp->n_can;
+  }
   const long C = ld.Nr * nb * nb * nb * nb;
   st = gmax ? launch_tau_to_w_as<BubblePairLoaderDF, cdf>(p, ld, chi0_wr, C, stream, want_df, skip_neg)
             : launch_tau_to_w_as<BubbleLoaderDF, cdf>(p, static_cast<const BubbleLoaderDF &>(ld), chi0_wr, C, stream,

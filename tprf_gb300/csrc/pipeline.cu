@@ -73,11 +73,15 @@ int bubble_to_wr(double beta, int n_iw, int n_tau, int nw, const int dims[3], in
   st = launch_lattice_fft(true, 2L * n_iw, dims, nb2, reinterpret_cast<const double2 *>(g_wk), g_wr, s);
   if (st || (st = mark(1))) return st;
   // gmax[0..1]: the real-input test of G(tau, r); gmax[2..3]: the Hermitian
-  // test of G(iv, r), which lets iv -> tau pair real columns
-  TPRF_CUDA(cudaMemsetAsync(gmax, 0, 4 * sizeof(unsigned), s));
-  if ((st = launch_hermitian_check(n_iw, nk * nb2, g_wr, gmax + 2, s))) return st;
+  // test of G(iv, r), which lets iv -> tau pair real columns;
+  // gmax[4]: the transposition test of G(iv, r), which lets iv -> tau and the
+  // bubble transform one column of each transposition pair
+  TPRF_CUDA(cudaMemsetAsync(gmax, 0, 8 * sizeof(unsigned), s));
+  if ((st = launch_hermitian_check(n_iw, nk * nb2, g_wr, gmax + 2, s, dims, nb))) return st;
+  const TransposePairs *tp2 = nullptr;
+  if ((st = get_transpose_pairs(dims, nb, 2, &tp2))) return st;
   st = launch_nu_to_tau_df(beta, n_iw, n_tau, nk * nb2, g_wr, reinterpret_cast<const double2 *>(moments), g_tr,
-                           g_tr_df, s, gmax, gmax + 2, nw > 1);
+                           g_tr_df, s, gmax, gmax + 2, nw > 1, tp2);
   if (st || (st = mark(2))) return st;
   // chi0(w, r) goes from the bubble to the r -> q transform as double-float
   // pairs (same bytes) on the double-float path: no conversion in between

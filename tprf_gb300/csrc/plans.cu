@@ -554,6 +554,54 @@ int get_tail_fit_plan(double beta, int n, bool fermion, const TailFitPlan **out)
   return TPRF_OK;
 }
 
+int get_transpose_pairs(const int dims[3], int nb, int rank, const TransposePairs **out) {
+  int dev = 0;
+  int st = current_device(&dev);
+  if (st) return st;
+  static std::map<std::tuple<int, int, int, int, int, int>, std::unique_ptr<TransposePairs>> cache;
+  auto key = std::make_tuple(dev, dims[0], dims[1], dims[2], nb, rank);
+  {
+    std::lock_guard<std::mutex> lock(g_mutex);
+    auto it = cache.find(key);
+    if (it != cache.end()) {
+      *out = it->second.get();
+      return TPRF_OK;
+    }
+  }
+  if (nb < 1 || (rank != 2 && rank != 4)) return set_error(TPRF_ERR_INVALID_ARGUMENT, "transpose pairs: bad shape");
+  const long nr = (long)dims[0] * dims[1] * dims[2];
+  long E = 1;
+  for (int i = 0; i < rank; ++i) E *= nb;
+  if (nr * E > 0x7fffffffL) return set_error(TPRF_ERR_INVALID_ARGUMENT, "transpose pairs: too many columns");
+  std::vector<int> rev((size_t)E);  // element with its indices reversed
+  for (long e = 0; e < E; ++e) {
+    long x = e, r = 0;
+    for (int i = 0; i < rank; ++i) {
+      r = r * nb + x % nb;
+      x /= nb;
+    }
+    rev[(size_t)e] = (int)r;
+  }
+  std::vector<int2> pairs;
+  pairs.reserve((size_t)(nr * E / 2 + E));
+  for (long r = 0; r < nr; ++r) {
+    const long i2 = r % dims[2], i1 = (r / dims[2]) % dims[1], i0 = r / ((long)dims[2] * dims[1]);
+    const long mr = (((dims[0] - i0) % dims[0]) * dims[1] + (dims[1] - i1) % dims[1]) * dims[2] + (dims[2] - i2) % dims[2];
+    for (long e = 0; e < E; ++e) {
+      const long c = r * E + e, t = mr * E + rev[(size_t)e];
+      if (c <= t) pairs.push_back(make_int2((int)c, (int)t));
+    }
+  }
+  auto p = std::make_unique<TransposePairs>();
+  p->n_can = (long)pairs.size();
+  if ((st = upload(pairs, &p->pairs))) return st;
+  std::lock_guard<std::mutex> lock(g_mutex);
+  auto &slot = cache[key];
+  if (!slot) slot = std::move(p);
+  *out = slot.get();
+  return TPRF_OK;
+}
+
 // Rows 0 and 1 of the inverse of the Vandermonde matrix V[m][j] = m^j (m = 1..8)
 // exactly as TPRF hard-codes them in fit_derivatives
 // (c++/triqs_tprf/fourier/fourier_matsubara.cpp:56-71). They differ from the

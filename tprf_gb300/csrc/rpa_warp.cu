@@ -250,9 +250,74 @@ __global__ void __launch_bounds__(512) rpa_warp_kernel(long n_points, int nb_in,
 // conj(chi0(w, -q)) (a real bubble gives this exactly) makes A(-w, q) the
 // conjugate of A(w, -q), and the elimination (conjugation only flips signs,
 // which every step preserves) gives chi(-w, q) = conj(chi(w, -q)) bit for bit.
-// A group takes a unit (w >= 0, q) with its partner (-w, -q); if the partner's
-// chi0 is that conjugate, bit for bit, it solves once and stores both, else it
-// solves both. Units: the nw x N_k points with w >= 0 (at w = 0 only q <= -q).
+//
+// Transposition partners: with real hoppings, G(tau, -r) = G(tau, r)^T, so the
+// grouped chi0(w, -q) is the transpose of chi0(w, q); with a symmetric grouped
+// U (Kanamori vertices are), chi(w, -q) = chi(w, q)^T as well (push-through:
+// (I - X^T U)^-1 X^T = [X (I - U X)^-1]^T = [(I - X U)^-1 X]^T). The computed
+// chi0 meets the symmetry to rounding only, so the transpose stands in for the
+// direct solve of (w, -q) when the asymmetry d = max |chi0(w, -q) -
+// chi0(w, q)^T| is small against the solve's conditioning estimate k:
+// d k <= kTransposeTol max |chi0(w, q)|; the transposed result then lies within
+// that bound of a direct solve. Otherwise (w, -q) is solved on its own. Never in
+// the FP64 mode, which solves every point as the plain path.
+//
+// A group takes a unit (w >= 0, q) and its partners: (-w, -q) (conjugate) and,
+// for w > 0, q != -q and a symmetric U, also (w, -q) (transpose) and (-w, q)
+// (its conjugate). Units: w = 0 with q <= -q; w > 0 with q <= -q when
+// transposes are allowed, else every q.
+constexpr double kTransposeTol = 1e-12;
+
+// max(|Re(a - b)|, |Im(a - b)|) and max(|Re a|, |Im a|) as floats
+__device__ __forceinline__ float el_diff_max(double2 a, double2 b) {
+  return (float)fmax(fabs(a.x - b.x), fabs(a.y - b.y));
+}
+__device__ __forceinline__ float el_diff_max(cdf a, cdf b) {
+  return fmaxf(fabsf(dsub(a.x, b.x).hi), fabsf(dsub(a.y, b.y).hi));
+}
+__device__ __forceinline__ float el_max_abs(double2 a) { return (float)fmax(fabs(a.x), fabs(a.y)); }
+__device__ __forceinline__ float el_max_abs(cdf a) { return fmaxf(fabsf(a.x.hi), fabsf(a.y.hi)); }
+
+// grouped column index j -> memory offset of that column inside a row
+__device__ __forceinline__ int offset_of_col(int j, int nb) { return (j % nb) * nb + j / nb; }
+
+// B = chi0 of the point at x written to the group's matrix M (as rpa_point_warp
+// would), and whether the point at xc holds its conjugate bit for bit (with
+// U real; only when test)
+template <class E, int G>
+__device__ __forceinline__ bool load_b_conj(const double2 *__restrict__ x, const double2 *__restrict__ xc, bool test,
+                                            bool ureal, E *M, int N, int nb, int lane, unsigned gmask) {
+  bool sym = ureal;
+  for (int o = lane; o < N * N; o += G) {
+    const double2 a = x[o];
+    M[(o / N) * 2 * N + N + col_of_offset(o % N, nb)] = el_from(a, (E *)nullptr);
+    if (test) {
+      const double2 b = xc[o];
+      sym = sym && __double_as_longlong(a.x) == __double_as_longlong(b.x) &&
+            __double_as_longlong(a.y) == __double_as_longlong(-b.y);
+    }
+  }
+  return test && __all_sync(gmask, sym);
+}
+
+// One point solve (B already in M when b_ready) writing chi to ys and, when yc
+// is given, its conjugate to yc; the FP64 re-solve when the conditioning
+// estimate asks for it. Returns the squared estimate, negated when the
+// solution left in M is the FP64 one.
+template <class E, int G, int NBC>
+__device__ __forceinline__ double solve_pair_point(const double2 *xs, double2 *ys, double2 *yc, bool b_ready, E *M,
+                                                   int N, int nb, const SparseU &u, int lane, unsigned gmask,
+                                                   unsigned *status) {
+  bool singular = false;
+  double cond2 = rpa_point_warp<E, G, NBC>(xs, ys, M, N, nb, u, lane, gmask, singular, yc, b_ready);
+  if (IsDf<E>::value && !(cond2 <= kDf64CondLimit2)) {
+    rpa_point_warp<double2, G, NBC>(xs, ys, reinterpret_cast<double2 *>(M), N, nb, u, lane, gmask, singular, yc);
+    cond2 = -cond2;
+  }
+  if (singular && lane == 0) atomicOr(status, kDevErrSingular);
+  return cond2;
+}
+
 template <class E, int G, int NBC = 0>
 __global__ void __launch_bounds__(512) rpa_pair_kernel(int nw, int d0, int d1, int d2, int nb_in,
                                                        const double2 *__restrict__ chi0, const double2 *__restrict__ U,
@@ -263,7 +328,7 @@ __global__ void __launch_bounds__(512) rpa_pair_kernel(int nw, int d0, int d1, i
   double2 *s_val = reinterpret_cast<double2 *>(smem_raw);
   int *s_row = reinterpret_cast<int *>(s_val + N * N);
   int *s_cs = s_row + N * N;
-  __shared__ int s_ureal;
+  __shared__ int s_ureal, s_usym;
   const size_t u_bytes = ((size_t)N * N * (sizeof(double2) + sizeof(int)) + (N + 1) * sizeof(int) + 15) & ~(size_t)15;
   constexpr int GPW = 32 / G;
   const int wl = threadIdx.x & 31, gw = wl / G;
@@ -272,12 +337,16 @@ __global__ void __launch_bounds__(512) rpa_pair_kernel(int nw, int d0, int d1, i
   const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (gw * G));
   E *M = reinterpret_cast<E *>(smem_raw + u_bytes) + (size_t)(active ? grp : 0) * 2 * N * N;
   if (threadIdx.x == 0) {
-    int t = 0, ureal = 1;
+    int t = 0, ureal = 1, usym = 1;
     for (int c = 0; c < N; ++c) {
       s_cs[c] = t;
       for (int m = 0; m < N; ++m) {
-        const double2 v = U[m * N + (c % nb) * nb + c / nb];
+        // grouped U[m][c] at memory offset m * N + offset(c); symmetric: U[m][c] == U[c][m]
+        const double2 v = U[m * N + offset_of_col(c, nb)], vt = U[c * N + offset_of_col(m, nb)];
         if (v.y != 0.0) ureal = 0;
+        if (__double_as_longlong(v.x) != __double_as_longlong(vt.x) ||
+            __double_as_longlong(v.y) != __double_as_longlong(vt.y))
+          usym = 0;
         if (v.x != 0.0 || v.y != 0.0) {
           s_row[t] = m;
           s_val[t] = v;
@@ -287,10 +356,12 @@ __global__ void __launch_bounds__(512) rpa_pair_kernel(int nw, int d0, int d1, i
     }
     s_cs[N] = t;
     s_ureal = ureal;
+    s_usym = usym;
   }
   __syncthreads();
   const SparseU u{s_val, s_row, s_cs};
   const bool ureal = s_ureal != 0;
+  const bool tpairs = s_usym != 0 && IsDf<E>::value;  // transposition partners (never in the FP64 mode)
   if (!active) return;
   const long nk = (long)d0 * d1 * d2, units = (long)(out.mh1 - out.mh0) * nk;
   for (long un = (long)blockIdx.x * n_grp + grp; un < units; un += (long)gridDim.x * n_grp) {
@@ -298,36 +369,75 @@ __global__ void __launch_bounds__(512) rpa_pair_kernel(int nw, int d0, int d1, i
     const long q = un - (long)(mh - out.mh0) * nk;
     const int q2 = (int)(q % d2), q1 = (int)((q / d2) % d1), q0 = (int)(q / ((long)d2 * d1));
     const long mq = ((long)((d0 - q0) % d0) * d1 + (d1 - q1) % d1) * d2 + (d2 - q2) % d2;
-    if (mh == 0 && q > mq) continue;  // its partner (0, -q) holds this unit
-    const long p = (long)(nw - 1 + mh) * nk + q, pm = (long)(nw - 1 - mh) * nk + mq;
-    const double2 *x = chi0 + p * N * N, *xm = chi0 + pm * N * N;
-    // one read of chi0(w, q): the symmetry test against the partner and B of
-    // the first solve (written to the group's matrix as rpa_point_warp would)
-    bool sym = ureal;
-    const bool partner = pm != p;
-    for (int o = lane; o < N * N; o += G) {
-      const double2 a = x[o];
-      M[(o / N) * 2 * N + N + col_of_offset(o % N, nb)] = el_from(a, (E *)nullptr);
-      if (partner) {
-        const double2 b = xm[o];
-        sym = sym && __double_as_longlong(a.x) == __double_as_longlong(b.x) &&
-              __double_as_longlong(a.y) == __double_as_longlong(-b.y);
+    if (q > mq && (mh == 0 || tpairs)) continue;  // a partner's unit holds this point
+    // the unit's points: 0 = (w, q), 1 = (-w, -q) its conjugate, and for a
+    // transposition unit 2 = (w, -q), 3 = (-w, q) its conjugate; each point's
+    // chi0 is read once
+    const long p0 = (long)(nw - 1 + mh) * nk + q, p1 = (long)(nw - 1 - mh) * nk + mq;
+    const bool quad = tpairs && mh > 0 && q < mq;
+    double2 *const row_pos = out.pos + (long)(mh - out.mh0) * out.row;
+    double2 *const row_neg = mh == 0 ? row_pos : out.neg + (long)(mh - out.mh0) * out.neg_step;
+    const bool done1 = p1 == p0;
+    // point 0 into B (with the conjugate test against point 1)
+    const bool sym = load_b_conj<E, G>(chi0 + p0 * N * N, chi0 + p1 * N * N, !done1, ureal, M, N, nb, lane, gmask);
+    __syncwarp(gmask);
+    // a quad: point 2 against the transpose of point 0's B (in the element type;
+    // bit-equal inputs give bit-equal elements), and the conjugate test of point 3
+    float dmax = 0.f, amax = 0.f;
+    bool sym3 = false;
+    if (quad) {
+      const double2 *x2 = chi0 + ((long)(nw - 1 + mh) * nk + mq) * N * N;
+      const double2 *x3 = chi0 + ((long)(nw - 1 - mh) * nk + q) * N * N;
+      bool s3 = ureal;
+      for (int o = lane; o < N * N; o += G) {
+        const int i = o / N, j = col_of_offset(o % N, nb);
+        const double2 b = x2[o], c = x3[o];
+        s3 = s3 && __double_as_longlong(b.x) == __double_as_longlong(c.x) &&
+             __double_as_longlong(b.y) == __double_as_longlong(-c.y);
+        const E a = M[j * 2 * N + N + i];  // chi0(w, q)[j][i]
+        dmax = fmaxf(dmax, el_diff_max(el_from(b, (E *)nullptr), a));
+        amax = fmaxf(amax, el_max_abs(a));
       }
+      sym3 = __all_sync(gmask, s3);
+      dmax = group_max<G>(dmax, gmask);
+      amax = group_max<G>(amax, gmask);
     }
-    if (partner) sym = __all_sync(gmask, sym);
-    double2 *y = out.pos + (long)(mh - out.mh0) * out.row + q * N * N;
-    double2 *ym = (mh == 0 ? out.pos + (long)(mh - out.mh0) * out.row : out.neg + (long)(mh - out.mh0) * out.neg_step) +
-                  mq * N * N;
-    for (int k = 0; k < 2; ++k) {
-      if (k == 1 && (pm == p || sym)) break;
-      const double2 *xs = k ? xm : x;
-      double2 *ys = k ? ym : y;
-      double2 *yc = (k == 0 && sym && pm != p) ? ym : nullptr;
-      bool singular = false;
-      const double cond2 = rpa_point_warp<E, G, NBC>(xs, ys, M, N, nb, u, lane, gmask, singular, yc, k == 0);
-      if (IsDf<E>::value && !(cond2 <= kDf64CondLimit2))
-        rpa_point_warp<double2, G, NBC>(xs, ys, reinterpret_cast<double2 *>(M), N, nb, u, lane, gmask, singular, yc);
-      if (singular && lane == 0) atomicOr(status, kDevErrSingular);
+    const double c2s = solve_pair_point<E, G, NBC>(chi0 + p0 * N * N, row_pos + q * N * N,
+                                                   sym ? row_neg + mq * N * N : nullptr, true, M, N, nb, u, lane,
+                                                   gmask, status);
+    // chi(w, -q) = chi(w, q)^T when chi0(w, -q) is chi0(w, q)^T to within the
+    // solve's conditioning (the transposed solution is read from M)
+    const double cond2 = fabs(c2s);
+    const bool take_t = quad && cond2 < 1e300 &&
+                        (double)dmax * (double)dmax * cond2 <= kTransposeTol * kTransposeTol * (double)amax * (double)amax;
+    if (take_t) {
+      const bool in64 = c2s < 0.0;  // the solution left in M is the FP64 one
+      double2 *y2 = row_pos + mq * N * N, *y3 = row_neg + q * N * N;
+      for (int o = lane; o < N * N; o += G) {
+        const int i = o / N, j = col_of_offset(o % N, nb);
+        const int at = j * 2 * N + N + i;
+        const double2 v = in64 ? reinterpret_cast<const double2 *>(M)[at] : el_to(M[at]);
+        y2[o] = v;
+        if (sym3) y3[o] = make_double2(v.x, -v.y);
+      }
+      __syncwarp(gmask);
+    }
+    if (!sym && !done1)
+      solve_pair_point<E, G, NBC>(chi0 + p1 * N * N, row_neg + mq * N * N, nullptr, false, M, N, nb, u, lane, gmask,
+                                  status);
+    if (quad && !(take_t && sym3)) {
+      // point 3 on its own (transpose taken, no conjugate), or points 2 and 3
+      const long p2 = (long)(nw - 1 + mh) * nk + mq, p3 = (long)(nw - 1 - mh) * nk + q;
+      bool sym2 = false;
+      if (!take_t) {
+        sym2 = load_b_conj<E, G>(chi0 + p2 * N * N, chi0 + p3 * N * N, true, ureal, M, N, nb, lane, gmask);
+        __syncwarp(gmask);
+        solve_pair_point<E, G, NBC>(chi0 + p2 * N * N, row_pos + mq * N * N, sym2 ? row_neg + q * N * N : nullptr,
+                                    true, M, N, nb, u, lane, gmask, status);
+      }
+      if (!sym2)
+        solve_pair_point<E, G, NBC>(chi0 + p3 * N * N, row_neg + q * N * N, nullptr, false, M, N, nb, u, lane, gmask,
+                                    status);
     }
   }
 }
