@@ -328,8 +328,19 @@ def setup_autotune(lib, args):
 
 
 def autotune_info(lib, args):
+    """The autotuner's mode and its choices ("wisdom": kernel/shape key -> value;
+    the *_radix keys name the FFT radix order, see fft_variants)."""
+    import tempfile
+    wisdom = {}
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "wisdom.txt")
+        if lib.tprf_autotune_save(path.encode()) == 0 and os.path.exists(path):
+            for ln in open(path):
+                parts = ln.split()
+                if len(parts) == 2:
+                    wisdom[parts[0].split("/", 1)[-1]] = int(parts[1])
     return {"mode": "fixed heuristics" if args.no_autotune else "measure (tuned during warm-up)",
-            "wisdom_entries": int(lib.tprf_autotune_entries())}
+            "wisdom_entries": int(lib.tprf_autotune_entries()), "wisdom": wisdom}
 
 
 def lattice_passes(dims) -> int:
@@ -539,7 +550,8 @@ def run_gpu(args):
         l1.record(stream)
         torch.cuda.synchronize()
         link_gbs = probe.numel() * 8 / (l0.elapsed_time(l1) * 1e6)
-        del probe
+        del probe, fws, chi0_buf
+        torch.cuda.empty_cache()
         # the bytes that crossed to the host: the frequencies w >= 0 when the host fills
         # chi(-w, q) = conj(chi(w, -q)) (real bubble, real U), else all of chi
         d2h = int(lib.tprf_imtime_bubble_rpa_to_host_last_d2h_bytes())
@@ -598,6 +610,15 @@ def run_gpu(args):
         "clocks": clocks.summary(),
         "autotune": autotune_info(lib, args),
     }
+    if not args.no_batched:
+        # the 512 uneven instances, forward and with gradients, after the buffers
+        # above are released
+        try:
+            del chi0, chi, g_wk, ws  # still held when the e2e leg did not run
+        except NameError:
+            pass
+        torch.cuda.empty_cache()
+        line["batched"] = batched_leg(args, dev, lib, world)
     if rank == 0 and not args.no_cpu_baseline:
         v, cores, wall = cpu_throughput(args.config, 1, scale=40)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
@@ -608,6 +629,110 @@ def run_gpu(args):
         dist.destroy_process_group()
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def batched_leg(args, dev, lib, world, steps=3):
+    """The 512 uneven instances (the batched configuration) inside the default run:
+    forward graph alone and forward + backward graphs per step (gradients of
+    L = sum_i sum |chi_i|^2 with respect to every instance's U, e(k) and t(R)),
+    and the plain single-instance paths over all 512 instances (public API per
+    instance; tprf_gb300.autodiff forward + backward per instance) beside them."""
+    import numpy as np
+    import torch
+
+    import tprf_gb300 as T
+    from tprf_gb300 import workloads
+    from tprf_gb300._native import check
+    from tprf_gb300.autodiff import HoppingModel, chi_rpa
+    from tprf_gb300.batch import BatchedRPAGrad, RPAInstance
+    from tprf_gb300.tight_binding import ek_tensor
+
+    specs = workloads.batched_instances(512, seed=0)
+    insts = [RPAInstance(e_k=ek_tensor(d["hoppings"], d["dims"], device=dev), U=d["U"], dims=d["dims"],
+                         beta=d["beta"], mu=d["mu"], n_max=d["n_max"], nw=d["nw"]) for d in specs]
+    lib.tprf_set_sync_checks(0)
+    t_setup = time.perf_counter()
+    batch = BatchedRPAGrad(insts, n_streams=args.streams, device=dev)
+    setup_s = time.perf_counter() - t_setup
+    points = batch.points
+    stream = torch.cuda.current_stream()
+
+    def timed(fn, n):
+        fn()
+        torch.cuda.synchronize()
+        barrier(world, dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(n):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return max_over_ranks(e0.elapsed_time(e1) / n, world, dev)
+
+    def step():
+        batch.forward()
+        torch.mul(batch.chi_flat, 2.0, out=batch.chi_grad_flat)  # dL/d conj(chi) of sum |chi|^2
+        batch.backward()
+
+    fwd_ms = timed(batch.forward, steps)
+    grad_ms = timed(step, steps)
+    check(lib.tprf_check_device_status(stream.cuda_stream), "batched graphs")
+    batch.close()
+    del batch
+    torch.cuda.empty_cache()
+    # the plain single-instance paths, one instance after the other, every instance
+    lib.tprf_set_sync_checks(1)
+
+    def plain_forward():
+        for a in insts:
+            g0 = T.lattice_dyson_g0_wk(a.mu, T.Gf(mesh=T.MeshBrZone(dims=a.dims), data=a.e_k),
+                                       T.MeshImFreq(a.beta, "Fermion", a.n_max))
+            T.solve_rpa_PH(T.imtime_bubble_chi0_wk(g0, nw=a.nw, verbose=False), a.U)
+
+    models = []
+    for d in specs:
+        nb = d["nb"]
+        models.append(HoppingModel(base=d["hoppings"], patterns=[{(1, 0): np.eye(nb), (-1, 0): np.eye(nb)}],
+                                   dims=d["dims"], beta=d["beta"], mu=d["mu"], n_max=d["n_max"], nw=d["nw"]))
+    Us = [torch.as_tensor(d["U"], dtype=torch.complex128, device=dev) for d in specs]
+    theta0 = torch.zeros(1, dtype=torch.float64, device=dev)
+
+    def plain_grad():
+        for m, U in zip(models, Us):
+            th = theta0.clone().requires_grad_(True)
+            u = U.clone().requires_grad_(True)
+            (chi_rpa(th, u, m).abs() ** 2).sum().backward()
+
+    def wall(fn):
+        fn()  # plans
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        fn()
+        torch.cuda.synchronize()
+        return max_over_ranks(time.perf_counter() - t0, world, dev)
+
+    plain_fwd_s = wall(plain_forward)
+    plain_grad_s = wall(plain_grad)
+    lib.tprf_set_sync_checks(0)
+    nb_counts = {nb: sum(1 for a in insts if a.nb == nb) for nb in (1, 2)}
+    fwd_v, grad_v = world * points / (fwd_ms / 1e3), world * points / (grad_ms / 1e3)
+    pf_v, pg_v = world * points / plain_fwd_s, world * points / plain_grad_s
+    return {
+        "workload": "batched_512_square_lattice_instances", "instances": len(insts), "nb_counts": nb_counts,
+        "k_meshes": "{8,16,24,32,48}^2", "beta": "U[5,40]", "n_max": "7-smooth nearest 12.8 beta in [32,512]",
+        "points_per_step": points, "unit": UNIT, "steps": steps, "streams": args.streams,
+        "launch": "forward graph (+ backward graph) per step", "graph_setup_s": round(setup_s, 2),
+        "forward": {"value": fwd_v, "ms_per_step": fwd_ms},
+        "forward_plus_gradient": {"value": grad_v, "ms_per_step": grad_ms, "loss": "sum_i sum |chi_i|^2",
+                                  "gradients": "dL/dU, dL/de(k), dL/dt(R) of every instance"},
+        "plain_single_instance": {
+            "instances_timed": len(insts),
+            "forward": {"value": pf_v, "s_per_pass": plain_fwd_s,
+                        "path": "lattice_dyson_g0_wk -> imtime_bubble_chi0_wk -> solve_rpa_PH per instance"},
+            "forward_plus_gradient": {"value": pg_v, "s_per_pass": plain_grad_s,
+                                      "path": "tprf_gb300.autodiff.chi_rpa forward + backward per instance"}},
+        "speedup_vs_plain_single_instance": {"forward": fwd_v / pf_v, "forward_plus_gradient": grad_v / pg_v},
+    }
 
 
 def run_gpu_batched(args):
@@ -959,6 +1084,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the FP64 comparison step (profiling runs)")
+    ap.add_argument("--no-batched", action="store_true", help="skip the 512-instance batched leg of the default run")
     ap.add_argument("--streams", type=int, default=32, help="concurrent streams of the batched graph (cfg2)")
     ap.add_argument("--grad", action="store_true", help="cfg2: forward + gradient graphs per step")
     ap.add_argument("--no-autotune", action="store_true", help="fixed launch-shape heuristics instead of measure mode")

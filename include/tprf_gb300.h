@@ -172,10 +172,13 @@ int tprf_fourier_wr_to_wk(long n_w, const int dims[3], long n_target,
  * belongs to their own pool allocator, hosts with a fixed device-memory
  * budget). No counterpart in the reference: it is an addition of this library.
  * Its FFT tables live in a static 1 MiB device array inside the library
- * image, 36 bytes per point of each distinct mesh length (about 29 000
- * points); larger requests return TPRF_ERR_INVALID_ARGUMENT. The first call
- * on a device looks up that array's address, so make it before any stream
- * capture. Calls share the array: calls overlapping on the GPU race. */
+ * image, 36 bytes per point of each distinct mesh length: tables beyond it
+ * return TPRF_ERR_INVALID_ARGUMENT. A mesh length above 12 799 points (6 399
+ * with a prime factor above 8) does not fit one CTA's shared memory and returns
+ * TPRF_ERR_UNSUPPORTED_SIZE. Both checks come before any work is queued. The
+ * first call on a device may load the library's device code there, so make it
+ * before any stream capture. Calls share the array: calls overlapping on the
+ * GPU race. */
 int tprf_fourier_lattice_noalloc(int forward, long n_w, const int dims[3], long n_target,
                                  const double *in, double *out, void *stream);
 
@@ -424,6 +427,13 @@ int tprf_chi_wr_from_chi_tr_adjoint(double beta, int n_tau, int nw, long n_r, lo
                                     const double *chi_wr_grad, double *chi_tr_grad, void *stream);
 int tprf_chi0_tr_from_grt_PH_adjoint(int n_tau, const int dims[3], int nb, const double *g_tr,
                                      const double *chi0_tr_grad, double *g_tr_grad, void *stream);
+/* Transpose of tprf_chi0_wr_from_grt_PH (the bubble fused with tau -> i omega):
+ * g_tr_grad [n_tau, N_r, nb, nb] from chi0_wr_grad [2 nw - 1, N_r, nb^4]. Each
+ * bubble column's tau -> i omega transpose stays in shared memory and adds its
+ * two product-rule terms to g_tr_grad, so chi0_grad(tau, r) is never stored
+ * (the order of the additions, by atomics, varies at rounding level). */
+int tprf_chi0_wr_from_grt_PH_adjoint(double beta, int n_tau, int nw, const int dims[3], int nb, const double *g_tr,
+                                     const double *chi0_wr_grad, double *g_tr_grad, void *stream);
 int tprf_fourier_wr_to_tr_adjoint(double beta, int n_iw, int n_tau, long n_r, long n_target,
                                   const double *g_tr_grad, int fitted, double *g_wr_grad, void *stream);
 int tprf_lattice_dyson_g_wk_adjoint(int n_iw, long n_k, int nb, const double *g_wk, const double *g_wk_grad,

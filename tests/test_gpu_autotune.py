@@ -168,3 +168,45 @@ def test_tma_plane_wait_that_runs_out_is_reported(cuda_lib, tmp_path):
     finally:
         lib.tprf_set_device_wait_limit_ns(200_000_000)
         tuning.clear_wisdom()
+
+
+def test_every_fft_radix_order_gives_the_same_chain(cuda_lib, tmp_path):
+    """The radix orders the autotuner chooses among for the Matsubara transforms
+    (forced one after the other through wisdom files rewritten from a measure-mode
+    run) give the same chi0, against the oracle. L = 3072 = 2^10 3 has four
+    distinct orders: 8 8 8 2 3, 4 4 4 4 4 3, 3 8 8 8 2, 2 8 8 8 3."""
+    import oracle as O
+    import tprf_gb300 as T
+    from conftest import PARITY_RTOL
+    from tprf_gb300 import tuning
+    dims, beta, n_max, nw = (4, 4, 1), 30.0, 512, 24
+    hop = {(1, 0): np.array([[-1.0, 0.3], [0.3, -0.7]]), (0, 1): np.array([[-0.8, 0.1], [0.1, -1.0]])}
+    hop.update({(-R[0], -R[1]): t.T for R, t in list(hop.items())})
+    ek = O.ek_from_hoppings(hop, dims)
+    ref = O.imtime_bubble_chi0_wk(O.lattice_dyson_g0_wk(0.0, ek, beta, n_max), beta, dims, nw=nw)
+    g0 = T.lattice_dyson_g0_wk(0.0, T.Gf(mesh=T.MeshBrZone(dims=dims), data=ek), T.MeshImFreq(beta, "Fermion", n_max))
+    try:
+        tuning.clear_wisdom()
+        tuning.set_autotune(True)
+        T.imtime_bubble_chi0_wk(g0, nw=nw, verbose=False)
+        tuning.set_autotune(False)
+        path = tmp_path / "measured.txt"
+        tuning.save_wisdom(path)
+        lines = path.read_text().splitlines()
+        assert any("/tau_to_w_radix/" in ln for ln in lines) and any("/nu_to_tau_radix/" in ln for ln in lines)
+        outs = []
+        for v in range(4):
+            forced = [ln.split()[0] + f" {v}" if "_radix/" in ln else ln for ln in lines]
+            w = tmp_path / f"radix{v}.txt"
+            w.write_text("\n".join(forced) + "\n")
+            tuning.clear_wisdom()
+            tuning.load_wisdom(w)
+            chi0 = T.imtime_bubble_chi0_wk(g0, nw=nw, verbose=False).data
+            torch.cuda.synchronize()
+            assert rel_err(chi0, ref) < PARITY_RTOL, v
+            outs.append(chi0.clone())
+        for v in range(1, 4):
+            assert rel_err(outs[v], outs[0]) < 1e-13, v
+    finally:
+        tuning.set_autotune(False)
+        tuning.clear_wisdom()

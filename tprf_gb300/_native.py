@@ -91,6 +91,8 @@ SIGNATURES = {
     "tprf_chi_wr_from_chi_tr_adjoint": (c_int, [c_double, c_int, c_int, c_long, c_long, c_void_p, c_void_p,
                                                 c_void_p]),
     "tprf_chi0_tr_from_grt_PH_adjoint": (c_int, [c_int, c_int3, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "tprf_chi0_wr_from_grt_PH_adjoint": (c_int, [c_double, c_int, c_int, c_int3, c_int, c_void_p, c_void_p, c_void_p,
+                                                 c_void_p]),
     "tprf_fourier_wr_to_tr_adjoint": (c_int, [c_double, c_int, c_int, c_long, c_long, c_void_p, c_int, c_void_p,
                                               c_void_p]),
     "tprf_lattice_dyson_g_wk_adjoint": (c_int, [c_int, c_long, c_int, c_void_p, c_void_p, c_void_p, c_void_p]),

@@ -104,16 +104,13 @@ class ChiRPA(torch.autograd.Function):
         chi0wr_grad = torch.empty_like(chi0_grad)
         check(lib.tprf_fourier_wk_to_wr(nwt, d3, nb4, chi0_grad.data_ptr(), chi0wr_grad.data_ptr(), _s()))
         chi0wr_grad.mul_(float(nk))
-        # tau -> iw, then the bubble (G recomputed: the forward pass does not keep it)
-        chi0tr_grad = torch.empty(n_tau, nk, nb4, dtype=torch.complex128, device=e_k.device)
-        check(lib.tprf_chi_wr_from_chi_tr_adjoint(m.beta, n_tau, m.nw, nk, nb4, chi0wr_grad.data_ptr(),
-                                                  chi0tr_grad.data_ptr(), _s()))
-        del chi0wr_grad
+        # the bubble fused with tau -> iw, transposed (G recomputed: the forward pass
+        # does not keep it); chi0_grad(tau, r) never exists in device memory
         g_wk, g_tr, _ = _forward_intermediates_g(e_k, m)
         g_tr_grad = torch.empty_like(g_tr)
-        check(lib.tprf_chi0_tr_from_grt_PH_adjoint(n_tau, d3, nb, g_tr.data_ptr(), chi0tr_grad.data_ptr(),
-                                                   g_tr_grad.data_ptr(), _s()))
-        del chi0tr_grad
+        check(lib.tprf_chi0_wr_from_grt_PH_adjoint(m.beta, n_tau, m.nw, d3, nb, g_tr.data_ptr(),
+                                                   chi0wr_grad.data_ptr(), g_tr_grad.data_ptr(), _s()))
+        del chi0wr_grad
         # iv -> tau with the fitted tail, k -> r (1/N_k FFTW_FORWARD): transpose = FFTW_BACKWARD / N_k
         g_wr_grad = torch.empty_like(g_wk)
         check(lib.tprf_fourier_wr_to_tr_adjoint(m.beta, m.n_max, n_tau, nk, nb2, g_tr_grad.data_ptr(), 1,

@@ -58,13 +58,12 @@ size_t al16(size_t n) { return (n * sizeof(double2) + 255) & ~size_t(255); }
 // The forward pass uses the first five (chi0 only when the caller does not keep
 // it); the backward pass reuses them for the gradients of the same shapes.
 struct Layout {
-  size_t g, gt, c, ct;
+  size_t g, gt, c;
   Layout(const tprf_instance &a) {
     const size_t nk = inst_nk(a), nb2 = (size_t)a.nb * a.nb, nb4 = nb2 * nb2;
     g = 2ull * a.n_iw * nk * nb2;
     gt = (size_t)inst_ntau(a) * nk * nb2;
     c = (size_t)(2 * a.nw - 1) * nk * nb4;
-    ct = (size_t)inst_ntau(a) * nk * nb4;
   }
   // 256 bytes first: the max |G|, max |Im G| words of the real-pair test
   static constexpr size_t kHdr = 256;
@@ -73,9 +72,9 @@ struct Layout {
   size_t off_gtr() const { return kHdr + 2 * al16(g); }
   size_t off_gdf() const { return kHdr + 2 * al16(g) + al16(gt); }
   size_t off_c() const { return kHdr + 2 * al16(g) + 2 * al16(gt); }
-  size_t off_ct() const { return off_c() + al16(c); }
+  size_t off_gk() const { return off_c() + al16(c); }  // backward: G_grad(iv, k)
   size_t forward_bytes() const { return off_c() + al16(c); }
-  size_t grad_bytes() const { return off_ct() + al16(ct); }
+  size_t grad_bytes() const { return off_gk() + al16(g); }
 };
 
 // Relative cost used to balance the streams: FFT work plus the RPA solves.
@@ -192,9 +191,9 @@ int enqueue_backward(const tprf_grad_instance &gi, unsigned char *scratch, cudaS
   auto at = [&](size_t off) { return reinterpret_cast<double2 *>(scratch + off); };
   double2 *g_wk = at(L.off_gwk()), *g_wr = at(L.off_gwr()), *g_tr = at(L.off_gtr());
   double2 *g_tr_grad = at(L.off_gdf());  // the double-float slot is not needed here
-  double2 *chi0_grad = at(L.off_c()), *chi0tr_grad = at(L.off_ct());
-  double2 *g_wr_grad = g_wr;        // G(iv, r) is dead once G(tau, r) is recomputed
-  double2 *g_wk_grad = chi0tr_grad;  // n_tau nb^4 >= 2 n_iw nb^2
+  double2 *chi0_grad = at(L.off_c());
+  double2 *g_wr_grad = g_wr;  // G(iv, r) is dead once G(tau, r) is recomputed
+  double2 *g_wk_grad = at(L.off_gk());
   double2 *e_grad = gi.e_grad ? reinterpret_cast<double2 *>(gi.e_grad) : chi0_grad;
   double2 *U_grad = reinterpret_cast<double2 *>(gi.U_grad);
   auto cd = [](const double *p) { return reinterpret_cast<const double2 *>(p); };
@@ -203,11 +202,11 @@ int enqueue_backward(const tprf_grad_instance &gi, unsigned char *scratch, cudaS
                                    U_grad, s, status);
   if (st) return st;
   if ((st = launch_lattice_fft_scaled(true, nwt, a.dims, nb4, chi0_grad, chi0_grad, 1.0, s))) return st;
-  if ((st = launch_tau_to_w_adjoint(a.beta, nt, a.nw, nk * nb4, chi0_grad, chi0tr_grad, s))) return st;
   if ((st = launch_dyson(a.beta, a.n_iw, nk, a.nb, a.mu, cd(a.e_k), nullptr, 0, g_wk, s))) return st;
   if ((st = launch_lattice_fft(true, 2L * a.n_iw, a.dims, nb2, g_wk, g_wr, s))) return st;
   if ((st = launch_nu_to_tau(a.beta, a.n_iw, nt, nk * nb2, g_wr, nullptr, g_tr, s))) return st;
-  if ((st = launch_bubble_adjoint(nt, a.dims, a.nb, g_tr, chi0tr_grad, g_tr_grad, s))) return st;
+  // tau -> iw and the bubble transposed together: chi0_grad(tau, r) is never stored
+  if ((st = launch_chi0_wr_from_grt_adjoint(a.beta, nt, a.nw, a.dims, a.nb, g_tr, chi0_grad, g_tr_grad, s))) return st;
   if ((st = launch_nu_to_tau_adjoint(a.beta, a.n_iw, nt, nk * nb2, g_tr_grad, g_wr_grad, true, s))) return st;
   if ((st = launch_lattice_fft_scaled(false, 2L * a.n_iw, a.dims, nb2, g_wr_grad, g_wk_grad, 1.0 / (double)nk, s)))
     return st;

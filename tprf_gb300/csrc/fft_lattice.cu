@@ -742,10 +742,14 @@ extern "C" int tprf_fourier_wr_to_wk(long n_w, const int dims[3], long n_target,
 //  * kNoAllocScratchBytes bounds the tables: each distinct mesh length n
 //    takes 36 n bytes (plus 256-byte alignment); a transform needing more is
 //    refused with TPRF_ERR_INVALID_ARGUMENT before any work is queued.
+//  * One CTA transforms whole columns of one mesh axis in shared memory: a
+//    mesh length above 12 799 points (6 399 when it has a prime factor above 8)
+//    is refused with TPRF_ERR_UNSUPPORTED_SIZE, also before any work.
 //  * Every GPU that loads the library holds the array until the process exits.
-//  * The first call on a device looks up the array's device address
-//    (cudaGetSymbolAddress) with that device current; make that first call
-//    before any stream capture.
+//  * Every call looks up the array's device address (cudaGetSymbolAddress,
+//    which allocates nothing) on the current device, so a device reset cannot
+//    leave a stale address behind; the first call on a device may load the
+//    library's device code there, so make it before any stream capture.
 //  * Every call rebuilds the tables it needs at the start of the array, in
 //    stream order before its transform, so nothing from an earlier call is
 //    read. Calls that overlap on the GPU (different streams at the same time)
@@ -757,21 +761,13 @@ namespace {
 constexpr size_t kNoAllocScratchBytes = 1u << 20;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
-std::mutex g_noalloc_mutex;
-std::map<int, unsigned char *> g_noalloc_addr;  // device -> device address of g_noalloc_scratch
-
+// The device address of g_noalloc_scratch on the current device. In host code
+// the array's name is only a host-side stand-in; kernels get this address.
 int noalloc_scratch_address(unsigned char **out) {
-  int dev = 0;
-  TPRF_CUDA(cudaGetDevice(&dev));
-  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-  auto it = g_noalloc_addr.find(dev);
-  if (it == g_noalloc_addr.end()) {
-    void *ptr = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
-    if (e != cudaSuccess) return cuda_status(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
-    it = g_noalloc_addr.emplace(dev, static_cast<unsigned char *>(ptr)).first;
-  }
-  *out = it->second;
+  void *ptr = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+  if (e != cudaSuccess) return cuda_status(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+  *out = static_cast<unsigned char *>(ptr);
   return TPRF_OK;
 }
 

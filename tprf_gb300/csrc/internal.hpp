@@ -59,6 +59,12 @@ struct FftDesc {
 };
 // Returns 0 or a status; fills *out. Cached per (device, n).
 int get_fft(int n, FftDesc *out);
+// The same factors of n in radix order `variant` (0 = get_fft's; see
+// factorize_variant in plans.cu); fft_variants(n): the variants giving distinct
+// stage sequences for n (the autotuner's candidates).
+constexpr int kFftVariants = 4;
+int get_fft_variant(int n, int variant, FftDesc *out);
+std::vector<int> fft_variants(int n);
 
 // Matsubara -> tau tables for one (beta, n, n_tau, statistic). Fermion: n = n_max,
 // inputs iv_n for n = -n_max .. n_max-1; boson: n = nw, inputs iw_m for
@@ -228,6 +234,10 @@ int launch_tau_to_w_adjoint(double beta, int n_tau, int nw, long C, const double
                             cudaStream_t stream);
 int launch_nu_to_tau_adjoint(double beta, int n_iw, int n_tau, long C, const double2 *yg, double2 *gg, bool fitted,
                              cudaStream_t stream);
+// The fused bubble + tau -> w (launch_chi0_wr_from_grt_df) transposed: gg = G_grad(tau, r)
+// [n_tau][N_r][nb^2] from yg = chi0_grad(w, r) [2nw-1][N_r][nb^4]; chi0_grad(tau, r) is never stored.
+int launch_chi0_wr_from_grt_adjoint(double beta, int n_tau, int nw, const int dims[3], int nb, const double2 *g_tr,
+                                    const double2 *yg, double2 *gg, cudaStream_t stream);
 int launch_bubble_adjoint(int n_tau, const int dims[3], int nb, const double2 *g_tr, const double2 *chig,
                           double2 *gg, cudaStream_t stream);
 int launch_dyson_adjoint(int n_iw, long n_k, int nb, const double2 *g, const double2 *gg, double2 *e_grad,

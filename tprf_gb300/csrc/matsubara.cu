@@ -805,15 +805,18 @@ int launch_tau_to_w_as(const TauWPlan *p, Loader ld, double2 *out, long C, cudaS
   if (p->fermion && !std::is_same<Loader, ArrayLoader>::value)
     return set_error(TPRF_ERR_INVALID_ARGUMENT, "tau -> w: fermionic transform of a bubble");
   const FitRows fr = make_fit_rows(p->beta, p->n_tau);
-  // columns [0, n_cols) of the C columns with icv columns per CTA
-  auto launch = [&](int icv, long n_cols) -> int {
-    const size_t sm = ic_smem(p->fft, extra, icv);
+  int radix = 0;  // radix order of the FFT (fft_variants), chosen after the columns per CTA
+  // columns [0, n_cols) of the C columns with icv columns per CTA and radix order rv
+  auto launch_rv = [&](int icv, long n_cols, int rv) -> int {
+    TauWPlan pv = *p;
+    if (rv != 0 && (st = get_fft_variant(p->L, rv, &pv.fft))) return st;
+    const size_t sm = ic_smem(pv.fft, extra, icv);
     const long blocks = (n_cols + icv - 1) / icv;
     if constexpr (std::is_same<Loader, ArrayLoader>::value) {
       if (p->fermion) {
         TPRF_CUDA(cudaFuncSetAttribute(tau_to_w_kernel<Loader, E, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)sm));
-        tau_to_w_kernel<Loader, E, true><<<(unsigned)blocks, kMatsubaraThreads, sm, stream>>>(*p, ld, fr, out, C, icv,
+        tau_to_w_kernel<Loader, E, true><<<(unsigned)blocks, kMatsubaraThreads, sm, stream>>>(pv, ld, fr, out, C, icv,
                                                                                               log2_ic(icv), out_df, skip_neg);
         TPRF_LAUNCH_CHECK("tau_to_w_kernel");
         return TPRF_OK;
@@ -821,16 +824,25 @@ int launch_tau_to_w_as(const TauWPlan *p, Loader ld, double2 *out, long C, cudaS
     }
     TPRF_CUDA(cudaFuncSetAttribute(tau_to_w_kernel<Loader, E, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)sm));
-    tau_to_w_kernel<Loader, E, false><<<(unsigned)blocks, kMatsubaraThreads, sm, stream>>>(*p, ld, fr, out, C, icv,
+    tau_to_w_kernel<Loader, E, false><<<(unsigned)blocks, kMatsubaraThreads, sm, stream>>>(pv, ld, fr, out, C, icv,
                                                                                            log2_ic(icv), out_df, skip_neg);
     TPRF_LAUNCH_CHECK("tau_to_w_kernel");
     return TPRF_OK;
   };
+  auto launch = [&](int icv, long n_cols) -> int { return launch_rv(icv, n_cols, radix); };
   const long Ct = tune_columns(C);
-  if (!aliases(ld, out) &&
-      (st = tune_pick(tune_key("tau_to_w", {p->L, p->nw, p->fermion, tune_tag(ld), out_df}), ic_candidates(p->fft, extra),
-                      ic, stream, [&](int v) { return launch(v, Ct); }, &ic)))
+  const std::vector<int> radix_cands = fft_variants(p->L);
+  const std::string rkey = tune_key("tau_to_w_radix", {p->L, p->nw, p->fermion, tune_tag(ld), out_df});
+  if (!aliases(ld, out)) {
+    if ((st = tune_pick(tune_key("tau_to_w", {p->L, p->nw, p->fermion, tune_tag(ld), out_df}),
+                        ic_candidates(p->fft, extra), ic, stream, [&](int v) { return launch(v, Ct); }, &ic)))
+      return st;
+    if (radix_cands.size() > 1 &&
+        (st = tune_pick(rkey, radix_cands, 0, stream, [&](int v) { return launch_rv(ic, Ct, v); }, &radix)))
+      return st;
+  } else if ((st = tune_lookup(rkey, radix_cands, 0, &radix))) {
     return st;
+  }
   return launch(ic, C);
 }
 
@@ -913,9 +925,18 @@ __device__ __forceinline__ void column_sum3(double2 v[3], double2 *red, int ic) 
 // gradient y to: (beta/L) FFT_FORWARD(y placed at rows k_m)[t] for t < L, plus
 // the moment terms D^T C^T (K^H y) on the end samples. K^H y is summed by all
 // threads of the CTA while y is placed.
-template <class C>
+//
+// FUSED: the columns are the bubble's (r, abcd) and, instead of storing
+// chi0_grad(tau, r), each column adds its two bubble-adjoint terms to
+// G_grad(tau, r) (zeroed by the caller) with FP64 atomics:
+//   G_grad_da(tau_t, r)           += conj(G_bc(tau_{N-1-t}, -r)) chi0_grad_abcd(tau_t, r),
+//   G_grad_bc(tau_{N-1-t}, -r)    += conj(G_da(tau_t, r))        chi0_grad_abcd(tau_t, r),
+// the transpose of chi0_abcd(tau_t, r) = G_da(tau_t, r) G_bc(tau_{N-1-t}, -r), so
+// chi0_grad(tau, r) never exists in device memory.
+template <class C, bool FUSED = false>
 __global__ void __launch_bounds__(256) tau_to_w_adjoint_kernel(TauWPlan p, VinvRows vr, const double2 *__restrict__ yg,
-                                                               double2 *__restrict__ xg, long Ccols, int ic, int lg) {
+                                                               double2 *__restrict__ xg, long Ccols, int ic, int lg,
+                                                               BubbleLoader ld) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C *a = reinterpret_cast<C *>(smem_raw);
   const int L = p.L, nw = p.nw, nwt = 2 * p.nw - 1;
@@ -923,9 +944,11 @@ __global__ void __launch_bounds__(256) tau_to_w_adjoint_kernel(TauWPlan p, VinvR
   C *b = p.fft.has_generic ? a + (size_t)L * ic : nullptr;
   double2 *ends = reinterpret_cast<double2 *>(a + (size_t)(p.fft.has_generic ? 2 : 1) * L * ic);  // [18][ic]
   double2 *red = ends + 18 * ic;                                      // [8][3][ic]
+  long *soff = reinterpret_cast<long *>(red + 24 * ic);               // FUSED: [2][ic] G offsets of the columns
   const int tid = threadIdx.x, nthr = blockDim.x;
   const long col0 = blockIdx.x * (long)ic;
   const int ncol = (int)min((long)ic, Ccols - col0);
+  if constexpr (FUSED) ld.setup(col0, ic, ncol, soff);  // ordered before use by the barriers below
   for (int w = tid; w < L * ic; w += nthr) a[w] = from_d2<C>(make_double2(0.0, 0.0));
   __syncthreads();
   double2 v[3] = {make_double2(0.0, 0.0), make_double2(0.0, 0.0), make_double2(0.0, 0.0)};
@@ -977,7 +1000,20 @@ __global__ void __launch_bounds__(256) tau_to_w_adjoint_kernel(TauWPlan p, VinvR
     double2 v = (t < L) ? cscale(as_d2(r[t * ic + c]), fact) : make_double2(0.0, 0.0);
     if (t <= 8) v = cadd(v, ends[t * ic + c]);
     if (t >= L - 8) v = cadd(v, ends[(9 + t - (L - 8)) * ic + c]);
-    xg[(long)t * Ccols + col0 + c] = v;
+    if constexpr (FUSED) {
+      const long slice = ld.Nr * ld.nb * ld.nb, ox = soff[c], oy = soff[ic + c];
+      const long tm = (long)ld.n_tau - 1 - t;
+      const double2 t1 = cmul(cconj(ld.g[tm * slice + oy]), v);       // into G_grad_da(tau_t, r)
+      const double2 t2 = cmul(cconj(ld.g[(long)t * slice + ox]), v);  // into G_grad_bc(tau_{N-1-t}, -r)
+      double *g1 = reinterpret_cast<double *>(xg + (long)t * slice + ox);
+      double *g2 = reinterpret_cast<double *>(xg + tm * slice + oy);
+      atomicAdd(g1, t1.x);
+      atomicAdd(g1 + 1, t1.y);
+      atomicAdd(g2, t2.x);
+      atomicAdd(g2 + 1, t2.y);
+    } else {
+      xg[(long)t * Ccols + col0 + c] = v;
+    }
   }
 }
 
@@ -1186,17 +1222,20 @@ int launch_nu_to_tau_stat(double beta, int n_iw, int n_tau, bool fermion, long C
   st = pick_ic(p->fft, extra, &ic, &lg, &smem);
   if (st) return st;
   const bool fp64 = arith_mode() == kArithFP64;
-  auto launch = [&](int icv, long n_cols) -> int {  // columns [0, n_cols), icv per CTA
-    const size_t sm = ic_smem(p->fft, extra, icv);
+  int radix = 0;  // radix order of the FFT (fft_variants), chosen after the columns per CTA
+  auto launch_rv = [&](int icv, long n_cols, int rv) -> int {  // columns [0, n_cols), icv per CTA, radix order rv
+    NuTauPlan pv = *p;
+    if (rv != 0 && (st = get_fft_variant(p->L, rv, &pv.fft))) return st;
+    const size_t sm = ic_smem(pv.fft, extra, icv);
     const long blocks = (n_cols + icv - 1) / icv;
     if (fp64) {
       TPRF_CUDA(cudaFuncSetAttribute(nu_to_tau_kernel<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-      nu_to_tau_kernel<double2><<<(unsigned)blocks, kMatsubaraThreads, sm, stream>>>(*p, gw, mom, gt, C, icv,
+      nu_to_tau_kernel<double2><<<(unsigned)blocks, kMatsubaraThreads, sm, stream>>>(pv, gw, mom, gt, C, icv,
                                                                                       log2_ic(icv), status, nullptr,
                                                                                       gmax, nullptr, 0, nullptr, 0L);
     } else {
       TPRF_CUDA(cudaFuncSetAttribute(nu_to_tau_kernel<cdf>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-      nu_to_tau_kernel<cdf><<<(unsigned)blocks, kMatsubaraThreads, sm, stream>>>(*p, gw, mom, gt, C, icv, log2_ic(icv),
+      nu_to_tau_kernel<cdf><<<(unsigned)blocks, kMatsubaraThreads, sm, stream>>>(pv, gw, mom, gt, C, icv, log2_ic(icv),
                                                                                   status, gt_df, gmax, hwords,
                                                                                   fit_rows_only ? 1 : 0,
                                                                                   tp ? tp->pairs : nullptr,
@@ -1205,11 +1244,20 @@ int launch_nu_to_tau_stat(double beta, int n_iw, int n_tau, bool fermion, long C
     TPRF_LAUNCH_CHECK("nu_to_tau_kernel");
     return TPRF_OK;
   };
+  auto launch = [&](int icv, long n_cols) -> int { return launch_rv(icv, n_cols, radix); };
   const long Ct = tune_columns(C);
-  if ((const void *)gw != (const void *)gt &&
-      (st = tune_pick(tune_key("nu_to_tau", {p->L, p->n_iw, p->fermion, mom != nullptr, gt_df != nullptr}),
-                      ic_candidates(p->fft, extra), ic, stream, [&](int v) { return launch(v, Ct); }, &ic)))
+  const std::vector<int> radix_cands = fft_variants(p->L);
+  const std::string rkey = tune_key("nu_to_tau_radix", {p->L, p->n_iw, p->fermion, mom != nullptr, gt_df != nullptr});
+  if ((const void *)gw != (const void *)gt) {
+    if ((st = tune_pick(tune_key("nu_to_tau", {p->L, p->n_iw, p->fermion, mom != nullptr, gt_df != nullptr}),
+                        ic_candidates(p->fft, extra), ic, stream, [&](int v) { return launch(v, Ct); }, &ic)))
+      return st;
+    if (radix_cands.size() > 1 &&
+        (st = tune_pick(rkey, radix_cands, 0, stream, [&](int v) { return launch_rv(ic, Ct, v); }, &radix)))
+      return st;
+  } else if ((st = tune_lookup(rkey, radix_cands, 0, &radix))) {
     return st;
+  }
   return launch(ic, C);
 }
 
@@ -1403,8 +1451,32 @@ int launch_tau_to_w_adjoint(double beta, int n_tau, int nw, long C, const double
   // double-float butterflies unless the FP64 arithmetic mode is set
   auto kern = arith_mode() == kArithFP64 ? tau_to_w_adjoint_kernel<double2> : tau_to_w_adjoint_kernel<cdf>;
   TPRF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  kern<<<(unsigned)((C + ic - 1) / ic), 256, smem, stream>>>(*p, make_vinv_rows(), yg, xg, C, ic, lg);
+  kern<<<(unsigned)((C + ic - 1) / ic), 256, smem, stream>>>(*p, make_vinv_rows(), yg, xg, C, ic, lg, BubbleLoader{});
   TPRF_LAUNCH_CHECK("tau_to_w_adjoint_kernel");
+  return TPRF_OK;
+}
+
+// The fused bubble + tau -> w transposed: G_grad(tau, r) from chi0_grad(w, r)
+// (FUSED tau_to_w_adjoint_kernel), chi0_grad(tau, r) never stored.
+int launch_chi0_wr_from_grt_adjoint(double beta, int n_tau, int nw, const int dims[3], int nb, const double2 *g_tr,
+                                    const double2 *yg, double2 *gg, cudaStream_t stream) {
+  int st = check_tau_w(beta, n_tau, nw);
+  if (st) return st;
+  if ((st = check_bubble(n_tau, dims, nb, g_tr, gg))) return st;
+  if ((st = bubble_columns(dims, nb))) return st;
+  if (!yg) return set_error(TPRF_ERR_INVALID_ARGUMENT, "bubble adjoint: null gradient");
+  const TauWPlan *p = nullptr;
+  if ((st = get_tau_w_plan(beta, n_tau, nw, &p))) return st;
+  const BubbleLoader ld = make_bubble(g_tr, n_tau, dims, nb);
+  const long C = ld.Nr * nb * nb * nb * nb;
+  TPRF_CUDA(cudaMemsetAsync(gg, 0, (size_t)n_tau * ld.Nr * nb * nb * sizeof(double2), stream));
+  int ic, lg;
+  size_t smem;
+  if ((st = pick_ic(p->fft, (18 + 24 + 1) * sizeof(double2), &ic, &lg, &smem))) return st;
+  auto kern = arith_mode() == kArithFP64 ? tau_to_w_adjoint_kernel<double2, true> : tau_to_w_adjoint_kernel<cdf, true>;
+  TPRF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  kern<<<(unsigned)((C + ic - 1) / ic), 256, smem, stream>>>(*p, make_vinv_rows(), yg, gg, C, ic, lg, ld);
+  TPRF_LAUNCH_CHECK("tau_to_w_adjoint_kernel<fused bubble>");
   return TPRF_OK;
 }
 
@@ -1455,6 +1527,14 @@ extern "C" int tprf_fourier_wr_to_tr_adjoint(double beta, int n_iw, int n_tau, l
   return launch_nu_to_tau_adjoint(beta, n_iw, n_tau, n_r * n_target, reinterpret_cast<const double2 *>(g_tr_grad),
                                   reinterpret_cast<double2 *>(g_wr_grad), fitted != 0,
                                   static_cast<cudaStream_t>(stream));
+}
+
+extern "C" int tprf_chi0_wr_from_grt_PH_adjoint(double beta, int n_tau, int nw, const int dims[3], int nb,
+                                                const double *g_tr, const double *chi0_wr_grad, double *g_tr_grad,
+                                                void *stream) {
+  return launch_chi0_wr_from_grt_adjoint(beta, n_tau, nw, dims, nb, reinterpret_cast<const double2 *>(g_tr),
+                                         reinterpret_cast<const double2 *>(chi0_wr_grad),
+                                         reinterpret_cast<double2 *>(g_tr_grad), static_cast<cudaStream_t>(stream));
 }
 
 extern "C" int tprf_chi0_tr_from_grt_PH_adjoint(int n_tau, const int dims[3], int nb, const double *g_tr,

@@ -169,14 +169,78 @@ static bool factorize(int n, int *radix, int *nst) {
   return m == 1;
 }
 
-int get_fft(int n, FftDesc *out) {
+// Radix orders the autotuner chooses among (the same factors in another order,
+// which changes the stage count and which radix the last stage has):
+//   0: 8s, one 4, one 2, then 3s, 5s, 7s, larger primes (factorize);
+//   1: 4s and at most one 2 instead of 8s, then the odd factors;
+//   2: the odd factors first, then 8s, one 4, one 2;
+//   3: the leftover 2 or 4 of the power of two first, then 8s, then the odd factors.
+static bool factorize_variant(int n, int v, int *radix, int *nst) {
+  if (v == 0) return factorize(n, radix, nst);
+  int m = n, p2 = 0;
+  while (m % 2 == 0) {
+    m /= 2;
+    ++p2;
+  }
+  int odd[kMaxStages], no = 0, mo = m;
+  for (int r : {3, 5, 7})
+    while (mo % r == 0 && no < kMaxStages) { odd[no++] = r; mo /= r; }
+  for (int r = 11; (long)r * r <= mo && no < kMaxStages; r += 2)
+    while (mo % r == 0 && no < kMaxStages) { odd[no++] = r; mo /= r; }
+  if (mo > 1 && no < kMaxStages) { odd[no++] = mo; mo = 1; }
+  int pw[kMaxStages], np = 0;  // the power-of-two stages of this variant
+  if (v == 1) {
+    for (int e = p2; e >= 2; e -= 2) pw[np++] = 4;
+    if (p2 % 2) pw[np++] = 2;
+  } else if (v == 2) {
+    int e = p2;
+    for (; e >= 3; e -= 3) pw[np++] = 8;
+    if (e == 2) pw[np++] = 4;
+    if (e == 1) pw[np++] = 2;
+  } else {
+    if (p2 % 3 == 1) pw[np++] = 2;
+    if (p2 % 3 == 2) pw[np++] = 4;
+    for (int e = p2 - p2 % 3; e >= 3; e -= 3) pw[np++] = 8;
+  }
+  if (np + no > kMaxStages || mo != 1) return false;
+  int s = 0;
+  if (v == 2) {
+    for (int i = 0; i < no; ++i) radix[s++] = odd[i];
+    for (int i = 0; i < np; ++i) radix[s++] = pw[i];
+  } else {
+    for (int i = 0; i < np; ++i) radix[s++] = pw[i];
+    for (int i = 0; i < no; ++i) radix[s++] = odd[i];
+  }
+  *nst = s;
+  return true;
+}
+
+std::vector<int> fft_variants(int n) {
+  std::vector<int> out;
+  std::vector<std::vector<int>> seen;
+  for (int v = 0; v < kFftVariants; ++v) {
+    int radix[kMaxStages], nst = 0;
+    if (!factorize_variant(n, v, radix, &nst)) continue;
+    std::vector<int> seq(radix, radix + nst);
+    bool dup = false;
+    for (const auto &x : seen) dup = dup || x == seq;
+    if (dup) continue;
+    seen.push_back(seq);
+    out.push_back(v);
+  }
+  return out;
+}
+
+int get_fft(int n, FftDesc *out) { return get_fft_variant(n, 0, out); }
+
+int get_fft_variant(int n, int variant, FftDesc *out) {
   if (n < 1) return set_error(TPRF_ERR_INVALID_ARGUMENT, "FFT length must be >= 1");
   int dev = 0;
   int st = current_device(&dev);
   if (st) return st;
-  static std::map<std::pair<int, int>, FftDesc> cache;
+  static std::map<std::tuple<int, int, int>, FftDesc> cache;
   std::lock_guard<std::mutex> lock(g_mutex);
-  auto key = std::make_pair(dev, n);
+  auto key = std::make_tuple(dev, n, variant);
   auto it = cache.find(key);
   if (it != cache.end()) {
     *out = it->second;
@@ -184,7 +248,7 @@ int get_fft(int n, FftDesc *out) {
   }
   FftDesc d{};
   d.n = n;
-  if (!factorize(n, d.radix, &d.nst))
+  if (!factorize_variant(n, variant, d.radix, &d.nst))
     return set_error(TPRF_ERR_UNSUPPORTED_SIZE, "FFT length " + std::to_string(n) + " has too many factors");
   std::vector<double2> tw(n);
   for (int t = 0; t < n; ++t) {
