@@ -38,19 +38,26 @@ C16 = 16  # bytes per complex128
 
 
 # ---------------------------------------------------------------------------
-# algorithmic traffic and flops per stage (one read of inputs, one write of outputs)
+# algorithmic traffic and flops per stage: one read of each input and one write
+# of each output, in the representation the stage hands on. On the real path
+# (real hoppings: G(tau, r) real, G(-iv) = G(iv)^dagger, chi0(-w) from chi0(w))
+# iv -> tau reads the frequencies v >= 0 and writes real G(tau, r) (8 bytes per
+# element), the bubble writes the frequencies w >= 0 and r -> q reads those and
+# writes all 2 nw - 1.
 
-def stage_model(nb, nk, n_nu, n_tau, nw):
+def stage_model(nb, nk, n_nu, n_tau, nw, real=True):
     nb2, nb4, nwt = nb * nb, nb ** 4, 2 * nw - 1
     L = n_tau - 1
     fft_flops = lambda n: 5.0 * n * math.log2(n) if n > 1 else 0.0  # noqa: E731
+    g_tau = (8 if real else C16) * nb2 * nk * n_tau
+    w_out = nw if real else nwt
     return {
-        "dyson": dict(bytes=C16 * nb2 * n_nu * nk, flops=n_nu * nk * 8.0 * nb ** 3),
+        "dyson": dict(bytes=C16 * nb2 * (n_nu + 1) * nk, flops=n_nu * nk * 8.0 * nb ** 3),
         "fft_k_to_r": dict(bytes=2 * C16 * nb2 * n_nu * nk, flops=n_nu * nb2 * fft_flops(nk)),
-        "nu_to_tau": dict(bytes=C16 * nb2 * nk * (n_nu + n_tau), flops=nk * nb2 * fft_flops(L)),
-        "bubble_tau_to_w": dict(bytes=C16 * nk * (nb2 * n_tau + nb4 * nwt),
-                                flops=nk * nb4 * (6.0 * n_tau + fft_flops(L))),
-        "fft_r_to_q": dict(bytes=2 * C16 * nb4 * nwt * nk, flops=nwt * nb4 * fft_flops(nk)),
+        "nu_to_tau": dict(bytes=C16 * nb2 * nk * (n_nu // 2 if real else n_nu) + g_tau,
+                          flops=nk * nb2 * fft_flops(L)),
+        "bubble_tau_to_w": dict(bytes=g_tau + C16 * nb4 * nk * w_out, flops=nk * nb4 * (6.0 * n_tau + fft_flops(L))),
+        "fft_r_to_q": dict(bytes=C16 * nb4 * nk * (w_out + nwt), flops=nwt * nb4 * fft_flops(nk)),
         "rpa": dict(bytes=2 * C16 * nb4 * nwt * nk, flops=nwt * nk * 8.0 * (nb2 ** 3 * 2 + nb2 ** 3 / 3.0)),
     }
 
@@ -324,13 +331,23 @@ def cpu_throughput(cfg_key, procs: int, scale=1.0, pool=None):
 def setup_autotune(lib, args):
     """Measure mode of the library's autotuner unless --no-autotune: the first
     (warm-up) call of each shape times the candidate launch shapes."""
+    from tprf_gb300._native import check
     lib.tprf_set_autotune(0 if args.no_autotune else 1)
+    if getattr(args, "load_wisdom", None):
+        check(lib.tprf_autotune_load(args.load_wisdom.encode()), "autotune_load")
+
+
+def save_wisdom(lib, args):
+    from tprf_gb300._native import check
+    if getattr(args, "save_wisdom", None):
+        check(lib.tprf_autotune_save(args.save_wisdom.encode()), "autotune_save")
 
 
 def autotune_info(lib, args):
     """The autotuner's mode and its choices ("wisdom": kernel/shape key -> value;
     the *_radix keys name the FFT radix order, see fft_variants)."""
     import tempfile
+    save_wisdom(lib, args)
     wisdom = {}
     with tempfile.TemporaryDirectory() as d:
         path = os.path.join(d, "wisdom.txt")
@@ -568,7 +585,8 @@ def run_gpu(args):
                "placement": placement}
 
     # ---- roofline of the dominant kernel
-    model = stage_model(nb, nk, n_nu, n_tau, nw)
+    real = all(not np.any(np.imag(np.asarray(h))) for h in cfg["hoppings"].values())
+    model = stage_model(nb, nk, n_nu, n_tau, nw, real=real)
     top = max(stage_ms, key=stage_ms.get)
     peaks = {}
     try:
@@ -584,9 +602,15 @@ def run_gpu(args):
                      "hbm_frac": round(model[s]["bytes"] / (stage_ms[s] * 1e-3) / 1e9 / hbm_peak, 4),
                      "fp64_tflops": round(model[s]["flops"] / (stage_ms[s] * 1e-3) / 1e12, 3)}
                  for s in stages}
+    traffic, traffic_src = stage_traffic(dims, nb, n_max, nw)
+    for s in stages:
+        if s in traffic:
+            per_stage[s]["traffic"] = round(traffic[s])
+            per_stage[s]["traffic_over_algorithmic"] = round(traffic[s] / model[s]["bytes"], 3)
     roofline = {"bound": "hbm", "kernel": top, "achieved": round(achieved, 1), "peak": hbm_peak, "unit": "GB/s",
                 "frac": round(achieved / hbm_peak, 4), "peak_source": peak_src,
-                "algorithmic_bytes": model[top]["bytes"], "traffic": TRAFFIC.get((args.config, top)),
+                "algorithmic_bytes": model[top]["bytes"],
+                "traffic": round(traffic[top]) if top in traffic else None, "traffic_source": traffic_src,
                 # algorithmic FP64 flops of the stage / time, against this GPU's native FP64 rate:
                 # above 1 where the butterflies run in double-float on the FP32 pipe
                 "fp64": {"achieved_tflops": per_stage[top]["fp64_tflops"], "peak_tflops": fp64_peak_tflops,
@@ -1024,15 +1048,125 @@ def measure_fp64_peak(lib, dev) -> float:
     return round(out.value, 3)
 
 
-# DRAM traffic (read + write) per launch, from the ncu captures summarised under
-# profiles/ (16x16x8 case, 2048 r points), scaled to 32^3 (x16) by the number of r
-# points: the kernels stream their columns, so traffic grows in proportion.
-TRAFFIC = {
-    # DRAM bytes of one launch from an ncu capture of the kernel on the 16x16x8 case,
-    # scaled to 32^3 by the columns (points) processed
-    ("cfg1", "bubble_tau_to_w"): 16 * 1.049e9,
-    ("cfg1", "rpa"): 16 * 2.685e9,
-}
+# ---------------------------------------------------------------------------
+# DRAM traffic per stage, from an ncu launch capture
+#
+# The table in profiles/ is written by
+#   python bench.py --traffic-from-ncu <capture.csv> --config <the captured workload> --traffic-out <table>
+# from a one-pass capture (dram__bytes_read.sum, dram__bytes_write.sum and
+# gpu__time_duration.sum of every launch, --print-units base). It records a hash of
+# the CUDA sources; the bench reports `traffic` only while the sources still hash
+# the same, scaled from the captured mesh to the benched one by the number of k
+# points (every stage streams its (frequency, r or k) columns, so its DRAM bytes
+# grow in proportion at fixed frequencies and orbitals).
+
+TRAFFIC_TABLE = os.path.join(ROOT, "profiles", "traffic_cubic3orb_32x32x32.txt")
+STAGES = ("dyson", "fft_k_to_r", "nu_to_tau", "bubble_tau_to_w", "fft_r_to_q", "rpa")
+
+
+def kernel_sources_hash() -> str:
+    """sha256 (first 16 hex digits) of the CUDA sources the kernels are built from."""
+    import hashlib
+    h = hashlib.sha256()
+    d = os.path.join(ROOT, "tprf_gb300", "csrc")
+    for name in sorted(os.listdir(d)):
+        if name.endswith((".cu", ".cuh", ".hpp", ".h")):
+            h.update(name.encode())
+            with open(os.path.join(d, name), "rb") as f:
+                h.update(f.read())
+    return h.hexdigest()[:16]
+
+
+def stage_of_kernel(name: str):
+    """The path stage a kernel of the forward chain belongs to (None: not one)."""
+    import re
+    n = name.split("(")[0]
+    if "dyson_kernel" in n and "adjoint" not in n:
+        return "dyson"
+    m = re.search(r"lattice_(?:axis|plane|plane_tma)_kernel<(\w+)", n)
+    if m:  # first template argument FWD: the k -> r direction
+        return "fft_k_to_r" if m.group(1) in ("1", "true") else "fft_r_to_q"
+    if "hermitian_check_kernel" in n or re.search(r"nu_to_tau_kernel\b", n):
+        return "nu_to_tau"
+    if re.search(r"tau_to_w_kernel\b", n):
+        return "bubble_tau_to_w"
+    if re.search(r"rpa_(?:pair|warp|lu|lu_pair)_kernel\b", n):
+        return "rpa"
+    return None
+
+
+def write_traffic_table(args):
+    """Per-stage DRAM bytes of one launch (median over the capture's launches of each
+    kernel, summed over the stage's kernels: each runs once per step) from
+    `ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum
+    --print-units base --csv`."""
+    import csv
+    import re
+    from tprf_gb300 import workloads
+    cfg = workloads.config(args.config)
+    launches = {}
+    with open(args.traffic_from_ncu, newline="") as f:
+        rows = [r for r in csv.reader(f) if len(r) > 5]
+    start = next(i for i, r in enumerate(rows) if "Kernel Name" in r and "Metric Value" in r)
+    head, rows = rows[start], rows[start:]
+    col = {k: head.index(k) for k in ("ID", "Kernel Name", "Metric Name", "Metric Unit", "Metric Value")}
+    scale = {"byte": 1.0, "ns": 1e-6, "nsecond": 1e-6, "us": 1e-3, "usecond": 1e-3, "ms": 1.0, "msecond": 1.0}
+    for r in rows[1:]:
+        unit = r[col["Metric Unit"]]
+        if unit not in scale:
+            raise SystemExit(f"unexpected unit {unit!r}: capture with --print-units base")
+        rec = launches.setdefault(r[col["ID"]], {"kernel": r[col["Kernel Name"]].split("(")[0]})
+        rec[r[col["Metric Name"]]] = float(r[col["Metric Value"]].replace(",", "")) * scale[unit]
+    per_kernel = {}
+    for rec in launches.values():
+        if stage_of_kernel(rec["kernel"]) and "dram__bytes_read.sum" in rec:
+            per_kernel.setdefault(rec["kernel"], []).append(rec)
+    nk = int(math.prod(cfg["dims"]))
+    lines = ["# DRAM traffic per stage of one step (bytes per launch, median over the captured launches of each",
+             "# kernel, summed over the stage's kernels), from one ncu launch capture.",
+             f"workload {cfg['name']}", f"dims {' '.join(str(d) for d in cfg['dims'])}",
+             f"nb {int(cfg['U'].shape[0])}", f"n_max {cfg['n_max']}", f"nw {cfg['nw']}", f"nk {nk}",
+             f"sources {kernel_sources_hash()}", "# kernel launches read_bytes write_bytes ms stage"]
+    stage_sum = {s: [0.0, 0.0, 0.0] for s in STAGES}
+    for k in sorted(per_kernel, key=lambda k: STAGES.index(stage_of_kernel(k))):
+        recs = per_kernel[k]
+        rd = statistics.median(x["dram__bytes_read.sum"] for x in recs)
+        wr = statistics.median(x["dram__bytes_write.sum"] for x in recs)
+        ms = statistics.median(x.get("gpu__time_duration.sum", 0.0) for x in recs)
+        s = stage_of_kernel(k)
+        stage_sum[s][0] += rd
+        stage_sum[s][1] += wr
+        stage_sum[s][2] += ms
+        short = re.search(r"\w+_kernel(?:<.*>)?", k).group(0).replace(" ", "")
+        lines.append(f"kernel {short} {len(recs)} {rd:.0f} {wr:.0f} {ms:.4f} {s}")
+    lines.append("# stage read_bytes write_bytes ms")
+    for s in STAGES:
+        lines.append(f"stage {s} {stage_sum[s][0]:.0f} {stage_sum[s][1]:.0f} {stage_sum[s][2]:.4f}")
+    text = "\n".join(lines) + "\n"
+    if args.traffic_out:
+        with open(args.traffic_out, "w") as f:
+            f.write(text)
+    print(text, end="")
+
+
+def stage_traffic(dims, nb, n_max, nw, path=TRAFFIC_TABLE):
+    """({stage: DRAM bytes per launch at this mesh}, provenance) from the committed
+    table, or ({}, reason) when it is absent, for other frequencies or orbitals, or
+    captured from other kernel sources."""
+    try:
+        with open(path) as f:
+            rows = [ln.split() for ln in f if ln.strip() and not ln.startswith("#")]
+    except OSError:
+        return {}, {"traffic": None, "reason": f"no table at {os.path.relpath(path, ROOT)}"}
+    meta = {r[0]: r[1:] for r in rows if r[0] not in ("kernel", "stage")}
+    src = {"table": os.path.relpath(path, ROOT), "captured_on": meta["workload"][0]}
+    if meta["sources"][0] != kernel_sources_hash():
+        return {}, dict(src, traffic=None, reason="stale: the CUDA sources changed since the capture")
+    if (int(meta["nb"][0]), int(meta["n_max"][0]), int(meta["nw"][0])) != (nb, n_max, nw):
+        return {}, dict(src, traffic=None, reason="captured at other frequencies or orbitals")
+    ratio = int(math.prod(dims)) / int(meta["nk"][0])
+    out = {r[1]: (float(r[2]) + float(r[3])) * ratio for r in rows if r[0] == "stage"}
+    return out, dict(src, scale_by_k_points=ratio)
 
 
 # ---------------------------------------------------------------------------
@@ -1088,7 +1222,16 @@ def main():
     ap.add_argument("--streams", type=int, default=32, help="concurrent streams of the batched graph (cfg2)")
     ap.add_argument("--grad", action="store_true", help="cfg2: forward + gradient graphs per step")
     ap.add_argument("--no-autotune", action="store_true", help="fixed launch-shape heuristics instead of measure mode")
+    ap.add_argument("--load-wisdom", metavar="PATH", help="autotuner choices to load before the run (profiling runs "
+                                                          "with --no-autotune: the tuned shapes, no trial launches)")
+    ap.add_argument("--save-wisdom", metavar="PATH", help="write the autotuner's choices after the run")
+    ap.add_argument("--traffic-from-ncu", metavar="CSV", help="write the per-stage DRAM traffic table of an ncu "
+                                                              "launch capture (see traffic_table) and exit")
+    ap.add_argument("--traffic-out", metavar="PATH", help="with --traffic-from-ncu: the table's path")
     args = ap.parse_args()
+    if args.traffic_from_ncu:
+        write_traffic_table(args)
+        return
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
     if args.impl == "reference":

@@ -90,6 +90,28 @@ __device__ __forceinline__ dfl ddot_sub(dfl a1, dfl b1, dfl a2, dfl b2) {
 // a1 b1 + a2 b2
 __device__ __forceinline__ dfl ddot_add(dfl a1, dfl b1, dfl a2, dfl b2) { return ddot_sub(a1, b1, dneg(a2), b2); }
 
+// c - p q + u v: the ddot_sub scheme with the accumulator as a third term. The
+// leading parts of c and of the two products meet in two TwoSums; their
+// rounding errors, the products' errors, c.lo and the four cross terms go to
+// one float, closed by one Fast2Sum (27 float operations against 30 for
+// dsub(c, ddot_sub(p, q, u, v))), with the same error bound relative to
+// |c| + |p q| + |u v|.
+__device__ __forceinline__ dfl dfms2(dfl c, dfl p, dfl q, dfl u, dfl v) {
+  const float p1 = __fmul_rn(-p.hi, q.hi);
+  const float e1 = __fmaf_rn(-p.hi, q.hi, -p1);
+  const float p2 = __fmul_rn(u.hi, v.hi);
+  const float e2 = __fmaf_rn(u.hi, v.hi, -p2);
+  float s, t1, t2;
+  two_sum(c.hi, p1, s, t1);
+  two_sum(s, p2, s, t2);
+  float e = __fadd_rn(__fadd_rn(t1, t2), __fadd_rn(c.lo, __fadd_rn(e1, e2)));
+  e = __fmaf_rn(-p.hi, q.lo, e);
+  e = __fmaf_rn(-p.lo, q.hi, e);
+  e = __fmaf_rn(u.hi, v.lo, e);
+  e = __fmaf_rn(u.lo, v.hi, e);
+  return fast_two_sum(s, e);
+}
+
 // ---- complex ----------------------------------------------------------------
 __device__ __forceinline__ cdf cadd(cdf a, cdf b) { return cdf{dadd(a.x, b.x), dadd(a.y, b.y)}; }
 __device__ __forceinline__ cdf csub(cdf a, cdf b) { return cdf{dsub(a.x, b.x), dsub(a.y, b.y)}; }
@@ -102,6 +124,10 @@ __device__ __forceinline__ cdf cscale(cdf a, dfl s) { return cdf{dmul(a.x, s), d
 __device__ __forceinline__ cdf cconj(cdf a) { return cdf{a.x, dneg(a.y)}; }
 // y + k x
 __device__ __forceinline__ cdf caxpy(dfl k, cdf x, cdf y) { return cadd(y, cscale(x, k)); }
+// acc - a b (the elimination update)
+__device__ __forceinline__ cdf cfms_df(cdf a, cdf b, cdf acc) {
+  return cdf{dfms2(acc.x, a.x, b.x, a.y, b.y), dfms2(acc.y, a.x, b.y, dneg(a.y), b.x)};
+}
 template <bool FWD>
 __device__ __forceinline__ cdf mul_mi(cdf a) {  // -i a (FWD) or +i a
   return FWD ? cdf{a.y, dneg(a.x)} : cdf{dneg(a.y), a.x};

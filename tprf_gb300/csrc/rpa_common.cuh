@@ -28,7 +28,7 @@ __device__ __forceinline__ float el_absf(cdf z) { return sqrtf(z.x.hi * z.x.hi +
 template <class E> struct IsDf { static constexpr bool value = false; };
 template <> struct IsDf<cdf> { static constexpr bool value = true; };
 __device__ __forceinline__ double2 el_fms(double2 a, double2 b, double2 acc) { return cfms(a, b, acc); }
-__device__ __forceinline__ cdf el_fms(cdf a, cdf b, cdf acc) { return csub(acc, cmul(a, b)); }
+__device__ __forceinline__ cdf el_fms(cdf a, cdf b, cdf acc) { return cfms_df(a, b, acc); }
 __device__ __forceinline__ double2 el_recip(double2 a) { return crecip(a); }
 __device__ __forceinline__ cdf el_recip(cdf a) {
   // 1/(x + iy) = (x - iy) / (x^2 + y^2); the real reciprocal by one Newton step from the float one

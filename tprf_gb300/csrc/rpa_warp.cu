@@ -7,7 +7,8 @@
 // Design: the warp keeps the augmented matrix M = [A | B] (N x 2N, row major,
 // A = I - chi0 U, B = chi0) of its point in shared memory. Lanes own columns
 // of M, so every row access of the warp touches consecutive 16-byte elements
-// (no bank conflicts). Elimination with partial pivoting (pivot search by warp
+// (the layout notes at row_ld and group_stride say where conflicts remain).
+// Elimination with partial pivoting (pivot search by warp
 // shuffles, physical row swaps in A and B) turns A into U and B into L^-1 P B;
 // back substitution then runs per B column with no cross-lane dependency. The
 // loops are not unrolled over N: one instantiation per element type serves
@@ -15,7 +16,7 @@
 // re-solve of points whose conditioning estimate exceeds the double-float
 // limit (the estimate of rpa.cu).
 #include <algorithm>
-
+#include <climits>
 #include <vector>
 
 #include "rpa_common.cuh"
@@ -31,6 +32,25 @@ struct SparseU {  // U grouped and compacted by columns: rows and FP64 values
 
 // the grouped column index of the memory offset m = c' * nb + d inside a row
 __device__ __forceinline__ int col_of_offset(int m, int nb) { return (m % nb) * nb + m / nb; }
+
+// Shared-memory layout of a group's augmented matrix [A | B] (N x 2N, 16-byte
+// elements; a quarter-warp's 16-byte accesses hit 8 distinct bank quads when
+// their element indices differ modulo 8):
+//  - rows are row_ld(N) = 2N elements apart. The column accesses (pivot
+//    search, scaling of the pivot column, transposed reads) then pair rows i
+//    and i + 4 on one quad. An odd stride (2N + 1) removes those conflicts
+//    (8.4 % of the shared wavefronts left instead of 15.9 % at nb = 3) but
+//    ran 4 % slower on the 32^3 cubic workload with 9 lanes (34.0 against
+//    32.6 ms), so the even stride stays;
+//  - group_stride(N, G) elements separate the matrices of two groups: N row_ld,
+//    padded when a quarter-warp spans two groups (G not a multiple of 8) so that
+//    group g starts g * G elements after group 0 modulo 8, and the row
+//    accesses of three 9-lane groups cover consecutive quads as one 27-lane
+//    group would.
+__host__ __device__ constexpr int row_ld(int N) { return 2 * N; }
+__host__ __device__ constexpr int group_stride(int N, int G) {
+  return (G % 8 == 0) ? N * row_ld(N) : N * row_ld(N) + (((G - N * row_ld(N)) % 8) + 8) % 8;
+}
 
 // Pivot magnitudes: float for double-float elements (from the high words; an
 // underflow to zero reads as a zero pivot and sends the point to the FP64
@@ -93,15 +113,17 @@ __device__ __forceinline__ void group_argmax(MagT &best, int &p, unsigned gmask)
 }
 
 // Gaussian elimination with partial pivoting on the group's augmented matrix
-// M = [A | B] (N x 2N, row major, shared memory), then back substitution: on
-// return the right half holds A^-1 B and the left half the LU factors.
+// M = [A | B] (N x 2N, rows ld elements apart, shared memory), then back
+// substitution: on return the right half holds A^-1 B and the left half the LU
+// factors.
 // Lanes own columns; the pivot search is a shuffle argmax inside the group.
 // Returns the smallest squared pivot magnitude; sets `sing` on a zero pivot.
 template <class E, int G, int NC = 0>
-__device__ __forceinline__ typename Mag<E>::type solve_augmented(E *M, int N_in, int lane, unsigned gmask, bool &sing) {
+__device__ __forceinline__ typename Mag<E>::type solve_augmented(E *M, int N_in, int ld, int lane, unsigned gmask,
+                                                                 bool &sing) {
   const int N = NC > 0 ? NC : N_in;  // a compile-time size when NC > 0
   const int W = 2 * N;
-#define MM(i, c) M[(i) * W + (c)]
+#define MM(i, c) M[(i) * ld + (c)]
   using MagT = typename Mag<E>::type;
   MagT pmin = Mag<E>::big;
   for (int j = 0; j < N; ++j) {
@@ -154,13 +176,13 @@ __device__ __forceinline__ typename Mag<E>::type solve_augmented(E *M, int N_in,
 // b_ready: the caller has already written B = chi0 (from x) into M, with the
 // same lane of the group writing element o as the load loop here would.
 template <class E, int G, int NBC = 0>
-__device__ double rpa_point_warp(const double2 *__restrict__ x, double2 *__restrict__ y, E *M, int N_in, int nb_in,
+__device__ typename Mag<E>::type rpa_point_warp(const double2 *__restrict__ x, double2 *__restrict__ y, E *M, int N_in, int nb_in,
                                  const SparseU &u, int lane, unsigned gmask, bool &singular,
                                  double2 *__restrict__ y_conj = nullptr, bool b_ready = false) {
   const int nb = NBC > 0 ? NBC : nb_in;  // a compile-time size when NBC > 0
   const int N = NBC > 0 ? NBC * NBC : N_in;
-  const int W = 2 * N;
-#define MM(i, c) M[(i) * W + (c)]
+  const int LD = row_ld(N);
+#define MM(i, c) M[(i) * LD + (c)]
   // B = chi0 in the grouped layout (coalesced global reads)
   if (!b_ready)
     for (int o = lane; o < N * N; o += G) MM(o / N, N + col_of_offset(o % N, nb)) = el_from(x[o], (E *)nullptr);
@@ -183,19 +205,34 @@ __device__ double rpa_point_warp(const double2 *__restrict__ x, double2 *__restr
   __syncwarp(gmask);
 #undef MM
   bool sing = false;
-  const auto pmin = solve_augmented<E, G, NBC * NBC>(M, N, lane, gmask, sing);
+  const auto pmin = solve_augmented<E, G, NBC * NBC>(M, N, LD, lane, gmask, sing);
   singular = sing;
   for (int o = lane; o < N * N; o += G) {
-    const double2 v = el_to(M[(o / N) * 2 * N + N + col_of_offset(o % N, nb)]);
+    const double2 v = el_to(M[(o / N) * LD + N + col_of_offset(o % N, nb)]);
     y[o] = v;
     if (y_conj) y_conj[o] = make_double2(v.x, -v.y);  // the solve of the conjugate system, bit for bit
   }
   amax = group_max<G>(amax, gmask);
   __syncwarp(gmask);
-  const double am = (double)amax * (double)amax;
-  return pmin > 0 ? am / (double)pmin : 1e300;
+  if constexpr (IsDf<E>::value) {
+    // in float: the estimate only meets the re-solve limit and the transpose
+    // test, and the FP64 pipe stays free of per-point bookkeeping
+    return pmin > 0.f ? amax * amax / pmin : INFINITY;
+  } else {
+    const double am = (double)amax * (double)amax;
+    return pmin > 0 ? am / (double)pmin : 1e300;
+  }
 }
 
+
+// The FP64 re-solve of a double-float point, out of line: it runs for points
+// near an instability only, and inlined its register demand would shape the
+// allocation (and the spills) of the double-float solve around it.
+template <int G, int NBC>
+__device__ __noinline__ void resolve_fp64(const double2 *x, double2 *y, double2 *M, int N, int nb, const SparseU &u,
+                                          int lane, unsigned gmask, bool &singular, double2 *y_conj) {
+  rpa_point_warp<double2, G, NBC>(x, y, M, N, nb, u, lane, gmask, singular, y_conj);
+}
 
 template <class E, int G, int NBC = 0>
 __global__ void __launch_bounds__(512) rpa_warp_kernel(long n_points, int nb_in, const double2 *__restrict__ chi0,
@@ -215,7 +252,7 @@ __global__ void __launch_bounds__(512) rpa_warp_kernel(long n_points, int nb_in,
   const int grp = (threadIdx.x >> 5) * GPW + gw, lane = wl - gw * G, n_grp = (blockDim.x >> 5) * GPW;
   const bool active = gw < GPW;
   const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (gw * G));
-  E *M = reinterpret_cast<E *>(smem_raw + u_bytes) + (size_t)(active ? grp : 0) * 2 * N * N;
+  E *M = reinterpret_cast<E *>(smem_raw + u_bytes) + (size_t)(active ? grp : 0) * group_stride(N, G);
   if (threadIdx.x == 0) {
     int t = 0;
     for (int c = 0; c < N; ++c) {
@@ -239,9 +276,9 @@ __global__ void __launch_bounds__(512) rpa_warp_kernel(long n_points, int nb_in,
     const double2 *x = chi0 + pt * N * N;
     double2 *y = chi + pt * N * N;
     bool singular = false;
-    const double cond2 = rpa_point_warp<E, G, NBC>(x, y, M, N, nb, u, lane, gmask, singular);
-    if (IsDf<E>::value && !(cond2 <= kDf64CondLimit2))
-      rpa_point_warp<double2, G, NBC>(x, y, reinterpret_cast<double2 *>(M), N, nb, u, lane, gmask, singular);
+    const auto cond2 = rpa_point_warp<E, G, NBC>(x, y, M, N, nb, u, lane, gmask, singular);
+    if (IsDf<E>::value && !(cond2 <= (typename Mag<E>::type)kDf64CondLimit2))
+      resolve_fp64<G, NBC>(x, y, reinterpret_cast<double2 *>(M), N, nb, u, lane, gmask, singular, nullptr);
     if (singular && lane == 0) atomicOr(status, kDevErrSingular);
   }
 }
@@ -266,7 +303,7 @@ __global__ void __launch_bounds__(512) rpa_warp_kernel(long n_points, int nb_in,
 // for w > 0, q != -q and a symmetric U, also (w, -q) (transpose) and (-w, q)
 // (its conjugate). Units: w = 0 with q <= -q; w > 0 with q <= -q when
 // transposes are allowed, else every q.
-constexpr double kTransposeTol = 1e-12;
+constexpr float kTransposeTol2 = 1e-24f;  // kTransposeTol = 1e-12, squared
 
 // max(|Re(a - b)|, |Im(a - b)|) and max(|Re a|, |Im a|) as floats
 __device__ __forceinline__ float el_diff_max(double2 a, double2 b) {
@@ -290,7 +327,7 @@ __device__ __forceinline__ bool load_b_conj(const double2 *__restrict__ x, const
   bool sym = ureal;
   for (int o = lane; o < N * N; o += G) {
     const double2 a = x[o];
-    M[(o / N) * 2 * N + N + col_of_offset(o % N, nb)] = el_from(a, (E *)nullptr);
+    M[(o / N) * row_ld(N) + N + col_of_offset(o % N, nb)] = el_from(a, (E *)nullptr);
     if (test) {
       const double2 b = xc[o];
       sym = sym && __double_as_longlong(a.x) == __double_as_longlong(b.x) &&
@@ -302,24 +339,32 @@ __device__ __forceinline__ bool load_b_conj(const double2 *__restrict__ x, const
 
 // One point solve (B already in M when b_ready) writing chi to ys and, when yc
 // is given, its conjugate to yc; the FP64 re-solve when the conditioning
-// estimate asks for it. Returns the squared estimate, negated when the
+// estimate asks for it. Returns the squared estimate (float) and whether the
 // solution left in M is the FP64 one.
+struct PairSolve {
+  float cond2;
+  bool in64;
+};
 template <class E, int G, int NBC>
-__device__ __forceinline__ double solve_pair_point(const double2 *xs, double2 *ys, double2 *yc, bool b_ready, E *M,
-                                                   int N, int nb, const SparseU &u, int lane, unsigned gmask,
-                                                   unsigned *status) {
+__device__ __forceinline__ PairSolve solve_pair_point(const double2 *xs, double2 *ys, double2 *yc, bool b_ready, E *M,
+                                                      int N, int nb, const SparseU &u, int lane, unsigned gmask,
+                                                      unsigned *status) {
   bool singular = false;
-  double cond2 = rpa_point_warp<E, G, NBC>(xs, ys, M, N, nb, u, lane, gmask, singular, yc, b_ready);
-  if (IsDf<E>::value && !(cond2 <= kDf64CondLimit2)) {
-    rpa_point_warp<double2, G, NBC>(xs, ys, reinterpret_cast<double2 *>(M), N, nb, u, lane, gmask, singular, yc);
-    cond2 = -cond2;
+  PairSolve r{(float)rpa_point_warp<E, G, NBC>(xs, ys, M, N, nb, u, lane, gmask, singular, yc, b_ready), false};
+  if (IsDf<E>::value && !(r.cond2 <= (float)kDf64CondLimit2)) {
+    resolve_fp64<G, NBC>(xs, ys, reinterpret_cast<double2 *>(M), N, nb, u, lane, gmask, singular, yc);
+    r.in64 = true;
   }
   if (singular && lane == 0) atomicOr(status, kDevErrSingular);
-  return cond2;
+  return r;
 }
 
+// 448 threads and two CTAs per SM: a 72-register budget. Measured on the
+// 32^3 cubic workload (nb = 3, 9 lanes): 32.6 ms, against 34.7 ms at 80
+// registers (384 threads), 36.2 ms at 64 (512 threads, some spills) and
+// 42.4 ms unbounded (102 registers, 19 warps per SM).
 template <class E, int G, int NBC = 0>
-__global__ void __launch_bounds__(512) rpa_pair_kernel(int nw, int d0, int d1, int d2, int nb_in,
+__global__ void __launch_bounds__(448, 2) rpa_pair_kernel(int nw, int d0, int d1, int d2, int nb_in,
                                                        const double2 *__restrict__ chi0, const double2 *__restrict__ U,
                                                        PairOut out, unsigned *status) {
   const int nb = NBC > 0 ? NBC : nb_in;
@@ -335,7 +380,7 @@ __global__ void __launch_bounds__(512) rpa_pair_kernel(int nw, int d0, int d1, i
   const int grp = (threadIdx.x >> 5) * GPW + gw, lane = wl - gw * G, n_grp = (blockDim.x >> 5) * GPW;
   const bool active = gw < GPW;
   const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (gw * G));
-  E *M = reinterpret_cast<E *>(smem_raw + u_bytes) + (size_t)(active ? grp : 0) * 2 * N * N;
+  E *M = reinterpret_cast<E *>(smem_raw + u_bytes) + (size_t)(active ? grp : 0) * group_stride(N, G);
   if (threadIdx.x == 0) {
     int t = 0, ureal = 1, usym = 1;
     for (int c = 0; c < N; ++c) {
@@ -363,11 +408,14 @@ __global__ void __launch_bounds__(512) rpa_pair_kernel(int nw, int d0, int d1, i
   const bool ureal = s_ureal != 0;
   const bool tpairs = s_usym != 0 && IsDf<E>::value;  // transposition partners (never in the FP64 mode)
   if (!active) return;
-  const long nk = (long)d0 * d1 * d2, units = (long)(out.mh1 - out.mh0) * nk;
-  for (long un = (long)blockIdx.x * n_grp + grp; un < units; un += (long)gridDim.x * n_grp) {
-    const int mh = out.mh0 + (int)(un / nk);
-    const long q = un - (long)(mh - out.mh0) * nk;
-    const int q2 = (int)(q % d2), q1 = (int)((q / d2) % d1), q0 = (int)(q / ((long)d2 * d1));
+  // fewer than 2^31 units per launch (launch_pair_as splits larger frequency
+  // ranges): 32-bit index arithmetic, no 64-bit division
+  const unsigned nk = (unsigned)d0 * d1 * d2, d12 = (unsigned)d1 * d2, units = (unsigned)(out.mh1 - out.mh0) * nk;
+  for (unsigned un = blockIdx.x * n_grp + grp; un < units; un += gridDim.x * n_grp) {
+    const unsigned fm = un / nk, qu = un - fm * nk;
+    const int mh = out.mh0 + (int)fm;
+    const long q = qu;
+    const unsigned q0 = qu / d12, r12 = qu - q0 * d12, q1 = r12 / d2, q2 = r12 - q1 * d2;
     const long mq = ((long)((d0 - q0) % d0) * d1 + (d1 - q1) % d1) * d2 + (d2 - q2) % d2;
     if (q > mq && (mh == 0 || tpairs)) continue;  // a partner's unit holds this point
     // the unit's points: 0 = (w, q), 1 = (-w, -q) its conjugate, and for a
@@ -394,7 +442,7 @@ __global__ void __launch_bounds__(512) rpa_pair_kernel(int nw, int d0, int d1, i
         const double2 b = x2[o], c = x3[o];
         s3 = s3 && __double_as_longlong(b.x) == __double_as_longlong(c.x) &&
              __double_as_longlong(b.y) == __double_as_longlong(-c.y);
-        const E a = M[j * 2 * N + N + i];  // chi0(w, q)[j][i]
+        const E a = M[j * row_ld(N) + N + i];  // chi0(w, q)[j][i]
         dmax = fmaxf(dmax, el_diff_max(el_from(b, (E *)nullptr), a));
         amax = fmaxf(amax, el_max_abs(a));
       }
@@ -402,20 +450,20 @@ __global__ void __launch_bounds__(512) rpa_pair_kernel(int nw, int d0, int d1, i
       dmax = group_max<G>(dmax, gmask);
       amax = group_max<G>(amax, gmask);
     }
-    const double c2s = solve_pair_point<E, G, NBC>(chi0 + p0 * N * N, row_pos + q * N * N,
-                                                   sym ? row_neg + mq * N * N : nullptr, true, M, N, nb, u, lane,
-                                                   gmask, status);
+    const PairSolve s0 = solve_pair_point<E, G, NBC>(chi0 + p0 * N * N, row_pos + q * N * N,
+                                                     sym ? row_neg + mq * N * N : nullptr, true, M, N, nb, u, lane,
+                                                     gmask, status);
     // chi(w, -q) = chi(w, q)^T when chi0(w, -q) is chi0(w, q)^T to within the
-    // solve's conditioning (the transposed solution is read from M)
-    const double cond2 = fabs(c2s);
-    const bool take_t = quad && cond2 < 1e300 &&
-                        (double)dmax * (double)dmax * cond2 <= kTransposeTol * kTransposeTol * (double)amax * (double)amax;
+    // solve's conditioning (the transposed solution is read from M); in float
+    // (a threshold test: underflow of amax^2 only refuses the transpose)
+    const bool take_t =
+        quad && s0.cond2 < INFINITY && dmax * dmax * s0.cond2 <= kTransposeTol2 * amax * amax;
     if (take_t) {
-      const bool in64 = c2s < 0.0;  // the solution left in M is the FP64 one
+      const bool in64 = s0.in64;  // the solution left in M is the FP64 one
       double2 *y2 = row_pos + mq * N * N, *y3 = row_neg + q * N * N;
       for (int o = lane; o < N * N; o += G) {
         const int i = o / N, j = col_of_offset(o % N, nb);
-        const int at = j * 2 * N + N + i;
+        const int at = j * row_ld(N) + N + i;
         const double2 v = in64 ? reinterpret_cast<const double2 *>(M)[at] : el_to(M[at]);
         y2[o] = v;
         if (sym3) y3[o] = make_double2(v.x, -v.y);
@@ -447,7 +495,7 @@ int launch_as(long n_points, int nb, const double2 *chi0, const double2 *U, doub
               unsigned *status) {
   const int N = nb * nb;
   const size_t u_bytes = ((size_t)N * N * (sizeof(double2) + sizeof(int)) + (N + 1) * sizeof(int) + 15) & ~(size_t)15;
-  const size_t per_point = (size_t)2 * N * N * 16;
+  const size_t per_point = (size_t)group_stride(N, G) * 16;
   const int ppw = 32 / G;  // points per warp
   const size_t limit = (size_t)max_smem_optin();
   if (u_bytes + ppw * per_point > limit) return set_error(TPRF_ERR_INVALID_ARGUMENT, "solve_rpa_PH: nb too large");
@@ -527,7 +575,7 @@ __global__ void __launch_bounds__(256) screened_w_kernel(long n_points, long nk,
     }
     __syncwarp();
     bool sing = false;
-    solve_augmented<double2, 32>(M, N, lane, 0xffffffffu, sing);
+    solve_augmented<double2, 32>(M, N, 2 * N, lane, 0xffffffffu, sing);
     if (sing && lane == 0) atomicOr(status, kDevErrSingular);
     double2 *w = Wout + pt * N * N;
     for (int o = lane; o < N * N; o += 32) {
@@ -699,7 +747,8 @@ __global__ void __launch_bounds__(512) rpa_adjoint_warp_kernel(long n_points, in
 }  // namespace
 
 // lanes per point (measured on GB300 with the compiled sizes: nb = 3 9 lanes,
-// 90.2 ms for 16.7 M points, against 92.9 ms with 8 and 97.1 ms with 16;
+// 32.6 ms for the 16.7 M points of the 32^3 cubic workload in conjugate and
+// transposition partners, against 34.0 ms with 8 and 33.7 ms with 16;
 // nb = 5 32 lanes, 248 ms for 2.1 M points, against 376 ms with 16)
 int rpa_group_lanes(int nb) { return nb <= 2 ? 8 : nb == 3 ? 9 : 32; }
 
@@ -708,14 +757,16 @@ int launch_pair_as(int nw, const int dims[3], int nb, const double2 *chi0, const
                    cudaStream_t stream, unsigned *status) {
   const int N = nb * nb;
   const size_t u_bytes = ((size_t)N * N * (sizeof(double2) + sizeof(int)) + (N + 1) * sizeof(int) + 15) & ~(size_t)15;
-  const size_t per_point = (size_t)2 * N * N * 16;
+  const size_t per_point = (size_t)group_stride(N, G) * 16;
   const int ppw = 32 / G;
   const size_t limit = (size_t)max_smem_optin() - 64;  // the kernel's static word
   if (u_bytes + ppw * per_point > limit) return set_error(TPRF_ERR_INVALID_ARGUMENT, "solve_rpa_PH: nb too large");
   auto kern = rpa_pair_kernel<E, G, NBC>;
   TPRF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)limit));
+  cudaFuncAttributes fa{};
+  TPRF_CUDA(cudaFuncGetAttributes(&fa, kern));
   int best_w = 1, best_total = 0;
-  for (int w = 1; w <= 16; ++w) {
+  for (int w = 1; w <= std::min(16, fa.maxThreadsPerBlock / 32); ++w) {
     const size_t smem = u_bytes + (size_t)w * ppw * per_point;
     if (smem > limit) break;
     int per_sm = 0;
@@ -727,11 +778,22 @@ int launch_pair_as(int nw, const int dims[3], int nb, const double2 *chi0, const
   }
   if (best_total == 0) return set_error(TPRF_ERR_INVALID_ARGUMENT, "solve_rpa_PH: nb too large");
   const size_t smem = u_bytes + (size_t)best_w * ppw * per_point;
-  const long units = (long)(out.mh1 - out.mh0) * dims[0] * dims[1] * dims[2], per_block = (long)best_w * ppw;
-  long blocks = (units + per_block - 1) / per_block;
-  blocks = std::max(1L, std::min(blocks, (long)num_sms() * (best_total / best_w) * 8));
-  kern<<<(unsigned)blocks, 32 * best_w, smem, stream>>>(nw, dims[0], dims[1], dims[2], nb, chi0, U, out, status);
-  TPRF_LAUNCH_CHECK("rpa_pair_kernel");
+  const long nk = (long)dims[0] * dims[1] * dims[2], per_block = (long)best_w * ppw;
+  if (nk > INT_MAX) return set_error(TPRF_ERR_INVALID_ARGUMENT, "solve_rpa_PH: k mesh too large");
+  // frequency ranges of fewer than 2^31 units per launch (32-bit unit indices)
+  const int per_launch = (int)std::max(1L, (long)INT_MAX / nk);
+  for (int m0 = out.mh0; m0 < out.mh1; m0 += per_launch) {
+    PairOut part = out;
+    part.mh0 = m0;
+    part.mh1 = std::min(out.mh1, m0 + per_launch);
+    part.pos = out.pos + (long)(m0 - out.mh0) * out.row;
+    part.neg = out.neg ? out.neg + (long)(m0 - out.mh0) * out.neg_step : nullptr;
+    const long units = (long)(part.mh1 - part.mh0) * nk;
+    long blocks = (units + per_block - 1) / per_block;
+    blocks = std::max(1L, std::min(blocks, (long)num_sms() * (best_total / best_w) * 8));
+    kern<<<(unsigned)blocks, 32 * best_w, smem, stream>>>(nw, dims[0], dims[1], dims[2], nb, chi0, U, part, status);
+    TPRF_LAUNCH_CHECK("rpa_pair_kernel");
+  }
   return TPRF_OK;
 }
 
@@ -765,7 +827,7 @@ int launch_rpa_warp(long n_points, int nb, const double2 *chi0, const double2 *U
   std::vector<int> cands;
   // 9 lanes (three groups per warp) own two of the 18 columns of a 9 x 9 system each
   for (int g : {8, 9, 16, 32})
-    if ((g != 9 || N == 9) && u_bytes + (size_t)(32 / g) * 2 * N * N * 16 <= (size_t)max_smem_optin())
+    if ((g != 9 || N == 9) && u_bytes + (size_t)(32 / g) * group_stride(N, g) * 16 <= (size_t)max_smem_optin())
       cands.push_back(g);
   int lanes = rpa_group_lanes(nb);
   const long n_tune = std::min(n_points, (long)num_sms() * 2048);
@@ -786,7 +848,7 @@ int launch_rpa_warp_pairs(int nw, const int dims[3], int nb, const double2 *chi0
   const size_t u_bytes = ((size_t)N * N * (sizeof(double2) + sizeof(int)) + (N + 1) * sizeof(int) + 15) & ~(size_t)15;
   std::vector<int> cands;
   for (int g : {8, 9, 16, 32})
-    if ((g != 9 || N == 9) && u_bytes + (size_t)(32 / g) * 2 * N * N * 16 <= (size_t)max_smem_optin() - 64)
+    if ((g != 9 || N == 9) && u_bytes + (size_t)(32 / g) * group_stride(N, g) * 16 <= (size_t)max_smem_optin() - 64)
       cands.push_back(g);
   auto launch = [&](int lanes, PairOut o) -> int {
     switch (lanes) {
@@ -799,10 +861,15 @@ int launch_rpa_warp_pairs(int nw, const int dims[3], int nb, const double2 *chi0
   int lanes = rpa_group_lanes(nb);
   int st;
   if ((const void *)chi0 != (const void *)(out.pos - (long)(nw - 1 - out.mh0) * out.row)) {
-    // a trial solves the units of the first frequency of the range, the same
-    // values the full run writes there
+    // a trial solves the units of the first frequencies after w = 0 (w = 0 has
+    // no transposition quads), at least 65536 units, the same values the full
+    // run writes there
+    const long nk = (long)dims[0] * dims[1] * dims[2];
     PairOut first = out;
-    first.mh1 = out.mh0 + 1;
+    first.mh0 = (out.mh0 == 0 && out.mh1 > 1) ? 1 : out.mh0;
+    first.mh1 = (int)std::min<long>(out.mh1, first.mh0 + std::max(1L, (65536 + nk - 1) / nk));
+    first.pos = out.pos + (long)(first.mh0 - out.mh0) * out.row;
+    first.neg = out.neg ? out.neg + (long)(first.mh0 - out.mh0) * out.neg_step : nullptr;
     st = tune_pick(tune_key("rpa_group", {nb}), cands, lanes, stream, [&](int v) { return launch(v, first); },
                    &lanes);
   } else {

@@ -31,17 +31,23 @@ std::mutex g_tune_mu;
 std::map<std::string, int> g_wisdom;
 std::atomic<int> g_tune_mode{0};
 
-// Seconds per launch of one candidate: one untimed launch, then the mean of two.
+// Milliseconds per launch of one candidate: one untimed launch, then the
+// shortest of three timed launches (the minimum ranks candidates a few percent
+// apart more reliably than a mean of short launches).
 int time_candidate(const std::function<int(int)> &launch, int value, cudaStream_t s, cudaEvent_t e0, cudaEvent_t e1,
                    float *ms) {
   int st = launch(value);
   if (st) return st;
-  TPRF_CUDA(cudaEventRecord(e0, s));
-  for (int rep = 0; rep < 2; ++rep)
+  *ms = 3.0e38f;
+  for (int rep = 0; rep < 3; ++rep) {
+    TPRF_CUDA(cudaEventRecord(e0, s));
     if ((st = launch(value))) return st;
-  TPRF_CUDA(cudaEventRecord(e1, s));
-  TPRF_CUDA(cudaEventSynchronize(e1));
-  TPRF_CUDA(cudaEventElapsedTime(ms, e0, e1));
+    TPRF_CUDA(cudaEventRecord(e1, s));
+    TPRF_CUDA(cudaEventSynchronize(e1));
+    float t = 0.f;
+    TPRF_CUDA(cudaEventElapsedTime(&t, e0, e1));
+    *ms = std::min(*ms, t);
+  }
   return TPRF_OK;
 }
 
