@@ -507,7 +507,11 @@ def run_gpu(args):
         torch.cuda.empty_cache()
         from tprf_gb300.lattice_utils import imtime_bubble_rpa_wk, join_host_copies
         block = max(1, -(-nw // 16))
-        fws = torch.empty(lib.tprf_imtime_bubble_rpa_to_host_workspace_bytes(n_max, n_tau, nw, d3, nb, block, 3),
+        # a ring slot for every block of the frequencies w >= 0 (real bubble): the
+        # solves never wait for the call's own copies, which drain behind the next
+        # call's chain
+        slots = min(32, -(-nw // block))
+        fws = torch.empty(lib.tprf_imtime_bubble_rpa_to_host_workspace_bytes(n_max, n_tau, nw, d3, nb, block, slots),
                           dtype=torch.uint8, device=dev)
         chi0_buf = torch.empty((nwt, nk) + (nb,) * 4, dtype=torch.complex128, device=dev)
 
@@ -516,7 +520,7 @@ def run_gpu(args):
             # copied to the pinned host buffer in frequency blocks while later blocks solve
             ekd = ek_host.to(dev, non_blocking=True)
             g = T.lattice_dyson_g0_wk(mu, T.Gf(mesh=kmesh, data=ekd), wmesh)
-            imtime_bubble_rpa_wk(g, cfg["U"], nw, out=out_host, block_freqs=block, slots=3, chi0=chi0_buf,
+            imtime_bubble_rpa_wk(g, cfg["U"], nw, out=out_host, block_freqs=block, slots=slots, chi0=chi0_buf,
                                  workspace=fws, wait=wait)
             del g
 
@@ -544,7 +548,9 @@ def run_gpu(args):
                     "fill_threads": int(st[7]), "real_path": bool(st[8]),
                     "blocks_with_negative_rows_over_link": round(st[9], 3)}
 
-        e2e_steps = max(1, min(args.steps, 5))
+        # the run ends when the last step's chi is on the host: that drain (one call's
+        # copies and fill behind its compute) is part of the time, spread over 10 steps
+        e2e_steps = 10
         # pipelined: a step's chi copy (bound by the device-to-host link) runs behind the
         # next step's chain; device errors are read once, after the run
         lib.tprf_set_sync_checks(0)
@@ -577,7 +583,7 @@ def run_gpu(args):
                "path": "lattice_dyson_g0_wk -> imtime_bubble_rpa_wk(wait=False) (chain + RPA, chi to pinned host "
                        "memory, the copies of a step overlapping the next step's chain; host threads fill "
                        "chi(-w, q) = conj(chi(w, -q)) when only w >= 0 crossed)",
-               "steps": e2e_steps, "ms_per_step": e2e_s * 1e3,
+               "steps": e2e_steps, "ms_per_step": e2e_s * 1e3, "block_freqs": block, "ring_slots": slots,
                "serial": {"value": world * points / serial_s, "ms_per_step": serial_s * 1e3,
                           "path": "imtime_bubble_rpa_wk(wait=True): each call returns with chi on the host",
                           "host_side_last_step": rec_serial},

@@ -275,8 +275,10 @@ int tprf_solve_rpa_PH_wk(int nw, const int dims[3], int nb, const double *chi0, 
  * chi_wk). chi0_wk is a device buffer of chi_wk's shape, used as scratch (it
  * ends holding chi0 for the frequencies the blocks transformed). The r -> q
  * transform, the RPA and the copies to the host run in blocks of block_freqs
- * bosonic frequencies with `slots` device buffers (1..8), so that the copy of
- * one block overlaps the solve of the next. Same chi as the two calls. With a
+ * bosonic frequencies with `slots` device buffers (1..32), so that the copy of
+ * one block overlaps the solve of the next. With a slot for every block, a
+ * call's solves never wait for its own copies, and with wait = 0 those copies
+ * drain behind the next call's chain. Same chi as the two calls. With a
  * real bubble and a real U, chi(-w, q) = conj(chi(w, -q)) exactly, and only the
  * frequencies w >= 0 cross to the host: host threads fill the others there.
  * Stream-ordered: `stream` waits for the last copy, and with sync checks on

@@ -39,7 +39,7 @@ int launch_rpa(long n_points, int nb, const double2 *chi0, const double2 *U, dou
 
 namespace {
 
-constexpr int kMaxSlots = 8;
+constexpr int kMaxSlots = 32;
 
 // Host threads that fill the negative frequencies of chi in host memory from
 // the non-negative ones already copied there, chi(-w, q) = conj(chi(w, -q)),
@@ -175,6 +175,19 @@ void CUDART_CB wait_host_mirrors(void *data) {
   delete sp;
 }
 
+// One call's copies and host fill: timing events around every copy (grown on
+// demand), the bytes that crossed the link and that the host filled, and the
+// fill record.
+constexpr int kRecords = 4;
+struct CallRecord {
+  std::vector<cudaEvent_t> copy_begin, copy_end;
+  int copies = 0;
+  size_t d2h = 0, filled = 0;
+  std::shared_ptr<FillStats> fill;
+  bool real = false, mirror = false, fold_pending = false;
+  double frac = 1.0;
+};
+
 // One copy stream and its events per device, created on first use. copied[i]
 // marks the last copy out of ring slot i (of this call or an earlier one: a
 // call that does not wait for its copies leaves them running while the next
@@ -184,12 +197,11 @@ struct CopyCtx {
   cudaStream_t copy = nullptr;
   cudaEvent_t computed[kMaxSlots], copied[kMaxSlots], done;
   bool pending[kMaxSlots] = {};
-  size_t last_d2h = 0;  // bytes the last call copied to the host
-  // timing events around every copy of the last call (grown on demand) and
-  // its host-fill record
-  std::vector<cudaEvent_t> copy_begin, copy_end;
-  int last_copies = 0;
-  std::shared_ptr<FillStats> last_fill;
+  // the records of the last kRecords calls (a call that does not wait for its
+  // copies is still in flight when the next ones start; its rates are folded
+  // into the split by whichever later call finds it complete)
+  CallRecord rec[kRecords];
+  long calls = 0;  // calls enqueued so far; the last one's record is rec[(calls - 1) % kRecords]
   // Split of the negative frequencies of a real chi between the link and the host
   // threads: block k copies its rows -m over the link (both signs solved on the
   // device) when floor((k + 1) f + 1/2) > floor(k f + 1/2), so a fraction f of the
@@ -201,42 +213,40 @@ struct CopyCtx {
   // to the balance point (kept in [0, 0.9], so the fill rate stays measured).
   int host_fill_mode = -1;  // -1 adaptive, 0 every row over the link, 1 every row -m filled on the host
   double dma_frac = 0.4;    // current f of the adaptive mode
-  bool fold_pending = false;
-  bool last_real = false, last_mirror = false;
-  double last_frac = 0.0;
-  size_t last_filled = 0;   // bytes of rows -m the host filled in the last call
   std::mutex mu;        // one call at a time enqueues on this device's copy stream
+  CallRecord &last() { return rec[(calls + kRecords - 1) % kRecords]; }
 };
 
-// the i-th pair of timing events of a call (created on first use)
-int copy_events(CopyCtx *c, int i, cudaEvent_t *b, cudaEvent_t *e) {
-  while ((int)c->copy_begin.size() <= i) {
+// the i-th pair of timing events of a call's record (created on first use)
+int copy_events(CallRecord *r, int i, cudaEvent_t *b, cudaEvent_t *e) {
+  while ((int)r->copy_begin.size() <= i) {
     cudaEvent_t x, y;
     TPRF_CUDA(cudaEventCreate(&x));
     TPRF_CUDA(cudaEventCreate(&y));
-    c->copy_begin.push_back(x);
-    c->copy_end.push_back(y);
+    r->copy_begin.push_back(x);
+    r->copy_end.push_back(y);
   }
-  *b = c->copy_begin[i];
-  *e = c->copy_end[i];
+  *b = r->copy_begin[i];
+  *e = r->copy_end[i];
   return TPRF_OK;
 }
 
-// Adaptive split: fold the last call's rates into dma_frac once its copies and
-// fill have finished (checked without waiting; a call still in flight is folded
-// by a later call).
-void fold_split_rates(CopyCtx *c) {
-  if (!c->fold_pending || c->last_copies == 0 || !c->last_fill) return;
-  if (cudaEventQuery(c->copy_end[c->last_copies - 1]) != cudaSuccess) {
+// Adaptive split: fold a call's rates into dma_frac once its copies and fill
+// have finished (checked without waiting). fold_split_rates folds every
+// recorded call that has, oldest first; a record reused before its call was
+// found complete is dropped.
+void fold_record(CopyCtx *c, CallRecord *r) {
+  if (!r->fold_pending || r->copies == 0 || !r->fill) return;
+  if (cudaEventQuery(r->copy_end[r->copies - 1]) != cudaSuccess) {
     cudaGetLastError();  // a not-ready query is not an error of the next call
     return;
   }
-  if (!c->last_fill->complete.load()) return;
-  c->fold_pending = false;
+  if (!r->fill->complete.load()) return;
+  r->fold_pending = false;
   double copy_ms = 0.0;
-  for (int i = 0; i < c->last_copies; ++i) {
+  for (int i = 0; i < r->copies; ++i) {
     float ms = 0.f;
-    if (cudaEventElapsedTime(&ms, c->copy_begin[i], c->copy_end[i]) != cudaSuccess) {
+    if (cudaEventElapsedTime(&ms, r->copy_begin[i], r->copy_end[i]) != cudaSuccess) {
       cudaGetLastError();
       return;
     }
@@ -244,13 +254,16 @@ void fold_split_rates(CopyCtx *c) {
   }
   double fill_busy_ms;
   {
-    std::lock_guard<std::mutex> l(c->last_fill->mu);
-    fill_busy_ms = c->last_fill->job_ms / std::max(1, HostPool::get().threads());
+    std::lock_guard<std::mutex> l(r->fill->mu);
+    fill_busy_ms = r->fill->job_ms / std::max(1, HostPool::get().threads());
   }
-  if (copy_ms <= 0.0 || fill_busy_ms <= 0.0 || c->last_filled == 0) return;
-  const double r_link = (double)c->last_d2h / copy_ms, r_fill = (double)c->last_filled / fill_busy_ms;
+  if (copy_ms <= 0.0 || fill_busy_ms <= 0.0 || r->filled == 0) return;
+  const double r_link = (double)r->d2h / copy_ms, r_fill = (double)r->filled / fill_busy_ms;
   const double target = std::min(0.9, std::max(0.0, (r_link - r_fill) / (r_link + r_fill)));
   c->dma_frac = 0.5 * (c->dma_frac + target);
+}
+void fold_split_rates(CopyCtx *c) {
+  for (long k = std::max(0L, c->calls - kRecords); k < c->calls; ++k) fold_record(c, &c->rec[k % kRecords]);
 }
 std::mutex g_copy_mu;
 std::map<int, CopyCtx> g_copy;
@@ -342,10 +355,12 @@ int bubble_rpa_to_host(double beta, int n_iw, int n_tau, int nw, const int dims[
   const int n_blocks = real ? (nw + block_freqs - 1) / block_freqs : (n_w + block_freqs - 1) / block_freqs;
   auto fill = std::make_shared<FillStats>();
   int n_copies = 0;
+  CallRecord *rec = &c->rec[c->calls % kRecords];
+  rec->fold_pending = false;  // a record still unfolded here is dropped
   // one device-to-host copy on the copy stream, between this call's timing events
   auto d2h_copy = [&](double2 *dst, const double2 *src, size_t bytes) -> int {
     cudaEvent_t b, e;
-    if (int r = copy_events(c, n_copies++, &b, &e)) return r;
+    if (int r = copy_events(rec, n_copies++, &b, &e)) return r;
     TPRF_CUDA(cudaEventRecord(b, c->copy));
     TPRF_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->copy));
     TPRF_CUDA(cudaEventRecord(e, c->copy));
@@ -396,14 +411,15 @@ int bubble_rpa_to_host(double beta, int n_iw, int n_tau, int nw, const int dims[
   }
   if (host_mirror)
     TPRF_CUDA(cudaLaunchHostFunc(c->copy, wait_host_mirrors, new std::shared_ptr<FillStats>(fill)));
-  c->last_d2h = d2h;
-  c->last_copies = n_copies;
-  c->last_fill = fill;
-  c->last_real = real;
-  c->last_mirror = host_mirror;
-  c->last_frac = frac;
-  c->last_filled = filled;
-  c->fold_pending = host_mirror && filled > 0;
+  rec->d2h = d2h;
+  rec->copies = n_copies;
+  rec->fill = fill;
+  rec->real = real;
+  rec->mirror = host_mirror;
+  rec->frac = frac;
+  rec->filled = filled;
+  rec->fold_pending = host_mirror && filled > 0;
+  ++c->calls;
   TPRF_CUDA(cudaEventRecord(c->done, c->copy));
   if (join) TPRF_CUDA(cudaStreamWaitEvent(s, c->done, 0));
   return finish_with_checks(s, "imtime_bubble_rpa_to_host");
@@ -431,7 +447,7 @@ extern "C" size_t tprf_imtime_bubble_rpa_to_host_last_d2h_bytes(void) {
   CopyCtx *c = nullptr;
   if (copy_ctx(&c)) return 0;
   std::lock_guard<std::mutex> lock(c->mu);
-  return c->last_d2h;
+  return c->calls > 0 ? c->last().d2h : 0;
 }
 
 extern "C" int tprf_imtime_bubble_rpa_to_host_last_stats(double *out, int n) {
@@ -439,33 +455,40 @@ extern "C" int tprf_imtime_bubble_rpa_to_host_last_stats(double *out, int n) {
   CopyCtx *c = nullptr;
   if (int st = copy_ctx(&c)) return st;
   std::lock_guard<std::mutex> lock(c->mu);
-  double v[10] = {(double)c->last_d2h, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, (double)HostPool::get().threads(),
-                  c->last_real ? 1.0 : 0.0, c->last_mirror ? c->last_frac : 1.0};
-  if (c->last_copies > 0) {
-    TPRF_CUDA(cudaEventSynchronize(c->copy_end[c->last_copies - 1]));
+  double v[10] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, (double)HostPool::get().threads(), 0.0, 1.0};
+  if (c->calls == 0) {
+    for (int i = 0; i < n && i < 10; ++i) out[i] = v[i];
+    return TPRF_OK;
+  }
+  CallRecord *r = &c->last();
+  v[0] = (double)r->d2h;
+  v[8] = r->real ? 1.0 : 0.0;
+  v[9] = r->mirror ? r->frac : 1.0;
+  if (r->copies > 0) {
+    TPRF_CUDA(cudaEventSynchronize(r->copy_end[r->copies - 1]));
     float ms = 0.f;
-    for (int i = 0; i < c->last_copies; ++i) {
-      TPRF_CUDA(cudaEventElapsedTime(&ms, c->copy_begin[i], c->copy_end[i]));
+    for (int i = 0; i < r->copies; ++i) {
+      TPRF_CUDA(cudaEventElapsedTime(&ms, r->copy_begin[i], r->copy_end[i]));
       v[1] += ms;
     }
-    TPRF_CUDA(cudaEventElapsedTime(&ms, c->copy_begin[0], c->copy_end[c->last_copies - 1]));
+    TPRF_CUDA(cudaEventElapsedTime(&ms, r->copy_begin[0], r->copy_end[r->copies - 1]));
     v[2] = ms;
   }
-  if (c->last_fill && c->last_mirror) {
+  if (r->fill && r->mirror) {
     // the copy stream's last host function sets the flag after the fill jobs (the
     // copies above have finished, so it runs next); bounded wait
     const Clock::time_point t0 = Clock::now();
-    while (!c->last_fill->complete.load()) {
+    while (!r->fill->complete.load()) {
       if (Clock::now() - t0 > std::chrono::seconds(60))
         return set_error(TPRF_ERR_CUDA, "imtime_bubble_rpa_to_host_last_stats: host fill did not finish in 60 s");
       std::this_thread::sleep_for(std::chrono::microseconds(200));
     }
-    v[3] = c->last_fill->span_ms();
-    std::lock_guard<std::mutex> l(c->last_fill->mu);
-    v[4] = c->last_fill->job_ms;
-    v[5] = (double)c->last_fill->cpus.size();
+    v[3] = r->fill->span_ms();
+    std::lock_guard<std::mutex> l(r->fill->mu);
+    v[4] = r->fill->job_ms;
+    v[5] = (double)r->fill->cpus.size();
   }
-  v[6] = (double)c->last_copies;
+  v[6] = (double)r->copies;
   for (int i = 0; i < n && i < 10; ++i) out[i] = v[i];
   return TPRF_OK;
 }

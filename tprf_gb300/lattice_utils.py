@@ -62,9 +62,12 @@ def imtime_bubble_rpa_wk(g_wk, U, nw, out=None, nt=-1, moments=None, block_freqs
     to host memory (``out``: a pinned complex128 host tensor of chi's shape,
     allocated if None), the two reference calls in one: the r -> q transform,
     the RPA and the copies to the host run in blocks of ``block_freqs`` bosonic
-    frequencies, the copy of one block overlapping the solve of the next.
-    ``chi0`` (device tensor of chi's shape) and ``workspace`` (uint8 device
-    tensor) may be given to avoid allocations. Returns a host Gf.
+    frequencies, the copy of one block overlapping the solve of the next, with
+    ``slots`` device buffers of one block (1..32): with one per block the solves
+    never wait for the call's own copies (the fastest pipeline, for a device
+    ring of chi's size). ``chi0`` (device tensor of chi's shape) and
+    ``workspace`` (uint8 device tensor) may be given to avoid allocations.
+    Returns a host Gf.
 
     ``wait=False`` returns without waiting for the copies: they run on behind
     the compute, so that the next call's chain overlaps them (a pipeline over
