@@ -1070,13 +1070,19 @@ TRAFFIC_TABLE = os.path.join(ROOT, "profiles", "traffic_cubic3orb_32x32x32.txt")
 STAGES = ("dyson", "fft_k_to_r", "nu_to_tau", "bubble_tau_to_w", "fft_r_to_q", "rpa")
 
 
+# the translation units that define or launch the forward chain's kernels (the
+# headers count too); the host-copy, batch, GW, Lindhard and nb <= 2 RPA units
+# do not change those kernels' traffic
+CHAIN_SOURCES = ("dyson.cu", "fft_lattice.cu", "matsubara.cu", "pipeline.cu", "plans.cu", "rpa_warp.cu", "tune.cu")
+
+
 def kernel_sources_hash() -> str:
-    """sha256 (first 16 hex digits) of the CUDA sources the kernels are built from."""
+    """sha256 (first 16 hex digits) of the CUDA sources the chain's kernels are built from."""
     import hashlib
     h = hashlib.sha256()
     d = os.path.join(ROOT, "tprf_gb300", "csrc")
     for name in sorted(os.listdir(d)):
-        if name.endswith((".cu", ".cuh", ".hpp", ".h")):
+        if name in CHAIN_SOURCES or name.endswith((".cuh", ".hpp", ".h")):
             h.update(name.encode())
             with open(os.path.join(d, name), "rb") as f:
                 h.update(f.read())
