@@ -446,10 +446,12 @@ def run_gpu(args):
     with clocks:
         t_start = torch.cuda.Event(enable_timing=True)
         t_end = torch.cuda.Event(enable_timing=True)
+        l0 = lib.tprf_kernel_launches()
         t_start.record(stream)
         for k in range(args.steps):
             step((evs[k], handles[k]))
         t_end.record(stream)
+        launches = lib.tprf_kernel_launches() - l0
         torch.cuda.synchronize()
     barrier(world, dev)
     check(lib.tprf_check_device_status(sh), "timed steps")
@@ -465,14 +467,35 @@ def run_gpu(args):
     # its own), compared with the benched step's chi over the whole tensor
     accuracy = None
     if not args.no_accuracy:
-        chi_ref = torch.empty_like(chi)
+        # chi_ref beside chi and chi0 when the device has room; otherwise the FP64
+        # chain's chi0 replaces the benched one and its RPA (the point form, which in
+        # the FP64 mode equals the mesh form bit for bit) is solved and compared in
+        # chunks of frequencies
+        whole = torch.cuda.mem_get_info(dev)[0] > chi.numel() * C16 + (4 << 30)
+        chi_ref = torch.empty_like(chi) if whole else None
+        chunk = 32
+        num = den = 0.0
         mode0, tune0 = lib.tprf_get_arithmetic(), lib.tprf_get_autotune()
         lib.tprf_set_autotune(0)
         check(lib.tprf_set_arithmetic(1))
         try:
             a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a0.record(stream)
-            step(out=chi_ref)
+            if whole:
+                step(out=chi_ref)
+            else:
+                check(lib.tprf_lattice_dyson_g_wk(beta, n_max, nk, nb, mu, e_k.data_ptr(), None, 0, g_wk.data_ptr(),
+                                                  sh))
+                check(lib.tprf_imtime_bubble_chi0_wk(beta, n_max, n_tau, nw, d3, nb, g_wk.data_ptr(), None,
+                                                     chi0.data_ptr(), ws.data_ptr(), ws_bytes, sh))
+                part = torch.empty((chunk,) + tuple(chi.shape[1:]), dtype=chi.dtype, device=dev)
+                for a in range(0, nwt, chunk):
+                    b = min(nwt, a + chunk)
+                    check(lib.tprf_solve_rpa_PH((b - a) * nk, nb, chi0[a:b].data_ptr(), U.data_ptr(),
+                                                part.data_ptr(), sh))
+                    num = max(num, float((chi[a:b] - part[: b - a]).abs().max()))
+                    den = max(den, float(part[: b - a].abs().max()))
+                del part
             a1.record(stream)
             torch.cuda.synchronize()
             check(lib.tprf_check_device_status(sh), "FP64 step")
@@ -480,11 +503,11 @@ def run_gpu(args):
             lib.tprf_set_arithmetic(mode0)
             lib.tprf_set_autotune(tune0)
         fp64_ms = a0.elapsed_time(a1)
-        num = den = 0.0
-        for a in range(0, nwt, 32):  # chunks of frequencies bound the temporaries
-            b = min(nwt, a + 32)
-            num = max(num, float((chi[a:b] - chi_ref[a:b]).abs().max()))
-            den = max(den, float(chi_ref[a:b].abs().max()))
+        if whole:
+            for a in range(0, nwt, 32):  # chunks of frequencies bound the temporaries
+                b = min(nwt, a + 32)
+                num = max(num, float((chi[a:b] - chi_ref[a:b]).abs().max()))
+                den = max(den, float(chi_ref[a:b].abs().max()))
         accuracy = {"max_rel_err_vs_fp64": num / den, "bar": 1e-10,
                     "definition": "max |chi - chi_fp64| / max |chi_fp64| over the whole (iw, q, orbital) tensor",
                     "arithmetic": {0: "df64", 1: "fp64", 2: "df64_all"}[mode0],
@@ -492,8 +515,24 @@ def run_gpu(args):
                                          "the Dyson inversion and the nb >= 3 RPA (points with a conditioning "
                                          "estimate above 100 re-solved in FP64); tail fits and fit_derivatives "
                                          "samples in FP64" if mode0 == 0 else "see tprf_set_arithmetic",
-                    "fp64_path": {"value": world * points / (fp64_ms / 1e3), "unit": UNIT, "ms_per_step": fp64_ms}}
-        del chi_ref
+                    "fp64_path": {"value": world * points / (fp64_ms / 1e3), "unit": UNIT, "ms_per_step": fp64_ms,
+                                  "timing": "one step" if whole else "the step with the RPA and the comparison in "
+                                                                    "chunks of 32 frequencies (chi_ref did not fit)"}}
+        # how ill-conditioned the RPA is: chi = A^-1 chi0 with A = I - chi0 U amplifies a
+        # relative change of chi0 by up to ~kappa(A), so two FP64 implementations of the
+        # chain (chi0 ~1e-15 apart) agree on chi only to ~kappa x 1e-15. Measured on the
+        # static slice w = 0, where the RPA is closest to an instability; chi0 holds the
+        # FP64 step's chi0 here.
+        grouped = torch.swapaxes(chi0[nw - 1].reshape((nk,) + (nb,) * 4), -1, -2).reshape(nk, nb2, nb2)
+        A = torch.eye(nb2, dtype=chi0.dtype, device=dev) - grouped @ torch.swapaxes(U, -1, -2).reshape(nb2, nb2)
+        kappa = torch.linalg.cond(A)
+        accuracy["rpa_condition_w0"] = {
+            "kappa_max": float(kappa.max()), "kappa_median": float(kappa.median()),
+            "q_points_kappa_over_1e4": int((kappa > 1e4).sum()),
+            "fp64_agreement_floor": float(kappa.max()) * 1e-15,
+            "meaning": "2-norm condition number of I - chi0 U over q at w = 0; kappa x 1e-15 is the level at "
+                       "which two FP64 implementations of the chain agree on chi"}
+        del chi_ref, grouped, A, kappa
         torch.cuda.empty_cache()
 
     # ---- end to end through the public API, host buffers in and out
@@ -635,7 +674,9 @@ def run_gpu(args):
                    "parallelism": f"replicas x{world}"},
         "e2e": e2e,
         "accuracy": accuracy,
-        "gpu_launches": launches_per_step * args.steps,
+        # counted by the library (tprf_kernel_launches) over the timed steps; the
+        # expected count is launches_per_step per step
+        "gpu_launches": int(launches), "gpu_launches_expected": launches_per_step * args.steps,
         "roofline": roofline,
         "clocks": clocks.summary(),
         "autotune": autotune_info(lib, args),
@@ -692,12 +733,16 @@ def batched_leg(args, dev, lib, world, steps=3):
         torch.cuda.synchronize()
         barrier(world, dev)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        l0 = lib.tprf_kernel_launches()
         e0.record(stream)
         for _ in range(n):
             fn()
         e1.record(stream)
+        launched[fn.__name__] = int(lib.tprf_kernel_launches() - l0)
         torch.cuda.synchronize()
         return max_over_ranks(e0.elapsed_time(e1) / n, world, dev)
+
+    launched = {}
 
     def step():
         batch.forward()
@@ -752,9 +797,10 @@ def batched_leg(args, dev, lib, world, steps=3):
         "k_meshes": "{8,16,24,32,48}^2", "beta": "U[5,40]", "n_max": "7-smooth nearest 12.8 beta in [32,512]",
         "points_per_step": points, "unit": UNIT, "steps": steps, "streams": args.streams,
         "launch": "forward graph (+ backward graph) per step", "graph_setup_s": round(setup_s, 2),
-        "forward": {"value": fwd_v, "ms_per_step": fwd_ms},
+        "forward": {"value": fwd_v, "ms_per_step": fwd_ms, "gpu_launches": launched["forward"]},
         "forward_plus_gradient": {"value": grad_v, "ms_per_step": grad_ms, "loss": "sum_i sum |chi_i|^2",
-                                  "gradients": "dL/dU, dL/de(k), dL/dt(R) of every instance"},
+                                  "gradients": "dL/dU, dL/de(k), dL/dt(R) of every instance",
+                                  "gpu_launches": launched["step"]},
         "plain_single_instance": {
             "instances_timed": len(insts),
             "forward": {"value": pf_v, "s_per_pass": plain_fwd_s,
@@ -803,10 +849,12 @@ def run_gpu_batched(args):
     barrier(world, dev)
     torch.cuda.synchronize()
     with clocks:
+        l0 = lib.tprf_kernel_launches()
         e0.record(stream)
         for _ in range(args.steps):
             batch.run()
         e1.record(stream)
+        launches = lib.tprf_kernel_launches() - l0
         torch.cuda.synchronize()
     barrier(world, dev)
     ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, world, dev)
@@ -836,7 +884,7 @@ def run_gpu_batched(args):
         "plain_single_instance": {"value": plain, "unit": UNIT, "instances_timed": n_plain,
                                   "path": "lattice_dyson_g0_wk -> imtime_bubble_chi0_wk -> solve_rpa_PH per instance"},
         "speedup_vs_plain_single_instance": value / plain,
-        "gpu_launches": None,
+        "gpu_launches": int(launches),
         "clocks": clocks.summary(),
         "autotune": autotune_info(lib, args),
     }
@@ -892,10 +940,12 @@ def run_gpu_batched_grad(args):
     barrier(world, dev)
     torch.cuda.synchronize()
     with clocks:
+        l0 = lib.tprf_kernel_launches()
         e0.record(stream)
         for _ in range(args.steps):
             step()
         e1.record(stream)
+        launches = lib.tprf_kernel_launches() - l0
         torch.cuda.synchronize()
     barrier(world, dev)
     _native.check(lib.tprf_check_device_status(stream.cuda_stream), "timed steps")
@@ -945,7 +995,7 @@ def run_gpu_batched_grad(args):
         "plain_single_instance": {"value": plain, "unit": UNIT, "instances_timed": n_plain,
                                   "path": "tprf_gb300.autodiff.chi_rpa forward + backward per instance"},
         "speedup_vs_plain_single_instance": value / plain,
-        "gpu_launches": None,
+        "gpu_launches": int(launches),
         "clocks": clocks.summary(),
         "autotune": autotune_info(lib, args),
     }
@@ -1003,18 +1053,21 @@ def run_gpu_grad(args):
         barrier(world, dev)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         t0 = time.perf_counter()
+        l0 = lib.tprf_kernel_launches()
         e0.record(stream)
         for _ in range(args.steps):
             step(backward)
         e1.record(stream)
+        n_launch = lib.tprf_kernel_launches() - l0
         torch.cuda.synchronize()
         wall = (time.perf_counter() - t0) / args.steps
-        return max_over_ranks(e0.elapsed_time(e1) / args.steps, world, dev), max_over_ranks(wall, world, dev)
+        return (max_over_ranks(e0.elapsed_time(e1) / args.steps, world, dev), max_over_ranks(wall, world, dev),
+                n_launch)
 
-    fwd_ms, _ = timed(False)
+    fwd_ms, _, _ = timed(False)
     clocks = ClockSampler(local)
     with clocks:
-        ms, wall_s = timed(True)
+        ms, wall_s, launches = timed(True)
     _native.check(lib.tprf_check_device_status(stream.cuda_stream), "timed steps")
     nb = model.patterns[0][(1, 0)].shape[0]
     line = {
@@ -1030,7 +1083,7 @@ def run_gpu_grad(args):
         "e2e": {"value": world * points / wall_s, "unit": UNIT,
                 "h2d_bytes_per_step": int(theta_h.numel() * 8 + U_h.numel() * 16),
                 "d2h_bytes_per_step": int(grads_h.numel() * 8 + 8)},
-        "gpu_launches": None,
+        "gpu_launches": int(launches),
         "clocks": clocks.summary(),
         "autotune": autotune_info(lib, args),
     }

@@ -59,6 +59,12 @@ const char *tprf_version(void);
 void tprf_set_sync_checks(int on);
 int tprf_check_device_status(void *stream);
 
+/* Kernels this library has put on the GPU since the process started: one per
+ * launch of one of its kernels, and the kernel count of one of its graphs
+ * (tprf_batch_*) each time that graph is launched. Process-wide. No reference
+ * counterpart. */
+unsigned long long tprf_kernel_launches(void);
+
 /* Bound of the device-side waits of the TMA-staged lattice pass on the tile
  * copies it has in flight, in nanoseconds of the GPU's global timer (default
  * 200 ms; 0 makes every such wait give up at once). A wait that runs out sets

@@ -37,6 +37,7 @@ SIGNATURES = {
     "tprf_version": (ctypes.c_char_p, []),
     "tprf_set_sync_checks": (None, [c_int]),
     "tprf_check_device_status": (c_int, [c_void_p]),
+    "tprf_kernel_launches": (ctypes.c_ulonglong, []),
     "tprf_set_device_wait_limit_ns": (c_int, [ctypes.c_longlong]),
     "tprf_set_arithmetic": (c_int, [c_int]),
     "tprf_get_arithmetic": (c_int, []),

@@ -45,6 +45,7 @@ struct tprf_batch {
   std::vector<cudaEvent_t> events;
   cudaGraph_t graph = nullptr, graph_bwd = nullptr;
   cudaGraphExec_t exec = nullptr, exec_bwd = nullptr;
+  unsigned long long kernels = 0, kernels_bwd = 0;  // kernel launches captured into each graph
 };
 
 namespace {
@@ -229,10 +230,11 @@ void destroy_parts(tprf_batch *b) {
 // stream, forked from and joined into streams[0], into one graph.
 template <class Body>
 int capture(tprf_batch *b, const std::vector<std::vector<int>> &per, uintptr_t base, Body body, cudaGraph_t *graph,
-            cudaGraphExec_t *exec) {
+            cudaGraphExec_t *exec, unsigned long long *kernels) {
   const int K = b->n_streams;
   cudaStream_t s0 = b->streams[0];
   TPRF_CUDA(cudaStreamBeginCapture(s0, cudaStreamCaptureModeThreadLocal));
+  begin_capture_tally();
   int st = TPRF_OK;
   cudaEventRecord(b->events[K], s0);
   for (int k = 1; k < K; ++k) cudaStreamWaitEvent(b->streams[k], b->events[K], 0);
@@ -246,6 +248,7 @@ int capture(tprf_batch *b, const std::vector<std::vector<int>> &per, uintptr_t b
     cudaStreamWaitEvent(s0, b->events[k], 0);
   }
   cudaError_t e = cudaStreamEndCapture(s0, graph);
+  *kernels = end_capture_tally();
   if (st == TPRF_OK && e != cudaSuccess) st = cuda_status(e, "batch_create: capture");
   if (st == TPRF_OK) {
     e = cudaGraphInstantiate(exec, *graph, 0);
@@ -308,8 +311,8 @@ int create_batch(const tprf_instance *inst, const tprf_grad_instance *grad, int 
   }
   cudaError_t e = cudaStreamSynchronize(s0);
   if (e != cudaSuccess) return fail(cuda_status(e, "batch_create: first run"));
-  int st = capture(b.get(), A.per, base, fwd, &b->graph, &b->exec);
-  if (!st && grad) st = capture(b.get(), A.per, base, bwd, &b->graph_bwd, &b->exec_bwd);
+  int st = capture(b.get(), A.per, base, fwd, &b->graph, &b->exec, &b->kernels);
+  if (!st && grad) st = capture(b.get(), A.per, base, bwd, &b->graph_bwd, &b->exec_bwd, &b->kernels_bwd);
   if (st) return fail(st);
   *out = b.release();
   return TPRF_OK;
@@ -357,6 +360,7 @@ extern "C" int tprf_batch_backward(tprf_batch *b, void *stream) {
   if (!b || !b->exec_bwd) return set_error(TPRF_ERR_INVALID_ARGUMENT, "batch_backward: not a gradient batch");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   TPRF_CUDA(cudaGraphLaunch(b->exec_bwd, s));
+  count_graph_launch(b->kernels_bwd);
   return finish_with_checks(s, "batch_backward");
 }
 
@@ -364,6 +368,7 @@ extern "C" int tprf_batch_run(tprf_batch *b, void *stream) {
   if (!b || !b->exec) return set_error(TPRF_ERR_INVALID_ARGUMENT, "batch_run: not a batch");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   TPRF_CUDA(cudaGraphLaunch(b->exec, s));
+  count_graph_launch(b->kernels);
   return finish_with_checks(s, "batch_run");
 }
 

@@ -152,7 +152,7 @@ int launch_dyson_nb(double beta, int n_iw, long n_k, double mu, const double2 *e
     else
       dyson_kernel<NB, cdf><<<(unsigned)blocks, threads, 0, stream>>>(beta, n_iw, n_k, mu, e_k, sigma, sigma_kind, g,
                                                                       status);
-    TPRF_LAUNCH_CHECK("dyson_kernel");
+    TPRF_KERNEL_LAUNCHED("dyson_kernel");
     return TPRF_OK;
   };
   int threads = 128;
@@ -261,7 +261,7 @@ int launch_dyson_adjoint_nb(int n_nu, long n_k, const double2 *g, const double2 
   const long slices = std::max(1L, std::min((long)((n_nu + kWarps - 1) / kWarps), (target + k_tiles - 1) / k_tiles));
   if (k_tiles > 0x7fffffffL) return set_error(TPRF_ERR_UNSUPPORTED_SIZE, "lattice_dyson_g_wk_adjoint: too many k");
   dyson_adjoint_kernel<NB><<<dim3((unsigned)k_tiles, (unsigned)slices), 32 * kWarps, 0, s>>>(n_nu, n_k, g, gg, ekg);
-  TPRF_LAUNCH_CHECK("dyson_adjoint_kernel");
+  TPRF_KERNEL_LAUNCHED("dyson_adjoint_kernel");
   return TPRF_OK;
 }
 

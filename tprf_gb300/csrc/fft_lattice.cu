@@ -233,7 +233,7 @@ int launch_axis_as(const void *in, void *out, long outer, int n, long inner, dou
   auto kern = lattice_axis_kernel<FWD, E, IN_DF, OUT_DF>;
   TPRF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   kern<<<(unsigned)blocks, 256, smem, stream>>>(in, out, ncols_total, inner, ncol, lg, d, scale, skip, mir);
-  TPRF_LAUNCH_CHECK("lattice_axis_kernel");
+  TPRF_KERNEL_LAUNCHED("lattice_axis_kernel");
   return TPRF_OK;
 }
 
@@ -441,7 +441,7 @@ int launch_plane_as(const void *in, void *out, long outer, int n1, int n2, long 
   TPRF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   kern<<<(unsigned)tiles, 256, smem, stream>>>(in, out, outer, n_target, nt, log2i(nt), d1, d2, log2i(n2), scale,
                                                skip, mir);
-  TPRF_LAUNCH_CHECK("lattice_plane_kernel");
+  TPRF_KERNEL_LAUNCHED("lattice_plane_kernel");
   return TPRF_OK;
 }
 
@@ -494,7 +494,7 @@ int launch_plane_tma_nt(const void *in, bool in_df, void *out, bool out_df, long
   const long grid = std::max(1L, std::min(tiles, (long)num_sms() * std::max(1, per_sm)));
   kern<<<(unsigned)grid, 256, smem, stream>>>(map, out, outer, n_target, nt, log2i(nt), d1, d2, log2i(n2), scale,
                                               status, device_wait_limit_ns());
-  TPRF_LAUNCH_CHECK("lattice_plane_tma_kernel");
+  TPRF_KERNEL_LAUNCHED("lattice_plane_tma_kernel");
   return TPRF_OK;
 }
 
@@ -591,7 +591,7 @@ int launch_lattice_fft_fmt(bool forward, long n_w, const int dims[3], long n_tar
     } else {
       scale_copy_kernel<<<(unsigned)std::min((n + 255) / 256, (long)num_sms() * 8), 256, 0, stream>>>(src, dst, n,
                                                                                                       scale_last);
-      TPRF_LAUNCH_CHECK("scale_copy_kernel");
+      TPRF_KERNEL_LAUNCHED("scale_copy_kernel");
     }
     return TPRF_OK;
   }
@@ -836,7 +836,7 @@ int noalloc_axis(const double2 *in, double2 *out, long outer, long inner, const 
   TPRF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   kern<<<(unsigned)blocks, 256, smem, stream>>>(in, out, ncols_total, inner, ncol, lg, d, scale, SkipRows{nullptr, 0},
                                                 kNoRowMirror);
-  TPRF_LAUNCH_CHECK("lattice_axis_kernel (no-alloc)");
+  TPRF_KERNEL_LAUNCHED("lattice_axis_kernel (no-alloc)");
   return TPRF_OK;
 }
 
@@ -888,7 +888,7 @@ extern "C" int tprf_fourier_lattice_noalloc(int forward, long n_w, const int dim
     desc[i].twf = twf;
     desc[i].rev = rev;
     noalloc_tables_kernel<<<(n + 255) / 256, 256, 0, s>>>(desc[i], tw, twf, rev);
-    TPRF_LAUNCH_CHECK("noalloc_tables_kernel");
+    TPRF_KERNEL_LAUNCHED("noalloc_tables_kernel");
     off += noalloc_table_bytes(n);
   }
   const long nk = (long)dims[0] * dims[1] * dims[2];

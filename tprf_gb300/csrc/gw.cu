@@ -66,7 +66,7 @@ extern "C" int tprf_gw_dynamic_sigma(long n_tau, long n_r, int nb, const double 
   gw_sigma_kernel<<<(unsigned)grid_of(n_out), 256, 0, s>>>(n_out, nb, reinterpret_cast<const double2 *>(W_tr),
                                                           reinterpret_cast<const double2 *>(g_tr),
                                                           reinterpret_cast<double2 *>(sigma_tr));
-  TPRF_LAUNCH_CHECK("gw_sigma_kernel");
+  TPRF_KERNEL_LAUNCHED("gw_sigma_kernel");
   return TPRF_OK;
 }
 
@@ -98,6 +98,6 @@ extern "C" int tprf_split_into_dynamic_wk_and_constant_k(double beta, int nw, lo
                                                                reinterpret_cast<const double2 *>(chi_wk),
                                                                reinterpret_cast<double2 *>(chi_dyn_wk),
                                                                reinterpret_cast<double2 *>(chi_const_k));
-  TPRF_LAUNCH_CHECK("split_const_kernel");
+  TPRF_KERNEL_LAUNCHED("split_const_kernel");
   return TPRF_OK;
 }

@@ -28,6 +28,20 @@ int cuda_status(cudaError_t e, const char *what);
     if (e_ != cudaSuccess) return ::tprf::cuda_status(e_, what);     \
   } while (0)
 
+// Kernel launches of this library (tprf_kernel_launches): count_launch() at
+// every launch site; while this thread captures one of the library's own
+// graphs the launches go to its capture tally instead, and every launch of
+// such a graph adds the kernels it holds (count_graph_launch).
+void count_launch();
+void count_graph_launch(unsigned long long kernels);
+void begin_capture_tally();
+unsigned long long end_capture_tally();
+#define TPRF_KERNEL_LAUNCHED(what) \
+  do {                             \
+    ::tprf::count_launch();        \
+    TPRF_LAUNCH_CHECK(what);       \
+  } while (0)
+
 bool sync_checks_enabled();
 // Bound (ns of the GPU's global timer) of the device-side waits on copies in
 // flight (the TMA-staged passes); tprf_set_device_wait_limit_ns.

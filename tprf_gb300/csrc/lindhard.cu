@@ -176,13 +176,13 @@ extern "C" int tprf_lindhard_chi00(long n_k, const int dims[3], int nb, const do
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const long eb = std::max(1L, std::min((n_k + 127) / 128, (long)num_sms() * 16));
   hermitian_eig_kernel<<<(unsigned)eb, 128, 0, s>>>(n_k, nb, reinterpret_cast<const double2 *>(e_k), mu, evals, evecs);
-  TPRF_LAUNCH_CHECK("hermitian_eig_kernel");
+  TPRF_KERNEL_LAUNCHED("hermitian_eig_kernel");
   const size_t smem = 2 * nb * nb * sizeof(double2) + 4 * nb * sizeof(double);
   const long n_out = (2L * nw - 1) * nb * nb * nb * nb;
   const long blocks = n_k * ((n_out + 256 * kPer - 1) / (256 * kPer));
   if (blocks > 0x7fffffffL) return set_error(TPRF_ERR_UNSUPPORTED_SIZE, "lindhard_chi00: mesh too large");
   lindhard_kernel<<<(unsigned)blocks, 256, smem, s>>>(n_k, dims[0], dims[1], dims[2], nb, nw, beta, evals, evecs,
                                                    reinterpret_cast<double2 *>(chi_wk));
-  TPRF_LAUNCH_CHECK("lindhard_kernel");
+  TPRF_KERNEL_LAUNCHED("lindhard_kernel");
   return TPRF_OK;
 }

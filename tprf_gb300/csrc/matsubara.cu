@@ -818,7 +818,7 @@ int launch_tau_to_w_as(const TauWPlan *p, Loader ld, double2 *out, long C, cudaS
                                        (int)sm));
         tau_to_w_kernel<Loader, E, true><<<(unsigned)blocks, kMatsubaraThreads, sm, stream>>>(pv, ld, fr, out, C, icv,
                                                                                               log2_ic(icv), out_df, skip_neg);
-        TPRF_LAUNCH_CHECK("tau_to_w_kernel");
+        TPRF_KERNEL_LAUNCHED("tau_to_w_kernel");
         return TPRF_OK;
       }
     }
@@ -826,7 +826,7 @@ int launch_tau_to_w_as(const TauWPlan *p, Loader ld, double2 *out, long C, cudaS
                                    (int)sm));
     tau_to_w_kernel<Loader, E, false><<<(unsigned)blocks, kMatsubaraThreads, sm, stream>>>(pv, ld, fr, out, C, icv,
                                                                                            log2_ic(icv), out_df, skip_neg);
-    TPRF_LAUNCH_CHECK("tau_to_w_kernel");
+    TPRF_KERNEL_LAUNCHED("tau_to_w_kernel");
     return TPRF_OK;
   };
   auto launch = [&](int icv, long n_cols) -> int { return launch_rv(icv, n_cols, radix); };
@@ -1189,7 +1189,7 @@ int launch_hermitian_check(int n_iw, long C, const double2 *gw, unsigned *hwords
   const bool layout = dims && nb > 0 && (long)dims[0] * dims[1] * dims[2] * nb * nb == C && C < 0x7fffffffL;
   hermitian_check_kernel<<<blocks, 256, 0, stream>>>(gw, n_iw, C, hwords, layout ? nb : 0, layout ? dims[0] : 1,
                                                      layout ? dims[1] : 1, layout ? dims[2] : 1);
-  TPRF_LAUNCH_CHECK("hermitian_check_kernel");
+  TPRF_KERNEL_LAUNCHED("hermitian_check_kernel");
   return TPRF_OK;
 }
 
@@ -1241,7 +1241,7 @@ int launch_nu_to_tau_stat(double beta, int n_iw, int n_tau, bool fermion, long C
                                                                                   tp ? tp->pairs : nullptr,
                                                                                   tp ? tp->n_can : 0L);
     }
-    TPRF_LAUNCH_CHECK("nu_to_tau_kernel");
+    TPRF_KERNEL_LAUNCHED("nu_to_tau_kernel");
     return TPRF_OK;
   };
   auto launch = [&](int icv, long n_cols) -> int { return launch_rv(icv, n_cols, radix); };
@@ -1330,7 +1330,7 @@ int launch_chi0_w0r_from_grt(double beta, int n_tau, const int dims[3], int nb, 
   const BubbleLoader ld = make_bubble(g, n_tau, dims, nb);
   const long C = ld.Nr * nb * nb * nb * nb;
   trapz_kernel<BubbleLoader><<<(unsigned)grid_for(C, 256), 256, 0, stream>>>(ld, chi0_wr, C, n_tau, beta);
-  TPRF_LAUNCH_CHECK("trapz_kernel<bubble>");
+  TPRF_KERNEL_LAUNCHED("trapz_kernel<bubble>");
   return TPRF_OK;
 }
 
@@ -1394,7 +1394,7 @@ extern "C" int tprf_chi_w0r_from_chi_tr(double beta, int n_tau, long n_r, long n
   const long C = n_r * n_target;
   trapz_kernel<ArrayLoader><<<(unsigned)grid_for(C, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
       ArrayLoader{reinterpret_cast<const double2 *>(chi_tr), C}, reinterpret_cast<double2 *>(chi_wr), C, n_tau, beta);
-  TPRF_LAUNCH_CHECK("trapz_kernel<array>");
+  TPRF_KERNEL_LAUNCHED("trapz_kernel<array>");
   return TPRF_OK;
 }
 
@@ -1406,7 +1406,7 @@ extern "C" int tprf_chi0_tr_from_grt_PH(int n_tau, const int dims[3], int nb, co
   const long C = ld.Nr * nb * nb * nb * nb;
   bubble_kernel<<<(unsigned)grid_for(C * n_tau, 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
       ld, reinterpret_cast<double2 *>(chi0_tr), C);
-  TPRF_LAUNCH_CHECK("bubble_kernel");
+  TPRF_KERNEL_LAUNCHED("bubble_kernel");
   return TPRF_OK;
 }
 
@@ -1452,7 +1452,7 @@ int launch_tau_to_w_adjoint(double beta, int n_tau, int nw, long C, const double
   auto kern = arith_mode() == kArithFP64 ? tau_to_w_adjoint_kernel<double2> : tau_to_w_adjoint_kernel<cdf>;
   TPRF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   kern<<<(unsigned)((C + ic - 1) / ic), 256, smem, stream>>>(*p, make_vinv_rows(), yg, xg, C, ic, lg, BubbleLoader{});
-  TPRF_LAUNCH_CHECK("tau_to_w_adjoint_kernel");
+  TPRF_KERNEL_LAUNCHED("tau_to_w_adjoint_kernel");
   return TPRF_OK;
 }
 
@@ -1476,7 +1476,7 @@ int launch_chi0_wr_from_grt_adjoint(double beta, int n_tau, int nw, const int di
   auto kern = arith_mode() == kArithFP64 ? tau_to_w_adjoint_kernel<double2, true> : tau_to_w_adjoint_kernel<cdf, true>;
   TPRF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   kern<<<(unsigned)((C + ic - 1) / ic), 256, smem, stream>>>(*p, make_vinv_rows(), yg, gg, C, ic, lg, ld);
-  TPRF_LAUNCH_CHECK("tau_to_w_adjoint_kernel<fused bubble>");
+  TPRF_KERNEL_LAUNCHED("tau_to_w_adjoint_kernel<fused bubble>");
   return TPRF_OK;
 }
 
@@ -1493,7 +1493,7 @@ int launch_nu_to_tau_adjoint(double beta, int n_iw, int n_tau, long C, const dou
   auto kern = arith_mode() == kArithFP64 ? nu_to_tau_adjoint_kernel<double2> : nu_to_tau_adjoint_kernel<cdf>;
   TPRF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   kern<<<(unsigned)((C + ic - 1) / ic), 256, smem, stream>>>(*p, yg, gg, C, ic, lg, fitted ? 1 : 0);
-  TPRF_LAUNCH_CHECK("nu_to_tau_adjoint_kernel");
+  TPRF_KERNEL_LAUNCHED("nu_to_tau_adjoint_kernel");
   return TPRF_OK;
 }
 
@@ -1505,7 +1505,7 @@ int launch_bubble_adjoint(int n_tau, const int dims[3], int nb, const double2 *g
   const BubbleLoader ld = make_bubble(g_tr, n_tau, dims, nb);
   const long total = (long)n_tau * ld.Nr * nb * nb;
   bubble_adjoint_kernel<<<(unsigned)grid_for(total, 256), 256, 0, stream>>>(ld, chig, gg);
-  TPRF_LAUNCH_CHECK("bubble_adjoint_kernel");
+  TPRF_KERNEL_LAUNCHED("bubble_adjoint_kernel");
   return TPRF_OK;
 }
 

@@ -83,6 +83,25 @@ int cuda_status(cudaError_t e, const char *what) {
 
 bool sync_checks_enabled() { return g_sync_checks.load(); }
 
+std::atomic<unsigned long long> g_kernel_launches{0};
+thread_local bool t_tallying = false;
+thread_local unsigned long long t_tally = 0;
+void count_launch() {
+  if (t_tallying)
+    ++t_tally;
+  else
+    g_kernel_launches.fetch_add(1, std::memory_order_relaxed);
+}
+void count_graph_launch(unsigned long long kernels) { g_kernel_launches.fetch_add(kernels, std::memory_order_relaxed); }
+void begin_capture_tally() {
+  t_tallying = true;
+  t_tally = 0;
+}
+unsigned long long end_capture_tally() {
+  t_tallying = false;
+  return t_tally;
+}
+
 int arith_mode() { return g_arith.load(); }
 
 std::atomic<unsigned long long> g_wait_limit_ns{200000000ull};  // 200 ms
@@ -728,6 +747,8 @@ extern "C" const char *tprf_last_error(void) { return tprf::g_last_error.c_str()
 extern "C" const char *tprf_version(void) { return "0.1.0"; }
 
 extern "C" void tprf_set_sync_checks(int on) { tprf::g_sync_checks.store(on != 0); }
+
+extern "C" unsigned long long tprf_kernel_launches(void) { return tprf::g_kernel_launches.load(); }
 
 extern "C" int tprf_set_arithmetic(int mode) {
   if (mode != TPRF_ARITH_DF64 && mode != TPRF_ARITH_FP64 && mode != TPRF_ARITH_DF64_ALL)

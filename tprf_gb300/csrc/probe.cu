@@ -50,7 +50,7 @@ extern "C" int tprf_measure_fp64_tflops(double *tflops, void *scratch, size_t sc
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  TPRF_LAUNCH_CHECK("fp64_fma_probe");
+  TPRF_KERNEL_LAUNCHED("fp64_fma_probe");
   *tflops = best;
   return TPRF_OK;
 }

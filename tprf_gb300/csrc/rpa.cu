@@ -280,7 +280,7 @@ int launch_rpa_pair_as(int nw, const int dims[3], const double2 *chi0, const dou
   long blocks = (units + NT - 1) / NT;
   blocks = std::max(1L, std::min(blocks, (long)num_sms() * 64));
   kern<<<(unsigned)blocks, NT, smem, stream>>>(nw, dims[0], dims[1], dims[2], chi0, U, out, status);
-  TPRF_LAUNCH_CHECK("rpa_lu_pair_kernel");
+  TPRF_KERNEL_LAUNCHED("rpa_lu_pair_kernel");
   return TPRF_OK;
 }
 
@@ -296,7 +296,7 @@ int launch_rpa_as(long n_points, const double2 *chi0, const double2 *U, double2 
   const long cap = (long)num_sms() * 64;
   blocks = std::max(1L, std::min(blocks, cap));
   rpa_lu_kernel<NB, NT, E><<<(unsigned)blocks, NT, smem, stream>>>(n_points, chi0, U, chi, status);
-  TPRF_LAUNCH_CHECK("rpa_lu_kernel");
+  TPRF_KERNEL_LAUNCHED("rpa_lu_kernel");
   return TPRF_OK;
 }
 
@@ -648,7 +648,7 @@ int launch_rpa_adjoint_point(long n_points, const double2 *chi0, const double2 *
   long blocks = (n_points + NT - 1) / NT;
   blocks = std::max(1L, std::min(blocks, (long)num_sms() * std::max(1, per_sm)));
   kern<<<(unsigned)blocks, NT, smem, stream>>>(n_points, chi0, U, chi, chig, chi0g, Ug, status);
-  TPRF_LAUNCH_CHECK("rpa_adjoint_point_kernel");
+  TPRF_KERNEL_LAUNCHED("rpa_adjoint_point_kernel");
   return TPRF_OK;
 }
 

@@ -518,7 +518,7 @@ int launch_as(long n_points, int nb, const double2 *chi0, const double2 *U, doub
   long blocks = (n_points + per_block - 1) / per_block;
   blocks = std::max(1L, std::min(blocks, (long)num_sms() * (best_total / best_w) * 8));
   rpa_warp_kernel<E, G, NBC><<<(unsigned)blocks, 32 * best_w, smem, stream>>>(n_points, nb, chi0, U, chi, status);
-  TPRF_LAUNCH_CHECK("rpa_warp_kernel");
+  TPRF_KERNEL_LAUNCHED("rpa_warp_kernel");
   return TPRF_OK;
 }
 
@@ -792,7 +792,7 @@ int launch_pair_as(int nw, const int dims[3], int nb, const double2 *chi0, const
     long blocks = (units + per_block - 1) / per_block;
     blocks = std::max(1L, std::min(blocks, (long)num_sms() * (best_total / best_w) * 8));
     kern<<<(unsigned)blocks, 32 * best_w, smem, stream>>>(nw, dims[0], dims[1], dims[2], nb, chi0, U, part, status);
-    TPRF_LAUNCH_CHECK("rpa_pair_kernel");
+    TPRF_KERNEL_LAUNCHED("rpa_pair_kernel");
   }
   return TPRF_OK;
 }
@@ -905,7 +905,7 @@ int launch_rpa_adjoint_warp(long n_points, int nb, const double2 *chi0, const do
   blocks = std::max(1L, std::min(blocks, (long)num_sms() * (best_total / best_w)));
   rpa_adjoint_warp_kernel<<<(unsigned)blocks, 32 * best_w, smem, stream>>>(n_points, nb, chi0, U, chi, chig, chi0g,
                                                                           Ug, status);
-  TPRF_LAUNCH_CHECK("rpa_adjoint_warp_kernel");
+  TPRF_KERNEL_LAUNCHED("rpa_adjoint_warp_kernel");
   return TPRF_OK;
 }
 
@@ -922,7 +922,7 @@ int launch_screened_w(long n_points, long nk, int nb, bool swap, bool v_per_poin
   blocks = std::max(1L, std::min(blocks, (long)num_sms() * 16));
   screened_w_kernel<<<(unsigned)blocks, 32 * warps, smem, stream>>>(n_points, nk, nb, swap ? 1 : 0,
                                                                      v_per_point ? 1 : 0, PI, V, W, status);
-  TPRF_LAUNCH_CHECK("screened_w_kernel");
+  TPRF_KERNEL_LAUNCHED("screened_w_kernel");
   return TPRF_OK;
 }
 
