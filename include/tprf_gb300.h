@@ -46,6 +46,7 @@ extern "C" {
 #define TPRF_ERR_CUDA (-6)              /* a CUDA runtime call failed */
 #define TPRF_ERR_ALLOC (-7)             /* device allocation failed or workspace too small */
 #define TPRF_ERR_SINGULAR (-8)          /* exactly singular matrix in Dyson or RPA */
+#define TPRF_ERR_RANGE (-9)             /* double-float chain: max |G(iv, r)| outside [1e-15, 1e15] (use TPRF_ARITH_FP64) */
 
 const char *tprf_status_string(int status);
 const char *tprf_last_error(void);

@@ -40,6 +40,7 @@ def test_status_strings(lib):
     assert lib.tprf_version().decode() == "0.1.0"
     assert lib.tprf_status_string(0).decode() == "ok"
     assert "tail" in lib.tprf_status_string(-4).decode()
+    assert "double-float range" in lib.tprf_status_string(-9).decode()
 
 
 def test_tail_fit_matrix_matches_oracle(lib):

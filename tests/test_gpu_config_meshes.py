@@ -179,3 +179,53 @@ def test_real_bubble_threshold(cuda_lib, arithmetic, eps, real_path):
         assert not took_real
     elif real_path is not None:
         assert took_real == real_path
+
+
+def _scaled_non_hermitian_g0(scale, dims, beta, n_max, nb=2, seed=7):
+    """G0(iv, k) of a random non-Hermitian e(k) (so G(-iv) != G(iv)^dagger and the
+    real-input words must say no), times `scale`: on the device and in the oracle."""
+    import tprf_gb300 as T
+    rng = np.random.default_rng(seed)
+    nk = int(np.prod(dims))
+    ek = rng.standard_normal((nk, nb, nb)) + 1j * rng.standard_normal((nk, nb, nb))
+    g0 = T.lattice_dyson_g0_wk(0.0, T.Gf(mesh=T.MeshBrZone(dims=dims), data=ek), T.MeshImFreq(beta, "Fermion", n_max))
+    g0.data.mul_(scale)
+    return g0, scale * O.lattice_dyson_g0_wk(0.0, ek, beta, n_max)
+
+
+@pytest.mark.parametrize("scale", [1e-12, 1e8])
+def test_scaled_non_hermitian_g_takes_the_complex_path(cuda_lib, arithmetic, scale):
+    """Far from 1 but inside the double-float range: the decision words compare
+    magnitudes (no squares to overflow or underflow), send the non-Hermitian G down
+    the complex path, and chi0 meets the parity bar."""
+    import tprf_gb300 as T
+    dims, beta, n_max, nw = (4, 4, 1), 6.0, 32, 4
+    cuda_lib.tprf_set_sync_checks(1)
+    g0, ref_g = _scaled_non_hermitian_g0(scale, dims, beta, n_max)
+    chi0 = T.imtime_bubble_chi0_wk(g0, nw=nw, verbose=False)
+    ref0 = O.imtime_bubble_chi0_wk(ref_g, beta, dims, nw=nw)
+    assert rel_err(chi0.data, ref0) < PARITY_RTOL
+
+
+@pytest.mark.parametrize("scale", [1e-25, 1e25])
+def test_chain_outside_the_double_float_range_is_reported(cuda_lib, scale):
+    """max |G| beyond [1e-15, 1e15]: the double-float chain (FP32 exponent range)
+    reports TPRF_ERR_RANGE and names the FP64 mode instead of returning a chi0
+    whose products overflowed or lost their low words; the FP64 mode computes it
+    (shown at 1e-25, where the absolute tail-fit residual stays small)."""
+    import tprf_gb300 as T
+    from tprf_gb300._native import TprfError
+    dims, beta, n_max, nw = (4, 4, 1), 6.0, 32, 4
+    cuda_lib.tprf_set_sync_checks(1)
+    assert cuda_lib.tprf_set_arithmetic(0) == 0
+    g0, ref_g = _scaled_non_hermitian_g0(scale, dims, beta, n_max)
+    with pytest.raises(TprfError) as err:
+        T.imtime_bubble_chi0_wk(g0, nw=nw, verbose=False)
+    assert err.value.status == -9 and "TPRF_ARITH_FP64" in str(err.value)
+    if scale < 1:
+        assert cuda_lib.tprf_set_arithmetic(1) == 0
+        try:
+            chi0 = T.imtime_bubble_chi0_wk(g0, nw=nw, verbose=False)
+        finally:
+            cuda_lib.tprf_set_arithmetic(0)
+        assert rel_err(chi0.data, O.imtime_bubble_chi0_wk(ref_g, beta, dims, nw=nw)) < PARITY_RTOL

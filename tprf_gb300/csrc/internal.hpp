@@ -53,7 +53,12 @@ enum : unsigned {
   kDevErrSingular = 2u,     // zero pivot in Dyson / RPA
   kDevErrNonFinite = 4u,    // NaN / Inf in a result
   kDevErrTimeout = 8u,      // bounded wait expired (persistent kernels)
+  kDevErrRange = 16u,       // data outside the double-float chain's exponent range
 };
+// The double-float chain keeps FP32's exponent range (~1e+-38): the bubble's
+// products of G and their transforms stay inside it, with their low words, while
+// max |G(iv, r)| lies in [kDfGMin, kDfGMax] (or G is zero).
+constexpr float kDfGMin = 1e-15f, kDfGMax = 1e15f;
 unsigned *device_status_word();  // nullptr on failure (error set)
 // Reads and clears the device word after synchronising `stream`.
 int finish_with_checks(cudaStream_t stream, const char *what);

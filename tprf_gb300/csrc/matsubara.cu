@@ -148,6 +148,10 @@ __global__ void __launch_bounds__(kMatsubaraThreads, 2) nu_to_tau_kernel(NuTauPl
   // stored at that column and at its partner tpairs[f].y.
   bool pairs = false, canon = false;
   if constexpr (IsDfElem<C>::value) {
+    if (hwords != nullptr && status != nullptr && blockIdx.x == 0 && tid == 0) {
+      const float gm = __uint_as_float(hwords[0]);  // max |G(iv, r)|; inf when beyond FP32
+      if (!(gm <= kDfGMax) || (gm > 0.f && gm < kDfGMin)) atomicOr(status, kDevErrRange);
+    }
     pairs = hermitian_says_yes(hwords);
     canon = pairs && tpairs != nullptr && transpose_says_yes(hwords);
   }

@@ -139,6 +139,9 @@ int read_and_clear_status(cudaStream_t stream, unsigned *flags) {
 }
 
 int status_from_flags(unsigned f, const char *what) {
+  if (f & kDevErrRange)
+    return set_error(TPRF_ERR_RANGE, std::string(what) + ": max |G| outside [1e-15, 1e15], the double-float range "
+                                                         "of the chain; run it with TPRF_ARITH_FP64");
   if (f & kDevErrTailFit)
     return set_error(TPRF_ERR_TAIL_FIT, std::string(what) + ": high frequency moments have an error greater than 1e-3");
   if (f & kDevErrSingular) return set_error(TPRF_ERR_SINGULAR, std::string(what) + ": singular matrix");
@@ -738,6 +741,7 @@ extern "C" const char *tprf_status_string(int status) {
     case TPRF_ERR_CUDA: return "CUDA error";
     case TPRF_ERR_ALLOC: return "allocation failed or workspace too small";
     case TPRF_ERR_SINGULAR: return "singular matrix";
+    case TPRF_ERR_RANGE: return "values outside the double-float range";
     default: return "unknown status";
   }
 }
