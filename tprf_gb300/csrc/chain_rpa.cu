@@ -266,11 +266,11 @@ void fold_split_rates(CopyCtx *c) {
   for (long k = std::max(0L, c->calls - kRecords); k < c->calls; ++k) fold_record(c, &c->rec[k % kRecords]);
 }
 std::mutex g_copy_mu;
-std::map<int, CopyCtx> g_copy;
+std::map<unsigned long long, CopyCtx> g_copy;  // per context (its streams and events die with it)
 
 int copy_ctx(CopyCtx **out) {
-  int dev = 0;
-  TPRF_CUDA(cudaGetDevice(&dev));
+  unsigned long long dev = 0;
+  if (int st = current_context_key(&dev)) return st;
   std::lock_guard<std::mutex> lock(g_copy_mu);
   CopyCtx &c = g_copy[dev];
   if (!c.ready) {

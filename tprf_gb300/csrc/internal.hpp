@@ -60,6 +60,12 @@ enum : unsigned {
 // max |G(iv, r)| lies in [kDfGMin, kDfGMax] (or G is zero).
 constexpr float kDfGMin = 1e-15f, kDfGMax = 1e15f;
 unsigned *device_status_word();  // nullptr on failure (error set)
+// The current device's context as a cache key: its unique id (cuCtxGetId). The
+// plans, the status word and the copy stream belong to a context, which
+// cudaDeviceReset destroys; the device's next context has another id, so
+// nothing cached for the old one is handed out. The device number (with the top
+// bit set) where the driver has no cuCtxGetId.
+int current_context_key(unsigned long long *key);
 // Reads and clears the device word after synchronising `stream`.
 int finish_with_checks(cudaStream_t stream, const char *what);
 

@@ -13,6 +13,8 @@
 #include <tuple>
 #include <vector>
 
+#include <cuda.h>
+
 #include "internal.hpp"
 
 namespace tprf {
@@ -72,6 +74,39 @@ std::vector<cd> unit_roots(int L, double sign) {
 
 }  // namespace
 
+int current_context_key(unsigned long long *key) {
+  using GetCurrent = CUresult (*)(CUcontext *);
+  using GetId = CUresult (*)(CUcontext, unsigned long long *);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<GetCurrent>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<GetId>(f);
+  });
+  int dev = 0;
+  if (int st = current_device(&dev)) return st;
+  unsigned long long id = 0;
+  if (get_current && get_id) {
+    CUcontext ctx = nullptr;
+    if (get_current(&ctx) != CUDA_SUCCESS || ctx == nullptr) {
+      cudaError_t e = cudaFree(nullptr);  // the runtime creates the device's context on first use
+      if (e != cudaSuccess) return cuda_status(e, "cudaFree(nullptr)");
+      if (get_current(&ctx) != CUDA_SUCCESS) ctx = nullptr;
+    }
+    if (ctx == nullptr || get_id(ctx, &id) != CUDA_SUCCESS) id = 0;
+  }
+  *key = id != 0 ? id : ((1ull << 63) | (unsigned long long)dev);
+  return TPRF_OK;
+}
+
 int set_error(int status, const std::string &msg) {
   g_last_error = msg;
   return status;
@@ -108,9 +143,9 @@ std::atomic<unsigned long long> g_wait_limit_ns{200000000ull};  // 200 ms
 unsigned long long device_wait_limit_ns() { return g_wait_limit_ns.load(); }
 
 unsigned *device_status_word() {
-  static std::map<int, unsigned *> words;
-  int dev = 0;
-  if (current_device(&dev) != TPRF_OK) return nullptr;
+  static std::map<unsigned long long, unsigned *> words;
+  unsigned long long dev = 0;
+  if (current_context_key(&dev) != TPRF_OK) return nullptr;
   std::lock_guard<std::mutex> lock(g_mutex);
   auto it = words.find(dev);
   if (it != words.end()) return it->second;
@@ -257,10 +292,10 @@ int get_fft(int n, FftDesc *out) { return get_fft_variant(n, 0, out); }
 
 int get_fft_variant(int n, int variant, FftDesc *out) {
   if (n < 1) return set_error(TPRF_ERR_INVALID_ARGUMENT, "FFT length must be >= 1");
-  int dev = 0;
-  int st = current_device(&dev);
+  unsigned long long dev = 0;  // the context: plans die with it
+  int st = current_context_key(&dev);
   if (st) return st;
-  static std::map<std::tuple<int, int, int>, FftDesc> cache;
+  static std::map<std::tuple<unsigned long long, int, int>, FftDesc> cache;
   std::lock_guard<std::mutex> lock(g_mutex);
   auto key = std::make_tuple(dev, n, variant);
   auto it = cache.find(key);
@@ -460,10 +495,10 @@ int get_nu_tau_plan(double beta, int n_iw, int n_tau, const NuTauPlan **out) {
 // Matsubara -> tau for either statistic (fourier_matsubara.cpp:218-308): n is
 // the fermionic n_max or the bosonic nw.
 int get_nu_tau_plan_stat(double beta, int n, int n_tau, bool fermion, const NuTauPlan **out) {
-  int dev = 0;
-  int st = current_device(&dev);
+  unsigned long long dev = 0;  // the context: plans die with it
+  int st = current_context_key(&dev);
   if (st) return st;
-  static std::map<std::tuple<int, uint64_t, int, int, int>, std::unique_ptr<NuTauPlan>> cache;
+  static std::map<std::tuple<unsigned long long, uint64_t, int, int, int>, std::unique_ptr<NuTauPlan>> cache;
   uint64_t bbits;
   std::memcpy(&bbits, &beta, 8);
   auto key = std::make_tuple(dev, bbits, n, n_tau, fermion ? 1 : 0);
@@ -543,10 +578,10 @@ int get_tau_w_plan(double beta, int n_tau, int nw, const TauWPlan **out) {
 // the bosonic nw (outputs m = -(nw-1) .. nw-1) or the fermionic n_max
 // (outputs n = -n_max .. n_max-1).
 int get_tau_w_plan_stat(double beta, int n_tau, int n, bool fermion, const TauWPlan **out) {
-  int dev = 0;
-  int st = current_device(&dev);
+  unsigned long long dev = 0;  // the context: plans die with it
+  int st = current_context_key(&dev);
   if (st) return st;
-  static std::map<std::tuple<int, uint64_t, int, int, int>, std::unique_ptr<TauWPlan>> cache;
+  static std::map<std::tuple<unsigned long long, uint64_t, int, int, int>, std::unique_ptr<TauWPlan>> cache;
   uint64_t bbits;
   std::memcpy(&bbits, &beta, 8);
   auto key = std::make_tuple(dev, bbits, n_tau, n, fermion ? 1 : 0);
@@ -610,10 +645,10 @@ int get_tau_w_plan_stat(double beta, int n_tau, int n, bool fermion, const TauWP
 }
 
 int get_tail_fit_plan(double beta, int n, bool fermion, const TailFitPlan **out) {
-  int dev = 0;
-  int st = current_device(&dev);
+  unsigned long long dev = 0;  // the context: plans die with it
+  int st = current_context_key(&dev);
   if (st) return st;
-  static std::map<std::tuple<int, uint64_t, int, int>, std::unique_ptr<TailFitPlan>> cache;
+  static std::map<std::tuple<unsigned long long, uint64_t, int, int>, std::unique_ptr<TailFitPlan>> cache;
   uint64_t bbits;
   std::memcpy(&bbits, &beta, 8);
   auto key = std::make_tuple(dev, bbits, n, fermion ? 1 : 0);
@@ -641,10 +676,10 @@ int get_tail_fit_plan(double beta, int n, bool fermion, const TailFitPlan **out)
 }
 
 int get_transpose_pairs(const int dims[3], int nb, int rank, const TransposePairs **out) {
-  int dev = 0;
-  int st = current_device(&dev);
+  unsigned long long dev = 0;  // the context: plans die with it
+  int st = current_context_key(&dev);
   if (st) return st;
-  static std::map<std::tuple<int, int, int, int, int, int>, std::unique_ptr<TransposePairs>> cache;
+  static std::map<std::tuple<unsigned long long, int, int, int, int, int>, std::unique_ptr<TransposePairs>> cache;
   auto key = std::make_tuple(dev, dims[0], dims[1], dims[2], nb, rank);
   {
     std::lock_guard<std::mutex> lock(g_mutex);
