@@ -496,7 +496,7 @@ def test_hubbard_1d_fazekas_rpa_on_gpu(cuda_lib):
 
 
 @pytest.mark.parametrize("case", range(len(CASES)))
-@pytest.mark.parametrize("u_kind", ["real", "complex"])
+@pytest.mark.parametrize("u_kind", ["real", "complex", "kanamori"])
 def test_rpa_on_the_wk_mesh_equals_the_point_solve(cuda_lib, case, u_kind):
     """solve_rpa_PH on a chi0 Gf (mesh-aware C ABI: conjugate point pairs solved
     once where chi0 and U allow, and with a symmetric U the transposition
@@ -511,7 +511,11 @@ def test_rpa_on_the_wk_mesh_equals_the_point_solve(cuda_lib, case, u_kind):
     chi0 = T.imtime_bubble_chi0_wk(g_wk, nw=6, verbose=False)
     nb = ek.shape[-1]
     rng = np.random.default_rng(10 + case)
-    U = 0.3 * rng.standard_normal((nb,) * 4) + (0.1j * rng.standard_normal((nb,) * 4) if u_kind == "complex" else 0j)
+    if u_kind == "kanamori":  # real and symmetric in the grouped indices: transposition partners apply
+        from tprf_gb300.workloads import kanamori_spin_vertex
+        U = np.full((1, 1, 1, 1), 0.8 + 0j) if nb == 1 else np.asarray(kanamori_spin_vertex(nb, 0.8, 0.15), complex)
+    else:
+        U = 0.3 * rng.standard_normal((nb,) * 4) + (0.1j * rng.standard_normal((nb,) * 4) if u_kind == "complex" else 0j)
     chi = T.solve_rpa_PH(chi0, U)
     flat = torch.empty_like(chi0.data)
     Ud = torch.as_tensor(U, dtype=torch.complex128, device="cuda").contiguous()
