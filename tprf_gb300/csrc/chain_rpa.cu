@@ -208,9 +208,9 @@ struct CopyCtx {
   // blocks does, spread evenly; the other blocks' rows -m are filled on the host.
   // Both draw on host memory bandwidth (a DMA write of a row against a read, a
   // write and a write-allocate read of the fill), so the best f balances the
-  // link's time (1 + f) B / R_link against the fill's (1 - f) B / R_fill.
-  // Adaptive mode measures both rates on each completed call and moves f halfway
-  // to the balance point (kept in [0, 0.9], so the fill rate stays measured).
+  // link's busy time against the fill's. Adaptive mode measures both on each
+  // completed call and moves f by a quarter of their relative imbalance (kept
+  // in [0.1, 0.8], so both stay measured).
   int host_fill_mode = -1;  // -1 adaptive, 0 every row over the link, 1 every row -m filled on the host
   double dma_frac = 0.4;    // current f of the adaptive mode
   std::mutex mu;        // one call at a time enqueues on this device's copy stream
@@ -258,9 +258,11 @@ void fold_record(CopyCtx *c, CallRecord *r) {
     fill_busy_ms = r->fill->job_ms / std::max(1, HostPool::get().threads());
   }
   if (copy_ms <= 0.0 || fill_busy_ms <= 0.0 || r->filled == 0) return;
-  const double r_link = (double)r->d2h / copy_ms, r_fill = (double)r->filled / fill_busy_ms;
-  const double target = std::min(0.9, std::max(0.0, (r_link - r_fill) / (r_link + r_fill)));
-  c->dma_frac = 0.5 * (c->dma_frac + target);
+  // move f by a quarter of the relative imbalance of the two busy times, as
+  // measured with each other's contention for host memory (a balance point
+  // computed from the rates would assume they do not depend on f)
+  const double step = 0.25 * (fill_busy_ms - copy_ms) / (fill_busy_ms + copy_ms);
+  c->dma_frac = std::min(0.8, std::max(0.1, c->dma_frac + step));
 }
 void fold_split_rates(CopyCtx *c) {
   for (long k = std::max(0L, c->calls - kRecords); k < c->calls; ++k) fold_record(c, &c->rec[k % kRecords]);
