@@ -128,6 +128,10 @@ __device__ __forceinline__ cdf caxpy(dfl k, cdf x, cdf y) { return cadd(y, cscal
 __device__ __forceinline__ cdf cfms_df(cdf a, cdf b, cdf acc) {
   return cdf{dfms2(acc.x, a.x, b.x, a.y, b.y), dfms2(acc.y, a.x, b.y, dneg(a.y), b.x)};
 }
+// acc + a b
+__device__ __forceinline__ cdf cfma_df(cdf a, cdf b, cdf acc) {
+  return cdf{dfms2(acc.x, a.y, b.y, a.x, b.x), dfms2(acc.y, dneg(a.x), b.y, a.y, b.x)};
+}
 template <bool FWD>
 __device__ __forceinline__ cdf mul_mi(cdf a) {  // -i a (FWD) or +i a
   return FWD ? cdf{a.y, dneg(a.x)} : cdf{dneg(a.y), a.x};

@@ -483,173 +483,128 @@ extern "C" int tprf_solve_rpa_PH_to_host(long n_points, int nb, const double *ch
 namespace tprf {
 namespace {
 
-template <int NB, int NT>
+__device__ __forceinline__ double2 ad_fma(double2 a, double2 b, double2 acc) { return cfma(a, b, acc); }
+__device__ __forceinline__ cdf ad_fma(cdf a, cdf b, cdf acc) { return cfma_df(a, b, acc); }
+
+// The thread-per-point adjoint needs no factorisation: A^-1 = (I - X0 Ug)^-1 =
+// I + X Ug (push-through, X = A^-1 X0), so Z = A^-H Y = Y + Ug^H (X^H Y). Then
+// P = Z X^H row by row, each row used at once by chi0_grad = Z + P Ug^H and by
+// U_grad += X0^H P (row i of P meets row i of X0). Products only, with
+// independent accumulators: double-float on the FP32 pipe by default (native
+// FP64 in the FP64 mode), FP64 at the boundary.
+template <int NB, int NT, class E>
 __global__ void __launch_bounds__(NT) rpa_adjoint_point_kernel(long n_points, const double2 *chi0,
                                                                const double2 *__restrict__ U, const double2 *chi,
-                                                               const double2 *chig, double2 *chi0g, double2 *Ug_out,
-                                                               unsigned *status) {
+                                                               const double2 *chig, double2 *chi0g, double2 *Ug_out) {
   constexpr int N = NB * NB;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  // Layout: [N*N] grouped U, [N*N][NT] LU of A^H, [N*N][NT] U_grad partial sums
-  // (both [element][thread]: conflict-free), [N][NT] row permutations.
-  double2 *ug = reinterpret_cast<double2 *>(smem_raw);
-  double2 *A = ug + N * N;
-  double2 *acc = A + N * N * NT;
-  int *perm = reinterpret_cast<int *>(acc + N * N * NT) + threadIdx.x;
+  // Layout: [N*N] grouped U, then per thread ([element][thread]: conflict-free)
+  // the U_grad partial sums and conj(X) in the element type.
+  E *ug = reinterpret_cast<E *>(smem_raw);
+  E *acc = ug + N * N;
+  E *xs = acc + N * N * NT;
   const int tid = threadIdx.x;
-  for (int e = tid; e < N * N; e += NT) ug[e] = U[(e / N) * N + colmap<NB>(e % N)];
+  for (int e = tid; e < N * N; e += NT) ug[e] = el_from(U[(e / N) * N + colmap<NB>(e % N)], (E *)nullptr);
 #pragma unroll
-  for (int e = 0; e < N * N; ++e) acc[e * NT + tid] = make_double2(0.0, 0.0);
+  for (int e = 0; e < N * N; ++e) acc[e * NT + tid] = el_zero((E *)nullptr);
   __syncthreads();
-#define AE(i, k) A[((i) * N + (k)) * NT + tid]
 #define ACC(i, k) acc[((i) * N + (k)) * NT + tid]
-  bool singular = false;
+#define XC(i, k) xs[((i) * N + (k)) * NT + tid]
   for (long pt = blockIdx.x * (long)NT + tid; pt < n_points; pt += (long)gridDim.x * NT) {
     const double2 *x0 = chi0 + pt * N * N, *x = chi + pt * N * N, *y = chig + pt * N * N;
-    // A^H[i][j] = delta_ij - sum_m conj(Ug[m][i]) conj(X0[j][m]), one row of X0 at a time
+    // W = X^H Y, one row of X and Y at a time (conj(X) kept for P)
+    E W[N][N];
 #pragma unroll
-    for (int j = 0; j < N; ++j) {
-      double2 xr[N];
+    for (int i = 0; i < N; ++i)
 #pragma unroll
-      for (int m = 0; m < N; ++m) xr[m] = x0[j * N + colmap<NB>(m)];
+      for (int j = 0; j < N; ++j) W[i][j] = el_zero((E *)nullptr);
 #pragma unroll
-      for (int i = 0; i < N; ++i) {
-        double2 s = make_double2(i == j ? 1.0 : 0.0, 0.0);
+    for (int l = 0; l < N; ++l) {
+      E xr[N], yr[N];
 #pragma unroll
-        for (int m = 0; m < N; ++m) s = cfms(cconj(ug[m * N + i]), cconj(xr[m]), s);
-        AE(i, j) = s;
+      for (int m = 0; m < N; ++m) {
+        xr[m] = cconj(el_from(x[l * N + colmap<NB>(m)], (E *)nullptr));
+        yr[m] = el_from(y[l * N + colmap<NB>(m)], (E *)nullptr);
+        XC(l, m) = xr[m];
       }
-      perm[j * NT] = j;
-    }
-    // LU of A^H with partial pivoting
-#pragma unroll 1
-    for (int j = 0; j < N; ++j) {
-      int p = j;
-      double best = cabs2(AE(j, j));
 #pragma unroll
       for (int i = 0; i < N; ++i)
-        if (i > j) {
-          const double v = cabs2(AE(i, j));
-          if (v > best) {
-            best = v;
-            p = i;
-          }
-        }
-      if (best == 0.0) singular = true;
-      if (p != j) {
 #pragma unroll
-        for (int k = 0; k < N; ++k) {
-          const double2 t = AE(j, k);
-          AE(j, k) = AE(p, k);
-          AE(p, k) = t;
-        }
-        const int t = perm[j * NT];
-        perm[j * NT] = perm[p * NT];
-        perm[p * NT] = t;
-      }
-      const double2 inv = crecip(AE(j, j));
-      AE(j, j) = inv;
-#pragma unroll
-      for (int i = 0; i < N; ++i)
-        if (i > j) {
-          const double2 f = cmul(AE(i, j), inv);
-          AE(i, j) = f;
-#pragma unroll
-          for (int k = 0; k < N; ++k)
-            if (k > j) AE(i, k) = cfms(f, AE(j, k), AE(i, k));
-        }
+        for (int j = 0; j < N; ++j) W[i][j] = ad_fma(xr[i], yr[j], W[i][j]);
     }
-    // Z = A^-H Y, column by column, in registers
-    double2 Z[N][N];
-#pragma unroll
-    for (int c = 0; c < N; ++c) {
-      const int cm = colmap<NB>(c);
-      double2 b[N];
-#pragma unroll
-      for (int r = 0; r < N; ++r) b[r] = y[perm[r * NT] * N + cm];
-#pragma unroll
-      for (int r = 1; r < N; ++r)
-#pragma unroll
-        for (int l = 0; l < r; ++l) b[r] = cfms(AE(r, l), b[l], b[r]);
-#pragma unroll
-      for (int rr = 0; rr < N; ++rr) {
-        const int r = N - 1 - rr;
-#pragma unroll
-        for (int l = r + 1; l < N; ++l) b[r] = cfms(AE(r, l), b[l], b[r]);
-        b[r] = cmul(b[r], AE(r, r));
-      }
-#pragma unroll
-      for (int r = 0; r < N; ++r) Z[r][c] = b[r];
-    }
-    // P = Z X^H, one row of X at a time
-    double2 P[N][N];
-#pragma unroll
-    for (int m = 0; m < N; ++m) {
-      double2 xr[N];
-#pragma unroll
-      for (int l = 0; l < N; ++l) xr[l] = cconj(x[m * N + colmap<NB>(l)]);
-#pragma unroll
-      for (int i = 0; i < N; ++i) {
-        double2 s = make_double2(0.0, 0.0);
-#pragma unroll
-        for (int l = 0; l < N; ++l) s = cfma(Z[i][l], xr[l], s);
-        P[i][m] = s;
-      }
-    }
-    // chi0_grad = Z + P Ug^H
-    double2 *g = chi0g + pt * N * N;
+    // Z = Y + Ug^H W
+    E Z[N][N];
 #pragma unroll
     for (int i = 0; i < N; ++i)
 #pragma unroll
       for (int j = 0; j < N; ++j) {
-        double2 s = Z[i][j];
+        E s = el_from(y[i * N + colmap<NB>(j)], (E *)nullptr);
 #pragma unroll
-        for (int m = 0; m < N; ++m) s = cfma(P[i][m], cconj(ug[j * N + m]), s);
-        g[i * N + colmap<NB>(j)] = s;
+        for (int m = 0; m < N; ++m) s = ad_fma(cconj(ug[m * N + i]), W[m][j], s);
+        Z[i][j] = s;
       }
-    // U_grad += X0^H P, one column of X0 at a time
+    double2 *g = chi0g + pt * N * N;
 #pragma unroll
     for (int i = 0; i < N; ++i) {
-      double2 xc[N];
+      E pr[N];  // row i of P = Z X^H
 #pragma unroll
-      for (int l = 0; l < N; ++l) xc[l] = cconj(x0[l * N + colmap<NB>(i)]);
+      for (int m = 0; m < N; ++m) {
+        E s = el_zero((E *)nullptr);
+#pragma unroll
+        for (int l = 0; l < N; ++l) s = ad_fma(Z[i][l], XC(m, l), s);
+        pr[m] = s;
+      }
 #pragma unroll
       for (int j = 0; j < N; ++j) {
-        double2 s = ACC(i, j);
+        E s = Z[i][j];
 #pragma unroll
-        for (int l = 0; l < N; ++l) s = cfma(xc[l], P[l][j], s);
-        ACC(i, j) = s;
+        for (int m = 0; m < N; ++m) s = ad_fma(pr[m], cconj(ug[j * N + m]), s);
+        g[i * N + colmap<NB>(j)] = el_to(s);
+      }
+#pragma unroll
+      for (int k = 0; k < N; ++k) {
+        const E xk = cconj(el_from(x0[i * N + colmap<NB>(k)], (E *)nullptr));
+#pragma unroll
+        for (int j = 0; j < N; ++j) ACC(k, j) = ad_fma(xk, pr[j], ACC(k, j));
       }
     }
   }
-#undef AE
 #undef ACC
-  if (singular) atomicOr(status, kDevErrSingular);
+#undef XC
   __syncthreads();
   // CTA sum of the partials, one atomic per entry: grouped (m, c) -> offset m * N + colmap(c)
   for (int e = tid; e < N * N; e += NT) {
-    double2 s = make_double2(0.0, 0.0);
+    E s = el_zero((E *)nullptr);
     for (int t = 0; t < NT; ++t) s = cadd(s, acc[e * NT + t]);
+    const double2 v = el_to(s);
     const int off = (e / N) * N + colmap<NB>(e % N);
-    atomicAdd(&reinterpret_cast<double *>(Ug_out)[2 * off], s.x);
-    atomicAdd(&reinterpret_cast<double *>(Ug_out)[2 * off + 1], s.y);
+    atomicAdd(&reinterpret_cast<double *>(Ug_out)[2 * off], v.x);
+    atomicAdd(&reinterpret_cast<double *>(Ug_out)[2 * off + 1], v.y);
   }
 }
 
-template <int NB>
-int launch_rpa_adjoint_point(long n_points, const double2 *chi0, const double2 *U, const double2 *chi,
-                             const double2 *chig, double2 *chi0g, double2 *Ug, cudaStream_t stream, unsigned *status) {
+template <int NB, class E>
+int launch_rpa_adjoint_point_as(long n_points, const double2 *chi0, const double2 *U, const double2 *chi,
+                                const double2 *chig, double2 *chi0g, double2 *Ug, cudaStream_t stream) {
   constexpr int N = NB * NB, NT = 128;
-  const size_t smem = (size_t)N * N * 16 * (1 + 2 * NT) + (size_t)N * NT * sizeof(int);
-  auto kern = rpa_adjoint_point_kernel<NB, NT>;
+  const size_t smem = (size_t)N * N * 16 * (1 + 2 * NT);
+  auto kern = rpa_adjoint_point_kernel<NB, NT, E>;
   TPRF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0;
   TPRF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, smem));
   long blocks = (n_points + NT - 1) / NT;
   blocks = std::max(1L, std::min(blocks, (long)num_sms() * std::max(1, per_sm)));
-  kern<<<(unsigned)blocks, NT, smem, stream>>>(n_points, chi0, U, chi, chig, chi0g, Ug, status);
+  kern<<<(unsigned)blocks, NT, smem, stream>>>(n_points, chi0, U, chi, chig, chi0g, Ug);
   TPRF_KERNEL_LAUNCHED("rpa_adjoint_point_kernel");
   return TPRF_OK;
+}
+
+template <int NB>
+int launch_rpa_adjoint_point(long n_points, const double2 *chi0, const double2 *U, const double2 *chi,
+                             const double2 *chig, double2 *chi0g, double2 *Ug, cudaStream_t stream, unsigned *) {
+  return arith_mode() == kArithFP64
+             ? launch_rpa_adjoint_point_as<NB, double2>(n_points, chi0, U, chi, chig, chi0g, Ug, stream)
+             : launch_rpa_adjoint_point_as<NB, cdf>(n_points, chi0, U, chi, chig, chi0g, Ug, stream);
 }
 
 }  // namespace
