@@ -128,6 +128,28 @@ __device__ __forceinline__ cdf caxpy(dfl k, cdf x, cdf y) { return cadd(y, cscal
 __device__ __forceinline__ cdf cfms_df(cdf a, cdf b, cdf acc) {
   return cdf{dfms2(acc.x, a.x, b.x, a.y, b.y), dfms2(acc.y, a.x, b.y, dneg(a.y), b.x)};
 }
+// acc - a b without the closing Fast2Sums (dfms2 stops at s + e: the same value,
+// |lo| not bounded by half an ulp of hi). Only for a value that goes on into
+// further updates; renormalise (cnorm) before a product reads it, a magnitude is
+// taken from its high words, or it is converted.
+__device__ __forceinline__ dfl dfms2_lazy(dfl c, dfl p, dfl q, dfl u, dfl v) {
+  const float p1 = __fmul_rn(-p.hi, q.hi);
+  const float e1 = __fmaf_rn(-p.hi, q.hi, -p1);
+  const float p2 = __fmul_rn(u.hi, v.hi);
+  const float e2 = __fmaf_rn(u.hi, v.hi, -p2);
+  float s, t1, t2;
+  two_sum(c.hi, p1, s, t1);
+  two_sum(s, p2, s, t2);
+  float e = __fadd_rn(__fadd_rn(t1, t2), __fadd_rn(c.lo, __fadd_rn(e1, e2)));
+  e = __fmaf_rn(-p.hi, q.lo, e);
+  e = __fmaf_rn(-p.lo, q.hi, e);
+  e = __fmaf_rn(u.hi, v.lo, e);
+  e = __fmaf_rn(u.lo, v.hi, e);
+  return dfl{s, e};
+}
+__device__ __forceinline__ cdf cfms_df_lazy(cdf a, cdf b, cdf acc) {
+  return cdf{dfms2_lazy(acc.x, a.x, b.x, a.y, b.y), dfms2_lazy(acc.y, a.x, b.y, dneg(a.y), b.x)};
+}
 // acc + a b
 __device__ __forceinline__ cdf cfma_df(cdf a, cdf b, cdf acc) {
   return cdf{dfms2(acc.x, a.y, b.y, a.x, b.x), dfms2(acc.y, dneg(a.x), b.y, a.y, b.x)};

@@ -29,6 +29,12 @@ template <class E> struct IsDf { static constexpr bool value = false; };
 template <> struct IsDf<cdf> { static constexpr bool value = true; };
 __device__ __forceinline__ double2 el_fms(double2 a, double2 b, double2 acc) { return cfms(a, b, acc); }
 __device__ __forceinline__ cdf el_fms(cdf a, cdf b, cdf acc) { return cfms_df(a, b, acc); }
+// the elimination's updates: unnormalised double-float (cfms_df_lazy), with
+// el_norm before a value is read by a product, a magnitude or a conversion
+__device__ __forceinline__ double2 el_fms_lazy(double2 a, double2 b, double2 acc) { return cfms(a, b, acc); }
+__device__ __forceinline__ cdf el_fms_lazy(cdf a, cdf b, cdf acc) { return cfms_df_lazy(a, b, acc); }
+__device__ __forceinline__ double2 el_norm(double2 a) { return a; }
+__device__ __forceinline__ cdf el_norm(cdf a) { return cnorm(a); }
 __device__ __forceinline__ double2 el_recip(double2 a) { return crecip(a); }
 __device__ __forceinline__ cdf el_recip(cdf a) {
   // 1/(x + iy) = (x - iy) / (x^2 + y^2); the real reciprocal by one Newton step from the float one

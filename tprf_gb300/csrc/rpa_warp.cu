@@ -127,6 +127,10 @@ __device__ __forceinline__ typename Mag<E>::type solve_augmented(E *M, int N_in,
   using MagT = typename Mag<E>::type;
   MagT pmin = Mag<E>::big;
   for (int j = 0; j < N; ++j) {
+    // the updates leave unnormalised double-float values: renormalise the pivot
+    // column (read by the search, the reciprocal and the multipliers) and,
+    // below, the pivot row (read by the update products)
+    for (int i = j + lane; i < N; i += G) MM(i, j) = el_norm(MM(i, j));
     int p = j;
     MagT best = -1;
     for (int i = j + lane; i < N; i += G) {
@@ -151,21 +155,22 @@ __device__ __forceinline__ typename Mag<E>::type solve_augmented(E *M, int N_in,
     for (int i = j + 1 + lane; i < N; i += G) MM(i, j) = cmul(MM(i, j), inv);
     __syncwarp(gmask);
     for (int c = j + 1 + lane; c < W; c += G) {
-      const E piv = MM(j, c);
+      const E piv = el_norm(MM(j, c));
+      MM(j, c) = piv;
 #pragma unroll 2
-      for (int i = j + 1; i < N; ++i) MM(i, c) = el_fms(MM(i, j), piv, MM(i, c));
+      for (int i = j + 1; i < N; ++i) MM(i, c) = el_fms_lazy(MM(i, j), piv, MM(i, c));
     }
     __syncwarp(gmask);
     if (lane == 0) MM(j, j) = inv;
     __syncwarp(gmask);
   }
-  // back substitution, one B column per lane
+  // back substitution, one B column per lane (B renormalised as it is read)
   for (int c = N + lane; c < W; c += G) {
     for (int j = N - 1; j >= 0; --j) {
-      const E xj = cmul(MM(j, c), MM(j, j));
+      const E xj = cmul(el_norm(MM(j, c)), MM(j, j));
       MM(j, c) = xj;
 #pragma unroll 2
-      for (int i = 0; i < j; ++i) MM(i, c) = el_fms(MM(i, j), xj, MM(i, c));
+      for (int i = 0; i < j; ++i) MM(i, c) = el_fms_lazy(MM(i, j), xj, MM(i, c));
     }
   }
   __syncwarp(gmask);
