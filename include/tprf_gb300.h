@@ -97,11 +97,13 @@ int tprf_get_arithmetic(void);
 /* Autotuner of launch shapes. The reference plans its FFTs with FFTW_ESTIMATE
  * (c++/triqs_tprf/fourier/fourier_common.cpp:32-43): a fixed heuristic. Mode 0
  * (default) uses fixed heuristics here too; mode 1 ("measure", as FFTW_MEASURE)
- * times every candidate on the first call of each shape and keeps the fastest:
- * columns per CTA of the iv -> tau and tau -> i omega kernels (fused bubble
- * included), lanes per point of the RPA group kernel (nb >= 3), threads per
- * CTA of the Dyson kernel, and the tile size of the TMA-staged lattice plane
- * pass (0 = the plain pass; in-place calls only read it from wisdom).
+ * times every candidate on the first call of each shape (the shortest of three
+ * launches) and keeps the fastest, or the heuristic's choice when no candidate
+ * beats it by more than 2 %: columns per CTA and the radix order of the FFT of
+ * the iv -> tau and tau -> i omega kernels (fused bubble included), lanes per
+ * point of the RPA group kernels (nb >= 3), threads per CTA of the Dyson
+ * kernel, and the tile size of the TMA-staged lattice plane pass (0 = the
+ * plain pass; in-place calls only read it from wisdom).
  * Candidates run on a prefix of the call's own columns or points, or on the
  * whole call (out-of-place kernels only), so results do not depend on the mode
  * beyond rounding (the TMA plane pass rounds as a decimation-in-frequency FFT). A tuning call waits for its stream;

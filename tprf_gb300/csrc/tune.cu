@@ -98,12 +98,13 @@ int tune_pick(const std::string &key, const std::vector<int> &candidates, int fa
     cudaEventDestroy(e0);
     return cuda_status(ce, "autotune: event");
   }
-  float best = 3.0e38f;
+  float best = 3.0e38f, fallback_ms = 3.0e38f;
   int best_v = fallback, st = TPRF_OK;
   for (int v : candidates) {
     float ms = 0.f;
     st = time_candidate(launch, v, s, e0, e1, &ms);
     if (st) break;
+    if (v == fallback) fallback_ms = ms;
     if (ms < best) {
       best = ms;
       best_v = v;
@@ -112,6 +113,9 @@ int tune_pick(const std::string &key, const std::vector<int> &candidates, int fa
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (st) return st;
+  // the heuristic's choice stands unless another candidate is more than 2 %
+  // faster: closer than that, the trials' noise decides
+  if (fallback_ms <= 1.02f * best) best_v = fallback;
   *choice = best_v;
   std::lock_guard<std::mutex> lock(g_tune_mu);
   g_wisdom[key] = best_v;
