@@ -332,7 +332,9 @@ int tprf_imtime_bubble_rpa_to_host_last_stats(double *out, int n);
  * of a copy), mode 0 copies every row over the link, mode -1 (default) splits the
  * frequency blocks between the two, moving the split on every completed call
  * toward the point where the link's and the host threads' measured times meet.
- * Per device, process-wide. No reference counterpart. */
+ * Per device, process-wide. The fill runs on one host thread per CPU the
+ * process may use (at most 16; the environment variable TPRF_HOST_FILL_THREADS,
+ * 1..64, read once, overrides the count). No reference counterpart. */
 int tprf_set_host_fill(int mode);
 
 /* solve_rpa_PH with chi written to HOST memory, as the reference's C++ function

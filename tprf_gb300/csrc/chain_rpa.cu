@@ -20,6 +20,7 @@
 #include <chrono>
 #include <cmath>
 #include <condition_variable>
+#include <cstdlib>
 #include <cstring>
 #include <deque>
 #include <functional>
@@ -71,8 +72,19 @@ class HostPool {
 
  private:
   HostPool() {
-    const unsigned hw = std::thread::hardware_concurrency();
-    n_ = std::max(1u, std::min(hw ? hw : 4u, 16u));
+    // one thread per CPU this process may run on, at most 16 (on the 16-core
+    // GB300 host, 16 threads filled faster than 15 or 12 with the enqueuing
+    // thread beside them); TPRF_HOST_FILL_THREADS (1..64) overrides the count
+    unsigned cpus = 0;
+    cpu_set_t set;
+    CPU_ZERO(&set);
+    if (sched_getaffinity(0, sizeof(set), &set) == 0) cpus = (unsigned)CPU_COUNT(&set);
+    if (cpus == 0) cpus = std::thread::hardware_concurrency();
+    n_ = std::max(1u, std::min(cpus, 16u));
+    if (const char *env = std::getenv("TPRF_HOST_FILL_THREADS")) {
+      const long v = std::strtol(env, nullptr, 10);
+      if (v >= 1 && v <= 64) n_ = (unsigned)v;
+    }
     for (unsigned i = 0; i < n_; ++i) {
       std::thread t([this] { run(); });
       pthread_setname_np(t.native_handle(), "tprf-host-fill");  // visible in /proc/<pid>/task/*/comm
