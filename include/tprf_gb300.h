@@ -336,6 +336,12 @@ int tprf_imtime_bubble_rpa_to_host_last_stats(double *out, int n);
  * process may use (at most 16; the environment variable TPRF_HOST_FILL_THREADS,
  * 1..64, read once, overrides the count). No reference counterpart. */
 int tprf_set_host_fill(int mode);
+/* A fixed split: the negative frequencies of a fraction f in [0, 1] of the
+ * frequency blocks cross the link, the others are filled on the host (f = 1 is
+ * mode 0, f = 0 mode 1). TPRF_ERR_INVALID_ARGUMENT outside [0, 1];
+ * tprf_set_host_fill(-1) returns to the adaptive split. Per device,
+ * process-wide. No reference counterpart. */
+int tprf_set_host_fill_fraction(double f);
 
 /* solve_rpa_PH with chi written to HOST memory, as the reference's C++ function
  * returns it (rpa.cpp:29-68 returns a host gf). The points are solved in chunks

@@ -105,6 +105,10 @@ def test_argument_errors_are_reported_without_a_gpu(lib):
     assert lib.tprf_solve_rpa_PH_to_host_workspace_bytes(10, 3, 2) == 2 * 10 * 81 * 16 + 256
     assert lib.tprf_solve_rpa_PH_to_host(100, 3, fake, fake, fake, 10, fake, 1000, None) == -1
     assert "chunk" in lib.tprf_last_error().decode()
+    # a fixed link / host split outside [0, 1] (checked before the device is touched)
+    for f in (-0.1, 1.5, float("nan")):
+        assert lib.tprf_set_host_fill_fraction(f) == -1
+    assert "[0, 1]" in lib.tprf_last_error().decode()
 
 
 def test_workspace_size(lib):

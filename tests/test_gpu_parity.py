@@ -601,12 +601,15 @@ def test_partner_stores_on_every_mesh_layout(cuda_lib, arithmetic, dims):
         assert torch.equal(fused.data, two.data.cpu())
 
 
+@pytest.mark.parametrize("fill", ["host", "half"])
 @pytest.mark.parametrize("case", [0, 3, len(CASES) - 1])
-def test_pipelined_fused_calls_equal_the_waiting_call(cuda_lib, arithmetic, case):
+def test_pipelined_fused_calls_equal_the_waiting_call(cuda_lib, arithmetic, case, fill):
     """imtime_bubble_rpa_wk(wait=False) back to back on several inputs sharing
     one workspace (the copies of a call running behind the next call's chain,
     whose solves wait for the ring slots they reuse), then join_host_copies:
-    every output equals the waiting call's chi."""
+    every output equals the waiting call's chi. fill: every negative frequency
+    of a real chi filled on the host, or a fixed split with half of the blocks'
+    negative frequencies over the link."""
     T = tp()
     from tprf_gb300 import _native
     from tprf_gb300.lattice_utils import imtime_bubble_rpa_wk, join_host_copies
@@ -623,7 +626,10 @@ def test_pipelined_fused_calls_equal_the_waiting_call(cuda_lib, arithmetic, case
     expect = [imtime_bubble_rpa_wk(g_wk, U, nw, block_freqs=block, slots=slots).data.clone() for U in Us]
     outs = [torch.empty_like(e).pin_memory() for e in expect]
     lib.tprf_set_sync_checks(0)
-    lib.tprf_set_host_fill(1)  # every negative frequency of a real chi filled on the host
+    if fill == "host":
+        lib.tprf_set_host_fill(1)  # every negative frequency of a real chi filled on the host
+    else:
+        assert lib.tprf_set_host_fill_fraction(0.5) == 0
     try:
         for U, out in zip(Us, outs):
             imtime_bubble_rpa_wk(g_wk, U, nw, out=out, block_freqs=block, slots=slots, chi0=chi0, workspace=ws,
@@ -637,8 +643,10 @@ def test_pipelined_fused_calls_equal_the_waiting_call(cuda_lib, arithmetic, case
     for e, out in zip(expect, outs):
         assert torch.equal(out, e)
     # real hoppings and a real U on the double-float path (which records that the
-    # bubble is real): only the frequencies w >= 0 crossed to the host
-    rows = nw if case != 3 and arithmetic != "fp64" else 2 * nw - 1
+    # bubble is real): only the frequencies w >= 0 crossed to the host, plus, with
+    # half the blocks (one frequency each) sending their negative rows, those of
+    # blocks 2 and 4 (block 0 holds w = 0 alone)
+    rows = (nw if fill == "host" else nw + 2) if case != 3 and arithmetic != "fp64" else 2 * nw - 1
     assert lib.tprf_imtime_bubble_rpa_to_host_last_d2h_bytes() == rows * int(np.prod(dims)) * nb ** 4 * 16
     with pytest.raises(ValueError):
         imtime_bubble_rpa_wk(g_wk, Us[0], nw, wait=False)

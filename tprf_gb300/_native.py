@@ -71,6 +71,7 @@ SIGNATURES = {
     "tprf_imtime_bubble_rpa_to_host_last_d2h_bytes": (c_size_t, []),
     "tprf_imtime_bubble_rpa_to_host_last_stats": (c_int, [ctypes.POINTER(c_double), c_int]),
     "tprf_set_host_fill": (c_int, [c_int]),
+    "tprf_set_host_fill_fraction": (c_int, [c_double]),
     "tprf_lindhard_chi00_workspace_bytes": (c_size_t, [c_long, c_int]),
     "tprf_lindhard_chi00": (c_int, [c_long, c_int3, c_int, c_void_p, c_double, c_double, c_int, c_void_p, c_void_p,
                                     c_size_t, c_void_p]),

@@ -223,8 +223,11 @@ struct CopyCtx {
   // link's busy time against the fill's. Adaptive mode measures both on each
   // completed call and moves f by a quarter of their relative imbalance (kept
   // in [0.1, 0.8], so both stay measured).
-  int host_fill_mode = -1;  // -1 adaptive, 0 every row over the link, 1 every row -m filled on the host
+  // -1 adaptive, 0 every row over the link, 1 every row -m filled on the host,
+  // 2 a fixed f (tprf_set_host_fill_fraction)
+  int host_fill_mode = -1;
   double dma_frac = 0.4;    // current f of the adaptive mode
+  double fixed_frac = 1.0;  // f of mode 2
   std::mutex mu;        // one call at a time enqueues on this device's copy stream
   CallRecord &last() { return rec[(calls + kRecords - 1) % kRecords]; }
 };
@@ -361,7 +364,11 @@ int bubble_rpa_to_host(double beta, int n_iw, int n_tau, int nw, const int dims[
   if ((st = copy_ctx(&c))) return st;
   std::lock_guard<std::mutex> lock(c->mu);
   fold_split_rates(c);
-  const double frac = !host_mirror ? 1.0 : c->host_fill_mode == 0 ? 1.0 : c->host_fill_mode == 1 ? 0.0 : c->dma_frac;
+  const double frac = !host_mirror               ? 1.0
+                      : c->host_fill_mode == 0 ? 1.0
+                      : c->host_fill_mode == 1 ? 0.0
+                      : c->host_fill_mode == 2 ? c->fixed_frac
+                                               : c->dma_frac;
   size_t filled = 0;
   TPRF_CUDA(cudaEventRecord(c->done, s));  // the copy stream starts after the chain
   TPRF_CUDA(cudaStreamWaitEvent(c->copy, c->done, 0));
@@ -513,6 +520,17 @@ extern "C" int tprf_set_host_fill(int mode) {
   if (int st = copy_ctx(&c)) return st;
   std::lock_guard<std::mutex> lock(c->mu);
   c->host_fill_mode = mode;
+  return TPRF_OK;
+}
+
+extern "C" int tprf_set_host_fill_fraction(double f) {
+  if (!(f >= 0.0 && f <= 1.0))
+    return set_error(TPRF_ERR_INVALID_ARGUMENT, "set_host_fill_fraction: the fraction must lie in [0, 1]");
+  CopyCtx *c = nullptr;
+  if (int st = copy_ctx(&c)) return st;
+  std::lock_guard<std::mutex> lock(c->mu);
+  c->host_fill_mode = 2;
+  c->fixed_frac = f;
   return TPRF_OK;
 }
 
