@@ -650,3 +650,44 @@ def test_pipelined_fused_calls_equal_the_waiting_call(cuda_lib, arithmetic, case
     assert lib.tprf_imtime_bubble_rpa_to_host_last_d2h_bytes() == rows * int(np.prod(dims)) * nb ** 4 * 16
     with pytest.raises(ValueError):
         imtime_bubble_rpa_wk(g_wk, Us[0], nw, wait=False)
+
+
+def _orbital_reversal(nb):
+    """o = abcd (a slowest) -> dcba for the nb^4 bubble columns."""
+    rev = []
+    for o in range(nb ** 4):
+        x, r = o, 0
+        for _ in range(4):
+            r, x = r * nb + x % nb, x // nb
+        rev.append(r)
+    return np.array(rev)
+
+
+@pytest.mark.parametrize("complex_hop", [False, True])
+def test_compact_orbital_columns_on_a_3d_mesh(cuda_lib, arithmetic, complex_hop):
+    """The chain on a three-dimensional mesh whose last two axes share one plane
+    pass: with real hoppings the bubble is real and transpose-symmetric, so only
+    the canonical orbital columns abcd <= dcba are transformed r -> q and the last
+    pass stores chi0(w, -q)_dcba = chi0(w, q)_abcd bit for bit; with complex
+    hoppings the same mesh takes the full path. Both against the oracle."""
+    T = tp()
+    from tprf_gb300 import workloads
+    hop = workloads.cubic_3orb(3)
+    if complex_hop:
+        extra = 0.2j * np.array([[0.0, 1.0, 0.5], [-0.3, 0.0, 0.2], [0.1, -0.6, 0.0]])
+        hop[(1, 0, 0)] = hop[(1, 0, 0)] + extra
+        hop[(-1, 0, 0)] = hop[(-1, 0, 0)] + extra.conj().T
+    dims, beta, n_max, nw = (4, 4, 2), 12.0, 24, 6
+    ek, g_wk, _, _ = _g_wr(hop, dims, beta, n_max)
+    chi0 = T.imtime_bubble_chi0_wk(g_wk, nw=nw, verbose=False)
+    ref = O.imtime_bubble_chi0_wk(O.lattice_dyson_g0_wk(0.0, ek, beta, n_max), beta, dims, nw=nw)
+    assert rel_err(chi0.data, ref) < PARITY_RTOL
+    x = chi0.data.cpu().numpy().reshape((2 * nw - 1,) + dims + (81,))
+    mq = np.roll(x[:, ::-1, ::-1, ::-1, :], 1, axis=(1, 2, 3))  # chi0(w, -q)
+    rev = _orbital_reversal(3)
+    refl = mq[..., rev]  # chi0(w, -q)_dcba
+    off = rev != np.arange(81)
+    if complex_hop:
+        assert not np.array_equal(x[..., off], refl[..., off])
+    elif arithmetic != "fp64":  # the FP64 mode transforms every column
+        assert np.array_equal(x[..., off], refl[..., off])

@@ -35,7 +35,7 @@
 namespace tprf {
 int bubble_to_wr(double beta, int n_iw, int n_tau, int nw, const int dims[3], int nb, const double *g_wk,
                  const double *moments, double2 *out, void *workspace, size_t workspace_bytes, void *const *events,
-                 cudaStream_t s, bool *chi_df, unsigned **gmax_out);
+                 cudaStream_t s, bool *chi_df, unsigned **gmax_out, CompactChi *cc);
 int launch_rpa(long n_points, int nb, const double2 *chi0, const double2 *U, double2 *chi, cudaStream_t stream);
 
 namespace {
@@ -338,8 +338,9 @@ int bubble_rpa_to_host(double beta, int n_iw, int n_tau, int nw, const int dims[
   const double2 *Ud = reinterpret_cast<const double2 *>(U);
   bool chi_df = false;
   unsigned *gmax = nullptr;
+  CompactChi cc;  // the canonical orbital columns of a transpose-symmetric real bubble, where they apply
   int st = bubble_to_wr(beta, n_iw, n_tau, nw, dims, nb, g_wk, moments, chi0, workspace, chain_bytes, nullptr, s,
-                        &chi_df, &gmax);
+                        &chi_df, &gmax, &cc);
   if (st) return st;
   // the plan depends on whether the bubble was real: read its two words (and
   // U: with U real as well the host fills the negative frequencies)
@@ -397,9 +398,17 @@ int bubble_rpa_to_host(double beta, int n_iw, int n_tau, int nw, const int dims[
       const int m0 = k * block_freqs, m1 = std::min(nw, m0 + block_freqs), m_lo = std::max(m0, 1);
       double2 *rows = chi0 + (long)(nw - 1 + m0) * row;
       // the r -> q pass also stores chi0(-m, -q) = conj(chi0(m, q)) for m in
-      // [max(m0, 1), m1): row j of the block (m = m0 + j) at row -2 m0 - j from `rows`
+      // [max(m0, 1), m1): row j of the block (m = m0 + j) at row -2 m0 - j from
+      // `rows`; from the block's compact rows when the bubble wrote them
+      CompactChi cb;
+      if (cc.gmax && chi_df) {
+        cb = cc;
+        cb.buf = static_cast<char *>(cc.buf) + (size_t)m0 * nk * cc.oc->nc * sizeof(double2);
+        cb.rows = m1 - m0;
+        cb.w0 = m0;
+      }
       if ((st = launch_lattice_fft_fmt(false, m1 - m0, dims, nb4, rows, chi_df, rows, false, 1.0, s, nullptr, true,
-                                       -2L * m0)))
+                                       -2L * m0, cb.gmax ? &cb : nullptr)))
         return st;
       // frequency m at pos row m - m0; frequency -m (m >= m_lo) at neg row m1 - 1 - m
       const PairOut out{pos, neg + (long)(m1 - 1 - m0) * row, row, -row, m0, m1};

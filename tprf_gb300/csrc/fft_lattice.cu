@@ -129,23 +129,75 @@ __device__ __forceinline__ int4 conj_bits(int4 v) {
   return v;
 }
 
+// A pass on the compact canonical orbital columns of a real bubble
+// (CompactChi), active when gmax is set and the words say canon_says_yes. The
+// plane pass then runs in place on buf ([outer][n1][n2][n_target], n_target =
+// nc); the last (axis) pass reads buf ([outer][n][inner], inner = e1 e2 nc,
+// outer = the rows w >= 0) and stores, for the element (w, i, k, j) of the
+// canonical column t = ocan[j] and its reflection tr = orev[j]:
+//   (w, i, k, t) and, unless t is a palindrome, (w, -i, -k, tr) (the same value:
+//   chi0(w, -q)_dcba = chi0(w, q)_abcd), and for w > 0 the conjugates at
+//   (-w, -i, -k, t) and (-w, i, k, tr): every column of both signs of w in out.
+struct CompactPass {
+  const unsigned *gmax;  // null: off
+  void *buf;
+  long outer, n_target;  // plane: rows x (dims before the plane), nc; axis: rows, e1 e2 nc
+  int nc, nb4;
+  // axis: compact row o (frequency w0 + o) goes to output row row0 + o, its
+  // conjugate partner (for w0 + o > 0) to row prow0 - o
+  long row0, prow0, w0;
+  const int *ocan, *orev;
+  __device__ __forceinline__ bool active() const { return gmax != nullptr && canon_says_yes(gmax); }
+};
+constexpr CompactPass kNoCompact{nullptr, nullptr, 0, 0, 0, 0, 0, 0, 0, nullptr, nullptr};
+
 template <bool FWD, class E, bool IN_DF, bool OUT_DF>
 __global__ void __launch_bounds__(256) lattice_axis_kernel(const void *in, void *out, long ncols_total,
                                                            long inner, int ncol, int lgcol, FftDesc d, double scale,
-                                                           SkipRows skip, RowMirror mir) {
+                                                           SkipRows skip, RowMirror mir, CompactPass cp) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int n = d.n;
   E *a = reinterpret_cast<E *>(smem_raw);
   E *b = d.has_generic ? a + (size_t)n * ncol : nullptr;
   long *base = reinterpret_cast<long *>(smem_raw + (size_t)(d.has_generic ? 2 : 1) * n * ncol * sizeof(E));
   long *pbase = base + ncol;  // partner stores (the launcher sizes shared memory for them when mir.on)
+  long *cdst = base + ncol;   // compact pass: four store bases per column, [4][ncol]
   // The tile is ncol consecutive columns of the flattened (outer, inner) index;
   // element (row, column f) sits at (f / inner) * n * inner + row * inner + f % inner.
   const long f0 = blockIdx.x * (long)ncol;
-  if (f0 + ncol <= skip.columns && gmax_says_real(skip.gmax)) return;  // rows the partner rows fill
-  const bool mirror = mir.active();
+  const bool cm = cp.active();
+  const void *src = cm ? cp.buf : in;
+  const long istride = cm ? cp.n_target : inner;  // row stride of the input
+  if (cm) {
+    if (f0 >= cp.outer * cp.n_target) return;  // the grid is sized for the full layout
+  } else if (f0 + ncol <= skip.columns && gmax_says_real(skip.gmax)) {
+    return;  // rows the partner rows fill
+  }
+  const bool mirror = !cm && mir.active();
   for (int c = threadIdx.x; c < ncol; c += blockDim.x) {
     const long f = f0 + c;
+    if (cm) {
+      long bs = -1, s[4] = {kNoPartner, kNoPartner, kNoPartner, kNoPartner};
+      if (f < cp.outer * cp.n_target) {
+        const long o = f / cp.n_target, rem = f - o * cp.n_target;
+        const long kk = rem / cp.nc;
+        const int j = (int)(rem - kk * cp.nc);
+        const long k1 = kk / mir.e2, k2 = kk - k1 * mir.e2;
+        const long mk = (k1 ? mir.e1 - k1 : 0) * (long)mir.e2 + (k2 ? mir.e2 - k2 : 0);
+        const int t = cp.ocan[j], tr = cp.orev[j];
+        const long O = cp.row0 + o, P = cp.prow0 - o;
+        bs = o * n * cp.n_target + rem;
+        s[0] = O * n * inner + kk * cp.nb4 + t;
+        if (tr != t) s[1] = O * n * inner + mk * cp.nb4 + tr;
+        if (cp.w0 + o > 0) {
+          s[2] = P * n * inner + mk * cp.nb4 + t;
+          if (tr != t) s[3] = P * n * inner + kk * cp.nb4 + tr;
+        }
+      }
+      base[c] = bs;
+      for (int q = 0; q < 4; ++q) cdst[q * ncol + c] = s[q];
+      continue;
+    }
     const long o = f / inner;
     long bs = (f < ncols_total) ? o * n * inner + (f - o * inner) : -1;
     if (mirror) {
@@ -175,7 +227,7 @@ __global__ void __launch_bounds__(256) lattice_axis_kernel(const void *in, void 
       const int w = w0 + u * blockDim.x;
       const int c = w & (ncol - 1), row = w >> lgcol;
       const long bs = w < tile ? base[c] : -1;
-      if (bs >= 0) v[u] = load_raw<E, IN_DF>(in, bs + (long)row * inner);
+      if (bs >= 0) v[u] = load_raw<E, IN_DF>(src, bs + (long)row * istride);
     }
 #pragma unroll
     for (int u = 0; u < kLoadBatch; ++u) {
@@ -188,6 +240,21 @@ __global__ void __launch_bounds__(256) lattice_axis_kernel(const void *in, void 
   E *r = fft_smem<FWD>(a, b, d, ncol);
   const bool scaled = scale != 1.0;
   const dfl sd = split_double(scale);
+  if (cm) {
+    int4 *o4 = reinterpret_cast<int4 *>(out);
+    for (int w = threadIdx.x; w < tile; w += blockDim.x) {
+      const int c = w & (ncol - 1), row = w >> lgcol;
+      if (base[c] < 0) continue;
+      const long nrow = row ? n - row : 0;
+      const int4 v = stored_bits<E, OUT_DF>(r[row * ncol + c], scale, sd, scaled);
+      o4[cdst[c] + (long)row * inner] = v;
+      const long s1 = cdst[ncol + c], s2 = cdst[2 * ncol + c], s3 = cdst[3 * ncol + c];
+      if (s1 != kNoPartner) o4[s1 + nrow * inner] = v;
+      if (s2 != kNoPartner) o4[s2 + nrow * inner] = conj_bits<OUT_DF>(v);
+      if (s3 != kNoPartner) o4[s3 + (long)row * inner] = conj_bits<OUT_DF>(v);
+    }
+    return;
+  }
   if (mirror) {
     int4 *o4 = reinterpret_cast<int4 *>(out);
     for (int w = threadIdx.x; w < tile; w += blockDim.x) {
@@ -210,15 +277,15 @@ __global__ void __launch_bounds__(256) lattice_axis_kernel(const void *in, void 
 
 template <bool FWD, class E, bool IN_DF, bool OUT_DF>
 int launch_axis_as(const void *in, void *out, long outer, int n, long inner, double scale, cudaStream_t stream,
-                   SkipRows skip = SkipRows{nullptr, 0}, RowMirror mir = kNoRowMirror) {
+                   SkipRows skip = SkipRows{nullptr, 0}, RowMirror mir = kNoRowMirror, CompactPass cp = kNoCompact) {
   FftDesc d;
   int st = get_fft(n, &d);
   if (st) return st;
   // Tile of up to 64 columns (a power of two dividing the 256 threads), limited
   // by shared memory: one buffer of n x ncol elements (two with a generic radix)
-  // and the column offsets (twice with partner stores).
+  // and the column offsets (twice with partner stores, five for a compact pass).
   const int bufs = d.has_generic ? 2 : 1;
-  const size_t offs = (mir.on ? 2 : 1) * sizeof(long);
+  const size_t offs = (cp.gmax ? 5 : mir.on ? 2 : 1) * sizeof(long);
   const size_t budget = (size_t)std::min(max_smem_optin(), 200 * 1024);
   int ncol = 64;
   while (ncol > 1 && (size_t)bufs * n * ncol * sizeof(E) + ncol * offs > budget) ncol /= 2;
@@ -232,7 +299,7 @@ int launch_axis_as(const void *in, void *out, long outer, int n, long inner, dou
   if (blocks > 0x7fffffffL) return set_error(TPRF_ERR_INVALID_ARGUMENT, "lattice FFT: too many tiles");
   auto kern = lattice_axis_kernel<FWD, E, IN_DF, OUT_DF>;
   TPRF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  kern<<<(unsigned)blocks, 256, smem, stream>>>(in, out, ncols_total, inner, ncol, lg, d, scale, skip, mir);
+  kern<<<(unsigned)blocks, 256, smem, stream>>>(in, out, ncols_total, inner, ncol, lg, d, scale, skip, mir, cp);
   TPRF_KERNEL_LAUNCHED("lattice_axis_kernel");
   return TPRF_OK;
 }
@@ -241,15 +308,17 @@ int launch_axis_as(const void *in, void *out, long outer, int n, long inner, dou
 // input and output; double-float only with double-float arithmetic.
 template <bool FWD>
 int launch_axis(const void *in, bool in_df, void *out, bool out_df, long outer, int n, long inner, double scale,
-                cudaStream_t stream, SkipRows skip = SkipRows{nullptr, 0}, RowMirror mir = kNoRowMirror) {
+                cudaStream_t stream, SkipRows skip = SkipRows{nullptr, 0}, RowMirror mir = kNoRowMirror,
+                CompactPass cp = kNoCompact) {
   if (arith_mode() == kArithFP64) {
     if (in_df || out_df) return set_error(TPRF_ERR_INVALID_ARGUMENT, "lattice FFT: double-float storage in FP64 mode");
-    return launch_axis_as<FWD, double2, false, false>(in, out, outer, n, inner, scale, stream, skip, mir);
+    return launch_axis_as<FWD, double2, false, false>(in, out, outer, n, inner, scale, stream, skip, mir, cp);
   }
-  if (in_df && out_df) return launch_axis_as<FWD, cdf, true, true>(in, out, outer, n, inner, scale, stream, skip, mir);
-  if (in_df) return launch_axis_as<FWD, cdf, true, false>(in, out, outer, n, inner, scale, stream, skip, mir);
-  if (out_df) return launch_axis_as<FWD, cdf, false, true>(in, out, outer, n, inner, scale, stream, skip, mir);
-  return launch_axis_as<FWD, cdf, false, false>(in, out, outer, n, inner, scale, stream, skip, mir);
+  if (in_df && out_df)
+    return launch_axis_as<FWD, cdf, true, true>(in, out, outer, n, inner, scale, stream, skip, mir, cp);
+  if (in_df) return launch_axis_as<FWD, cdf, true, false>(in, out, outer, n, inner, scale, stream, skip, mir, cp);
+  if (out_df) return launch_axis_as<FWD, cdf, false, true>(in, out, outer, n, inner, scale, stream, skip, mir, cp);
+  return launch_axis_as<FWD, cdf, false, false>(in, out, outer, n, inner, scale, stream, skip, mir, cp);
 }
 
 // Two adjacent mesh axes in one pass: the array is [outer, n1, n2, n_target]
@@ -262,15 +331,26 @@ int launch_axis(const void *in, bool in_df, void *out, bool out_df, long outer, 
 template <bool FWD, class E, bool IN_DF, bool OUT_DF>
 __global__ void __launch_bounds__(256) lattice_plane_kernel(const void *in, void *out, long outer, long n_target,
                                                             int nt, int lgt, FftDesc d1, FftDesc d2, int lg2,
-                                                            double scale, SkipRows skip, RowMirror mir) {
+                                                            double scale, SkipRows skip, RowMirror mir,
+                                                            CompactPass cp) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   E *a = reinterpret_cast<E *>(smem_raw);
   const int n1 = d1.n, n2 = d2.n, P = n1 * n2;
+  // a compact pass runs in place on the canonical orbital columns (the grid is
+  // sized for the full layout; the CTAs past the compact tiles leave)
+  const bool cm = cp.active();
+  if (cm) {
+    in = cp.buf;
+    out = cp.buf;
+    outer = cp.outer;
+    n_target = cp.n_target;
+  }
   const long tiles_t = (n_target + nt - 1) / nt;
   const long o = blockIdx.x / tiles_t;
-  if (o < skip.columns && gmax_says_real(skip.gmax)) return;  // rows the partner rows fill
+  if (o >= outer) return;
+  if (!cm && o < skip.columns && gmax_says_real(skip.gmax)) return;  // rows the partner rows fill
   // partner stores: o is the row (the dims before the plane are trivial)
-  const bool mirror = mir.active();
+  const bool mirror = !cm && mir.active();
   const long prow = mir.c - o;
   if (mirror && prow > o) return;  // stored by the partner row's tiles
   const long t0 = (blockIdx.x - o * tiles_t) * (long)nt;
@@ -427,7 +507,7 @@ int plane_targets(int n1, int n2, long n_target) {
 
 template <bool FWD, class E, bool IN_DF, bool OUT_DF>
 int launch_plane_as(const void *in, void *out, long outer, int n1, int n2, long n_target, double scale,
-                    cudaStream_t stream, SkipRows skip, RowMirror mir) {
+                    cudaStream_t stream, SkipRows skip, RowMirror mir, CompactPass cp) {
   FftDesc d1, d2;
   int st = get_fft(n1, &d1);
   if (st) return st;
@@ -440,7 +520,7 @@ int launch_plane_as(const void *in, void *out, long outer, int n1, int n2, long 
   auto kern = lattice_plane_kernel<FWD, E, IN_DF, OUT_DF>;
   TPRF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   kern<<<(unsigned)tiles, 256, smem, stream>>>(in, out, outer, n_target, nt, log2i(nt), d1, d2, log2i(n2), scale,
-                                               skip, mir);
+                                               skip, mir, cp);
   TPRF_KERNEL_LAUNCHED("lattice_plane_kernel");
   return TPRF_OK;
 }
@@ -448,16 +528,19 @@ int launch_plane_as(const void *in, void *out, long outer, int n1, int n2, long 
 template <bool FWD>
 int launch_plane(const void *in, bool in_df, void *out, bool out_df, long outer, int n1, int n2, long n_target,
                  double scale, cudaStream_t stream, SkipRows skip = SkipRows{nullptr, 0},
-                 RowMirror mir = kNoRowMirror) {
+                 RowMirror mir = kNoRowMirror, CompactPass cp = kNoCompact) {
   if (arith_mode() == kArithFP64) {
     if (in_df || out_df) return set_error(TPRF_ERR_INVALID_ARGUMENT, "lattice FFT: double-float storage in FP64 mode");
-    return launch_plane_as<FWD, double2, false, false>(in, out, outer, n1, n2, n_target, scale, stream, skip, mir);
+    return launch_plane_as<FWD, double2, false, false>(in, out, outer, n1, n2, n_target, scale, stream, skip, mir,
+                                                       cp);
   }
   if (in_df && out_df)
-    return launch_plane_as<FWD, cdf, true, true>(in, out, outer, n1, n2, n_target, scale, stream, skip, mir);
-  if (in_df) return launch_plane_as<FWD, cdf, true, false>(in, out, outer, n1, n2, n_target, scale, stream, skip, mir);
-  if (out_df) return launch_plane_as<FWD, cdf, false, true>(in, out, outer, n1, n2, n_target, scale, stream, skip, mir);
-  return launch_plane_as<FWD, cdf, false, false>(in, out, outer, n1, n2, n_target, scale, stream, skip, mir);
+    return launch_plane_as<FWD, cdf, true, true>(in, out, outer, n1, n2, n_target, scale, stream, skip, mir, cp);
+  if (in_df)
+    return launch_plane_as<FWD, cdf, true, false>(in, out, outer, n1, n2, n_target, scale, stream, skip, mir, cp);
+  if (out_df)
+    return launch_plane_as<FWD, cdf, false, true>(in, out, outer, n1, n2, n_target, scale, stream, skip, mir, cp);
+  return launch_plane_as<FWD, cdf, false, false>(in, out, outer, n1, n2, n_target, scale, stream, skip, mir, cp);
 }
 
 // The TMA-staged plane pass with nt targets per tile (two tiles per CTA).
@@ -557,9 +640,13 @@ int launch_lattice_fft_scaled(bool forward, long n_w, const int dims[3], long n_
 // The general form: input and output each stored as complex128 or (with
 // double-float arithmetic) as double-float pairs; the passes in between hand
 // each other double-float pairs whenever the arithmetic is double-float.
+bool compact_r_to_q_applies(const int dims[3], long n_target) {
+  return dims[0] > 1 && dims[1] > 1 && dims[2] > 1 && plane_targets(dims[1], dims[2], n_target) > 0;
+}
+
 int launch_lattice_fft_fmt(bool forward, long n_w, const int dims[3], long n_target, const void *in, bool in_df,
                            void *out, bool out_df, double scale_last, cudaStream_t stream, const unsigned *gmax,
-                           bool fill_partners, long partner_c) {
+                           bool fill_partners, long partner_c, const CompactChi *cc) {
   const bool mid_df = arith_mode() != kArithFP64;
   // with gmax: the n_w = 2 nw - 1 bosonic rows of a real bubble; the first nw - 1
   // (negative frequencies) are left out of the passes, and the last pass stores
@@ -574,6 +661,24 @@ int launch_lattice_fft_fmt(bool forward, long n_w, const int dims[3], long n_tar
   int nontriv[3], nn = 0;
   for (int ax = 0; ax < 3; ++ax)
     if (dims[ax] > 1) nontriv[nn++] = ax;
+  // the compact canonical orbital columns (CompactChi): the plane pass in place
+  // on them, the axis pass from them to every column of `out`
+  // (the chain: the rows of both signs with the words, compact rows w = 0 .. nw - 1;
+  // a frequency block: its rows w = w0 .. with partner stores at partner_c - row)
+  CompactPass cplane = kNoCompact, caxis = kNoCompact;
+  if (cc && cc->gmax) {
+    const bool whole = gmax && cc->gmax == gmax && n_skip > 0 && cc->rows == n_skip + 1 && cc->w0 == 0;
+    const bool block = !gmax && fill_partners && cc->rows == n_w && cc->w0 >= 0;
+    if (!(whole || block) || !cc->buf || !cc->oc || !mid_df || !in_df || in != out ||
+        !compact_r_to_q_applies(dims, n_target))
+      return set_error(TPRF_ERR_INVALID_ARGUMENT, "lattice FFT: compact columns do not apply to this transform");
+    const OrbCanon &oc = *cc->oc;
+    const long row0 = whole ? n_skip : 0, prow0 = whole ? n_skip : partner_c;
+    cplane = CompactPass{cc->gmax, cc->buf, cc->rows * dims[0], oc.nc, oc.nc, (int)n_target, 0, 0, 0,
+                         oc.ocan, oc.orev};
+    caxis = CompactPass{cc->gmax, cc->buf, cc->rows, (long)dims[1] * dims[2] * oc.nc, oc.nc, (int)n_target,
+                        row0, prow0, cc->w0, oc.ocan, oc.orev};
+  }
   // the partner stores of the last pass, which transforms axis nontriv[0]
   auto mirror_for = [&](int ax) {
     if (!fill_partners) return kNoRowMirror;
@@ -614,9 +719,9 @@ int launch_lattice_fft_fmt(bool forward, long n_w, const int dims[3], long n_tar
                                                stream);
       if (st == kNotApplicable)
         st = forward ? launch_plane<true>(in, in_df, out, plane_out_df, outer, dims[A], dims[B], n_target, scale,
-                                          stream, pskip, pmir)
+                                          stream, pskip, pmir, cplane)
                      : launch_plane<false>(in, in_df, out, plane_out_df, outer, dims[A], dims[B], n_target, scale,
-                                           stream, pskip, pmir);
+                                           stream, pskip, pmir, cplane);
       if (st) return st;
       if (nn == 3) {
         const int ax = nontriv[0];
@@ -626,9 +731,9 @@ int launch_lattice_fft_fmt(bool forward, long n_w, const int dims[3], long n_tar
         const SkipRows askip{gmax, n_skip * (outer0 / n_w) * inner0};
         const RowMirror amir = mirror_for(ax);
         st = forward ? launch_axis<true>(out, mid_df, out, out_df, outer0, dims[ax], inner0, scale_last, stream, askip,
-                                         amir)
+                                         amir, caxis)
                      : launch_axis<false>(out, mid_df, out, out_df, outer0, dims[ax], inner0, scale_last, stream,
-                                          askip, amir);
+                                          askip, amir, caxis);
         if (st) return st;
       }
       return TPRF_OK;
@@ -835,7 +940,7 @@ int noalloc_axis(const double2 *in, double2 *out, long outer, long inner, const 
   auto kern = lattice_axis_kernel<FWD, E, false, false>;
   TPRF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   kern<<<(unsigned)blocks, 256, smem, stream>>>(in, out, ncols_total, inner, ncol, lg, d, scale, SkipRows{nullptr, 0},
-                                                kNoRowMirror);
+                                                kNoRowMirror, kNoCompact);
   TPRF_KERNEL_LAUNCHED("lattice_axis_kernel (no-alloc)");
   return TPRF_OK;
 }

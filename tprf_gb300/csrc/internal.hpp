@@ -208,6 +208,40 @@ int launch_lattice_fft(bool forward, long n_w, const int dims[3], long n_target,
                        cudaStream_t stream);
 int launch_lattice_fft_scaled(bool forward, long n_w, const int dims[3], long n_target, const double2 *in,
                               double2 *out, double scale, cudaStream_t stream);
+// Canonical orbital columns of a rank-4 bubble: the column o = abcd (a slowest,
+// o = ((a nb + b) nb + c) nb + d) is canonical when o <= rev(o) = dcba. When
+// the bubble's transposition pairs hold (chi0(w, -r)_dcba = chi0(w, r)_abcd bit
+// for bit), its r -> q transform gives chi0(w, -q)_dcba = chi0(w, q)_abcd, so
+// only the (nb^4 + nb^2) / 2 canonical columns need a transform.
+struct OrbCanon {
+  int nc;            // canonical columns
+  const int *ocan;   // device [nc]: the canonical columns in increasing order
+  const int *orev;   // device [nc]: rev(ocan[j])
+  const int *ocomp;  // device [nb^4]: j with ocan[j] == o, or -1
+};
+int get_orb_canon(int nb, const OrbCanon **out);
+
+// The compact form of chi0(w, r) on a real, transpose-symmetric bubble: the
+// rows w = 0 .. nw - 1 of the canonical columns, [nw][N_r][nc] as double-float
+// pairs in caller memory. The bubble writes it (instead of its output) and the
+// r -> q passes read it when the chain's words say so on the device
+// (canon_says_yes); otherwise it is left untouched and the full path runs.
+struct CompactChi {
+  const unsigned *gmax = nullptr;  // the chain's words; null: not used
+  void *buf = nullptr;             // compact row w0
+  long rows = 0;                   // nw (the whole chain), or the rows of a frequency block
+  const OrbCanon *oc = nullptr;
+  long w0 = 0;                     // the frequency of buf's first row
+};
+#ifdef __CUDACC__
+__device__ __forceinline__ bool canon_says_yes(const unsigned *gmax) {
+  return gmax_says_real(gmax) && hermitian_says_yes(gmax + 2) && transpose_says_yes(gmax + 2);
+}
+#endif
+// Whether the r -> q transform of launch_lattice_fft_fmt can take a CompactChi
+// on this mesh: three non-trivial axes, the last two in one plane pass.
+bool compact_r_to_q_applies(const int dims[3], long n_target);
+
 // Input / output stored as complex128 or (in_df / out_df, double-float
 // arithmetic only, N_k > 1) as double-float pairs of the same 16 bytes.
 // gmax (nullable): the rows are the 2 nw - 1 bosonic frequencies of a real
@@ -221,19 +255,26 @@ int launch_lattice_fft_scaled(bool forward, long n_w, const int dims[3], long n_
 // row partner_c - j; rows with partner_c - j > j are then not stored, and the
 // row with partner_c - j == j has no partner (a frequency block m0 .. m1 - 1
 // of the non-negative rows, out at row nw - 1 + m0: partner_c = -2 m0).
+// cc (with gmax, on a mesh where compact_r_to_q_applies): when the words say
+// canon_says_yes, the passes read cc->buf instead of `in` (the first in place,
+// the last writing every column and both signs of w to `out`); otherwise as
+// above.
 int launch_lattice_fft_fmt(bool forward, long n_w, const int dims[3], long n_target, const void *in, bool in_df,
                            void *out, bool out_df, double scale, cudaStream_t stream, const unsigned *gmax = nullptr,
-                           bool fill_partners = false, long partner_c = 0);
+                           bool fill_partners = false, long partner_c = 0, const CompactChi *cc = nullptr);
 // The fused bubble + tau -> iw, writing chi0(iw, r) as double-float pairs when
 // want_df and the double-float path runs (*wrote_df tells which). skip_neg:
 // on a real bubble (gmax words), the negative frequencies are left unwritten
 // for a following launch_lattice_fft_fmt with the same words, which fills them.
 // With gmax and the transposition words (gmax[2], gmax[4]) saying yes, only the
 // canonical columns of the rank-4 transposition pairs are transformed, each
-// result stored at its column and its partner.
+// result stored at its column and its partner; with cc as well (skip_neg and
+// want_df required), each result goes to the canonical orbital column of the
+// pair in cc->buf instead, and chi0_wr is not written.
 int launch_chi0_wr_from_grt_df(double beta, int n_tau, int nw, const int dims[3], int nb, const double2 *g,
                                const void *g_df, double2 *chi0_wr, cudaStream_t stream, bool want_df, bool *wrote_df,
-                               const unsigned *gmax = nullptr, bool skip_neg = false);
+                               const unsigned *gmax = nullptr, bool skip_neg = false,
+                               const CompactChi *cc = nullptr);
 // iv -> tau writing the double-float copy as well; gmax (nullable, zeroed by
 // the caller) receives max |G| and max |Im G| for launch_chi0_wr_from_grt_df,
 // which pairs real bubble columns when G is real.

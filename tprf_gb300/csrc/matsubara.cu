@@ -467,6 +467,12 @@ struct BubblePairLoaderDF : BubbleLoaderDF {
   bool pairs = false;
   bool compact = false;  // gdf holds real parts only (dfl per element): iv -> tau ran on real pairs
   bool canon = false;    // transform the canonical columns of tpairs only
+  // canonical orbital output (CompactChi): in the canonical mode each result
+  // goes to cout[w][r][ocomp[o]] for whichever of its column (r, o) and partner
+  // is a canonical orbital column (both when o is a palindrome), rows w >= 0
+  cdf *cout = nullptr;
+  const int *ocomp = nullptr;
+  int nc = 0;
   __device__ __forceinline__ void init() {
     pairs = gmax_says_real(gmax);
     compact = pairs && hermitian_says_yes(gmax + 2);
@@ -545,13 +551,25 @@ __global__ void __launch_bounds__(kMatsubaraThreads, 2) tau_to_w_kernel(TauWPlan
   const int ncol = (int)min((long)ic, n_fft_cols - col0);
   ld.setup(col0, ic, ncol, soff);
   __shared__ int s_tcol[64], s_tpar[64];  // canonical mode: the CTA's real columns and partners (ic <= 32)
+  bool corb = false;  // canonical orbital output: s_tcol / s_tpar hold compact offsets r nc + j (or -1)
   if constexpr (HasPairs<Loader>::value) {
+    corb = canon && ld.cout != nullptr;
     if (canon)
       for (int k = tid; k < 2 * ic; k += nthr) {
         const long f = 2 * col0 + k;
         const int2 cp = f < n_real ? ld.tpairs[f] : make_int2(0, 0);
-        s_tcol[k] = cp.x;
-        s_tpar[k] = cp.y;
+        if (corb) {
+          const int nb4 = ld.nb * ld.nb * ld.nb * ld.nb;
+          auto dst = [&](int col) {
+            const int r = col / nb4, j = ld.ocomp[col - r * nb4];
+            return j >= 0 ? r * ld.nc + j : -1;
+          };
+          s_tcol[k] = dst(cp.x);
+          s_tpar[k] = cp.y != cp.x ? dst(cp.y) : -1;
+        } else {
+          s_tcol[k] = cp.x;
+          s_tpar[k] = cp.y;
+        }
       }
   }
   __syncthreads();
@@ -693,6 +711,13 @@ __global__ void __launch_bounds__(kMatsubaraThreads, 2) tau_to_w_kernel(TauWPlan
         const bool neg = mh > 0 && !skip_neg;
         // real column fh gets val (its memory column, and in the canonical mode its partner)
         auto put = [&](long fh, C val) {
+          if (corb) {  // the canonical orbital column(s) of the pair, row w = mh of cout
+            const long row = (long)mh * ld.Nr * ld.nc;
+            const int d1 = s_tcol[fh - 2 * col0], d2 = s_tpar[fh - 2 * col0];
+            if (d1 >= 0) reinterpret_cast<C *>(ld.cout)[row + d1] = val;
+            if (d2 >= 0) reinterpret_cast<C *>(ld.cout)[row + d2] = val;
+            return;
+          }
           long col = fh, pc = -1;
           if (canon) {
             col = s_tcol[fh - 2 * col0];
@@ -1302,7 +1327,7 @@ int launch_chi0_wr_from_grt(double beta, int n_tau, int nw, const int dims[3], i
 // takes the complex128 path.
 int launch_chi0_wr_from_grt_df(double beta, int n_tau, int nw, const int dims[3], int nb, const double2 *g,
                                const void *g_df, double2 *chi0_wr, cudaStream_t stream, bool want_df, bool *wrote_df,
-                               const unsigned *gmax, bool skip_neg) {
+                               const unsigned *gmax, bool skip_neg, const CompactChi *cc) {
   if (wrote_df) *wrote_df = false;
   if (!g_df || arith_mode() == kArithFP64) return launch_chi0_wr_from_grt(beta, n_tau, nw, dims, nb, g, chi0_wr, stream);
   int st = check_tau_w(beta, n_tau, nw);
@@ -1319,6 +1344,11 @@ int launch_chi0_wr_from_grt_df(double beta, int n_tau, int nw, const int dims[3]
     if ((st = get_transpose_pairs(dims, nb, 4, &tp))) return st;
     ld.tpairs = tp->pairs;
     ld.n_can = tp->n_can;
+    if (cc && cc->gmax == gmax && cc->buf && cc->oc && skip_neg && want_df) {
+      ld.cout = reinterpret_cast<cdf *>(cc->buf);
+      ld.ocomp = cc->oc->ocomp;
+      ld.nc = cc->oc->nc;
+    }
   }
   const long C = ld.Nr * nb * nb * nb * nb;
   st = gmax ? launch_tau_to_w_as<BubblePairLoaderDF, cdf>(p, ld, chi0_wr, C, stream, want_df, skip_neg)

@@ -47,9 +47,15 @@ namespace tprf {
 // events[0..3] (nullable) are recorded before and after each stage. *chi_df:
 // chi0(w, r) was written as double-float pairs; *gmax_out: the real-input words
 // of the bubble, which the r -> q mirror and the pair solves use.
+// cc (nullable): the caller transforms r -> q next with launch_lattice_fft_fmt
+// and can take the compact canonical orbital columns (CompactChi); where they
+// apply, *cc is filled (cc->gmax set) and the bubble writes them when its words
+// say canon_says_yes. They live in rows 9 .. n_tau - 10 of the complex128
+// G(tau, r), which the bubble does not read on that path (it reads the
+// double-float copy and the 18 sampled rows at both ends).
 int bubble_to_wr(double beta, int n_iw, int n_tau, int nw, const int dims[3], int nb, const double *g_wk,
                  const double *moments, double2 *out, void *workspace, size_t workspace_bytes, void *const *events,
-                 cudaStream_t s, bool *chi_df, unsigned **gmax_out) {
+                 cudaStream_t s, bool *chi_df, unsigned **gmax_out, CompactChi *cc) {
   if (!dims || !g_wk || !out || !workspace || nb < 1 || nb > 8 || nw < 1 || n_iw < 1)
     return set_error(TPRF_ERR_INVALID_ARGUMENT, "imtime_bubble_chi0_wk: bad shape or null pointer");
   if (n_tau < 0) n_tau = default_n_tau(n_iw);
@@ -86,10 +92,21 @@ int bubble_to_wr(double beta, int n_iw, int n_tau, int nw, const int dims[3], in
   // chi0(w, r) goes from the bubble to the r -> q transform as double-float
   // pairs (same bytes) on the double-float path: no conversion in between
   *chi_df = false;
+  if (cc) {
+    *cc = CompactChi{};
+    const OrbCanon *oc = nullptr;
+    const long nb4 = nb2 * nb2;
+    if (nw >= 2 && nk > 1 && arith_mode() != kArithFP64 && compact_r_to_q_applies(dims, nb4) && n_tau >= 19) {
+      if ((st = get_orb_canon(nb, &oc))) return st;
+      if ((long)nw * oc->nc <= (long)(n_tau - 18) * nb2)
+        *cc = CompactChi{gmax, g_tr + 9L * nk * nb2, (long)nw, oc};
+    }
+  }
   if (nw == 1)
     st = launch_chi0_w0r_from_grt(beta, n_tau, dims, nb, g_tr, out, s);
   else
-    st = launch_chi0_wr_from_grt_df(beta, n_tau, nw, dims, nb, g_tr, g_tr_df, out, s, nk > 1, chi_df, gmax, nk > 1);
+    st = launch_chi0_wr_from_grt_df(beta, n_tau, nw, dims, nb, g_tr, g_tr_df, out, s, nk > 1, chi_df, gmax, nk > 1,
+                                    cc && cc->gmax ? cc : nullptr);
   if (st || (st = mark(3))) return st;
   return TPRF_OK;
 }
@@ -104,13 +121,16 @@ extern "C" int tprf_imtime_bubble_chi0_wk_timed(double beta, int n_iw, int n_tau
   double2 *out = reinterpret_cast<double2 *>(chi0_wk);
   bool chi_df = false;
   unsigned *gmax = nullptr;
+  CompactChi cc;
   int st = bubble_to_wr(beta, n_iw, n_tau, nw, dims, nb, g_wk, moments, out, workspace, workspace_bytes, events, s,
-                        &chi_df, &gmax);
+                        &chi_df, &gmax, &cc);
   if (st) return st;
   const long nb4 = (long)nb * nb * nb * nb;
   // on a real bubble (the same words) only the non-negative frequencies are
-  // transformed; the others follow by symmetry
-  st = launch_lattice_fft_fmt(false, 2L * nw - 1, dims, nb4, out, chi_df, out, false, 1.0, s, chi_df ? gmax : nullptr);
+  // transformed; the others follow by symmetry; on a transpose-symmetric one
+  // only the canonical orbital columns (cc)
+  st = launch_lattice_fft_fmt(false, 2L * nw - 1, dims, nb4, out, chi_df, out, false, 1.0, s, chi_df ? gmax : nullptr,
+                              false, 0, chi_df && cc.gmax ? &cc : nullptr);
   if (st) return st;
   if (events && events[4]) TPRF_CUDA(cudaEventRecord(static_cast<cudaEvent_t>(events[4]), s));
   return finish_with_checks(s, "imtime_bubble_chi0_wk");

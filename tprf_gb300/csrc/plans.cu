@@ -675,6 +675,46 @@ int get_tail_fit_plan(double beta, int n, bool fermion, const TailFitPlan **out)
   return TPRF_OK;
 }
 
+int get_orb_canon(int nb, const OrbCanon **out) {
+  if (nb < 1 || nb > 8) return set_error(TPRF_ERR_INVALID_ARGUMENT, "orbital canon: bad nb");
+  unsigned long long dev = 0;  // the context: tables die with it
+  int st = current_context_key(&dev);
+  if (st) return st;
+  static std::map<std::tuple<unsigned long long, int>, std::unique_ptr<OrbCanon>> cache;
+  auto key = std::make_tuple(dev, nb);
+  {
+    std::lock_guard<std::mutex> lock(g_mutex);
+    auto it = cache.find(key);
+    if (it != cache.end()) {
+      *out = it->second.get();
+      return TPRF_OK;
+    }
+  }
+  const int E = nb * nb * nb * nb;
+  std::vector<int> ocan, orev, ocomp((size_t)E, -1);
+  for (int o = 0; o < E; ++o) {
+    // dcba of o = abcd: the base-nb digits in reverse order
+    int x = o, r = 0;
+    for (int i = 0; i < 4; ++i) {
+      r = r * nb + x % nb;
+      x /= nb;
+    }
+    if (o <= r) {
+      ocomp[(size_t)o] = (int)ocan.size();
+      ocan.push_back(o);
+      orev.push_back(r);
+    }
+  }
+  auto p = std::make_unique<OrbCanon>();
+  p->nc = (int)ocan.size();
+  if ((st = upload(ocan, &p->ocan)) || (st = upload(orev, &p->orev)) || (st = upload(ocomp, &p->ocomp))) return st;
+  std::lock_guard<std::mutex> lock(g_mutex);
+  auto &slot = cache[key];
+  if (!slot) slot = std::move(p);
+  *out = slot.get();
+  return TPRF_OK;
+}
+
 int get_transpose_pairs(const int dims[3], int nb, int rank, const TransposePairs **out) {
   unsigned long long dev = 0;  // the context: plans die with it
   int st = current_context_key(&dev);
