@@ -147,9 +147,13 @@ struct CompactPass {
   // conjugate partner (for w0 + o > 0) to row prow0 - o
   long row0, prow0, w0;
   const int *ocan, *orev;
+  // axis: the k points in tile order (get_k_pair_order), so that the columns of
+  // k and -k, which fill each other's output rows, are stored close in time and
+  // their 32-byte sectors reach DRAM whole
+  const int *kperm;
   __device__ __forceinline__ bool active() const { return gmax != nullptr && canon_says_yes(gmax); }
 };
-constexpr CompactPass kNoCompact{nullptr, nullptr, 0, 0, 0, 0, 0, 0, 0, nullptr, nullptr};
+constexpr CompactPass kNoCompact{nullptr, nullptr, 0, 0, 0, 0, 0, 0, 0, nullptr, nullptr, nullptr};
 
 template <bool FWD, class E, bool IN_DF, bool OUT_DF>
 __global__ void __launch_bounds__(256) lattice_axis_kernel(const void *in, void *out, long ncols_total,
@@ -180,13 +184,14 @@ __global__ void __launch_bounds__(256) lattice_axis_kernel(const void *in, void 
       long bs = -1, s[4] = {kNoPartner, kNoPartner, kNoPartner, kNoPartner};
       if (f < cp.outer * cp.n_target) {
         const long o = f / cp.n_target, rem = f - o * cp.n_target;
-        const long kk = rem / cp.nc;
-        const int j = (int)(rem - kk * cp.nc);
+        const long pos = rem / cp.nc;
+        const int j = (int)(rem - pos * cp.nc);
+        const long kk = cp.kperm[pos];
         const long k1 = kk / mir.e2, k2 = kk - k1 * mir.e2;
         const long mk = (k1 ? mir.e1 - k1 : 0) * (long)mir.e2 + (k2 ? mir.e2 - k2 : 0);
         const int t = cp.ocan[j], tr = cp.orev[j];
         const long O = cp.row0 + o, P = cp.prow0 - o;
-        bs = o * n * cp.n_target + rem;
+        bs = o * n * cp.n_target + kk * cp.nc + j;
         s[0] = O * n * inner + kk * cp.nb4 + t;
         if (tr != t) s[1] = O * n * inner + mk * cp.nb4 + tr;
         if (cp.w0 + o > 0) {
@@ -674,10 +679,12 @@ int launch_lattice_fft_fmt(bool forward, long n_w, const int dims[3], long n_tar
       return set_error(TPRF_ERR_INVALID_ARGUMENT, "lattice FFT: compact columns do not apply to this transform");
     const OrbCanon &oc = *cc->oc;
     const long row0 = whole ? n_skip : 0, prow0 = whole ? n_skip : partner_c;
+    const int *kperm = nullptr;
+    if (int st = get_k_pair_order(dims[1], dims[2], &kperm)) return st;
     cplane = CompactPass{cc->gmax, cc->buf, cc->rows * dims[0], oc.nc, oc.nc, (int)n_target, 0, 0, 0,
-                         oc.ocan, oc.orev};
+                         oc.ocan, oc.orev, nullptr};
     caxis = CompactPass{cc->gmax, cc->buf, cc->rows, (long)dims[1] * dims[2] * oc.nc, oc.nc, (int)n_target,
-                        row0, prow0, cc->w0, oc.ocan, oc.orev};
+                        row0, prow0, cc->w0, oc.ocan, oc.orev, kperm};
   }
   // the partner stores of the last pass, which transforms axis nontriv[0]
   auto mirror_for = [&](int ax) {

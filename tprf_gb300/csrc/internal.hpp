@@ -220,6 +220,10 @@ struct OrbCanon {
   const int *ocomp;  // device [nb^4]: j with ocan[j] == o, or -1
 };
 int get_orb_canon(int nb, const OrbCanon **out);
+// The points k = (k1, k2) of a d1 x d2 mesh (k = k1 d2 + k2) ordered so that each
+// k is followed by -k (unless k = -k): the last r -> q pass on compact columns
+// writes the columns of k and of -k from one tile or two neighbouring ones.
+int get_k_pair_order(int d1, int d2, const int **out);
 
 // The compact form of chi0(w, r) on a real, transpose-symmetric bubble: the
 // rows w = 0 .. nw - 1 of the canonical columns, [nw][N_r][nc] as double-float

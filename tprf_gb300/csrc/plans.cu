@@ -715,6 +715,42 @@ int get_orb_canon(int nb, const OrbCanon **out) {
   return TPRF_OK;
 }
 
+int get_k_pair_order(int d1, int d2, const int **out) {
+  if (d1 < 1 || d2 < 1) return set_error(TPRF_ERR_INVALID_ARGUMENT, "k pair order: bad mesh");
+  unsigned long long dev = 0;  // the context: tables die with it
+  int st = current_context_key(&dev);
+  if (st) return st;
+  static std::map<std::tuple<unsigned long long, int, int>, const int *> cache;
+  auto key = std::make_tuple(dev, d1, d2);
+  {
+    std::lock_guard<std::mutex> lock(g_mutex);
+    auto it = cache.find(key);
+    if (it != cache.end()) {
+      *out = it->second;
+      return TPRF_OK;
+    }
+  }
+  std::vector<int> order;
+  order.reserve((size_t)d1 * d2);
+  for (int k1 = 0; k1 < d1; ++k1)
+    for (int k2 = 0; k2 < d2; ++k2) {
+      const int k = k1 * d2 + k2, mk = ((d1 - k1) % d1) * d2 + (d2 - k2) % d2;
+      if (k < mk) {
+        order.push_back(k);
+        order.push_back(mk);
+      } else if (k == mk) {
+        order.push_back(k);
+      }
+    }
+  const int *p = nullptr;
+  if ((st = upload(order, &p))) return st;
+  std::lock_guard<std::mutex> lock(g_mutex);
+  auto &slot = cache[key];
+  if (!slot) slot = p;
+  *out = slot;
+  return TPRF_OK;
+}
+
 int get_transpose_pairs(const int dims[3], int nb, int rank, const TransposePairs **out) {
   unsigned long long dev = 0;  // the context: plans die with it
   int st = current_context_key(&dev);
