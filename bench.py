@@ -43,21 +43,35 @@ C16 = 16  # bytes per complex128
 # (real hoppings: G(tau, r) real, G(-iv) = G(iv)^dagger, chi0(-w) from chi0(w))
 # iv -> tau reads the frequencies v >= 0 and writes real G(tau, r) (8 bytes per
 # element), the bubble writes the frequencies w >= 0 and r -> q reads those and
-# writes all 2 nw - 1.
+# writes all 2 nw - 1. On a three-dimensional mesh whose last two axes are
+# powers of two, the bubble writes only the canonical orbital columns
+# abcd <= dcba ((nb^4 + nb^2) / 2 of nb^4; compact_columns) and r -> q reads those.
 
-def stage_model(nb, nk, n_nu, n_tau, nw, real=True):
+def compact_columns(dims, nb, n_tau, nw, real=True):
+    """Canonical orbital columns the bubble hands to r -> q on this workload (the
+    library's compact path), or None where the full columns are used."""
+    pow2 = lambda n: n >= 2 and n & (n - 1) == 0  # noqa: E731
+    nc = (nb ** 4 + nb ** 2) // 2
+    if (real and nw >= 2 and all(d > 1 for d in dims) and pow2(dims[1]) and pow2(dims[2])
+            and max(dims[1], dims[2]) <= 256 and nw * nc <= (n_tau - 18) * nb * nb):
+        return nc
+    return None
+
+
+def stage_model(nb, nk, n_nu, n_tau, nw, real=True, nc=None):
     nb2, nb4, nwt = nb * nb, nb ** 4, 2 * nw - 1
     L = n_tau - 1
     fft_flops = lambda n: 5.0 * n * math.log2(n) if n > 1 else 0.0  # noqa: E731
     g_tau = (8 if real else C16) * nb2 * nk * n_tau
     w_out = nw if real else nwt
+    cols = nc or nb4  # the columns of chi0(w, r) the bubble writes
     return {
         "dyson": dict(bytes=C16 * nb2 * (n_nu + 1) * nk, flops=n_nu * nk * 8.0 * nb ** 3),
         "fft_k_to_r": dict(bytes=2 * C16 * nb2 * n_nu * nk, flops=n_nu * nb2 * fft_flops(nk)),
         "nu_to_tau": dict(bytes=C16 * nb2 * nk * (n_nu // 2 if real else n_nu) + g_tau,
                           flops=nk * nb2 * fft_flops(L)),
-        "bubble_tau_to_w": dict(bytes=g_tau + C16 * nb4 * nk * w_out, flops=nk * nb4 * (6.0 * n_tau + fft_flops(L))),
-        "fft_r_to_q": dict(bytes=C16 * nb4 * nk * (w_out + nwt), flops=nwt * nb4 * fft_flops(nk)),
+        "bubble_tau_to_w": dict(bytes=g_tau + C16 * cols * nk * w_out, flops=nk * nb4 * (6.0 * n_tau + fft_flops(L))),
+        "fft_r_to_q": dict(bytes=C16 * nk * (cols * w_out + nb4 * nwt), flops=nwt * nb4 * fft_flops(nk)),
         "rpa": dict(bytes=2 * C16 * nb4 * nwt * nk, flops=nwt * nk * 8.0 * (nb2 ** 3 * 2 + nb2 ** 3 / 3.0)),
     }
 
@@ -631,7 +645,7 @@ def run_gpu(args):
 
     # ---- roofline of the dominant kernel
     real = all(not np.any(np.imag(np.asarray(h))) for h in cfg["hoppings"].values())
-    model = stage_model(nb, nk, n_nu, n_tau, nw, real=real)
+    model = stage_model(nb, nk, n_nu, n_tau, nw, real=real, nc=compact_columns(dims, nb, n_tau, nw, real=real))
     top = max(stage_ms, key=stage_ms.get)
     peaks = {}
     try:

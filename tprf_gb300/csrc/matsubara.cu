@@ -703,9 +703,24 @@ __global__ void __launch_bounds__(kMatsubaraThreads, 2) tau_to_w_kernel(TauWPlan
         const int c = w & (ic - 1), mh = w >> lg;
         if (c >= ncol) continue;
         const int mp = nw - 1 + mh, mn = nw - 1 - mh;
-        const C vp = value(c, mp), vn = conj_el(value(c, mn));
-        const C F = half_el(cadd(vp, vn)), D = half_el(csub(vp, vn));
-        const C H = mul_mi<true>(D);  // (vp - conj(vn)) / (2 i)
+        // F = (T(z)(m) + conj(T(z)(-m))) / 2 and H = (T(z)(m) - conj(T(z)(-m))) / (2 i),
+        // the FFT terms as such; in the tail, a_j = a_j(f) + i a_j(h) with real
+        // a_j(f), a_j(h) (the fit is linear with real coefficients) and
+        // K_j(-m) = conj(K_j(m)) (the transform of a real one-pole function), so
+        // F takes a_j(f) K_j(m) and H takes a_j(h) K_j(m)
+        auto fft_term = [&](int mi) {
+          const int m = mi + p.out0;
+          return cscale(last_stage_output<false>(r, p.fft, ic, c, m < 0 ? m + L : m), fact);
+        };
+        const C vp = fft_term(mp), vn = conj_el(fft_term(mn));
+        C F = half_el(cadd(vp, vn));
+        C H = mul_mi<true>(half_el(csub(vp, vn)));
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          const C k = table<C>(p.K, p.Kf, (long)j * nwt + mp), a = am[j * ic + c];
+          F = cadd(F, cscale(k, a.x));
+          H = cadd(H, cscale(k, a.y));
+        }
         const long f = 2 * (col0 + c);
         // the negative frequencies only when the caller does not fill them by symmetry
         const bool neg = mh > 0 && !skip_neg;
