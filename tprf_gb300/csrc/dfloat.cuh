@@ -12,7 +12,10 @@
 // is what an FFT needs. Every float operation uses a _rn intrinsic so the
 // compiler can neither contract nor reassociate it.
 //
-// Conversions from and to FP64 use integer bit operations only.
+// Conversions from FP64 use integer bit operations only (the FP64 pipe's
+// conversion instructions are slower on GB300); conversions to FP64 widen the
+// two floats by bit operations and add them with one FP64 addition
+// (to_double_add), or use bit operations only (to_double).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -227,6 +230,13 @@ __device__ __forceinline__ double to_double(dfl a) {
   }
   const unsigned long long sign = (unsigned long long)(hb & 0x80000000u) << 32;
   return __longlong_as_double((long long)(sign | ((unsigned long long)(e - 127 + 1023) << 52) | (M & ((1ull << 52) - 1))));
+}
+
+// hi + lo as a double with one FP64 operation: both floats widened exactly by
+// bit operations, then a correctly rounded FP64 addition. Fewer instructions
+// than to_double where the FP64 pipe has room (the RPA's outputs).
+__device__ __forceinline__ double to_double_add(dfl a) {
+  return __dadd_rn(float_to_double_exact(a.hi), float_to_double_exact(a.lo));
 }
 
 __device__ __forceinline__ cdf to_cdf(double2 z) { return cdf{split_double(z.x), split_double(z.y)}; }

@@ -16,7 +16,10 @@ __device__ __forceinline__ int colmap(int c) {  // grouped column (d, c') -> off
 __device__ __forceinline__ double2 el_from(double2 z, double2 *) { return z; }
 __device__ __forceinline__ cdf el_from(double2 z, cdf *) { return to_cdf(z); }
 __device__ __forceinline__ double2 el_to(double2 z) { return z; }
-__device__ __forceinline__ double2 el_to(cdf z) { return to_double2(z); }
+// the solves' outputs: one FP64 addition per part (the FP64 pipe is otherwise
+// nearly idle in the RPA kernels, and the bit-operation conversion took a tenth
+// of the pair kernel's time)
+__device__ __forceinline__ double2 el_to(cdf z) { return make_double2(to_double_add(z.x), to_double_add(z.y)); }
 __device__ __forceinline__ double2 el_one(double2 *) { return make_double2(1.0, 0.0); }
 __device__ __forceinline__ cdf el_one(cdf *) { return cdf{dfl{1.f, 0.f}, dfl{0.f, 0.f}}; }
 __device__ __forceinline__ double2 el_zero(double2 *) { return make_double2(0.0, 0.0); }

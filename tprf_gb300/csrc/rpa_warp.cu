@@ -311,12 +311,6 @@ __global__ void __launch_bounds__(512) rpa_warp_kernel(long n_points, int nb_in,
 constexpr float kTransposeTol2 = 1e-24f;  // kTransposeTol = 1e-12, squared
 
 // max(|Re(a - b)|, |Im(a - b)|) and max(|Re a|, |Im a|) as floats
-__device__ __forceinline__ float el_diff_max(double2 a, double2 b) {
-  return (float)fmax(fabs(a.x - b.x), fabs(a.y - b.y));
-}
-__device__ __forceinline__ float el_diff_max(cdf a, cdf b) {
-  return fmaxf(fabsf(dsub(a.x, b.x).hi), fabsf(dsub(a.y, b.y).hi));
-}
 __device__ __forceinline__ float el_max_abs(double2 a) { return (float)fmax(fabs(a.x), fabs(a.y)); }
 __device__ __forceinline__ float el_max_abs(cdf a) { return fmaxf(fabsf(a.x.hi), fabsf(a.y.hi)); }
 
@@ -439,19 +433,29 @@ __global__ void __launch_bounds__(448, 2) rpa_pair_kernel(int nw, int d0, int d1
     float dmax = 0.f, amax = 0.f;
     bool sym3 = false;
     if (quad) {
+      const double2 *x0 = chi0 + p0 * N * N;
       const double2 *x2 = chi0 + ((long)(nw - 1 + mh) * nk + mq) * N * N;
       const double2 *x3 = chi0 + ((long)(nw - 1 - mh) * nk + q) * N * N;
       bool s3 = ureal;
+      // the largest |chi0(w, -q) - chi0(w, q)^T| in FP64, kept as the bits of a
+      // non-negative double (which order as integers; a NaN difference sorts above
+      // every number and refuses the transpose)
+      unsigned long long dbits = 0ull;
       for (int o = lane; o < N * N; o += G) {
         const int i = o / N, j = col_of_offset(o % N, nb);
         const double2 b = x2[o], c = x3[o];
         s3 = s3 && __double_as_longlong(b.x) == __double_as_longlong(c.x) &&
              __double_as_longlong(b.y) == __double_as_longlong(-c.y);
-        const E a = M[j * row_ld(N) + N + i];  // chi0(w, q)[j][i]
-        dmax = fmaxf(dmax, el_diff_max(el_from(b, (E *)nullptr), a));
-        amax = fmaxf(amax, el_max_abs(a));
+        const double2 a0 = x0[j * N + offset_of_col(i, nb)];  // chi0(w, q)[j][i], as loaded into B
+        const unsigned long long dx = (unsigned long long)__double_as_longlong(__dsub_rn(b.x, a0.x)) & ~(1ull << 63);
+        const unsigned long long dy = (unsigned long long)__double_as_longlong(__dsub_rn(b.y, a0.y)) & ~(1ull << 63);
+        dbits = dbits > dx ? dbits : dx;
+        dbits = dbits > dy ? dbits : dy;
+        amax = fmaxf(amax, el_max_abs(M[j * row_ld(N) + N + i]));
       }
       sym3 = __all_sync(gmask, s3);
+      const double dm = __longlong_as_double((long long)dbits);
+      dmax = dm != dm ? INFINITY : __double2float_ru(dm);  // rounded up: the test stays conservative
       dmax = group_max<G>(dmax, gmask);
       amax = group_max<G>(amax, gmask);
     }
