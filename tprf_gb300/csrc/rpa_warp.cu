@@ -97,10 +97,13 @@ __device__ __forceinline__ void group_argmax(MagT &best, int &p, unsigned gmask)
       }
     }
   } else if constexpr (sizeof(MagT) == 4) {
-    const unsigned key = best > 0 ? __float_as_uint(best) : 0u;
+    // one reduction: the magnitude's bits above the low six, then 63 - row (N <= 64),
+    // so the largest key is the largest magnitude (to 2^-17 relative, which is all
+    // the choice of a pivot needs) with the smallest row among equals
+    const unsigned key = (best > 0 ? (__float_as_uint(best) & ~63u) : 0u) | (63u - (unsigned)p);
     const unsigned kmax = __reduce_max_sync(gmask, key);
-    p = (int)__reduce_min_sync(gmask, key == kmax ? (unsigned)p : 0xffffffffu);
-    best = __uint_as_float(kmax);
+    p = 63 - (int)(kmax & 63u);
+    best = __uint_as_float(kmax & ~63u);
   } else {
     const unsigned long long key = best > 0 ? (unsigned long long)__double_as_longlong(best) : 0ull;
     const unsigned hi = (unsigned)(key >> 32), lo = (unsigned)key;
