@@ -24,14 +24,35 @@
 namespace tprf {
 namespace {
 
-struct SparseU {  // U grouped and compacted by columns: rows and FP64 values
-  const double2 *val;
-  const int *row;
-  const int *cs;  // [N + 1] column starts
-};
-
 // the grouped column index of the memory offset m = c' * nb + d inside a row
 __device__ __forceinline__ int col_of_offset(int m, int nb) { return (m % nb) * nb + m / nb; }
+// grouped column index j -> memory offset of that column inside a row
+__device__ __forceinline__ int offset_of_col(int j, int nb) { return (j % nb) * nb + j / nb; }
+
+// U grouped and compacted by columns in shared memory: rows and values, the
+// values as the kernel's element type (double-float pairs in the double-float
+// kernels, converted once per CTA, so that no solve converts them); an FP64
+// solve inside a double-float kernel (the re-solve) reads U itself.
+struct SparseU {
+  const void *val;     // [nnz] E
+  const int *row;
+  const int *cs;       // [N + 1] column starts
+  const double2 *Ug;   // U in memory order
+  bool df;             // val holds double-float pairs
+};
+template <class E> __device__ __forceinline__ E u_el(const SparseU &u, int t, int c, int N, int nb);
+template <>
+__device__ __forceinline__ double2 u_el<double2>(const SparseU &u, int t, int c, int N, int nb) {
+  return u.df ? u.Ug[u.row[t] * N + offset_of_col(c, nb)] : static_cast<const double2 *>(u.val)[t];
+}
+template <> __device__ __forceinline__ cdf u_el<cdf>(const SparseU &u, int t, int, int, int) {
+  return static_cast<const cdf *>(u.val)[t];
+}
+
+// Shared memory of a CTA's compacted U: [N^2] values, [N^2] rows, [N + 1] column starts
+__host__ __device__ constexpr size_t sparse_u_bytes(int N) {
+  return ((size_t)N * N * (sizeof(double2) + sizeof(int)) + (N + 1) * sizeof(int) + 15) & ~(size_t)15;
+}
 
 // Shared-memory layout of a group's augmented matrix [A | B] (N x 2N, 16-byte
 // elements; a quarter-warp's 16-byte accesses hit 8 distinct bank quads when
@@ -203,7 +224,7 @@ __device__ typename Mag<E>::type rpa_point_warp(const double2 *__restrict__ x, d
     float mag = (r == c) ? 1.f : 0.f;
     for (int t = u.cs[c]; t < u.cs[c + 1]; ++t) {
       const E xv = MM(r, N + u.row[t]);
-      const E uv = el_from(u.val[t], (E *)nullptr);
+      const E uv = u_el<E>(u, t, c, N, nb);
       s = el_fms(xv, uv, s);
       mag = fmaf(el_absf(xv), el_absf(uv), mag);
     }
@@ -252,7 +273,7 @@ __global__ void __launch_bounds__(512) rpa_warp_kernel(long n_points, int nb_in,
   double2 *s_val = reinterpret_cast<double2 *>(smem_raw);
   int *s_row = reinterpret_cast<int *>(s_val + N * N);
   int *s_cs = s_row + N * N;
-  const size_t u_bytes = ((size_t)N * N * (sizeof(double2) + sizeof(int)) + (N + 1) * sizeof(int) + 15) & ~(size_t)15;
+  const size_t u_bytes = sparse_u_bytes(N);
   // groups of G lanes, one point per group, 32 / G groups in each warp (the
   // lanes past the last whole group of a warp stay idle)
   constexpr int GPW = 32 / G;
@@ -278,7 +299,14 @@ __global__ void __launch_bounds__(512) rpa_warp_kernel(long n_points, int nb_in,
     s_cs[N] = t;
   }
   __syncthreads();
-  const SparseU u{s_val, s_row, s_cs};
+  if constexpr (IsDf<E>::value) {  // the values in the element type, in place
+    for (int t = threadIdx.x; t < s_cs[N]; t += blockDim.x) {
+      const double2 v = s_val[t];
+      reinterpret_cast<cdf *>(s_val)[t] = to_cdf(v);
+    }
+    __syncthreads();
+  }
+  const SparseU u{s_val, s_row, s_cs, U, IsDf<E>::value};
   if (!active) return;
   for (long pt = (long)blockIdx.x * n_grp + grp; pt < n_points; pt += (long)gridDim.x * n_grp) {
     const double2 *x = chi0 + pt * N * N;
@@ -316,9 +344,6 @@ constexpr float kTransposeTol2 = 1e-24f;  // kTransposeTol = 1e-12, squared
 // max(|Re(a - b)|, |Im(a - b)|) and max(|Re a|, |Im a|) as floats
 __device__ __forceinline__ float el_max_abs(double2 a) { return (float)fmax(fabs(a.x), fabs(a.y)); }
 __device__ __forceinline__ float el_max_abs(cdf a) { return fmaxf(fabsf(a.x.hi), fabsf(a.y.hi)); }
-
-// grouped column index j -> memory offset of that column inside a row
-__device__ __forceinline__ int offset_of_col(int j, int nb) { return (j % nb) * nb + j / nb; }
 
 // B = chi0 of the point at x written to the group's matrix M (as rpa_point_warp
 // would), and whether the point at xc holds its conjugate bit for bit (with
@@ -376,7 +401,7 @@ __global__ void __launch_bounds__(448, 2) rpa_pair_kernel(int nw, int d0, int d1
   int *s_row = reinterpret_cast<int *>(s_val + N * N);
   int *s_cs = s_row + N * N;
   __shared__ int s_ureal, s_usym;
-  const size_t u_bytes = ((size_t)N * N * (sizeof(double2) + sizeof(int)) + (N + 1) * sizeof(int) + 15) & ~(size_t)15;
+  const size_t u_bytes = sparse_u_bytes(N);
   constexpr int GPW = 32 / G;
   const int wl = threadIdx.x & 31, gw = wl / G;
   const int grp = (threadIdx.x >> 5) * GPW + gw, lane = wl - gw * G, n_grp = (blockDim.x >> 5) * GPW;
@@ -406,7 +431,14 @@ __global__ void __launch_bounds__(448, 2) rpa_pair_kernel(int nw, int d0, int d1
     s_usym = usym;
   }
   __syncthreads();
-  const SparseU u{s_val, s_row, s_cs};
+  if constexpr (IsDf<E>::value) {  // the values in the element type, in place
+    for (int t = threadIdx.x; t < s_cs[N]; t += blockDim.x) {
+      const double2 v = s_val[t];
+      reinterpret_cast<cdf *>(s_val)[t] = to_cdf(v);
+    }
+    __syncthreads();
+  }
+  const SparseU u{s_val, s_row, s_cs, U, IsDf<E>::value};
   const bool ureal = s_ureal != 0;
   const bool tpairs = s_usym != 0 && IsDf<E>::value;  // transposition partners (never in the FP64 mode)
   if (!active) return;
@@ -506,7 +538,7 @@ template <class E, int G, int NBC = 0>
 int launch_as(long n_points, int nb, const double2 *chi0, const double2 *U, double2 *chi, cudaStream_t stream,
               unsigned *status) {
   const int N = nb * nb;
-  const size_t u_bytes = ((size_t)N * N * (sizeof(double2) + sizeof(int)) + (N + 1) * sizeof(int) + 15) & ~(size_t)15;
+  const size_t u_bytes = sparse_u_bytes(N);
   const size_t per_point = (size_t)group_stride(N, G) * 16;
   const int ppw = 32 / G;  // points per warp
   const size_t limit = (size_t)max_smem_optin();
@@ -768,7 +800,7 @@ template <class E, int G, int NBC>
 int launch_pair_as(int nw, const int dims[3], int nb, const double2 *chi0, const double2 *U, PairOut out,
                    cudaStream_t stream, unsigned *status) {
   const int N = nb * nb;
-  const size_t u_bytes = ((size_t)N * N * (sizeof(double2) + sizeof(int)) + (N + 1) * sizeof(int) + 15) & ~(size_t)15;
+  const size_t u_bytes = sparse_u_bytes(N);
   const size_t per_point = (size_t)group_stride(N, G) * 16;
   const int ppw = 32 / G;
   const size_t limit = (size_t)max_smem_optin() - 64;  // the kernel's static word
@@ -835,7 +867,7 @@ int launch_rpa_warp(long n_points, int nb, const double2 *chi0, const double2 *U
   };
   // candidates: the group sizes whose per-warp tiles fit one CTA (as launch_as sizes them)
   const int N = nb * nb;
-  const size_t u_bytes = ((size_t)N * N * (sizeof(double2) + sizeof(int)) + (N + 1) * sizeof(int) + 15) & ~(size_t)15;
+  const size_t u_bytes = sparse_u_bytes(N);
   std::vector<int> cands;
   // 9 lanes (three groups per warp) own two of the 18 columns of a 9 x 9 system each
   for (int g : {8, 9, 16, 32})
@@ -857,7 +889,7 @@ int launch_rpa_warp(long n_points, int nb, const double2 *chi0, const double2 *U
 int launch_rpa_warp_pairs(int nw, const int dims[3], int nb, const double2 *chi0, const double2 *U, PairOut out,
                           cudaStream_t stream, unsigned *status) {
   const int N = nb * nb;
-  const size_t u_bytes = ((size_t)N * N * (sizeof(double2) + sizeof(int)) + (N + 1) * sizeof(int) + 15) & ~(size_t)15;
+  const size_t u_bytes = sparse_u_bytes(N);
   std::vector<int> cands;
   for (int g : {8, 9, 16, 32})
     if ((g != 9 || N == 9) && u_bytes + (size_t)(32 / g) * group_stride(N, g) * 16 <= (size_t)max_smem_optin() - 64)
