@@ -553,7 +553,11 @@ def run_gpu(args):
     e2e = None
     if not args.no_e2e:
         ek_host = e_k.cpu().pin_memory()
-        out_host = torch.empty((nwt, nk) + (nb,) * 4, dtype=torch.complex128, pin_memory=True)
+        # two pinned outputs used in turn: a pipelined call's chi (its copies and host
+        # fill running behind the next call) must not be the next call's output
+        out_hosts = [torch.empty((nwt, nk) + (nb,) * 4, dtype=torch.complex128, pin_memory=True) for _ in range(2)]
+        out_host = out_hosts[0]
+        turn = [0]
         wmesh = T.MeshImFreq(beta, "Fermion", n_max)
         kmesh = T.MeshBrZone(dims=dims)
         del g_wk, ws, chi0, chi
@@ -573,7 +577,9 @@ def run_gpu(args):
             # copied to the pinned host buffer in frequency blocks while later blocks solve
             ekd = ek_host.to(dev, non_blocking=True)
             g = T.lattice_dyson_g0_wk(mu, T.Gf(mesh=kmesh, data=ekd), wmesh)
-            imtime_bubble_rpa_wk(g, cfg["U"], nw, out=out_host, block_freqs=block, slots=slots, chi0=chi0_buf,
+            out = out_hosts[turn[0] % 2]
+            turn[0] += 1
+            imtime_bubble_rpa_wk(g, cfg["U"], nw, out=out, block_freqs=block, slots=slots, chi0=chi0_buf,
                                  workspace=fws, wait=wait)
             del g
 

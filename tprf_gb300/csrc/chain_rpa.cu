@@ -20,6 +20,7 @@
 #include <chrono>
 #include <cmath>
 #include <condition_variable>
+#include <cstdint>
 #include <cstdlib>
 #include <cstring>
 #include <deque>
@@ -48,8 +49,13 @@ constexpr int kMaxSlots = 32;
 // conjugate-pair solve stores the conjugate of the same values): half the
 // bytes cross the device-to-host link, which bounds the call. Jobs are
 // submitted by host functions on the copy stream once a block's copy has
-// landed; a last host function waits for them, so that the copy stream (and a
-// stream joined to it) passes only when chi is complete. No CUDA calls here.
+// landed. The copy stream does not wait for them: the next call's copies
+// follow at once (holding the copy stream until each call's fill ended left
+// the link idle for the fill's tail; on the 3-orbital 32^3 workload a pipelined
+// step went from 127.6 to 112.3 ms with this and the word-wise fill). A stream
+// joined to the copies (the waiting call, tprf_imtime_bubble_rpa_to_host_join)
+// runs a host function that waits until the pool is idle, so it passes only
+// when chi is complete. No CUDA calls here.
 class HostPool {
  public:
   static HostPool &get() {
@@ -121,6 +127,17 @@ using Clock = std::chrono::steady_clock;
 struct FillStats {
   std::mutex mu;
   std::atomic<bool> complete{false};  // set once the call's last fill job has ended
+  // jobs submitted and not yet ended, and whether the call's last submission has
+  // happened (the copy stream's mark_fill_submitted): complete when both say done
+  std::atomic<long> pending{0};
+  std::atomic<bool> all_submitted{false};
+  void job_done() {
+    if (pending.fetch_sub(1) == 1 && all_submitted.load()) complete = true;
+  }
+  void mark_submitted() {
+    all_submitted = true;
+    if (pending.load() == 0) complete = true;
+  }
   bool any = false;
   Clock::time_point first, last;
   double job_ms = 0.0;
@@ -148,16 +165,26 @@ struct HostMirror {
   std::shared_ptr<FillStats> stats;
 };
 
+// The conjugate is the source with the sign bit of every imaginary part flipped:
+// the block as 64-bit words, eight loads before the eight stores (a host
+// measurement filled 6 to 12 % faster than element by element).
 void host_mirror_range(const HostMirror &j, long b0, long b1) {
   const long nk = (long)j.d0 * j.d1 * j.d2;
+  const long n = 2 * j.n_target;  // 64-bit words per block
   for (long b = b0; b < b1; ++b) {
     const int m = j.m_lo + (int)(b / nk);
     const long k = b - (long)(m - j.m_lo) * nk;
     const int k2 = (int)(k % j.d2), k1 = (int)((k / j.d2) % j.d1), k0 = (int)(k / ((long)j.d2 * j.d1));
     const long mk = ((long)((j.d0 - k0) % j.d0) * j.d1 + (j.d1 - k1) % j.d1) * j.d2 + (j.d2 - k2) % j.d2;
-    const double2 *src = j.host + ((long)(j.nw - 1 + m) * nk + mk) * j.n_target;
-    double2 *dst = j.host + ((long)(j.nw - 1 - m) * nk + k) * j.n_target;
-    for (long e = 0; e < j.n_target; ++e) dst[e] = make_double2(src[e].x, -src[e].y);
+    const uint64_t *src = reinterpret_cast<const uint64_t *>(j.host + ((long)(j.nw - 1 + m) * nk + mk) * j.n_target);
+    uint64_t *dst = reinterpret_cast<uint64_t *>(j.host + ((long)(j.nw - 1 - m) * nk + k) * j.n_target);
+    long e = 0;
+    for (; e + 8 <= n; e += 8) {
+      uint64_t v[8];
+      for (int u = 0; u < 8; ++u) v[u] = src[e + u];
+      for (int u = 0; u < 8; ++u) dst[e + u] = v[u] ^ ((uint64_t)(u & 1) << 63);
+    }
+    for (; e < n; ++e) dst[e] = src[e] ^ ((uint64_t)(e & 1) << 63);
   }
 }
 
@@ -166,6 +193,7 @@ void CUDART_CB submit_host_mirror(void *data) {
   HostPool &pool = HostPool::get();
   const long blocks = (long)(j->m_hi - j->m_lo) * j->d0 * j->d1 * j->d2;
   const long parts = std::min<long>(blocks, pool.threads());
+  j->stats->pending += parts;
   for (long i = 0; i < parts; ++i) {
     const long b0 = blocks * i / parts, b1 = blocks * (i + 1) / parts;
     const HostMirror copy = *j;
@@ -173,19 +201,24 @@ void CUDART_CB submit_host_mirror(void *data) {
       const Clock::time_point t0 = Clock::now();
       host_mirror_range(copy, b0, b1);
       copy.stats->add(t0, Clock::now(), sched_getcpu());
+      copy.stats->job_done();
     });
   }
   delete j;
 }
 
-// the copy stream's last host function of a call: waits for the call's fill jobs
-// (host functions of one stream run in order, so no later call's jobs are queued yet)
-void CUDART_CB wait_host_mirrors(void *data) {
+// the copy stream's last host function of a call: every fill job of the call has
+// been submitted (host functions of one stream run in order). It does not wait
+// for them, so the next call's copies follow at once; join_fills waits.
+void CUDART_CB mark_fill_submitted(void *data) {
   auto *sp = static_cast<std::shared_ptr<FillStats> *>(data);
-  HostPool::get().wait_idle();
-  (*sp)->complete = true;
+  (*sp)->mark_submitted();
   delete sp;
 }
+
+// on the caller's stream, after it has waited for the copy stream: every fill
+// job submitted so far has ended (the host's part of chi is in place)
+void CUDART_CB join_fills(void *) { HostPool::get().wait_idle(); }
 
 // One call's copies and host fill: timing events around every copy (grown on
 // demand), the bytes that crossed the link and that the host filled, and the
@@ -440,7 +473,7 @@ int bubble_rpa_to_host(double beta, int n_iw, int n_tau, int nw, const int dims[
     c->pending[slot] = true;
   }
   if (host_mirror)
-    TPRF_CUDA(cudaLaunchHostFunc(c->copy, wait_host_mirrors, new std::shared_ptr<FillStats>(fill)));
+    TPRF_CUDA(cudaLaunchHostFunc(c->copy, mark_fill_submitted, new std::shared_ptr<FillStats>(fill)));
   rec->d2h = d2h;
   rec->copies = n_copies;
   rec->fill = fill;
@@ -451,7 +484,10 @@ int bubble_rpa_to_host(double beta, int n_iw, int n_tau, int nw, const int dims[
   rec->fold_pending = host_mirror && filled > 0;
   ++c->calls;
   TPRF_CUDA(cudaEventRecord(c->done, c->copy));
-  if (join) TPRF_CUDA(cudaStreamWaitEvent(s, c->done, 0));
+  if (join) {
+    TPRF_CUDA(cudaStreamWaitEvent(s, c->done, 0));
+    if (host_mirror) TPRF_CUDA(cudaLaunchHostFunc(s, join_fills, nullptr));
+  }
   return finish_with_checks(s, "imtime_bubble_rpa_to_host");
 }
 }  // namespace
@@ -549,5 +585,6 @@ extern "C" int tprf_imtime_bubble_rpa_to_host_join(void *stream) {
   std::lock_guard<std::mutex> lock(c->mu);
   TPRF_CUDA(cudaEventRecord(c->done, c->copy));
   TPRF_CUDA(cudaStreamWaitEvent(static_cast<cudaStream_t>(stream), c->done, 0));
+  TPRF_CUDA(cudaLaunchHostFunc(static_cast<cudaStream_t>(stream), join_fills, nullptr));
   return TPRF_OK;
 }
