@@ -119,8 +119,9 @@ int tprf_autotune_load(const char *path);
 
 /* Device capability: sustained FP64 FMA throughput (TFLOP/s) of the current
  * GPU, best of three timed runs of a fixed-length FMA loop; synchronises
- * `stream`. The path's kernels are bound by this pipe on GB300, so the
- * benchmark reports FP64 fractions against it. No reference counterpart.
+ * `stream`. A native FP64 form of the path would be bound by this pipe on
+ * GB300; the benchmark reports FP64 fractions against it. No reference
+ * counterpart.
  * scratch: device buffer of at least 2048 doubles per SM. */
 int tprf_measure_fp64_tflops(double *tflops, void *scratch, size_t scratch_bytes, void *stream);
 
@@ -303,14 +304,15 @@ int tprf_imtime_bubble_rpa_to_host(double beta, int n_iw, int n_tau, int nw, con
  * library's copy stream of the device after the compute on `stream` is done,
  * so that the next call's chain overlaps them (a pipeline over many inputs;
  * that call's solves wait for the device buffers they reuse). chi_host is
- * complete after tprf_imtime_bubble_rpa_to_host_join(stream) once `stream`
- * gets there, or after a device-wide synchronisation. Do not reuse chi_host or
- * chi0_wk before then. */
+ * complete once `stream` gets past tprf_imtime_bubble_rpa_to_host_join(stream)
+ * (a device-wide synchronisation alone does not wait for the host threads that
+ * fill the negative frequencies). Do not reuse chi_host or chi0_wk before then. */
 int tprf_imtime_bubble_rpa_to_host_async(double beta, int n_iw, int n_tau, int nw, const int dims[3], int nb,
                                          const double *g_wk, const double *moments, const double *U,
                                          double *chi0_wk, double *chi_host, int block_freqs, int slots,
                                          void *workspace, size_t workspace_bytes, void *stream);
-/* `stream` waits for every copy the calls above have enqueued on this device. */
+/* `stream` waits for every copy the calls above have enqueued on this device
+ * and for the host threads' fill of every such call. */
 int tprf_imtime_bubble_rpa_to_host_join(void *stream);
 /* Bytes the last of these calls on this device copied from the device to the host. */
 size_t tprf_imtime_bubble_rpa_to_host_last_d2h_bytes(void);

@@ -72,7 +72,8 @@ def imtime_bubble_rpa_wk(g_wk, U, nw, out=None, nt=-1, moments=None, block_freqs
     ``wait=False`` returns without waiting for the copies: they run on behind
     the compute, so that the next call's chain overlaps them (a pipeline over
     many inputs). ``out`` is then complete after :func:`join_host_copies` and a
-    synchronisation of the current stream (or of the device); ``out`` and
+    synchronisation of the current stream (a device synchronisation alone does
+    not wait for the host threads that fill the negative frequencies); ``out`` and
     ``chi0`` must not be reused before, and ``workspace`` (whose ring buffers
     the copies read) must be given and held by the caller."""
     if not wait and workspace is None:
