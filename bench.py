@@ -553,9 +553,17 @@ def run_gpu(args):
     e2e = None
     if not args.no_e2e:
         ek_host = e_k.cpu().pin_memory()
-        # two pinned outputs used in turn: a pipelined call's chi (its copies and host
-        # fill running behind the next call) must not be the next call's output
-        out_hosts = [torch.empty((nwt, nk) + (nb,) * 4, dtype=torch.complex128, pin_memory=True) for _ in range(2)]
+        # two pinned outputs used in turn where host memory allows: a pipelined call's chi
+        # (its copies and host fill running behind the next call) must not be the next
+        # call's output; with one (a chi too large to pin twice) the calls share it
+        chi_bytes = nwt * nk * nb ** 4 * C16
+        try:
+            host_bytes = os.sysconf("SC_PHYS_PAGES") * os.sysconf("SC_PAGE_SIZE")
+        except (ValueError, OSError):
+            host_bytes = 0
+        n_out = 2 if 2 * chi_bytes <= 0.3 * host_bytes else 1
+        out_hosts = [torch.empty((nwt, nk) + (nb,) * 4, dtype=torch.complex128, pin_memory=True)
+                     for _ in range(n_out)]
         out_host = out_hosts[0]
         turn = [0]
         wmesh = T.MeshImFreq(beta, "Fermion", n_max)
@@ -577,7 +585,7 @@ def run_gpu(args):
             # copied to the pinned host buffer in frequency blocks while later blocks solve
             ekd = ek_host.to(dev, non_blocking=True)
             g = T.lattice_dyson_g0_wk(mu, T.Gf(mesh=kmesh, data=ekd), wmesh)
-            out = out_hosts[turn[0] % 2]
+            out = out_hosts[turn[0] % n_out]
             turn[0] += 1
             imtime_bubble_rpa_wk(g, cfg["U"], nw, out=out, block_freqs=block, slots=slots, chi0=chi0_buf,
                                  workspace=fws, wait=wait)
@@ -643,6 +651,7 @@ def run_gpu(args):
                        "memory, the copies of a step overlapping the next step's chain; host threads fill "
                        "chi(-w, q) = conj(chi(w, -q)) when only w >= 0 crossed)",
                "steps": e2e_steps, "ms_per_step": e2e_s * 1e3, "block_freqs": block, "ring_slots": slots,
+               "host_outputs": n_out,
                "serial": {"value": world * points / serial_s, "ms_per_step": serial_s * 1e3,
                           "path": "imtime_bubble_rpa_wk(wait=True): each call returns with chi on the host",
                           "host_side_last_step": rec_serial},
