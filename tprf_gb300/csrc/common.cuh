@@ -364,7 +364,9 @@ template <bool FWD, class C>
 __device__ __forceinline__ C last_stage_output(const C *__restrict__ a, const FftDesc &d, int ncol, int col, int i) {
   const C *tw = twiddles<C>(d);
   const int n = d.n, R = d.radix[d.nst - 1], Ns = n / R;
-  const int k = i % Ns;
+  // k = i mod Ns; the outputs kept (|m| < nw <= Ns) lie in the first and the last
+  // block of Ns, which need no division
+  const int k = i < Ns ? i : i >= n - Ns ? i - (n - Ns) : i % Ns;
   C v = a[k * ncol + col];
   int e = 0;
   for (int r = 1; r < R; ++r) {
