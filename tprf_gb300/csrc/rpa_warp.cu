@@ -905,19 +905,11 @@ int launch_rpa_warp_pairs(int nw, const int dims[3], int nb, const double2 *chi0
   int lanes = rpa_group_lanes(nb);
   int st;
   if ((const void *)chi0 != (const void *)(out.pos - (long)(nw - 1 - out.mh0) * out.row)) {
-    // a trial solves the units of the first frequencies after w = 0 (w = 0 has
-    // no transposition quads), at least 524288 units (shorter trials ranked the
-    // lane counts by their tails: on the 32^3 cubic workload 16 lanes won a
-    // 65536-unit trial and lost the full call by 5 %), the same values the full
-    // run writes there
-    const long nk = (long)dims[0] * dims[1] * dims[2];
-    PairOut first = out;
-    first.mh0 = (out.mh0 == 0 && out.mh1 > 1) ? 1 : out.mh0;
-    first.mh1 = (int)std::min<long>(out.mh1, first.mh0 + std::max(1L, (524288 + nk - 1) / nk));
-    first.pos = out.pos + (long)(first.mh0 - out.mh0) * out.row;
-    first.neg = out.neg ? out.neg + (long)(first.mh0 - out.mh0) * out.neg_step : nullptr;
-    st = tune_pick(tune_key("rpa_group", {nb}), cands, lanes, stream, [&](int v) { return launch(v, first); },
-                   &lanes);
+    // a trial is the whole call (it writes what the call writes): trials on the
+    // first frequencies ranked the lane counts wrongly (on the 32^3 cubic
+    // workload 16 lanes won a 65536-unit and a 524288-unit trial, yet on the full
+    // call 9 lanes take 28.9 ms, 16 lanes 29.4 and 8 lanes 30.0)
+    st = tune_pick(tune_key("rpa_group", {nb}), cands, lanes, stream, [&](int v) { return launch(v, out); }, &lanes);
   } else {
     st = tune_lookup(tune_key("rpa_group", {nb}), cands, lanes, &lanes);
   }
