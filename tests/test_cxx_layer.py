@@ -98,8 +98,13 @@ def test_reference_cxx_chain_matches_the_oracle(program, cuda_lib, tmp_path):
     assert rel_err(load("chi0_wr_back", (nwt, nk) + t4), O.fourier_wk_to_wr(chi0_wk, dims)) < PARITY_RTOL
     assert rel_err(load("g_wk_back", (2 * n_max, nk, nb, nb)), g_wk) < PARITY_RTOL
     assert rel_err(load("g_wr_from_tr", (2 * n_max, nk, nb, nb)), O.fourier_tr_to_wr(g_tr, beta, n_max)) < PARITY_RTOL
+    # the bosonic w -> tau transform of the program's own chi0(w, r), against the
+    # oracle on that same input: its tail fit amplifies a change of its input
+    # about a hundredfold (the chain's chi0(w, r), 7e-13 from the oracle's, gives
+    # 9e-11 after it; the transform itself adds 4e-12), so each stage is held to
+    # the bar on the input it is given, as in the Matsubara parity tests
     assert rel_err(load("chi0_tr_from_wr", (6 * nw + 1, nk) + t4),
-                   O.chi_tr_from_chi_wr(chi0_wr, beta, -1)) < PARITY_RTOL
+                   O.chi_tr_from_chi_wr(load("chi0_wr", (nwt, nk) + t4), beta, -1)) < PARITY_RTOL
     assert rel_err(load("lindhard", (nwt, nk) + t4), O.lindhard_chi00(ek, dims, beta, mu, nw)) < PARITY_RTOL
     iw = O.fermionic_iw(beta, n_max)
     sigma = np.zeros((2 * n_max, nb, nb), complex)
