@@ -90,3 +90,18 @@ def test_vertex_builders_equal_the_oracle_restatement():
                         O.kanamori_charge_and_spin_quartic_interaction_tensors(norb, *pars)):
             assert np.array_equal(a, b)
         assert np.array_equal(R.kanamori_quartic_tensor(norb, *pars), O.kanamori_quartic_tensor(norb, *pars))
+
+
+def test_bench_models_the_compact_orbital_columns():
+    """bench.py's algorithmic bytes follow the library's compact r -> q path: the
+    45 canonical orbital columns abcd <= dcba of a 3-orbital bubble on a 3-d mesh
+    whose last two axes are powers of two, none on a 2-d mesh or where the compact
+    rows would not fit the free rows of G(tau, r)."""
+    import bench
+    assert bench.compact_columns((32, 32, 32), 3, 1537, 256) == 45
+    assert bench.compact_columns((16, 16, 8), 3, 1537, 256) == 45
+    assert bench.compact_columns((64, 64, 4), 5, 3073, 256) is None  # 256 x 325 > 3055 x 25
+    assert bench.compact_columns((48, 48, 1), 2, 1537, 256) is None
+    assert bench.compact_columns((32, 32, 32), 3, 1537, 256, real=False) is None
+    m = bench.stage_model(3, 32768, 512, 1537, 256, real=True, nc=45)
+    assert m["fft_r_to_q"]["bytes"] == 16 * 32768 * (45 * 256 + 81 * 511)
