@@ -159,3 +159,22 @@ def test_autotune_wisdom_file_round_trip(lib, tmp_path):
     assert lib.tprf_set_autotune(2) != 0
     assert not tuning.autotune_enabled()
     tuning.clear_wisdom()
+
+
+def test_tuned_block_loads_and_writes_back_the_wisdom(lib, tmp_path):
+    """tuning.tuned(path): loads the file, turns measure mode on for the block and
+    back off after it, and writes every choice back (host-only)."""
+    from tprf_gb300 import tuning
+    tuning.clear_wisdom()
+    tuning.set_autotune(False)
+    path = tmp_path / "w.txt"
+    path.write_text("sm103x152/rpa_group/0/3 9\n")
+    with tuning.tuned(path):
+        assert tuning.autotune_enabled()
+        assert tuning.wisdom_entries() == 1
+    assert not tuning.autotune_enabled()
+    assert "sm103x152/rpa_group/0/3 9" in path.read_text().splitlines()
+    tuning.clear_wisdom()
+    with tuning.tuned(tmp_path / "new.txt", measure=False):  # no file yet: nothing loaded
+        assert not tuning.autotune_enabled() and tuning.wisdom_entries() == 0
+    assert (tmp_path / "new.txt").exists()
