@@ -663,18 +663,21 @@ def _orbital_reversal(nb):
     return np.array(rev)
 
 
+@pytest.mark.parametrize("model", ["cubic_3orb", "layered_5orb"])
 @pytest.mark.parametrize("complex_hop", [False, True])
-def test_compact_orbital_columns_on_a_3d_mesh(cuda_lib, arithmetic, complex_hop):
+def test_compact_orbital_columns_on_a_3d_mesh(cuda_lib, arithmetic, complex_hop, model):
     """The chain on a three-dimensional mesh whose last two axes share one plane
     pass: with real hoppings the bubble is real and transpose-symmetric, so only
-    the canonical orbital columns abcd <= dcba are transformed r -> q and the last
-    pass stores chi0(w, -q)_dcba = chi0(w, q)_abcd bit for bit; with complex
-    hoppings the same mesh takes the full path. Both against the oracle."""
+    the canonical orbital columns abcd <= dcba are transformed r -> q (45 of 81
+    at nb = 3, 325 of 625 at nb = 5) and the last pass stores
+    chi0(w, -q)_dcba = chi0(w, q)_abcd bit for bit; with complex hoppings the
+    same mesh takes the full path. Both against the oracle."""
     T = tp()
     from tprf_gb300 import workloads
-    hop = workloads.cubic_3orb(3)
+    hop = workloads.cubic_3orb(3) if model == "cubic_3orb" else workloads.layered_5orb(1)
+    nbm = hop[(1, 0, 0)].shape[0]
     if complex_hop:
-        extra = 0.2j * np.array([[0.0, 1.0, 0.5], [-0.3, 0.0, 0.2], [0.1, -0.6, 0.0]])
+        extra = 0.2j * np.random.default_rng(9).standard_normal((nbm, nbm))
         hop[(1, 0, 0)] = hop[(1, 0, 0)] + extra
         hop[(-1, 0, 0)] = hop[(-1, 0, 0)] + extra.conj().T
     dims, beta, n_max, nw = (4, 4, 2), 12.0, 24, 6
@@ -682,11 +685,12 @@ def test_compact_orbital_columns_on_a_3d_mesh(cuda_lib, arithmetic, complex_hop)
     chi0 = T.imtime_bubble_chi0_wk(g_wk, nw=nw, verbose=False)
     ref = O.imtime_bubble_chi0_wk(O.lattice_dyson_g0_wk(0.0, ek, beta, n_max), beta, dims, nw=nw)
     assert rel_err(chi0.data, ref) < PARITY_RTOL
-    x = chi0.data.cpu().numpy().reshape((2 * nw - 1,) + dims + (81,))
+    nb4 = nbm ** 4
+    x = chi0.data.cpu().numpy().reshape((2 * nw - 1,) + dims + (nb4,))
     mq = np.roll(x[:, ::-1, ::-1, ::-1, :], 1, axis=(1, 2, 3))  # chi0(w, -q)
-    rev = _orbital_reversal(3)
+    rev = _orbital_reversal(nbm)
     refl = mq[..., rev]  # chi0(w, -q)_dcba
-    off = rev != np.arange(81)
+    off = rev != np.arange(nb4)
     if complex_hop:
         assert not np.array_equal(x[..., off], refl[..., off])
     elif arithmetic != "fp64":  # the FP64 mode transforms every column
